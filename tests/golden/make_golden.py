@@ -1,0 +1,301 @@
+"""Generate the golden fixtures used by the parity tests.
+
+Run once in a checkout that has the picca sources next to it
+(``python tests/golden/make_golden.py /path/to/picca``). It writes:
+
+* ``delta_lya.npz`` / ``delta_lya_image.npz`` / ``cat.npz``: the inputs of
+  picca's correlation tests (``py/picca/tests/data/test_delta``) converted to
+  compact numpy arrays, so tests can rebuild the FITS files anywhere;
+* ``cor_<case>.npz``: every column and the ATTRI header of picca's golden
+  correlation outputs (``py/picca/tests/data/test_cor/*.fits.gz``), produced by
+  the commands at ``py/picca/tests/test_3_cor.py:229-316, :458-488,
+  :636-664, :791-1002``;
+* ``pair_cases.npz``: inputs and outputs of picca's own
+  ``cf.compute_xi_forest_pairs_fast`` and ``xcf.compute_xi_forest_pairs_fast``
+  run here as plain Python (numba, healpy, fitsio, camb and iminuit replaced by
+  import stand-ins, the functions themselves unmodified) on forest pairs from
+  the test data, for every option branch of the kernels.
+"""
+
+import os
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(os.path.dirname(HERE)))
+
+from picca_gb300 import fitsio_lite  # noqa: E402
+from picca_gb300 import constants as gb_constants  # noqa: E402
+from picca_gb300 import io as gb_io  # noqa: E402
+from picca_gb300.healpix import ang2pix_ring  # noqa: E402
+
+
+def _convert_delta_dir(src_dir, out_path):
+    files = sorted(f for f in os.listdir(src_dir) if f.endswith(".fits.gz"))
+    rec = {k: [] for k in ("file_index", "los_id", "ra", "dec", "z", "plate", "mjd",
+                           "fiberid", "npix")}
+    pix = {k: [] for k in ("LOGLAM", "DELTA", "WEIGHT", "CONT")}
+    for index, name in enumerate(files):
+        hdul = fitsio_lite.FITS(os.path.join(src_dir, name))
+        for hdu in hdul[1:]:
+            header = hdu.read_header()
+            rec["file_index"].append(index)
+            rec["los_id"].append(header["THING_ID"])
+            rec["ra"].append(header["RA"])
+            rec["dec"].append(header["DEC"])
+            rec["z"].append(header["Z"])
+            rec["plate"].append(header["PLATE"])
+            rec["mjd"].append(header["MJD"])
+            rec["fiberid"].append(header["FIBERID"])
+            rec["npix"].append(hdu.get_nrows())
+            for key in pix:
+                pix[key].append(hdu[key][:])
+    out = {k: np.asarray(v) for k, v in rec.items()}
+    out.update({k: np.concatenate(v) for k, v in pix.items()})
+    out["file_names"] = np.asarray(files)
+    np.savez_compressed(out_path, **out)
+
+
+def _convert_image_dir(src_dir, out_path):
+    files = sorted(f for f in os.listdir(src_dir) if f.endswith(".fits.gz"))
+    out = {"file_names": np.asarray(files)}
+    for index, name in enumerate(files):
+        hdul = fitsio_lite.FITS(os.path.join(src_dir, name))
+        meta = hdul["METADATA"]
+        out[f"f{index}_LAMBDA"] = hdul["LAMBDA"][:]
+        for key in ("DELTA", "WEIGHT", "CONT"):
+            out[f"f{index}_{key}"] = np.asarray(hdul[key].read(), dtype=float)
+        for col in meta.get_colnames():
+            out[f"f{index}_META_{col}"] = meta[col][:]
+        out[f"f{index}_BLINDING"] = np.asarray(meta.read_header().get("BLINDING", "none"))
+    np.savez_compressed(out_path, **out)
+
+
+def _convert_cat(src, out_path):
+    table = fitsio_lite.FITS(src)[1]
+    np.savez_compressed(out_path, **{c: table[c][:] for c in table.get_colnames()})
+
+
+def _convert_cor(src, out_path):
+    hdul = fitsio_lite.FITS(src)
+    attri = hdul["ATTRI"]
+    cor = hdul["COR"]
+    out = {c: attri[c][:] for c in attri.get_colnames()}
+    out.update({c: cor[c][:] for c in cor.get_colnames()})
+    header = attri.read_header()
+    for key in ("RPMIN", "RPMAX", "RTMAX", "NP", "NT", "NSIDE"):
+        out["hdr_" + key] = np.asarray(header[key])
+    np.savez_compressed(out_path, **out)
+
+
+def _install_stand_ins():
+    """Stand-ins for the reference's third-party imports (no code of those
+    projects is involved; the pair functions need none of them)."""
+    numba = types.ModuleType("numba")
+
+    def njit(*args, **kwargs):
+        if args and callable(args[0]):
+            return args[0]
+        return lambda func: func
+
+    numba.njit = njit
+    numba.jit = njit
+    numba.int32 = np.int32
+    numba.prange = range
+    healpy = types.ModuleType("healpy")
+    healpy.query_disc = lambda nside, vec, radius, inclusive=True: np.arange(12 * nside * nside)
+    healpy.ang2pix = lambda nside, theta, phi: ang2pix_ring(nside, theta, phi)
+    fitsio = types.ModuleType("fitsio")
+    fitsio.FITS = fitsio_lite.FITS
+    camb = types.ModuleType("camb")
+    iminuit = types.ModuleType("iminuit")
+    iminuit.util = types.SimpleNamespace(IMinuitWarning=Warning)
+    for name, mod in (("numba", numba), ("healpy", healpy), ("fitsio", fitsio),
+                      ("camb", camb), ("iminuit", iminuit)):
+        sys.modules[name] = mod
+
+
+def _pair_cases(reference_py, delta_dir, attributes):
+    sys.dont_write_bytecode = True
+    _install_stand_ins()
+    sys.path.insert(0, reference_py)
+    import picca.cf as ref_cf  # pylint: disable=import-outside-toplevel
+    import picca.xcf as ref_xcf  # pylint: disable=import-outside-toplevel
+
+    cosmo = gb_constants.Cosmo(Om=0.315, verbose=False)
+    data, _, _, _ = gb_io.read_deltas(delta_dir, 16, 1215.67, 2.9, 2.25, cosmo,
+                                      delta_attributes=attributes)
+    deltas = [d for hp in sorted(data) for d in data[hp]]
+    rng = np.random.default_rng(20261203)
+    # pick close pairs so that many pixel pairs land inside the grid
+    pairs = []
+    for _ in range(4000):
+        a, b = rng.integers(0, len(deltas), 2)
+        if a == b:
+            continue
+        ang = deltas[a].get_angle_between(deltas[b])
+        if ang < 0.01 and abs(deltas[a].z_qso - deltas[b].z_qso) < 0.4:
+            pairs.append((a, b, ang))
+        if len(pairs) >= 6:
+            break
+    # one same-plate pair for the half-plate veto
+    for a in range(len(deltas)):
+        for b in range(a + 1, len(deltas)):
+            if deltas[a].plate == deltas[b].plate and (
+                    (deltas[a].fiberid <= 500) == (deltas[b].fiberid <= 500)) and (
+                        abs(deltas[a].z_qso - deltas[b].z_qso) < 0.5):
+                ang = deltas[a].get_angle_between(deltas[b])
+                if ang < 0.016:
+                    pairs.append((a, b, ang))
+                    break
+        if len(pairs) >= 7:
+            break
+
+    cf_variants = [
+        dict(name="auto", r_par_min=0., r_par_max=60., r_trans_max=60., np=15, nt=15,
+             x_correlation=False, remove_shp=True),
+        dict(name="auto_zcut", r_par_min=0., r_par_max=60., r_trans_max=60., np=15, nt=15,
+             z_min_pairs=2.25, z_max_pairs=2.3, remove_shp=True),
+        dict(name="cross", r_par_min=-60., r_par_max=60., r_trans_max=60., np=30, nt=15,
+             x_correlation=True, remove_shp=True),
+        dict(name="zerr", r_par_min=0., r_par_max=200., r_trans_max=200., np=50, nt=50,
+             zerr_cut_deg=2.0, zerr_cut_kms=30000.),
+        dict(name="rmu", r_par_min=0., r_par_max=1., r_trans_max=60., np=10, nt=15,
+             rmu_binning=True),
+        dict(name="angl", r_par_min=1., r_par_max=1.02, r_trans_max=0.01, np=10, nt=10,
+             ang_correlation=True),
+        dict(name="auto_fine", r_par_min=0., r_par_max=200., r_trans_max=200., np=50, nt=50),
+    ]
+    out = {}
+    case_index = 0
+    for variant in cf_variants:
+        for (a, b, _) in pairs:
+            d1, d2 = deltas[a], deltas[b]
+            ref_cf.r_par_min = variant["r_par_min"]
+            ref_cf.r_par_max = variant["r_par_max"]
+            ref_cf.r_trans_max = variant["r_trans_max"]
+            ref_cf.num_bins_r_par = variant["np"]
+            ref_cf.num_bins_r_trans = variant["nt"]
+            ref_cf.z_min_pairs = variant.get("z_min_pairs")
+            ref_cf.z_max_pairs = variant.get("z_max_pairs")
+            ref_cf.zerr_cut_deg = variant.get("zerr_cut_deg")
+            ref_cf.zerr_cut_kms = variant.get("zerr_cut_kms")
+            ref_cf.x_correlation = variant.get("x_correlation", False)
+            ref_cf.rmu_binning = variant.get("rmu_binning", False)
+            ref_cf.ang_correlation = variant.get("ang_correlation", False)
+            ref_cf.remove_same_half_plate_close_pairs = variant.get("remove_shp", False)
+            nbins = variant["np"] * variant["nt"]
+            arrays = [np.zeros(nbins) for _ in range(5)] + [np.zeros(nbins, dtype=np.int64)]
+            ang = d1.get_angle_between(d2)
+            same_half_plate = (d1.plate == d2.plate) and (
+                (d1.fiberid <= 500 and d2.fiberid <= 500) or
+                (d1.fiberid > 500 and d2.fiberid > 500))
+            if ref_cf.ang_correlation:
+                r1, m1 = 10.0**d1.log_lambda, 10.0**d1.log_lambda
+                r2, m2 = 10.0**d2.log_lambda, 10.0**d2.log_lambda
+            else:
+                r1, m1, r2, m2 = d1.r_comov, d1.dist_m, d2.r_comov, d2.dist_m
+            ref_cf.compute_xi_forest_pairs_fast(
+                d1.z, r1, m1, d1.weights, d1.delta, d1.z_qso,
+                d2.z, r2, m2, d2.weights, d2.delta, d2.z_qso,
+                ang, same_half_plate, *arrays)
+            prefix = f"cf{case_index}_"
+            out[prefix + "params"] = np.array([
+                variant["r_par_min"], variant["r_par_max"], variant["r_trans_max"],
+                variant["np"], variant["nt"],
+                np.nan if variant.get("z_min_pairs") is None else variant["z_min_pairs"],
+                np.nan if variant.get("z_max_pairs") is None else variant["z_max_pairs"],
+                np.nan if variant.get("zerr_cut_deg") is None else variant["zerr_cut_deg"],
+                np.nan if variant.get("zerr_cut_kms") is None else variant["zerr_cut_kms"],
+                float(ref_cf.x_correlation), float(ref_cf.rmu_binning),
+                float(ref_cf.ang_correlation),
+                float(ref_cf.remove_same_half_plate_close_pairs)])
+            out[prefix + "scalars"] = np.array([d1.z_qso, d2.z_qso, ang, float(same_half_plate)])
+            for key, val in (("z1", d1.z), ("r1", r1), ("m1", m1), ("w1", d1.weights),
+                             ("d1", d1.delta), ("z2", d2.z), ("r2", r2), ("m2", m2),
+                             ("w2", d2.weights), ("d2", d2.delta)):
+                out[prefix + key] = np.asarray(val, dtype=float)
+            for key, val in zip(("we", "xi", "rp", "rt", "z", "nb"), arrays):
+                out[prefix + "out_" + key] = val
+            out[prefix + "name"] = np.asarray(variant["name"])
+            case_index += 1
+    out["num_cf_cases"] = np.asarray(case_index)
+
+    # xcf: one forest against many quasars (the other forests' quasars)
+    xcf_variants = [
+        dict(name="xcf", r_par_min=-60., r_par_max=60., r_trans_max=60., np=30, nt=15),
+        dict(name="xcf_zcut", r_par_min=-60., r_par_max=60., r_trans_max=60., np=30, nt=15,
+             z_min_pairs=2.25, z_max_pairs=2.3),
+        dict(name="xcf_rmu", r_par_min=-1., r_par_max=1., r_trans_max=60., np=20, nt=15,
+             rmu_binning=True),
+        dict(name="xcf_wide", r_par_min=-200., r_par_max=200., r_trans_max=200., np=100, nt=50),
+    ]
+    xcase = 0
+    qso_ids = rng.permutation(len(deltas))
+    for variant in xcf_variants:
+        for forest_index in (int(pairs[0][0]), int(pairs[1][0]), int(pairs[2][1])):
+            d1 = deltas[forest_index]
+            cands = [deltas[i] for i in qso_ids[:400] if i != forest_index]
+            ang = d1.get_angle_between(cands)
+            keep = ang < 0.03
+            objs = [c for c, k in zip(cands, keep) if k]
+            ang = ang[keep]
+            z_qso = np.array([o.z_qso for o in objs])
+            r_qso = np.asarray(cosmo.get_r_comov(z_qso), dtype=float)
+            m_qso = np.asarray(cosmo.get_dist_m(z_qso), dtype=float)
+            w_qso = ((1. + z_qso) / (1. + 2.25))**(1.44 - 1.)
+            ref_xcf.r_par_min = variant["r_par_min"]
+            ref_xcf.r_par_max = variant["r_par_max"]
+            ref_xcf.r_trans_max = variant["r_trans_max"]
+            ref_xcf.num_bins_r_par = variant["np"]
+            ref_xcf.num_bins_r_trans = variant["nt"]
+            ref_xcf.z_min_pairs = variant.get("z_min_pairs")
+            ref_xcf.z_max_pairs = variant.get("z_max_pairs")
+            ref_xcf.rmu_binning = variant.get("rmu_binning", False)
+            ref_xcf.ang_correlation = False
+            nbins = variant["np"] * variant["nt"]
+            arrays = [np.zeros(nbins) for _ in range(5)] + [np.zeros(nbins, dtype=np.int64)]
+            ref_xcf.compute_xi_forest_pairs_fast(
+                d1.z, d1.r_comov, d1.dist_m, d1.weights, d1.delta,
+                z_qso, r_qso, m_qso, w_qso, ang, *arrays)
+            prefix = f"xcf{xcase}_"
+            out[prefix + "params"] = np.array([
+                variant["r_par_min"], variant["r_par_max"], variant["r_trans_max"],
+                variant["np"], variant["nt"],
+                np.nan if variant.get("z_min_pairs") is None else variant["z_min_pairs"],
+                np.nan if variant.get("z_max_pairs") is None else variant["z_max_pairs"],
+                float(ref_xcf.rmu_binning)])
+            for key, val in (("z1", d1.z), ("r1", d1.r_comov), ("m1", d1.dist_m),
+                             ("w1", d1.weights), ("d1", d1.delta), ("zq", z_qso),
+                             ("rq", r_qso), ("mq", m_qso), ("wq", w_qso), ("ang", ang)):
+                out[prefix + key] = np.asarray(val, dtype=float)
+            for key, val in zip(("we", "xi", "rp", "rt", "z", "nb"), arrays):
+                out[prefix + "out_" + key] = val
+            out[prefix + "name"] = np.asarray(variant["name"])
+            xcase += 1
+    out["num_xcf_cases"] = np.asarray(xcase)
+    np.savez_compressed(os.path.join(HERE, "pair_cases.npz"), **out)
+    return case_index, xcase
+
+
+def main(picca_root):
+    tests = os.path.join(picca_root, "py", "picca", "tests", "data")
+    _convert_delta_dir(os.path.join(tests, "test_delta", "Delta_LYA"),
+                       os.path.join(HERE, "delta_lya.npz"))
+    _convert_image_dir(os.path.join(tests, "test_delta", "Delta_LYA_image"),
+                       os.path.join(HERE, "delta_lya_image.npz"))
+    _convert_cat(os.path.join(tests, "test_delta", "cat.fits"), os.path.join(HERE, "cat.npz"))
+    for case in ("cf", "cf_zcuts", "cf_cross", "cf_cross_zcuts", "cf_image",
+                 "cf_image_zcuts", "xcf", "xcf_zcuts"):
+        _convert_cor(os.path.join(tests, "test_cor", case + ".fits.gz"),
+                     os.path.join(HERE, f"cor_{case}.npz"))
+    ncf, nxcf = _pair_cases(os.path.join(picca_root, "py"),
+                            os.path.join(tests, "test_delta", "Delta_LYA") + "/",
+                            os.path.join(tests, "test_delta", "delta_attributes.fits.gz"))
+    print(f"wrote fixtures: {ncf} cf pair cases, {nxcf} xcf cases")
+
+
+if __name__ == "__main__":
+    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
