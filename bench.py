@@ -1,0 +1,361 @@
+"""Benchmark of the GPU correlation path (one JSON line on stdout).
+
+A step is one pass of the hot path over the whole synthetic survey: neighbour
+lists of every forest + pair accumulation into per-healpix rows (the work of
+``cf.fill_neighs`` + ``cf.compute_xi`` over every healpix,
+py/picca/bin/picca_cf.py:452-458). ``value`` is candidate pixel pairs per
+second with inputs resident in HBM; ``e2e`` is the same through the public
+host API (pinned host arrays uploaded, rows read back, every step).
+
+Default workload: the 400k-forest auto-correlation on 8,000 deg^2 (50 x 50
+bins, r_par and r_trans 0-200 Mpc/h, precision form). ``--impl reference``
+times the CPU oracle (FP64 C restatement of picca's numba kernel, OpenMP over
+all host cores) on a bounded sample of the same workload.
+"""
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, HERE)
+
+CONFIGS = {
+    # name: (num forests, area deg^2, grid, description)
+    "0": (1000, None, "log", "1,000 forests in a 4.5x4.5 deg patch (config 0)"),
+    "1": (100_000, 2000.0, "log", "100k forests on 2,000 deg^2 (config 1)"),
+    "1lin": (100_000, 2000.0, "lin", "100k forests on 2,000 deg^2, 0.8 A grid (config 1 lin)"),
+    "2": (400_000, 8000.0, "log", "400k forests on 8,000 deg^2 (config 2)"),
+}
+METRIC = "cf pixel-pairs/s at stated FP64-oracle error; continuum fits/s plain vs learned"
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", choices=["ours", "reference"], default="ours")
+    p.add_argument("--config", default="2", choices=sorted(CONFIGS))
+    p.add_argument("--precision", choices=["fp32_guard", "fp64"], default="fp32_guard")
+    p.add_argument("--check-fraction", type=float, default=0.01,
+                   help="fraction of work items re-run in FP64 for the error report")
+    p.add_argument("--cpu-seconds", type=float, default=15.0,
+                   help="target CPU time of the oracle sample")
+    return p.parse_args()
+
+
+def make_workload(cfg):
+    from picca_gb300 import synthetic
+    num, area, grid, _ = CONFIGS[cfg]
+    if area is None:
+        fs = synthetic.config0()
+    else:
+        fs = synthetic.config_area(num, area, seed=20261203, grid=grid)
+    params = dict(r_par_min=0.0, r_par_max=200.0, r_trans_max=200.0, num_bins_r_par=50,
+                  num_bins_r_trans=50)
+    ang_max = synthetic.correlation_ang_max(200.0, float(fs.z.min()))
+    return fs, params, ang_max
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during the timed region."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.lines = []
+        self.thread = None
+
+    def start(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+        except (OSError, ValueError):
+            self.proc = None
+            return
+        self.thread = threading.Thread(target=self._read, daemon=True)
+        self.thread.start()
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def stop(self):
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        if self.thread:
+            self.thread.join(timeout=5)
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [x.strip() for x in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                smax = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": smax,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    path = os.path.join(HERE, "MEASURED_PEAKS.json")
+    try:
+        with open(path) as handle:
+            return json.load(handle), "measured"
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "sm_max_mhz": 2070.0}, "fallback"
+
+
+def cpu_sample(fs, params, ang_max, seconds, cfg):
+    """Time the CPU oracle on a bounded sample of the workload, parallel over
+    healpix rows as the reference's Pool is: 2 x cores healpix, a few forests
+    (with all their neighbours) in each. Returns (pixel pairs/s, sample
+    description, threads)."""
+    from oracle import cpu as oracle
+    p = oracle.make_params(**params)
+    rng = np.random.default_rng(5)
+    cores = os.cpu_count() or 1
+    rows = rng.choice(len(fs.healpix_list), size=min(len(fs.healpix_list), 2 * cores),
+                      replace=False)
+    npix = np.diff(fs.pix_offset)
+    per_forest = float(np.mean(npix)) ** 2 * 900.0  # ~pairs of one forest with its neighbours
+    per_row = max(1, int(seconds * 1.5e8 * cores / (per_forest * len(rows))))
+    picks = []
+    for r in rows:
+        members = np.where(fs.row == r)[0]
+        picks.append(rng.choice(members, size=min(len(members), per_row), replace=False))
+    sample = np.sort(np.concatenate(picks))
+    sub = fs.take(sample)
+    t0 = time.perf_counter()
+    offsets, index = oracle.neighbours(sub, fs, p, ang_max, auto_mode=1)
+    oracle.rows(sub, fs, p, offsets, index)
+    elapsed = time.perf_counter() - t0
+    csum = np.concatenate([[0], np.cumsum(npix[index])])
+    cand = int((npix[sample] * (csum[offsets[1:]] - csum[offsets[:-1]])).sum())
+    return cand / elapsed, (f"{len(sample)} forests with all their neighbours, from "
+                            f"{len(rows)} healpix of config {cfg}; {elapsed:.1f} s"), cores
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return
+    fs, params, ang_max = make_workload(args.config)
+    vals = []
+    for _ in range(args.warmup):
+        cpu_sample(fs, params, ang_max, min(5.0, args.cpu_seconds), args.config)
+    desc, cores = "", 1
+    for _ in range(args.steps):
+        v, desc, cores = cpu_sample(fs, params, ang_max, args.cpu_seconds, args.config)
+        vals.append(v)
+    value = float(np.median(vals))
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": "pixel-pairs/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": CONFIGS[args.config][3], "bins": "50x50",
+                   "r_par": "0-200", "r_trans": "0-200"},
+        "cpu_baseline": {"value": value, "unit": "pixel-pairs/s", "cores": cores,
+                         "kind": "port", "sample": desc},
+        "e2e": {"value": value, "unit": "pixel-pairs/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import torch
+    import torch.distributed as dist
+
+    from picca_gb300 import pairs
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    if world > 1:
+        dist.init_process_group("nccl")
+
+    def barrier():
+        if world > 1:
+            dist.barrier()
+        torch.cuda.synchronize()
+
+    fs, params, ang_max = make_workload(args.config)
+    mode = pairs.MODE_FP32_GUARD if args.precision == "fp32_guard" else pairs.MODE_FP64
+    cparams = pairs.make_params(ang_max=ang_max, **params)
+    engine = pairs.PairEngine()
+    packed = pairs.pack_host(fs, pinned=True)
+    dev = pairs.DeviceForests(fs, engine.device, packed=packed)
+    nbins = params["num_bins_r_par"] * params["num_bins_r_trans"]
+    num_rows = len(fs.healpix_list)
+    stream = torch.cuda.current_stream()
+
+    def step(timings=None, device_forests=dev):
+        offsets, index, total = engine.neighbours(cparams, device_forests)
+        order, num_work, cand = engine.work_order(device_forests, None, offsets, index, total)
+        rows = engine.alloc_rows(num_rows, nbins)
+        ev0 = torch.cuda.Event(enable_timing=True)
+        ev1 = torch.cuda.Event(enable_timing=True)
+        ev0.record(stream)
+        engine.accumulate(cparams, device_forests, None, offsets, index, order, num_work, rows,
+                          mode)
+        ev1.record(stream)
+        if timings is not None:
+            timings.append((ev0, ev1))
+        return rows, cand, total, (offsets, index, order, num_work)
+
+    for _ in range(args.warmup):
+        step()
+    torch.cuda.synchronize()
+
+    # device-resident timed region
+    kern = []
+    sampler = ClockSampler(local)
+    sampler.start()
+    barrier()
+    t_start = torch.cuda.Event(enable_timing=True)
+    t_end = torch.cuda.Event(enable_timing=True)
+    t_start.record(stream)
+    cands = []
+    for _ in range(args.steps):
+        rows, cand, total, work = step(kern)
+        cands.append(cand)
+    t_end.record(stream)
+    barrier()
+    clocks = sampler.stop()
+    elapsed = t_start.elapsed_time(t_end) / 1e3
+    kernel_s = [a.elapsed_time(b) / 1e3 for a, b in kern]
+    stats = engine.stats()
+    if world > 1:
+        t = torch.tensor([elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        elapsed = float(t.item())
+    pairs_per_step = cands[0]
+    value = pairs_per_step * args.steps * world / elapsed
+
+    # end to end through the host API: pinned upload, compute, rows back
+    barrier()
+    e2e_t0 = time.perf_counter()
+    h2d = d2h = 0
+    for _ in range(args.steps):
+        dev_e = pairs.DeviceForests(fs, engine.device, packed=packed)
+        rows_e, _, _, _ = step(device_forests=dev_e)
+        host_rows = [r.cpu() for r in rows_e]
+        h2d = dev_e.h2d_bytes
+        d2h = sum(int(r.numel() * r.element_size()) for r in host_rows)
+    torch.cuda.synchronize()
+    e2e_elapsed = time.perf_counter() - e2e_t0
+    if world > 1:
+        t = torch.tensor([e2e_elapsed], device="cuda")
+        dist.all_reduce(t, op=dist.ReduceOp.MAX)
+        e2e_elapsed = float(t.item())
+    e2e_value = pairs_per_step * args.steps * world / e2e_elapsed
+
+    # FP64 error report on a sample of work items (plain FP64 kernel vs ours)
+    offsets, index, order, num_work = work
+    n_check = max(1, int(num_work * args.check_fraction))
+    check = {}
+    if n_check > 0 and mode != pairs.MODE_FP64:
+        sub_order = order[:num_work][torch.randperm(num_work, device=order.device)[:n_check]]
+        sub_order = sub_order.contiguous()
+        r32 = engine.alloc_rows(num_rows, nbins)
+        r64 = engine.alloc_rows(num_rows, nbins)
+        engine.accumulate(cparams, dev, None, offsets, index, sub_order, n_check, r32, mode)
+        engine.accumulate(cparams, dev, None, offsets, index, sub_order, n_check, r64,
+                          pairs.MODE_FP64)
+        torch.cuda.synchronize()
+        a = [r.cpu().numpy() for r in r32]
+        b = [r.cpu().numpy() for r in r64]
+        nz = b[0] > 0
+        rel_we = np.abs(a[0][nz] - b[0][nz]) / b[0][nz]
+        rel_xi = np.abs(a[1][nz] - b[1][nz]) / np.maximum(np.abs(b[1][nz]), 1e-300)
+        xi_sum = np.abs(a[1].sum() - b[1].sum()) / abs(b[1].sum())
+        check = {
+            "work_items_checked": int(n_check), "nb_identical": bool(np.array_equal(a[5], b[5])),
+            "we_max_rel": float(rel_we.max()), "we_median_rel": float(np.median(rel_we)),
+            "xi_median_rel": float(np.median(rel_xi)),
+            "xi_p99_rel": float(np.percentile(rel_xi, 99)),
+            "xi_total_rel": float(xi_sum),
+        }
+
+    # roofline of the pair kernel (FP32 CUDA-core bound)
+    pk, source = peaks()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    accepted = int(rows[5].sum().item())
+    flops = 10.0 * pairs_per_step + 9.0 * accepted
+    kmean = float(np.mean(kernel_s))
+    achieved = flops / kmean / 1e12
+    fp32_peak = sms * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    launches_per_step = 2 + (5 if mode != pairs.MODE_FP64 else 1)
+
+    if rank != 0:
+        return
+    cpu_val, cpu_desc, cores = cpu_sample(fs, params, ang_max, args.cpu_seconds, args.config)
+    line = {
+        "metric": METRIC, "value": value, "unit": "pixel-pairs/s", "n_gpus": world,
+        "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64guard"
+        if mode != pairs.MODE_FP64 else "f64", "data": "synthetic",
+        "config": {"workload": CONFIGS[args.config][3] + ", auto-correlation 50x50 bins, "
+                   "r_par 0-200, r_trans 0-200 Mpc/h", "forests": fs.num,
+                   "pixels": int(dev.num_pixels), "forest_pairs": int(total),
+                   "candidate_pixel_pairs_per_step": int(pairs_per_step),
+                   "accepted_pixel_pairs_per_step": accepted, "precision": args.precision,
+                   "l2": "inputs larger than L2 (%.1f GB resident)" % (dev.h2d_bytes / 1e9),
+                   "parallelism": f"replicas x{world}"},
+        "e2e": {"value": e2e_value, "unit": "pixel-pairs/s", "h2d_bytes_per_step": int(h2d),
+                "d2h_bytes_per_step": int(d2h)},
+        "gpu_launches": launches_per_step * args.steps,
+        "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                     "kernel_ms": kmean * 1e3,
+                     "peak_source": f"SMs x 128 FP32 lanes x 2 x sm_max_mhz ({source} peaks file)",
+                     "flops_per_launch": flops},
+        "precision_check_vs_fp64_kernel": check,
+        "rechecked_pairs_last_step": int(stats.rechecked_pairs),
+        "clocks": clocks,
+        "cpu_baseline": {"value": cpu_val, "unit": "pixel-pairs/s", "cores": cores,
+                         "kind": "port", "sample": cpu_desc},
+    }
+    print(json.dumps(line), flush=True)
+    if world > 1:
+        dist.destroy_process_group()
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

@@ -188,11 +188,18 @@ int64_t oracle_cf_neighbours(const oracle_set *s1, const oracle_set *s2, int32_t
                              int64_t *counts, const int64_t *offsets, int64_t *index)
 {
     int64_t total = 0;
+    /* cheap pre-test standing in for healpy.query_disc: a pair whose dot
+     * product is 1e-5 below cos(ang_max) is > 1e-4 rad beyond ang_max */
+    const double dot_min = (ang_max < 1e-3 || ang_max >= 3.141592653589793) ? -2.0
+                                                                               : cos(ang_max) - 1e-5;
 #pragma omp parallel for schedule(dynamic, 4) reduction(+ : total)
     for (int64_t f = f_begin; f < f_end; ++f) {
         int64_t n = 0;
         int64_t out = offsets ? offsets[f - f_begin] : 0;
         for (int64_t g = 0; g < s2->num; ++g) {
+            if (s2->x_cart[g] * s1->x_cart[f] + s2->y_cart[g] * s1->y_cart[f] +
+                    s2->z_cart[g] * s1->z_cart[f] < dot_min)
+                continue;
             if (s1->thingid[f] == s2->thingid[g]) continue;
             double ang = oracle_angle(s1->x_cart[f], s1->y_cart[f], s1->z_cart[f], s1->ra[f],
                                       s1->dec[f], s1->cos_dec[f], s2->x_cart[g], s2->y_cart[g],
@@ -218,12 +225,17 @@ int64_t oracle_xcf_neighbours(const oracle_set *forests, const oracle_set *objs,
 {
     int64_t total = 0;
     const double f = p->rmu_binning ? p->r_trans_max : 1;
+    const double dot_min = (ang_max < 1e-3 || ang_max >= 3.141592653589793) ? -2.0
+                                                                               : cos(ang_max) - 1e-5;
 #pragma omp parallel for schedule(dynamic, 4) reduction(+ : total)
     for (int64_t k = f_begin; k < f_end; ++k) {
         int64_t n = 0;
         int64_t out = offsets ? offsets[k - f_begin] : 0;
         int64_t p0 = forests->pix_offset[k], p1 = forests->pix_offset[k + 1];
         for (int64_t g = 0; g < objs->num; ++g) {
+            if (objs->x_cart[g] * forests->x_cart[k] + objs->y_cart[g] * forests->y_cart[k] +
+                    objs->z_cart[g] * forests->z_cart[k] < dot_min)
+                continue;
             if (objs->thingid[g] == forests->thingid[k]) continue;
             double ang = oracle_angle(forests->x_cart[k], forests->y_cart[k], forests->z_cart[k],
                                       forests->ra[k], forests->dec[k], forests->cos_dec[k],

@@ -1,0 +1,129 @@
+"""ctypes binding of ``libpicca_gb300.so`` (C ABI in ``include/picca_gb300.h``).
+
+There is no CPU fallback: if the shared library or a CUDA device is missing,
+every entry point raises :class:`NativeError`.
+"""
+
+import ctypes
+import os
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libpicca_gb300.so")
+
+PG_OK = 0
+PG_MODE_FP64 = 0
+PG_MODE_FP32_GUARD = 1
+
+_P = ctypes.POINTER
+_c_double_p = ctypes.c_void_p  # device pointers are passed as integers
+
+
+class NativeError(RuntimeError):
+    """A libpicca_gb300 call failed (status code and message)."""
+
+
+class CorrParams(ctypes.Structure):
+    _fields_ = [
+        ("r_par_min", ctypes.c_double), ("r_par_max", ctypes.c_double),
+        ("r_trans_max", ctypes.c_double),
+        ("num_bins_r_par", ctypes.c_int32), ("num_bins_r_trans", ctypes.c_int32),
+        ("z_min_pairs", ctypes.c_double), ("z_max_pairs", ctypes.c_double),
+        ("zerr_cut_deg", ctypes.c_double), ("zerr_cut_kms", ctypes.c_double),
+        ("ang_max", ctypes.c_double),
+        ("x_correlation", ctypes.c_int32), ("rmu_binning", ctypes.c_int32),
+        ("ang_correlation", ctypes.c_int32),
+        ("remove_same_half_plate_close_pairs", ctypes.c_int32),
+    ]
+
+
+FOREST_SET_PTR_FIELDS = (
+    "pix_offset", "z", "r_comov", "dist_m", "weights", "delta", "ra", "dec", "x_cart", "y_cart",
+    "z_cart", "cos_dec", "z_qso", "r_first", "r_last", "obj_r_comov", "obj_dist_m", "obj_weight",
+    "thingid", "plate", "fiberid", "row")
+
+
+class ForestSetC(ctypes.Structure):
+    _fields_ = ([("num", ctypes.c_int64), ("num_pixels", ctypes.c_int64)]
+                + [(name, ctypes.c_void_p) for name in FOREST_SET_PTR_FIELDS]
+                + [("num_rows", ctypes.c_int32), ("max_pixels", ctypes.c_int32)])
+
+
+class XiRowsC(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_void_p) for name in
+                ("weights", "xi", "r_par", "r_trans", "z", "num_pairs")]
+
+
+class RunStats(ctypes.Structure):
+    _fields_ = [("status", ctypes.c_int32), ("error_detail", ctypes.c_int32),
+                ("rechecked_pairs", ctypes.c_int64), ("recheck_overflows", ctypes.c_int64),
+                ("work_items", ctypes.c_int64)]
+
+
+_LIB = None
+
+
+def lib():
+    """Load the library once; raise NativeError when it cannot be used."""
+    global _LIB
+    if _LIB is not None:
+        return _LIB
+    if not os.path.exists(LIB_PATH):
+        raise NativeError(
+            f"{LIB_PATH} is missing: build it with `python -m picca_gb300.build_ext` "
+            "(this package has no CPU fallback)")
+    handle = ctypes.CDLL(LIB_PATH)
+    handle.pg_strerror.restype = ctypes.c_char_p
+    handle.pg_strerror.argtypes = [ctypes.c_int]
+    handle.pg_version.restype = ctypes.c_int
+    handle.pg_plan_create.argtypes = [_P(ctypes.c_void_p)]
+    handle.pg_plan_destroy.argtypes = [ctypes.c_void_p]
+    handle.pg_plan_stats.argtypes = [ctypes.c_void_p, _P(RunStats)]
+    handle.pg_cf_neighbours.argtypes = [
+        ctypes.c_void_p, _P(CorrParams), _P(ForestSetC), _P(ForestSetC), ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    handle.pg_xcf_neighbours.argtypes = handle.pg_cf_neighbours.argtypes
+    handle.pg_cf_xi.argtypes = [
+        ctypes.c_void_p, _P(CorrParams), _P(ForestSetC), _P(ForestSetC), ctypes.c_void_p,
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
+        _P(XiRowsC), ctypes.c_void_p]
+    handle.pg_xcf_xi.argtypes = handle.pg_cf_xi.argtypes
+    for name in ("pg_plan_create", "pg_plan_destroy", "pg_plan_stats", "pg_cf_neighbours",
+                 "pg_xcf_neighbours", "pg_cf_xi", "pg_xcf_xi"):
+        getattr(handle, name).restype = ctypes.c_int
+    _LIB = handle
+    return handle
+
+
+def check(status, what):
+    """Raise NativeError for a nonzero status."""
+    if status != PG_OK:
+        msg = lib().pg_strerror(status).decode()
+        raise NativeError(f"{what} failed: {msg} (status {status})")
+
+
+class Plan:
+    """Owns a pg_plan (device scratch) on the current CUDA device."""
+
+    def __init__(self):
+        self._handle = ctypes.c_void_p()
+        check(lib().pg_plan_create(ctypes.byref(self._handle)), "pg_plan_create")
+
+    @property
+    def handle(self):
+        return self._handle
+
+    def stats(self):
+        out = RunStats()
+        check(lib().pg_plan_stats(self._handle, ctypes.byref(out)), "pg_plan_stats")
+        return out
+
+    def close(self):
+        if self._handle:
+            lib().pg_plan_destroy(self._handle)
+            self._handle = ctypes.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:  # pylint: disable=broad-except
+            pass

@@ -127,6 +127,23 @@ class ForestSet:
             healpix=hp_of, healpix_list=np.array(keys, dtype=np.int64),
         )
 
+    def take(self, indices):
+        """Forests ``indices`` (sorted), with rows renumbered over their healpix."""
+        idx = np.asarray(indices, dtype=np.int64)
+        npix = self.npix[idx]
+        offset = np.zeros(len(idx) + 1, dtype=np.int64)
+        np.cumsum(npix, out=offset[1:])
+        starts = self.pix_offset[idx]
+        fid = np.repeat(np.arange(len(idx)), npix)
+        pix_idx = starts[fid] + (np.arange(offset[-1]) - offset[fid])
+        kwargs = {"pix_offset": offset}
+        if self.num_pixels:
+            for key in PIXEL_FIELDS:
+                kwargs[key] = getattr(self, key)[pix_idx]
+        for key in FOREST_F64 + FOREST_I64:
+            kwargs[key] = getattr(self, key)[idx]
+        return ForestSet(**kwargs)
+
     def subset_rows(self, rows):
         """Forests whose row is in ``rows`` (keeps pixel data contiguous)."""
         rows = np.asarray(rows)

@@ -1,0 +1,182 @@
+"""Drop-in replacement for the correlation part of ``picca.xcf``.
+
+Same module globals (py/picca/xcf.py:27-68) and functions ``fill_neighs``
+(:71-123), ``compute_xi`` (:126-220) and the 16-argument
+``compute_xi_forest_pairs_fast`` (:223-322), computed on the GPU. As in
+``picca_gb300.cf``, the first call runs every healpix in one launch
+(``compute_xi_all``) and later calls are served from that result.
+"""
+
+import numpy as np
+
+from . import pairs as _pairs
+from .forests import ForestSet
+
+num_bins_r_par = None
+num_bins_r_trans = None
+num_model_bins_r_par = None
+num_model_bins_r_trans = None
+r_par_max = None
+r_par_min = None
+r_trans_max = None
+z_min_pairs = None
+z_max_pairs = None
+ang_max = None
+nside = None
+
+zerr_cut_deg = None
+zerr_cut_kms = None
+
+counter = None
+num_data = None
+
+z_ref = None
+alpha = None
+alpha_obj = None
+lambda_abs = None
+alpha_abs = None
+
+data = None
+objs = None
+
+reject = None
+lock = None
+
+cosmo = None
+rmu_binning = False
+ang_correlation = False
+
+precision = "fp32_guard"
+
+_cache = {"key": None, "result": None, "engine": None}
+
+
+def _mode():
+    if precision == "fp64":
+        return _pairs.MODE_FP64
+    if precision == "fp32_guard":
+        return _pairs.MODE_FP32_GUARD
+    raise ValueError(f"unknown precision {precision!r}")
+
+
+def _params(angle_max=None):
+    return _pairs.make_params(
+        r_par_min, r_par_max, r_trans_max, num_bins_r_par, num_bins_r_trans,
+        ang_max if angle_max is None else angle_max, z_min_pairs=z_min_pairs,
+        z_max_pairs=z_max_pairs, zerr_cut_deg=zerr_cut_deg, zerr_cut_kms=zerr_cut_kms,
+        x_correlation=True, rmu_binning=rmu_binning, ang_correlation=ang_correlation)
+
+
+def _engine():
+    if _cache["engine"] is None:
+        _cache["engine"] = _pairs.PairEngine()
+    return _cache["engine"]
+
+
+def _state_key():
+    return (id(data), id(objs), num_bins_r_par, num_bins_r_trans, r_par_min, r_par_max,
+            r_trans_max, z_min_pairs, z_max_pairs, zerr_cut_deg, zerr_cut_kms, ang_max,
+            rmu_binning, ang_correlation, precision)
+
+
+def compute_xi_all():
+    """Quasar neighbours and pair sums of every healpix in one GPU pass."""
+    key = _state_key()
+    if _cache["key"] == key and _cache["result"] is not None:
+        return _cache["result"]
+    if data is None or objs is None:
+        raise ValueError("xcf.data and xcf.objs must be set")
+    if ang_max is None or num_bins_r_par is None:
+        raise ValueError("xcf module globals must be set before computing correlations")
+    fs = ForestSet.from_deltas(data, ang_correlation=ang_correlation)
+    qs = ForestSet.from_objects(objs, ang_correlation=ang_correlation)
+    res = _pairs.correlate(fs, qs, _params(), mode=_mode(), xcf=True, engine=_engine())
+    we, xi, rp, rt, zz, nb = res["raw"]
+    xi_n, rp_n, rt_n, zz_n = _pairs.normalise(we, xi, rp, rt, zz)
+    result = {
+        "healpix_list": fs.healpix_list, "weights": we, "xi": xi_n, "r_par": rp_n,
+        "r_trans": rt_n, "z": zz_n, "num_pairs": nb, "raw": res["raw"],
+        "candidate_pairs": res["candidate_pairs"], "rechecked_pairs": res["rechecked_pairs"],
+        "forest_pairs": res["num_pairs_forest"],
+        "nbr_offsets": res["offsets"].cpu().numpy(),
+        "nbr_index": res["index"].cpu().numpy()[: res["num_pairs_forest"]],
+        "set1": fs, "set2": qs,
+    }
+    _cache["key"] = key
+    _cache["result"] = result
+    return result
+
+
+def fill_neighs(healpixs):
+    """Set ``delta.neighbours`` (array of QSO) for every delta of healpixs."""
+    result = compute_xi_all()
+    fs, qs = result["set1"], result["set2"]
+    quasars = [o for hp in qs.healpix_list for o in objs[hp]]
+    firsts = np.searchsorted(fs.row, np.arange(len(fs.healpix_list)))
+    offsets, index = result["nbr_offsets"], result["nbr_index"]
+    for healpix in healpixs:
+        row = int(np.searchsorted(fs.healpix_list, healpix))
+        for k, delta in enumerate(data[healpix]):
+            f = firsts[row] + k
+            delta.neighbours = np.array([quasars[g] for g in index[offsets[f]:offsets[f + 1]]])
+
+
+def compute_xi(healpixs):
+    """(weights, xi, r_par, r_trans, z, num_pairs) summed over healpixs."""
+    result = compute_xi_all()
+    rows = np.searchsorted(result["healpix_list"], np.asarray(list(healpixs)))
+    we, xi, rp, rt, zz, nb = result["raw"]
+    weights = we[rows].sum(axis=0)
+    sums = [a[rows].sum(axis=0) for a in (xi, rp, rt, zz)]
+    num_pairs = nb[rows].sum(axis=0).astype(np.int64)
+    for healpix in healpixs:
+        for delta in data[healpix]:
+            delta.neighbours = None
+    xi_n, rp_n, rt_n, z_n = _pairs.normalise(weights, *sums)
+    return weights, xi_n, rp_n, rt_n, z_n, num_pairs
+
+
+def compute_xi_forest_pairs_fast(z1, r_comov1, dist_m1, weights1, delta1, z2, r_comov2, dist_m2,
+                                 weights2, ang, rebin_weight, rebin_xi, rebin_r_par,
+                                 rebin_r_trans, rebin_z, rebin_num_pairs):
+    """One forest against quasar arrays (z2, r_comov2, dist_m2, weights2,
+    ang), accumulated in place (py/picca/xcf.py:223-322 signature)."""
+    import torch  # pylint: disable=import-outside-toplevel
+
+    n = len(z1)
+    m = len(z2)
+    fs = ForestSet(
+        pix_offset=np.array([0, n], dtype=np.int64), z=np.asarray(z1, float),
+        r_comov=np.asarray(r_comov1, float), dist_m=np.asarray(dist_m1, float),
+        weights=np.asarray(weights1, float), delta=np.asarray(delta1, float),
+        log_lambda=np.zeros(n), ra=np.zeros(1), dec=np.zeros(1), x_cart=np.ones(1),
+        y_cart=np.zeros(1), z_cart=np.zeros(1), cos_dec=np.ones(1), z_qso=np.zeros(1),
+        thingid=np.array([-1]), healpix=np.zeros(1, dtype=np.int64))
+    qs = ForestSet(
+        ra=np.zeros(m), dec=np.zeros(m), x_cart=np.ones(m), y_cart=np.zeros(m),
+        z_cart=np.zeros(m), cos_dec=np.ones(m), z_qso=np.asarray(z2, float),
+        obj_r_comov=np.asarray(r_comov2, float), obj_dist_m=np.asarray(dist_m2, float),
+        obj_weight=np.asarray(weights2, float), thingid=np.arange(m, dtype=np.int64),
+        healpix=np.zeros(m, dtype=np.int64))
+    engine = _engine()
+    dev1 = _pairs.DeviceForests(fs, engine.device)
+    dev2 = _pairs.DeviceForests(qs, engine.device)
+    dev = engine.device
+    offsets = torch.tensor([0, m], dtype=torch.int64, device=dev)
+    index = torch.arange(max(m, 1), dtype=torch.int32, device=dev)
+    angles = torch.tensor(np.asarray(ang, dtype=float).reshape(-1) if m else [0.0],
+                          dtype=torch.float64, device=dev)
+    order = torch.zeros(1, dtype=torch.int32, device=dev)
+    nbins = len(rebin_weight)
+    rows = engine.alloc_rows(1, nbins)
+    if m:
+        engine.accumulate(_params(np.pi), dev1, dev2, offsets, index, order, 1, rows, _mode(),
+                          xcf=True, angles=angles)
+        engine.stats()
+    we, xi, rp, rt, zz, nb = [r.cpu().numpy() for r in rows]
+    rebin_weight += we
+    rebin_xi += xi
+    rebin_r_par += rp
+    rebin_r_trans += rt
+    rebin_z += zz
+    rebin_num_pairs += nb
