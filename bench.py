@@ -43,12 +43,17 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--config", default="2", choices=sorted(CONFIGS))
+    p.add_argument("--config", default="1", choices=sorted(CONFIGS))
     p.add_argument("--precision", choices=["fp32_guard", "fp64"], default="fp32_guard")
     p.add_argument("--check-fraction", type=float, default=0.01,
                    help="fraction of work items re-run in FP64 for the error report")
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="target CPU time of the oracle sample")
+    p.add_argument("--continuum-forests", type=int, default=400_000,
+                   help="raw forests of the continuum-fit leg (configs 3/4); 0 skips it")
+    p.add_argument("--continuum-train", type=int, default=200_000,
+                   help="raw forests (separate seed) the warm-start network is trained on")
+    p.add_argument("--continuum-iterations", type=int, default=5)
     return p.parse_args()
 
 
@@ -159,6 +164,101 @@ def cpu_sample(fs, params, ang_max, seconds, cfg):
     cand = int((npix[sample] * (csum[offsets[1:]] - csum[offsets[:-1]])).sum())
     return cand / elapsed, (f"{len(sample)} forests with all their neighbours, from "
                             f"{len(rows)} healpix of config {cfg}; {elapsed:.1f} s"), cores
+
+
+def continuum_leg(args, cpu_seconds):
+    """Configs 3 and 4: the plain batched Dr16 fit and the learned warm start.
+
+    A fit is one forest in one outer iteration. Both legs run the same
+    number of iterations of the whole Dr16 loop (fits, GPU histograms, host
+    updates) on the same forests; the warm-start network is trained first
+    on plain fits of a separate set (training time reported separately)."""
+    import torch
+
+    from picca_gb300 import continuum, learned, synthetic_spectra
+    if args.continuum_forests <= 0:
+        return None
+    iters = args.continuum_iterations
+    eval_raw = synthetic_spectra.make_raw_forests(args.continuum_forests, 20261204)
+    train_raw = synthetic_spectra.make_raw_forests(args.continuum_train, 20261205)
+
+    def timed_loop(run):
+        torch.cuda.synchronize()
+        start = torch.cuda.Event(enable_timing=True)
+        end = torch.cuda.Event(enable_timing=True)
+        start.record()
+        out = run()
+        end.record()
+        torch.cuda.synchronize()
+        return out, start.elapsed_time(end) / 1e3
+
+    # warm-up on a small set (module loading, first launches)
+    small = synthetic_spectra.make_raw_forests(2000, 7)
+    eng = continuum.Dr16Gpu(small.grid, num_iterations=2)
+    eng.run(continuum.DeviceSpectra(small, eng.device))
+
+    # plain leg (config 3): fit kernel time measured separately
+    eng_p = continuum.Dr16Gpu(eval_raw.grid, num_iterations=iters)
+    spectra = continuum.DeviceSpectra(eval_raw, eng_p.device)
+    fit_events = []
+    orig_fit = eng_p.fit
+
+    def fit_timed(sp, **kw):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        out = orig_fit(sp, **kw)
+        e1.record()
+        fit_events.append((e0, e1))
+        return out
+
+    eng_p.fit = fit_timed
+    plain_fit, plain_s = timed_loop(lambda: eng_p.run(spectra))
+    fit_ms = [a.elapsed_time(b) for a, b in fit_events]
+    plain = continuum.fit_results_to_host(plain_fit)
+
+    # training (separate seed) on plain fits
+    eng_t = continuum.Dr16Gpu(train_raw.grid, num_iterations=iters)
+    train = continuum.DeviceSpectra(train_raw, eng_t.device)
+    (feats, targs, _), collect_s = timed_loop(lambda: learned.collect_training(eng_t, train))
+    net = learned.WarmStartMLP(seed=0)
+    hist, train_s = timed_loop(lambda: net.train(feats, targs, epochs=4, batch=4096, lr=2e-3))
+    num_samples = int(feats.shape[0])
+    del feats, targs, train
+
+    # learned leg (config 4) on the same evaluation forests
+    eng_w = continuum.Dr16Gpu(eval_raw.grid, num_iterations=iters)
+    (warm_fit, stats), warm_s = timed_loop(lambda: learned.run_warm(eng_w, spectra, net))
+    warm = continuum.fit_results_to_host(warm_fit)
+    ok = (plain["status"] == 0) & (warm["status"] == 0)
+    scale = np.maximum(1.0, np.maximum(np.abs(plain["zero_point"]), np.abs(plain["slope"])))
+    dab = np.maximum(np.abs(warm["zero_point"] - plain["zero_point"]),
+                     np.abs(warm["slope"] - plain["slope"]))[ok] / scale[ok]
+    dchi = np.abs(warm["chi2"] - plain["chi2"])[ok] / np.abs(plain["chi2"][ok])
+    nfits = eval_raw.num * iters
+    # bytes per forest-fit: 40 n + 32 (n pixels; four FP64 inputs, continuum out)
+    npix = float(eval_raw.pix_offset[-1])
+    fit_bytes = 40.0 * npix + 32.0 * eval_raw.num
+    pk, source = peaks()
+    achieved = fit_bytes / (np.mean(fit_ms) / 1e3) / 1e9
+    return {
+        "forests": eval_raw.num, "iterations": iters, "solver": "FP64 damped Newton, warp per forest",
+        "plain_fits_per_s": nfits / plain_s, "learned_fits_per_s": nfits / warm_s,
+        "learned_over_plain": plain_s / warm_s,
+        "fallback_rate": float(np.mean([st["fallback"] for st in stats]) / eval_raw.num),
+        "newton_iterations_plain_last": float(plain["iterations"].mean()),
+        "newton_iterations_learned_last": float(warm["iterations"].mean()),
+        "ab_max_rel_diff": float(dab.max()) if dab.size else None,
+        "chi2_max_rel_diff": float(dchi.max()) if dchi.size else None,
+        "accepted_fraction": float(ok.mean()),
+        "fit_kernel_ms_mean": float(np.mean(fit_ms)),
+        "fit_roofline": {"bound": "hbm", "achieved": achieved, "peak": pk.get("hbm_gbs"),
+                         "unit": "GB/s", "frac": achieved / pk.get("hbm_gbs", 6800.0),
+                         "bytes_per_launch": fit_bytes, "peak_source": source},
+        "training": {"forests": args.continuum_train, "samples": num_samples, "epochs": len(hist),
+                     "collect_s": collect_s, "train_s": train_s, "loss_first": hist[0],
+                     "loss_last": hist[-1]},
+    }
 
 
 def run_reference(args):
@@ -318,6 +418,9 @@ def run_ours(args):
     if rank != 0:
         return
     cpu_val, cpu_desc, cores = cpu_sample(fs, params, ang_max, args.cpu_seconds, args.config)
+    del dev, packed, engine
+    torch.cuda.empty_cache()
+    cont = continuum_leg(args, args.cpu_seconds)
     line = {
         "metric": METRIC, "value": value, "unit": "pixel-pairs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
@@ -343,6 +446,7 @@ def run_ours(args):
         "clocks": clocks,
         "cpu_baseline": {"value": cpu_val, "unit": "pixel-pairs/s", "cores": cores,
                          "kind": "port", "sample": cpu_desc},
+        "continuum": cont,
     }
     print(json.dumps(line), flush=True)
     if world > 1:

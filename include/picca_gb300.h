@@ -149,6 +149,150 @@ int pg_xcf_xi(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *
               const double *nbr_angle, const int32_t *work_order, int64_t num_work,
               int32_t mode, const pg_xi_rows *out, void *stream);
 
+/* ------------------------------------------------------------------------ */
+/* Dr16 continuum fit                                                        */
+/* ------------------------------------------------------------------------ */
+/* Reference interfaces replaced (picca v9.21.0):
+ *  - pg_cont_fit_batch  <- expected_fluxes/utils.py:12-136 compute_continuum
+ *                          with least_squares_cont_model.py:65-197 (chi2 of
+ *                          the (zero_point, slope) continuum model), run for
+ *                          every forest (dr16_expected_flux.py:389-425)
+ *  - pg_cont_stacks     <- expected_flux.py:256-308 _compute_mean_cont,
+ *                          least_squares_var_stats.py:134-198
+ *                          initialize_delta_arrays, expected_flux.py:190-236
+ *                          compute_delta_stack (bin sums; normalisation and
+ *                          the 20 variance fits stay on the host)
+ *  - pg_cont_deltas     <- dr16_expected_flux.py:706-740 populate_los_ids +
+ *                          expected_flux.py:328-349 extract_deltas
+ * All paths under delta_extraction/ are relative to py/picca. */
+
+/* Raw forests (device pointers): pixels of forest f are
+ * [pix_offset[f], pix_offset[f+1]). */
+typedef struct pg_spectra {
+    int64_t num;
+    int64_t num_pixels;
+    const int64_t *pix_offset;
+    const double *log_lambda, *flux, *ivar, *transmission_correction;
+    const double *z_qso;
+} pg_spectra;
+
+/* Current model of the Dr16 iteration (device pointers).
+ * Mean continuum: linear interpolation with extrapolation on
+ * (mean_cont_x, mean_cont_y), num_mean_cont points (rest-frame log lambda).
+ * eta, var_lss, fudge: piecewise cubics on var_breaks[0..num_var_intervals]
+ * with coefficients coef[k*num_var_intervals + i], k = 0..3 highest power
+ * first (the polynomial form of scipy's not-a-knot cubic interp1d),
+ * extrapolated with the end pieces. Stack of deltas: nearest-point lookup
+ * on stack_x (num_stack points); NULL means 1. */
+typedef struct pg_cont_model {
+    int32_t num_mean_cont;
+    const double *mean_cont_x, *mean_cont_y;
+    int32_t num_var_intervals;
+    const double *var_breaks, *eta_coef, *var_lss_coef, *fudge_coef;
+    int32_t num_stack;
+    const double *stack_x, *stack_y;
+    double log_lambda_rest_min, log_lambda_rest_max;  /* rest-frame grid ends */
+    double var_lss_mod;
+    int32_t order;                /* 0: slope fixed at 0; 1: free slope */
+    int32_t use_constant_weight;
+} pg_cont_model;
+
+/* Per-forest fit results (device pointers, [num]); continuum is per pixel
+ * ([num_pixels], may be NULL). status: 0 ok, 1 not converged, 2 negative
+ * continuum, 3 zero continuum (the bad_continuum_reason values of
+ * compute_continuum). */
+typedef struct pg_cont_fit {
+    double *zero_point, *slope, *chi2;
+    int32_t *ndata, *status, *iterations;
+    double *continuum;
+} pg_cont_fit;
+
+/* Histograms of one Dr16 iteration (device pointers, ACCUMULATED into;
+ * NULL skips a group): rest-frame mean continuum (mean_cont_num,
+ * mean_cont_weight, [rest_bins]), variance statistics (var_mean, var_delta2,
+ * var_delta4, var_npix, var_nqso, [20 * 100] = wavelength x log var_pipe
+ * bins), observed-frame stack (stack_num, stack_weight, [obs_bins]). */
+typedef struct pg_cont_stacks {
+    int32_t rest_bins;
+    double rest_grid0, rest_step;
+    double *mean_cont_num, *mean_cont_weight;
+    int32_t var_lambda_bins;
+    double var_grid0, var_step;
+    double *var_mean, *var_delta2, *var_delta4, *var_npix, *var_nqso;
+    int32_t obs_bins;
+    double obs_grid0, obs_step;
+    double *stack_num, *stack_weight;
+} pg_cont_stacks;
+
+#define PG_FIT_FP64 0        /* per-pixel chi2 terms in FP64                   */
+#define PG_FIT_MIXED 1       /* per-pixel terms in FP32, sums and the 2x2
+                                Newton solve in FP64                         */
+
+/* Fit (zero_point, slope) of every forest by damped Newton iterations on the
+ * chi2 of the continuum model. start (optional, [2*num], device) gives a
+ * warm start (zero_point, slope) per forest; NULL starts from the
+ * ivar-weighted mean flux and slope 0 (utils.py:92-94). Iterations stop
+ * when the step is below tol * max(1, |a|, |b|) or after max_iter. */
+int pg_cont_fit_batch(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
+                const double *start, int32_t max_iter, double tol, int32_t mode,
+                const pg_cont_fit *out, void *stream);
+
+/* Accumulate the histograms of one Dr16 iteration from fitted continua
+ * (forests with status != 0 are skipped, as bad_continuum_reason is). */
+int pg_cont_stacks_accumulate(pg_plan *plan, const pg_spectra *spectra,
+                              const pg_cont_model *model, const pg_cont_fit *fit,
+                              const pg_cont_stacks *stacks, void *stream);
+
+/* Final deltas and weights per pixel: expected flux = continuum * stack,
+ * weights of compute_forest_weights, delta = flux / expected - 1 where the
+ * weight is positive (0 elsewhere). Forests with status != 0 get weight 0. */
+int pg_cont_deltas(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
+                   const pg_cont_fit *fit, double *delta, double *weights, void *stream);
+
+/* ------------------------------------------------------------------------ */
+/* Learned warm start for the continuum fit. No counterpart in the           */
+/* reference: kernels of a small MLP (BF16 tensor-core GEMM with FP32        */
+/* accumulation, bias-gradient column sums, MSE gradient, Adam).            */
+/* All pointers are device pointers; bf16 values are passed as uint16_t.     */
+/* ------------------------------------------------------------------------ */
+#define PG_MLP_EPI_NONE 0
+#define PG_MLP_EPI_GELU 1        /* out = gelu(acc + bias)                     */
+#define PG_MLP_EPI_GELU_GRAD 2   /* out = (acc + bias) * gelu'(zin)            */
+
+/* C[m, n] = A[m, k] B[k, n] with element strides A(i, l) = a[i*sam + l*sak],
+ * B(l, j) = b[l*sbk + j*sbn]; optional bias[n], epilogue, pre-activation
+ * output zout / input zin ([m, ldz] FP32), bf16 output c and/or FP32 output
+ * cf ([m, ldc]; cf = result + beta * cf). */
+int pg_mlp_gemm(const uint16_t *a, int64_t sam, int64_t sak, const uint16_t *b, int64_t sbk,
+                int64_t sbn, int32_t m, int32_t n, int32_t k, const float *bias, int32_t epilogue,
+                const float *zin, float *zout, int64_t ldz, uint16_t *c, float *cf, int64_t ldc,
+                float beta, void *stream);
+
+/* out[j] = sum_i x[i, j] for a bf16 [m, ldx] matrix. */
+int pg_mlp_colsum(const uint16_t *x, int32_t m, int32_t n, int64_t ldx, float *out,
+                  void *stream);
+
+/* dy = 2 (y - t) / m as bf16 ([m, n]); loss += sum (y - t)^2 / m if loss. */
+int pg_mlp_mse_grad(const float *y, const float *t, int32_t m, int32_t n, uint16_t *dy,
+                    float *loss, void *stream);
+
+/* One Adam step on n FP32 parameters (bias-corrected, optional decoupled
+ * weight decay); writes the bf16 copy when params_bf16 is not NULL. */
+int pg_mlp_adam(float *params, const float *grads, float *m1, float *m2, uint16_t *params_bf16,
+                int64_t n, float lr, float beta1, float beta2, float eps, int32_t step,
+                float weight_decay, void *stream);
+
+/* bf16 copy of an FP32 array. */
+int pg_mlp_to_bf16(const float *x, uint16_t *y, int64_t n, void *stream);
+
+/* Per-forest input features of the warm-start network: 64 bins of
+ * flux / mean continuum over the rest-frame range (ivar-weighted means,
+ * divided by the forest's ivar-weighted mean flux a0, minus 1; empty bins
+ * 0), (z_qso - 3), and log of the mean flux*sqrt(ivar); features[f *
+ * feat_stride + j] as bf16 (columns 66..feat_stride-1 zeroed); a0[f] FP64. */
+int pg_mlp_features(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
+                    uint16_t *features, int32_t feat_stride, double *a0, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

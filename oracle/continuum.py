@@ -183,3 +183,184 @@ def var_stats_fit(var_delta, var2_delta, num_qso, var_pipe_values, min_num_qso, 
     for k, v in zip(keep, res.x):
         out[k] = v
     return out[0], out[1], out[2] * FUDGE_REF
+
+
+def find_bins_log(values, grid):
+    """find_bins_log (py/picca/delta_extraction/utils.py:163-186)."""
+    step = grid[1] - grid[0]
+    return ((values - grid[0]) / step + 0.5).astype(np.int64)
+
+
+def forest_weights(log_lambda, ivar, continuum, get_eta, get_var_lss, get_fudge, var_lss_mod=1.0):
+    """Dr16ExpectedFlux.compute_forest_weights (dr16_expected_flux.py:466-488)."""
+    w = ivar > 0
+    weights = np.empty_like(log_lambda)
+    weights[~w] = 0.0
+    var_pipe = 1. / ivar[w] / continuum[w]**2
+    weights[w] = 1.0 / (get_eta(log_lambda[w]) * var_pipe +
+                        var_lss_mod * get_var_lss(log_lambda[w]) +
+                        get_fudge(log_lambda[w]) / var_pipe)
+    return weights
+
+
+class Dr16Oracle:
+    """Dr16ExpectedFlux.compute_expected_flux restated per forest in numpy
+    (dr16_expected_flux.py:380-464 with the helpers cited above)."""
+
+    def __init__(self, grid, num_iterations=5, order=1, limit_eta=(0.5, 1.5),
+                 limit_var_lss=(0., 0.3), min_num_qso_in_fit=100, num_bins_variance=20,
+                 var_lss_mod=1.0):
+        self.grid = grid
+        self.num_iterations = num_iterations
+        self.order = order
+        self.limit_eta = limit_eta
+        self.limit_var_lss = limit_var_lss
+        self.min_num_qso_in_fit = min_num_qso_in_fit
+        self.var_lss_mod = var_lss_mod
+        rest = grid.log_lambda_rest_frame_grid
+        self.var_grid = np.linspace(grid.log_lambda_grid[0], grid.log_lambda_grid[-1],
+                                    num_bins_variance)
+        self.get_mean_cont = interp1d(rest, np.ones_like(rest), fill_value="extrapolate")
+        nvb = num_bins_variance
+        self.get_eta = interp1d(self.var_grid, np.ones(nvb), fill_value="extrapolate",
+                                kind="cubic")
+        self.get_var_lss = interp1d(self.var_grid, np.full(nvb, 0.1), fill_value="extrapolate",
+                                    kind="cubic")
+        self.get_fudge = interp1d(self.var_grid, np.zeros(nvb), fill_value="extrapolate",
+                                  kind="cubic")
+        self.get_stack_delta = None
+
+    def fit_all(self, raw):
+        rest = self.grid.log_lambda_rest_frame_grid
+        conts, params = [], []
+        for k in range(raw.num):
+            ll, fl, iv, tc = raw.forest(k)
+            cont, reason, fit, _ = fit_forest(ll, fl, iv, raw.z_qso[k], self.get_mean_cont,
+                                              self.get_eta, self.get_var_lss, self.get_fudge,
+                                              rest[0], rest[-1], transmission_correction=tc,
+                                              order=self.order)
+            conts.append(cont)
+            params.append((fit, reason))
+        return conts, params
+
+    def stacks(self, raw, conts):
+        grid = self.grid
+        rest, obs = grid.log_lambda_rest_frame_grid, grid.log_lambda_grid
+        out = {"mc_num": np.zeros_like(rest), "mc_w": np.zeros_like(rest),
+               "s_num": np.zeros_like(obs), "s_w": np.zeros_like(obs)}
+        nvar = len(self.var_grid) * NUM_VAR_BINS
+        for key in ("v_mean", "v_d2", "v_d4", "v_np", "v_nq"):
+            out[key] = np.zeros(nvar)
+        for k in range(raw.num):
+            cont = conts[k]
+            if cont is None:
+                continue
+            ll, fl, iv, _ = raw.forest(k)
+            weights = forest_weights(ll, iv, cont, self.get_eta, self.get_var_lss,
+                                     self.get_fudge, self.var_lss_mod)
+            bins = find_bins_log(ll - np.log10(1 + raw.z_qso[k]), rest)
+            out["mc_num"] += np.bincount(bins, weights=fl / (cont + 1e-16) * weights,
+                                         minlength=len(rest))
+            out["mc_w"] += np.bincount(bins, weights=weights, minlength=len(rest))
+            delta = np.zeros_like(ll)
+            w = iv > 0
+            delta[w] = fl[w] / cont[w]
+            bins = find_bins_log(ll, obs)
+            out["s_num"] += np.bincount(bins, weights=delta * weights, minlength=len(obs))
+            out["s_w"] += np.bincount(bins, weights=weights, minlength=len(obs))
+            var_pipe = np.empty_like(ll)
+            var_pipe[w] = 1 / iv[w] / cont[w]**2
+            var_pipe[~w] = np.inf
+            w &= (np.log10(var_pipe) > VAR_PIPE_MIN) & (np.log10(var_pipe) < VAR_PIPE_MAX)
+            vbins = ((np.log10(var_pipe[w]) - VAR_PIPE_MIN) /
+                     (VAR_PIPE_MAX - VAR_PIPE_MIN) * NUM_VAR_BINS).astype(int)
+            lbins = find_bins_log(ll[w], self.var_grid)
+            bins = vbins + NUM_VAR_BINS * lbins
+            d = fl[w] / cont[w] - 1
+            out["v_mean"] += np.bincount(bins, weights=d, minlength=nvar)
+            out["v_d2"] += np.bincount(bins, weights=d**2, minlength=nvar)
+            out["v_d4"] += np.bincount(bins, weights=d**4, minlength=nvar)
+            out["v_np"] += np.bincount(bins, minlength=nvar)
+            out["v_nq"][np.unique(bins)] += 1
+        return out
+
+    def update(self, sums, last):
+        """Mean continuum (expected_flux.py:291-308), variance functions
+        (least_squares_var_stats.py:183-198, dr16_expected_flux.py:531-617)
+        and the delta stack (expected_flux.py:226-236) from the bin sums."""
+        grid = self.grid
+        if not last:
+            mean_cont = sums["mc_num"].copy()
+            w = sums["mc_w"] > 0
+            mean_cont[w] /= sums["mc_w"][w]
+            mean_cont /= mean_cont[w].mean()
+            rest = grid.log_lambda_rest_frame_grid[w]
+            new_cont = self.get_mean_cont(rest) * mean_cont[w]
+            self.get_mean_cont = interp1d(rest, new_cont, fill_value="extrapolate")
+            var_delta = sums["v_d2"].copy()
+            mean_delta = sums["v_mean"].copy()
+            var2 = sums["v_d4"].copy()
+            npix = sums["v_np"]
+            w = npix > 0
+            var_delta[w] /= npix[w]
+            mean_delta[w] /= npix[w]
+            var_delta -= mean_delta**2
+            var2[w] /= npix[w]
+            var2 -= var_delta**2
+            var2[w] /= npix[w]
+            var_pipe = 10**(VAR_PIPE_MIN + ((np.arange(NUM_VAR_BINS) + .5) *
+                                            (VAR_PIPE_MAX - VAR_PIPE_MIN) / NUM_VAR_BINS))
+            eta = self.get_eta(self.var_grid)
+            vlss = self.get_var_lss(self.var_grid)
+            fudge = self.get_fudge(self.var_grid)
+            npix_bin = np.zeros(len(self.var_grid))
+            for index in range(len(self.var_grid)):
+                sl = slice(index * NUM_VAR_BINS, (index + 1) * NUM_VAR_BINS)
+                npix_bin[index] = npix[sl].sum()
+                sel = (sums["v_nq"][sl] > self.min_num_qso_in_fit) & (var2[sl] > 0)
+                if sel.sum() == 0:
+                    continue
+                sol = var_stats_fit(var_delta[sl], var2[sl], sums["v_nq"][sl], var_pipe,
+                                    self.min_num_qso_in_fit, self.limit_eta, self.limit_var_lss,
+                                    start=[eta[index], vlss[index], fudge[index] / FUDGE_REF])
+                eta[index], vlss[index], fudge[index] = sol
+            w = npix_bin > 0
+            self.get_eta = interp1d(self.var_grid[w], eta[w], fill_value="extrapolate",
+                                    kind="cubic")
+            self.get_var_lss = interp1d(self.var_grid[w], vlss[w], fill_value="extrapolate",
+                                        kind="cubic")
+            self.get_fudge = interp1d(self.var_grid[w], fudge[w], fill_value="extrapolate",
+                                      kind="cubic")
+        stack = sums["s_num"].copy()
+        w = sums["s_w"] > 0
+        stack[w] /= sums["s_w"][w]
+        self.get_stack_delta = interp1d(grid.log_lambda_grid[w], stack[w], kind="nearest",
+                                        fill_value="extrapolate")
+
+    def run(self, raw):
+        """All iterations; returns the last (continua, fit parameters)."""
+        conts = params = None
+        for iteration in range(self.num_iterations):
+            conts, params = self.fit_all(raw)
+            last = iteration == self.num_iterations - 1
+            self.update(self.stacks(raw, conts), last)
+        return conts, params
+
+    def deltas(self, raw, conts):
+        """populate_los_ids + extract_deltas (dr16_expected_flux.py:706-740,
+        expected_flux.py:328-349): per-pixel deltas and weights."""
+        delta = np.zeros(raw.pix_offset[-1])
+        weights = np.zeros(raw.pix_offset[-1])
+        for k in range(raw.num):
+            if conts[k] is None:
+                continue
+            ll, fl, iv, _ = raw.forest(k)
+            expected = conts[k] * self.get_stack_delta(ll)
+            w = forest_weights(ll, iv, expected, self.get_eta, self.get_var_lss, self.get_fudge,
+                               self.var_lss_mod)
+            sl = slice(raw.pix_offset[k], raw.pix_offset[k + 1])
+            d = np.zeros_like(fl)
+            d[w > 0] = fl[w > 0] / expected[w > 0] - 1
+            delta[sl] = d
+            weights[sl] = w
+        return delta, weights

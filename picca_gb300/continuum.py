@@ -1,0 +1,422 @@
+"""GPU Dr16 continuum fitting (host driver of the ``pg_cont_*`` C ABI).
+
+Mirrors ``Dr16ExpectedFlux.compute_expected_flux``
+(py/picca/delta_extraction/expected_fluxes/dr16_expected_flux.py:380-464):
+for ``num_iterations`` iterations, fit every forest's continuum
+(``compute_continuum``, expected_fluxes/utils.py:12-136) on the GPU, then,
+except after the last iteration, update the mean continuum
+(expected_flux.py:256-308) and the variance functions eta, var_lss and
+fudge (dr16_expected_flux.py:516-617), and stack the deltas
+(expected_flux.py:190-236). The bin sums run on the GPU; the normalisations,
+interpolators and the twenty (eta, var_lss, fudge) fits (a box-constrained
+linear least-squares problem per wavelength bin, solved exactly) run on the
+host. ``deltas()`` returns the final deltas and weights
+(populate_los_ids + extract_deltas, dr16_expected_flux.py:706-740,
+expected_flux.py:328-349).
+"""
+
+import ctypes
+
+import numpy as np
+import torch
+from scipy.interpolate import PPoly, interp1d, make_interp_spline
+from scipy.optimize import lsq_linear
+
+from . import _native
+from ._native import check
+
+VAR_PIPE_MIN = np.log10(1e-5)
+VAR_PIPE_MAX = np.log10(2.)
+NUM_VAR_BINS = 100
+FUDGE_REF = 1e-7
+ETA_DEFAULT, VAR_LSS_DEFAULT, FUDGE_DEFAULT = 1.0, 0.1, 0.0
+FIT_FP64 = 0
+FIT_MIXED = 1
+STATUS_REASONS = {0: None, 1: "minuit didn't converge", 2: "negative continuum",
+                  3: "zero continuum"}
+
+_P = ctypes.POINTER
+
+
+class SpectraC(ctypes.Structure):
+    _fields_ = [("num", ctypes.c_int64), ("num_pixels", ctypes.c_int64)] + [
+        (n, ctypes.c_void_p) for n in ("pix_offset", "log_lambda", "flux", "ivar",
+                                       "transmission_correction", "z_qso")]
+
+
+class ContModelC(ctypes.Structure):
+    _fields_ = [
+        ("num_mean_cont", ctypes.c_int32), ("mean_cont_x", ctypes.c_void_p),
+        ("mean_cont_y", ctypes.c_void_p), ("num_var_intervals", ctypes.c_int32),
+        ("var_breaks", ctypes.c_void_p), ("eta_coef", ctypes.c_void_p),
+        ("var_lss_coef", ctypes.c_void_p), ("fudge_coef", ctypes.c_void_p),
+        ("num_stack", ctypes.c_int32), ("stack_x", ctypes.c_void_p), ("stack_y", ctypes.c_void_p),
+        ("log_lambda_rest_min", ctypes.c_double), ("log_lambda_rest_max", ctypes.c_double),
+        ("var_lss_mod", ctypes.c_double), ("order", ctypes.c_int32),
+        ("use_constant_weight", ctypes.c_int32)]
+
+
+class ContFitC(ctypes.Structure):
+    _fields_ = [(n, ctypes.c_void_p) for n in ("zero_point", "slope", "chi2", "ndata", "status",
+                                               "iterations", "continuum")]
+
+
+class ContStacksC(ctypes.Structure):
+    _fields_ = [
+        ("rest_bins", ctypes.c_int32), ("rest_grid0", ctypes.c_double),
+        ("rest_step", ctypes.c_double), ("mean_cont_num", ctypes.c_void_p),
+        ("mean_cont_weight", ctypes.c_void_p), ("var_lambda_bins", ctypes.c_int32),
+        ("var_grid0", ctypes.c_double), ("var_step", ctypes.c_double),
+        ("var_mean", ctypes.c_void_p), ("var_delta2", ctypes.c_void_p),
+        ("var_delta4", ctypes.c_void_p), ("var_npix", ctypes.c_void_p),
+        ("var_nqso", ctypes.c_void_p), ("obs_bins", ctypes.c_int32),
+        ("obs_grid0", ctypes.c_double), ("obs_step", ctypes.c_double),
+        ("stack_num", ctypes.c_void_p), ("stack_weight", ctypes.c_void_p)]
+
+
+def _bind():
+    lib = _native.lib()
+    if getattr(lib, "_cont_bound", False):
+        return lib
+    lib.pg_cont_fit_batch.argtypes = [ctypes.c_void_p, _P(SpectraC), _P(ContModelC),
+                                      ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,
+                                      ctypes.c_int32, _P(ContFitC), ctypes.c_void_p]
+    lib.pg_cont_stacks_accumulate.argtypes = [ctypes.c_void_p, _P(SpectraC), _P(ContModelC),
+                                              _P(ContFitC), _P(ContStacksC), ctypes.c_void_p]
+    lib.pg_cont_deltas.argtypes = [ctypes.c_void_p, _P(SpectraC), _P(ContModelC), _P(ContFitC),
+                                   ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    for name in ("pg_cont_fit_batch", "pg_cont_stacks_accumulate", "pg_cont_deltas"):
+        getattr(lib, name).restype = ctypes.c_int
+    lib._cont_bound = True
+    return lib
+
+
+def cubic_ppoly(x, y):
+    """Breakpoints and (4, m) coefficients of scipy's interp1d(kind='cubic')
+    (a not-a-knot cubic B-spline) in piecewise-polynomial form."""
+    spl = make_interp_spline(np.asarray(x, float), np.asarray(y, float), k=3)
+    pp = PPoly.from_spline(spl)
+    keep = np.diff(pp.x) > 0
+    breaks = np.concatenate([pp.x[:-1][keep], [pp.x[1:][keep][-1]]])
+    return breaks, np.ascontiguousarray(pp.c[:, keep])
+
+
+def find_bins_log(values, grid):
+    """find_bins_log (py/picca/delta_extraction/utils.py:163-186)."""
+    step = grid[1] - grid[0]
+    return ((values - grid[0]) / step + 0.5).astype(np.int64)
+
+
+class DeviceSpectra:
+    """Raw forests resident on the device."""
+
+    def __init__(self, raw, device):
+        arrays = {"pix_offset": np.asarray(raw.pix_offset, np.int64),
+                  "log_lambda": raw.log_lambda, "flux": raw.flux, "ivar": raw.ivar,
+                  "transmission_correction": raw.transmission_correction,
+                  "z_qso": raw.z_qso}
+        self.tensors = {k: torch.as_tensor(np.ascontiguousarray(v)).to(device)
+                        for k, v in arrays.items()}
+        self.num = int(raw.num)
+        self.num_pixels = int(raw.pix_offset[-1])
+        self.c = SpectraC(self.num, self.num_pixels,
+                          *[self.tensors[k].data_ptr() for k in
+                            ("pix_offset", "log_lambda", "flux", "ivar",
+                             "transmission_correction", "z_qso")])
+        self.h2d_bytes = sum(int(t.numel() * t.element_size()) for t in self.tensors.values())
+
+
+class Dr16Gpu:
+    """The Dr16 iteration on the GPU for a set of raw forests."""
+
+    def __init__(self, grid, num_iterations=5, order=1, limit_eta=(0.5, 1.5),
+                 limit_var_lss=(0., 0.3), min_num_qso_in_fit=100, num_bins_variance=20,
+                 var_lss_mod=1.0, use_constant_weight=False, use_ivar_as_weight=False,
+                 force_stack_delta_to_zero=True, fit_mode=FIT_FP64, max_iter=100, tol=1e-10,
+                 device=None):
+        from .pairs import require_cuda
+        require_cuda()
+        self.device = torch.device(device or "cuda")
+        self.grid = grid
+        self.num_iterations = num_iterations
+        self.order = order
+        self.limit_eta = limit_eta
+        self.limit_var_lss = limit_var_lss
+        self.min_num_qso_in_fit = min_num_qso_in_fit
+        self.num_bins_variance = num_bins_variance
+        self.var_lss_mod = var_lss_mod
+        self.use_constant_weight = use_constant_weight
+        self.use_ivar_as_weight = use_ivar_as_weight
+        self.force_stack_delta_to_zero = force_stack_delta_to_zero
+        self.fit_mode = fit_mode
+        self.max_iter = max_iter
+        self.tol = tol
+        with torch.cuda.device(self.device):
+            self.plan = _native.Plan()
+        _bind()
+        rest = grid.log_lambda_rest_frame_grid
+        self.log_lambda_var_func_grid = np.linspace(grid.log_lambda_grid[0],
+                                                    grid.log_lambda_grid[-1], num_bins_variance)
+        # initial interpolators (dr16_expected_flux.py:198-286, expected_flux.py:95-113)
+        self.mean_cont_x = rest.copy()
+        self.mean_cont_y = np.ones_like(rest)
+        self.mean_cont_weight = np.zeros_like(rest)
+        nvb = num_bins_variance
+        if use_ivar_as_weight:
+            eta, vlss = np.ones(nvb), np.zeros(nvb)
+        elif use_constant_weight:
+            eta, vlss = np.zeros(nvb), np.ones(nvb)
+        else:
+            eta, vlss = np.full(nvb, ETA_DEFAULT), np.full(nvb, VAR_LSS_DEFAULT)
+        self.fit_functions = not (use_ivar_as_weight or use_constant_weight)
+        self.var_x = self.log_lambda_var_func_grid.copy()
+        self.eta = eta
+        self.var_lss = vlss
+        self.fudge = np.full(nvb, FUDGE_DEFAULT)
+        self.num_pixels_var = np.zeros(nvb)
+        self.valid_fit = np.ones(nvb, bool) if not self.fit_functions else np.zeros(nvb, bool)
+        self.stack_x = None
+        self.stack_y = None
+        self.stack_weight = None
+        self.history = []
+
+    # -- model -------------------------------------------------------------
+    def _model(self, with_stack=False):
+        dev = self.device
+        keep = {}
+        keep["mcx"] = torch.as_tensor(self.mean_cont_x, dtype=torch.float64).to(dev)
+        keep["mcy"] = torch.as_tensor(self.mean_cont_y, dtype=torch.float64).to(dev)
+        coefs = []
+        for vals in (self.eta, self.var_lss, self.fudge):
+            breaks, coef = cubic_ppoly(self.var_x, vals)
+            coefs.append(coef)
+        keep["brk"] = torch.as_tensor(breaks).to(dev)
+        keep["eta"] = torch.as_tensor(coefs[0]).to(dev)
+        keep["vlss"] = torch.as_tensor(coefs[1]).to(dev)
+        keep["fudge"] = torch.as_tensor(coefs[2]).to(dev)
+        rest = self.grid.log_lambda_rest_frame_grid
+        model = ContModelC()
+        model.num_mean_cont = len(self.mean_cont_x)
+        model.mean_cont_x = keep["mcx"].data_ptr()
+        model.mean_cont_y = keep["mcy"].data_ptr()
+        model.num_var_intervals = coefs[0].shape[1]
+        model.var_breaks = keep["brk"].data_ptr()
+        model.eta_coef = keep["eta"].data_ptr()
+        model.var_lss_coef = keep["vlss"].data_ptr()
+        model.fudge_coef = keep["fudge"].data_ptr()
+        if with_stack and self.stack_x is not None:
+            keep["sx"] = torch.as_tensor(self.stack_x).to(dev)
+            keep["sy"] = torch.as_tensor(self.stack_y).to(dev)
+            model.num_stack = len(self.stack_x)
+            model.stack_x = keep["sx"].data_ptr()
+            model.stack_y = keep["sy"].data_ptr()
+        model.log_lambda_rest_min = float(rest[0])
+        model.log_lambda_rest_max = float(rest[-1])
+        model.var_lss_mod = float(self.var_lss_mod)
+        model.order = int(self.order)
+        model.use_constant_weight = int(bool(self.use_constant_weight))
+        return model, keep
+
+    def _stream(self):
+        return ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
+
+    # -- steps -------------------------------------------------------------
+    def fit(self, spectra, start=None, mode=None, max_iter=None):
+        """Continuum fit of every forest; returns a dict of device tensors."""
+        lib = _bind()
+        dev = self.device
+        n = spectra.num
+        out = {"zero_point": torch.empty(n, dtype=torch.float64, device=dev),
+               "slope": torch.empty(n, dtype=torch.float64, device=dev),
+               "chi2": torch.empty(n, dtype=torch.float64, device=dev),
+               "ndata": torch.empty(n, dtype=torch.int32, device=dev),
+               "status": torch.empty(n, dtype=torch.int32, device=dev),
+               "iterations": torch.empty(n, dtype=torch.int32, device=dev),
+               "continuum": torch.empty(max(spectra.num_pixels, 1), dtype=torch.float64,
+                                        device=dev)}
+        fit_c = ContFitC(*[out[k].data_ptr() for k in ("zero_point", "slope", "chi2", "ndata",
+                                                        "status", "iterations", "continuum")])
+        model, keep = self._model()
+        start_ptr = None
+        if start is not None:
+            start = torch.as_tensor(start, dtype=torch.float64, device=dev).contiguous()
+            start_ptr = start.data_ptr()
+        with torch.cuda.device(dev):
+            check(lib.pg_cont_fit_batch(
+                self.plan.handle, ctypes.byref(spectra.c), ctypes.byref(model), start_ptr,
+                int(max_iter or self.max_iter), float(self.tol),
+                int(self.fit_mode if mode is None else mode), ctypes.byref(fit_c), self._stream()),
+                "continuum fit")
+        out["_keep"] = (keep, start, fit_c)
+        return out
+
+    def _stacks(self, spectra, fit, mean_cont=True, var_stats=True, delta_stack=True):
+        lib = _bind()
+        dev = self.device
+        grid = self.grid
+        rest, obs = grid.log_lambda_rest_frame_grid, grid.log_lambda_grid
+        nvar = self.num_bins_variance * NUM_VAR_BINS
+        bufs = {k: torch.zeros(n, dtype=torch.float64, device=dev) for k, n in (
+            ("mc_num", len(rest)), ("mc_w", len(rest)), ("v_mean", nvar), ("v_d2", nvar),
+            ("v_d4", nvar), ("v_np", nvar), ("v_nq", nvar), ("s_num", len(obs)),
+            ("s_w", len(obs)))}
+        st = ContStacksC()
+        st.rest_bins = len(rest)
+        st.rest_grid0 = float(rest[0])
+        st.rest_step = float(rest[1] - rest[0])
+        if mean_cont:
+            st.mean_cont_num = bufs["mc_num"].data_ptr()
+            st.mean_cont_weight = bufs["mc_w"].data_ptr()
+        st.var_lambda_bins = self.num_bins_variance
+        st.var_grid0 = float(self.log_lambda_var_func_grid[0])
+        st.var_step = float(self.log_lambda_var_func_grid[1] - self.log_lambda_var_func_grid[0])
+        if var_stats:
+            st.var_mean = bufs["v_mean"].data_ptr()
+            st.var_delta2 = bufs["v_d2"].data_ptr()
+            st.var_delta4 = bufs["v_d4"].data_ptr()
+            st.var_npix = bufs["v_np"].data_ptr()
+            st.var_nqso = bufs["v_nq"].data_ptr()
+        st.obs_bins = len(obs)
+        st.obs_grid0 = float(obs[0])
+        st.obs_step = float(obs[1] - obs[0])
+        if delta_stack:
+            st.stack_num = bufs["s_num"].data_ptr()
+            st.stack_weight = bufs["s_w"].data_ptr()
+        model, keep = self._model()
+        fit_c = fit["_keep"][2]
+        with torch.cuda.device(dev):
+            check(lib.pg_cont_stacks_accumulate(self.plan.handle, ctypes.byref(spectra.c),
+                                                ctypes.byref(model), ctypes.byref(fit_c),
+                                                ctypes.byref(st), self._stream()), "stacks")
+        stats = self.plan.stats()
+        if stats.status != 0:
+            raise _native.NativeError(f"stack accumulation: device status {stats.status}")
+        del keep
+        return {k: v.cpu().numpy() for k, v in bufs.items()}
+
+    def update_mean_cont(self, sums):
+        """_compute_mean_cont normalisation (expected_flux.py:291-308)."""
+        mean_cont = sums["mc_num"].copy()
+        weight = sums["mc_w"]
+        w = weight > 0
+        mean_cont[w] /= weight[w]
+        mean_cont /= mean_cont[w].mean()
+        rest = self.grid.log_lambda_rest_frame_grid[w]
+        old = interp1d(self.mean_cont_x, self.mean_cont_y, fill_value="extrapolate")
+        self.mean_cont_y = old(rest) * mean_cont[w]
+        self.mean_cont_x = rest
+        self.mean_cont_weight = weight[w]
+
+    def update_var_functions(self, sums):
+        """Variance statistics and the (eta, var_lss, fudge) fits
+        (least_squares_var_stats.py:183-198, dr16_expected_flux.py:531-617)."""
+        nvb = self.num_bins_variance
+        var_delta = sums["v_d2"].copy()
+        mean_delta = sums["v_mean"].copy()
+        var2_delta = sums["v_d4"].copy()
+        num_pixels = sums["v_np"]
+        num_qso = sums["v_nq"]
+        w = num_pixels > 0
+        var_delta[w] /= num_pixels[w]
+        mean_delta[w] /= num_pixels[w]
+        var_delta -= mean_delta**2
+        var2_delta[w] /= num_pixels[w]
+        var2_delta -= var_delta**2
+        var2_delta[w] /= num_pixels[w]
+        var_pipe_values = 10**(VAR_PIPE_MIN + ((np.arange(NUM_VAR_BINS) + .5) *
+                                               (VAR_PIPE_MAX - VAR_PIPE_MIN) / NUM_VAR_BINS))
+        eta = interp1d(self.var_x, self.eta, kind="cubic", fill_value="extrapolate")(
+            self.log_lambda_var_func_grid)
+        vlss = interp1d(self.var_x, self.var_lss, kind="cubic", fill_value="extrapolate")(
+            self.log_lambda_var_func_grid)
+        fudge = interp1d(self.var_x, self.fudge, kind="cubic", fill_value="extrapolate")(
+            self.log_lambda_var_func_grid)
+        npix_bin = np.zeros(nvb)
+        valid = np.zeros(nvb, bool)
+        for index in range(nvb):
+            sl = slice(index * NUM_VAR_BINS, (index + 1) * NUM_VAR_BINS)
+            npix_bin[index] = num_pixels[sl].sum()
+            sol = fit_var_bin(var_delta[sl], var2_delta[sl], num_qso[sl], var_pipe_values,
+                              self.min_num_qso_in_fit, self.limit_eta, self.limit_var_lss,
+                              (eta[index], vlss[index], fudge[index] / FUDGE_REF))
+            if sol is None:
+                eta[index], vlss[index], fudge[index] = ETA_DEFAULT, VAR_LSS_DEFAULT, FUDGE_DEFAULT
+            else:
+                eta[index], vlss[index], fudge[index] = sol
+                valid[index] = True
+        w = npix_bin > 0
+        self.var_x = self.log_lambda_var_func_grid[w]
+        self.eta, self.var_lss, self.fudge = eta[w], vlss[w], fudge[w]
+        self.num_pixels_var = npix_bin[w]
+        self.valid_fit = valid[w]
+
+    def update_stack(self, sums):
+        """compute_delta_stack normalisation and interpolator (expected_flux.py:226-236)."""
+        stack = sums["s_num"].copy()
+        weight = sums["s_w"]
+        w = weight > 0
+        stack[w] /= weight[w]
+        self.stack_x = self.grid.log_lambda_grid[w]
+        self.stack_y = stack[w]
+        self.stack_weight = weight[w]
+
+    def run(self, spectra, start=None, mode=None):
+        """The Dr16 outer loop. ``start`` optionally warm-starts every
+        iteration's fit (e.g. with learned (a, b)). Returns the last fit."""
+        fit = None
+        for iteration in range(self.num_iterations):
+            fit = self.fit(spectra, start=start, mode=mode)
+            last = iteration == self.num_iterations - 1
+            sums = self._stacks(spectra, fit, mean_cont=not last,
+                                var_stats=(not last) and self.fit_functions, delta_stack=True)
+            if not last:
+                self.update_mean_cont(sums)
+                if self.fit_functions:
+                    self.update_var_functions(sums)
+            self.update_stack(sums)
+            self.history.append({"iteration": iteration,
+                                 "iterations_mean": float(fit["iterations"].float().mean()),
+                                 "accepted": int((fit["status"] == 0).sum())})
+        return fit
+
+    def deltas(self, spectra, fit):
+        """Final deltas and weights per pixel (device tensors)."""
+        lib = _bind()
+        dev = self.device
+        delta = torch.empty(max(spectra.num_pixels, 1), dtype=torch.float64, device=dev)
+        weights = torch.empty_like(delta)
+        model, keep = self._model(with_stack=self.force_stack_delta_to_zero)
+        fit_c = fit["_keep"][2]
+        with torch.cuda.device(dev):
+            check(lib.pg_cont_deltas(self.plan.handle, ctypes.byref(spectra.c),
+                                     ctypes.byref(model), ctypes.byref(fit_c), delta.data_ptr(),
+                                     weights.data_ptr(), self._stream()), "deltas")
+        torch.cuda.synchronize(dev)
+        del keep
+        return delta, weights
+
+
+def fit_var_bin(var_delta, var2_delta, num_qso, var_pipe_values, min_num_qso, limit_eta,
+                limit_var_lss, start):
+    """(eta, var_lss, fudge) of one wavelength bin. The chi2 of
+    least_squares_var_stats.py:104-132 is linear in (eta, var_lss,
+    fudge / FUDGE_REF) with box limits (dr16_expected_flux.py:549-563), so
+    its minimum is found exactly by bounded least squares."""
+    sel = (num_qso > min_num_qso) & (var2_delta > 0)
+    if sel.sum() == 0:
+        # flat chi2: the minimiser stays at its starting point
+        return float(start[0]), float(start[1]), float(start[2]) * FUDGE_REF
+    wgt = 1.0 / np.sqrt(var2_delta[sel])
+    mat = np.stack([var_pipe_values[sel], np.ones(sel.sum()),
+                    FUDGE_REF / var_pipe_values[sel]], axis=1) * wgt[:, None]
+    res = lsq_linear(mat, var_delta[sel] * wgt,
+                     bounds=([limit_eta[0], limit_var_lss[0], 0.0],
+                             [limit_eta[1], limit_var_lss[1], np.inf]),
+                     method="bvls", tol=1e-14)
+    if not res.success:
+        return None
+    return float(res.x[0]), float(res.x[1]), float(res.x[2]) * FUDGE_REF
+
+
+def fit_results_to_host(fit):
+    return {k: v.cpu().numpy() for k, v in fit.items() if not k.startswith("_")}

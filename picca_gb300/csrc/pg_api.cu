@@ -246,4 +246,101 @@ int pg_xcf_xi(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *
                               *out, scratch_of(plan), plan->num_sms, st);
 }
 
+static int validate_spectra(const pg_spectra *sp) {
+    if (!sp || sp->num < 0 || sp->num_pixels < 0) return PG_ERR_INVALID_ARGUMENT;
+    if (sp->num == 0) return PG_OK;
+    if (!sp->pix_offset || !sp->log_lambda || !sp->flux || !sp->ivar ||
+        !sp->transmission_correction || !sp->z_qso)
+        return PG_ERR_INVALID_ARGUMENT;
+    return PG_OK;
+}
+
+static int validate_model(const pg_cont_model *m) {
+    if (!m || m->num_mean_cont < 2 || !m->mean_cont_x || !m->mean_cont_y)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (!m->use_constant_weight &&
+        (m->num_var_intervals < 1 || !m->var_breaks || !m->eta_coef || !m->var_lss_coef ||
+         !m->fudge_coef))
+        return PG_ERR_INVALID_ARGUMENT;
+    if (m->stack_x && (m->num_stack < 1 || !m->stack_y)) return PG_ERR_INVALID_ARGUMENT;
+    if (!(m->log_lambda_rest_max > m->log_lambda_rest_min)) return PG_ERR_INVALID_ARGUMENT;
+    return PG_OK;
+}
+
+static int validate_fit(const pg_cont_fit *f, bool need_continuum) {
+    if (!f || !f->zero_point || !f->slope || !f->chi2 || !f->ndata || !f->status ||
+        !f->iterations)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (need_continuum && !f->continuum) return PG_ERR_INVALID_ARGUMENT;
+    return PG_OK;
+}
+
+int pg_cont_fit_batch(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
+                const double *start, int32_t max_iter, double tol, int32_t mode,
+                const pg_cont_fit *out, void *stream) {
+    if (!plan) return PG_ERR_INVALID_ARGUMENT;
+    int rc;
+    if ((rc = validate_spectra(spectra)) || (rc = validate_model(model)) ||
+        (rc = validate_fit(out, false)))
+        return rc;
+    if (max_iter < 1 || !(tol > 0) || (mode != PG_FIT_FP64 && mode != PG_FIT_MIXED))
+        return PG_ERR_INVALID_ARGUMENT;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    if ((rc = reset_scratch(plan, st))) return rc;
+    return launch_cont_fit(*spectra, *model, start, max_iter, tol, mode, *out, scratch_of(plan),
+                           plan->num_sms, st);
+}
+
+int pg_cont_stacks_accumulate(pg_plan *plan, const pg_spectra *spectra,
+                              const pg_cont_model *model, const pg_cont_fit *fit,
+                              const pg_cont_stacks *stacks, void *stream) {
+    if (!plan || !stacks) return PG_ERR_INVALID_ARGUMENT;
+    int rc;
+    if ((rc = validate_spectra(spectra)) || (rc = validate_model(model)) ||
+        (rc = validate_fit(fit, true)))
+        return rc;
+    if (stacks->mean_cont_num && (!stacks->mean_cont_weight || stacks->rest_bins < 1 ||
+                                  !(stacks->rest_step > 0)))
+        return PG_ERR_INVALID_ARGUMENT;
+    if (stacks->var_mean && (!stacks->var_delta2 || !stacks->var_delta4 || !stacks->var_npix ||
+                             !stacks->var_nqso || stacks->var_lambda_bins < 1 ||
+                             !(stacks->var_step > 0)))
+        return PG_ERR_INVALID_ARGUMENT;
+    if (stacks->stack_num && (!stacks->stack_weight || stacks->obs_bins < 1 ||
+                              !(stacks->obs_step > 0)))
+        return PG_ERR_INVALID_ARGUMENT;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    if ((rc = reset_scratch(plan, st))) return rc;
+    return launch_cont_stacks(*spectra, *model, *fit, *stacks, scratch_of(plan), plan->num_sms,
+                              st);
+}
+
+int pg_cont_deltas(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
+                   const pg_cont_fit *fit, double *delta, double *weights, void *stream) {
+    if (!plan || !delta || !weights) return PG_ERR_INVALID_ARGUMENT;
+    int rc;
+    if ((rc = validate_spectra(spectra)) || (rc = validate_model(model)) ||
+        (rc = validate_fit(fit, true)))
+        return rc;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    return launch_cont_deltas(*spectra, *model, *fit, delta, weights, plan->num_sms, st);
+}
+
+int pg_mlp_features(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
+                    uint16_t *features, int32_t feat_stride, double *a0, void *stream) {
+    if (!plan || !features || !a0 || feat_stride < 66) return PG_ERR_INVALID_ARGUMENT;
+    int rc;
+    if ((rc = validate_spectra(spectra)) || (rc = validate_model(model))) return rc;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    return launch_mlp_features(*spectra, *model, features, feat_stride, a0, plan->num_sms, st);
+}
+
 }  // extern "C"

@@ -1,0 +1,549 @@
+// Batched Dr16 continuum fit (delta_extraction/expected_fluxes/utils.py:12-136
+// and least_squares/least_squares_cont_model.py:65-197, paths under
+// py/picca), the per-iteration histograms of Dr16ExpectedFlux and the final
+// delta extraction.
+//
+// One warp fits one forest: every lane holds up to K pixels in registers as
+// the coefficients of
+//     C = (a + b x) mc,      x = (L - Lmin)/(Lmax - Lmin),
+//     D = eta/ivar + var_lss C^2 + fudge ivar C^4,
+//     chi2 = sum (f - C)^2 / D + sum log D
+// (the reference's chi2 - sum log w with w = 1/D), evaluates chi2, its
+// gradient and Hessian in (a, b) in one pass, reduces them in FP64 with warp
+// shuffles and takes a damped Newton step solved in FP64 (backtracking
+// Armijo line search). The per-pixel terms are FP64 (PG_FIT_FP64) or FP32
+// (PG_FIT_MIXED); the reported chi2 is always re-evaluated in FP64.
+// The reference minimises the same function with iminuit's MIGRAD.
+#include <cuda_bf16.h>
+
+#include "pg_internal.cuh"
+
+namespace pg {
+namespace {
+
+constexpr int kContBlock = 256;
+constexpr int kContK = 7;  // pixels per lane held in registers (forests <= 224 pixels)
+constexpr int kVarBins = 100;
+constexpr double kVarPipeMin = -5.0;                  // log10(1e-5)
+constexpr double kVarPipeMax = 0.30102999566398120;   // log10(2)
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+// scipy interp1d(kind="linear", fill_value="extrapolate"): searchsorted
+// (left) clipped to [1, n-1], then slope * (v - x_lo) + y_lo.
+__device__ double interp_linear(const double *__restrict__ x, const double *__restrict__ y, int n,
+                                double v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (x[mid] < v) lo = mid + 1;
+        else hi = mid;
+    }
+    int idx = lo < 1 ? 1 : (lo > n - 1 ? n - 1 : lo);
+    const double xl = x[idx - 1], xh = x[idx], yl = y[idx - 1], yh = y[idx];
+    const double slope = (yh - yl) / (xh - xl);
+    return __dadd_rn(__dmul_rn(slope, __dsub_rn(v, xl)), yl);
+}
+
+// Piecewise cubic (highest power first), extrapolated with the end pieces.
+__device__ double eval_ppoly(const double *__restrict__ brk, const double *__restrict__ coef, int m,
+                             double v) {
+    int lo = 0, hi = m + 1;  // searchsorted right over the m + 1 breakpoints
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (brk[mid] <= v) lo = mid + 1;
+        else hi = mid;
+    }
+    int i = lo - 1;
+    i = i < 0 ? 0 : (i > m - 1 ? m - 1 : i);
+    const double dx = v - brk[i];
+    return ((coef[i] * dx + coef[m + i]) * dx + coef[2 * m + i]) * dx + coef[3 * m + i];
+}
+
+// scipy interp1d(kind="nearest"): index of the nearest stack point.
+__device__ double interp_nearest(const double *__restrict__ x, const double *__restrict__ y, int n,
+                                 double v) {
+    // midpoints x_bds[i] = (x[i] + x[i+1]) / 2; idx = searchsorted(x_bds, v, "left")
+    int lo = 0, hi = n - 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const double bd = (x[mid] + x[mid + 1]) / 2.0;
+        if (bd < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return y[lo];
+}
+
+struct ModelEval {
+    double mc, eta, var_lss, fudge;
+};
+
+__device__ __forceinline__ ModelEval eval_model(const pg_cont_model &m, double ll, double zp1,
+                                                double tc) {
+    ModelEval e;
+    e.mc = interp_linear(m.mean_cont_x, m.mean_cont_y, m.num_mean_cont, ll - zp1) * tc;
+    if (m.use_constant_weight) {
+        e.eta = 0.;
+        e.var_lss = 1.;
+        e.fudge = 0.;
+    } else {
+        e.eta = eval_ppoly(m.var_breaks, m.eta_coef, m.num_var_intervals, ll);
+        e.var_lss = eval_ppoly(m.var_breaks, m.var_lss_coef, m.num_var_intervals, ll);
+        e.fudge = eval_ppoly(m.var_breaks, m.fudge_coef, m.num_var_intervals, ll);
+    }
+    return e;
+}
+
+template <typename T>
+struct PixelTerms {
+    T ja[kContK], jb[kContK], f[kContK], q[kContK], vl[kContK], fi[kContK];
+    unsigned valid;
+};
+
+// chi2 / 2 and its derivatives of one lane's pixels (accumulated in T,
+// returned in FP64); constant weights use q = 1, vl = fi = 0 with no log.
+// U is the arithmetic type of the per-pixel terms (T or FP64).
+template <typename U, typename T>
+__device__ __forceinline__ void lane_terms(const PixelTerms<T> &px, double a, double b,
+                                           bool const_w, double s[6]) {
+    U val = 0, ga = 0, gb = 0, haa = 0, hab = 0, hbb = 0;
+    const U ua = (U)a, ub = (U)b;
+#pragma unroll
+    for (int k = 0; k < kContK; ++k) {
+        if (!((px.valid >> k) & 1u)) continue;
+        const U ja = (U)px.ja[k], jb = (U)px.jb[k];
+        const U q = (U)px.q[k], vl = (U)px.vl[k], fi = (U)px.fi[k];
+        const U c = ua * ja + ub * jb;
+        const U c2 = c * c;
+        const U d = q + vl * c2 + fi * c2 * c2;
+        const U dd = (U)2 * vl * c + (U)4 * fi * c2 * c;
+        const U d2d = (U)2 * vl + (U)12 * fi * c2;
+        const U r = (U)px.f[k] - c;
+        const U id = (U)1 / d;
+        const U rid = r * id;
+        const U ddid = dd * id;
+        val += r * rid + (const_w ? (U)0 : log(d));
+        const U g = (U)-2 * rid - rid * rid * dd + ddid;
+        const U h = (U)2 * id + (U)4 * rid * ddid + (U)2 * rid * rid * dd * ddid - rid * rid * d2d
+                    + d2d * id - ddid * ddid;
+        ga += g * ja;
+        gb += g * jb;
+        haa += h * ja * ja;
+        hab += h * ja * jb;
+        hbb += h * jb * jb;
+    }
+    s[0] = (double)val; s[1] = (double)ga; s[2] = (double)gb;
+    s[3] = (double)haa; s[4] = (double)hab; s[5] = (double)hbb;
+}
+
+template <typename U, typename T>
+__device__ __forceinline__ void eval_all(const PixelTerms<T> &px, double a, double b, bool const_w,
+                                         double s[6]) {
+    lane_terms<U>(px, a, b, const_w, s);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s[k] = warp_sum(s[k]);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(kContBlock) cont_fit_kernel(
+    const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
+    const double *__restrict__ start, int max_iter, double tol,
+    const __grid_constant__ pg_cont_fit out, Scratch *scratch) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const bool const_w = m.use_constant_weight != 0;
+    for (int64_t f = warp_global; f < sp.num; f += nwarps) {
+        const int64_t off = sp.pix_offset[f];
+        const int64_t n64 = sp.pix_offset[f + 1] - off;
+        if (n64 > 32 * kContK || n64 <= 0) {
+            if (lane == 0) {
+                if (n64 > 32 * kContK) report_error(scratch, PG_ERR_UNSUPPORTED, (int32_t)f);
+                out.zero_point[f] = NAN;
+                out.slope[f] = NAN;
+                out.chi2[f] = NAN;
+                out.ndata[f] = 0;
+                out.status[f] = 1;
+                out.iterations[f] = 0;
+            }
+            continue;
+        }
+        const int n = (int)n64;
+        const double zp1 = log10(1 + sp.z_qso[f]);
+        const double ll_min = m.log_lambda_rest_min + zp1;
+        const double ll_max = m.log_lambda_rest_max + zp1;
+        PixelTerms<T> px;
+        px.valid = 0;
+        double sfi = 0., si = 0.;
+#pragma unroll
+        for (int k = 0; k < kContK; ++k) {
+            const int p = lane + 32 * k;
+            px.ja[k] = px.jb[k] = px.f[k] = px.q[k] = px.vl[k] = px.fi[k] = (T)0;
+            if (p < n) {
+                const double ll = sp.log_lambda[off + p], fl = sp.flux[off + p];
+                const double iv = sp.ivar[off + p];
+                sfi += fl * iv;
+                si += iv;
+                if (iv > 0) {
+                    const ModelEval e = eval_model(m, ll, zp1, sp.transmission_correction[off + p]);
+                    const double x = (ll - ll_min) / (ll_max - ll_min);
+                    px.ja[k] = (T)e.mc;
+                    px.jb[k] = (T)(x * e.mc);
+                    px.f[k] = (T)fl;
+                    px.q[k] = (T)(const_w ? 1. : e.eta / iv);
+                    px.vl[k] = (T)(const_w ? 0. : e.var_lss);
+                    px.fi[k] = (T)(const_w ? 0. : e.fudge * iv);
+                    px.valid |= 1u << k;
+                }
+            }
+        }
+        sfi = warp_sum(sfi);
+        si = warp_sum(si);
+        const double a0 = sfi / si;  // utils.py:92
+        // ndata: pixels with a positive weight at the reference's starting
+        // point (a0, 0) (cont_model.py:88-92)
+        int nd = 0;
+#pragma unroll
+        for (int k = 0; k < kContK; ++k) {
+            if ((px.valid >> k) & 1u) {
+                const double c = a0 * (double)px.ja[k];
+                const double d = (double)px.q[k] + (double)px.vl[k] * c * c +
+                                 (double)px.fi[k] * c * c * c * c;
+                nd += (d > 0.) ? 1 : 0;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) nd += __shfl_xor_sync(0xffffffffu, nd, o);
+        double a = a0, b = 0.;
+        if (start) {
+            a = start[2 * f];
+            b = m.order == 0 ? 0. : start[2 * f + 1];
+        }
+
+        double s[6];
+        eval_all<T>(px, a, b, const_w, s);
+        int it = 0;
+        bool converged = false;
+        for (; it < max_iter; ++it) {
+            double da, db;
+            if (m.order == 0) {
+                da = s[3] > 0 ? -s[1] / s[3] : -s[1];
+                db = 0.;
+            } else {
+                const double det = s[3] * s[5] - s[4] * s[4];
+                if (det > 0 && s[3] > 0) {
+                    da = -(s[5] * s[1] - s[4] * s[2]) / det;
+                    db = -(s[3] * s[2] - s[4] * s[1]) / det;
+                } else {
+                    const double scale = fmax(fabs(s[3]), fabs(s[5]));
+                    da = -s[1] / (scale > 0 ? scale : 1.);
+                    db = -s[2] / (scale > 0 ? scale : 1.);
+                }
+                if (da * s[1] + db * s[2] >= 0) {  // not a descent direction
+                    const double scale = fmax(fabs(s[3]), fabs(s[5]));
+                    da = -s[1] / (scale > 0 ? scale : 1.);
+                    db = -s[2] / (scale > 0 ? scale : 1.);
+                }
+            }
+            const double slope_dir = da * s[1] + db * s[2];
+            double t = 1.;
+            double trial[6];
+            bool accepted = false;
+            for (int ls = 0; ls < 40; ++ls) {
+                eval_all<T>(px, a + t * da, b + t * db, const_w, trial);
+                if (isfinite(trial[0]) && trial[0] <= s[0] + 1e-4 * t * slope_dir) {
+                    accepted = true;
+                    break;
+                }
+                t *= 0.5;
+            }
+            if (!accepted) {
+                converged = fabs(s[1]) + fabs(s[2]) < 1e-6 * fmax(1., fabs(s[0]));
+                break;
+            }
+            a += t * da;
+            b += t * db;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) s[k] = trial[k];
+            if (fabs(t * da) < tol * fmax(1., fmax(fabs(a), fabs(b))) &&
+                fabs(t * db) < tol * fmax(1., fmax(fabs(a), fabs(b)))) {
+                converged = true;
+                ++it;
+                break;
+            }
+        }
+        // chi2 at the solution in FP64, and the continuum with the
+        // reference's operation order (cont_model.py:138-144)
+        double fin[6];
+        eval_all<double>(px, a, b, const_w, fin);
+        bool negative = false, all_zero = true;
+        for (int p = lane; p < n; p += 32) {
+            const double ll = sp.log_lambda[off + p];
+            const double mc = interp_linear(m.mean_cont_x, m.mean_cont_y, m.num_mean_cont,
+                                            ll - zp1) * sp.transmission_correction[off + p];
+            const double line = b * (ll - ll_min) / (ll_max - ll_min) + a;
+            const double c = line * mc;
+            if (out.continuum) out.continuum[off + p] = c;
+            negative |= c < 0;
+            all_zero &= c == 0;
+        }
+        negative = __any_sync(0xffffffffu, negative);
+        all_zero = __all_sync(0xffffffffu, all_zero);
+        if (lane == 0) {
+            int status = converged ? 0 : 1;
+            if (negative) status = 2;
+            if (all_zero) status = 3;
+            out.zero_point[f] = status == 0 ? a : NAN;
+            out.slope[f] = status == 0 ? b : NAN;
+            out.chi2[f] = status == 0 ? fin[0] : NAN;
+            out.ndata[f] = nd;
+            out.status[f] = status;
+            out.iterations[f] = it;
+        }
+    }
+}
+
+// forest weights of Dr16ExpectedFlux.compute_forest_weights
+// (dr16_expected_flux.py:466-488)
+__device__ __forceinline__ double forest_weight(const pg_cont_model &m, double ll, double iv,
+                                                double cont) {
+    if (!(iv > 0)) return 0.;
+    const double var_pipe = 1. / iv / (cont * cont);
+    double eta = 0., vlss = 1., fudge = 0.;
+    if (!m.use_constant_weight) {
+        eta = eval_ppoly(m.var_breaks, m.eta_coef, m.num_var_intervals, ll);
+        vlss = eval_ppoly(m.var_breaks, m.var_lss_coef, m.num_var_intervals, ll);
+        fudge = eval_ppoly(m.var_breaks, m.fudge_coef, m.num_var_intervals, ll);
+    }
+    return 1.0 / (eta * var_pipe + m.var_lss_mod * vlss + fudge / var_pipe);
+}
+
+__global__ void __launch_bounds__(kContBlock) cont_stacks_kernel(
+    const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
+    const __grid_constant__ pg_cont_fit fit, const __grid_constant__ pg_cont_stacks st,
+    Scratch *scratch) {
+    __shared__ uint32_t seen[kContBlock / 32][64];  // per-warp bitmap of var bins (<= 2048)
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const int nvar = st.var_lambda_bins * kVarBins;
+    for (int64_t f = warp_global; f < sp.num; f += nwarps) {
+        if (fit.status[f] != 0) continue;
+        const int64_t off = sp.pix_offset[f];
+        const int64_t n = sp.pix_offset[f + 1] - off;
+        const double zp1 = log10(1 + sp.z_qso[f]);
+        const bool do_var = st.var_mean != nullptr && nvar <= 2048;
+        if (do_var) {
+            for (int k = lane; k < 64; k += 32) seen[wib][k] = 0u;
+            __syncwarp();
+        }
+        for (int64_t p = lane; p < n; p += 32) {
+            const double ll = sp.log_lambda[off + p], fl = sp.flux[off + p];
+            const double iv = sp.ivar[off + p];
+            const double cont = fit.continuum[off + p];
+            if (st.mean_cont_num) {
+                // _compute_mean_cont: (f / (C + 1e-16)) * w binned in the rest frame
+                const double w = forest_weight(m, ll, iv, cont);
+                const int64_t bin = (int64_t)((ll - zp1 - st.rest_grid0) / st.rest_step + 0.5);
+                if (bin >= 0 && bin < st.rest_bins) {
+                    atomicAdd(&st.mean_cont_num[bin], fl / (cont + 1e-16) * w);
+                    atomicAdd(&st.mean_cont_weight[bin], w);
+                } else {
+                    report_error(scratch, PG_ERR_BIN_RANGE, (int32_t)bin);
+                }
+            }
+            if (st.stack_num) {
+                // compute_delta_stack: delta = f / C where ivar > 0
+                const double w = forest_weight(m, ll, iv, cont);
+                const double delta = iv > 0 ? fl / cont : 0.;
+                const int64_t bin = (int64_t)((ll - st.obs_grid0) / st.obs_step + 0.5);
+                if (bin >= 0 && bin < st.obs_bins) {
+                    atomicAdd(&st.stack_num[bin], delta * w);
+                    atomicAdd(&st.stack_weight[bin], w);
+                } else {
+                    report_error(scratch, PG_ERR_BIN_RANGE, (int32_t)bin);
+                }
+            }
+            if (do_var && iv > 0) {
+                // LeastsSquaresVarStats.initialize_delta_arrays
+                const double var_pipe = 1 / iv / (cont * cont);
+                const double lv = log10(var_pipe);
+                if (lv > kVarPipeMin && lv < kVarPipeMax) {
+                    const int vbin = (int)((lv - kVarPipeMin) / (kVarPipeMax - kVarPipeMin) * kVarBins);
+                    const int64_t lbin = (int64_t)((ll - st.var_grid0) / st.var_step + 0.5);
+                    const int64_t bin = vbin + (int64_t)kVarBins * lbin;
+                    if (bin >= 0 && bin < nvar) {
+                        const double delta = fl / cont - 1;
+                        const double d2 = delta * delta;
+                        atomicAdd(&st.var_mean[bin], delta);
+                        atomicAdd(&st.var_delta2[bin], d2);
+                        atomicAdd(&st.var_delta4[bin], d2 * d2);
+                        atomicAdd(&st.var_npix[bin], 1.0);
+                        atomicOr(&seen[wib][bin >> 5], 1u << (bin & 31));
+                    } else {
+                        report_error(scratch, PG_ERR_BIN_RANGE, (int32_t)bin);
+                    }
+                }
+            }
+        }
+        if (do_var) {
+            __syncwarp();
+            for (int k = lane; k < 64; k += 32) {
+                uint32_t bits = seen[wib][k];
+                while (bits) {
+                    const int bit = __ffs(bits) - 1;
+                    bits &= bits - 1;
+                    atomicAdd(&st.var_nqso[k * 32 + bit], 1.0);
+                }
+            }
+            __syncwarp();
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kContBlock) cont_deltas_kernel(
+    const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
+    const __grid_constant__ pg_cont_fit fit, double *__restrict__ delta,
+    double *__restrict__ weights) {
+    const int lane = threadIdx.x & 31;
+    const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t f = warp_global; f < sp.num; f += nwarps) {
+        const int64_t off = sp.pix_offset[f];
+        const int64_t n = sp.pix_offset[f + 1] - off;
+        const bool ok = fit.status[f] == 0;
+        for (int64_t p = lane; p < n; p += 32) {
+            double w = 0., d = 0.;
+            if (ok) {
+                const double ll = sp.log_lambda[off + p];
+                double expected = fit.continuum[off + p];
+                if (m.stack_x) expected *= interp_nearest(m.stack_x, m.stack_y, m.num_stack, ll);
+                w = forest_weight(m, ll, sp.ivar[off + p], expected);
+                if (w > 0) d = sp.flux[off + p] / expected - 1;
+            }
+            delta[off + p] = d;
+            weights[off + p] = w;
+        }
+    }
+}
+
+constexpr int kFeatBins = 64;
+
+// Warm-start network inputs (see pg_mlp_features in include/picca_gb300.h).
+__global__ void __launch_bounds__(kContBlock) mlp_features_kernel(
+    const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
+    __nv_bfloat16 *__restrict__ feat, int stride, double *__restrict__ a0_out) {
+    __shared__ float sums[kContBlock / 32][2][kFeatBins];
+    const int lane = threadIdx.x & 31;
+    const int wib = threadIdx.x >> 5;
+    const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const double span = m.log_lambda_rest_max - m.log_lambda_rest_min;
+    for (int64_t f = warp_global; f < sp.num; f += nwarps) {
+        for (int k = lane; k < kFeatBins; k += 32) {
+            sums[wib][0][k] = 0.f;
+            sums[wib][1][k] = 0.f;
+        }
+        __syncwarp();
+        const int64_t off = sp.pix_offset[f];
+        const int64_t n = sp.pix_offset[f + 1] - off;
+        const double zp1 = log10(1 + sp.z_qso[f]);
+        double sfi = 0., si = 0., snr = 0., cnt = 0.;
+        for (int64_t p = lane; p < n; p += 32) {
+            const double ll = sp.log_lambda[off + p], fl = sp.flux[off + p];
+            const double iv = sp.ivar[off + p];
+            sfi += fl * iv;
+            si += iv;
+            if (iv > 0) {
+                snr += fl * sqrt(iv);
+                cnt += 1.;
+                const double mc = interp_linear(m.mean_cont_x, m.mean_cont_y, m.num_mean_cont,
+                                                ll - zp1) * sp.transmission_correction[off + p];
+                int bin = (int)floor((ll - zp1 - m.log_lambda_rest_min) / span * kFeatBins);
+                bin = bin < 0 ? 0 : (bin >= kFeatBins ? kFeatBins - 1 : bin);
+                if (mc != 0.) {
+                    atomicAdd(&sums[wib][0][bin], (float)(fl / mc * iv));
+                    atomicAdd(&sums[wib][1][bin], (float)iv);
+                }
+            }
+        }
+        sfi = warp_sum(sfi);
+        si = warp_sum(si);
+        snr = warp_sum(snr);
+        cnt = warp_sum(cnt);
+        __syncwarp();
+        const double a0 = si > 0 ? sfi / si : 0.;
+        __nv_bfloat16 *row = feat + f * (int64_t)stride;
+        for (int k = lane; k < stride; k += 32) {
+            float v = 0.f;
+            if (k < kFeatBins) {
+                const float w = sums[wib][1][k];
+                v = (w > 0.f && a0 != 0.) ? (float)(sums[wib][0][k] / w / a0) - 1.f : 0.f;
+            } else if (k == kFeatBins) {
+                v = (float)(sp.z_qso[f] - 3.0);
+            } else if (k == kFeatBins + 1) {
+                v = (float)log(fmax(cnt > 0 ? snr / cnt : 0., 1e-3));
+            }
+            row[k] = __float2bfloat16(v);
+        }
+        if (lane == 0) a0_out[f] = a0;
+        __syncwarp();
+    }
+}
+
+unsigned blocks_for(int64_t num, int num_sms) {
+    const int64_t warps = (num + 0) > 0 ? num : 1;
+    int64_t blocks = (warps * 32 + kContBlock - 1) / kContBlock;
+    const int64_t cap = (int64_t)num_sms * 16;
+    if (blocks > cap) blocks = cap;
+    return (unsigned)(blocks < 1 ? 1 : blocks);
+}
+
+}  // namespace
+
+int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *start,
+                    int max_iter, double tol, int mode, const pg_cont_fit &out, Scratch *scratch,
+                    int num_sms, cudaStream_t stream) {
+    if (sp.num <= 0) return PG_OK;
+    const unsigned blocks = blocks_for(sp.num, num_sms);
+    if (mode == PG_FIT_MIXED)
+        cont_fit_kernel<float><<<blocks, kContBlock, 0, stream>>>(sp, m, start, max_iter, tol,
+                                                                   out, scratch);
+    else
+        cont_fit_kernel<double><<<blocks, kContBlock, 0, stream>>>(sp, m, start, max_iter, tol,
+                                                                    out, scratch);
+    return check_cuda(cudaGetLastError());
+}
+
+int launch_cont_stacks(const pg_spectra &sp, const pg_cont_model &m, const pg_cont_fit &fit,
+                       const pg_cont_stacks &st, Scratch *scratch, int num_sms,
+                       cudaStream_t stream) {
+    if (sp.num <= 0) return PG_OK;
+    if (st.var_mean && st.var_lambda_bins * kVarBins > 2048) return PG_ERR_UNSUPPORTED;
+    cont_stacks_kernel<<<blocks_for(sp.num, num_sms), kContBlock, 0, stream>>>(sp, m, fit, st,
+                                                                               scratch);
+    return check_cuda(cudaGetLastError());
+}
+
+int launch_mlp_features(const pg_spectra &sp, const pg_cont_model &m, uint16_t *features,
+                        int stride, double *a0, int num_sms, cudaStream_t stream) {
+    if (sp.num <= 0) return PG_OK;
+    mlp_features_kernel<<<blocks_for(sp.num, num_sms), kContBlock, 0, stream>>>(
+        sp, m, reinterpret_cast<__nv_bfloat16 *>(features), stride, a0);
+    return check_cuda(cudaGetLastError());
+}
+
+int launch_cont_deltas(const pg_spectra &sp, const pg_cont_model &m, const pg_cont_fit &fit,
+                       double *delta, double *weights, int num_sms, cudaStream_t stream) {
+    if (sp.num <= 0) return PG_OK;
+    cont_deltas_kernel<<<blocks_for(sp.num, num_sms), kContBlock, 0, stream>>>(sp, m, fit, delta,
+                                                                               weights);
+    return check_cuda(cudaGetLastError());
+}
+
+}  // namespace pg

@@ -211,4 +211,15 @@ int launch_xcf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &fo
                        const pg_xi_rows &out, Scratch *scratch, void *fast_const, int num_sms,
                        cudaStream_t stream);
 
+int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *start,
+                    int max_iter, double tol, int mode, const pg_cont_fit &out, Scratch *scratch,
+                    int num_sms, cudaStream_t stream);
+int launch_cont_stacks(const pg_spectra &sp, const pg_cont_model &m, const pg_cont_fit &fit,
+                       const pg_cont_stacks &st, Scratch *scratch, int num_sms,
+                       cudaStream_t stream);
+int launch_cont_deltas(const pg_spectra &sp, const pg_cont_model &m, const pg_cont_fit &fit,
+                       double *delta, double *weights, int num_sms, cudaStream_t stream);
+int launch_mlp_features(const pg_spectra &sp, const pg_cont_model &m, uint16_t *features,
+                        int stride, double *a0, int num_sms, cudaStream_t stream);
+
 }  // namespace pg

@@ -5,11 +5,12 @@
 // of set 1 with all its neighbours; warps take neighbour forests; lanes own
 // forest-2 pixels in registers and loop over the forest-1 pixels staged in
 // shared memory). For every pixel pair the kernel evaluates, in FP32,
-//     p = cp*(r1' - r2')            (= r_par * np/(r_par_max - r_par_min))
-//     x_par = |p| - r_par_min*inv_p (p itself for signed, cross correlations)
-//     x_tr  = st*d1 + st*d2         (= r_trans * nt/r_trans_max)
-// with cp = cos(theta/2) * inv_p, st = sin(theta/2) * inv_t, r' = r_comov -
-// R0. The bin index of py/picca/cf.py:372-376 is floor(x). It is taken with
+//     p = cp*((r1h - r2h) + (r1l - r2l))   (= r_par * np/(r_par_max - r_par_min))
+//     x_par = |p| - r_par_min*inv_p       (p itself for signed, cross correlations)
+//     x_tr  = st*d1 + st*d2               (= r_trans * nt/r_trans_max)
+// with cp = cos(theta/2) * inv_p, st = sin(theta/2) * inv_t, and the comoving
+// distance carried as an FP32 pair r = rh + rl, so that r1 - r2 is exact to
+// ~1e-7 of itself (not of r). The bin index of py/picca/cf.py:372-376 is floor(x). It is taken with
 // one round-toward-minus-infinity add: y = x + (2^23 + 1) rounded down is
 // 2^23 + 1 + floor(x) for every x >= -1, so floor(x) = bits(y) - bits(2^23)
 // - 1 and x - (y - (2^23 + 1)) is the fractional part. A pair whose
@@ -40,7 +41,7 @@ constexpr int kXcfP = 2;                   // quasars per lane per pass
 constexpr int kCfBlock = 384;              // cf threads per CTA (2 CTAs per SM)
 
 struct FastConst {
-    double inv_p, inv_t, r0;
+    double inv_p, inv_t;
     float pmin;             // r_par_min * inv_p
     float g_par, g_tr;      // guard bands (fraction of a bin)
     float one_m_g_par, one_m_g_tr;
@@ -176,15 +177,16 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
     const int warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
     const int hs = fcp->hstride;
-    const double inv_p = fcp->inv_p, inv_t = fcp->inv_t, r0 = fcp->r0;
+    const double inv_p = fcp->inv_p, inv_t = fcp->inv_t;
     const float pmin = fcp->pmin;
     const float g_par = fcp->g_par, g_tr = fcp->g_tr;
     const float omg_par = fcp->one_m_g_par, omg_tr = fcp->one_m_g_tr;
     const unsigned np = fcp->np, nt = fcp->nt;
     float *h = reinterpret_cast<float *>(smem);
     float4 *p1 = reinterpret_cast<float4 *>(h + H_COUNT * hs);
-    float *dw1s = reinterpret_cast<float *>(p1 + max_pix1);
-    uint32_t *queue = reinterpret_cast<uint32_t *>(dw1s + max_pix1) + warp * kQueue;
+    float2 *p2 = reinterpret_cast<float2 *>(p1 + max_pix1);
+    uint32_t *queue = reinterpret_cast<uint32_t *>(p2 + max_pix1) + warp * kQueue;
+    __shared__ long long nbr_next;
     zero_all(h, hs);
     unsigned long long rechecks = 0, overflows = 0;
 
@@ -200,19 +202,27 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
             continue;
         }
         const int n1 = (int)n1_64;
-        // stage forest 1: r' = r - R0, dist_m, z, w and delta*w in FP32
+        // stage forest 1 in FP32: r as (hi, lo), dist_m, z; (w, delta*w)
         for (int i = threadIdx.x; i < n1; i += blockDim.x) {
             const double w = s1.weights[a0 + i];
-            p1[i] = make_float4((float)(s1.r_comov[a0 + i] - r0), (float)s1.dist_m[a0 + i],
-                                (float)s1.z[a0 + i], weight32(w));
-            dw1s[i] = (float)(s1.delta[a0 + i] * w);
+            const double r = s1.r_comov[a0 + i];
+            const float rh = (float)r;
+            p1[i] = make_float4(rh, (float)(r - (double)rh), (float)s1.dist_m[a0 + i],
+                                (float)s1.z[a0 + i]);
+            p2[i] = make_float2(weight32(w), (float)(s1.delta[a0 + i] * w));
         }
-        __syncthreads();
         const double x1 = s1.x_cart[f1], y1 = s1.y_cart[f1], zc1 = s1.z_cart[f1];
         const double ra1 = s1.ra[f1], dec1 = s1.dec[f1], cd1 = s1.cos_dec[f1];
         const double zq1 = s1.z_qso[f1];
         const int64_t k0 = nbr_offsets[f1], k1 = nbr_offsets[f1 + 1];
-        for (int64_t k = k0 + warp; k < k1; k += nwarps) {
+        if (threadIdx.x == 0) nbr_next = k0;
+        __syncthreads();
+        for (;;) {
+            // warps take neighbour forests dynamically (balances uneven lengths)
+            int64_t k = 0;
+            if (lane == 0) k = (int64_t)atomicAdd((unsigned long long *)&nbr_next, 1ull);
+            k = __shfl_sync(0xffffffffu, k, 0);
+            if (k >= k1) break;
             CfPairCtx ctx;
             const int64_t g = nbr_index[k];
             ctx.a0 = a0;
@@ -244,12 +254,12 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
             const float st = (float)(ctx.s * inv_t);
             int qn = 0;
             for (int jb = 0; jb < n2; jb += 32 * kCfP) {
-                float a[kCfP], t[kCfP], zv[kCfP], wv[kCfP], dv[kCfP];
+                float rh[kCfP], rl[kCfP], t[kCfP], zv[kCfP], wv[kCfP], dv[kCfP];
                 unsigned vmask = 0;
 #pragma unroll
                 for (int p = 0; p < kCfP; ++p) {
                     const int j = jb + lane + 32 * p;
-                    a[p] = 0.f; t[p] = 0.f; zv[p] = 0.f; wv[p] = 0.f; dv[p] = 0.f;
+                    rh[p] = 0.f; rl[p] = 0.f; t[p] = 0.f; zv[p] = 0.f; wv[p] = 0.f; dv[p] = 0.f;
                     if (j < n2) {
                         const int64_t jj = ctx.b0 + j;
                         const double w2 = s2.weights[jj];
@@ -257,7 +267,9 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
                         if (EXTRA && zerr_pair && ok) ok = !zerr_veto(s2.z[jj], zq1, b.zerr_kms);
                         if (ok) {
                             vmask |= 1u << p;
-                            a[p] = cp * (float)(s2.r_comov[jj] - r0);
+                            const double r = s2.r_comov[jj];
+                            rh[p] = (float)r;
+                            rl[p] = (float)(r - (double)rh[p]);
                             t[p] = st * (float)s2.dist_m[jj];
                             zv[p] = (float)s2.z[jj];
                             wv[p] = weight32(w2);
@@ -267,16 +279,16 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
                 }
                 if (__ballot_sync(0xffffffffu, vmask != 0) == 0) continue;
                 for (int i = 0; i < n1; ++i) {
-                    const float4 q = p1[i];
-                    if (q.w == 0.f) continue;  // zero-weight pixel (warp-uniform)
+                    const float2 qw = p2[i];
+                    if (qw.x == 0.f) continue;  // zero-weight pixel (warp-uniform)
                     if (EXTRA && zerr_pair && zerr_veto(s1.z[a0 + i], zq2, b.zerr_kms)) continue;
-                    const float dw1 = dw1s[i];
-                    const float bi = cp * q.x;
-                    const float ui = st * q.y;
+                    const float4 q = p1[i];
+                    const float dw1 = qw.y;
+                    const float ui = st * q.z;
                     unsigned near_mask = 0;
 #pragma unroll
                     for (int p = 0; p < kCfP; ++p) {
-                        const float diff = bi - a[p];
+                        const float diff = cp * ((q.x - rh[p]) + (q.y - rl[p]));
                         const float v = fabsf(diff);
                         const float pv = AUTO ? v : diff;
                         const float tv = ui + t[p];
@@ -285,7 +297,7 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
                         const unsigned it = floor_frac(tv, ft);
                         bool near = (fp < g_par) | (fp > omg_par) | (ft < g_tr) | (ft > omg_tr);
                         bool ok = (ip < np) & (it < nt);
-                        const float zs = q.z + zv[p];
+                        const float zs = q.w + zv[p];
                         if (EXTRA) {
                             if (ctx.shp) {
                                 near |= fabsf(v - 1.f) < fcp->guard_v;
@@ -303,7 +315,7 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
                         const bool valid = (vmask >> p) & 1u;
                         near_mask |= (unsigned)(near & valid) << p;
                         if (ok & valid & !near) {
-                            const float w12 = q.w * wv[p];
+                            const float w12 = qw.x * wv[p];
                             acc_pair(h, hs, (int)(ip * nt + it), dw1 * dv[p], w12, pv * w12,
                                      tv * w12, zs * w12);
                         }
@@ -408,15 +420,15 @@ __global__ void __launch_bounds__(512, 1) xcf_xi_fast_kernel(
     const int warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
     const int hs = fcp->hstride;
-    const double inv_p = fcp->inv_p, inv_t = fcp->inv_t, r0 = fcp->r0;
+    const double inv_p = fcp->inv_p, inv_t = fcp->inv_t;
     const float pmin = fcp->pmin;
     const float g_par = fcp->g_par, g_tr = fcp->g_tr;
     const float omg_par = fcp->one_m_g_par, omg_tr = fcp->one_m_g_tr;
     const unsigned np = fcp->np, nt = fcp->nt;
     float *h = reinterpret_cast<float *>(smem);
     float4 *p1 = reinterpret_cast<float4 *>(h + H_COUNT * hs);
-    float *dw1s = reinterpret_cast<float *>(p1 + max_pix1);
-    uint32_t *queue = reinterpret_cast<uint32_t *>(dw1s + max_pix1) + warp * kQueue;
+    float2 *p2 = reinterpret_cast<float2 *>(p1 + max_pix1);
+    uint32_t *queue = reinterpret_cast<uint32_t *>(p2 + max_pix1) + warp * kQueue;
     zero_all(h, hs);
     unsigned long long rechecks = 0, overflows = 0;
 
@@ -436,9 +448,11 @@ __global__ void __launch_bounds__(512, 1) xcf_xi_fast_kernel(
         const int n1 = (int)n1_64;
         for (int i = threadIdx.x; i < n1; i += blockDim.x) {
             const double w = fs.weights[ctx.a0 + i];
-            p1[i] = make_float4((float)(fs.r_comov[ctx.a0 + i] - r0), (float)fs.dist_m[ctx.a0 + i],
-                                (float)fs.z[ctx.a0 + i], weight32(w));
-            dw1s[i] = (float)(fs.delta[ctx.a0 + i] * w);
+            const double r = fs.r_comov[ctx.a0 + i];
+            const float rh = (float)r;
+            p1[i] = make_float4(rh, (float)(r - (double)rh), (float)fs.dist_m[ctx.a0 + i],
+                                (float)fs.z[ctx.a0 + i]);
+            p2[i] = make_float2(weight32(w), (float)(fs.delta[ctx.a0 + i] * w));
         }
         __syncthreads();
         ctx.x1 = fs.x_cart[f]; ctx.y1 = fs.y_cart[f]; ctx.zc1 = fs.z_cart[f];
@@ -446,12 +460,13 @@ __global__ void __launch_bounds__(512, 1) xcf_xi_fast_kernel(
         ctx.k0 = nbr_offsets[f];
         const int nq = (int)nq_64;
         for (int kb = warp * 32 * kXcfP; kb < nq; kb += nwarps * 32 * kXcfP) {
-            float cp[kXcfP], st[kXcfP], a[kXcfP], t[kXcfP], zv[kXcfP], wv[kXcfP];
+            float cp[kXcfP], st[kXcfP], rh[kXcfP], rl[kXcfP], t[kXcfP], zv[kXcfP], wv[kXcfP];
             unsigned vmask = 0;
 #pragma unroll
             for (int p = 0; p < kXcfP; ++p) {
                 const int kk = kb + lane + 32 * p;
-                cp[p] = 0.f; st[p] = 0.f; a[p] = 0.f; t[p] = 0.f; zv[p] = 0.f; wv[p] = 0.f;
+                cp[p] = 0.f; st[p] = 0.f; rh[p] = 0.f; rl[p] = 0.f; t[p] = 0.f; zv[p] = 0.f;
+                wv[p] = 0.f;
                 if (kk < nq) {
                     const int64_t g = nbr_index[ctx.k0 + kk];
                     const double wq = objs.obj_weight[g];
@@ -464,7 +479,9 @@ __global__ void __launch_bounds__(512, 1) xcf_xi_fast_kernel(
                                                       objs.z_cart[g], objs.ra[g], objs.dec[g]);
                         cp[p] = (float)(cos(ang / 2) * inv_p);
                         st[p] = (float)(sin(ang / 2) * inv_t);
-                        a[p] = cp[p] * (float)(objs.obj_r_comov[g] - r0);
+                        const double r = objs.obj_r_comov[g];
+                        rh[p] = (float)r;
+                        rl[p] = (float)(r - (double)rh[p]);
                         t[p] = st[p] * (float)objs.obj_dist_m[g];
                         zv[p] = (float)objs.z_qso[g];
                         wv[p] = weight32(wq);
@@ -474,20 +491,21 @@ __global__ void __launch_bounds__(512, 1) xcf_xi_fast_kernel(
             if (__ballot_sync(0xffffffffu, vmask != 0) == 0) continue;
             int qn = 0;
             for (int i = 0; i < n1; ++i) {
+                const float2 qw = p2[i];
+                if (qw.x == 0.f) continue;
                 const float4 q = p1[i];
-                if (q.w == 0.f) continue;
-                const float dw1 = dw1s[i];
+                const float dw1 = qw.y;
                 unsigned near_mask = 0;
 #pragma unroll
                 for (int p = 0; p < kXcfP; ++p) {
-                    const float pv = __fmaf_rn(cp[p], q.x, -a[p]);
-                    const float tv = __fmaf_rn(st[p], q.y, t[p]);
+                    const float pv = cp[p] * ((q.x - rh[p]) + (q.y - rl[p]));
+                    const float tv = __fmaf_rn(st[p], q.z, t[p]);
                     float fp, ft;
                     const unsigned ip = floor_frac(pv - pmin, fp);
                     const unsigned it = floor_frac(tv, ft);
                     bool near = (fp < g_par) | (fp > omg_par) | (ft < g_tr) | (ft > omg_tr);
                     bool ok = (ip < np) & (it < nt);
-                    const float zs = q.z + zv[p];
+                    const float zs = q.w + zv[p];
                     if (EXTRA) {
                         if (b.zmin_on) {
                             near |= fabsf(zs - fcp->zmin2) < fcp->guard_z;
@@ -501,7 +519,7 @@ __global__ void __launch_bounds__(512, 1) xcf_xi_fast_kernel(
                     const bool valid = (vmask >> p) & 1u;
                     near_mask |= (unsigned)(near & valid) << p;
                     if (ok & valid & !near) {
-                        const float w12 = q.w * wv[p];
+                        const float w12 = qw.x * wv[p];
                         acc_pair(h, hs, (int)(ip * nt + it), dw1 * wv[p], w12, pv * w12,
                                  tv * w12, zs * w12);
                     }
@@ -543,33 +561,27 @@ __global__ void __launch_bounds__(512, 1) xcf_xi_fast_kernel(
     }
 }
 
-// Guard bands. Let u = 2^-24. The FP32 inputs carry rounding errors |r'| u
-// (r' = r - R0, |r'| <= R) and d u (d <= D). In p = cp*r1' - cp*r2' each of
-// the roundings (two products, one difference, and cp = c*inv_p itself) is
-// at most u times a value bounded by X_p = cp_max*R + |p| <= 2 cp_max R;
-// the input errors add 2 cp_max R u; subtracting pmin adds u(|p| + |pmin|).
-// Likewise x_tr = st*d1 + st*d2 with X_t = 2 st_max D. Summing and doubling
-// for margin:
-//   g_par = 2 u (8 (2 cp_max R + np + |pmin| + 1) + 2 cp_max R)
-//   g_tr  = 2 u (8 (2 st_max D + nt + 1) + 2 st_max D)
+// Guard bands. Let u = 2^-24. r is carried as rh + rl with |r - rh - rl|
+// <= u^2 r (negligible), so r1 - r2 = (r1h - r2h) + (r1l - r2l) is formed
+// with two roundings of size u |r1 - r2| and u |r1l - r2l|; the product with
+// cp (itself rounded, relative u) and the subtraction of pmin add u |p| and
+// u |x|. Altogether |x_par(FP32) - x_par| <= 6 u (|x| + |pmin| + 1). For
+// x_tr = st d1 + st d2 the FP32 rounding of d1 and d2 (relative u), of the
+// two products, of st and of the sum give <= 5 u |x_tr|. Only pairs whose
+// exact x lies in [-1, n + 1] matter (the others are rejected either way),
+// so with a factor > 2 of margin
+//   g = 16 u (n + |pmin| + 2) + 1e-6.
 // The reference's own FP64 evaluation is within 1e-12 of the exact value,
-// far inside these bands. floor(x) is exact; its fractional part carries one
-// more rounding of size u*|x|, covered by the margin.
-__host__ __device__ FastConst make_fast_const(const Binning &b, double r0, double r_span,
-                                              double d_max, double ang_max) {
+// far inside these bands.
+FastConst make_fast_const(const Binning &b) {
     FastConst fc{};
     const double u = 1.0 / 16777216.0;
     fc.inv_p = (double)b.np / b.r_par_range;
     fc.inv_t = (double)b.nt / b.r_trans_max;
-    fc.r0 = r0;
     fc.pmin = (float)(b.r_par_min * fc.inv_p);
-    const double cp_max = fc.inv_p;  // cos(theta/2) <= 1
-    const double st_max = sin(fmin(ang_max, kPi) / 2) * fc.inv_t;
-    const double xr = 2 * cp_max * r_span + b.np + fabs(b.r_par_min * fc.inv_p) + 1;
-    const double xt = 2 * st_max * d_max + b.nt + 1;
-    double g_par = 2 * u * (8 * xr + 2 * cp_max * r_span) + 1e-6;
-    double g_tr = 2 * u * (8 * xt + 2 * st_max * d_max) + 1e-6;
-    if (!(g_par < 0.05)) g_par = 0.05;  // degenerate inputs: almost everything is re-decided
+    double g_par = 16 * u * (b.np + fabs(b.r_par_min * fc.inv_p) + 2) + 1e-6;
+    double g_tr = 16 * u * (b.nt + 2) + 1e-6;
+    if (!(g_par < 0.05)) g_par = 0.05;  // absurd bin counts: almost everything is re-decided
     if (!(g_tr < 0.05)) g_tr = 0.05;
     fc.g_par = (float)g_par;
     fc.g_tr = (float)g_tr;
@@ -586,59 +598,11 @@ __host__ __device__ FastConst make_fast_const(const Binning &b, double r0, doubl
     return fc;
 }
 
-// Data ranges of r_comov and dist_m (pixels and quasar objects).
-__global__ void range_kernel(const double *__restrict__ r, const double *__restrict__ d, int64_t n,
-                             Scratch *scratch) {
-    double rmin = INFINITY, rmax = -INFINITY, dmax = 0.;
-    for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n;
-         i += (int64_t)gridDim.x * blockDim.x) {
-        const double rv = r[i], dv = fabs(d[i]);
-        rmin = fmin(rmin, rv);
-        rmax = fmax(rmax, rv);
-        dmax = fmax(dmax, dv);
-    }
-    for (int o = 16; o > 0; o >>= 1) {
-        rmin = fmin(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
-        rmax = fmax(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-        dmax = fmax(dmax, __shfl_xor_sync(0xffffffffu, dmax, o));
-    }
-    if ((threadIdx.x & 31) == 0) {
-        atomicMin(&scratch->r_min_key, order_key(rmin));
-        atomicMax(&scratch->r_max_key, order_key(rmax));
-        atomicMax(&scratch->d_max_key, order_key(dmax));
-    }
-}
-
-__global__ void init_ranges_kernel(Scratch *scratch) {
-    scratch->r_min_key = order_key(INFINITY);
-    scratch->r_max_key = order_key(-INFINITY);
-    scratch->d_max_key = order_key(0.);
-}
-
-__global__ void fast_const_kernel(Binning b, double ang_max, const Scratch *scratch,
-                                  FastConst *fc) {
-    const double rmin = order_value(scratch->r_min_key);
-    const double rmax = order_value(scratch->r_max_key);
-    const double dmax = order_value(scratch->d_max_key);
-    double r0 = 0.5 * (rmin + rmax), span = 0.5 * (rmax - rmin);
-    if (!(rmin <= rmax)) {
-        r0 = 0.;
-        span = 0.;
-    }
-    *fc = make_fast_const(b, r0, span, dmax, ang_max);
-}
-
-int scan_ranges(const double *r, const double *d, int64_t n, Scratch *scratch,
-                cudaStream_t stream) {
-    if (n <= 0 || r == nullptr || d == nullptr) return PG_OK;
-    int64_t blocks = (n + 255) / 256;
-    if (blocks > 4096) blocks = 4096;
-    range_kernel<<<(unsigned)blocks, 256, 0, stream>>>(r, d, n, scratch);
-    return check_cuda(cudaGetLastError());
-}
+// Writes the constants into the plan's device buffer in stream order.
+__global__ void store_const_kernel(FastConst value, FastConst *dst) { *dst = value; }
 
 size_t fast_smem_bytes(int hstride, int max_pix1, int nwarps) {
-    return (size_t)hstride * H_COUNT * 4 + (size_t)max_pix1 * 20 + (size_t)nwarps * kQueue * 4;
+    return (size_t)hstride * H_COUNT * 4 + (size_t)max_pix1 * 24 + (size_t)nwarps * kQueue * 4;
 }
 
 template <typename K>
@@ -656,15 +620,8 @@ int persistent_grid(K kernel, int block, size_t smem, int num_sms, int64_t num_w
     return PG_OK;
 }
 
-int prepare_fast(const Binning &b, double ang_max, const double *r1, const double *d1, int64_t n1,
-                 const double *r2, const double *d2, int64_t n2, Scratch *scratch,
-                 FastConst *fc, cudaStream_t stream) {
-    init_ranges_kernel<<<1, 1, 0, stream>>>(scratch);
-    int rc = check_cuda(cudaGetLastError());
-    if (rc) return rc;
-    if ((rc = scan_ranges(r1, d1, n1, scratch, stream))) return rc;
-    if (r2 != r1 && (rc = scan_ranges(r2, d2, n2, scratch, stream))) return rc;
-    fast_const_kernel<<<1, 1, 0, stream>>>(b, ang_max, scratch, fc);
+int prepare_fast(const Binning &b, FastConst *fc, cudaStream_t stream) {
+    store_const_kernel<<<1, 1, 0, stream>>>(make_fast_const(b), fc);
     return check_cuda(cudaGetLastError());
 }
 
@@ -684,8 +641,8 @@ int launch_cf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &s1,
     const int max_pix1 = s1.max_pixels;
     const size_t smem = fast_smem_bytes((b.nbins + 3) & ~3, max_pix1, block / 32);
     if (smem > 227 * 1024) return PG_ERR_UNSUPPORTED;
-    int rc = prepare_fast(b, ang_max, s1.r_comov, s1.dist_m, s1.num_pixels, s2.r_comov,
-                          s2.dist_m, s2.num_pixels, scratch, fc, stream);
+    (void)ang_max;
+    int rc = prepare_fast(b, fc, stream);
     if (rc) return rc;
     const bool extra = b.remove_shp || b.zmin_on || b.zmax_on || b.zerr_on;
     const bool autoc = !b.x_correlation;
@@ -716,8 +673,8 @@ int launch_xcf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &fo
     const int max_pix1 = forests.max_pixels;
     const size_t smem = fast_smem_bytes((b.nbins + 3) & ~3, max_pix1, block / 32);
     if (smem > 227 * 1024) return PG_ERR_UNSUPPORTED;
-    int rc = prepare_fast(b, ang_max, forests.r_comov, forests.dist_m, forests.num_pixels,
-                          objs.obj_r_comov, objs.obj_dist_m, objs.num, scratch, fc, stream);
+    (void)ang_max;
+    int rc = prepare_fast(b, fc, stream);
     if (rc) return rc;
     const bool extra = b.zmin_on || b.zmax_on;
     int grid = 0;

@@ -280,6 +280,52 @@ def _pair_cases(reference_py, delta_dir, attributes):
     return case_index, xcase
 
 
+def _continuum_cases(reference_py):
+    """chi2 of picca's own LeastsSquaresContModel (least_squares_cont_model.py:
+    65-197) on synthetic forests at several (zero_point, slope) points."""
+    sys.dont_write_bytecode = True
+    if reference_py not in sys.path:
+        sys.path.insert(0, reference_py)
+    from picca.delta_extraction.least_squares.least_squares_cont_model import (  # noqa: E501 pylint: disable=import-outside-toplevel
+        LeastsSquaresContModel)
+    from picca_gb300 import synthetic_spectra
+    raw = synthetic_spectra.make_raw_forests(12, 424242)
+    rng = np.random.default_rng(77)
+    grid = raw.grid
+    out = {"num_cases": np.asarray(raw.num)}
+    for k in range(raw.num):
+        ll, fl, iv, _ = raw.forest(k)
+        iv = iv.copy()
+        iv[rng.random(len(iv)) < 0.05] = 0.0  # some masked pixels
+        zq = raw.z_qso[k]
+        mean_cont = 1.0 + 0.2 * np.sin(ll * 40.0)
+        eta = 0.8 + 0.4 * rng.random(len(ll))
+        var_lss = 0.05 + 0.1 * rng.random(len(ll))
+        fudge = 1e-3 * rng.random(len(ll))
+        ll_min = grid.log_lambda_rest_frame_grid[0] + np.log10(1 + zq)
+        ll_max = grid.log_lambda_rest_frame_grid[-1] + np.log10(1 + zq)
+        forest = types.SimpleNamespace(log_lambda=ll, flux=fl, ivar=iv)
+        model = LeastsSquaresContModel(
+            forest=forest,
+            mean_cont_kwargs={"mean_cont": mean_cont, "log_lambda_max": ll_max,
+                              "log_lambda_min": ll_min},
+            weights_kwargs={"use_constant_weight": False, "eta": eta, "var_lss": var_lss,
+                            "fudge": fudge})
+        a0 = (fl * iv).sum() / iv.sum()
+        points = [(a0, 0.0), (1.1 * a0, 0.3 * a0), (0.8 * a0, -0.2 * a0), (a0, 0.05)]
+        values = [model(a, b) for a, b in points]
+        pre = f"c{k}_"
+        for key, val in (("ll", ll), ("flux", fl), ("ivar", iv), ("mean_cont", mean_cont),
+                         ("eta", eta), ("var_lss", var_lss), ("fudge", fudge)):
+            out[pre + key] = np.asarray(val, dtype=float)
+        out[pre + "scalars"] = np.array([zq, ll_min, ll_max])
+        out[pre + "points"] = np.array(points)
+        out[pre + "chi2"] = np.array(values)
+        out[pre + "ndata"] = np.asarray(model.get_ndata())
+    np.savez_compressed(os.path.join(HERE, "continuum_cases.npz"), **out)
+    return raw.num
+
+
 def main(picca_root):
     tests = os.path.join(picca_root, "py", "picca", "tests", "data")
     _convert_delta_dir(os.path.join(tests, "test_delta", "Delta_LYA"),
@@ -294,7 +340,8 @@ def main(picca_root):
     ncf, nxcf = _pair_cases(os.path.join(picca_root, "py"),
                             os.path.join(tests, "test_delta", "Delta_LYA") + "/",
                             os.path.join(tests, "test_delta", "delta_attributes.fits.gz"))
-    print(f"wrote fixtures: {ncf} cf pair cases, {nxcf} xcf cases")
+    ncont = _continuum_cases(os.path.join(picca_root, "py"))
+    print(f"wrote fixtures: {ncf} cf pair cases, {nxcf} xcf cases, {ncont} continuum cases")
 
 
 if __name__ == "__main__":
