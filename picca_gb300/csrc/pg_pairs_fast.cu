@@ -51,6 +51,8 @@ struct FastConst {
     unsigned np, nt;
     int nbins;
     int hstride;            // histogram array stride (nbins rounded up to 4)
+    int lower_exact;        // auto-correlation with r_par_min = 0: x_par = |p| >= 0, so
+                            // the lower edge of bin 0 can never be crossed
 };
 
 enum {
@@ -175,13 +177,13 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
     __shared__ int item_slot;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int nwarps = blockDim.x >> 5;
     const int hs = fcp->hstride;
     const double inv_p = fcp->inv_p, inv_t = fcp->inv_t;
     const float pmin = fcp->pmin;
     const float g_par = fcp->g_par, g_tr = fcp->g_tr;
     const float omg_par = fcp->one_m_g_par, omg_tr = fcp->one_m_g_tr;
     const unsigned np = fcp->np, nt = fcp->nt;
+    const bool lower_exact = AUTO && fcp->lower_exact;
     float *h = reinterpret_cast<float *>(smem);
     float4 *p1 = reinterpret_cast<float4 *>(h + H_COUNT * hs);
     float2 *p2 = reinterpret_cast<float2 *>(p1 + max_pix1);
@@ -295,7 +297,8 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
                         float fp, ft;
                         const unsigned ip = floor_frac(pv - pmin, fp);
                         const unsigned it = floor_frac(tv, ft);
-                        bool near = (fp < g_par) | (fp > omg_par) | (ft < g_tr) | (ft > omg_tr);
+                        bool near = ((fp < g_par) & ((ip != 0u) | !lower_exact)) | (fp > omg_par) |
+                                    (ft < g_tr) | (ft > omg_tr);
                         bool ok = (ip < np) & (it < nt);
                         const float zs = q.w + zv[p];
                         if (EXTRA) {
@@ -595,6 +598,7 @@ FastConst make_fast_const(const Binning &b) {
     fc.nt = (unsigned)b.nt;
     fc.nbins = b.nbins;
     fc.hstride = (b.nbins + 3) & ~3;
+    fc.lower_exact = (!b.x_correlation && b.r_par_min == 0.0) ? 1 : 0;
     return fc;
 }
 
