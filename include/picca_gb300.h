@@ -149,6 +149,24 @@ int pg_xcf_xi(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *
               const double *nbr_angle, const int32_t *work_order, int64_t num_work,
               int32_t mode, const pg_xi_rows *out, void *stream);
 
+/* pg_cf_xi for callers that cannot allocate device memory. No counterpart
+ * in the reference. Some callers cannot call cudaMalloc (a framework owns
+ * the device allocator, or every buffer is sized at start-up), and a
+ * pg_plan allocates its scratch. This variant needs no plan: the scratch
+ * lives in a library-owned device array of PG_STATIC_SCRATCH_BYTES bytes
+ * (held by every GPU that loads the library until exit). All calls on a
+ * device share that array: calls that overlap on the GPU race and give
+ * wrong results. The first call with a device current looks up the
+ * array's address and should come before any stream capture. The call
+ * synchronises `stream` and returns the kernel's device-side status;
+ * PG_ERR_UNSUPPORTED if the scratch would not fit in the array. */
+#define PG_STATIC_SCRATCH_BYTES 4096
+int pg_cf_xi_static(const pg_corr_params *params, const pg_forest_set *s1,
+                    const pg_forest_set *s2, const int64_t *nbr_offsets,
+                    const int32_t *nbr_index, const double *nbr_angle,
+                    const int32_t *work_order, int64_t num_work, int32_t mode,
+                    const pg_xi_rows *out, void *stream);
+
 /* ------------------------------------------------------------------------ */
 /* Dr16 continuum fit                                                        */
 /* ------------------------------------------------------------------------ */
