@@ -193,13 +193,16 @@ def continuum_leg(args, cpu_seconds):
         torch.cuda.synchronize()
         return out, start.elapsed_time(end) / 1e3
 
+    mixed = continuum.FIT_MIXED
     # warm-up on a small set (module loading, first launches)
     small = synthetic_spectra.make_raw_forests(2000, 7)
-    eng = continuum.Dr16Gpu(small.grid, num_iterations=2)
-    eng.run(continuum.DeviceSpectra(small, eng.device))
+    for mode in (mixed, continuum.FIT_FP64):
+        eng = continuum.Dr16Gpu(small.grid, num_iterations=2, fit_mode=mode)
+        eng.run(continuum.DeviceSpectra(small, eng.device))
 
-    # plain leg (config 3): fit kernel time measured separately
-    eng_p = continuum.Dr16Gpu(eval_raw.grid, num_iterations=iters)
+    # plain leg (config 3): FP32 per-pixel terms, FP64 2x2 Newton solve;
+    # fit kernel time measured separately
+    eng_p = continuum.Dr16Gpu(eval_raw.grid, num_iterations=iters, fit_mode=mixed)
     spectra = continuum.DeviceSpectra(eval_raw, eng_p.device)
     fit_events = []
     orig_fit = eng_p.fit
@@ -218,8 +221,22 @@ def continuum_leg(args, cpu_seconds):
     fit_ms = [a.elapsed_time(b) for a, b in fit_events]
     plain = continuum.fit_results_to_host(plain_fit)
 
+    # the same first-iteration fit with every per-pixel term in FP64
+    eng_64 = continuum.Dr16Gpu(eval_raw.grid, num_iterations=1)
+    eng_32 = continuum.Dr16Gpu(eval_raw.grid, num_iterations=1, fit_mode=mixed)
+    f32, _ = timed_loop(lambda: eng_32.fit(spectra))
+    f64, fp64_s = timed_loop(lambda: eng_64.fit(spectra))
+    f32, f64 = continuum.fit_results_to_host(f32), continuum.fit_results_to_host(f64)
+    both = (f32["status"] == 0) & (f64["status"] == 0)
+    sc64 = np.maximum(1.0, np.maximum(np.abs(f64["zero_point"]), np.abs(f64["slope"])))
+    d_mixed = (np.maximum(np.abs(f32["zero_point"] - f64["zero_point"]),
+                          np.abs(f32["slope"] - f64["slope"]))[both] / sc64[both])
+    chi_scale = np.maximum(np.abs(f64["chi2"]), f64["ndata"])
+    dchi_mixed = (np.abs(f32["chi2"] - f64["chi2"]) / chi_scale)[both]
+    del eng_64, eng_32
+
     # training (separate seed) on plain fits
-    eng_t = continuum.Dr16Gpu(train_raw.grid, num_iterations=iters)
+    eng_t = continuum.Dr16Gpu(train_raw.grid, num_iterations=iters, fit_mode=mixed)
     train = continuum.DeviceSpectra(train_raw, eng_t.device)
     (feats, targs, _), collect_s = timed_loop(lambda: learned.collect_training(eng_t, train))
     net = learned.WarmStartMLP(seed=0)
@@ -228,14 +245,16 @@ def continuum_leg(args, cpu_seconds):
     del feats, targs, train
 
     # learned leg (config 4) on the same evaluation forests
-    eng_w = continuum.Dr16Gpu(eval_raw.grid, num_iterations=iters)
+    eng_w = continuum.Dr16Gpu(eval_raw.grid, num_iterations=iters, fit_mode=mixed)
     (warm_fit, stats), warm_s = timed_loop(lambda: learned.run_warm(eng_w, spectra, net))
     warm = continuum.fit_results_to_host(warm_fit)
     ok = (plain["status"] == 0) & (warm["status"] == 0)
     scale = np.maximum(1.0, np.maximum(np.abs(plain["zero_point"]), np.abs(plain["slope"])))
     dab = np.maximum(np.abs(warm["zero_point"] - plain["zero_point"]),
                      np.abs(warm["slope"] - plain["slope"]))[ok] / scale[ok]
-    dchi = np.abs(warm["chi2"] - plain["chi2"])[ok] / np.abs(plain["chi2"][ok])
+    # chi2 sums terms of both signs: relative to max(|chi2|, ndata)
+    dchi = (np.abs(warm["chi2"] - plain["chi2"]) /
+            np.maximum(np.abs(plain["chi2"]), plain["ndata"]))[ok]
     nfits = eval_raw.num * iters
     # bytes per forest-fit: 40 n + 32 (n pixels; four FP64 inputs, continuum out)
     npix = float(eval_raw.pix_offset[-1])
@@ -243,7 +262,10 @@ def continuum_leg(args, cpu_seconds):
     pk, source = peaks()
     achieved = fit_bytes / (np.mean(fit_ms) / 1e3) / 1e9
     return {
-        "forests": eval_raw.num, "iterations": iters, "solver": "FP64 damped Newton, warp per forest",
+        "forests": eval_raw.num, "iterations": iters,
+        "solver": "damped Newton, warp per forest; FP32 per-pixel terms, FP64 2x2 solve",
+        "fp64_terms_fit_s": fp64_s, "mixed_vs_fp64_ab_max_rel": float(d_mixed.max()),
+        "mixed_vs_fp64_chi2_max_rel": float(dchi_mixed.max()),
         "plain_fits_per_s": nfits / plain_s, "learned_fits_per_s": nfits / warm_s,
         "learned_over_plain": plain_s / warm_s,
         "fallback_rate": float(np.mean([st["fallback"] for st in stats]) / eval_raw.num),

@@ -255,6 +255,18 @@ int pg_cont_fit_batch(pg_plan *plan, const pg_spectra *spectra, const pg_cont_mo
                 const double *start, int32_t max_iter, double tol, int32_t mode,
                 const pg_cont_fit *out, void *stream);
 
+/* pg_cont_fit_batch restricted to the forests forest_index[0..num_index)
+ * (device, int32; NULL with num_index = spectra->num: every forest). Results
+ * are written at each listed forest's position; the others are untouched.
+ * Used for the fallback fits of the learned warm start. In PG_FIT_MIXED the
+ * per-pixel terms are FP32, the iteration stops at a step below
+ * max(tol, 1e-6) * max(1, |a|, |b|) (the FP32 gradient leaves about 1e-8 of
+ * relative error), and the continuum is formed in FP32. */
+int pg_cont_fit_select(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
+                       const double *start, const int32_t *forest_index, int64_t num_index,
+                       int32_t max_iter, double tol, int32_t mode, const pg_cont_fit *out,
+                       void *stream);
+
 /* Accumulate the histograms of one Dr16 iteration from fitted continua
  * (forests with status != 0 are skipped, as bad_continuum_reason is). */
 int pg_cont_stacks_accumulate(pg_plan *plan, const pg_spectra *spectra,

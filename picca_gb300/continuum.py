@@ -81,11 +81,16 @@ def _bind():
     lib.pg_cont_fit_batch.argtypes = [ctypes.c_void_p, _P(SpectraC), _P(ContModelC),
                                       ctypes.c_void_p, ctypes.c_int32, ctypes.c_double,
                                       ctypes.c_int32, _P(ContFitC), ctypes.c_void_p]
+    lib.pg_cont_fit_select.argtypes = [ctypes.c_void_p, _P(SpectraC), _P(ContModelC),
+                                       ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                       ctypes.c_int32, ctypes.c_double, ctypes.c_int32,
+                                       _P(ContFitC), ctypes.c_void_p]
     lib.pg_cont_stacks_accumulate.argtypes = [ctypes.c_void_p, _P(SpectraC), _P(ContModelC),
                                               _P(ContFitC), _P(ContStacksC), ctypes.c_void_p]
     lib.pg_cont_deltas.argtypes = [ctypes.c_void_p, _P(SpectraC), _P(ContModelC), _P(ContFitC),
                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
-    for name in ("pg_cont_fit_batch", "pg_cont_stacks_accumulate", "pg_cont_deltas"):
+    for name in ("pg_cont_fit_batch", "pg_cont_fit_select", "pg_cont_stacks_accumulate",
+                 "pg_cont_deltas"):
         getattr(lib, name).restype = ctypes.c_int
     lib._cont_bound = True
     return lib
@@ -221,19 +226,22 @@ class Dr16Gpu:
         return ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
 
     # -- steps -------------------------------------------------------------
-    def fit(self, spectra, start=None, mode=None, max_iter=None):
-        """Continuum fit of every forest; returns a dict of device tensors."""
+    def fit(self, spectra, start=None, mode=None, max_iter=None, index=None, out=None):
+        """Continuum fit of every forest (or of the forests listed in the
+        int32 device tensor ``index``, written into an existing result dict
+        ``out``); returns a dict of device tensors."""
         lib = _bind()
         dev = self.device
         n = spectra.num
-        out = {"zero_point": torch.empty(n, dtype=torch.float64, device=dev),
-               "slope": torch.empty(n, dtype=torch.float64, device=dev),
-               "chi2": torch.empty(n, dtype=torch.float64, device=dev),
-               "ndata": torch.empty(n, dtype=torch.int32, device=dev),
-               "status": torch.empty(n, dtype=torch.int32, device=dev),
-               "iterations": torch.empty(n, dtype=torch.int32, device=dev),
-               "continuum": torch.empty(max(spectra.num_pixels, 1), dtype=torch.float64,
-                                        device=dev)}
+        if out is None:
+            out = {"zero_point": torch.empty(n, dtype=torch.float64, device=dev),
+                   "slope": torch.empty(n, dtype=torch.float64, device=dev),
+                   "chi2": torch.empty(n, dtype=torch.float64, device=dev),
+                   "ndata": torch.empty(n, dtype=torch.int32, device=dev),
+                   "status": torch.empty(n, dtype=torch.int32, device=dev),
+                   "iterations": torch.empty(n, dtype=torch.int32, device=dev),
+                   "continuum": torch.empty(max(spectra.num_pixels, 1), dtype=torch.float64,
+                                            device=dev)}
         fit_c = ContFitC(*[out[k].data_ptr() for k in ("zero_point", "slope", "chi2", "ndata",
                                                         "status", "iterations", "continuum")])
         model, keep = self._model()
@@ -241,13 +249,17 @@ class Dr16Gpu:
         if start is not None:
             start = torch.as_tensor(start, dtype=torch.float64, device=dev).contiguous()
             start_ptr = start.data_ptr()
+        if index is not None:
+            index = torch.as_tensor(index, dtype=torch.int32, device=dev).contiguous()
         with torch.cuda.device(dev):
-            check(lib.pg_cont_fit_batch(
+            check(lib.pg_cont_fit_select(
                 self.plan.handle, ctypes.byref(spectra.c), ctypes.byref(model), start_ptr,
+                None if index is None else index.data_ptr(),
+                n if index is None else int(index.numel()),
                 int(max_iter or self.max_iter), float(self.tol),
                 int(self.fit_mode if mode is None else mode), ctypes.byref(fit_c), self._stream()),
                 "continuum fit")
-        out["_keep"] = (keep, start, fit_c)
+        out["_keep"] = (keep, start, fit_c, index)
         return out
 
     def _stacks(self, spectra, fit, mean_cont=True, var_stats=True, delta_stack=True):
@@ -360,9 +372,11 @@ class Dr16Gpu:
         self.stack_y = stack[w]
         self.stack_weight = weight[w]
 
-    def run(self, spectra, start=None, mode=None):
+    def run(self, spectra, start=None, mode=None, on_iteration=None):
         """The Dr16 outer loop. ``start`` optionally warm-starts every
-        iteration's fit (e.g. with learned (a, b)). Returns the last fit."""
+        iteration's fit (e.g. with learned (a, b)); ``on_iteration(iteration,
+        fit)`` is called after each iteration's updates (picca saves its
+        iteration files there). Returns the last fit."""
         fit = None
         for iteration in range(self.num_iterations):
             fit = self.fit(spectra, start=start, mode=mode)
@@ -377,6 +391,8 @@ class Dr16Gpu:
             self.history.append({"iteration": iteration,
                                  "iterations_mean": float(fit["iterations"].float().mean()),
                                  "accepted": int((fit["status"] == 0).sum())})
+            if on_iteration is not None:
+                on_iteration(iteration, fit)
         return fit
 
     def deltas(self, spectra, fit):

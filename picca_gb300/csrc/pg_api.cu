@@ -278,6 +278,15 @@ static int validate_fit(const pg_cont_fit *f, bool need_continuum) {
 int pg_cont_fit_batch(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
                 const double *start, int32_t max_iter, double tol, int32_t mode,
                 const pg_cont_fit *out, void *stream) {
+    if (!spectra) return PG_ERR_INVALID_ARGUMENT;
+    return pg_cont_fit_select(plan, spectra, model, start, nullptr, spectra->num, max_iter, tol,
+                              mode, out, stream);
+}
+
+int pg_cont_fit_select(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
+                       const double *start, const int32_t *forest_index, int64_t num_index,
+                       int32_t max_iter, double tol, int32_t mode, const pg_cont_fit *out,
+                       void *stream) {
     if (!plan) return PG_ERR_INVALID_ARGUMENT;
     int rc;
     if ((rc = validate_spectra(spectra)) || (rc = validate_model(model)) ||
@@ -289,8 +298,11 @@ int pg_cont_fit_batch(pg_plan *plan, const pg_spectra *spectra, const pg_cont_mo
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     plan->last_stream = st;
     if ((rc = reset_scratch(plan, st))) return rc;
-    return launch_cont_fit(*spectra, *model, start, max_iter, tol, mode, *out, scratch_of(plan),
-                           plan->num_sms, st);
+    if (num_index < 0 || (forest_index == nullptr && num_index != spectra->num) ||
+        num_index > INT32_MAX)
+        return PG_ERR_INVALID_ARGUMENT;
+    return launch_cont_fit(*spectra, *model, start, forest_index, num_index, max_iter, tol, mode,
+                           *out, scratch_of(plan), plan->num_sms, st);
 }
 
 int pg_cont_stacks_accumulate(pg_plan *plan, const pg_spectra *spectra,

@@ -107,9 +107,9 @@ struct PixelTerms {
 // chi2 / 2 and its derivatives of one lane's pixels (accumulated in T,
 // returned in FP64); constant weights use q = 1, vl = fi = 0 with no log.
 // U is the arithmetic type of the per-pixel terms (T or FP64).
-template <typename U, typename T>
+template <typename U, typename T, typename O>
 __device__ __forceinline__ void lane_terms(const PixelTerms<T> &px, double a, double b,
-                                           bool const_w, double s[6]) {
+                                           bool const_w, O s[6]) {
     U val = 0, ga = 0, gb = 0, haa = 0, hab = 0, hbb = 0;
     const U ua = (U)a, ub = (U)b;
 #pragma unroll
@@ -136,14 +136,14 @@ __device__ __forceinline__ void lane_terms(const PixelTerms<T> &px, double a, do
         hab += h * ja * jb;
         hbb += h * jb * jb;
     }
-    s[0] = (double)val; s[1] = (double)ga; s[2] = (double)gb;
-    s[3] = (double)haa; s[4] = (double)hab; s[5] = (double)hbb;
+    s[0] = (O)val; s[1] = (O)ga; s[2] = (O)gb;
+    s[3] = (O)haa; s[4] = (O)hab; s[5] = (O)hbb;
 }
 
 template <typename U, typename T>
 __device__ __forceinline__ void eval_all(const PixelTerms<T> &px, double a, double b, bool const_w,
                                          double s[6]) {
-    lane_terms<U>(px, a, b, const_w, s);
+    lane_terms<U, T, double>(px, a, b, const_w, s);
 #pragma unroll
     for (int k = 0; k < 6; ++k) s[k] = warp_sum(s[k]);
 }
@@ -151,13 +151,14 @@ __device__ __forceinline__ void eval_all(const PixelTerms<T> &px, double a, doub
 template <typename T>
 __global__ void __launch_bounds__(kContBlock) cont_fit_kernel(
     const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
-    const double *__restrict__ start, int max_iter, double tol,
-    const __grid_constant__ pg_cont_fit out, Scratch *scratch) {
+    const double *__restrict__ start, const int32_t *__restrict__ index, int64_t count,
+    int max_iter, double tol, const __grid_constant__ pg_cont_fit out, Scratch *scratch) {
     const int lane = threadIdx.x & 31;
     const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const bool const_w = m.use_constant_weight != 0;
-    for (int64_t f = warp_global; f < sp.num; f += nwarps) {
+    for (int64_t w = warp_global; w < count; w += nwarps) {
+        const int64_t f = index ? (int64_t)index[w] : w;
         const int64_t off = sp.pix_offset[f];
         const int64_t n64 = sp.pix_offset[f + 1] - off;
         if (n64 > 32 * kContK || n64 <= 0) {
@@ -300,6 +301,302 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_kernel(
             out.zero_point[f] = status == 0 ? a : NAN;
             out.slope[f] = status == 0 ? b : NAN;
             out.chi2[f] = status == 0 ? fin[0] : NAN;
+            out.ndata[f] = nd;
+            out.status[f] = status;
+            out.iterations[f] = it;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Mixed-precision fit (PG_FIT_MIXED): FP32 per-pixel terms, FP32 lane and
+// warp sums, FP64 2x2 Newton solve. GB300 executes FP64 at 1/64 of the FP32
+// rate, so the per-pixel work avoids FP64 except for the three differences
+// whose operands are close (the rest-frame argument of the mean continuum,
+// its offset from the interpolation node, and the offset from the forest's
+// lower wavelength limit). The model tables are copied to shared memory in
+// FP32 (plus the FP64 nodes of the mean continuum and per-interval slopes
+// computed in FP64), so the interpolation searches use FP32 comparisons.
+// Newton steps larger than 1e-3 of max(1, |a|, |b|) are damped by an Armijo
+// line search on chi2; smaller steps, inside the region of quadratic
+// convergence, are taken in full, because there the change of chi2 is below
+// the resolution of FP32 sums. The iteration stops when the step is below
+// max(tol, 1e-6) * max(1, |a|, |b|): the error left is about the square of
+// the last step plus the FP32 rounding of the gradient (about 1e-8
+// relative). The reported chi2 sums the FP32 terms with compensation; the
+// continuum is (b x + a) mc in FP32, stored as FP64.
+// ---------------------------------------------------------------------------
+struct MixedTables {
+    const double *mcx_d;
+    const float *mcx_f, *mcy_f, *slope_f;
+    const float *brk_f, *coef_f;  // coef_f: eta, var_lss, fudge, each [4][m]
+    int nmc, m;
+};
+
+__host__ __device__ inline size_t mixed_smem_bytes(int nmc, int m) {
+    return (size_t)nmc * 8 + (size_t)nmc * 12 + (size_t)(m + 1) * 4 + (size_t)12 * m * 4 + 16;
+}
+
+__device__ MixedTables load_tables(const pg_cont_model &m, unsigned char *smem) {
+    MixedTables t;
+    const int nmc = m.num_mean_cont, mi = m.num_var_intervals;
+    double *mcx_d = reinterpret_cast<double *>(smem);
+    float *mcx_f = reinterpret_cast<float *>(mcx_d + nmc);
+    float *mcy_f = mcx_f + nmc;
+    float *slope_f = mcy_f + nmc;
+    float *brk_f = slope_f + nmc;
+    float *coef_f = brk_f + mi + 1;
+    for (int i = threadIdx.x; i < nmc; i += blockDim.x) {
+        const double x = m.mean_cont_x[i], y = m.mean_cont_y[i];
+        mcx_d[i] = x;
+        mcx_f[i] = (float)x;
+        mcy_f[i] = (float)y;
+        slope_f[i] = i + 1 < nmc ? (float)((m.mean_cont_y[i + 1] - y) / (m.mean_cont_x[i + 1] - x))
+                                 : 0.f;
+    }
+    if (!m.use_constant_weight) {
+        for (int i = threadIdx.x; i <= mi; i += blockDim.x) brk_f[i] = (float)m.var_breaks[i];
+        for (int i = threadIdx.x; i < 4 * mi; i += blockDim.x) {
+            coef_f[i] = (float)m.eta_coef[i];
+            coef_f[4 * mi + i] = (float)m.var_lss_coef[i];
+            coef_f[8 * mi + i] = (float)m.fudge_coef[i];
+        }
+    }
+    __syncthreads();
+    t.mcx_d = mcx_d; t.mcx_f = mcx_f; t.mcy_f = mcy_f; t.slope_f = slope_f;
+    t.brk_f = brk_f; t.coef_f = coef_f; t.nmc = nmc; t.m = mi;
+    return t;
+}
+
+// Linear interpolation with extrapolation (interp_linear) searched in FP32;
+// v - x_lo is formed in FP64. Next to a node the FP32 search may pick the
+// neighbouring interval, which changes the value by (slope difference) x
+// (FP32 rounding of v), far below the FP32 rounding of the result.
+__device__ __forceinline__ float interp_mc(const MixedTables &t, double v) {
+    const float vf = (float)v;
+    int lo = 0, hi = t.nmc;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (t.mcx_f[mid] < vf) lo = mid + 1;
+        else hi = mid;
+    }
+    const int idx = lo < 1 ? 1 : (lo > t.nmc - 1 ? t.nmc - 1 : lo);
+    const float dv = (float)(v - t.mcx_d[idx - 1]);
+    return t.slope_f[idx - 1] * dv + t.mcy_f[idx - 1];
+}
+
+__device__ __forceinline__ float ppoly_f(const float *brk, const float *coef, int m, float v) {
+    int lo = 0, hi = m + 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (brk[mid] <= v) lo = mid + 1;
+        else hi = mid;
+    }
+    int i = lo - 1;
+    i = i < 0 ? 0 : (i > m - 1 ? m - 1 : i);
+    const float dx = v - brk[i];
+    return ((coef[i] * dx + coef[m + i]) * dx + coef[2 * m + i]) * dx + coef[3 * m + i];
+}
+
+__device__ __forceinline__ float warp_sum_f(float v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    return v;
+}
+
+__device__ __forceinline__ void eval_all_f(const PixelTerms<float> &px, double a, double b,
+                                           bool const_w, double s[6]) {
+    float v[6];
+    lane_terms<float, float, float>(px, a, b, const_w, v);
+#pragma unroll
+    for (int k = 0; k < 6; ++k) s[k] = (double)warp_sum_f(v[k]);
+}
+
+__global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
+    const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
+    const double *__restrict__ start, const int32_t *__restrict__ index, int64_t count,
+    int max_iter, double tol, const __grid_constant__ pg_cont_fit out, Scratch *scratch) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const MixedTables tab = load_tables(m, smem);
+    const int lane = threadIdx.x & 31;
+    const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const bool const_w = m.use_constant_weight != 0;
+    const double eff_tol = tol > 1e-6 ? tol : 1e-6;
+    const int mi = tab.m;
+    for (int64_t w = warp_global; w < count; w += nwarps) {
+        const int64_t f = index ? (int64_t)index[w] : w;
+        const int64_t off = sp.pix_offset[f];
+        const int64_t n64 = sp.pix_offset[f + 1] - off;
+        if (n64 > 32 * kContK || n64 <= 0) {
+            if (lane == 0) {
+                if (n64 > 32 * kContK) report_error(scratch, PG_ERR_UNSUPPORTED, (int32_t)f);
+                out.zero_point[f] = NAN;
+                out.slope[f] = NAN;
+                out.chi2[f] = NAN;
+                out.ndata[f] = 0;
+                out.status[f] = 1;
+                out.iterations[f] = 0;
+            }
+            continue;
+        }
+        const int n = (int)n64;
+        const double zp1 = log10(1 + sp.z_qso[f]);
+        const double ll_min = m.log_lambda_rest_min + zp1;
+        const float inv_span = (float)(1.0 / (m.log_lambda_rest_max - m.log_lambda_rest_min));
+        PixelTerms<float> px;
+        px.valid = 0;
+        float sfi = 0.f, si = 0.f;
+        float xs[kContK];
+#pragma unroll
+        for (int k = 0; k < kContK; ++k) {
+            const int p = lane + 32 * k;
+            px.ja[k] = px.jb[k] = px.f[k] = px.q[k] = px.vl[k] = px.fi[k] = 0.f;
+            xs[k] = 0.f;
+            if (p < n) {
+                const double ll = sp.log_lambda[off + p];
+                const float fl = (float)sp.flux[off + p];
+                const float iv = (float)sp.ivar[off + p];
+                sfi += fl * iv;
+                si += iv;
+                if (iv > 0.f) {
+                    const float mc = interp_mc(tab, ll - zp1) * (float)sp.transmission_correction[off + p];
+                    const float x = (float)(ll - ll_min) * inv_span;
+                    xs[k] = x;
+                    px.ja[k] = mc;
+                    px.jb[k] = x * mc;
+                    px.f[k] = fl;
+                    if (const_w) {
+                        px.q[k] = 1.f;
+                    } else {
+                        const float llf = (float)ll;
+                        const float eta = ppoly_f(tab.brk_f, tab.coef_f, mi, llf);
+                        px.q[k] = eta / fmaxf(iv, 1.17549435e-38f);
+                        px.vl[k] = ppoly_f(tab.brk_f, tab.coef_f + 4 * mi, mi, llf);
+                        px.fi[k] = ppoly_f(tab.brk_f, tab.coef_f + 8 * mi, mi, llf) * iv;
+                    }
+                    px.valid |= 1u << k;
+                }
+            }
+        }
+        const double sfi_d = warp_sum((double)sfi), si_d = warp_sum((double)si);
+        const double a0 = sfi_d / si_d;
+        int nd = 0;
+        const float a0f = (float)a0;
+#pragma unroll
+        for (int k = 0; k < kContK; ++k) {
+            if ((px.valid >> k) & 1u) {
+                const float c = a0f * px.ja[k];
+                const float c2 = c * c;
+                const float d = px.q[k] + px.vl[k] * c2 + px.fi[k] * c2 * c2;
+                nd += (d > 0.f) ? 1 : 0;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) nd += __shfl_xor_sync(0xffffffffu, nd, o);
+        double a = a0, b = 0.;
+        if (start) {
+            a = start[2 * f];
+            b = m.order == 0 ? 0. : start[2 * f + 1];
+        }
+        double s[6];
+        eval_all_f(px, a, b, const_w, s);
+        int it = 0;
+        bool converged = false;
+        for (; it < max_iter; ++it) {
+            double da, db;
+            if (m.order == 0) {
+                da = s[3] > 0 ? -s[1] / s[3] : -s[1];
+                db = 0.;
+            } else {
+                const double det = s[3] * s[5] - s[4] * s[4];
+                if (det > 0 && s[3] > 0) {
+                    da = -(s[5] * s[1] - s[4] * s[2]) / det;
+                    db = -(s[3] * s[2] - s[4] * s[1]) / det;
+                } else {
+                    const double scale = fmax(fabs(s[3]), fabs(s[5]));
+                    da = -s[1] / (scale > 0 ? scale : 1.);
+                    db = -s[2] / (scale > 0 ? scale : 1.);
+                }
+                if (da * s[1] + db * s[2] >= 0) {
+                    const double scale = fmax(fabs(s[3]), fabs(s[5]));
+                    da = -s[1] / (scale > 0 ? scale : 1.);
+                    db = -s[2] / (scale > 0 ? scale : 1.);
+                }
+            }
+            const double ref = fmax(1., fmax(fabs(a), fabs(b)));
+            double trial[6];
+            double t = 1.;
+            if (fabs(da) < 1e-3 * ref && fabs(db) < 1e-3 * ref) {
+                eval_all_f(px, a + da, b + db, const_w, trial);
+            } else {
+                const double slope_dir = da * s[1] + db * s[2];
+                bool accepted = false;
+                for (int ls = 0; ls < 40; ++ls) {
+                    eval_all_f(px, a + t * da, b + t * db, const_w, trial);
+                    if (isfinite(trial[0]) && trial[0] <= s[0] + 1e-4 * t * slope_dir) {
+                        accepted = true;
+                        break;
+                    }
+                    t *= 0.5;
+                }
+                if (!accepted) break;
+            }
+            a += t * da;
+            b += t * db;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) s[k] = trial[k];
+            const double ref2 = fmax(1., fmax(fabs(a), fabs(b)));
+            if (fabs(t * da) < eff_tol * ref2 && fabs(t * db) < eff_tol * ref2) {
+                converged = true;
+                ++it;
+                break;
+            }
+        }
+        // chi2 at the solution: compensated FP32 lane sums, FP64 warp sum
+        float cs = 0.f, ce = 0.f;
+        const float af = (float)a, bf = (float)b;
+#pragma unroll
+        for (int k = 0; k < kContK; ++k) {
+            if (!((px.valid >> k) & 1u)) continue;
+            const float c = af * px.ja[k] + bf * px.jb[k];
+            const float c2 = c * c;
+            const float d = px.q[k] + px.vl[k] * c2 + px.fi[k] * c2 * c2;
+            const float r = px.f[k] - c;
+            const float term = r * r / d + (const_w ? 0.f : logf(d));
+            const float ns = cs + term;
+            const float bb = ns - cs;
+            ce += (cs - (ns - bb)) + (term - bb);
+            cs = ns;
+        }
+        const double chi2 = warp_sum((double)cs + (double)ce);
+        bool negative = false, all_zero = true;
+#pragma unroll
+        for (int k = 0; k < kContK; ++k) {
+            const int p = lane + 32 * k;
+            if (p >= n) continue;
+            float mc;
+            if ((px.valid >> k) & 1u) {
+                mc = px.ja[k];
+            } else {
+                const double ll = sp.log_lambda[off + p];
+                mc = interp_mc(tab, ll - zp1) * (float)sp.transmission_correction[off + p];
+                xs[k] = (float)(ll - ll_min) * inv_span;
+            }
+            const float c = (bf * xs[k] + af) * mc;
+            if (out.continuum) out.continuum[off + p] = (double)c;
+            negative |= c < 0.f;
+            all_zero &= c == 0.f;
+        }
+        negative = __any_sync(0xffffffffu, negative);
+        all_zero = __all_sync(0xffffffffu, all_zero);
+        if (lane == 0) {
+            int status = converged ? 0 : 1;
+            if (negative) status = 2;
+            if (all_zero) status = 3;
+            out.zero_point[f] = status == 0 ? a : NAN;
+            out.slope[f] = status == 0 ? b : NAN;
+            out.chi2[f] = status == 0 ? chi2 : NAN;
             out.ndata[f] = nd;
             out.status[f] = status;
             out.iterations[f] = it;
@@ -507,16 +804,22 @@ unsigned blocks_for(int64_t num, int num_sms) {
 }  // namespace
 
 int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *start,
-                    int max_iter, double tol, int mode, const pg_cont_fit &out, Scratch *scratch,
-                    int num_sms, cudaStream_t stream) {
-    if (sp.num <= 0) return PG_OK;
-    const unsigned blocks = blocks_for(sp.num, num_sms);
-    if (mode == PG_FIT_MIXED)
-        cont_fit_kernel<float><<<blocks, kContBlock, 0, stream>>>(sp, m, start, max_iter, tol,
-                                                                   out, scratch);
-    else
-        cont_fit_kernel<double><<<blocks, kContBlock, 0, stream>>>(sp, m, start, max_iter, tol,
-                                                                    out, scratch);
+                    const int32_t *index, int64_t count, int max_iter, double tol, int mode,
+                    const pg_cont_fit &out, Scratch *scratch, int num_sms, cudaStream_t stream) {
+    if (count <= 0) return PG_OK;
+    const unsigned blocks = blocks_for(count, num_sms);
+    if (mode == PG_FIT_MIXED) {
+        const size_t smem = mixed_smem_bytes(m.num_mean_cont, m.num_var_intervals);
+        if (smem > 200 * 1024) return PG_ERR_UNSUPPORTED;
+        cudaError_t err = cudaFuncSetAttribute(
+            cont_fit_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        if (err != cudaSuccess) return check_cuda(err);
+        cont_fit_mixed_kernel<<<blocks, kContBlock, smem, stream>>>(sp, m, start, index, count,
+                                                                    max_iter, tol, out, scratch);
+    } else {
+        cont_fit_kernel<double><<<blocks, kContBlock, 0, stream>>>(sp, m, start, index, count,
+                                                                    max_iter, tol, out, scratch);
+    }
     return check_cuda(cudaGetLastError());
 }
 

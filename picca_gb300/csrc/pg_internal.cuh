@@ -212,8 +212,8 @@ int launch_xcf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &fo
                        cudaStream_t stream);
 
 int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *start,
-                    int max_iter, double tol, int mode, const pg_cont_fit &out, Scratch *scratch,
-                    int num_sms, cudaStream_t stream);
+                    const int32_t *index, int64_t count, int max_iter, double tol, int mode,
+                    const pg_cont_fit &out, Scratch *scratch, int num_sms, cudaStream_t stream);
 int launch_cont_stacks(const pg_spectra &sp, const pg_cont_model &m, const pg_cont_fit &fit,
                        const pg_cont_stacks &st, Scratch *scratch, int num_sms,
                        cudaStream_t stream);

@@ -1,64 +1,77 @@
 // Precision-form pair accumulation: FP32 geometry with an FP64 bin-edge
 // guard, compensated FP32 shared-memory block sums, FP64 rows.
 //
-// Same persistent structure as the FP64 kernels (one work item = one forest
-// of set 1 with all its neighbours; warps take neighbour forests; lanes own
-// forest-2 pixels in registers and loop over the forest-1 pixels staged in
-// shared memory). For every pixel pair the kernel evaluates, in FP32,
-//     p = cp*((r1h - r2h) + (r1l - r2l))   (= r_par * np/(r_par_max - r_par_min))
-//     x_par = |p| - r_par_min*inv_p       (p itself for signed, cross correlations)
-//     x_tr  = st*d1 + st*d2               (= r_trans * nt/r_trans_max)
+// Persistent structure: one work item = one forest of set 1 with all its
+// neighbours; the forest-1 pixels are staged in shared memory, warps take
+// neighbour forests dynamically, and each lane holds P consecutive forest-2
+// pixels in registers while it loops over the forest-1 pixels. For every
+// pixel pair the kernel evaluates, in FP32,
+//     p   = cp*((r1h - r2h) + (r1l - r2l))   (= r_par * np/(r_par_max - r_par_min))
+//     x'  = |p| - (r_par_min*inv_p + 1/2)   (p itself for signed, cross correlations)
+//     xt' = st*d1 + (st*d2 - 1/2)           (= r_trans * nt/r_trans_max - 1/2)
 // with cp = cos(theta/2) * inv_p, st = sin(theta/2) * inv_t, and the comoving
 // distance carried as an FP32 pair r = rh + rl, so that r1 - r2 is exact to
-// ~1e-7 of itself (not of r). The bin index of py/picca/cf.py:372-376 is floor(x). It is taken with
-// one round-toward-minus-infinity add: y = x + (2^23 + 1) rounded down is
-// 2^23 + 1 + floor(x) for every x >= -1, so floor(x) = bits(y) - bits(2^23)
-// - 1 and x - (y - (2^23 + 1)) is the fractional part. A pair whose
-// fractional part is within a guard band g of 0 or 1 in either coordinate
-// (bin edges and the r_par / r_trans acceptance limits), or within a guard
+// ~1e-7 of itself (not of r). The bin index of py/picca/cf.py:372-376 is
+// floor(x) = round(x'), taken with one round-to-nearest add of 1.5 * 2^23:
+// y = x' + 1.5*2^23 is an integer for |x'| < 2^22, so round(x') is the bit
+// pattern of y minus that of 1.5*2^23 and f = x' - (y - 1.5*2^23), in
+// [-1/2, 1/2], is exact. A pair with |f| > 1/2 - g in either coordinate (a bin
+// edge or an acceptance limit within the guard band g), or within a guard
 // of the half-plate r_par cut or the z-pair cuts, is queued and re-decided
 // in FP64 with the reference's operation order (cf_pair_bin /
 // xcf_pair_bin), so every accepted pair, bin index and pair count equals
 // the FP64 reference. g exceeds the worst-case FP32 error (make_fast_const).
+// Forest-2 slots past the end of the forest or with zero weight carry
+// r = t = z = 1e30 (and cp = 1 for quasars), which lands far outside every
+// bin, edge and cut, so such a slot is neither accepted nor queued.
 //
-// Sums: per-CTA FP32 histograms of xi, w, p*w, x_tr*w, (z1+z2)*w and an
-// int32 count. xi (products of signed deltas, strongly cancelling) and w
-// (the normalisation) are accumulated error-free: the atomic add returns the
-// previous value, Knuth's TwoSum recovers the exact rounding error of the add
-// and a second histogram collects it. After each work item the partials are
-// added to the FP64 rows and mapped back to picca's units (r_par = p/inv_p,
-// r_trans = x_tr/inv_t, z = (z1+z2)/2).
+// Sums: per-CTA FP32 shared-memory histograms of xi, w, p*w, x_tr*w,
+// (z1+z2)*w and an int32 count. xi (products of signed deltas, strongly
+// cancelling) and w (the normalisation) are summed error-free: the atomic add
+// returns the previous value, Knuth's TwoSum recovers the exact rounding
+// error of the add and a second histogram collects it. Accepted pairs first
+// go to a per-warp ring, and the warp applies them 32 at a time, so the
+// eight atomic adds of a pair run with every lane active instead of in the
+// divergent branch of each pair. After each work item the histograms are
+// added to the FP64 rows and mapped back to picca's units (r_par =
+// p/inv_p, r_trans = x_tr/inv_t, z = (z1+z2)/2).
 #include "pg_internal.cuh"
 
 namespace pg {
 namespace {
 
-constexpr float kFloorMagic = 8388609.0f;  // 2^23 + 1, exact in FP32
-constexpr int kFloorBits = 0x4B000001;     // bits of 2^23 + 1
-constexpr int kQueue = 128;                // recheck entries per warp
-constexpr int kCfP = 4;                    // forest-2 pixels per lane per pass
-constexpr int kXcfP = 2;                   // quasars per lane per pass
-constexpr int kCfBlock = 384;              // cf threads per CTA (2 CTAs per SM)
+constexpr float kMagic = 12582912.0f;        // 1.5 * 2^23
+constexpr unsigned kMagicBits = 0x4B400000u;  // bits of 1.5 * 2^23
+constexpr float kFar = 1e30f;                 // r and t of an empty slot
+constexpr int kQueue = 128;                   // FP64 recheck entries per warp
+constexpr int kAccQ = 256;                    // accepted-pair ring per warp
+constexpr int kCfP = 4;                       // forest-2 pixels per lane
+constexpr int kXcfP = 2;                      // quasars per lane per pass
+constexpr int kCfBlock = 512;
+constexpr int kXcfBlock = 512;
 
 struct FastConst {
     double inv_p, inv_t;
-    float pmin;             // r_par_min * inv_p
-    float g_par, g_tr;      // guard bands (fraction of a bin)
-    float one_m_g_par, one_m_g_tr;
+    float pc;               // r_par_min * inv_p + 1/2
+    float low_clamp;        // -1/2 + 2 g_par (auto-correlation with r_par_min = 0)
+    float h_par, h_tr;      // 1/2 - g: |f| above this is near an edge
     float guard_v;          // half-plate cut guard (in units of p)
     float guard_z;          // guard on z1 + z2
     float zmin2, zmax2;     // 2 z_min, 2 z_max
     unsigned np, nt;
     int nbins;
     int hstride;            // histogram array stride (nbins rounded up to 4)
-    int lower_exact;        // auto-correlation with r_par_min = 0: x_par = |p| >= 0, so
+    int lower_exact;        // auto-correlation with r_par_min = 0: x = |p| >= 0, so
                             // the lower edge of bin 0 can never be crossed
 };
 
-enum {
-    H_XI = 0, H_XIL, H_WE, H_WEL, H_PW, H_TW, H_ZW, H_NB, H_COUNT
-};
+// ---------------------------------------------------------------------------
+// shared-memory histograms: H_COUNT float arrays of stride hstride
+// ---------------------------------------------------------------------------
+enum { H_XI = 0, H_XIL, H_WE, H_WEL, H_PW, H_TW, H_ZW, H_NB, H_COUNT };
 
+// *hi += v with the rounding error of the addition (Knuth's TwoSum of the
+// value returned by the atomic add and v) added to *lo.
 __device__ __forceinline__ void two_sum_add(float *hi, float *lo, float v) {
     const float old = atomicAdd(hi, v);
     const float s = old + v;
@@ -66,8 +79,8 @@ __device__ __forceinline__ void two_sum_add(float *hi, float *lo, float v) {
     atomicAdd(lo, (old - (s - bb)) + (v - bb));
 }
 
-__device__ __forceinline__ void acc_pair(float *h, int hs, int bin, float xi, float w, float pw,
-                                         float tw, float zw) {
+__device__ __forceinline__ void hist_add(float *h, int hs, unsigned bin, float xi, float w,
+                                         float pw, float tw, float zw) {
     float *hx = h + bin;
     two_sum_add(hx + H_XI * hs, hx + H_XIL * hs, xi);
     two_sum_add(hx + H_WE * hs, hx + H_WEL * hs, w);
@@ -75,21 +88,6 @@ __device__ __forceinline__ void acc_pair(float *h, int hs, int bin, float xi, fl
     atomicAdd(hx + H_TW * hs, tw);
     atomicAdd(hx + H_ZW * hs, zw);
     atomicAdd(reinterpret_cast<int *>(hx + H_NB * hs), 1);
-}
-
-// FP32 value of a weight that stays nonzero when the FP64 weight is nonzero
-// (a weight below the FP32 range still counts its pairs, as in FP64).
-__device__ __forceinline__ float weight32(double w) {
-    const float f = (float)w;
-    if (f == 0.f && w != 0.) return w > 0 ? 1.401298464e-45f : -1.401298464e-45f;
-    return f;
-}
-
-// floor(x) (as unsigned, x >= -1) and the fractional part x - floor(x).
-__device__ __forceinline__ unsigned floor_frac(float x, float &frac) {
-    const float y = __fadd_rd(x, kFloorMagic);
-    frac = x - (y - kFloorMagic);
-    return (unsigned)(__float_as_int(y) - kFloorBits);
 }
 
 __device__ __forceinline__ void flush_rows(float *h, const FastConst &fc, const pg_xi_rows &out,
@@ -112,8 +110,8 @@ __device__ __forceinline__ void flush_rows(float *h, const FastConst &fc, const 
     }
 }
 
-__device__ __forceinline__ void zero_all(float *h, int hs) {
-    for (int b = threadIdx.x; b < H_COUNT * hs; b += blockDim.x) h[b] = 0.f;
+__device__ __forceinline__ void zero_all(float *h, int n) {
+    for (int b = threadIdx.x; b < n; b += blockDim.x) h[b] = 0.f;
 }
 
 __device__ __forceinline__ int next_item(Scratch *scratch, int *slot) {
@@ -121,6 +119,41 @@ __device__ __forceinline__ int next_item(Scratch *scratch, int *slot) {
     if (threadIdx.x == 0) *slot = atomicAdd(&scratch->work_counter, 1);
     __syncthreads();
     return *slot;
+}
+
+// FP32 value of a weight that stays nonzero when the FP64 weight is nonzero
+// (a weight below the FP32 range still counts its pairs, as in FP64).
+__device__ __forceinline__ float weight32(double w) {
+    const float f = (float)w;
+    if (f == 0.f && w != 0.) return w > 0 ? 1.401298464e-45f : -1.401298464e-45f;
+    return f;
+}
+
+// round(x) (as unsigned; negative results wrap to large values) and the
+// remainder x - round(x) in [-1/2, 1/2].
+__device__ __forceinline__ unsigned round_rem(float x, float &rem) {
+    const float y = x + kMagic;
+    rem = x - (y - kMagic);
+    return __float_as_uint(y) - kMagicBits;
+}
+
+// Shared-memory layout of both kernels (offsets in bytes from the start).
+struct SmemLayout {
+    size_t cells, p1, p2, acc0, acc1, queue, total;
+};
+
+__host__ __device__ inline SmemLayout smem_layout(int nbins, int max_pix1, int nwarps,
+                                                  bool acc_queue) {
+    SmemLayout l;
+    const size_t mp = (size_t)((max_pix1 + 1) & ~1);
+    l.cells = 0;
+    l.p1 = l.cells + (size_t)((nbins + 3) & ~3) * H_COUNT * 4;
+    l.p2 = l.p1 + mp * 16;
+    l.acc0 = l.p2 + mp * 8;
+    l.acc1 = l.acc0 + (acc_queue ? (size_t)nwarps * kAccQ * 16 : 0);
+    l.queue = l.acc1 + (acc_queue ? (size_t)nwarps * kAccQ * 8 : 0);
+    l.total = l.queue + (size_t)nwarps * kQueue * 4;
+    return l;
 }
 
 // ---------------------------------------------------------------------------
@@ -132,7 +165,7 @@ struct CfPairCtx {
     bool shp;
 };
 
-// FP64 re-decision of queued (i, j) pairs, then FP32 accumulation.
+// FP64 re-decision of queued (i, j) pairs, then accumulation.
 __device__ __forceinline__ void cf_drain(const Binning &b, const FastConst *__restrict__ fcp,
                                       const pg_forest_set &s1, const pg_forest_set &s2,
                                       CfPairCtx ctx, const uint32_t *queue, int count, float *h,
@@ -140,7 +173,6 @@ __device__ __forceinline__ void cf_drain(const Binning &b, const FastConst *__re
     __syncwarp();
     const int lane = threadIdx.x & 31;
     const double inv_p = fcp->inv_p, inv_t = fcp->inv_t;
-    const int hs = fcp->hstride;
     for (int e = lane; e < count; e += 32) {
         const uint32_t entry = queue[e];
         const int64_t ia = ctx.a0 + (entry >> 16), jb = ctx.b0 + (entry & 0xFFFF);
@@ -160,14 +192,79 @@ __device__ __forceinline__ void cf_drain(const Binning &b, const FastConst *__re
         const float pv = (float)(r_par * inv_p);
         const float tv = (float)(r_trans * inv_t);
         const float zs = (float)z1 + (float)z2;
-        acc_pair(h, hs, (int)bin, dw12, w12, pv * w12, tv * w12, zs * w12);
+        hist_add(h, fcp->hstride, (unsigned)bin, dw12, w12, pv * w12, tv * w12, zs * w12);
     }
     __syncwarp();
 }
 
+// Applies n (<= 32) queued accepted pairs starting at ring position head.
+// Entry: {p, xt', w1 w2, dw1 dw2} and {z1 + z2, bin}.
+__device__ __forceinline__ void apply_accepted(const float4 *acc0, const float2 *acc1, int head,
+                                               int n, float *h, int hs) {
+    __syncwarp();
+    const int lane = threadIdx.x & 31;
+    if (lane < n) {
+        const int e = (head + lane) & (kAccQ - 1);
+        const float4 v = acc0[e];
+        const float2 u = acc1[e];
+        const unsigned bin = __float_as_uint(u.y);
+        const float w = v.z;
+        hist_add(h, hs, bin, v.w, w, v.x * w, (v.y + 0.5f) * w, u.x * w);
+    }
+    __syncwarp();
+}
+
+// Number of leading forest-1 pixels whose field (0: r, 1: dist_m) is below v
+// (UPPER: not above v), for pixels in increasing order of that field.
+template <int FIELD, bool UPPER>
+__device__ __forceinline__ int count_below(const float4 *p1, int n, float v) {
+    int lo = 0, hi = n;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        const float4 q = p1[mid];
+        const float x = FIELD == 0 ? q.x : q.z;
+        if (UPPER ? x <= v : x < v) lo = mid + 1;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// Forest-1 pixel range [i_lo, i_hi) that can pair with this warp's
+// forest-2 block, for forest-1 pixels in increasing r and dist_m. Pairs
+// outside it have x = p - pmin more than one bin outside [0, np] (r1 beyond
+// the block's r range +- the offsets) or x_tr' = st d1 + t above nt + 1
+// (d1 beyond (nt + 1 - min t) / st); their FP32 values are then far from
+// every bin and edge, so the FP32 test would reject them without queueing.
+__device__ __forceinline__ void window(const float4 *p1, int n1, const float *rh, const float *t,
+                                       float st, float lo_off, float hi_off, float t_end,
+                                       int &i_lo, int &i_hi) {
+    float rmin = kFar, rmax = -kFar, tmin = kFar;
+#pragma unroll
+    for (int p = 0; p < kCfP; ++p) {
+        if (rh[p] < 0.5f * kFar) {
+            rmin = fminf(rmin, rh[p]);
+            rmax = fmaxf(rmax, rh[p]);
+            tmin = fminf(tmin, t[p]);
+        }
+    }
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        rmin = fminf(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
+        rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
+        tmin = fminf(tmin, __shfl_xor_sync(0xffffffffu, tmin, o));
+    }
+    i_lo = count_below<0, false>(p1, n1, rmin + lo_off);
+    i_hi = count_below<0, true>(p1, n1, rmax + hi_off);
+    if (st > 0.f) {
+        const int it_end = count_below<1, false>(p1, n1, (t_end - tmin) / st);
+        if (it_end < i_hi) i_hi = it_end;
+    }
+}
+
 // EXTRA: half-plate veto, z-pair cuts or zerr cut may be active.
-template <bool AUTO, bool EXTRA>
-__global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
+// LOWX: auto-correlation with r_par_min = 0 (lower edge of bin 0 exempt).
+template <bool AUTO, bool EXTRA, bool LOWX>
+__global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
     const __grid_constant__ Binning b, const FastConst *__restrict__ fcp,
     const __grid_constant__ pg_forest_set s1, const __grid_constant__ pg_forest_set s2,
     const int64_t *__restrict__ nbr_offsets, const int32_t *__restrict__ nbr_index,
@@ -175,21 +272,27 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
     int64_t num_work, const __grid_constant__ pg_xi_rows out, Scratch *scratch, int max_pix1) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int item_slot;
+    __shared__ long long nbr_next;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
-    const int hs = fcp->hstride;
+    const int nwarps = blockDim.x >> 5;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int nbins = fcp->nbins;
     const double inv_p = fcp->inv_p, inv_t = fcp->inv_t;
-    const float pmin = fcp->pmin;
-    const float g_par = fcp->g_par, g_tr = fcp->g_tr;
-    const float omg_par = fcp->one_m_g_par, omg_tr = fcp->one_m_g_tr;
+    const float pc = fcp->pc, low_clamp = fcp->low_clamp;
+    const float pmin_f = fcp->pc - 0.5f;
+    const float h_par = fcp->h_par, h_tr = fcp->h_tr;
     const unsigned np = fcp->np, nt = fcp->nt;
-    const bool lower_exact = AUTO && fcp->lower_exact;
-    float *h = reinterpret_cast<float *>(smem);
-    float4 *p1 = reinterpret_cast<float4 *>(h + H_COUNT * hs);
-    float2 *p2 = reinterpret_cast<float2 *>(p1 + max_pix1);
-    uint32_t *queue = reinterpret_cast<uint32_t *>(p2 + max_pix1) + warp * kQueue;
-    __shared__ long long nbr_next;
-    zero_all(h, hs);
+    const float t_end = (float)nt + 1.f;  // x_tr' above this: rejected with a bin of margin
+    const int hs = fcp->hstride;
+    const SmemLayout L = smem_layout(nbins, max_pix1, nwarps, true);
+    float *h = reinterpret_cast<float *>(smem + L.cells);
+    float4 *p1 = reinterpret_cast<float4 *>(smem + L.p1);
+    float2 *p2 = reinterpret_cast<float2 *>(smem + L.p2);
+    float4 *acc0 = reinterpret_cast<float4 *>(smem + L.acc0) + warp * kAccQ;
+    float2 *acc1 = reinterpret_cast<float2 *>(smem + L.acc1) + warp * kAccQ;
+    uint32_t *queue = reinterpret_cast<uint32_t *>(smem + L.queue) + warp * kQueue;
+    zero_all(h, H_COUNT * hs);
     unsigned long long rechecks = 0, overflows = 0;
 
     for (;;) {
@@ -205,6 +308,7 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
         }
         const int n1 = (int)n1_64;
         // stage forest 1 in FP32: r as (hi, lo), dist_m, z; (w, delta*w)
+        bool ordered = true;
         for (int i = threadIdx.x; i < n1; i += blockDim.x) {
             const double w = s1.weights[a0 + i];
             const double r = s1.r_comov[a0 + i];
@@ -212,13 +316,20 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
             p1[i] = make_float4(rh, (float)(r - (double)rh), (float)s1.dist_m[a0 + i],
                                 (float)s1.z[a0 + i]);
             p2[i] = make_float2(weight32(w), (float)(s1.delta[a0 + i] * w));
+            if (i + 1 < n1)
+                ordered &= (float)s1.r_comov[a0 + i + 1] >= rh &&
+                           (float)s1.dist_m[a0 + i + 1] >= (float)s1.dist_m[a0 + i];
         }
+        // forest-1 pixels in increasing distance: each forest-2 block only
+        // visits the forest-1 pixels that can pair with it (see below)
+        const bool sorted1 = __syncthreads_and(ordered) != 0;
         const double x1 = s1.x_cart[f1], y1 = s1.y_cart[f1], zc1 = s1.z_cart[f1];
         const double ra1 = s1.ra[f1], dec1 = s1.dec[f1], cd1 = s1.cos_dec[f1];
         const double zq1 = s1.z_qso[f1];
         const int64_t k0 = nbr_offsets[f1], k1 = nbr_offsets[f1 + 1];
         if (threadIdx.x == 0) nbr_next = k0;
         __syncthreads();
+        int head = 0, tail = 0;  // accepted-pair ring of this warp (warp-uniform)
         for (;;) {
             // warps take neighbour forests dynamically (balances uneven lengths)
             int64_t k = 0;
@@ -254,51 +365,58 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
             }
             const float cp = (float)(ctx.c * inv_p);
             const float st = (float)(ctx.s * inv_t);
+            // r1 - r2 limits of pairs that can land in a bin, one bin of margin
+            // each side: x = p - pmin in [-1, np + 1], |p| for auto-correlations
+            const float lo_off = AUTO ? -(float)(np + 1u) / cp : (pmin_f - 1.f) / cp;
+            const float hi_off = AUTO ? (float)(np + 1u) / cp : (pmin_f + (float)np + 1.f) / cp;
             int qn = 0;
             for (int jb = 0; jb < n2; jb += 32 * kCfP) {
+                // lane owns pixels jb + kCfP*lane + p (consecutive pixels, so the
+                // lanes of a warp mostly fall in different r_par bins)
                 float rh[kCfP], rl[kCfP], t[kCfP], zv[kCfP], wv[kCfP], dv[kCfP];
-                unsigned vmask = 0;
+                bool any = false;
 #pragma unroll
                 for (int p = 0; p < kCfP; ++p) {
-                    const int j = jb + lane + 32 * p;
-                    rh[p] = 0.f; rl[p] = 0.f; t[p] = 0.f; zv[p] = 0.f; wv[p] = 0.f; dv[p] = 0.f;
+                    const int j = jb + kCfP * lane + p;
+                    rh[p] = kFar; rl[p] = 0.f; t[p] = kFar; zv[p] = kFar; wv[p] = 0.f; dv[p] = 0.f;
                     if (j < n2) {
                         const int64_t jj = ctx.b0 + j;
                         const double w2 = s2.weights[jj];
                         bool ok = w2 != 0;
                         if (EXTRA && zerr_pair && ok) ok = !zerr_veto(s2.z[jj], zq1, b.zerr_kms);
                         if (ok) {
-                            vmask |= 1u << p;
+                            any = true;
                             const double r = s2.r_comov[jj];
                             rh[p] = (float)r;
                             rl[p] = (float)(r - (double)rh[p]);
-                            t[p] = st * (float)s2.dist_m[jj];
+                            t[p] = st * (float)s2.dist_m[jj] - 0.5f;
                             zv[p] = (float)s2.z[jj];
                             wv[p] = weight32(w2);
                             dv[p] = (float)(s2.delta[jj] * w2);
                         }
                     }
                 }
-                if (__ballot_sync(0xffffffffu, vmask != 0) == 0) continue;
-                for (int i = 0; i < n1; ++i) {
+                if (!__any_sync(0xffffffffu, any)) continue;
+                int i_lo = 0, i_hi = n1;
+                if (sorted1) window(p1, n1, rh, t, st, lo_off, hi_off, t_end, i_lo, i_hi);
+                for (int i = i_lo; i < i_hi; ++i) {
                     const float2 qw = p2[i];
                     if (qw.x == 0.f) continue;  // zero-weight pixel (warp-uniform)
                     if (EXTRA && zerr_pair && zerr_veto(s1.z[a0 + i], zq2, b.zerr_kms)) continue;
                     const float4 q = p1[i];
-                    const float dw1 = qw.y;
                     const float ui = st * q.z;
                     unsigned near_mask = 0;
 #pragma unroll
                     for (int p = 0; p < kCfP; ++p) {
-                        const float diff = cp * ((q.x - rh[p]) + (q.y - rl[p]));
-                        const float v = fabsf(diff);
-                        const float pv = AUTO ? v : diff;
-                        const float tv = ui + t[p];
+                        const float pp = cp * ((q.x - rh[p]) + (q.y - rl[p]));
+                        const float v = fabsf(pp);
+                        const float pv = AUTO ? v : pp;
+                        const float xp = LOWX ? fmaxf(pv - pc, low_clamp) : pv - pc;
+                        const float xt = ui + t[p];
                         float fp, ft;
-                        const unsigned ip = floor_frac(pv - pmin, fp);
-                        const unsigned it = floor_frac(tv, ft);
-                        bool near = ((fp < g_par) & ((ip != 0u) | !lower_exact)) | (fp > omg_par) |
-                                    (ft < g_tr) | (ft > omg_tr);
+                        const unsigned ip = round_rem(xp, fp);
+                        const unsigned it = round_rem(xt, ft);
+                        bool near = (fabsf(fp) > h_par) | (fabsf(ft) > h_tr);
                         bool ok = (ip < np) & (it < nt);
                         const float zs = q.w + zv[p];
                         if (EXTRA) {
@@ -315,13 +433,20 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
                                 ok &= !(zs > fcp->zmax2);
                             }
                         }
-                        const bool valid = (vmask >> p) & 1u;
-                        near_mask |= (unsigned)(near & valid) << p;
-                        if (ok & valid & !near) {
-                            const float w12 = qw.x * wv[p];
-                            acc_pair(h, hs, (int)(ip * nt + it), dw1 * dv[p], w12, pv * w12,
-                                     tv * w12, zs * w12);
+                        near_mask |= (unsigned)near << p;
+                        const bool acc = ok & !near;
+                        const unsigned m = __ballot_sync(0xffffffffu, acc);
+                        if (acc) {
+                            const int pos = (tail + __popc(m & lt_mask)) & (kAccQ - 1);
+                            acc0[pos] = make_float4(pv, xt, qw.x * wv[p], qw.y * dv[p]);
+                            acc1[pos] = make_float2(zs, __uint_as_float(ip * nt + it));
                         }
+                        tail += __popc(m);
+                    }
+                    // at most 32 kCfP entries per pixel: the ring (kAccQ) never overflows
+                    while (tail - head >= 32) {
+                        apply_accepted(acc0, acc1, head, 32, h, hs);
+                        head += 32;
                     }
                     if (__any_sync(0xffffffffu, near_mask != 0)) {
                         // rare path: queue the pairs near an edge for FP64 re-decision
@@ -338,8 +463,8 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
                                 qn = 0;
                             }
                             if (near) {
-                                const int pos = qn + __popc(nmask & ((1u << lane) - 1u));
-                                queue[pos] = ((uint32_t)i << 16) | (uint32_t)(jb + lane + 32 * p);
+                                const int pos = qn + __popc(nmask & lt_mask);
+                                queue[pos] = ((uint32_t)i << 16) | (uint32_t)(jb + kCfP * lane + p);
                             }
                             qn += cnt;
                         }
@@ -351,6 +476,7 @@ __global__ void __launch_bounds__(kCfBlock, 2) cf_xi_fast_kernel(
                 rechecks += qn;
             }
         }
+        if (tail != head) apply_accepted(acc0, acc1, head, tail - head, h, hs);
         __syncthreads();
         flush_rows(h, *fcp, out, row);
         if (threadIdx.x == 0) atomicAdd(&scratch->work_items, 1ull);
@@ -379,7 +505,6 @@ __device__ __forceinline__ void xcf_drain(const Binning &b, const FastConst *__r
     __syncwarp();
     const int lane = threadIdx.x & 31;
     const double inv_p = fcp->inv_p, inv_t = fcp->inv_t;
-    const int hs = fcp->hstride;
     for (int e = lane; e < count; e += 32) {
         const uint32_t entry = queue[e];
         const int64_t ia = ctx.a0 + (entry >> 16);
@@ -405,13 +530,13 @@ __device__ __forceinline__ void xcf_drain(const Binning &b, const FastConst *__r
         const float pv = (float)(r_par * inv_p);
         const float tv = (float)(r_trans * inv_t);
         const float zs = (float)z1 + (float)zq;
-        acc_pair(h, hs, (int)bin, dw, w12, pv * w12, tv * w12, zs * w12);
+        hist_add(h, fcp->hstride, (unsigned)bin, dw, w12, pv * w12, tv * w12, zs * w12);
     }
     __syncwarp();
 }
 
 template <bool EXTRA>
-__global__ void __launch_bounds__(512, 1) xcf_xi_fast_kernel(
+__global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
     const __grid_constant__ Binning b, const FastConst *__restrict__ fcp,
     const __grid_constant__ pg_forest_set fs, const __grid_constant__ pg_forest_set objs,
     const int64_t *__restrict__ nbr_offsets, const int32_t *__restrict__ nbr_index,
@@ -422,17 +547,19 @@ __global__ void __launch_bounds__(512, 1) xcf_xi_fast_kernel(
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
-    const int hs = fcp->hstride;
+    const unsigned lt_mask = (1u << lane) - 1u;
+    const int nbins = fcp->nbins;
     const double inv_p = fcp->inv_p, inv_t = fcp->inv_t;
-    const float pmin = fcp->pmin;
-    const float g_par = fcp->g_par, g_tr = fcp->g_tr;
-    const float omg_par = fcp->one_m_g_par, omg_tr = fcp->one_m_g_tr;
+    const float pc = fcp->pc;
+    const float h_par = fcp->h_par, h_tr = fcp->h_tr;
     const unsigned np = fcp->np, nt = fcp->nt;
-    float *h = reinterpret_cast<float *>(smem);
-    float4 *p1 = reinterpret_cast<float4 *>(h + H_COUNT * hs);
-    float2 *p2 = reinterpret_cast<float2 *>(p1 + max_pix1);
-    uint32_t *queue = reinterpret_cast<uint32_t *>(p2 + max_pix1) + warp * kQueue;
-    zero_all(h, hs);
+    const int hs = fcp->hstride;
+    const SmemLayout L = smem_layout(nbins, max_pix1, nwarps, false);
+    float *h = reinterpret_cast<float *>(smem + L.cells);
+    float4 *p1 = reinterpret_cast<float4 *>(smem + L.p1);
+    float2 *p2 = reinterpret_cast<float2 *>(smem + L.p2);
+    uint32_t *queue = reinterpret_cast<uint32_t *>(smem + L.queue) + warp * kQueue;
+    zero_all(h, H_COUNT * hs);
     unsigned long long rechecks = 0, overflows = 0;
 
     for (;;) {
@@ -464,17 +591,17 @@ __global__ void __launch_bounds__(512, 1) xcf_xi_fast_kernel(
         const int nq = (int)nq_64;
         for (int kb = warp * 32 * kXcfP; kb < nq; kb += nwarps * 32 * kXcfP) {
             float cp[kXcfP], st[kXcfP], rh[kXcfP], rl[kXcfP], t[kXcfP], zv[kXcfP], wv[kXcfP];
-            unsigned vmask = 0;
+            bool any = false;
 #pragma unroll
             for (int p = 0; p < kXcfP; ++p) {
                 const int kk = kb + lane + 32 * p;
-                cp[p] = 0.f; st[p] = 0.f; rh[p] = 0.f; rl[p] = 0.f; t[p] = 0.f; zv[p] = 0.f;
+                cp[p] = 1.f; st[p] = 0.f; rh[p] = kFar; rl[p] = 0.f; t[p] = kFar; zv[p] = kFar;
                 wv[p] = 0.f;
                 if (kk < nq) {
                     const int64_t g = nbr_index[ctx.k0 + kk];
                     const double wq = objs.obj_weight[g];
                     if (wq != 0) {
-                        vmask |= 1u << p;
+                        any = true;
                         const double ang =
                             nbr_angle ? nbr_angle[ctx.k0 + kk]
                                       : angle_between(ctx.x1, ctx.y1, ctx.zc1, ctx.ra1, ctx.dec1,
@@ -485,28 +612,27 @@ __global__ void __launch_bounds__(512, 1) xcf_xi_fast_kernel(
                         const double r = objs.obj_r_comov[g];
                         rh[p] = (float)r;
                         rl[p] = (float)(r - (double)rh[p]);
-                        t[p] = st[p] * (float)objs.obj_dist_m[g];
+                        t[p] = st[p] * (float)objs.obj_dist_m[g] - 0.5f;
                         zv[p] = (float)objs.z_qso[g];
                         wv[p] = weight32(wq);
                     }
                 }
             }
-            if (__ballot_sync(0xffffffffu, vmask != 0) == 0) continue;
+            if (!__any_sync(0xffffffffu, any)) continue;
             int qn = 0;
             for (int i = 0; i < n1; ++i) {
                 const float2 qw = p2[i];
                 if (qw.x == 0.f) continue;
                 const float4 q = p1[i];
-                const float dw1 = qw.y;
                 unsigned near_mask = 0;
 #pragma unroll
                 for (int p = 0; p < kXcfP; ++p) {
                     const float pv = cp[p] * ((q.x - rh[p]) + (q.y - rl[p]));
-                    const float tv = __fmaf_rn(st[p], q.z, t[p]);
+                    const float xt = __fmaf_rn(st[p], q.z, t[p]);
                     float fp, ft;
-                    const unsigned ip = floor_frac(pv - pmin, fp);
-                    const unsigned it = floor_frac(tv, ft);
-                    bool near = (fp < g_par) | (fp > omg_par) | (ft < g_tr) | (ft > omg_tr);
+                    const unsigned ip = round_rem(pv - pc, fp);
+                    const unsigned it = round_rem(xt, ft);
+                    bool near = (fabsf(fp) > h_par) | (fabsf(ft) > h_tr);
                     bool ok = (ip < np) & (it < nt);
                     const float zs = q.w + zv[p];
                     if (EXTRA) {
@@ -519,12 +645,12 @@ __global__ void __launch_bounds__(512, 1) xcf_xi_fast_kernel(
                             ok &= !(zs > fcp->zmax2);
                         }
                     }
-                    const bool valid = (vmask >> p) & 1u;
-                    near_mask |= (unsigned)(near & valid) << p;
-                    if (ok & valid & !near) {
+                    near_mask |= (unsigned)near << p;
+                    if (ok & !near) {
                         const float w12 = qw.x * wv[p];
-                        acc_pair(h, hs, (int)(ip * nt + it), dw1 * wv[p], w12, pv * w12,
-                                 tv * w12, zs * w12);
+                        const unsigned bin = ip * nt + it;
+                        hist_add(h, hs, bin, qw.y * wv[p], w12, pv * w12, (xt + 0.5f) * w12,
+                                 zs * w12);
                     }
                 }
                 if (__any_sync(0xffffffffu, near_mask != 0)) {
@@ -542,7 +668,7 @@ __global__ void __launch_bounds__(512, 1) xcf_xi_fast_kernel(
                             qn = 0;
                         }
                         if (near) {
-                            const int pos = qn + __popc(nmask & ((1u << lane) - 1u));
+                            const int pos = qn + __popc(nmask & lt_mask);
                             queue[pos] = ((uint32_t)i << 16) | (uint32_t)(kb + lane + 32 * p);
                         }
                         qn += cnt;
@@ -567,29 +693,34 @@ __global__ void __launch_bounds__(512, 1) xcf_xi_fast_kernel(
 // Guard bands. Let u = 2^-24. r is carried as rh + rl with |r - rh - rl|
 // <= u^2 r (negligible), so r1 - r2 = (r1h - r2h) + (r1l - r2l) is formed
 // with two roundings of size u |r1 - r2| and u |r1l - r2l|; the product with
-// cp (itself rounded, relative u) and the subtraction of pmin add u |p| and
-// u |x|. Altogether |x_par(FP32) - x_par| <= 6 u (|x| + |pmin| + 1). For
-// x_tr = st d1 + st d2 the FP32 rounding of d1 and d2 (relative u), of the
-// two products, of st and of the sum give <= 5 u |x_tr|. Only pairs whose
-// exact x lies in [-1, n + 1] matter (the others are rejected either way),
-// so with a factor > 2 of margin
+// cp (itself rounded, relative u), the rounding of pc = pmin + 1/2 and the
+// subtraction add u |p|, u (|pmin| + 1/2) and u |x'|. Altogether the FP32 x'
+// is within 6 u (|x| + |pmin| + 1) of the exact x - 1/2. For x_tr the FP32
+// rounding of d1 and d2 (relative u), of st, of the two products, of the
+// shift by 1/2 and of the sum give <= 6 u (|x_tr| + 1). round(x') and the
+// remainder are exact (the magic-number add rounds to an integer and the
+// subtraction is exact). Only pairs whose exact x lies in [-1, n + 1] matter
+// (the others are rejected either way), so with a factor > 2 of margin
 //   g = 16 u (n + |pmin| + 2) + 1e-6.
 // The reference's own FP64 evaluation is within 1e-12 of the exact value,
-// far inside these bands.
+// far inside these bands. With r_par_min = 0 in an auto-correlation x = |p|
+// >= 0 and the lower edge of bin 0 cannot be crossed: x' is clamped from
+// below at -1/2 + 2g, which keeps pairs with |p| < 2g (same-wavelength pixels
+// give p = 0 exactly) in bin 0 without flagging them.
 FastConst make_fast_const(const Binning &b) {
     FastConst fc{};
     const double u = 1.0 / 16777216.0;
     fc.inv_p = (double)b.np / b.r_par_range;
     fc.inv_t = (double)b.nt / b.r_trans_max;
-    fc.pmin = (float)(b.r_par_min * fc.inv_p);
-    double g_par = 16 * u * (b.np + fabs(b.r_par_min * fc.inv_p) + 2) + 1e-6;
+    const double pmin = b.r_par_min * fc.inv_p;
+    fc.pc = (float)(pmin + 0.5);
+    double g_par = 16 * u * (b.np + fabs(pmin) + 2) + 1e-6;
     double g_tr = 16 * u * (b.nt + 2) + 1e-6;
     if (!(g_par < 0.05)) g_par = 0.05;  // absurd bin counts: almost everything is re-decided
     if (!(g_tr < 0.05)) g_tr = 0.05;
-    fc.g_par = (float)g_par;
-    fc.g_tr = (float)g_tr;
-    fc.one_m_g_par = (float)(1.0 - g_par);
-    fc.one_m_g_tr = (float)(1.0 - g_tr);
+    fc.h_par = (float)(0.5 - g_par);
+    fc.h_tr = (float)(0.5 - g_tr);
+    fc.low_clamp = (float)(-0.5 + 2 * g_par);
     fc.guard_v = (float)g_par;
     fc.guard_z = 1e-5f;  // z1 + z2 < 20: FP32 error below 5e-6
     fc.zmin2 = (float)(2 * b.z_min);
@@ -604,10 +735,6 @@ FastConst make_fast_const(const Binning &b) {
 
 // Writes the constants into the plan's device buffer in stream order.
 __global__ void store_const_kernel(FastConst value, FastConst *dst) { *dst = value; }
-
-size_t fast_smem_bytes(int hstride, int max_pix1, int nwarps) {
-    return (size_t)hstride * H_COUNT * 4 + (size_t)max_pix1 * 24 + (size_t)nwarps * kQueue * 4;
-}
 
 template <typename K>
 int persistent_grid(K kernel, int block, size_t smem, int num_sms, int64_t num_work, int *grid) {
@@ -641,26 +768,34 @@ int launch_cf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &s1,
                       cudaStream_t stream) {
     if (num_work <= 0) return PG_OK;
     FastConst *fc = static_cast<FastConst *>(fast_const);
-    const int block = kCfBlock;
     const int max_pix1 = s1.max_pixels;
-    const size_t smem = fast_smem_bytes((b.nbins + 3) & ~3, max_pix1, block / 32);
+    // as many warps (up to kCfBlock / 32) as the per-warp queues leave room for
+    int nwarps = kCfBlock / 32;
+    while (nwarps > 1 && smem_layout(b.nbins, max_pix1, nwarps, true).total > 227 * 1024)
+        --nwarps;
+    const int block = nwarps * 32;
+    const size_t smem = smem_layout(b.nbins, max_pix1, nwarps, true).total;
     if (smem > 227 * 1024) return PG_ERR_UNSUPPORTED;
     (void)ang_max;
     int rc = prepare_fast(b, fc, stream);
     if (rc) return rc;
     const bool extra = b.remove_shp || b.zmin_on || b.zmax_on || b.zerr_on;
     const bool autoc = !b.x_correlation;
+    const bool lowx = autoc && b.r_par_min == 0.0;
     int grid = 0;
-#define PG_LAUNCH_CF(A, E)                                                                     \
-    rc = persistent_grid(cf_xi_fast_kernel<A, E>, block, smem, num_sms, num_work, &grid);      \
+#define PG_LAUNCH_CF(A, E, L)                                                                  \
+    rc = persistent_grid(cf_xi_fast_kernel<A, E, L>, block, smem, num_sms, num_work, &grid);   \
     if (rc) return rc;                                                                         \
-    cf_xi_fast_kernel<A, E><<<grid, block, smem, stream>>>(b, fc, s1, s2, nbr_offsets,         \
-                                                           nbr_index, nbr_angle, work_order,   \
-                                                           num_work, out, scratch, max_pix1);
-    if (autoc && !extra) { PG_LAUNCH_CF(true, false) }
-    else if (autoc && extra) { PG_LAUNCH_CF(true, true) }
-    else if (!autoc && !extra) { PG_LAUNCH_CF(false, false) }
-    else { PG_LAUNCH_CF(false, true) }
+    cf_xi_fast_kernel<A, E, L><<<grid, block, smem, stream>>>(b, fc, s1, s2, nbr_offsets,      \
+                                                              nbr_index, nbr_angle,            \
+                                                              work_order, num_work, out,       \
+                                                              scratch, max_pix1);
+    if (autoc && lowx && !extra) { PG_LAUNCH_CF(true, false, true) }
+    else if (autoc && lowx && extra) { PG_LAUNCH_CF(true, true, true) }
+    else if (autoc && !extra) { PG_LAUNCH_CF(true, false, false) }
+    else if (autoc && extra) { PG_LAUNCH_CF(true, true, false) }
+    else if (!extra) { PG_LAUNCH_CF(false, false, false) }
+    else { PG_LAUNCH_CF(false, true, false) }
 #undef PG_LAUNCH_CF
     return check_cuda(cudaGetLastError());
 }
@@ -673,9 +808,9 @@ int launch_xcf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &fo
                        cudaStream_t stream) {
     if (num_work <= 0) return PG_OK;
     FastConst *fc = static_cast<FastConst *>(fast_const);
-    const int block = 512;
+    const int block = kXcfBlock;
     const int max_pix1 = forests.max_pixels;
-    const size_t smem = fast_smem_bytes((b.nbins + 3) & ~3, max_pix1, block / 32);
+    const size_t smem = smem_layout(b.nbins, max_pix1, block / 32, false).total;
     if (smem > 227 * 1024) return PG_ERR_UNSUPPORTED;
     (void)ang_max;
     int rc = prepare_fast(b, fc, stream);

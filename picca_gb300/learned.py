@@ -227,16 +227,12 @@ def warm_fit(engine, spectra, mlp, warm_max_iter=8, mode=None):
     start = predict_start(mlp, feat, a0)
     fit = engine.fit(spectra, start=start, mode=mode, max_iter=warm_max_iter)
     fallback = fit["status"] != 0
-    nfall = int(fallback.sum().item())
-    if nfall:
-        plain = engine.fit(spectra, mode=mode)
-        # merge in place: the fit's C struct keeps pointing at these tensors
-        for key in ("zero_point", "slope", "chi2", "ndata", "status", "iterations"):
-            fit[key][fallback] = plain[key][fallback]
-        pix = torch.repeat_interleave(fallback, torch.diff(spectra.tensors["pix_offset"]))
-        cont = fit["continuum"][: spectra.num_pixels]
-        cont[pix] = plain["continuum"][: spectra.num_pixels][pix]
-        fit["plain_iterations"] = plain["iterations"]
+    index = torch.nonzero(fallback).flatten().to(torch.int32)
+    if index.numel():
+        # plain fits of the fallback forests only, written in place
+        keep_fit = fit["_keep"]
+        engine.fit(spectra, mode=mode, index=index, out=fit)
+        fit["_keep"] = keep_fit
     del keep
     return fit, start, fallback
 

@@ -2,9 +2,10 @@
 
 Tolerances: the GPU and the oracle minimise the same chi2 to the same
 optimum (|step| < 1e-10 relative); FP64 mode: (a, b) within 1e-7 relative,
-chi2 within 1e-10 relative; mixed mode (FP32 per-pixel terms, FP64 sums and
-solve; the FP32 gradient terms limit the position of the optimum): (a, b)
-within 1e-3, chi2 within 1e-6. chi2 = sum (f - C)^2 / D + sum log D is a sum
+chi2 within 1e-10 relative; mixed mode (FP32 per-pixel terms and sums, FP64
+2x2 solve; the FP32 rounding of the gradient and of the model leaves about
+1e-7 on the optimum): (a, b) within 2e-6, chi2 within 1e-6, the FP32
+continuum within 2e-6 relative. chi2 = sum (f - C)^2 / D + sum log D is a sum
 of terms of either sign that can cancel, so its tolerance is relative to
 max(|chi2|, ndata), the scale of the sum of |terms| (each (f - C)^2 / D is
 about one). Histogram sums of positive terms agree to 1e-8 relative (only
@@ -47,7 +48,7 @@ def test_fit_matches_oracle(cuda, raw, mode):
     res = continuum.fit_results_to_host(gpu.fit(spectra))
     orc = oc.Dr16Oracle(raw.grid)
     conts, params = orc.fit_all(raw)
-    tol_ab, tol_chi2 = (1e-7, 1e-10) if mode == "fp64" else (1e-3, 1e-6)
+    tol_ab, tol_chi2 = (1e-7, 1e-10) if mode == "fp64" else (2e-6, 1e-6)
     for k in range(raw.num):
         (a, b, chi2, ndata), reason = params[k]
         status = res["status"][k]
@@ -103,3 +104,26 @@ def test_dr16_loop_matches_oracle(cuda, raw):
     assert np.array_equal(weights.cpu().numpy() > 0, w)
     assert np.allclose(weights.cpu().numpy(), ref_weights, rtol=1e-6)
     assert np.allclose(delta.cpu().numpy()[w], ref_delta[w], rtol=0, atol=1e-6)
+
+
+def test_fit_select_matches_full_fit(cuda, raw):
+    """pg_cont_fit_select fits only the listed forests, writes them in
+    place, and gives the results of the full fit."""
+    import torch
+    from picca_gb300 import continuum
+    gpu = continuum.Dr16Gpu(raw.grid, num_iterations=1, fit_mode=continuum.FIT_MIXED)
+    spectra = continuum.DeviceSpectra(raw, gpu.device)
+    full = continuum.fit_results_to_host(gpu.fit(spectra))
+    out = gpu.fit(spectra)
+    for key in ("zero_point", "slope", "chi2"):
+        out[key].fill_(-7.0)
+    index = torch.arange(1, raw.num, 3, dtype=torch.int32, device=gpu.device)
+    gpu.fit(spectra, index=index, out=out)
+    got = continuum.fit_results_to_host(out)
+    sel = np.zeros(raw.num, bool)
+    sel[index.cpu().numpy()] = True
+    ok = sel & (full["status"] == 0)
+    for key in ("zero_point", "slope", "chi2"):
+        assert np.array_equal(got[key][ok], full[key][ok]), key
+        assert np.all(got[key][~sel] == -7.0), key
+    assert np.array_equal(got["status"][sel], full["status"][sel])
