@@ -55,6 +55,8 @@ def parse():
     p.add_argument("--continuum-train", type=int, default=200_000,
                    help="raw forests (separate seed) the warm-start network is trained on")
     p.add_argument("--continuum-iterations", type=int, default=5)
+    p.add_argument("--continuum-correlation", type=int, default=50_000,
+                   help="forests whose plain- and learned-fit deltas are correlated (0 skips)")
     return p.parse_args()
 
 
@@ -255,6 +257,31 @@ def continuum_leg(args, cpu_seconds):
     # chi2 sums terms of both signs: relative to max(|chi2|, ndata)
     dchi = (np.abs(warm["chi2"] - plain["chi2"]) /
             np.maximum(np.abs(plain["chi2"]), plain["ndata"]))[ok]
+    # config 4 end to end: the deltas of both fits feed the auto-correlation
+    # (50k forests of a contiguous stretch of the survey band)
+    e2e_corr = None
+    if args.continuum_correlation > 0:
+        from picca_gb300 import pairs, pipeline
+        from picca_gb300.synthetic import correlation_ang_max
+        sel = np.argsort(eval_raw.ra, kind="stable")[:min(args.continuum_correlation,
+                                                          eval_raw.num)]
+        sel.sort()
+        xis = []
+        for eng, fit in ((eng_p, plain_fit), (eng_w, warm_fit)):
+            delta, weights = eng.deltas(spectra, fit)
+            fs = pipeline.forests_from_continuum(eval_raw, delta.cpu().numpy(),
+                                                 weights.cpu().numpy(), select=sel)
+            ang_max = correlation_ang_max(200.0, float(fs.z.min()))
+            params = pairs.make_params(0.0, 200.0, 200.0, 50, 50, ang_max)
+            res = pairs.correlate(fs, None, params, mode=pairs.MODE_FP32_GUARD)
+            we, xi = res["raw"][0].sum(axis=0), res["raw"][1].sum(axis=0)
+            xis.append(np.where(we > 0, xi / np.where(we > 0, we, 1.0), 0.0))
+        scale = np.max(np.abs(xis[0]))
+        e2e_corr = {"forests": int(sel.size), "bins": int(xis[0].size),
+                    "xi_max_abs_diff_over_max_xi": float(np.max(np.abs(xis[1] - xis[0])) / scale),
+                    "xi_rms_diff_over_rms_xi": float(np.sqrt(np.mean((xis[1] - xis[0])**2)) /
+                                                     np.sqrt(np.mean(xis[0]**2)))}
+
     nfits = eval_raw.num * iters
     # bytes per forest-fit: 40 n + 32 (n pixels; four FP64 inputs, continuum out)
     npix = float(eval_raw.pix_offset[-1])
@@ -265,6 +292,7 @@ def continuum_leg(args, cpu_seconds):
         "forests": eval_raw.num, "iterations": iters,
         "solver": "damped Newton, warp per forest; FP32 per-pixel terms, FP64 2x2 solve",
         "fp64_terms_fit_s": fp64_s, "mixed_vs_fp64_ab_max_rel": float(d_mixed.max()),
+        "fp64_finish_fraction": float(np.mean(eng_p.refined) / eval_raw.num),
         "mixed_vs_fp64_chi2_max_rel": float(dchi_mixed.max()),
         "plain_fits_per_s": nfits / plain_s, "learned_fits_per_s": nfits / warm_s,
         "learned_over_plain": plain_s / warm_s,
@@ -278,6 +306,7 @@ def continuum_leg(args, cpu_seconds):
         "fit_roofline": {"bound": "hbm", "achieved": achieved, "peak": pk.get("hbm_gbs"),
                          "unit": "GB/s", "frac": achieved / pk.get("hbm_gbs", 6800.0),
                          "bytes_per_launch": fit_bytes, "peak_source": source},
+        "deltas_to_xi_plain_vs_learned": e2e_corr,
         "training": {"forests": args.continuum_train, "samples": num_samples, "epochs": len(hist),
                      "collect_s": collect_s, "train_s": train_s, "loss_first": hist[0],
                      "loss_last": hist[-1]},

@@ -218,7 +218,8 @@ typedef struct pg_cont_model {
 /* Per-forest fit results (device pointers, [num]); continuum is per pixel
  * ([num_pixels], may be NULL). status: 0 ok, 1 not converged, 2 negative
  * continuum, 3 zero continuum (the bad_continuum_reason values of
- * compute_continuum). */
+ * compute_continuum), 4 mixed-precision fit to be finished in FP64 (see
+ * pg_cont_fit_select). */
 typedef struct pg_cont_fit {
     double *zero_point, *slope, *chi2;
     int32_t *ndata, *status, *iterations;
@@ -260,8 +261,11 @@ int pg_cont_fit_batch(pg_plan *plan, const pg_spectra *spectra, const pg_cont_mo
  * are written at each listed forest's position; the others are untouched.
  * Used for the fallback fits of the learned warm start. In PG_FIT_MIXED the
  * per-pixel terms are FP32, the iteration stops at a step below
- * max(tol, 1e-6) * max(1, |a|, |b|) (the FP32 gradient leaves about 1e-8 of
- * relative error), and the continuum is formed in FP32. */
+ * max(tol, 1e-6) * max(1, |a|, |b|), and the continuum is formed in FP32.
+ * A converged mixed fit whose optimum the FP32 rounding of the gradient is
+ * estimated to move by more than 5e-7 * max(1, |a|, |b|) (a forest whose
+ * pixels barely separate a from b) gets status 4 with its (a, b): finish it
+ * with PG_FIT_FP64 on those forests, starting from that (a, b). */
 int pg_cont_fit_select(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
                        const double *start, const int32_t *forest_index, int64_t num_index,
                        int32_t max_iter, double tol, int32_t mode, const pg_cont_fit *out,

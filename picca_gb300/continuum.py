@@ -34,6 +34,7 @@ FIT_FP64 = 0
 FIT_MIXED = 1
 STATUS_REASONS = {0: None, 1: "minuit didn't converge", 2: "negative continuum",
                   3: "zero continuum"}
+STATUS_REFINE = 4  # mixed-precision fit to be finished in FP64 (never left in results)
 
 _P = ctypes.POINTER
 
@@ -184,6 +185,7 @@ class Dr16Gpu:
         self.stack_y = None
         self.stack_weight = None
         self.history = []
+        self.refined = []  # forests finished in FP64 per mixed fit
 
     # -- model -------------------------------------------------------------
     def _model(self, with_stack=False):
@@ -251,14 +253,27 @@ class Dr16Gpu:
             start_ptr = start.data_ptr()
         if index is not None:
             index = torch.as_tensor(index, dtype=torch.int32, device=dev).contiguous()
+        mode = int(self.fit_mode if mode is None else mode)
         with torch.cuda.device(dev):
             check(lib.pg_cont_fit_select(
                 self.plan.handle, ctypes.byref(spectra.c), ctypes.byref(model), start_ptr,
                 None if index is None else index.data_ptr(),
                 n if index is None else int(index.numel()),
-                int(max_iter or self.max_iter), float(self.tol),
-                int(self.fit_mode if mode is None else mode), ctypes.byref(fit_c), self._stream()),
-                "continuum fit")
+                int(max_iter or self.max_iter), float(self.tol), mode, ctypes.byref(fit_c),
+                self._stream()), "continuum fit")
+            if mode == FIT_MIXED:
+                # forests whose optimum the FP32 terms cannot place to 1e-7:
+                # FP64 Newton from the mixed solution
+                refine = torch.nonzero(out["status"] == STATUS_REFINE).flatten().to(torch.int32)
+                self.refined.append(int(refine.numel()))
+                if refine.numel():
+                    warm = torch.stack([out["zero_point"], out["slope"]], dim=1).contiguous()
+                    check(lib.pg_cont_fit_select(
+                        self.plan.handle, ctypes.byref(spectra.c), ctypes.byref(model),
+                        warm.data_ptr(), refine.data_ptr(), int(refine.numel()),
+                        int(max_iter or self.max_iter), float(self.tol), FIT_FP64,
+                        ctypes.byref(fit_c), self._stream()), "continuum refinement")
+                    keep["refine"] = (warm, refine)
         out["_keep"] = (keep, start, fit_c, index)
         return out
 

@@ -553,8 +553,11 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
                 break;
             }
         }
-        // chi2 at the solution: compensated FP32 lane sums, FP64 warp sum
-        float cs = 0.f, ce = 0.f;
+        // chi2 at the solution (compensated FP32 lane sums, FP64 warp sum)
+        // and the scale of the gradient's FP32 rounding: the per-pixel
+        // roundings are independent, so it grows as the root of the sum of
+        // squares of the per-pixel gradient terms
+        float cs = 0.f, ce = 0.f, ga_abs = 0.f, gb_abs = 0.f;
         const float af = (float)a, bf = (float)b;
 #pragma unroll
         for (int k = 0; k < kContK; ++k) {
@@ -563,13 +566,38 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
             const float c2 = c * c;
             const float d = px.q[k] + px.vl[k] * c2 + px.fi[k] * c2 * c2;
             const float r = px.f[k] - c;
-            const float term = r * r / d + (const_w ? 0.f : logf(d));
+            const float id = 1.f / d;
+            const float rid = r * id;
+            const float dd = 2.f * px.vl[k] * c + 4.f * px.fi[k] * c2 * c;
+            const float g = fabsf(2.f * rid) + rid * rid * fabsf(dd) + fabsf(dd * id);
+            ga_abs += (g * px.ja[k]) * (g * px.ja[k]);
+            gb_abs += (g * px.jb[k]) * (g * px.jb[k]);
+            const float term = r * rid + (const_w ? 0.f : logf(d));
             const float ns = cs + term;
             const float bb = ns - cs;
             ce += (cs - (ns - bb)) + (term - bb);
             cs = ns;
         }
         const double chi2 = warp_sum((double)cs + (double)ce);
+        // estimate of the optimum's shift by that rounding, |H^-1| (8 u
+        // rms(g)): large when the data barely separate a from b (a forest
+        // covering a short stretch of the rest-frame window)
+        bool refine = false;
+        {
+            const double ua = 8.0 * 5.96e-8 * sqrt((double)warp_sum_f(ga_abs));
+            const double ub = 8.0 * 5.96e-8 * sqrt((double)warp_sum_f(gb_abs));
+            const double ref = fmax(1., fmax(fabs(a), fabs(b)));
+            double ea, eb;
+            if (m.order == 0) {
+                ea = s[3] > 0 ? ua / s[3] : INFINITY;
+                eb = 0.;
+            } else {
+                const double det = s[3] * s[5] - s[4] * s[4];
+                ea = det > 0 ? (fabs(s[5]) * ua + fabs(s[4]) * ub) / det : INFINITY;
+                eb = det > 0 ? (fabs(s[4]) * ua + fabs(s[3]) * ub) / det : INFINITY;
+            }
+            refine = converged && !(ea <= 5e-7 * ref && eb <= 5e-7 * ref);
+        }
         bool negative = false, all_zero = true;
 #pragma unroll
         for (int k = 0; k < kContK; ++k) {
@@ -591,12 +619,13 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
         negative = __any_sync(0xffffffffu, negative);
         all_zero = __all_sync(0xffffffffu, all_zero);
         if (lane == 0) {
-            int status = converged ? 0 : 1;
+            int status = converged ? (refine ? 4 : 0) : 1;
             if (negative) status = 2;
             if (all_zero) status = 3;
-            out.zero_point[f] = status == 0 ? a : NAN;
-            out.slope[f] = status == 0 ? b : NAN;
-            out.chi2[f] = status == 0 ? chi2 : NAN;
+            const bool keep = status == 0 || status == 4;
+            out.zero_point[f] = keep ? a : NAN;
+            out.slope[f] = keep ? b : NAN;
+            out.chi2[f] = keep ? chi2 : NAN;
             out.ndata[f] = nd;
             out.status[f] = status;
             out.iterations[f] = it;

@@ -43,11 +43,11 @@ namespace {
 constexpr float kMagic = 12582912.0f;        // 1.5 * 2^23
 constexpr unsigned kMagicBits = 0x4B400000u;  // bits of 1.5 * 2^23
 constexpr float kFar = 1e30f;                 // r and t of an empty slot
-constexpr int kQueue = 128;                   // FP64 recheck entries per warp
-constexpr int kAccQ = 256;                    // accepted-pair ring per warp
+constexpr int kQueue = 256;                   // FP64 recheck entries per warp
+constexpr int kAccQ = 128;                    // accepted-pair ring per warp
 constexpr int kCfP = 4;                       // forest-2 pixels per lane
 constexpr int kXcfP = 2;                      // quasars per lane per pass
-constexpr int kCfBlock = 512;
+constexpr int kCfBlock = 768;
 constexpr int kXcfBlock = 512;
 
 struct FastConst {
@@ -161,15 +161,15 @@ __host__ __device__ inline SmemLayout smem_layout(int nbins, int max_pix1, int n
 // ---------------------------------------------------------------------------
 struct CfPairCtx {
     int64_t a0, b0;
-    double ang, c, s;
+    double ang, c, s, zq2;
     bool shp;
 };
 
 // FP64 re-decision of queued (i, j) pairs, then accumulation.
 __device__ __forceinline__ void cf_drain(const Binning &b, const FastConst *__restrict__ fcp,
                                       const pg_forest_set &s1, const pg_forest_set &s2,
-                                      CfPairCtx ctx, const uint32_t *queue, int count, float *h,
-                                      Scratch *scratch) {
+                                      const CfPairCtx &ctx, const uint32_t *queue, int count,
+                                      float *h, Scratch *scratch) {
     __syncwarp();
     const int lane = threadIdx.x & 31;
     const double inv_p = fcp->inv_p, inv_t = fcp->inv_t;
@@ -194,6 +194,7 @@ __device__ __forceinline__ void cf_drain(const Binning &b, const FastConst *__re
         const float zs = (float)z1 + (float)z2;
         hist_add(h, fcp->hstride, (unsigned)bin, dw12, w12, pv * w12, tv * w12, zs * w12);
     }
+    if (lane == 0) atomicAdd(&scratch->rechecked_pairs, (unsigned long long)count);
     __syncwarp();
 }
 
@@ -273,6 +274,10 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int item_slot;
     __shared__ long long nbr_next;
+    // state read only off the hot loop lives in shared memory, which keeps
+    // the registers for the pixel pairs (and 24 warps per SM resident)
+    __shared__ double f1_geom[7];  // x, y, z, ra, dec, cos dec, z_qso of forest 1
+    __shared__ CfPairCtx pair_ctx[kCfBlock / 32];
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
@@ -293,7 +298,7 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
     float2 *acc1 = reinterpret_cast<float2 *>(smem + L.acc1) + warp * kAccQ;
     uint32_t *queue = reinterpret_cast<uint32_t *>(smem + L.queue) + warp * kQueue;
     zero_all(h, H_COUNT * hs);
-    unsigned long long rechecks = 0, overflows = 0;
+    CfPairCtx &ctx = pair_ctx[warp];
 
     for (;;) {
         const int item = next_item(scratch, &item_slot);
@@ -322,13 +327,14 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
         }
         // forest-1 pixels in increasing distance: each forest-2 block only
         // visits the forest-1 pixels that can pair with it (see below)
+        if (threadIdx.x == 0) {
+            f1_geom[0] = s1.x_cart[f1]; f1_geom[1] = s1.y_cart[f1]; f1_geom[2] = s1.z_cart[f1];
+            f1_geom[3] = s1.ra[f1]; f1_geom[4] = s1.dec[f1]; f1_geom[5] = s1.cos_dec[f1];
+            f1_geom[6] = s1.z_qso[f1];
+            nbr_next = nbr_offsets[f1];
+        }
         const bool sorted1 = __syncthreads_and(ordered) != 0;
-        const double x1 = s1.x_cart[f1], y1 = s1.y_cart[f1], zc1 = s1.z_cart[f1];
-        const double ra1 = s1.ra[f1], dec1 = s1.dec[f1], cd1 = s1.cos_dec[f1];
-        const double zq1 = s1.z_qso[f1];
-        const int64_t k0 = nbr_offsets[f1], k1 = nbr_offsets[f1 + 1];
-        if (threadIdx.x == 0) nbr_next = k0;
-        __syncthreads();
+        const int64_t k1 = nbr_offsets[f1 + 1];
         int head = 0, tail = 0;  // accepted-pair ring of this warp (warp-uniform)
         for (;;) {
             // warps take neighbour forests dynamically (balances uneven lengths)
@@ -336,41 +342,55 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
             if (lane == 0) k = (int64_t)atomicAdd((unsigned long long *)&nbr_next, 1ull);
             k = __shfl_sync(0xffffffffu, k, 0);
             if (k >= k1) break;
-            CfPairCtx ctx;
             const int64_t g = nbr_index[k];
-            ctx.a0 = a0;
-            ctx.b0 = s2.pix_offset[g];
-            const int64_t n2_64 = s2.pix_offset[g + 1] - ctx.b0;
+            const int64_t b0 = s2.pix_offset[g];
+            const int64_t n2_64 = s2.pix_offset[g + 1] - b0;
             if (n2_64 > 65535) {
                 if (lane == 0) report_error(scratch, PG_ERR_UNSUPPORTED, (int32_t)g);
                 continue;
             }
             const int n2 = (int)n2_64;
-            ctx.ang = nbr_angle ? nbr_angle[k]
-                                : angle_between(x1, y1, zc1, ra1, dec1, cd1, s2.x_cart[g],
-                                                s2.y_cart[g], s2.z_cart[g], s2.ra[g], s2.dec[g]);
-            ctx.c = cos(ctx.ang / 2);
-            ctx.s = sin(ctx.ang / 2);
-            ctx.shp = false;
-            bool zerr_pair = false;
-            double zq2 = 0.;
+            const double ang = nbr_angle ? nbr_angle[k]
+                                         : angle_between(f1_geom[0], f1_geom[1], f1_geom[2],
+                                                         f1_geom[3], f1_geom[4], f1_geom[5],
+                                                         s2.x_cart[g], s2.y_cart[g],
+                                                         s2.z_cart[g], s2.ra[g], s2.dec[g]);
+            const double chalf = cos(ang / 2), shalf = sin(ang / 2);
+            bool shp = false, zerr_pair = false;
             if (EXTRA) {
                 if (b.remove_shp) {
                     const int64_t fb1 = s1.fiberid[f1], fb2 = s2.fiberid[g];
-                    ctx.shp = (s1.plate[f1] == s2.plate[g]) &&
-                              ((fb1 <= 500 && fb2 <= 500) || (fb1 > 500 && fb2 > 500));
+                    shp = (s1.plate[f1] == s2.plate[g]) &&
+                          ((fb1 <= 500 && fb2 <= 500) || (fb1 > 500 && fb2 > 500));
                 }
-                zerr_pair = b.zerr_on && (ctx.ang < b.zerr_ang);
-                zq2 = s2.z_qso[g];
+                zerr_pair = b.zerr_on && (ang < b.zerr_ang);
             }
-            const float cp = (float)(ctx.c * inv_p);
-            const float st = (float)(ctx.s * inv_t);
+            __syncwarp();
+            if (lane == 0) {
+                ctx.a0 = a0;
+                ctx.b0 = b0;
+                ctx.ang = ang;
+                ctx.c = chalf;
+                ctx.s = shalf;
+                ctx.shp = shp;
+                ctx.zq2 = EXTRA ? s2.z_qso[g] : 0.;
+            }
+            __syncwarp();
+            const float cp = (float)(chalf * inv_p);
+            const float st = (float)(shalf * inv_t);
             // r1 - r2 limits of pairs that can land in a bin, one bin of margin
             // each side: x = p - pmin in [-1, np + 1], |p| for auto-correlations
             const float lo_off = AUTO ? -(float)(np + 1u) / cp : (pmin_f - 1.f) / cp;
             const float hi_off = AUTO ? (float)(np + 1u) / cp : (pmin_f + (float)np + 1.f) / cp;
             int qn = 0;
             for (int jb = 0; jb < n2; jb += 32 * kCfP) {
+              // The FP64 re-decision queue is drained between passes over the
+              // forest-1 pixels, outside the pixel loop, so that its FP64 code
+              // does not hold registers in the loop; a pass stops early when
+              // one more pixel could overflow the queue, and the next pass
+              // reloads the forest-2 slots and resumes at that pixel.
+              int i_next = -1, i_end = n1;
+              for (;;) {
                 // lane owns pixels jb + kCfP*lane + p (consecutive pixels, so the
                 // lanes of a warp mostly fall in different r_par bins)
                 float rh[kCfP], rl[kCfP], t[kCfP], zv[kCfP], wv[kCfP], dv[kCfP];
@@ -380,10 +400,11 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                     const int j = jb + kCfP * lane + p;
                     rh[p] = kFar; rl[p] = 0.f; t[p] = kFar; zv[p] = kFar; wv[p] = 0.f; dv[p] = 0.f;
                     if (j < n2) {
-                        const int64_t jj = ctx.b0 + j;
+                        const int64_t jj = b0 + j;
                         const double w2 = s2.weights[jj];
                         bool ok = w2 != 0;
-                        if (EXTRA && zerr_pair && ok) ok = !zerr_veto(s2.z[jj], zq1, b.zerr_kms);
+                        if (EXTRA && zerr_pair && ok)
+                            ok = !zerr_veto(s2.z[jj], f1_geom[6], b.zerr_kms);
                         if (ok) {
                             any = true;
                             const double r = s2.r_comov[jj];
@@ -396,13 +417,20 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                         }
                     }
                 }
-                if (!__any_sync(0xffffffffu, any)) continue;
-                int i_lo = 0, i_hi = n1;
-                if (sorted1) window(p1, n1, rh, t, st, lo_off, hi_off, t_end, i_lo, i_hi);
-                for (int i = i_lo; i < i_hi; ++i) {
+                if (!__any_sync(0xffffffffu, any)) break;
+                if (i_next < 0) {
+                    int i_lo = 0, i_hi = n1;
+                    if (sorted1) window(p1, n1, rh, t, st, lo_off, hi_off, t_end, i_lo, i_hi);
+                    i_next = i_lo;
+                    i_end = i_hi;
+                }
+                int i = i_next;
+                for (; i < i_end; ++i) {
+                    if (qn > kQueue - 32 * kCfP) break;  // drain first (below)
                     const float2 qw = p2[i];
                     if (qw.x == 0.f) continue;  // zero-weight pixel (warp-uniform)
-                    if (EXTRA && zerr_pair && zerr_veto(s1.z[a0 + i], zq2, b.zerr_kms)) continue;
+                    if (EXTRA && zerr_pair && zerr_veto(s1.z[a0 + i], ctx.zq2, b.zerr_kms))
+                        continue;
                     const float4 q = p1[i];
                     const float ui = st * q.z;
                     unsigned near_mask = 0;
@@ -420,7 +448,7 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                         bool ok = (ip < np) & (it < nt);
                         const float zs = q.w + zv[p];
                         if (EXTRA) {
-                            if (ctx.shp) {
+                            if (shp) {
                                 near |= fabsf(v - 1.f) < fcp->guard_v;
                                 ok &= !(v < 1.f);
                             }
@@ -442,11 +470,14 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                             acc1[pos] = make_float2(zs, __uint_as_float(ip * nt + it));
                         }
                         tail += __popc(m);
-                    }
-                    // at most 32 kCfP entries per pixel: the ring (kAccQ) never overflows
-                    while (tail - head >= 32) {
-                        apply_accepted(acc0, acc1, head, 32, h, hs);
-                        head += 32;
+                        if (p & 1) {
+                            // at most 64 entries since the last check: the ring
+                            // (kAccQ = 128 > 31 + 64) never overflows
+                            while (tail - head >= 32) {
+                                apply_accepted(acc0, acc1, head, 32, h, hs);
+                                head += 32;
+                            }
+                        }
                     }
                     if (__any_sync(0xffffffffu, near_mask != 0)) {
                         // rare path: queue the pairs near an edge for FP64 re-decision
@@ -456,12 +487,6 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                             const unsigned nmask = __ballot_sync(0xffffffffu, near);
                             if (!nmask) continue;
                             const int cnt = __popc(nmask);
-                            if (qn + cnt > kQueue) {
-                                cf_drain(b, fcp, s1, s2, ctx, queue, qn, h, scratch);
-                                rechecks += qn;
-                                ++overflows;
-                                qn = 0;
-                            }
                             if (near) {
                                 const int pos = qn + __popc(nmask & lt_mask);
                                 queue[pos] = ((uint32_t)i << 16) | (uint32_t)(jb + kCfP * lane + p);
@@ -470,21 +495,19 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                         }
                     }
                 }
-            }
-            if (qn) {
+                if (i >= i_end) break;
                 cf_drain(b, fcp, s1, s2, ctx, queue, qn, h, scratch);
-                rechecks += qn;
+                if (lane == 0) atomicAdd(&scratch->recheck_overflows, 1ull);
+                qn = 0;
+                i_next = i;
+              }
             }
+            if (qn) cf_drain(b, fcp, s1, s2, ctx, queue, qn, h, scratch);
         }
         if (tail != head) apply_accepted(acc0, acc1, head, tail - head, h, hs);
         __syncthreads();
         flush_rows(h, *fcp, out, row);
         if (threadIdx.x == 0) atomicAdd(&scratch->work_items, 1ull);
-    }
-    if (lane == 0) {
-        // per-warp counters are warp-uniform
-        atomicAdd(&scratch->rechecked_pairs, rechecks);
-        atomicAdd(&scratch->recheck_overflows, overflows);
     }
 }
 

@@ -4,8 +4,9 @@ Tolerances: the GPU and the oracle minimise the same chi2 to the same
 optimum (|step| < 1e-10 relative); FP64 mode: (a, b) within 1e-7 relative,
 chi2 within 1e-10 relative; mixed mode (FP32 per-pixel terms and sums, FP64
 2x2 solve; the FP32 rounding of the gradient and of the model leaves about
-1e-7 on the optimum): (a, b) within 2e-6, chi2 within 1e-6, the FP32
-continuum within 2e-6 relative. chi2 = sum (f - C)^2 / D + sum log D is a sum
+1e-7 on the optimum, and forests where it is estimated above 5e-7 are finished
+in FP64): (a, b) within 3e-6, chi2 within 1e-6, the FP32 continuum within
+3e-6 relative. chi2 = sum (f - C)^2 / D + sum log D is a sum
 of terms of either sign that can cancel, so its tolerance is relative to
 max(|chi2|, ndata), the scale of the sum of |terms| (each (f - C)^2 / D is
 about one). Histogram sums of positive terms agree to 1e-8 relative (only
@@ -48,7 +49,7 @@ def test_fit_matches_oracle(cuda, raw, mode):
     res = continuum.fit_results_to_host(gpu.fit(spectra))
     orc = oc.Dr16Oracle(raw.grid)
     conts, params = orc.fit_all(raw)
-    tol_ab, tol_chi2 = (1e-7, 1e-10) if mode == "fp64" else (2e-6, 1e-6)
+    tol_ab, tol_chi2 = (1e-7, 1e-10) if mode == "fp64" else (3e-6, 1e-6)
     for k in range(raw.num):
         (a, b, chi2, ndata), reason = params[k]
         status = res["status"][k]
