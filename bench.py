@@ -55,6 +55,11 @@ def parse():
     p.add_argument("--continuum-train", type=int, default=200_000,
                    help="raw forests (separate seed) the warm-start network is trained on")
     p.add_argument("--continuum-iterations", type=int, default=5)
+    p.add_argument("--profile-items", type=int, default=0,
+                   help="profiling aid: run the pair kernel once on this many randomly chosen "
+                        "work items of the workload and exit (no timing, no JSON line)")
+    p.add_argument("--config2", action="store_true",
+                   help="also run the 400k-forest auto and 600k-quasar cross correlations")
     p.add_argument("--continuum-correlation", type=int, default=50_000,
                    help="forests whose plain- and learned-fit deltas are correlated (0 skips)")
     return p.parse_args()
@@ -242,7 +247,7 @@ def continuum_leg(args, cpu_seconds):
     train = continuum.DeviceSpectra(train_raw, eng_t.device)
     (feats, targs, _), collect_s = timed_loop(lambda: learned.collect_training(eng_t, train))
     net = learned.WarmStartMLP(seed=0)
-    hist, train_s = timed_loop(lambda: net.train(feats, targs, epochs=4, batch=4096, lr=2e-3))
+    hist, train_s = timed_loop(lambda: net.train(feats, targs, epochs=16, batch=4096, lr=2e-3))
     num_samples = int(feats.shape[0])
     del feats, targs, train
 
@@ -311,6 +316,68 @@ def continuum_leg(args, cpu_seconds):
                      "collect_s": collect_s, "train_s": train_s, "loss_first": hist[0],
                      "loss_last": hist[-1]},
     }
+
+
+def config2_leg(args):
+    """Config 2: the 400k-forest auto-correlation on 8,000 deg^2 and the
+    cross-correlation with 600k quasars on the same band (r_par -200..200 in
+    100 bins x r_trans 0..200 in 50), both in the precision form; each kernel
+    timed once after a warm-up run, with its error against the plain FP64
+    kernel on 0.5% of the work items."""
+    import torch
+
+    from picca_gb300 import pairs, synthetic
+    fs = synthetic.config_area(400_000, 8000.0, seed=20261206)
+    ra_r, dec_r = synthetic.band_for_area(8000.0, 30.0)
+    qs = synthetic.make_quasars(600_000, 20261207, ra_r, dec_r)
+    ang_max = synthetic.correlation_ang_max(200.0, float(fs.z.min()))
+    stream = torch.cuda.current_stream()
+    out = {}
+    for name, xcf in (("auto", False), ("xcf", True)):
+        kw = (dict(r_par_min=-200.0, r_par_max=200.0, r_trans_max=200.0, num_bins_r_par=100,
+                   num_bins_r_trans=50, x_correlation=True) if xcf else
+              dict(r_par_min=0.0, r_par_max=200.0, r_trans_max=200.0, num_bins_r_par=50,
+                   num_bins_r_trans=50))
+        params = pairs.make_params(ang_max=ang_max, **kw)
+        engine = pairs.PairEngine()
+        d1 = pairs.DeviceForests(fs, engine.device)
+        d2 = pairs.DeviceForests(qs, engine.device) if xcf else None
+        offsets, index, total = engine.neighbours(params, d1, d2, xcf=xcf)
+        order, num_work, cand = engine.work_order(d1, d2, offsets, index, total, xcf=xcf)
+        nbins = kw["num_bins_r_par"] * kw["num_bins_r_trans"]
+        times = []
+        for _ in range(2):
+            rows = engine.alloc_rows(len(fs.healpix_list), nbins)
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            engine.accumulate(params, d1, d2, offsets, index, order, num_work, rows,
+                              pairs.MODE_FP32_GUARD, xcf=xcf)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+        n_check = max(1, num_work // 200)
+        sub = order[:num_work][torch.randperm(num_work, device=order.device)[:n_check]]
+        sub = sub.contiguous()
+        r32 = engine.alloc_rows(len(fs.healpix_list), nbins)
+        r64 = engine.alloc_rows(len(fs.healpix_list), nbins)
+        engine.accumulate(params, d1, d2, offsets, index, sub, n_check, r32,
+                          pairs.MODE_FP32_GUARD, xcf=xcf)
+        engine.accumulate(params, d1, d2, offsets, index, sub, n_check, r64, pairs.MODE_FP64,
+                          xcf=xcf)
+        torch.cuda.synchronize()
+        a = [r.cpu().numpy() for r in r32]
+        b = [r.cpu().numpy() for r in r64]
+        nz = b[0] > 0
+        out[name] = {
+            "forests": fs.num, "quasars": qs.num if xcf else None, "bins": nbins,
+            "candidate_pairs": int(cand), "kernel_s": times[-1],
+            "pairs_per_s": cand / times[-1], "nb_identical_on_sample": bool(
+                np.array_equal(a[5], b[5])),
+            "we_max_rel_on_sample": float(np.max(np.abs(a[0][nz] - b[0][nz]) / b[0][nz]))
+            if nz.any() else None}
+        del engine, d1, d2, offsets, index, order, rows, r32, r64
+        torch.cuda.empty_cache()
+    return out
 
 
 def run_reference(args):
@@ -383,6 +450,26 @@ def run_ours(args):
             timings.append((ev0, ev1))
         return rows, cand, total, (offsets, index, order, num_work)
 
+    if args.profile_items > 0:
+        offsets, index, total = engine.neighbours(cparams, dev)
+        order, num_work, _ = engine.work_order(dev, None, offsets, index, total)
+        gen = torch.Generator(device=order.device).manual_seed(1)
+        n = min(args.profile_items, num_work)
+        sub = order[:num_work][torch.randperm(num_work, device=order.device,
+                                              generator=gen)[:n]].contiguous()
+        npix = torch.diff(dev.tensors["pix_offset"])
+        sub_l = sub.long()
+        cand = 0
+        for f in sub_l.tolist():
+            nb = index[offsets[f]:offsets[f + 1]].long()
+            cand += int(npix[f].item()) * int(npix[nb].sum().item())
+        rows = engine.alloc_rows(num_rows, nbins)
+        engine.accumulate(cparams, dev, None, offsets, index, sub, n, rows, mode)
+        torch.cuda.synchronize()
+        print(json.dumps({"profile_items": n, "candidate_pixel_pairs": cand,
+                          "workload": CONFIGS[args.config][3]}), flush=True)
+        return
+
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -439,10 +526,18 @@ def run_ours(args):
         sub_order = sub_order.contiguous()
         r32 = engine.alloc_rows(num_rows, nbins)
         r64 = engine.alloc_rows(num_rows, nbins)
+        sample_cand = int(engine.last_cost[sub_order.long()].sum().item())
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        ev[0].record(stream)
         engine.accumulate(cparams, dev, None, offsets, index, sub_order, n_check, r32, mode)
+        ev[1].record(stream)
+        ev[2].record(stream)
         engine.accumulate(cparams, dev, None, offsets, index, sub_order, n_check, r64,
                           pairs.MODE_FP64)
+        ev[3].record(stream)
         torch.cuda.synchronize()
+        fast_s = ev[0].elapsed_time(ev[1]) / 1e3
+        fp64_s = ev[2].elapsed_time(ev[3]) / 1e3
         # the scale of xi's rounding: sum of |delta1 w1 delta2 w2| per bin (FP64 kernel on |delta|)
         packed_abs = dict(packed)
         packed_abs["delta"] = np.abs(np.asarray(packed["delta"]))
@@ -468,6 +563,9 @@ def run_ours(args):
             "xi_median_rel": float(np.median(rel_xi)),
             "xi_p99_rel": float(np.percentile(rel_xi, 99)),
             "xi_total_rel": float(xi_sum),
+            "sample_candidate_pixel_pairs": sample_cand,
+            "precision_form_pairs_per_s_on_sample": sample_cand / fast_s,
+            "plain_fp64_kernel_pairs_per_s_on_sample": sample_cand / fp64_s,
         }
 
     # roofline of the pair kernel (FP32 CUDA-core bound)
@@ -487,6 +585,7 @@ def run_ours(args):
     del dev, packed, engine
     torch.cuda.empty_cache()
     cont = continuum_leg(args, args.cpu_seconds)
+    cfg2 = config2_leg(args) if args.config2 else None
     print("continuum leg: " + json.dumps(cont), file=sys.stderr, flush=True)
     line = {
         "metric": METRIC, "value": value, "unit": "pixel-pairs/s", "n_gpus": world,
@@ -510,11 +609,14 @@ def run_ours(args):
                      "flops_per_launch": flops},
         "precision_check_vs_fp64_kernel": check,
         "rechecked_pairs_last_step": int(stats.rechecked_pairs),
+        "evaluated_pixel_pair_slots_last_step": int(stats.visited_pairs),
         "clocks": clocks,
         "cpu_baseline": {"value": cpu_val, "unit": "pixel-pairs/s", "cores": cores,
                          "kind": "port", "sample": cpu_desc},
         "continuum": cont,
     }
+    if cfg2 is not None:
+        line["config2"] = cfg2
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -101,6 +101,8 @@ typedef struct pg_run_stats {
     int64_t rechecked_pairs;    /* FP32_GUARD: pairs re-decided in FP64       */
     int64_t recheck_overflows;  /* FP32_GUARD: early recheck-queue drains     */
     int64_t work_items;         /* work items processed                        */
+    int64_t visited_pairs;      /* FP32_GUARD cf: pixel-pair slots evaluated
+                                   (after the per-block pixel windows)         */
 } pg_run_stats;
 
 typedef struct pg_plan pg_plan;
@@ -263,7 +265,7 @@ int pg_cont_fit_batch(pg_plan *plan, const pg_spectra *spectra, const pg_cont_mo
  * per-pixel terms are FP32, the iteration stops at a step below
  * max(tol, 1e-6) * max(1, |a|, |b|), and the continuum is formed in FP32.
  * A converged mixed fit whose optimum the FP32 rounding of the gradient is
- * estimated to move by more than 5e-7 * max(1, |a|, |b|) (a forest whose
+ * estimated to move by more than 2e-6 * max(1, |a|, |b|) (a forest whose
  * pixels barely separate a from b) gets status 4 with its (a, b): finish it
  * with PG_FIT_FP64 on those forests, starting from that (a, b). */
 int pg_cont_fit_select(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,

@@ -148,6 +148,7 @@ int pg_plan_stats(pg_plan *plan, pg_run_stats *stats) {
     stats->rechecked_pairs = (int64_t)host.rechecked_pairs;
     stats->recheck_overflows = (int64_t)host.recheck_overflows;
     stats->work_items = (int64_t)host.work_items;
+    stats->visited_pairs = (int64_t)host.visited_pairs;
     return PG_OK;
 }
 

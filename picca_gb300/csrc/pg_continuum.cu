@@ -107,9 +107,9 @@ struct PixelTerms {
 // chi2 / 2 and its derivatives of one lane's pixels (accumulated in T,
 // returned in FP64); constant weights use q = 1, vl = fi = 0 with no log.
 // U is the arithmetic type of the per-pixel terms (T or FP64).
-template <typename U, typename T, typename O>
-__device__ __forceinline__ void lane_terms(const PixelTerms<T> &px, double a, double b,
-                                           bool const_w, O s[6]) {
+template <typename U, typename T, typename O, typename A>
+__device__ __forceinline__ void lane_terms(const PixelTerms<T> &px, A a, A b, bool const_w,
+                                           O s[6]) {
     U val = 0, ga = 0, gb = 0, haa = 0, hab = 0, hbb = 0;
     const U ua = (U)a, ub = (U)b;
 #pragma unroll
@@ -143,7 +143,7 @@ __device__ __forceinline__ void lane_terms(const PixelTerms<T> &px, double a, do
 template <typename U, typename T>
 __device__ __forceinline__ void eval_all(const PixelTerms<T> &px, double a, double b, bool const_w,
                                          double s[6]) {
-    lane_terms<U, T, double>(px, a, b, const_w, s);
+    lane_terms<U, T, double, double>(px, a, b, const_w, s);
 #pragma unroll
     for (int k = 0; k < 6; ++k) s[k] = warp_sum(s[k]);
 }
@@ -404,12 +404,11 @@ __device__ __forceinline__ float warp_sum_f(float v) {
     return v;
 }
 
-__device__ __forceinline__ void eval_all_f(const PixelTerms<float> &px, double a, double b,
-                                           bool const_w, double s[6]) {
-    float v[6];
-    lane_terms<float, float, float>(px, a, b, const_w, v);
+__device__ __forceinline__ void eval_all_f(const PixelTerms<float> &px, float a, float b,
+                                           bool const_w, float s[6]) {
+    lane_terms<float, float, float, float>(px, a, b, const_w, s);
 #pragma unroll
-    for (int k = 0; k < 6; ++k) s[k] = (double)warp_sum_f(v[k]);
+    for (int k = 0; k < 6; ++k) s[k] = warp_sum_f(s[k]);
 }
 
 __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
@@ -422,7 +421,7 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
     const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const bool const_w = m.use_constant_weight != 0;
-    const double eff_tol = tol > 1e-6 ? tol : 1e-6;
+    const float eff_tol = tol > 1e-6 ? (float)tol : 1e-6f;
     const int mi = tab.m;
     for (int64_t w = warp_global; w < count; w += nwarps) {
         const int64_t f = index ? (int64_t)index[w] : w;
@@ -441,7 +440,12 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
             continue;
         }
         const int n = (int)n64;
-        const double zp1 = log10(1 + sp.z_qso[f]);
+        // scalar FP64 work runs on lane 0 and is broadcast: GB300's FP64
+        // pipe is narrow, and a warp-wide scalar computation would cost 32
+        // lanes' worth of it
+        double zp1 = 0.;
+        if (lane == 0) zp1 = log10(1 + sp.z_qso[f]);
+        zp1 = __shfl_sync(0xffffffffu, zp1, 0);
         const double ll_min = m.log_lambda_rest_min + zp1;
         const float inv_span = (float)(1.0 / (m.log_lambda_rest_max - m.log_lambda_rest_min));
         PixelTerms<float> px;
@@ -479,10 +483,9 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
                 }
             }
         }
-        const double sfi_d = warp_sum((double)sfi), si_d = warp_sum((double)si);
-        const double a0 = sfi_d / si_d;
+        // starting point (utils.py:92): FP32 sums, only a start
+        const float a0f = warp_sum_f(sfi) / warp_sum_f(si);
         int nd = 0;
-        const float a0f = (float)a0;
 #pragma unroll
         for (int k = 0; k < kContK; ++k) {
             if ((px.valid >> k) & 1u) {
@@ -494,71 +497,96 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
         }
 #pragma unroll
         for (int o = 16; o > 0; o >>= 1) nd += __shfl_xor_sync(0xffffffffu, nd, o);
-        double a = a0, b = 0.;
+        // (a, b) as unevaluated sums of two floats (hi + lo): the steps are
+        // accumulated without rounding them away
+        float ah = a0f, al = 0.f, bh = 0.f, bl = 0.f;
         if (start) {
-            a = start[2 * f];
-            b = m.order == 0 ? 0. : start[2 * f + 1];
+            const double a_s = start[2 * f];
+            const double b_s = m.order == 0 ? 0. : start[2 * f + 1];
+            ah = (float)a_s;
+            al = (float)(a_s - (double)ah);
+            bh = (float)b_s;
+            bl = (float)(b_s - (double)bh);
         }
-        double s[6];
-        eval_all_f(px, a, b, const_w, s);
+        float s[6];
+        eval_all_f(px, ah, bh, const_w, s);
         int it = 0;
         bool converged = false;
         for (; it < max_iter; ++it) {
-            double da, db;
+            // Newton step. The 2x2 determinant and numerators are formed in
+            // FP64 from the FP32 sums (products of two FP32 numbers are exact
+            // in FP64, so only the final subtraction rounds): they cancel
+            // when the data barely separate a from b. The quotient and the
+            // rest of the step logic are FP32.
+            float da = 0.f, db = 0.f;
             if (m.order == 0) {
-                da = s[3] > 0 ? -s[1] / s[3] : -s[1];
-                db = 0.;
+                da = s[3] > 0.f ? -s[1] / s[3] : -s[1];
             } else {
-                const double det = s[3] * s[5] - s[4] * s[4];
-                if (det > 0 && s[3] > 0) {
-                    da = -(s[5] * s[1] - s[4] * s[2]) / det;
-                    db = -(s[3] * s[2] - s[4] * s[1]) / det;
-                } else {
-                    const double scale = fmax(fabs(s[3]), fabs(s[5]));
-                    da = -s[1] / (scale > 0 ? scale : 1.);
-                    db = -s[2] / (scale > 0 ? scale : 1.);
+                if (lane == 0) {
+                    const double s1 = s[1], s2 = s[2], s3 = s[3], s4 = s[4], s5 = s[5];
+                    const double det = fma(s3, s5, -s4 * s4);
+                    if (det > 0. && s[3] > 0.f) {
+                        const float inv = (float)(1.0 / det);
+                        da = -(float)fma(s5, s1, -s4 * s2) * inv;
+                        db = -(float)fma(s3, s2, -s4 * s1) * inv;
+                    } else {
+                        da = db = 0.f;
+                    }
                 }
-                if (da * s[1] + db * s[2] >= 0) {
-                    const double scale = fmax(fabs(s[3]), fabs(s[5]));
-                    da = -s[1] / (scale > 0 ? scale : 1.);
-                    db = -s[2] / (scale > 0 ? scale : 1.);
+                da = __shfl_sync(0xffffffffu, da, 0);
+                db = __shfl_sync(0xffffffffu, db, 0);
+                const float scale = fmaxf(fabsf(s[3]), fabsf(s[5]));
+                if ((da == 0.f && db == 0.f) || da * s[1] + db * s[2] >= 0.f) {
+                    // singular Hessian or not a descent direction: gradient step
+                    da = -s[1] / (scale > 0.f ? scale : 1.f);
+                    db = -s[2] / (scale > 0.f ? scale : 1.f);
                 }
             }
-            const double ref = fmax(1., fmax(fabs(a), fabs(b)));
-            double trial[6];
-            double t = 1.;
-            if (fabs(da) < 1e-3 * ref && fabs(db) < 1e-3 * ref) {
-                eval_all_f(px, a + da, b + db, const_w, trial);
+            const float ref = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));
+            float trial[6];
+            float t = 1.f;
+            if (fabsf(da) < 1e-3f * ref && fabsf(db) < 1e-3f * ref) {
+                eval_all_f(px, ah + da, bh + db, const_w, trial);
             } else {
-                const double slope_dir = da * s[1] + db * s[2];
+                const float slope_dir = da * s[1] + db * s[2];
                 bool accepted = false;
                 for (int ls = 0; ls < 40; ++ls) {
-                    eval_all_f(px, a + t * da, b + t * db, const_w, trial);
-                    if (isfinite(trial[0]) && trial[0] <= s[0] + 1e-4 * t * slope_dir) {
+                    eval_all_f(px, ah + t * da, bh + t * db, const_w, trial);
+                    if (isfinite(trial[0]) && trial[0] <= s[0] + 1e-4f * t * slope_dir) {
                         accepted = true;
                         break;
                     }
-                    t *= 0.5;
+                    t *= 0.5f;
                 }
                 if (!accepted) break;
             }
-            a += t * da;
-            b += t * db;
+            {
+                // (ah, al) += t da exactly to FP32-pair precision (TwoSum)
+                const float sa = t * da, sb = t * db;
+                float hi = ah + sa, bb = hi - ah;
+                al += (ah - (hi - bb)) + (sa - bb);
+                ah = hi;
+                hi = bh + sb;
+                bb = hi - bh;
+                bl += (bh - (hi - bb)) + (sb - bb);
+                bh = hi;
+            }
 #pragma unroll
             for (int k = 0; k < 6; ++k) s[k] = trial[k];
-            const double ref2 = fmax(1., fmax(fabs(a), fabs(b)));
-            if (fabs(t * da) < eff_tol * ref2 && fabs(t * db) < eff_tol * ref2) {
+            const float ref2 = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));
+            if (fabsf(t * da) < eff_tol * ref2 && fabsf(t * db) < eff_tol * ref2) {
                 converged = true;
                 ++it;
                 break;
             }
         }
-        // chi2 at the solution (compensated FP32 lane sums, FP64 warp sum)
-        // and the scale of the gradient's FP32 rounding: the per-pixel
-        // roundings are independent, so it grows as the root of the sum of
-        // squares of the per-pixel gradient terms
+        const double a = (double)ah + (double)al, b = (double)bh + (double)bl;
+        // chi2 at the solution (compensated FP32 sums, lanes and warp) and
+        // the scale of the gradient's FP32 rounding: the per-pixel roundings
+        // are independent, so it grows as the root of the sum of squares of
+        // the per-pixel gradient terms
         float cs = 0.f, ce = 0.f, ga_abs = 0.f, gb_abs = 0.f;
-        const float af = (float)a, bf = (float)b;
+        const float af = ah, bf = bh;
 #pragma unroll
         for (int k = 0; k < kContK; ++k) {
             if (!((px.valid >> k) & 1u)) continue;
@@ -578,25 +606,37 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
             ce += (cs - (ns - bb)) + (term - bb);
             cs = ns;
         }
-        const double chi2 = warp_sum((double)cs + (double)ce);
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float os = __shfl_xor_sync(0xffffffffu, cs, o);
+            const float oe = __shfl_xor_sync(0xffffffffu, ce, o);
+            const float ns = cs + os;
+            const float bb = ns - cs;
+            ce += oe + ((cs - (ns - bb)) + (os - bb));
+            cs = ns;
+        }
+        const double chi2 = (double)cs + (double)ce;
+        ga_abs = warp_sum_f(ga_abs);
+        gb_abs = warp_sum_f(gb_abs);
         // estimate of the optimum's shift by that rounding, |H^-1| (8 u
         // rms(g)): large when the data barely separate a from b (a forest
         // covering a short stretch of the rest-frame window)
         bool refine = false;
-        {
-            const double ua = 8.0 * 5.96e-8 * sqrt((double)warp_sum_f(ga_abs));
-            const double ub = 8.0 * 5.96e-8 * sqrt((double)warp_sum_f(gb_abs));
-            const double ref = fmax(1., fmax(fabs(a), fabs(b)));
-            double ea, eb;
+        if (lane == 0 && converged) {
+            const float ua = 8.f * 5.96e-8f * sqrtf(ga_abs);
+            const float ub = 8.f * 5.96e-8f * sqrtf(gb_abs);
+            const float ref = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));
+            float ea, eb;
             if (m.order == 0) {
-                ea = s[3] > 0 ? ua / s[3] : INFINITY;
-                eb = 0.;
+                ea = s[3] > 0.f ? ua / s[3] : INFINITY;
+                eb = 0.f;
             } else {
-                const double det = s[3] * s[5] - s[4] * s[4];
-                ea = det > 0 ? (fabs(s[5]) * ua + fabs(s[4]) * ub) / det : INFINITY;
-                eb = det > 0 ? (fabs(s[4]) * ua + fabs(s[3]) * ub) / det : INFINITY;
+                const double s3 = s[3], s4 = s[4], s5 = s[5];
+                const float det = (float)fma(s3, s5, -s4 * s4);
+                ea = det > 0.f ? (fabsf(s[5]) * ua + fabsf(s[4]) * ub) / det : INFINITY;
+                eb = det > 0.f ? (fabsf(s[4]) * ua + fabsf(s[3]) * ub) / det : INFINITY;
             }
-            refine = converged && !(ea <= 5e-7 * ref && eb <= 5e-7 * ref);
+            refine = !(ea <= 2e-6f * ref && eb <= 2e-6f * ref);
         }
         bool negative = false, all_zero = true;
 #pragma unroll

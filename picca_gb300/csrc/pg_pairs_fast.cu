@@ -70,24 +70,25 @@ struct FastConst {
 // ---------------------------------------------------------------------------
 enum { H_XI = 0, H_XIL, H_WE, H_WEL, H_PW, H_TW, H_ZW, H_NB, H_COUNT };
 
-// *hi += v with the rounding error of the addition (Knuth's TwoSum of the
-// value returned by the atomic add and v) added to *lo.
-__device__ __forceinline__ void two_sum_add(float *hi, float *lo, float v) {
-    const float old = atomicAdd(hi, v);
-    const float s = old + v;
-    const float bb = s - old;
-    atomicAdd(lo, (old - (s - bb)) + (v - bb));
-}
-
+// One pair into the histograms. xi and w are compensated: the atomic add
+// returns the previous value, Knuth's TwoSum of it and the term gives the
+// exact rounding error of the add, which goes to the error histogram. The two
+// adds whose previous value is needed go first, so that their round trips
+// overlap the four plain adds.
 __device__ __forceinline__ void hist_add(float *h, int hs, unsigned bin, float xi, float w,
                                          float pw, float tw, float zw) {
     float *hx = h + bin;
-    two_sum_add(hx + H_XI * hs, hx + H_XIL * hs, xi);
-    two_sum_add(hx + H_WE * hs, hx + H_WEL * hs, w);
+    const float oxi = atomicAdd(hx + H_XI * hs, xi);
+    const float owe = atomicAdd(hx + H_WE * hs, w);
     atomicAdd(hx + H_PW * hs, pw);
     atomicAdd(hx + H_TW * hs, tw);
     atomicAdd(hx + H_ZW * hs, zw);
     atomicAdd(reinterpret_cast<int *>(hx + H_NB * hs), 1);
+    float sum = oxi + xi, bb = sum - oxi;
+    atomicAdd(hx + H_XIL * hs, (oxi - (sum - bb)) + (xi - bb));
+    sum = owe + w;
+    bb = sum - owe;
+    atomicAdd(hx + H_WEL * hs, (owe - (sum - bb)) + (w - bb));
 }
 
 __device__ __forceinline__ void flush_rows(float *h, const FastConst &fc, const pg_xi_rows &out,
@@ -278,6 +279,7 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
     // the registers for the pixel pairs (and 24 warps per SM resident)
     __shared__ double f1_geom[7];  // x, y, z, ra, dec, cos dec, z_qso of forest 1
     __shared__ CfPairCtx pair_ctx[kCfBlock / 32];
+    __shared__ unsigned long long visited[kCfBlock / 32];  // forest-1 pixel steps per warp
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
@@ -299,6 +301,7 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
     uint32_t *queue = reinterpret_cast<uint32_t *>(smem + L.queue) + warp * kQueue;
     zero_all(h, H_COUNT * hs);
     CfPairCtx &ctx = pair_ctx[warp];
+    if (lane == 0) visited[warp] = 0ull;
 
     for (;;) {
         const int item = next_item(scratch, &item_slot);
@@ -425,13 +428,19 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                     i_end = i_hi;
                 }
                 int i = i_next;
+                // the next forest-1 pixel is loaded one iteration ahead
+                float4 q_next = p1[i < n1 ? i : 0];
+                float2 qw_next = p2[i < n1 ? i : 0];
                 for (; i < i_end; ++i) {
                     if (qn > kQueue - 32 * kCfP) break;  // drain first (below)
-                    const float2 qw = p2[i];
+                    const float2 qw = qw_next;
+                    const float4 q = q_next;
+                    const int i1 = i + 1 < n1 ? i + 1 : i;
+                    q_next = p1[i1];
+                    qw_next = p2[i1];
                     if (qw.x == 0.f) continue;  // zero-weight pixel (warp-uniform)
                     if (EXTRA && zerr_pair && zerr_veto(s1.z[a0 + i], ctx.zq2, b.zerr_kms))
                         continue;
-                    const float4 q = p1[i];
                     const float ui = st * q.z;
                     unsigned near_mask = 0;
 #pragma unroll
@@ -495,6 +504,7 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                         }
                     }
                 }
+                if (lane == 0) visited[warp] += (unsigned long long)(i - i_next);
                 if (i >= i_end) break;
                 cf_drain(b, fcp, s1, s2, ctx, queue, qn, h, scratch);
                 if (lane == 0) atomicAdd(&scratch->recheck_overflows, 1ull);
@@ -509,6 +519,7 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
         flush_rows(h, *fcp, out, row);
         if (threadIdx.x == 0) atomicAdd(&scratch->work_items, 1ull);
     }
+    if (lane == 0) atomicAdd(&scratch->visited_pairs, visited[warp] * (32ull * kCfP));
 }
 
 // ---------------------------------------------------------------------------

@@ -183,6 +183,7 @@ class PairEngine:
             torch.cumsum(per_nbr, 0, out=csum[1:])
             per_forest = csum[offsets[1:]] - csum[offsets[:-1]]
         cost = npix1 * per_forest
+        self.last_cost = cost  # candidate pixel pairs per forest of set 1
         order = torch.argsort(cost, descending=True, stable=True)
         num_work = int((cost > 0).sum().item())
         candidates = int(cost.sum().item())
@@ -252,6 +253,7 @@ def correlate(fs1, fs2, params, mode=MODE_FP64, xcf=False, engine=None, device=N
     return {"raw": (we, xi, rp, rt, zz, nb), "num_rows": num_rows, "nbins": nbins,
             "num_pairs_forest": total, "candidate_pairs": candidates,
             "rechecked_pairs": int(stats.rechecked_pairs), "work_items": int(stats.work_items),
+            "visited_pairs": int(stats.visited_pairs),
             "offsets": offsets, "index": index}
 
 

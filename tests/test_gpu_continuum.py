@@ -4,7 +4,7 @@ Tolerances: the GPU and the oracle minimise the same chi2 to the same
 optimum (|step| < 1e-10 relative); FP64 mode: (a, b) within 1e-7 relative,
 chi2 within 1e-10 relative; mixed mode (FP32 per-pixel terms and sums, FP64
 2x2 solve; the FP32 rounding of the gradient and of the model leaves about
-1e-7 on the optimum, and forests where it is estimated above 5e-7 are finished
+1e-7 on the optimum, and forests where it is estimated above 2e-6 are finished
 in FP64): (a, b) within 3e-6, chi2 within 1e-6, the FP32 continuum within
 3e-6 relative. chi2 = sum (f - C)^2 / D + sum log D is a sum
 of terms of either sign that can cancel, so its tolerance is relative to
