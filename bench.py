@@ -36,6 +36,11 @@ CONFIGS = {
     "2": (400_000, 8000.0, "log", "400k forests on 8,000 deg^2 (config 2)"),
 }
 METRIC = "cf pixel-pairs/s at stated FP64-oracle error; continuum fits/s plain vs learned"
+# DRAM bytes (read + write) of the pair kernel per candidate pixel pair, from
+# one ncu capture on 1,000 random work items of config 1 (5.533 GB read +
+# 0.114 GB written for 2.628e10 candidate pairs; see profiles/); the roofline
+# entry scales it to the launch by the candidate pairs processed
+PAIR_DRAM_BYTES_PER_CANDIDATE = (5.532826e9 + 0.113620e9) / 26284549581
 
 
 def parse():
@@ -603,7 +608,11 @@ def run_ours(args):
                 "d2h_bytes_per_step": int(d2h)},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
-                     "unit": "TFLOP/s", "frac": achieved / fp32_peak, "traffic": None,
+                     "unit": "TFLOP/s", "frac": achieved / fp32_peak,
+                     "traffic": PAIR_DRAM_BYTES_PER_CANDIDATE * pairs_per_step
+                     if args.config in ("1", "2") else None,
+                     "traffic_source": "ncu capture of 1,000 config-1 work items, scaled by "
+                                       "candidate pairs",
                      "kernel_ms": kmean * 1e3,
                      "peak_source": f"SMs x 128 FP32 lanes x 2 x sm_max_mhz ({source} peaks file)",
                      "flops_per_launch": flops},
