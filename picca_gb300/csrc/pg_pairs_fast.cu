@@ -35,6 +35,8 @@
 // divergent branch of each pair. After each work item the histograms are
 // added to the FP64 rows and mapped back to picca's units (r_par =
 // p/inv_p, r_trans = x_tr/inv_t, z = (z1+z2)/2).
+#include <type_traits>
+
 #include "pg_internal.cuh"
 
 namespace pg {
@@ -45,7 +47,7 @@ constexpr unsigned kMagicBits = 0x4B400000u;  // bits of 1.5 * 2^23
 constexpr float kFar = 1e30f;                 // r and t of an empty slot
 constexpr int kQueue = 256;                   // FP64 recheck entries per warp
 constexpr int kAccQ = 128;                    // accepted-pair ring per warp
-constexpr int kCfP = 4;                       // forest-2 pixels per lane
+constexpr int kCfP = 4;                       // forest-2 pixels per lane (full passes)
 constexpr int kXcfP = 2;                      // quasars per lane per pass
 constexpr int kCfBlock = 768;
 constexpr int kXcfBlock = 512;
@@ -76,14 +78,14 @@ enum { H_XI = 0, H_XIL, H_WE, H_WEL, H_PW, H_TW, H_ZW, H_NB, H_COUNT };
 // adds whose previous value is needed go first, so that their round trips
 // overlap the four plain adds.
 __device__ __forceinline__ void hist_add(float *h, int hs, unsigned bin, float xi, float w,
-                                         float pw, float tw, float zw) {
+                                         float pw, float tw, float zw, int count) {
     float *hx = h + bin;
     const float oxi = atomicAdd(hx + H_XI * hs, xi);
     const float owe = atomicAdd(hx + H_WE * hs, w);
     atomicAdd(hx + H_PW * hs, pw);
     atomicAdd(hx + H_TW * hs, tw);
     atomicAdd(hx + H_ZW * hs, zw);
-    atomicAdd(reinterpret_cast<int *>(hx + H_NB * hs), 1);
+    atomicAdd(reinterpret_cast<int *>(hx + H_NB * hs), count);
     float sum = oxi + xi, bb = sum - oxi;
     atomicAdd(hx + H_XIL * hs, (oxi - (sum - bb)) + (xi - bb));
     sum = owe + w;
@@ -193,25 +195,27 @@ __device__ __forceinline__ void cf_drain(const Binning &b, const FastConst *__re
         const float pv = (float)(r_par * inv_p);
         const float tv = (float)(r_trans * inv_t);
         const float zs = (float)z1 + (float)z2;
-        hist_add(h, fcp->hstride, (unsigned)bin, dw12, w12, pv * w12, tv * w12, zs * w12);
+        hist_add(h, fcp->hstride, (unsigned)bin, dw12, w12, pv * w12, tv * w12, zs * w12, 1);
     }
     if (lane == 0) atomicAdd(&scratch->rechecked_pairs, (unsigned long long)count);
     __syncwarp();
 }
 
-// Applies n (<= 32) queued accepted pairs starting at ring position head.
-// Entry: {p, xt', w1 w2, dw1 dw2} and {z1 + z2, bin}.
+// Applies n (<= 32) queued entries starting at ring position head. An entry
+// is a run of accepted pairs of one lane in one bin (consecutive forest-2
+// pixels against one forest-1 pixel): {sum dw1 dw2, sum w1 w2, sum p w,
+// sum x_tr w} and {sum (z1 + z2) w, bin * 8 + pairs}.
+template <bool FULL>
 __device__ __forceinline__ void apply_accepted(const float4 *acc0, const float2 *acc1, int head,
                                                int n, float *h, int hs) {
     __syncwarp();
     const int lane = threadIdx.x & 31;
-    if (lane < n) {
+    if (FULL || lane < n) {  // FULL: n = 32, no divergence
         const int e = (head + lane) & (kAccQ - 1);
         const float4 v = acc0[e];
         const float2 u = acc1[e];
-        const unsigned bin = __float_as_uint(u.y);
-        const float w = v.z;
-        hist_add(h, hs, bin, v.w, w, v.x * w, (v.y + 0.5f) * w, u.x * w);
+        const unsigned key = __float_as_uint(u.y);
+        hist_add(h, hs, key >> 3, v.x, v.y, v.z, v.w, u.x, (int)(key & 7u));
     }
     __syncwarp();
 }
@@ -237,12 +241,13 @@ __device__ __forceinline__ int count_below(const float4 *p1, int n, float v) {
 // the block's r range +- the offsets) or x_tr' = st d1 + t above nt + 1
 // (d1 beyond (nt + 1 - min t) / st); their FP32 values are then far from
 // every bin and edge, so the FP32 test would reject them without queueing.
-__device__ __forceinline__ void window(const float4 *p1, int n1, const float *rh, const float *t,
-                                       float st, float lo_off, float hi_off, float t_end,
-                                       int &i_lo, int &i_hi) {
+template <int P>
+__device__ __forceinline__ void window(const float4 *p1, int n1, const float (&rh)[P],
+                                       const float (&t)[P], float st, float lo_off,
+                                       float hi_off, float t_end, int &i_lo, int &i_hi) {
     float rmin = kFar, rmax = -kFar, tmin = kFar;
 #pragma unroll
-    for (int p = 0; p < kCfP; ++p) {
+    for (int p = 0; p < P; ++p) {
         if (rh[p] < 0.5f * kFar) {
             rmin = fminf(rmin, rh[p]);
             rmax = fmaxf(rmax, rh[p]);
@@ -386,7 +391,12 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
             const float lo_off = AUTO ? -(float)(np + 1u) / cp : (pmin_f - 1.f) / cp;
             const float hi_off = AUTO ? (float)(np + 1u) / cp : (pmin_f + (float)np + 1.f) / cp;
             int qn = 0;
-            for (int jb = 0; jb < n2; jb += 32 * kCfP) {
+            // One pass over forest-2 pixels [jb, jb + 32 P): lane l holds pixels
+            // jb + P l + p, p < P. The forest is covered with P = 4 passes and
+            // a last pass of P = 2 or 1 for a short remainder, so that few
+            // slots are empty.
+            auto pass = [&](auto p_const, const int jb) {
+              constexpr int P = decltype(p_const)::value;
               // The FP64 re-decision queue is drained between passes over the
               // forest-1 pixels, outside the pixel loop, so that its FP64 code
               // does not hold registers in the loop; a pass stops early when
@@ -396,11 +406,11 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
               for (;;) {
                 // lane owns pixels jb + kCfP*lane + p (consecutive pixels, so the
                 // lanes of a warp mostly fall in different r_par bins)
-                float rh[kCfP], rl[kCfP], t[kCfP], zv[kCfP], wv[kCfP], dv[kCfP];
+                float rh[P], rl[P], t[P], zv[P], wv[P], dv[P];
                 bool any = false;
 #pragma unroll
-                for (int p = 0; p < kCfP; ++p) {
-                    const int j = jb + kCfP * lane + p;
+                for (int p = 0; p < P; ++p) {
+                    const int j = jb + P * lane + p;
                     rh[p] = kFar; rl[p] = 0.f; t[p] = kFar; zv[p] = kFar; wv[p] = 0.f; dv[p] = 0.f;
                     if (j < n2) {
                         const int64_t jj = b0 + j;
@@ -423,7 +433,8 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                 if (!__any_sync(0xffffffffu, any)) break;
                 if (i_next < 0) {
                     int i_lo = 0, i_hi = n1;
-                    if (sorted1) window(p1, n1, rh, t, st, lo_off, hi_off, t_end, i_lo, i_hi);
+                    if (sorted1)
+                        window<P>(p1, n1, rh, t, st, lo_off, hi_off, t_end, i_lo, i_hi);
                     i_next = i_lo;
                     i_end = i_hi;
                 }
@@ -432,7 +443,7 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                 float4 q_next = p1[i < n1 ? i : 0];
                 float2 qw_next = p2[i < n1 ? i : 0];
                 for (; i < i_end; ++i) {
-                    if (qn > kQueue - 32 * kCfP) break;  // drain first (below)
+                    if (qn > kQueue - 32 * P) break;  // drain first (below)
                     const float2 qw = qw_next;
                     const float4 q = q_next;
                     const int i1 = i + 1 < n1 ? i + 1 : i;
@@ -443,8 +454,25 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                         continue;
                     const float ui = st * q.z;
                     unsigned near_mask = 0;
+                    // Accepted pairs of this lane's consecutive slots that fall in
+                    // the same bin are summed in registers (a run) and go to the
+                    // ring as one entry, which halves the shared-memory atomics.
+                    unsigned run_bin = 0u;
+                    int run_n = 0;
+                    float r_xi = 0.f, r_w = 0.f, r_pw = 0.f, r_tw = 0.f, r_zw = 0.f;
+                    // stores the runs of the lanes in `flag` into the ring
+                    auto store_runs = [&](bool flag) {
+                        const unsigned m = __ballot_sync(0xffffffffu, flag);
+                        const int pos = (tail + __popc(m & lt_mask)) & (kAccQ - 1);
+                        if (flag) {
+                            acc0[pos] = make_float4(r_xi, r_w, r_pw, r_tw);
+                            acc1[pos] = make_float2(r_zw, __uint_as_float((run_bin << 3) |
+                                                                          (unsigned)run_n));
+                        }
+                        tail += __popc(m);
+                    };
 #pragma unroll
-                    for (int p = 0; p < kCfP; ++p) {
+                    for (int p = 0; p < P; ++p) {
                         const float pp = cp * ((q.x - rh[p]) + (q.y - rl[p]));
                         const float v = fabsf(pp);
                         const float pv = AUTO ? v : pp;
@@ -472,54 +500,83 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                         }
                         near_mask |= (unsigned)near << p;
                         const bool acc = ok & !near;
-                        const unsigned m = __ballot_sync(0xffffffffu, acc);
+                        const unsigned bin = ip * nt + it;
+                        const bool extend = acc & (run_n > 0) & (bin == run_bin);
+                        // a pair that starts a new run stores the previous one
+                        store_runs(acc & (run_n > 0) & !extend);
                         if (acc) {
-                            const int pos = (tail + __popc(m & lt_mask)) & (kAccQ - 1);
-                            acc0[pos] = make_float4(pv, xt, qw.x * wv[p], qw.y * dv[p]);
-                            acc1[pos] = make_float2(zs, __uint_as_float(ip * nt + it));
+                            if (!extend) {
+                                run_bin = bin;
+                                run_n = 0;
+                                r_xi = r_w = r_pw = r_tw = r_zw = 0.f;
+                            }
+                            const float w12 = qw.x * wv[p];
+                            r_xi += qw.y * dv[p];
+                            r_w += w12;
+                            r_pw += pv * w12;
+                            r_tw += (xt + 0.5f) * w12;
+                            r_zw += zs * w12;
+                            ++run_n;
                         }
-                        tail += __popc(m);
                         if (p & 1) {
                             // at most 64 entries since the last check: the ring
                             // (kAccQ = 128 > 31 + 64) never overflows
                             while (tail - head >= 32) {
-                                apply_accepted(acc0, acc1, head, 32, h, hs);
+                                apply_accepted<true>(acc0, acc1, head, 32, h, hs);
                                 head += 32;
                             }
                         }
                     }
+                    store_runs(run_n > 0);
+                    while (tail - head >= 32) {
+                        apply_accepted<true>(acc0, acc1, head, 32, h, hs);
+                        head += 32;
+                    }
                     if (__any_sync(0xffffffffu, near_mask != 0)) {
                         // rare path: queue the pairs near an edge for FP64 re-decision
 #pragma unroll
-                        for (int p = 0; p < kCfP; ++p) {
+                        for (int p = 0; p < P; ++p) {
                             const bool near = (near_mask >> p) & 1u;
                             const unsigned nmask = __ballot_sync(0xffffffffu, near);
                             if (!nmask) continue;
                             const int cnt = __popc(nmask);
                             if (near) {
                                 const int pos = qn + __popc(nmask & lt_mask);
-                                queue[pos] = ((uint32_t)i << 16) | (uint32_t)(jb + kCfP * lane + p);
+                                queue[pos] = ((uint32_t)i << 16) | (uint32_t)(jb + P * lane + p);
                             }
                             qn += cnt;
                         }
                     }
                 }
-                if (lane == 0) visited[warp] += (unsigned long long)(i - i_next);
+                if (lane == 0) visited[warp] += (unsigned long long)(i - i_next) * (32u * P);
                 if (i >= i_end) break;
                 cf_drain(b, fcp, s1, s2, ctx, queue, qn, h, scratch);
                 if (lane == 0) atomicAdd(&scratch->recheck_overflows, 1ull);
                 qn = 0;
                 i_next = i;
               }
+            };
+            for (int jb = 0; jb < n2;) {
+                const int rem = n2 - jb;
+                if (rem > 64) {
+                    pass(std::integral_constant<int, 4>{}, jb);
+                    jb += 128;
+                } else if (rem > 32) {
+                    pass(std::integral_constant<int, 2>{}, jb);
+                    jb += 64;
+                } else {
+                    pass(std::integral_constant<int, 1>{}, jb);
+                    jb += 32;
+                }
             }
             if (qn) cf_drain(b, fcp, s1, s2, ctx, queue, qn, h, scratch);
         }
-        if (tail != head) apply_accepted(acc0, acc1, head, tail - head, h, hs);
+        if (tail != head) apply_accepted<false>(acc0, acc1, head, tail - head, h, hs);
         __syncthreads();
         flush_rows(h, *fcp, out, row);
         if (threadIdx.x == 0) atomicAdd(&scratch->work_items, 1ull);
     }
-    if (lane == 0) atomicAdd(&scratch->visited_pairs, visited[warp] * (32ull * kCfP));
+    if (lane == 0) atomicAdd(&scratch->visited_pairs, visited[warp]);
 }
 
 // ---------------------------------------------------------------------------
@@ -564,7 +621,7 @@ __device__ __forceinline__ void xcf_drain(const Binning &b, const FastConst *__r
         const float pv = (float)(r_par * inv_p);
         const float tv = (float)(r_trans * inv_t);
         const float zs = (float)z1 + (float)zq;
-        hist_add(h, fcp->hstride, (unsigned)bin, dw, w12, pv * w12, tv * w12, zs * w12);
+        hist_add(h, fcp->hstride, (unsigned)bin, dw, w12, pv * w12, tv * w12, zs * w12, 1);
     }
     __syncwarp();
 }
@@ -684,7 +741,7 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
                         const float w12 = qw.x * wv[p];
                         const unsigned bin = ip * nt + it;
                         hist_add(h, hs, bin, qw.y * wv[p], w12, pv * w12, (xt + 0.5f) * w12,
-                                 zs * w12);
+                                 zs * w12, 1);
                     }
                 }
                 if (__any_sync(0xffffffffu, near_mask != 0)) {
