@@ -439,16 +439,11 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                     i_end = i_hi;
                 }
                 int i = i_next;
-                // the next forest-1 pixel is loaded one iteration ahead
-                float4 q_next = p1[i < n1 ? i : 0];
-                float2 qw_next = p2[i < n1 ? i : 0];
+
                 for (; i < i_end; ++i) {
                     if (qn > kQueue - 32 * P) break;  // drain first (below)
-                    const float2 qw = qw_next;
-                    const float4 q = q_next;
-                    const int i1 = i + 1 < n1 ? i + 1 : i;
-                    q_next = p1[i1];
-                    qw_next = p2[i1];
+                    const float2 qw = p2[i];
+                    const float4 q = p1[i];
                     if (qw.x == 0.f) continue;  // zero-weight pixel (warp-uniform)
                     if (EXTRA && zerr_pair && zerr_veto(s1.z[a0 + i], ctx.zq2, b.zerr_kms))
                         continue;
