@@ -1,8 +1,9 @@
 """Build the CPU oracle shared library (test infrastructure only).
 
-``python oracle/build.py`` compiles ``oracle/pairs_oracle.c`` into
-``oracle/_build/liboracle.so`` with FMA contraction disabled, so the FP64
-operation order is the one of picca's numba kernels.
+``python oracle/build.py`` compiles ``oracle/pairs_oracle.c`` and
+``oracle/dmat_oracle.c`` into ``oracle/_build/liboracle.so`` with FMA
+contraction disabled, so the FP64 operation order is the one of picca's numba
+kernels.
 """
 
 import os
@@ -16,14 +17,14 @@ LIB = os.path.join(OUT_DIR, "liboracle.so")
 
 def build(force=False, quiet=True):
     """Compile the oracle if it is missing or older than its source."""
-    src = os.path.join(HERE, "pairs_oracle.c")
+    srcs = [os.path.join(HERE, name) for name in ("pairs_oracle.c", "dmat_oracle.c")]
     if (not force and os.path.exists(LIB)
-            and os.path.getmtime(LIB) >= os.path.getmtime(src)):
+            and all(os.path.getmtime(LIB) >= os.path.getmtime(src) for src in srcs)):
         return LIB
     os.makedirs(OUT_DIR, exist_ok=True)
     tmp = LIB + f".tmp{os.getpid()}"
     cmd = ["gcc", "-O2", "-std=c11", "-fPIC", "-shared", "-fopenmp",
-           "-ffp-contract=off", "-fno-fast-math", "-o", tmp, src, "-lm"]
+           "-ffp-contract=off", "-fno-fast-math", "-o", tmp] + srcs + ["-lm"]
     if not quiet:
         print(" ".join(cmd))
     subprocess.check_call(cmd)

@@ -10,6 +10,10 @@ Run once in a checkout that has the picca sources next to it
   correlation outputs (``py/picca/tests/data/test_cor/*.fits.gz``), produced by
   the commands at ``py/picca/tests/test_3_cor.py:229-316, :458-488,
   :636-664, :791-1002``;
+* ``cor_dmat.npz``: picca's golden distortion matrix (``test_cor/dmat.fits.gz``,
+  command at ``py/picca/tests/test_3_cor.py:318-347``);
+* ``dmat_cases.npz``: inputs and outputs of picca's own
+  ``cf.compute_dmat_forest_pairs_fast`` on forest pairs of the test data;
 * ``pair_cases.npz``: inputs and outputs of picca's own
   ``cf.compute_xi_forest_pairs_fast`` and ``xcf.compute_xi_forest_pairs_fast``
   run here as plain Python (numba, healpy, fitsio, camb and iminuit replaced by
@@ -280,6 +284,122 @@ def _pair_cases(reference_py, delta_dir, attributes):
     return case_index, xcase
 
 
+def _convert_dmat(src, out_path):
+    hdul = fitsio_lite.FITS(src)
+    dm = hdul["DMAT"]
+    attri = hdul["ATTRI"]
+    out = {c: dm[c][:] for c in dm.get_colnames()}
+    out.update({c: attri[c][:] for c in attri.get_colnames()})
+    header = dm.read_header()
+    for key in ("RPMIN", "RPMAX", "RTMAX", "NP", "NT", "COEFMOD", "REJ", "NPALL", "NPUSED"):
+        out["hdr_" + key] = np.asarray(header[key])
+    np.savez_compressed(out_path, **out)
+
+
+def _dmat_cases(reference_py, delta_dir, attributes):
+    """Inputs and outputs of picca's own cf.compute_dmat_forest_pairs_fast
+    (run as plain Python) on forest pairs of the test data."""
+    sys.dont_write_bytecode = True
+    _install_stand_ins()
+    sys.path.insert(0, reference_py)
+    import picca.cf as ref_cf  # pylint: disable=import-outside-toplevel
+
+    cosmo = gb_constants.Cosmo(Om=0.315, verbose=False)
+    data, _, _, _ = gb_io.read_deltas(delta_dir, 16, 1215.67, 2.9, 2.25, cosmo,
+                                      delta_attributes=attributes)
+    deltas = [d for hp in sorted(data) for d in data[hp]]
+    rng = np.random.default_rng(20261204)
+    pairs = []
+    for _ in range(4000):
+        a, b = rng.integers(0, len(deltas), 2)
+        if a == b:
+            continue
+        ang = deltas[a].get_angle_between(deltas[b])
+        if ang < 0.01 and abs(deltas[a].z_qso - deltas[b].z_qso) < 0.4:
+            pairs.append((a, b))
+        if len(pairs) >= 3:
+            break
+    for a in range(len(deltas)):
+        for b in range(a + 1, len(deltas)):
+            if deltas[a].plate == deltas[b].plate and (
+                    (deltas[a].fiberid <= 500) == (deltas[b].fiberid <= 500)) and (
+                        abs(deltas[a].z_qso - deltas[b].z_qso) < 0.5):
+                if deltas[a].get_angle_between(deltas[b]) < 0.016:
+                    pairs.append((a, b))
+                    break
+        if len(pairs) >= 4:
+            break
+    variants = [
+        dict(name="auto", np=15, nt=15, coef=1, shp=True, zevol=False, order=(1, 1)),
+        dict(name="auto_zevol", np=15, nt=15, coef=1, shp=False, zevol=True, order=(1, 1)),
+        dict(name="auto_coef2_order0", np=10, nt=10, coef=2, shp=False, zevol=True,
+             order=(0, 1)),
+        dict(name="auto_zcut_zerr", np=15, nt=15, coef=1, shp=True, zevol=True, order=(1, 0),
+             z_min_pairs=2.2, z_max_pairs=2.4, zerr_cut_deg=2.0, zerr_cut_kms=30000.),
+    ]
+    out = {}
+    case = 0
+    for variant in variants:
+        for (a, b) in pairs:
+            d1, d2 = deltas[a], deltas[b]
+            ref_cf.r_par_min, ref_cf.r_par_max, ref_cf.r_trans_max = 0., 60., 60.
+            ref_cf.num_bins_r_par, ref_cf.num_bins_r_trans = variant["np"], variant["nt"]
+            ref_cf.num_model_bins_r_par = variant["np"] * variant["coef"]
+            ref_cf.num_model_bins_r_trans = variant["nt"] * variant["coef"]
+            ref_cf.z_min_pairs = variant.get("z_min_pairs")
+            ref_cf.z_max_pairs = variant.get("z_max_pairs")
+            ref_cf.zerr_cut_deg = variant.get("zerr_cut_deg")
+            ref_cf.zerr_cut_kms = variant.get("zerr_cut_kms")
+            ref_cf.x_correlation = False
+            ref_cf.rmu_binning = False
+            ref_cf.remove_same_half_plate_close_pairs = variant["shp"]
+            ref_cf.redshift_evolution_in_distortion_matrix = variant["zevol"]
+            ref_cf.z_ref, ref_cf.alpha, ref_cf.alpha2 = 2.25, 2.9, 2.9
+            nb = variant["np"] * variant["nt"]
+            nm = nb * variant["coef"] ** 2
+            arrays = dict(weights_dmat=np.zeros(nb), dmat=np.zeros(nb * nm),
+                          r_par_eff=np.zeros(nm), r_trans_eff=np.zeros(nm), z_eff=np.zeros(nm),
+                          weight_eff=np.zeros(nm))
+            ang = d1.get_angle_between(d2)
+            shp = (d1.plate == d2.plate) and (
+                (d1.fiberid <= 500 and d2.fiberid <= 500) or
+                (d1.fiberid > 500 and d2.fiberid > 500))
+            try:
+                ref_cf.compute_dmat_forest_pairs_fast(
+                    d1.log_lambda, d2.log_lambda, d1.r_comov, d2.r_comov, d1.dist_m,
+                    d2.dist_m, d1.z, d2.z, d1.weights, d2.weights, d1.z_qso, d2.z_qso, ang,
+                    arrays["weights_dmat"], arrays["dmat"], arrays["r_par_eff"],
+                    arrays["r_trans_eff"], arrays["z_eff"], arrays["weight_eff"], shp,
+                    variant["order"][0], variant["order"][1])
+            except IndexError:
+                # cf.py:544-568 counts the pairs without those vetoed as same
+                # half-plate, while cf.py:702 stores every pair in range: with a
+                # vetoed pair the reference writes past its array (silently
+                # under numba). Such a pair cannot serve as a fixture.
+                continue
+            prefix = f"dm{case}_"
+            out[prefix + "params"] = np.array([
+                variant["np"], variant["nt"], variant["coef"], float(variant["shp"]),
+                float(variant["zevol"]), variant["order"][0], variant["order"][1],
+                np.nan if variant.get("z_min_pairs") is None else variant["z_min_pairs"],
+                np.nan if variant.get("z_max_pairs") is None else variant["z_max_pairs"],
+                np.nan if variant.get("zerr_cut_deg") is None else variant["zerr_cut_deg"],
+                np.nan if variant.get("zerr_cut_kms") is None else variant["zerr_cut_kms"]])
+            out[prefix + "scalars"] = np.array([d1.z_qso, d2.z_qso, ang, float(shp)])
+            for key, val in (("ll1", d1.log_lambda), ("ll2", d2.log_lambda), ("r1", d1.r_comov),
+                             ("r2", d2.r_comov), ("m1", d1.dist_m), ("m2", d2.dist_m),
+                             ("z1", d1.z), ("z2", d2.z), ("w1", d1.weights),
+                             ("w2", d2.weights)):
+                out[prefix + key] = np.asarray(val, dtype=float)
+            for key, val in arrays.items():
+                out[prefix + "out_" + key] = val
+            out[prefix + "name"] = np.asarray(variant["name"])
+            case += 1
+    out["num_cases"] = np.asarray(case)
+    np.savez_compressed(os.path.join(HERE, "dmat_cases.npz"), **out)
+    return case
+
+
 def _continuum_cases(reference_py):
     """chi2 of picca's own LeastsSquaresContModel (least_squares_cont_model.py:
     65-197) on synthetic forests at several (zero_point, slope) points."""
@@ -341,7 +461,13 @@ def main(picca_root):
                             os.path.join(tests, "test_delta", "Delta_LYA") + "/",
                             os.path.join(tests, "test_delta", "delta_attributes.fits.gz"))
     ncont = _continuum_cases(os.path.join(picca_root, "py"))
-    print(f"wrote fixtures: {ncf} cf pair cases, {nxcf} xcf cases, {ncont} continuum cases")
+    _convert_dmat(os.path.join(tests, "test_cor", "dmat.fits.gz"),
+                  os.path.join(HERE, "cor_dmat.npz"))
+    ndm = _dmat_cases(os.path.join(picca_root, "py"),
+                      os.path.join(tests, "test_delta", "Delta_LYA") + "/",
+                      os.path.join(tests, "test_delta", "delta_attributes.fits.gz"))
+    print(f"wrote fixtures: {ncf} cf pair cases, {nxcf} xcf cases, {ncont} continuum cases, "
+          f"{ndm} distortion-matrix cases")
 
 
 if __name__ == "__main__":
