@@ -22,6 +22,8 @@
  *                          py/picca/cf.py:138-247, :250-387
  *  - pg_xcf_xi          <- xcf.compute_xi + xcf.compute_xi_forest_pairs_fast
  *                          py/picca/xcf.py:126-220, :223-322
+ *  - pg_cf_dmat         <- cf.compute_dmat + cf.compute_dmat_forest_pairs_fast
+ *                          py/picca/cf.py:390-517, :519-887
  *  - pg_corr_params     <- the cf / xcf module globals set by
  *                          py/picca/bin/picca_cf.py:343-368 and
  *                          py/picca/bin/picca_xcf.py:351-373
@@ -328,6 +330,62 @@ int pg_mlp_to_bf16(const float *x, uint16_t *y, int64_t n, void *stream);
  * feat_stride + j] as bf16 (columns 66..feat_stride-1 zeroed); a0[f] FP64. */
 int pg_mlp_features(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
                     uint16_t *features, int32_t feat_stride, double *a0, void *stream);
+
+/* ---------------------------------------------------------------------
+ * Distortion matrix (py/picca/cf.py:390-887, py/picca/bin/picca_dmat.py)
+ * --------------------------------------------------------------------- */
+
+/* The model binning and redshift evolution of the distortion matrix (the cf
+ * module globals num_model_bins_r_par / _r_trans,
+ * redshift_evolution_in_distortion_matrix, z_ref, alpha, alpha2 set by
+ * py/picca/bin/picca_dmat.py:366-400). */
+typedef struct pg_dmat_params {
+    int32_t num_model_bins_r_par, num_model_bins_r_trans;
+    int32_t redshift_evolution;
+    int32_t row_capacity;  /* data + model bins of one forest pair held at once
+                              (0: 512); more are processed in chunks        */
+    double z_ref, alpha, alpha2;
+} pg_dmat_params;
+
+/* Raw sums of the distortion matrix, ACCUMULATED into (the caller zeroes
+ * them), before the normalisation of py/picca/bin/picca_dmat.py:487-525:
+ * weights_dmat [nb], dmat [nb * nm] (dmat[data_bin * nm + model_bin]),
+ * r_par_eff, r_trans_eff, z_eff, weight_eff [nm]; nb = num_bins_r_par *
+ * num_bins_r_trans, nm = num_model_bins_r_par * num_model_bins_r_trans. */
+typedef struct pg_dmat_sums {
+    double *weights_dmat, *dmat;
+    double *r_par_eff, *r_trans_eff, *z_eff, *weight_eff;
+} pg_dmat_sums;
+
+/* Device work-buffer size (bytes) pg_cf_dmat wants for forests of at most
+ * max_pixels1 / max_pixels2 pixels: one slice per CTA of the persistent
+ * kernel, for every resident CTA or at most max_ctas of them (max_ctas > 0;
+ * pass the number of forest pairs for small runs). A smaller buffer runs
+ * fewer CTAs; PG_ERR_UNSUPPORTED if the forests do not fit in shared
+ * memory. */
+int pg_cf_dmat_work_bytes(pg_plan *plan, const pg_corr_params *params,
+                          const pg_dmat_params *dparams, int32_t max_pixels1,
+                          int32_t max_pixels2, int64_t max_ctas, uint64_t *bytes);
+
+/* Distortion matrix of the selected forest pairs (pair_first[q] of s1,
+ * pair_second[q] of s2; s2 = NULL for the auto-correlation, when s1 and its
+ * log_lambda / order arrays serve both sides). The pair selection (the
+ * random rejection of cf.compute_dmat) is the caller's. log_lambda* are
+ * pixel arrays aligned with the sets, order* per-forest polynomial orders (0
+ * or 1, Delta.order). pair_angle (optional, [num_pairs]) overrides the
+ * angles computed from the sets' unit vectors. Every pixel pair adds the
+ * reference's eta terms; sums are FP64 and reassociated with respect to the
+ * reference (agreement to a few ulp of the summed magnitudes). work is a
+ * device buffer of work_bytes (pg_cf_dmat_work_bytes). rmu_binning,
+ * x_correlation and the zerr / z cuts follow the reference;
+ * ang_correlation is PG_ERR_UNSUPPORTED (the reference has no angular
+ * distortion matrix). */
+int pg_cf_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_params *dparams,
+               const pg_forest_set *s1, const pg_forest_set *s2, const double *log_lambda1,
+               const double *log_lambda2, const int32_t *order1, const int32_t *order2,
+               const int32_t *pair_first, const int32_t *pair_second, const double *pair_angle,
+               int64_t num_pairs, void *work, uint64_t work_bytes, const pg_dmat_sums *out,
+               void *stream);
 
 #ifdef __cplusplus
 }

@@ -33,21 +33,24 @@ class DmatParams(ctypes.Structure):
         ("x_correlation", ctypes.c_int32), ("remove_same_half_plate_close_pairs", ctypes.c_int32),
         ("redshift_evolution", ctypes.c_int32),
         ("z_ref", ctypes.c_double), ("alpha", ctypes.c_double), ("alpha2", ctypes.c_double),
+        ("rmu_binning", ctypes.c_int32), ("pad", ctypes.c_int32),
     ]
 
 
 def make_params(r_par_min, r_par_max, r_trans_max, num_bins_r_par, num_bins_r_trans,
                 coef_binning_model=1, z_min_pairs=None, z_max_pairs=None, zerr_cut_deg=None,
                 zerr_cut_kms=None, remove_same_half_plate_close_pairs=False,
-                redshift_evolution=True, z_ref=2.25, alpha=2.9, alpha2=2.9):
+                redshift_evolution=True, z_ref=2.25, alpha=2.9, alpha2=2.9,
+                rmu_binning=False, x_correlation=False):
     nan = lambda v: float("nan") if v is None else float(v)  # noqa: E731
     return DmatParams(float(r_par_min), float(r_par_max), float(r_trans_max),
                       int(num_bins_r_par), int(num_bins_r_trans),
                       int(num_bins_r_par * coef_binning_model),
                       int(num_bins_r_trans * coef_binning_model), nan(z_min_pairs),
-                      nan(z_max_pairs), nan(zerr_cut_deg), nan(zerr_cut_kms), 0,
-                      int(bool(remove_same_half_plate_close_pairs)),
-                      int(bool(redshift_evolution)), float(z_ref), float(alpha), float(alpha2))
+                      nan(z_max_pairs), nan(zerr_cut_deg), nan(zerr_cut_kms),
+                      int(bool(x_correlation)), int(bool(remove_same_half_plate_close_pairs)),
+                      int(bool(redshift_evolution)), float(z_ref), float(alpha), float(alpha2),
+                      int(bool(rmu_binning)), 0)
 
 
 def _lib():

@@ -27,6 +27,7 @@ typedef struct {
     int32_t x_correlation, remove_same_half_plate_close_pairs;
     int32_t redshift_evolution;        /* redshift_evolution_in_distortion_matrix */
     double z_ref, alpha, alpha2;
+    int32_t rmu_binning, pad;
 } oracle_dmat_params;
 
 /* Same pair selection as the first loop of cf.py:544-568: returns 1 when the
@@ -37,6 +38,10 @@ static int in_range(const oracle_dmat_params *p, double r1, double r2, double d1
 {
     double rp = (r1 - r2) * c;
     double rt = (d1 + d2) * s;
+    if (p->rmu_binning) {
+        rt = sqrt(rt * rt + rp * rp);
+        rp /= rt;
+    }
     if (!p->x_correlation) rp = fabs(rp);
     *r_par = rp;
     *r_trans = rt;
@@ -185,7 +190,12 @@ void oracle_dmat_forest_pair(const oracle_dmat_params *p,
         }
     }
 
-    /* accumulation (cf.py:842-887) over the model bins touched by any pair */
+    /* accumulation (cf.py:842-887) over the model bins touched by any pair,
+     * ascending like np.unique(all_model_bins) */
+    int64_t num_touched = 0;
+    int32_t *touched_list = (int32_t *)malloc(sizeof(int32_t) * (nm > 0 ? nm : 1));
+    for (int64_t k = 0; k < nm; ++k)
+        if (touched[k]) touched_list[num_touched++] = (int32_t)k;
     for (int64_t q = 0; q < num_sel; ++q) {
         const int64_t i = sel_i[q], j = sel_j[q];
         const int64_t bins = sel_data[q];
@@ -195,8 +205,8 @@ void oracle_dmat_forest_pair(const oracle_dmat_params *p,
             zfac = pow((1 + z1[i]) / (1 + p->z_ref), p->alpha - 1) *
                    pow((1 + z2[j]) / (1 + p->z_ref), p->alpha2 - 1);
         dmat[sel_model[q] + nm * bins] += w12 * zfac;
-        for (int64_t k = 0; k < nm; ++k) {
-            if (!touched[k]) continue;
+        for (int64_t t = 0; t < num_touched; ++t) {
+            const int64_t k = touched_list[t];
             dmat[k + nm * bins] +=
                 w12 * (eta5[k] + eta6[k] * dll2[j] + eta7[k] * dll1[i] +
                        eta8[k] * dll1[i] * dll2[j] - eta1[i + n1 * k] - eta2[j + n2 * k] -
@@ -206,5 +216,5 @@ void oracle_dmat_forest_pair(const oracle_dmat_params *p,
     free(dll1); free(dll2);
     free(eta1); free(eta2); free(eta3); free(eta4);
     free(eta5); free(eta6); free(eta7); free(eta8);
-    free(touched); free(sel_model); free(sel_data); free(sel_i); free(sel_j);
+    free(touched); free(touched_list); free(sel_model); free(sel_data); free(sel_i); free(sel_j);
 }

@@ -53,6 +53,17 @@ class XiRowsC(ctypes.Structure):
                 ("weights", "xi", "r_par", "r_trans", "z", "num_pairs")]
 
 
+class DmatParamsC(ctypes.Structure):
+    _fields_ = [("num_model_bins_r_par", ctypes.c_int32), ("num_model_bins_r_trans", ctypes.c_int32),
+                ("redshift_evolution", ctypes.c_int32), ("row_capacity", ctypes.c_int32),
+                ("z_ref", ctypes.c_double), ("alpha", ctypes.c_double), ("alpha2", ctypes.c_double)]
+
+
+class DmatSumsC(ctypes.Structure):
+    _fields_ = [(name, ctypes.c_void_p) for name in
+                ("weights_dmat", "dmat", "r_par_eff", "r_trans_eff", "z_eff", "weight_eff")]
+
+
 class RunStats(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("error_detail", ctypes.c_int32),
                 ("rechecked_pairs", ctypes.c_int64), ("recheck_overflows", ctypes.c_int64),
@@ -87,8 +98,17 @@ def lib():
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
         _P(XiRowsC), ctypes.c_void_p]
     handle.pg_xcf_xi.argtypes = handle.pg_cf_xi.argtypes
+    handle.pg_cf_dmat_work_bytes.argtypes = [
+        ctypes.c_void_p, _P(CorrParams), _P(DmatParamsC), ctypes.c_int32, ctypes.c_int32,
+        ctypes.c_int64, _P(ctypes.c_uint64)]
+    handle.pg_cf_dmat.argtypes = [
+        ctypes.c_void_p, _P(CorrParams), _P(DmatParamsC), _P(ForestSetC), _P(ForestSetC)]
+    handle.pg_cf_dmat.argtypes += [ctypes.c_void_p] * 7 + [ctypes.c_int64, ctypes.c_void_p,
+                                                           ctypes.c_uint64, _P(DmatSumsC),
+                                                           ctypes.c_void_p]
     for name in ("pg_plan_create", "pg_plan_destroy", "pg_plan_stats", "pg_cf_neighbours",
-                 "pg_xcf_neighbours", "pg_cf_xi", "pg_xcf_xi"):
+                 "pg_xcf_neighbours", "pg_cf_xi", "pg_xcf_xi", "pg_cf_dmat_work_bytes",
+                 "pg_cf_dmat"):
         getattr(handle, name).restype = ctypes.c_int
     _LIB = handle
     return handle

@@ -6,7 +6,11 @@ Same module globals (py/picca/cf.py:28-79) and the same functions:
 * ``compute_xi(healpixs)`` returns ``(weights, xi, r_par, r_trans, z,
   num_pairs)`` for those healpix (py/picca/cf.py:138-247);
 * ``compute_xi_forest_pairs_fast(...)`` keeps the 20-argument signature and
-  accumulates one forest pair in place (py/picca/cf.py:250-387).
+  accumulates one forest pair in place (py/picca/cf.py:250-387);
+* ``compute_dmat(healpixs)`` returns the raw distortion-matrix sums of those
+  healpix with the reference's random rejection (py/picca/cf.py:390-517),
+  and ``compute_dmat_forest_pairs_fast(...)`` keeps the 22-argument signature
+  (py/picca/cf.py:519-887).
 
 All pair arithmetic runs on the GPU through ``libpicca_gb300``. The first
 ``fill_neighs`` / ``compute_xi`` call computes the neighbour lists and the
@@ -19,6 +23,7 @@ re-decision; bin indices and pair counts identical to FP64).
 
 import numpy as np
 
+from . import dmat as _dmat
 from . import pairs as _pairs
 from .forests import ForestSet
 
@@ -60,10 +65,14 @@ rmu_binning = False
 ang_correlation = False
 remove_same_half_plate_close_pairs = False
 
+# variables for distortion matrix
+redshift_evolution_in_distortion_matrix = True
+
 # arithmetic of the GPU pair kernel: "fp64" or "fp32_guard"
 precision = "fp32_guard"
 
-_cache = {"key": None, "result": None, "engine": None}
+_cache = {"key": None, "result": None, "engine": None, "dmat_engine": None,
+          "nbr_key": None, "nbr": None}
 
 
 def _mode():
@@ -179,6 +188,21 @@ def compute_xi(healpixs):
     return weights, xi_n, rp_n, rt_n, z_n, num_pairs
 
 
+def _single_forest(z, r, m, w, d, zq, plate, fiber, log_lambda=None, order=-1):
+    """A one-forest ForestSet (the per-pair drop-ins). Same-half-plate pairs
+    are expressed through the plate number with fiber ids on one half."""
+    n = len(z)
+    return ForestSet(
+        pix_offset=np.array([0, n], dtype=np.int64), z=np.asarray(z, float),
+        r_comov=np.asarray(r, float), dist_m=np.asarray(m, float),
+        weights=np.asarray(w, float), delta=np.asarray(d, float),
+        log_lambda=np.zeros(n) if log_lambda is None else np.asarray(log_lambda, float),
+        ra=np.zeros(1), dec=np.zeros(1), x_cart=np.ones(1), y_cart=np.zeros(1),
+        z_cart=np.zeros(1), cos_dec=np.ones(1), z_qso=np.array([float(zq)]),
+        thingid=np.array([plate]), plate=np.array([plate]), fiberid=np.array([fiber]),
+        order=np.array([order], dtype=np.int64), healpix=np.zeros(1, dtype=np.int64))
+
+
 def compute_xi_forest_pairs_fast(z1, r_comov1, dist_m1, weights1, delta1, z_qso_1, z2, r_comov2,
                                  dist_m2, weights2, delta2, z_qso_2, ang, same_half_plate,
                                  rebin_weight, rebin_xi, rebin_r_par, rebin_r_trans, rebin_z,
@@ -187,19 +211,9 @@ def compute_xi_forest_pairs_fast(z1, r_comov1, dist_m1, weights1, delta1, z_qso_
     (py/picca/cf.py:250-387 signature)."""
     import torch  # pylint: disable=import-outside-toplevel
 
-    def one(z, r, m, w, d, zq, plate, fiber):
-        n = len(z)
-        return ForestSet(
-            pix_offset=np.array([0, n], dtype=np.int64), z=np.asarray(z, float),
-            r_comov=np.asarray(r, float), dist_m=np.asarray(m, float),
-            weights=np.asarray(w, float), delta=np.asarray(d, float),
-            log_lambda=np.zeros(n), ra=np.zeros(1), dec=np.zeros(1), x_cart=np.ones(1),
-            y_cart=np.zeros(1), z_cart=np.zeros(1), cos_dec=np.ones(1),
-            z_qso=np.array([float(zq)]), thingid=np.array([plate]), plate=np.array([plate]),
-            fiberid=np.array([fiber]), healpix=np.zeros(1, dtype=np.int64))
-
-    fs1 = one(z1, r_comov1, dist_m1, weights1, delta1, z_qso_1, 0, 1)
-    fs2 = one(z2, r_comov2, dist_m2, weights2, delta2, z_qso_2, 0 if same_half_plate else 1, 1)
+    fs1 = _single_forest(z1, r_comov1, dist_m1, weights1, delta1, z_qso_1, 0, 1)
+    fs2 = _single_forest(z2, r_comov2, dist_m2, weights2, delta2, z_qso_2,
+                         0 if same_half_plate else 1, 1)
     engine = _engine()
     dev1 = _pairs.DeviceForests(fs1, engine.device)
     dev2 = _pairs.DeviceForests(fs2, engine.device)
@@ -226,3 +240,162 @@ def compute_xi_forest_pairs_fast(z1, r_comov1, dist_m1, weights1, delta1, z_qso_
     rebin_r_trans += rt
     rebin_z += zz
     rebin_num_pairs += nb
+
+
+def _dmat_params():
+    if num_model_bins_r_par is None or num_model_bins_r_trans is None:
+        raise ValueError("cf.num_model_bins_r_par / num_model_bins_r_trans must be set "
+                         "before computing a distortion matrix")
+    return _dmat.make_dmat_params(
+        num_bins_r_par, num_bins_r_trans,
+        redshift_evolution=redshift_evolution_in_distortion_matrix,
+        z_ref=2.25 if z_ref is None else z_ref, alpha=2.9 if alpha is None else alpha,
+        alpha2=(alpha if alpha2 is None else alpha2) if alpha is not None else 2.9,
+        num_model_bins_r_par=num_model_bins_r_par,
+        num_model_bins_r_trans=num_model_bins_r_trans)
+
+
+def _dmat_engine():
+    if _cache["dmat_engine"] is None:
+        _cache["dmat_engine"] = _dmat.DmatEngine(_engine())
+    return _cache["dmat_engine"]
+
+
+def _neighbour_state():
+    """Device forests and neighbour CSR of ``data`` (and ``data2``), cached
+    like compute_xi_all."""
+    key = _state_key()
+    if _cache["nbr_key"] == key and _cache["nbr"] is not None:
+        return _cache["nbr"]
+    if data is None:
+        raise ValueError("cf.data is not set")
+    if ang_correlation:
+        raise ValueError("the distortion matrix has no angular form")
+    engine = _engine()
+    fs1 = ForestSet.from_deltas(data)
+    fs2 = ForestSet.from_deltas(data2) if data2 is not None else None
+    _check_fiberids(fs1)
+    if fs2 is not None:
+        _check_fiberids(fs2)
+    dev1 = _pairs.DeviceForests(fs1, engine.device)
+    dev2 = _pairs.DeviceForests(fs2, engine.device) if fs2 is not None else None
+    offsets, index, total = engine.neighbours(_params(), dev1, dev2)
+    state = {"set1": fs1, "set2": fs2, "dev1": dev1, "dev2": dev2, "offsets": offsets,
+             "index": index, "total": total, "offsets_host": offsets.cpu().numpy()}
+    _cache["nbr_key"] = key
+    _cache["nbr"] = state
+    return state
+
+
+def _dmat_sums(state, mask):
+    """GPU sums of the pairs selected by ``mask`` (a bool array over the
+    neighbour CSR); returns host arrays."""
+    engine = _dmat_engine()
+    fs1, fs2 = state["set1"], state["set2"]
+    dev1, dev2 = state["dev1"], state["dev2"]
+    first, second, num_sel = engine.pair_list(dev1, dev2, state["offsets"], state["index"], mask)
+    if num_sel:
+        _dmat.check_orders(fs2 if fs2 is not None else fs1, np.unique(second.cpu().numpy()))
+    params, dparams = _params(), _dmat_params()
+    side1 = _dmat.DmatEngine.side_arrays(dev1, engine.device)
+    side2 = _dmat.DmatEngine.side_arrays(dev2, engine.device) if dev2 is not None else None
+    sums = engine.alloc_sums(params, dparams)
+    engine.accumulate(params, dparams, dev1, dev2, side1, side2, first, second, num_sel, sums)
+    engine.engine.stats()
+    return {k: v.cpu().numpy() for k, v in sums.items()}
+
+
+def compute_dmat(healpixs):
+    """Raw distortion-matrix sums of ``healpixs`` (py/picca/cf.py:390-517).
+
+    The random rejection draws ``np.random.rand(len(neighbours)) > reject``
+    from NumPy's global generator for every delta of the healpixs, in order,
+    as the reference does; the selected forest pairs run on the GPU. Returns
+    ``(weights_dmat, dmat [nb, nm], r_par_eff, r_trans_eff, z_eff,
+    weight_eff, num_pairs, num_pairs_used)``."""
+    state = _neighbour_state()
+    fs1 = state["set1"]
+    offsets = state["offsets_host"]
+    firsts = np.searchsorted(fs1.row, np.arange(len(fs1.healpix_list)))
+    mask = np.zeros(int(state["total"]), dtype=bool)
+    num_pairs = 0
+    num_pairs_used = 0
+    visited = []
+    for healpix in healpixs:
+        row = int(np.searchsorted(fs1.healpix_list, healpix))
+        for k, delta in enumerate(data[healpix]):
+            f = firsts[row] + k
+            visited.append(f)
+            if getattr(delta, "order", None) is None:
+                raise RuntimeError("Trying to compute the distortion matrix but order is not "
+                                   "defined for the deltas. Check previous warning to solve "
+                                   "this issue")
+            start, end = int(offsets[f]), int(offsets[f + 1])
+            w = np.random.rand(end - start) > reject
+            num_pairs += end - start
+            num_pairs_used += int(w.sum())
+            mask[start:end] = w
+    raw = _dmat_sums(state, mask)
+    for healpix in healpixs:
+        for delta in data[healpix]:
+            if hasattr(delta, "neighbours"):
+                delta.neighbours = None
+    nb = num_bins_r_par * num_bins_r_trans
+    return (raw["weights_dmat"], raw["dmat"].reshape(nb, -1), raw["r_par_eff"],
+            raw["r_trans_eff"], raw["z_eff"], raw["weight_eff"], num_pairs, num_pairs_used)
+
+
+def compute_dmat_all(nproc):
+    """The whole picca_dmat.py computation for ``nproc`` processes: the
+    random rejection of every chunk (healpix index % nproc, generator seeded
+    with the chunk's first healpix) and one GPU pass over all selected forest
+    pairs. Returns the normalised columns (WDM, DM, RP, RT, Z) and NPALL /
+    NPUSED."""
+    state = _neighbour_state()
+    fs1 = state["set1"]
+    _dmat.check_orders(fs1, np.arange(fs1.num))
+    mask = _dmat.selection_mask(fs1.healpix_list, fs1.row, state["offsets_host"], nproc, reject)
+    raw = _dmat_sums(state, mask)
+    result = _dmat.normalise(raw, _params(), _dmat_params(), state["total"], int(mask.sum()))
+    result["raw"] = raw
+    return result
+
+
+def compute_dmat_forest_pairs_fast(log_lambda1, log_lambda2, r_comov1, r_comov2, dist_m1,
+                                   dist_m2, z1, z2, weights1, weights2, z_qso_1, z_qso_2, ang,
+                                   weights_dmat, dmat, r_par_eff, r_trans_eff, z_eff,
+                                   weight_eff, same_half_plate, order1, order2):
+    """One forest pair on the GPU, accumulated in place into the six arrays
+    (py/picca/cf.py:519-545 signature)."""
+    import torch  # pylint: disable=import-outside-toplevel
+
+    zeros1, zeros2 = np.zeros(len(z1)), np.zeros(len(z2))
+    fs1 = _single_forest(z1, r_comov1, dist_m1, weights1, zeros1, z_qso_1, 0, 1,
+                         log_lambda=log_lambda1, order=int(order1))
+    fs2 = _single_forest(z2, r_comov2, dist_m2, weights2, zeros2, z_qso_2,
+                         0 if same_half_plate else 1, 1, log_lambda=log_lambda2,
+                         order=int(order2))
+    engine = _dmat_engine()
+    dev = engine.device
+    dev1 = _pairs.DeviceForests(fs1, dev)
+    dev2 = _pairs.DeviceForests(fs2, dev)
+    params = _pairs.make_params(
+        r_par_min, r_par_max, r_trans_max, num_bins_r_par, num_bins_r_trans, np.pi,
+        z_min_pairs=z_min_pairs, z_max_pairs=z_max_pairs, zerr_cut_deg=zerr_cut_deg,
+        zerr_cut_kms=zerr_cut_kms, x_correlation=x_correlation, rmu_binning=rmu_binning,
+        remove_same_half_plate_close_pairs=remove_same_half_plate_close_pairs)
+    dparams = _dmat_params()
+    side1 = _dmat.DmatEngine.side_arrays(dev1, dev)
+    side2 = _dmat.DmatEngine.side_arrays(dev2, dev)
+    pair = torch.zeros(1, dtype=torch.int32, device=dev)
+    angles = torch.tensor([float(ang)], dtype=torch.float64, device=dev)
+    sums = engine.alloc_sums(params, dparams)
+    engine.accumulate(params, dparams, dev1, dev2, side1, side2, pair, pair, 1, sums,
+                      angles=angles)
+    engine.engine.stats()
+    weights_dmat += sums["weights_dmat"].cpu().numpy()
+    dmat += sums["dmat"].cpu().numpy().reshape(np.shape(dmat))
+    r_par_eff += sums["r_par_eff"].cpu().numpy()
+    r_trans_eff += sums["r_trans_eff"].cpu().numpy()
+    z_eff += sums["z_eff"].cpu().numpy()
+    weight_eff += sums["weight_eff"].cpu().numpy()

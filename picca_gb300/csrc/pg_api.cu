@@ -1,6 +1,8 @@
 // C-ABI entry points of libpicca_gb300 (declared in include/picca_gb300.h).
 #include <stdlib.h>
 
+#include <algorithm>
+
 #include "pg_internal.cuh"
 
 struct pg_plan {
@@ -245,6 +247,68 @@ int pg_xcf_xi(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *
     return launch_xcf_xi_fp64(b, *forests, *objs, nbr_offsets, nbr_index, nbr_angle, work_order,
                               num_work,
                               *out, scratch_of(plan), plan->num_sms, st);
+}
+
+static int validate_dmat(const pg_corr_params *params, const pg_dmat_params *dparams) {
+    int rc = validate_params(params);
+    if (rc) return rc;
+    if (!dparams || dparams->num_model_bins_r_par <= 0 || dparams->num_model_bins_r_trans <= 0)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (params->ang_correlation) return PG_ERR_UNSUPPORTED;
+    return PG_OK;
+}
+
+int pg_cf_dmat_work_bytes(pg_plan *plan, const pg_corr_params *params,
+                          const pg_dmat_params *dparams, int32_t max_pixels1,
+                          int32_t max_pixels2, int64_t max_ctas, uint64_t *bytes) {
+    if (!plan || !bytes) return PG_ERR_INVALID_ARGUMENT;
+    int rc = validate_dmat(params, dparams);
+    if (rc) return rc;
+    if ((rc = select_device(plan))) return rc;
+    DmatConstHost h;
+    if ((rc = dmat_config(*params, *dparams, max_pixels1, max_pixels2, plan->num_sms, h)))
+        return rc;
+    if (max_ctas < 0) return PG_ERR_INVALID_ARGUMENT;
+    const int64_t ctas = max_ctas > 0 ? std::min<int64_t>(max_ctas, h.max_grid) : h.max_grid;
+    *bytes = (uint64_t)ctas * (uint64_t)h.cta_doubles * sizeof(double);
+    return PG_OK;
+}
+
+int pg_cf_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_params *dparams,
+               const pg_forest_set *s1, const pg_forest_set *s2, const double *log_lambda1,
+               const double *log_lambda2, const int32_t *order1, const int32_t *order2,
+               const int32_t *pair_first, const int32_t *pair_second, const double *pair_angle,
+               int64_t num_pairs, void *work, uint64_t work_bytes, const pg_dmat_sums *out,
+               void *stream) {
+    if (!plan || !s1 || !out) return PG_ERR_INVALID_ARGUMENT;
+    int rc = validate_dmat(params, dparams);
+    if (rc) return rc;
+    if ((rc = validate_set(s1, true, false))) return rc;
+    if (s2 && (rc = validate_set(s2, true, false))) return rc;
+    if (!out->weights_dmat || !out->dmat || !out->r_par_eff || !out->r_trans_eff ||
+        !out->z_eff || !out->weight_eff)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (num_pairs < 0 || num_pairs > INT32_MAX) return PG_ERR_INVALID_ARGUMENT;
+    if (num_pairs > 0 && (!pair_first || !pair_second || !log_lambda1 || !order1 || !work))
+        return PG_ERR_INVALID_ARGUMENT;
+    if (s2 && num_pairs > 0 && (!log_lambda2 || !order2)) return PG_ERR_INVALID_ARGUMENT;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    if ((rc = reset_scratch(plan, st))) return rc;
+    const pg_forest_set &other = s2 ? *s2 : *s1;
+    DmatConstHost h;
+    if ((rc = dmat_config(*params, *dparams, s1->max_pixels, other.max_pixels, plan->num_sms, h)))
+        return rc;
+    const uint64_t per_cta = (uint64_t)h.cta_doubles * sizeof(double);
+    const uint64_t fit = work_bytes / per_cta;
+    const int grid = (int)std::min<uint64_t>((uint64_t)h.max_grid, fit);
+    if (num_pairs > 0 && grid < 1) return PG_ERR_INVALID_ARGUMENT;
+    if (reinterpret_cast<uintptr_t>(work) % 16) return PG_ERR_INVALID_ARGUMENT;
+    return launch_cf_dmat(*params, *dparams, h, *s1, other, log_lambda1,
+                          s2 ? log_lambda2 : log_lambda1, order1, s2 ? order2 : order1,
+                          pair_first, pair_second, pair_angle, num_pairs,
+                          static_cast<double *>(work), grid, *out, scratch_of(plan), st);
 }
 
 static int validate_spectra(const pg_spectra *sp) {

@@ -212,6 +212,24 @@ int launch_xcf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &fo
                        const pg_xi_rows &out, Scratch *scratch, void *fast_const, int num_sms,
                        cudaStream_t stream);
 
+// Distortion matrix (pg_dmat.cu). Default number of U and E rows a CTA keeps
+// before the bins of one forest pair are split into chunks.
+constexpr int64_t kDmatRowCapacity = 512;
+struct DmatConstHost {
+    size_t smem;
+    int32_t p1, p2, mwords, dwords;
+    int64_t list_doubles, work_doubles, cta_doubles;
+    int max_grid;
+};
+int dmat_config(const pg_corr_params &p, const pg_dmat_params &d, int p1, int p2, int num_sms,
+                DmatConstHost &h);
+int launch_cf_dmat(const pg_corr_params &p, const pg_dmat_params &d, const DmatConstHost &h,
+                   const pg_forest_set &s1, const pg_forest_set &s2, const double *ll1,
+                   const double *ll2, const int32_t *order1, const int32_t *order2,
+                   const int32_t *pair_first, const int32_t *pair_second,
+                   const double *pair_angle, int64_t num_pairs, double *work, int grid,
+                   const pg_dmat_sums &out, Scratch *scratch, cudaStream_t stream);
+
 int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *start,
                     const int32_t *index, int64_t count, int max_iter, double tol, int mode,
                     const pg_cont_fit &out, Scratch *scratch, int num_sms, cudaStream_t stream);

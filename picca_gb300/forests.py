@@ -14,7 +14,7 @@ import numpy as np
 PIXEL_FIELDS = ("z", "r_comov", "dist_m", "weights", "delta", "log_lambda")
 FOREST_F64 = ("ra", "dec", "x_cart", "y_cart", "z_cart", "cos_dec", "z_qso",
               "obj_r_comov", "obj_dist_m", "obj_weight")
-FOREST_I64 = ("thingid", "plate", "fiberid", "healpix")
+FOREST_I64 = ("thingid", "plate", "fiberid", "healpix", "order")
 
 
 class ForestSet:
@@ -24,7 +24,8 @@ class ForestSet:
     ``delta``, ``log_lambda``, indexed through ``pix_offset`` (int64,
     ``num + 1``). Per-forest arrays: positions and redshift (float64), ids
     (int64), ``healpix`` and ``row`` (int32, rank of the healpix among
-    ``healpix_list``). Quasar sets carry ``obj_r_comov``, ``obj_dist_m`` and
+    ``healpix_list``), ``order`` (int64, the continuum polynomial order of
+    the deltas, -1 when unknown). Quasar sets carry ``obj_r_comov``, ``obj_dist_m`` and
     ``obj_weight`` and no pixels.
     """
 
@@ -40,6 +41,8 @@ class ForestSet:
         for key in FOREST_F64:
             if not hasattr(self, key):
                 setattr(self, key, np.zeros(self.num))
+        if not hasattr(self, "order"):
+            self.order = np.full(self.num, -1, dtype=np.int64)
         for key in FOREST_I64:
             if not hasattr(self, key):
                 setattr(self, key, np.zeros(self.num, dtype=np.int64))
@@ -95,6 +98,8 @@ class ForestSet:
             thingid=np.array([d.thingid for d in deltas], dtype=np.int64),
             plate=np.array([d.plate for d in deltas], dtype=np.int64),
             fiberid=np.array([0 if fiber_is_str else f for f in fiberid], dtype=np.int64),
+            order=np.array([-1 if getattr(d, "order", None) is None else int(d.order)
+                            for d in deltas], dtype=np.int64),
             healpix=hp_of, healpix_list=np.array(keys, dtype=np.int64),
             fiberid_is_str=fiber_is_str,
         )

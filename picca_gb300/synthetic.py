@@ -109,7 +109,7 @@ def make_forests(num, seed, ra_range_deg, dec_range_deg, z_lo=2.1, z_hi=3.5, z_l
         y_cart=np.sin(ra[order]) * np.cos(dec[order]), z_cart=np.sin(dec[order]),
         cos_dec=np.cos(dec[order]), z_qso=z_qso[order], thingid=thingid[order],
         plate=np.zeros(num, dtype=np.int64), fiberid=np.zeros(num, dtype=np.int64),
-        healpix=healpix[order])
+        order=np.full(num, 1 if project else 0, dtype=np.int64), healpix=healpix[order])
 
 
 def _gather_pixels(offset, order):
