@@ -65,6 +65,9 @@ def parse():
                         "work items of the workload and exit (no timing, no JSON line)")
     p.add_argument("--config2", action="store_true",
                    help="also run the 400k-forest auto and 600k-quasar cross correlations")
+    p.add_argument("--dmat-reject", type=float, default=0.99,
+                   help="random rejection of the distortion-matrix leg (picca_dmat.py --rej); "
+                        "a value >= 1 skips the leg")
     p.add_argument("--continuum-correlation", type=int, default=50_000,
                    help="forests whose plain- and learned-fit deltas are correlated (0 skips)")
     return p.parse_args()
@@ -177,6 +180,156 @@ def cpu_sample(fs, params, ang_max, seconds, cfg):
     cand = int((npix[sample] * (csum[offsets[1:]] - csum[offsets[:-1]])).sum())
     return cand / elapsed, (f"{len(sample)} forests with all their neighbours, from "
                             f"{len(rows)} healpix of config {cfg}; {elapsed:.1f} s"), cores
+
+
+def fp64_peak_tflops():
+    """FP64 throughput of this GPU measured live: cuBLAS DGEMM 4096^3, best
+    of 3 (CUDA events)."""
+    import torch
+    n = 4096
+    a = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    b = torch.randn(n, n, dtype=torch.float64, device="cuda")
+    torch.matmul(a, b)
+    best = float("inf")
+    for _ in range(3):
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record()
+        torch.matmul(a, b)
+        e1.record()
+        torch.cuda.synchronize()
+        best = min(best, e0.elapsed_time(e1) / 1e3)
+    return 2.0 * n ** 3 / best / 1e12
+
+
+def dmat_cpu_sample(fs, params, dparams, pairs_host, seconds):
+    """The oracle's forest-pair restatement of
+    cf.compute_dmat_forest_pairs_fast on a bounded sample of the selected
+    forest pairs, on every host core (threads: the ctypes call releases the
+    GIL). Returns (forest pairs/s, pixel pairs/s, sample description,
+    threads)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import cpu as ocpu
+    from oracle import dmat as odm
+    cores = os.cpu_count() or 1
+    op = odm.make_params(params["r_par_min"], params["r_par_max"], params["r_trans_max"],
+                         params["num_bins_r_par"], params["num_bins_r_trans"],
+                         redshift_evolution=bool(dparams.redshift_evolution))
+    po = np.asarray(fs.pix_offset)
+    first, second = pairs_host
+    rng = np.random.default_rng(9)
+
+    def work(chunk):
+        out = odm.new_outputs(op)
+        npp = 0
+        for f, g in chunk:
+            a = slice(po[f], po[f + 1])
+            b = slice(po[g], po[g + 1])
+            ang = ocpu.lib().oracle_angle(fs.x_cart[f], fs.y_cart[f], fs.z_cart[f], fs.ra[f],
+                                          fs.dec[f], fs.cos_dec[f], fs.x_cart[g], fs.y_cart[g],
+                                          fs.z_cart[g], fs.ra[g], fs.dec[g])
+            odm.forest_pair(op, fs.log_lambda[a], fs.log_lambda[b], fs.r_comov[a],
+                            fs.r_comov[b], fs.dist_m[a], fs.dist_m[b], fs.z[a], fs.z[b],
+                            fs.weights[a], fs.weights[b], fs.z_qso[f], fs.z_qso[g], ang, False,
+                            int(fs.order[f]), int(fs.order[g]), out)
+            npp += (po[f + 1] - po[f]) * (po[g + 1] - po[g])
+        return npp
+
+    order = rng.permutation(len(first))
+    n = npp = 0
+    elapsed = 0.0
+    with ThreadPoolExecutor(cores) as ex:
+        while elapsed < seconds and n < len(order):
+            pick = order[n:n + 8 * cores]
+            chunks = [list(zip(first[pick[k::cores]], second[pick[k::cores]]))
+                      for k in range(cores)]
+            t0 = time.perf_counter()
+            npp += sum(ex.map(work, chunks))
+            elapsed += time.perf_counter() - t0
+            n += len(pick)
+    return (n / elapsed, npp / elapsed,
+            f"{n} selected forest pairs of the same workload (random), {elapsed:.1f} s", cores)
+
+
+def dmat_leg(args, fs, params, ang_max, cpu_seconds):
+    """Distortion matrix (picca_dmat.py defaults: 50 x 50 bins, r 0-200 Mpc/h,
+    model bins = data bins, redshift evolution) of the same forests with
+    --rej args.dmat_reject: one warm-up and one timed kernel launch over
+    every selected forest pair (CUDA events on the launching stream), the
+    whole host-to-host call (upload, neighbours, random rejection, kernel,
+    download, normalisation) timed by the wall clock, and the oracle on a
+    sample of the selected pairs."""
+    import torch
+
+    from picca_gb300 import dmat, pairs
+    if args.dmat_reject >= 1.0:
+        return None
+    cparams = pairs.make_params(ang_max=ang_max, **params)
+    dparams = dmat.make_dmat_params(params["num_bins_r_par"], params["num_bins_r_trans"])
+    engine = dmat.DmatEngine()
+    pe = engine.engine
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    res = dmat.distortion_matrix(fs, None, cparams, dparams, args.dmat_reject, nproc=1,
+                                 engine=engine)
+    torch.cuda.synchronize()
+    e2e_first = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    res = dmat.distortion_matrix(fs, None, cparams, dparams, args.dmat_reject, nproc=1,
+                                 engine=engine)
+    torch.cuda.synchronize()
+    e2e_s = time.perf_counter() - t0
+    # kernel alone
+    dev = pairs.DeviceForests(fs, pe.device)
+    offsets, index, total = pe.neighbours(cparams, dev)
+    mask = dmat.selection_mask(fs.healpix_list, fs.row, offsets.cpu().numpy(), 1,
+                               args.dmat_reject)
+    first, second, nsel = engine.pair_list(dev, None, offsets, index, mask)
+    side = dmat.DmatEngine.side_arrays(dev, pe.device)
+    stream = torch.cuda.current_stream()
+    times = []
+    for _ in range(2):
+        sums = engine.alloc_sums(cparams, dparams)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        engine.accumulate(cparams, dparams, dev, None, side, None, first, second, nsel, sums)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+        stats = pe.stats()
+    kernel_s = times[-1]
+    f_h, g_h = first.cpu().numpy()[:nsel], second.cpu().numpy()[:nsel]
+    npix = dev.npix
+    pixel_pairs = float(np.sum(npix[f_h].astype(np.float64) * npix[g_h]))
+    macs = float(stats.gemm_macs)
+    peak = fp64_peak_tflops()
+    achieved = 2.0 * macs / kernel_s / 1e12
+    del dev, sums, side, first, second, offsets, index
+    torch.cuda.empty_cache()
+    cpu_pairs, cpu_pix, cpu_desc, cores = dmat_cpu_sample(fs, params, dparams, (f_h, g_h),
+                                                          cpu_seconds)
+    return {
+        "metric": "distortion-matrix forest pairs per second",
+        "value": nsel / kernel_s, "unit": "forest-pairs/s",
+        "pixel_pairs_per_s": pixel_pairs / kernel_s, "kernel_ms": kernel_s * 1e3,
+        "dtype": "f64",
+        "config": {"workload": "same forests, 50x50 data bins = model bins, r 0-200 Mpc/h, "
+                   "redshift evolution, random rejection %.2f (one chunk)" % args.dmat_reject,
+                   "neighbour_pairs": int(res["NPALL"]), "selected_forest_pairs": int(nsel),
+                   "pixel_pairs": pixel_pairs},
+        "e2e": {"value": nsel / e2e_s, "unit": "forest-pairs/s", "seconds": e2e_s,
+                "first_call_seconds": e2e_first},
+        "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+                     "frac": achieved / peak, "gemm_macs": macs,
+                     "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
+                     "achieved_counts": "2 x multiply-adds of the per-pair U E^T products"},
+        "cpu_baseline": {"value": cpu_pairs, "unit": "forest-pairs/s",
+                         "pixel_pairs_per_s": cpu_pix, "cores": cores, "kind": "port",
+                         "sample": cpu_desc},
+    }
 
 
 def continuum_leg(args, cpu_seconds):
@@ -589,6 +742,8 @@ def run_ours(args):
     num_pixels, resident_bytes = int(dev.num_pixels), int(dev.h2d_bytes)
     del dev, packed, engine
     torch.cuda.empty_cache()
+    dm = dmat_leg(args, fs, params, ang_max, args.cpu_seconds)
+    print("dmat leg: " + json.dumps(dm), file=sys.stderr, flush=True)
     cont = continuum_leg(args, args.cpu_seconds)
     cfg2 = config2_leg(args) if args.config2 else None
     print("continuum leg: " + json.dumps(cont), file=sys.stderr, flush=True)
@@ -623,6 +778,7 @@ def run_ours(args):
         "cpu_baseline": {"value": cpu_val, "unit": "pixel-pairs/s", "cores": cores,
                          "kind": "port", "sample": cpu_desc},
         "continuum": cont,
+        "dmat": dm,
     }
     if cfg2 is not None:
         line["config2"] = cfg2

@@ -103,6 +103,8 @@ typedef struct pg_run_stats {
     int64_t rechecked_pairs;    /* FP32_GUARD: pairs re-decided in FP64       */
     int64_t recheck_overflows;  /* FP32_GUARD: early recheck-queue drains     */
     int64_t work_items;         /* work items processed                        */
+    int64_t gemm_macs;          /* pg_cf_dmat: multiply-adds of the per-pair
+                                   products of the eta terms               */
     int64_t visited_pairs;      /* FP32_GUARD cf: pixel-pair slots evaluated
                                    (after the per-block pixel windows)         */
 } pg_run_stats;

@@ -67,7 +67,8 @@ class DmatSumsC(ctypes.Structure):
 class RunStats(ctypes.Structure):
     _fields_ = [("status", ctypes.c_int32), ("error_detail", ctypes.c_int32),
                 ("rechecked_pairs", ctypes.c_int64), ("recheck_overflows", ctypes.c_int64),
-                ("work_items", ctypes.c_int64), ("visited_pairs", ctypes.c_int64)]
+                ("work_items", ctypes.c_int64), ("gemm_macs", ctypes.c_int64),
+                ("visited_pairs", ctypes.c_int64)]
 
 
 _LIB = None

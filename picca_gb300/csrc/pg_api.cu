@@ -151,6 +151,7 @@ int pg_plan_stats(pg_plan *plan, pg_run_stats *stats) {
     stats->recheck_overflows = (int64_t)host.recheck_overflows;
     stats->work_items = (int64_t)host.work_items;
     stats->visited_pairs = (int64_t)host.visited_pairs;
+    stats->gemm_macs = (int64_t)host.gemm_macs;
     return PG_OK;
 }
 

@@ -25,7 +25,7 @@
 //      bins in registers; the row sweep also adds the Kronecker term
 //      w12 * zfac and the effective (r_par, r_trans, z, weight) sums,
 //   3. reduces the four rank rows,
-//   4. multiplies U by E^T in 64 x 64 FP64 tiles and adds the tile to the
+//   4. multiplies U by E^T in 32 x 32 FP64 tiles and adds the tile to the
 //      global matrix with atomics.
 // All arithmetic is FP64 (the library is compiled with -fmad=false); sums
 // are reassociated with respect to the reference, so results agree to a few
@@ -39,7 +39,7 @@ namespace {
 
 constexpr int kDmBlock = 256;
 constexpr int kDmWarps = kDmBlock / 32;
-constexpr int kTile = 64;   // GEMM output tile edge (data bins x model bins)
+constexpr int kTile = 32;   // GEMM output tile edge (data bins x model bins)
 constexpr int kSlab = 16;   // GEMM reduction step
 constexpr int kTilePad = kTile + 1;
 
@@ -48,6 +48,7 @@ struct DmatConst {
     int32_t nmp, nmt, nm;    // model bins along r_par, r_trans, total
     int32_t redshift_evolution;
     double z_ref, alpha, alpha2;
+    double inv_r_par_range, inv_r_trans_max;  // reciprocals for the bin estimate
     int32_t p1, p2;          // pixel capacity of the shared-memory forest slots
     int32_t mwords, dwords;  // bitmap words (model, data)
     int64_t list_doubles;    // per-CTA scratch: bin lists (nm + nb int32), in doubles
@@ -87,8 +88,21 @@ struct DmPair {
     bool zsel;     // passes the z_min / z_max cut
 };
 
+// floor(x * n) of the reference for x = num / den, from an estimate
+// x' = num * (1 / den) (a few ulp from x): the estimate decides unless
+// x' * n is within 1e-9 of an integer, where the exact quotient is formed.
+__device__ __forceinline__ double dm_floor_bin(double est, double num, double den, int32_t n) {
+    const double y = __dmul_rn(est, (double)n);
+    const double f = floor(y);
+    if (__dsub_rn(y, f) > 1e-9 && __dsub_rn(__dadd_rn(f, 1.), y) > 1e-9) return f;
+    return floor(__dmul_rn(num / den, (double)n));
+}
+
 // Pixel-pair decision and bins of compute_dmat_forest_pairs_fast
-// (py/picca/cf.py:544-568 and :620-700), in the reference's operation order.
+// (py/picca/cf.py:544-568 and :620-700), in the reference's operation order;
+// the bin quotients (r_par - r_par_min) / (r_par_max - r_par_min) and
+// r_trans / r_trans_max are estimated with reciprocals and formed exactly
+// only next to a bin edge (dm_floor_bin).
 __device__ __forceinline__ bool dm_pair(const DmatConst &c, double r1, double m1, double z1,
                                         double r2, double m2, double z2, double cc, double ss,
                                         bool shp, DmPair &o) {
@@ -100,13 +114,14 @@ __device__ __forceinline__ bool dm_pair(const DmatConst &c, double r1, double m1
     }
     if (!c.b.x_correlation) rp = fabs(rp);
     if (rp >= c.b.r_par_max || rt >= c.b.r_trans_max || rp < c.b.r_par_min) return false;
-    const double fp = __dsub_rn(rp, c.b.r_par_min) / c.b.r_par_range;
-    const double ft = rt / c.b.r_trans_max;
-    const double bp = floor(__dmul_rn(fp, (double)c.b.np));
-    const double bt = floor(__dmul_rn(ft, (double)c.b.nt));
+    const double np_num = __dsub_rn(rp, c.b.r_par_min);
+    const double fp = __dmul_rn(np_num, c.inv_r_par_range);
+    const double ft = __dmul_rn(rt, c.inv_r_trans_max);
+    const double bp = dm_floor_bin(fp, np_num, c.b.r_par_range, c.b.np);
+    const double bt = dm_floor_bin(ft, rt, c.b.r_trans_max, c.b.nt);
     o.db = (int32_t)__dadd_rn(bt, __dmul_rn((double)c.b.nt, bp));
-    const double mp = floor(__dmul_rn(fp, (double)c.nmp));
-    const double mt = floor(__dmul_rn(ft, (double)c.nmt));
+    const double mp = dm_floor_bin(fp, np_num, c.b.r_par_range, c.nmp);
+    const double mt = dm_floor_bin(ft, rt, c.b.r_trans_max, c.nmt);
     o.mb = (int32_t)__dadd_rn(mt, __dmul_rn((double)c.nmt, mp));
     o.z = __dadd_rn(z1, z2) / 2;
     o.counted = !(c.b.remove_shp && shp && fabs(rp) < c.b.half_plate_cut);
@@ -590,15 +605,18 @@ __global__ void __launch_bounds__(kDmBlock)
                 }
                 __syncthreads();
 
-                // 4. D = U E^T in 64 x 64 tiles, added to the global matrix
+                // 4. D = U E^T in 32 x 32 tiles, added to the global matrix
+                if (tid == 0)
+                    atomicAdd(&scratch->gemm_macs,
+                              (unsigned long long)dcc * (unsigned long long)mcc * (kR + 4));
                 const int tx = tid & 15, ty = tid >> 4;
                 for (int td = 0; td < dcc; td += kTile) {
                     for (int tm = 0; tm < mcc; tm += kTile) {
-                        double acc[4][4];
+                        double acc[2][2];
 #pragma unroll
-                        for (int a = 0; a < 4; ++a)
+                        for (int a = 0; a < 2; ++a)
 #pragma unroll
-                            for (int b2 = 0; b2 < 4; ++b2) acc[a][b2] = 0.;
+                            for (int b2 = 0; b2 < 2; ++b2) acc[a][b2] = 0.;
                         for (int k0 = 0; k0 < kst; k0 += kSlab) {
                             for (int e = tid; e < kTile * kSlab; e += kDmBlock) {
                                 const int rr = e / kSlab, kk = e % kSlab;
@@ -608,26 +626,26 @@ __global__ void __launch_bounds__(kDmBlock)
                             __syncthreads();
 #pragma unroll
                             for (int kk = 0; kk < kSlab; ++kk) {
-                                double av[4], bv[4];
+                                double av[2], bv[2];
 #pragma unroll
-                                for (int a = 0; a < 4; ++a) av[a] = ta[kk][ty + 16 * a];
+                                for (int a = 0; a < 2; ++a) av[a] = ta[kk][ty + 16 * a];
 #pragma unroll
-                                for (int b2 = 0; b2 < 4; ++b2) bv[b2] = tb[kk][tx + 16 * b2];
+                                for (int b2 = 0; b2 < 2; ++b2) bv[b2] = tb[kk][tx + 16 * b2];
 #pragma unroll
-                                for (int a = 0; a < 4; ++a)
+                                for (int a = 0; a < 2; ++a)
 #pragma unroll
-                                    for (int b2 = 0; b2 < 4; ++b2)
+                                    for (int b2 = 0; b2 < 2; ++b2)
                                         acc[a][b2] = __fma_rn(av[a], bv[b2], acc[a][b2]);
                             }
                             __syncthreads();
                         }
 #pragma unroll
-                        for (int a = 0; a < 4; ++a) {
+                        for (int a = 0; a < 2; ++a) {
                             const int dl = td + ty + 16 * a;
                             if (dl >= dcc) continue;
                             const int64_t base = (int64_t)dlist[d0 + dl] * nm;
 #pragma unroll
-                            for (int b2 = 0; b2 < 4; ++b2) {
+                            for (int b2 = 0; b2 < 2; ++b2) {
                                 const int ml = tm + tx + 16 * b2;
                                 if (ml < mcc && acc[a][b2] != 0.)
                                     atomicAdd(&out.dmat[base + mlist[m0 + ml]], acc[a][b2]);
@@ -694,6 +712,8 @@ int launch_cf_dmat(const pg_corr_params &p, const pg_dmat_params &d, const DmatC
     c.z_ref = d.z_ref;
     c.alpha = d.alpha;
     c.alpha2 = d.alpha2;
+    c.inv_r_par_range = 1. / c.b.r_par_range;
+    c.inv_r_trans_max = 1. / c.b.r_trans_max;
     c.p1 = h.p1;
     c.p2 = h.p2;
     c.mwords = h.mwords;

@@ -28,6 +28,7 @@ struct Scratch {
     unsigned long long recheck_overflows;
     unsigned long long work_items;
     unsigned long long visited_pairs;  // pixel-pair slots evaluated by the fast cf kernel
+    unsigned long long gemm_macs;      // distortion matrix: multiply-adds of the U E^T products
     // ordered-integer encodings of FP64 data ranges (guard-band inputs)
     unsigned long long r_min_key, r_max_key, d_max_key;
 };
