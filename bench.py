@@ -68,6 +68,10 @@ def parse():
     p.add_argument("--dmat-reject", type=float, default=0.99,
                    help="random rejection of the distortion-matrix leg (picca_dmat.py --rej); "
                         "a value >= 1 skips the leg")
+    p.add_argument("--dmat-only", action="store_true",
+                   help="run only the distortion-matrix leg on --config (prints its JSON)")
+    p.add_argument("--dmat-product", choices=["split_bf16", "fp64"], default="split_bf16",
+                   help="arithmetic of the eta products in the distortion-matrix leg")
     p.add_argument("--continuum-correlation", type=int, default=50_000,
                    help="forests whose plain- and learned-fit deltas are correlated (0 skips)")
     return p.parse_args()
@@ -266,7 +270,8 @@ def dmat_leg(args, fs, params, ang_max, cpu_seconds):
     if args.dmat_reject >= 1.0:
         return None
     cparams = pairs.make_params(ang_max=ang_max, **params)
-    dparams = dmat.make_dmat_params(params["num_bins_r_par"], params["num_bins_r_trans"])
+    dparams = dmat.make_dmat_params(params["num_bins_r_par"], params["num_bins_r_trans"],
+                                    product=args.dmat_product)
     engine = dmat.DmatEngine()
     pe = engine.engine
     torch.cuda.synchronize()
@@ -315,7 +320,9 @@ def dmat_leg(args, fs, params, ang_max, cpu_seconds):
         "metric": "distortion-matrix forest pairs per second",
         "value": nsel / kernel_s, "unit": "forest-pairs/s",
         "pixel_pairs_per_s": pixel_pairs / kernel_s, "kernel_ms": kernel_s * 1e3,
-        "dtype": "f64",
+        "dtype": "f32 geometry + f64 sums" + (", bf16 digit products" if
+                                               args.dmat_product == "split_bf16" else
+                                               ", f64 products"),
         "config": {"workload": "same forests, 50x50 data bins = model bins, r 0-200 Mpc/h, "
                    "redshift evolution, random rejection %.2f (one chunk)" % args.dmat_reject,
                    "neighbour_pairs": int(res["NPALL"]), "selected_forest_pairs": int(nsel),
@@ -585,6 +592,10 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     fs, params, ang_max = make_workload(args.config)
+    if args.dmat_only:
+        if rank == 0:
+            print(json.dumps(dmat_leg(args, fs, params, ang_max, args.cpu_seconds)), flush=True)
+        return
     mode = pairs.MODE_FP32_GUARD if args.precision == "fp32_guard" else pairs.MODE_FP64
     cparams = pairs.make_params(ang_max=ang_max, **params)
     engine = pairs.PairEngine()

@@ -341,11 +341,19 @@ int pg_mlp_features(pg_plan *plan, const pg_spectra *spectra, const pg_cont_mode
  * module globals num_model_bins_r_par / _r_trans,
  * redshift_evolution_in_distortion_matrix, z_ref, alpha, alpha2 set by
  * py/picca/bin/picca_dmat.py:366-400). */
+#define PG_DMAT_FP64 0        /* eta products in FP64 on the CUDA cores          */
+#define PG_DMAT_SPLIT_BF16 1  /* eta products on the BF16 tensor cores: rows scaled
+                                 by powers of two, 48-bit fixed point split into
+                                 six 8-bit digits, exact digit products and
+                                 integer level sums (error below 2^-46 of the
+                                 largest |row| x |column| product)            */
 typedef struct pg_dmat_params {
     int32_t num_model_bins_r_par, num_model_bins_r_trans;
     int32_t redshift_evolution;
     int32_t row_capacity;  /* data + model bins of one forest pair held at once
                               (0: 512); more are processed in chunks        */
+    int32_t product;       /* PG_DMAT_FP64 or PG_DMAT_SPLIT_BF16             */
+    int32_t reserved;
     double z_ref, alpha, alpha2;
 } pg_dmat_params;
 

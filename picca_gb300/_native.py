@@ -13,6 +13,8 @@ LIB_PATH = os.path.join(HERE, "libpicca_gb300.so")
 PG_OK = 0
 PG_MODE_FP64 = 0
 PG_MODE_FP32_GUARD = 1
+PG_DMAT_FP64 = 0
+PG_DMAT_SPLIT_BF16 = 1
 
 _P = ctypes.POINTER
 _c_double_p = ctypes.c_void_p  # device pointers are passed as integers
@@ -56,6 +58,7 @@ class XiRowsC(ctypes.Structure):
 class DmatParamsC(ctypes.Structure):
     _fields_ = [("num_model_bins_r_par", ctypes.c_int32), ("num_model_bins_r_trans", ctypes.c_int32),
                 ("redshift_evolution", ctypes.c_int32), ("row_capacity", ctypes.c_int32),
+                ("product", ctypes.c_int32), ("reserved", ctypes.c_int32),
                 ("z_ref", ctypes.c_double), ("alpha", ctypes.c_double), ("alpha2", ctypes.c_double)]
 
 

@@ -67,6 +67,9 @@ remove_same_half_plate_close_pairs = False
 
 # variables for distortion matrix
 redshift_evolution_in_distortion_matrix = True
+# arithmetic of the distortion-matrix eta products: "split_bf16" (tensor
+# cores, exact 8-bit digit products) or "fp64"
+dmat_product = "split_bf16"
 
 # arithmetic of the GPU pair kernel: "fp64" or "fp32_guard"
 precision = "fp32_guard"
@@ -252,7 +255,7 @@ def _dmat_params():
         z_ref=2.25 if z_ref is None else z_ref, alpha=2.9 if alpha is None else alpha,
         alpha2=(alpha if alpha2 is None else alpha2) if alpha is not None else 2.9,
         num_model_bins_r_par=num_model_bins_r_par,
-        num_model_bins_r_trans=num_model_bins_r_trans)
+        num_model_bins_r_trans=num_model_bins_r_trans, product=dmat_product)
 
 
 def _dmat_engine():

@@ -18,7 +18,11 @@
 // over the selected pairs of the bin. The kernel therefore
 //   1. classifies every pixel pair (bitmaps of the touched model bins and of
 //      the data bins of selected pairs; the reference's early return when no
-//      pair counts),
+//      pair counts). The geometry runs in FP32 (r as an FP32 hi/lo pair) with
+//      guard bands that bound its distance to the reference's FP64 values;
+//      pairs inside a guard band (a range limit, a bin edge, the half-plate
+//      cut) are decided in FP64 with the reference's expressions, so every
+//      decision and bin is the reference's,
 //   2. builds U (data bins x kappa) and E (model bins x kappa) in per-CTA
 //      global scratch with a row sweep (a thread per pixel of forest 1) and a
 //      column sweep (a thread per pixel of forest 2), merging runs of equal
@@ -27,9 +31,11 @@
 //   3. reduces the four rank rows,
 //   4. multiplies U by E^T in 32 x 32 FP64 tiles and adds the tile to the
 //      global matrix with atomics.
-// All arithmetic is FP64 (the library is compiled with -fmad=false); sums
-// are reassociated with respect to the reference, so results agree to a few
-// ulp of the summed magnitudes, not bit for bit.
+// Sums are FP64 (the library is compiled with -fmad=false) and reassociated
+// with respect to the reference (run sums of per-pixel factors, scaled once
+// per run), so results agree to a few ulp of the summed magnitudes, not bit
+// for bit; the product is FP64 on the CUDA cores or exact 8-bit digit
+// products on the tensor cores (PG_DMAT_SPLIT_BF16).
 #include <algorithm>
 
 #include "pg_internal.cuh"
@@ -42,6 +48,16 @@ constexpr int kDmWarps = kDmBlock / 32;
 constexpr int kTile = 32;   // GEMM output tile edge (data bins x model bins)
 constexpr int kSlab = 16;   // GEMM reduction step
 constexpr int kTilePad = kTile + 1;
+// Tensor-core form of the product (PG_DMAT_SPLIT_BF16): each FP64 row is
+// scaled by a power of two to |x| < 1, rounded to 48 fractional bits and
+// written as six signed 8-bit digits (exact in bf16). Products of digits
+// are exact in the FP32 accumulators of mma.sync m16n8k16; the 21 digit
+// pairs with p + q <= 5 (0-based) are summed per level p + q over 16
+// reduction steps (|sum| <= 2^21), moved into 32-bit integer level sums
+// (exact) and combined in FP64 at the end.
+constexpr int kSlices = 6;
+constexpr int kTcM = 32, kTcN = 32, kTcK = 32;
+constexpr int kTcRow = kTcK + 8;  // bf16 per staged row (pad: conflict-free fragments)
 
 struct DmatConst {
     Binning b;
@@ -49,11 +65,15 @@ struct DmatConst {
     int32_t redshift_evolution;
     double z_ref, alpha, alpha2;
     double inv_r_par_range, inv_r_trans_max;  // reciprocals for the bin estimate
+    double sp, smp, st, smt;  // bins per unit: np / range, nmp / range, nt / rt_max, nmt / rt_max
+    float f_rpmin, f_rpmax, f_rtmax, f_hpc;   // FP32 limits and half-plate cut
+    float f_sp, f_smp, f_st, f_smt;
     int32_t p1, p2;          // pixel capacity of the shared-memory forest slots
     int32_t mwords, dwords;  // bitmap words (model, data)
     int64_t list_doubles;    // per-CTA scratch: bin lists (nm + nb int32), in doubles
     int64_t work_doubles;    // per-CTA scratch: U and E rows
-    int64_t cta_doubles;     // list_doubles + work_doubles
+    int64_t cta_doubles;     // list_doubles + work_doubles (+ digits and exponents)
+    int32_t split;           // 1: tensor-core product (PG_DMAT_SPLIT_BF16)
 };
 
 // Shared-memory layout (bytes), identical on host and device.
@@ -63,11 +83,12 @@ struct DmSmem {
 
 __host__ __device__ inline size_t dm_align(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-__host__ __device__ inline DmSmem dm_smem(int p1, int p2, int mwords, int dwords) {
+__host__ __device__ inline DmSmem dm_smem(int p1, int p2, int mwords, int dwords, int split) {
     DmSmem s;
     size_t o = 0;
-    s.f1 = o; o += sizeof(double) * 6 * (size_t)p1;
-    s.f2 = o; o += sizeof(double) * 6 * (size_t)p2;
+    s.f1 = o; o += (sizeof(double) * 9 + sizeof(float) * 3) * (size_t)p1;
+    o = dm_align(o, 16);
+    s.f2 = o; o += (sizeof(double) * 12 + sizeof(float) * 3) * (size_t)p2;
     s.flags1 = o; o = dm_align(o + (size_t)p1, 8);
     s.flags2 = o; o = dm_align(o + (size_t)p2, 8);
     s.mbits = o; o += sizeof(uint32_t) * (size_t)mwords;
@@ -75,8 +96,13 @@ __host__ __device__ inline DmSmem dm_smem(int p1, int p2, int mwords, int dwords
     s.dbits = o; o += sizeof(uint32_t) * (size_t)dwords;
     s.dpref = o; o += sizeof(int32_t) * (size_t)dwords;
     o = dm_align(o, 16);
-    s.tile_a = o; o += sizeof(double) * kSlab * kTilePad;
-    s.tile_b = o; o += sizeof(double) * kSlab * kTilePad;
+    if (split) {
+        s.tile_a = o; o += sizeof(uint16_t) * kSlices * kTcM * kTcRow;
+        s.tile_b = o; o += sizeof(uint16_t) * kSlices * kTcN * kTcRow;
+    } else {
+        s.tile_a = o; o += sizeof(double) * kSlab * kTilePad;
+        s.tile_b = o; o += sizeof(double) * kSlab * kTilePad;
+    }
     s.total = dm_align(o, 16);
     return s;
 }
@@ -137,6 +163,31 @@ __device__ __forceinline__ int dm_rank(const uint32_t *bits, const int32_t *pref
     return pref[w] + __popc(below);
 }
 
+// round(x * 2^(48 - e)) for |x| < 2^e (zero and subnormal x give 0).
+__device__ __forceinline__ long long dm_fixed48(double x, int e) {
+    const long long bits = __double_as_longlong(x);
+    const int ex = (int)((bits >> 52) & 0x7FF);
+    if (ex == 0) return 0;
+    const long long man = (bits & 0xFFFFFFFFFFFFFLL) | 0x10000000000000LL;
+    const int sh = 1075 - 48 + e - ex;  // right shift (>= 5 for |x| < 2^e)
+    const long long m = sh >= 63 ? 0 : (man + (1LL << (sh - 1))) >> sh;
+    return bits < 0 ? -m : m;
+}
+
+// bf16 bits of a small integer |v| <= 256 (exact).
+__device__ __forceinline__ uint32_t dm_bf16_small(int v) {
+    const float f = __int_as_float(0x4B400000 + v) - 12582912.f;
+    return __float_as_uint(f) >> 16;
+}
+
+__device__ __forceinline__ void dm_mma(float d[4], const uint32_t a[4], const uint32_t b[2]) {
+    asm volatile(
+        "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 "
+        "{%0,%1,%2,%3}, {%4,%5,%6,%7}, {%8,%9}, {%0,%1,%2,%3};\n"
+        : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+        : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b[0]), "r"(b[1]));
+}
+
 __device__ __forceinline__ double warp_sum(double v) {
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
@@ -184,6 +235,115 @@ __device__ int dm_scan_bits(const uint32_t *bits, int32_t *pref, int words, int 
     return total;
 }
 
+// D = U E^T of one chunk on the tensor cores (see kSlices), added to the
+// global matrix: dmat[dlist[dl] * nm + mlist[ml]] += D[dl][ml]. U is
+// [dcc][kst], E is [mcc][kst] (FP64, zero-padded to kst, a multiple of 16).
+__device__ void dm_product_split(const double *U, const double *E, int dcc, int mcc, int kst,
+                                 uint16_t *digits, int32_t *rexp, uint16_t *sa, uint16_t *sb,
+                                 const int32_t *dlist, const int32_t *mlist, int nm,
+                                 double *dmat) {
+    const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+    // row exponents and digits (a warp per row)
+    for (int r = warp; r < dcc + mcc; r += kDmWarps) {
+        const double *row = r < dcc ? U + (int64_t)r * kst : E + (int64_t)(r - dcc) * kst;
+        double mx = 0.;
+        for (int k = lane; k < kst; k += 32) mx = fmax(mx, fabs(row[k]));
+        for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+        const int ex = (int)((__double_as_longlong(mx) >> 52) & 0x7FF);
+        const int e = ex == 0 ? -1022 : ex - 1022;  // |x| <= mx < 2^e
+        if (lane == 0) rexp[r] = e;
+        uint16_t *dst = digits + (int64_t)r * kSlices * kst;
+        for (int k = lane; k < kst; k += 32) {
+            long long m = dm_fixed48(row[k], e);
+#pragma unroll
+            for (int p = 0; p < kSlices; ++p) {
+                const int sh = 8 * (kSlices - 1 - p);
+                const long long d = sh ? (m + (1LL << (sh - 1))) >> sh : m;
+                m -= d << sh;
+                dst[(int64_t)p * kst + k] = (uint16_t)dm_bf16_small((int)d);
+            }
+        }
+    }
+    __syncthreads();
+    const int group = lane >> 2, tig = lane & 3;
+    const int wm = warp >> 2, wn = warp & 3;  // 2 x 4 warps, 16 x 8 each
+    for (int td = 0; td < dcc; td += kTcM) {
+        for (int tm = 0; tm < mcc; tm += kTcN) {
+            uint32_t lev[kSlices][4];
+#pragma unroll
+            for (int l = 0; l < kSlices; ++l)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) lev[l][q] = 0u;
+            uint32_t drains = 0;
+            for (int k0 = 0; k0 < kst; k0 += kTcK) {
+                // stage the digits of rows [td, td + 32) of U and [tm, tm + 32) of E:
+                // (slice, row, 8-element part) -> one 16-byte copy each
+                constexpr int kParts = kTcK / 8;
+                constexpr int kOne = kSlices * kTcM * kParts;
+                for (int e = tid; e < 2 * kOne; e += kDmBlock) {
+                    const bool isa = e < kOne;
+                    const int f = isa ? e : e - kOne;
+                    const int part = f % kParts;
+                    const int r = (f / kParts) % kTcM;
+                    const int p = f / (kParts * kTcM);
+                    const int grow = (isa ? td : tm) + r;
+                    const int kk = k0 + part * 8;
+                    uint4 v = make_uint4(0u, 0u, 0u, 0u);
+                    if (grow < (isa ? dcc : mcc) && kk < kst) {
+                        const int64_t src_row = isa ? grow : dcc + grow;
+                        v = *reinterpret_cast<const uint4 *>(
+                            digits + (src_row * kSlices + p) * (int64_t)kst + kk);
+                    }
+                    *reinterpret_cast<uint4 *>((isa ? sa : sb) + (p * kTcM + r) * kTcRow +
+                                               part * 8) = v;
+                }
+                __syncthreads();
+#pragma unroll
+                for (int ks = 0; ks < kTcK; ks += 16) {
+                    if (k0 + ks >= kst) break;
+                    uint32_t af[kSlices][4], bf[kSlices][2];
+#pragma unroll
+                    for (int p = 0; p < kSlices; ++p) {
+                        const uint16_t *a0 = sa + (p * kTcM + wm * 16 + group) * kTcRow + ks + tig * 2;
+                        af[p][0] = *reinterpret_cast<const uint32_t *>(a0);
+                        af[p][1] = *reinterpret_cast<const uint32_t *>(a0 + 8 * kTcRow);
+                        af[p][2] = *reinterpret_cast<const uint32_t *>(a0 + 8);
+                        af[p][3] = *reinterpret_cast<const uint32_t *>(a0 + 8 * kTcRow + 8);
+                        const uint16_t *b0 = sb + (p * kTcN + wn * 8 + group) * kTcRow + ks + tig * 2;
+                        bf[p][0] = *reinterpret_cast<const uint32_t *>(b0);
+                        bf[p][1] = *reinterpret_cast<const uint32_t *>(b0 + 8);
+                    }
+#pragma unroll
+                    for (int l = 0; l < kSlices; ++l) {
+                        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+#pragma unroll
+                        for (int p = 0; p <= l; ++p) dm_mma(acc, af[p], bf[l - p]);
+                        // exact integers |v| <= 2^21: bits of v + 1.5 * 2^23 carry v
+#pragma unroll
+                        for (int q = 0; q < 4; ++q) lev[l][q] += __float_as_uint(acc[q] + 12582912.f);
+                    }
+                    ++drains;
+                }
+                __syncthreads();
+            }
+            const uint32_t bias = drains * 0x4B400000u;
+#pragma unroll
+            for (int q = 0; q < 4; ++q) {
+                const int dl = td + wm * 16 + group + ((q >> 1) << 3);
+                const int ml = tm + wn * 8 + tig * 2 + (q & 1);
+                if (dl >= dcc || ml >= mcc) continue;
+                double v = 0.;
+#pragma unroll
+                for (int l = kSlices - 1; l >= 0; --l)
+                    v = __fma_rn(v, 0.00390625, (double)(int32_t)(lev[l][q] - bias));
+                // v = sum_l lev_l 2^(-8 l); the level l product carries 2^(-8 (l + 2))
+                v = ldexp(v, rexp[dl] + rexp[dcc + ml] - 16);
+                if (v != 0.) atomicAdd(&dmat[(int64_t)dlist[dl] * nm + mlist[ml]], v);
+            }
+        }
+    }
+}
+
 struct DmItem {
     int32_t n1, n2;
     double cc, ss;
@@ -193,20 +353,102 @@ struct DmItem {
     bool shp;
 };
 
-__global__ void __launch_bounds__(kDmBlock)
+// FP32 form of the pixel-pair geometry of one forest pair, with guard bands
+// that bound its distance to the FP64 computation of the reference.
+struct DmGuard {
+    float cc, ss;             // cos, sin of half the angle
+    float gp, gt;             // |r_par - r_par(FP64)|, |r_trans - r_trans(FP64)| bounds
+    float gyp, gyt, gymp, gymt;  // the same bounds in units of the four bin widths
+};
+
+// Per-pixel slots of the two forests in shared memory (FP64 unless noted).
+struct DmPix {
+    double *r, *m, *z, *w, *dll, *zf;
+    double *a;    // zf w / sum(w)
+    double *b;    // zf w dll / sum(w dll^2)
+    double *wd;   // w dll
+    double *wz;   // w zf       (forest 2 only)
+    double *wzz;  // w z        (forest 2 only)
+    double *wm;   // w dist_m   (forest 2 only)
+    float *rh, *rl, *mf;  // FP32: r = rh + rl, dist_m
+};
+
+__device__ __forceinline__ DmPix dm_pix(unsigned char *base, int p, bool second) {
+    DmPix x;
+    double *d = reinterpret_cast<double *>(base);
+    x.r = d; x.m = d + p; x.z = d + 2 * p; x.w = d + 3 * p; x.dll = d + 4 * p; x.zf = d + 5 * p;
+    x.a = d + 6 * p; x.b = d + 7 * p; x.wd = d + 8 * p;
+    const int nd = second ? 12 : 9;
+    x.wz = second ? d + 9 * p : nullptr;
+    x.wzz = second ? d + 10 * p : nullptr;
+    x.wm = second ? d + 11 * p : nullptr;
+    float *f = reinterpret_cast<float *>(d + nd * p);
+    x.rh = f; x.rl = f + p; x.mf = f + 2 * p;
+    return x;
+}
+
+// FP32 decision of a pixel pair: 0 outside the model range, 1 inside with
+// the bins and the half-plate flag set, 2 too close to a range limit, a bin
+// edge or the half-plate cut for FP32 to decide (the caller uses dm_pair).
+__device__ __forceinline__ int dm_pair_f32(const DmatConst &c, const DmGuard &g, float r1h,
+                                           float r1l, float m1, float r2h, float r2l, float m2,
+                                           bool shp, DmPair &o) {
+    const float d = __fadd_rn(__fsub_rn(r1h, r2h), __fsub_rn(r1l, r2l));
+    float rp = __fmul_rn(d, g.cc);
+    if (!c.b.x_correlation) rp = fabsf(rp);
+    const float rt = __fmul_rn(__fadd_rn(m1, m2), g.ss);
+    if (rp >= c.f_rpmax + g.gp || rt >= c.f_rtmax + g.gt || rp < c.f_rpmin - g.gp) return 0;
+    if (rp > c.f_rpmax - g.gp || rt > c.f_rtmax - g.gt || rp < c.f_rpmin + g.gp) return 2;
+    o.counted = true;
+    if (c.b.remove_shp && shp) {
+        const float a = fabsf(rp);
+        if (fabsf(__fsub_rn(a, c.f_hpc)) <= g.gp) return 2;
+        o.counted = a >= c.f_hpc;
+    }
+    const float xp = __fsub_rn(rp, c.f_rpmin);
+    const float yp = __fmul_rn(xp, c.f_sp), ymp = __fmul_rn(xp, c.f_smp);
+    const float yt = __fmul_rn(rt, c.f_st), ymt = __fmul_rn(rt, c.f_smt);
+    const float bp = floorf(yp), bt = floorf(yt), mp = floorf(ymp), mt = floorf(ymt);
+    if (yp - bp <= g.gyp || bp + 1.f - yp <= g.gyp || yt - bt <= g.gyt ||
+        bt + 1.f - yt <= g.gyt || ymp - mp <= g.gymp || mp + 1.f - ymp <= g.gymp ||
+        ymt - mt <= g.gymt || mt + 1.f - ymt <= g.gymt)
+        return 2;
+    o.db = (int32_t)bt + c.b.nt * (int32_t)bp;
+    o.mb = (int32_t)mt + c.nmt * (int32_t)mp;
+    return 1;
+}
+
+// Decision of pixel pair (i, j): 0 outside, 1 inside (FP32 form; o.rp,
+// o.rt not set), 2 inside (FP64 form, dm_pair: o.rp, o.rt, o.z set). o.zsel
+// is set in both inside cases.
+__device__ __forceinline__ int dm_decide(const DmatConst &c, const DmGuard &g, const DmItem &it,
+                                         const DmPix &p1, const DmPix &p2, int i, int j,
+                                         DmPair &o) {
+    int st = c.b.rmu ? 2
+                     : dm_pair_f32(c, g, p1.rh[i], p1.rl[i], p1.mf[i], p2.rh[j], p2.rl[j],
+                                   p2.mf[j], it.shp, o);
+    if (st == 0) return 0;
+    if (st == 2)
+        return dm_pair(c, p1.r[i], p1.m[i], p1.z[i], p2.r[j], p2.m[j], p2.z[j], it.cc, it.ss,
+                       it.shp, o) ? 2 : 0;
+    o.zsel = true;
+    if (c.b.zmin_on || c.b.zmax_on) {
+        const double z = __dadd_rn(p1.z[i], p2.z[j]) / 2;
+        o.zsel = !((c.b.zmin_on && z < c.b.z_min) || (c.b.zmax_on && z > c.b.z_max));
+    }
+    return 1;
+}
+
+__global__ void __launch_bounds__(kDmBlock, 2)
     cf_dmat_kernel(DmatConst c, pg_forest_set s1, pg_forest_set s2, const double *ll1,
                    const double *ll2, const int32_t *order1g, const int32_t *order2g,
                    const int32_t *pair_first, const int32_t *pair_second,
                    const double *pair_angle, int64_t num_pairs, pg_dmat_sums out,
                    double *work, Scratch *scratch) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const DmSmem L = dm_smem(c.p1, c.p2, c.mwords, c.dwords);
-    double *f1 = reinterpret_cast<double *>(smem + L.f1);
-    double *f2 = reinterpret_cast<double *>(smem + L.f2);
-    double *r1s = f1, *m1s = f1 + c.p1, *z1s = f1 + 2 * c.p1, *w1s = f1 + 3 * c.p1,
-           *d1s = f1 + 4 * c.p1, *zf1s = f1 + 5 * c.p1;
-    double *r2s = f2, *m2s = f2 + c.p2, *z2s = f2 + 2 * c.p2, *w2s = f2 + 3 * c.p2,
-           *d2s = f2 + 4 * c.p2, *zf2s = f2 + 5 * c.p2;
+    const DmSmem L = dm_smem(c.p1, c.p2, c.mwords, c.dwords, c.split);
+    const DmPix P1 = dm_pix(smem + L.f1, c.p1, false);
+    const DmPix P2 = dm_pix(smem + L.f2, c.p2, true);
     unsigned char *sel1 = smem + L.flags1, *sel2 = smem + L.flags2;
     uint32_t *mbits = reinterpret_cast<uint32_t *>(smem + L.mbits);
     int32_t *mpref = reinterpret_cast<int32_t *>(smem + L.mpref);
@@ -214,6 +456,8 @@ __global__ void __launch_bounds__(kDmBlock)
     int32_t *dpref = reinterpret_cast<int32_t *>(smem + L.dpref);
     double (*ta)[kTilePad] = reinterpret_cast<double (*)[kTilePad]>(smem + L.tile_a);
     double (*tb)[kTilePad] = reinterpret_cast<double (*)[kTilePad]>(smem + L.tile_b);
+    uint16_t *ta_raw = reinterpret_cast<uint16_t *>(smem + L.tile_a);
+    uint16_t *tb_raw = reinterpret_cast<uint16_t *>(smem + L.tile_b);
     __shared__ double red[kDmWarps];
     __shared__ int red_int[kDmWarps];
     __shared__ int s_item;
@@ -225,6 +469,9 @@ __global__ void __launch_bounds__(kDmBlock)
     int32_t *dlist = reinterpret_cast<int32_t *>(cta);  // [nb]
     int32_t *mlist = dlist + nb;                         // [nm]
     double *rows = cta + c.list_doubles;
+    // tensor-core form: digits [rows][kSlices][kst] bf16, then row exponents
+    uint16_t *digits = reinterpret_cast<uint16_t *>(rows + c.work_doubles);
+    int32_t *rexp = reinterpret_cast<int32_t *>(digits + (c.work_doubles * kSlices));
 
     for (;;) {
         if (tid == 0) s_item = atomicAdd(&scratch->work_counter, 1);
@@ -259,25 +506,76 @@ __global__ void __launch_bounds__(kDmBlock)
         const double zq1 = s1.z_qso[f], zq2 = s2.z_qso[g];
 
         // stage the pixels
+        double lmax = 0., lmmax = 0.;
         for (int t = tid; t < it.n1; t += kDmBlock) {
-            r1s[t] = s1.r_comov[o1 + t];
-            m1s[t] = s1.dist_m[o1 + t];
-            z1s[t] = s1.z[o1 + t];
-            w1s[t] = s1.weights[o1 + t];
-            d1s[t] = ll1[o1 + t];
-            sel1[t] = !(zerr_on && zerr_veto(z1s[t], zq2, c.b.zerr_kms));
+            const double r = s1.r_comov[o1 + t], m = s1.dist_m[o1 + t];
+            P1.r[t] = r;
+            P1.m[t] = m;
+            P1.z[t] = s1.z[o1 + t];
+            P1.w[t] = s1.weights[o1 + t];
+            P1.dll[t] = ll1[o1 + t];
+            const float rh = (float)r;
+            P1.rh[t] = rh;
+            P1.rl[t] = (float)__dsub_rn(r, (double)rh);
+            P1.mf[t] = (float)m;
+            lmax = fmax(lmax, fabs(r));
+            lmmax = fmax(lmmax, fabs(m));
+            sel1[t] = !(zerr_on && zerr_veto(P1.z[t], zq2, c.b.zerr_kms));
         }
         for (int t = tid; t < it.n2; t += kDmBlock) {
-            r2s[t] = s2.r_comov[o2 + t];
-            m2s[t] = s2.dist_m[o2 + t];
-            z2s[t] = s2.z[o2 + t];
-            w2s[t] = s2.weights[o2 + t];
-            d2s[t] = ll2[o2 + t];
-            sel2[t] = !(zerr_on && zerr_veto(z2s[t], zq1, c.b.zerr_kms));
+            const double r = s2.r_comov[o2 + t], m = s2.dist_m[o2 + t];
+            P2.r[t] = r;
+            P2.m[t] = m;
+            P2.z[t] = s2.z[o2 + t];
+            P2.w[t] = s2.weights[o2 + t];
+            P2.dll[t] = ll2[o2 + t];
+            const float rh = (float)r;
+            P2.rh[t] = rh;
+            P2.rl[t] = (float)__dsub_rn(r, (double)rh);
+            P2.mf[t] = (float)m;
+            lmax = fmax(lmax, fabs(r));
+            lmmax = fmax(lmmax, fabs(m));
+            sel2[t] = !(zerr_on && zerr_veto(P2.z[t], zq1, c.b.zerr_kms));
         }
         for (int t = tid; t < c.mwords; t += kDmBlock) mbits[t] = 0u;
         for (int t = tid; t < c.dwords; t += kDmBlock) dbits[t] = 0u;
+        // guard bands of the FP32 geometry: |r_par error| <= 2^-23 max|r| +
+        // 3 2^-24 |r_par| / cos, |r_trans error| <= 2^-22 max|dist_m| sin +
+        // 2^-23 r_trans (rounding of the inputs, the difference or sum, the
+        // half-angle trig and the products), doubled
+        for (int o = 16; o > 0; o >>= 1) {
+            lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+            lmmax = fmax(lmmax, __shfl_xor_sync(0xffffffffu, lmmax, o));
+        }
+        if ((tid & 31) == 0) {
+            red[tid >> 5] = lmax;
+            red_int[tid >> 5] = 0;
+        }
+        __syncthreads();
+        double rmax = 0.;
+        for (int k = 0; k < kDmWarps; ++k) rmax = fmax(rmax, red[k]);
+        __syncthreads();
+        if ((tid & 31) == 0) red[tid >> 5] = lmmax;
         if (tid == 0) s_count = 0;
+        __syncthreads();
+        double mmax = 0.;
+        for (int k = 0; k < kDmWarps; ++k) mmax = fmax(mmax, red[k]);
+        DmGuard gd;
+        {
+            const double u = 5.9604644775390625e-8;  // 2^-24
+            const double rlim = fmax(fabs(c.b.r_par_max), fabs(c.b.r_par_min));
+            const double gp = 2. * (2. * u * rmax + 3. * u * (rlim + 1.) / fmax(it.cc, 1e-6));
+            const double gt = 2. * (4. * u * mmax * it.ss + 2. * u * c.b.r_trans_max);
+            const double ey = 8. * u;  // relative error of the bin coordinate itself
+            gd.cc = (float)it.cc;
+            gd.ss = (float)it.ss;
+            gd.gp = (float)gp;
+            gd.gt = (float)gt;
+            gd.gyp = (float)(gp * c.sp + ey * (c.b.np + 1));
+            gd.gymp = (float)(gp * c.smp + ey * (c.nmp + 1));
+            gd.gyt = (float)(gt * c.st + ey * (c.b.nt + 1));
+            gd.gymt = (float)(gt * c.smt + ey * (c.nmt + 1));
+        }
         __syncthreads();
 
         // 1. classification: touched model bins, data bins of selected pairs
@@ -285,13 +583,11 @@ __global__ void __launch_bounds__(kDmBlock)
             const int warp = tid >> 5, lane = tid & 31;
             int counted = 0;
             for (int i = warp; i < it.n1; i += kDmWarps) {
-                const double r1 = r1s[i], m1 = m1s[i], z1 = z1s[i];
-                if (w1s[i] == 0.) continue;
+                if (P1.w[i] == 0.) continue;
                 for (int j = lane; j < it.n2; j += 32) {
-                    if (w2s[j] == 0.) continue;
+                    if (P2.w[j] == 0.) continue;
                     DmPair o;
-                    if (!dm_pair(c, r1, m1, z1, r2s[j], m2s[j], z2s[j], it.cc, it.ss, it.shp, o))
-                        continue;
+                    if (!dm_decide(c, gd, it, P1, P2, i, j, o)) continue;
                     if (o.db < 0 || o.db >= nb || o.mb < 0 || o.mb >= nm) {
                         report_error(scratch, PG_ERR_BIN_RANGE, o.mb);
                         continue;
@@ -342,38 +638,38 @@ __global__ void __launch_bounds__(kDmBlock)
         // auxiliary sums (py/picca/cf.py:573-595)
         double lw = 0., lsw = 0.;
         for (int t = tid; t < it.n1; t += kDmBlock) {
-            lw += w1s[t];
-            lsw += __dmul_rn(d1s[t], w1s[t]);
+            lw += P1.w[t];
+            lsw += __dmul_rn(P1.dll[t], P1.w[t]);
         }
         it.sw1 = dm_block_sum(lw, red);
         const double sll1 = dm_block_sum(lsw, red);
         lw = 0.;
         lsw = 0.;
         for (int t = tid; t < it.n2; t += kDmBlock) {
-            lw += w2s[t];
-            lsw += __dmul_rn(d2s[t], w2s[t]);
+            lw += P2.w[t];
+            lsw += __dmul_rn(P2.dll[t], P2.w[t]);
         }
         it.sw2 = dm_block_sum(lw, red);
         const double sll2 = dm_block_sum(lsw, red);
         const double mean1 = sll1 / it.sw1, mean2 = sll2 / it.sw2;
         double q1 = 0., q2 = 0.;
         for (int t = tid; t < it.n1; t += kDmBlock) {
-            const double d = __dsub_rn(d1s[t], mean1);
-            d1s[t] = d;
-            q1 += __dmul_rn(w1s[t], __dmul_rn(d, d));
-            zf1s[t] = c.redshift_evolution
-                          ? pow(__dadd_rn(1., z1s[t]) / __dadd_rn(1., c.z_ref),
-                                __dsub_rn(c.alpha, 1.))
-                          : 1.;
+            const double d = __dsub_rn(P1.dll[t], mean1);
+            P1.dll[t] = d;
+            q1 += __dmul_rn(P1.w[t], __dmul_rn(d, d));
+            P1.zf[t] = c.redshift_evolution
+                           ? pow(__dadd_rn(1., P1.z[t]) / __dadd_rn(1., c.z_ref),
+                                 __dsub_rn(c.alpha, 1.))
+                           : 1.;
         }
         for (int t = tid; t < it.n2; t += kDmBlock) {
-            const double d = __dsub_rn(d2s[t], mean2);
-            d2s[t] = d;
-            q2 += __dmul_rn(w2s[t], __dmul_rn(d, d));
-            zf2s[t] = c.redshift_evolution
-                          ? pow(__dadd_rn(1., z2s[t]) / __dadd_rn(1., c.z_ref),
-                                __dsub_rn(c.alpha2, 1.))
-                          : 1.;
+            const double d = __dsub_rn(P2.dll[t], mean2);
+            P2.dll[t] = d;
+            q2 += __dmul_rn(P2.w[t], __dmul_rn(d, d));
+            P2.zf[t] = c.redshift_evolution
+                           ? pow(__dadd_rn(1., P2.z[t]) / __dadd_rn(1., c.z_ref),
+                                 __dsub_rn(c.alpha2, 1.))
+                           : 1.;
         }
         it.swsll1 = dm_block_sum(q1, red);
         it.swsll2 = dm_block_sum(q2, red);
@@ -381,12 +677,37 @@ __global__ void __launch_bounds__(kDmBlock)
         it.inv_sw2 = 1. / it.sw2;
         it.inv_q1 = 1. / it.swsll1;
         it.inv_q2 = 1. / it.swsll2;
+        const bool ord1 = it.order1 == 1, ord2 = it.order2 == 1;
+        if ((ord1 && !(it.swsll1 != 0.)) || (ord2 && !(it.swsll2 != 0.))) {
+            // the reference divides by zero here (a forest without spread in
+            // log lambda); the pair is reported and skipped
+            if (tid == 0) report_error(scratch, PG_ERR_INVALID_ARGUMENT, (int32_t)q);
+            __syncthreads();
+            continue;
+        }
+        // per-pixel factors of the eta terms and of the effective sums
+        for (int t = tid; t < it.n1; t += kDmBlock) {
+            const double wz = __dmul_rn(P1.w[t], P1.zf[t]);
+            P1.a[t] = __dmul_rn(wz, it.inv_sw1);
+            P1.b[t] = __dmul_rn(__dmul_rn(wz, P1.dll[t]), it.inv_q1);
+            P1.wd[t] = __dmul_rn(P1.w[t], P1.dll[t]);
+        }
+        for (int t = tid; t < it.n2; t += kDmBlock) {
+            const double wz = __dmul_rn(P2.w[t], P2.zf[t]);
+            P2.a[t] = __dmul_rn(wz, it.inv_sw2);
+            P2.b[t] = __dmul_rn(__dmul_rn(wz, P2.dll[t]), it.inv_q2);
+            P2.wd[t] = __dmul_rn(P2.w[t], P2.dll[t]);
+            P2.wz[t] = wz;
+            P2.wzz[t] = __dmul_rn(P2.w[t], P2.z[t]);
+            P2.wm[t] = __dmul_rn(P2.w[t], P2.m[t]);
+        }
+        __syncthreads();
 
         // kappa layout of the U and E rows
         const int n1 = it.n1, n2 = it.n2;
         const int kU = 0, kX = n1, kV = n1 + n2;
-        const int kY = kV + (it.order2 == 1 ? n1 : 0);
-        const int kR = kY + (it.order1 == 1 ? n2 : 0);
+        const int kY = kV + (ord2 ? n1 : 0);
+        const int kR = kY + (ord1 ? n2 : 0);
         const int kst = (int)dm_align((size_t)kR + 4, kSlab);
         const int64_t cap = c.work_doubles / kst;
         int dc = nbt, mc = nmt;
@@ -394,7 +715,6 @@ __global__ void __launch_bounds__(kDmBlock)
             dc = (int)min((int64_t)nbt, cap / 2);
             mc = (int)(cap - dc);
         }
-        const bool ord1 = it.order1 == 1, ord2 = it.order2 == 1;
 
         for (int d0 = 0; d0 < nbt; d0 += dc) {
             const int dcc = min(dc, nbt - d0);
@@ -410,154 +730,157 @@ __global__ void __launch_bounds__(kDmBlock)
                 }
                 __syncthreads();
 
-                // 2a. row sweep: a thread per pixel i of forest 1
+                // 2a. row sweep: a thread per pixel i of forest 1. Run sums are
+                // per-pixel factors of forest 2, scaled by those of pixel i at
+                // the flush (zfac = zf1 zf2, w12 = w1 w2, z = (z1 + z2) / 2,
+                // r_trans = (dist_m1 + dist_m2) sin)
                 for (int i = tid; i < n1; i += kDmBlock) {
-                    const double w1 = w1s[i];
+                    const double w1 = P1.w[i];
                     if (w1 == 0.) continue;
-                    const double r1 = r1s[i], m1 = m1s[i], z1 = z1s[i], zf1 = zf1s[i];
+                    const double zf1 = P1.zf[i], r1 = P1.r[i];
                     const bool ok1 = sel1[i];
                     int run_m = -1, run_d = -1;
                     double e1 = 0., e3 = 0., u = 0., v = 0.;
                     int64_t run_k = -1;
                     int32_t k_db = 0, k_mb = 0;
                     double k_dm = 0., k_w = 0., k_rp = 0., k_rt = 0., k_z = 0.;
+                    auto flush_k = [&]() {
+                        const double w1zf = __dmul_rn(w1, zf1);
+                        atomicAdd(&out.dmat[run_k], __dmul_rn(w1zf, k_dm));
+                        atomicAdd(&out.weights_dmat[k_db], __dmul_rn(w1, k_w));
+                        atomicAdd(&out.r_par_eff[k_mb], __dmul_rn(w1, k_rp));
+                        const double rt = c.b.rmu ? k_rt
+                                                  : __dmul_rn(__dadd_rn(__dmul_rn(P1.m[i], k_w),
+                                                                        k_rt), it.ss);
+                        atomicAdd(&out.r_trans_eff[k_mb], __dmul_rn(w1, rt));
+                        atomicAdd(&out.z_eff[k_mb],
+                                  __dmul_rn(w1, __dmul_rn(0.5, __dadd_rn(__dmul_rn(P1.z[i], k_w),
+                                                                         k_z))));
+                        atomicAdd(&out.weight_eff[k_mb], __dmul_rn(w1, k_w));
+                    };
                     for (int j = 0; j < n2; ++j) {
-                        const double w2 = w2s[j];
-                        if (w2 == 0.) continue;
+                        if (P2.w[j] == 0.) continue;
                         DmPair o;
-                        if (!dm_pair(c, r1, m1, z1, r2s[j], m2s[j], z2s[j], it.cc, it.ss, it.shp,
-                                     o))
-                            continue;
+                        const int st = dm_decide(c, gd, it, P1, P2, i, j, o);
+                        if (!st) continue;
                         if (o.db < 0 || o.db >= nb || o.mb < 0 || o.mb >= nm) continue;
-                        const double zfac = c.redshift_evolution ? __dmul_rn(zf1, zf2s[j]) : 1.;
                         const int ml = dm_rank(mbits, mpref, o.mb) - m0;
                         if (ml >= 0 && ml < mcc) {
                             if (ml != run_m) {
                                 if (run_m >= 0) {
-                                    E[(int64_t)run_m * kst + kU + i] -= e1;
-                                    if (ord2) E[(int64_t)run_m * kst + kV + i] -= e3;
+                                    E[(int64_t)run_m * kst + kU + i] -= __dmul_rn(zf1, e1);
+                                    if (ord2) E[(int64_t)run_m * kst + kV + i] -= __dmul_rn(zf1, e3);
                                 }
                                 run_m = ml;
                                 e1 = 0.;
                                 e3 = 0.;
                             }
-                            e1 += __dmul_rn(__dmul_rn(zfac, w2), it.inv_sw2);
-                            if (ord2) e3 += __dmul_rn(__dmul_rn(__dmul_rn(zfac, w2), d2s[j]), it.inv_q2);
+                            e1 += P2.a[j];
+                            if (ord2) e3 += P2.b[j];
                         }
                         if (o.counted && o.zsel && ok1 && sel2[j]) {
-                            const double w12 = __dmul_rn(w1, w2);
                             const int dl = dm_rank(dbits, dpref, o.db) - d0;
                             if (dl >= 0 && dl < dcc) {
                                 if (dl != run_d) {
                                     if (run_d >= 0) {
-                                        U[(int64_t)run_d * kst + kU + i] += u;
-                                        if (ord2) U[(int64_t)run_d * kst + kV + i] += v;
+                                        U[(int64_t)run_d * kst + kU + i] += __dmul_rn(w1, u);
+                                        if (ord2) U[(int64_t)run_d * kst + kV + i] += __dmul_rn(w1, v);
                                     }
                                     run_d = dl;
                                     u = 0.;
                                     v = 0.;
                                 }
-                                u += w12;
-                                if (ord2) v += __dmul_rn(w12, d2s[j]);
+                                u += P2.w[j];
+                                if (ord2) v += P2.wd[j];
                             }
                             if (first) {
                                 const int64_t key = (int64_t)o.db * nm + o.mb;
                                 if (key != run_k) {
-                                    if (run_k >= 0) {
-                                        atomicAdd(&out.dmat[run_k], k_dm);
-                                        atomicAdd(&out.weights_dmat[k_db], k_w);
-                                        atomicAdd(&out.r_par_eff[k_mb], k_rp);
-                                        atomicAdd(&out.r_trans_eff[k_mb], k_rt);
-                                        atomicAdd(&out.z_eff[k_mb], k_z);
-                                        atomicAdd(&out.weight_eff[k_mb], k_w);
-                                    }
+                                    if (run_k >= 0) flush_k();
                                     run_k = key;
                                     k_db = o.db;
                                     k_mb = o.mb;
                                     k_dm = k_w = k_rp = k_rt = k_z = 0.;
                                 }
-                                k_dm += __dmul_rn(w12, zfac);
-                                k_w += w12;
-                                k_rp += __dmul_rn(w12, o.rp);
-                                k_rt += __dmul_rn(w12, o.rt);
-                                k_z += __dmul_rn(w12, o.z);
+                                const double w2 = P2.w[j];
+                                k_dm += P2.wz[j];
+                                k_w += w2;
+                                k_z += P2.wzz[j];
+                                if (st == 2) {
+                                    k_rp += __dmul_rn(w2, o.rp);
+                                    if (c.b.rmu) k_rt += __dmul_rn(w2, o.rt);
+                                    else k_rt += P2.wm[j];
+                                } else {
+                                    double rp = __dmul_rn(__dsub_rn(r1, P2.r[j]), it.cc);
+                                    if (!c.b.x_correlation) rp = fabs(rp);
+                                    k_rp += __dmul_rn(w2, rp);
+                                    k_rt += P2.wm[j];
+                                }
                             }
                         }
                     }
                     if (run_m >= 0) {
-                        E[(int64_t)run_m * kst + kU + i] -= e1;
-                        if (ord2) E[(int64_t)run_m * kst + kV + i] -= e3;
+                        E[(int64_t)run_m * kst + kU + i] -= __dmul_rn(zf1, e1);
+                        if (ord2) E[(int64_t)run_m * kst + kV + i] -= __dmul_rn(zf1, e3);
                     }
                     if (run_d >= 0) {
-                        U[(int64_t)run_d * kst + kU + i] += u;
-                        if (ord2) U[(int64_t)run_d * kst + kV + i] += v;
+                        U[(int64_t)run_d * kst + kU + i] += __dmul_rn(w1, u);
+                        if (ord2) U[(int64_t)run_d * kst + kV + i] += __dmul_rn(w1, v);
                     }
-                    if (run_k >= 0) {
-                        atomicAdd(&out.dmat[run_k], k_dm);
-                        atomicAdd(&out.weights_dmat[k_db], k_w);
-                        atomicAdd(&out.r_par_eff[k_mb], k_rp);
-                        atomicAdd(&out.r_trans_eff[k_mb], k_rt);
-                        atomicAdd(&out.z_eff[k_mb], k_z);
-                        atomicAdd(&out.weight_eff[k_mb], k_w);
-                    }
+                    if (run_k >= 0) flush_k();
                 }
 
                 // 2b. column sweep: a thread per pixel j of forest 2
                 for (int j = tid; j < n2; j += kDmBlock) {
-                    const double w2 = w2s[j];
+                    const double w2 = P2.w[j];
                     if (w2 == 0.) continue;
-                    const double r2 = r2s[j], m2 = m2s[j], z2 = z2s[j], zf2 = zf2s[j];
+                    const double zf2 = P2.zf[j];
                     const bool ok2 = sel2[j];
                     int run_m = -1, run_d = -1;
                     double e2 = 0., e4 = 0., x = 0., y = 0.;
                     for (int i = 0; i < n1; ++i) {
-                        const double w1 = w1s[i];
-                        if (w1 == 0.) continue;
+                        if (P1.w[i] == 0.) continue;
                         DmPair o;
-                        if (!dm_pair(c, r1s[i], m1s[i], z1s[i], r2, m2, z2, it.cc, it.ss, it.shp,
-                                     o))
-                            continue;
+                        if (!dm_decide(c, gd, it, P1, P2, i, j, o)) continue;
                         if (o.db < 0 || o.db >= nb || o.mb < 0 || o.mb >= nm) continue;
-                        const double zfac = c.redshift_evolution ? __dmul_rn(zf1s[i], zf2) : 1.;
                         const int ml = dm_rank(mbits, mpref, o.mb) - m0;
                         if (ml >= 0 && ml < mcc) {
                             if (ml != run_m) {
                                 if (run_m >= 0) {
-                                    E[(int64_t)run_m * kst + kX + j] -= e2;
-                                    if (ord1) E[(int64_t)run_m * kst + kY + j] -= e4;
+                                    E[(int64_t)run_m * kst + kX + j] -= __dmul_rn(zf2, e2);
+                                    if (ord1) E[(int64_t)run_m * kst + kY + j] -= __dmul_rn(zf2, e4);
                                 }
                                 run_m = ml;
                                 e2 = 0.;
                                 e4 = 0.;
                             }
-                            e2 += __dmul_rn(__dmul_rn(zfac, w1), it.inv_sw1);
-                            if (ord1) e4 += __dmul_rn(__dmul_rn(__dmul_rn(zfac, w1), d1s[i]), it.inv_q1);
+                            e2 += P1.a[i];
+                            if (ord1) e4 += P1.b[i];
                         }
                         if (o.counted && o.zsel && ok2 && sel1[i]) {
-                            const double w12 = __dmul_rn(w1, w2);
                             const int dl = dm_rank(dbits, dpref, o.db) - d0;
                             if (dl >= 0 && dl < dcc) {
                                 if (dl != run_d) {
                                     if (run_d >= 0) {
-                                        U[(int64_t)run_d * kst + kX + j] += x;
-                                        if (ord1) U[(int64_t)run_d * kst + kY + j] += y;
+                                        U[(int64_t)run_d * kst + kX + j] += __dmul_rn(w2, x);
+                                        if (ord1) U[(int64_t)run_d * kst + kY + j] += __dmul_rn(w2, y);
                                     }
                                     run_d = dl;
                                     x = 0.;
                                     y = 0.;
                                 }
-                                x += w12;
-                                if (ord1) y += __dmul_rn(w12, d1s[i]);
+                                x += P1.w[i];
+                                if (ord1) y += P1.wd[i];
                             }
                         }
                     }
                     if (run_m >= 0) {
-                        E[(int64_t)run_m * kst + kX + j] -= e2;
-                        if (ord1) E[(int64_t)run_m * kst + kY + j] -= e4;
+                        E[(int64_t)run_m * kst + kX + j] -= __dmul_rn(zf2, e2);
+                        if (ord1) E[(int64_t)run_m * kst + kY + j] -= __dmul_rn(zf2, e4);
                     }
                     if (run_d >= 0) {
-                        U[(int64_t)run_d * kst + kX + j] += x;
-                        if (ord1) U[(int64_t)run_d * kst + kY + j] += y;
+                        U[(int64_t)run_d * kst + kX + j] += __dmul_rn(w2, x);
+                        if (ord1) U[(int64_t)run_d * kst + kY + j] += __dmul_rn(w2, y);
                     }
                 }
                 __syncthreads();
@@ -572,19 +895,19 @@ __global__ void __launch_bounds__(kDmBlock)
                             for (int i = lane; i < n1; i += 32) {
                                 const double a = row[kU + i];
                                 s0 += a;
-                                s2v += __dmul_rn(d1s[i], a);
-                                if (ord1 && ord2) s3 += __dmul_rn(d1s[i], row[kV + i]);
+                                s2v += __dmul_rn(P1.dll[i], a);
+                                if (ord1 && ord2) s3 += __dmul_rn(P1.dll[i], row[kV + i]);
                             }
-                            for (int j = lane; j < n2; j += 32) s1v += __dmul_rn(d2s[j], row[kX + j]);
+                            for (int j = lane; j < n2; j += 32) s1v += __dmul_rn(P2.dll[j], row[kX + j]);
                         } else {
                             const double *row = E + (int64_t)(r - dcc) * kst;
                             for (int i = lane; i < n1; i += 32) {
-                                const double a1 = __dmul_rn(w1s[i], it.inv_sw1);
+                                const double a1 = __dmul_rn(P1.w[i], it.inv_sw1);
                                 const double e1 = row[kU + i];
                                 s0 -= __dmul_rn(a1, e1);
                                 if (ord2) s1v -= __dmul_rn(a1, row[kV + i]);
                                 if (ord1) {
-                                    const double a7 = __dmul_rn(__dmul_rn(w1s[i], d1s[i]), it.inv_q1);
+                                    const double a7 = __dmul_rn(__dmul_rn(P1.w[i], P1.dll[i]), it.inv_q1);
                                     s2v -= __dmul_rn(a7, e1);
                                     if (ord2) s3 -= __dmul_rn(a7, row[kV + i]);
                                 }
@@ -609,6 +932,12 @@ __global__ void __launch_bounds__(kDmBlock)
                 if (tid == 0)
                     atomicAdd(&scratch->gemm_macs,
                               (unsigned long long)dcc * (unsigned long long)mcc * (kR + 4));
+                if (c.split) {
+                    dm_product_split(U, E, dcc, mcc, kst, digits, rexp, ta_raw, tb_raw,
+                                     dlist + d0, mlist + m0, nm, out.dmat);
+                    __syncthreads();
+                    continue;
+                }
                 const int tx = tid & 15, ty = tid >> 4;
                 for (int td = 0; td < dcc; td += kTile) {
                     for (int tm = 0; tm < mcc; tm += kTile) {
@@ -669,8 +998,10 @@ int dmat_config(const pg_corr_params &p, const pg_dmat_params &d, int p1, int p2
     const int64_t nb = (int64_t)p.num_bins_r_par * p.num_bins_r_trans;
     if (nm > (1 << 26) || nb > (1 << 26)) return PG_ERR_UNSUPPORTED;
     const int mwords = (int)((nm + 31) / 32), dwords = (int)((nb + 31) / 32);
-    const DmSmem s = dm_smem(p1, p2, mwords, dwords);
-    if (s.total > 200 * 1024) return PG_ERR_UNSUPPORTED;
+    if (d.product != PG_DMAT_FP64 && d.product != PG_DMAT_SPLIT_BF16) return PG_ERR_INVALID_ARGUMENT;
+    const int split = d.product == PG_DMAT_SPLIT_BF16;
+    const DmSmem s = dm_smem(p1, p2, mwords, dwords, split);
+    if (s.total > 220 * 1024) return PG_ERR_UNSUPPORTED;
     h.smem = s.total;
     h.p1 = p1;
     h.p2 = p2;
@@ -683,7 +1014,10 @@ int dmat_config(const pg_corr_params &p, const pg_dmat_params &d, int p1, int p2
     const int64_t rows = std::min<int64_t>(nb + nm, wanted);
     h.list_doubles = (int64_t)dm_align((size_t)(nb + nm), 32) / 2;
     h.work_doubles = rows * kcap;
-    h.cta_doubles = (int64_t)dm_align((size_t)(h.list_doubles + h.work_doubles), 32);
+    // tensor-core form: six bf16 digits per element and one exponent per row
+    const int64_t extra = split ? h.work_doubles * kSlices / 4 + h.work_doubles / 32 : 0;
+    h.split = split;
+    h.cta_doubles = (int64_t)dm_align((size_t)(h.list_doubles + h.work_doubles + extra), 32);
     int occ = 0;
     if (cudaFuncSetAttribute(cf_dmat_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                              (int)s.total) != cudaSuccess)
@@ -714,6 +1048,18 @@ int launch_cf_dmat(const pg_corr_params &p, const pg_dmat_params &d, const DmatC
     c.alpha2 = d.alpha2;
     c.inv_r_par_range = 1. / c.b.r_par_range;
     c.inv_r_trans_max = 1. / c.b.r_trans_max;
+    c.sp = c.b.np / c.b.r_par_range;
+    c.smp = c.nmp / c.b.r_par_range;
+    c.st = c.b.nt / c.b.r_trans_max;
+    c.smt = c.nmt / c.b.r_trans_max;
+    c.f_rpmin = (float)c.b.r_par_min;
+    c.f_rpmax = (float)c.b.r_par_max;
+    c.f_rtmax = (float)c.b.r_trans_max;
+    c.f_hpc = (float)c.b.half_plate_cut;
+    c.f_sp = (float)c.sp;
+    c.f_smp = (float)c.smp;
+    c.f_st = (float)c.st;
+    c.f_smt = (float)c.smt;
     c.p1 = h.p1;
     c.p2 = h.p2;
     c.mwords = h.mwords;
@@ -721,6 +1067,7 @@ int launch_cf_dmat(const pg_corr_params &p, const pg_dmat_params &d, const DmatC
     c.list_doubles = h.list_doubles;
     c.work_doubles = h.work_doubles;
     c.cta_doubles = h.cta_doubles;
+    c.split = h.split;
     cf_dmat_kernel<<<grid, kDmBlock, h.smem, stream>>>(c, s1, s2, ll1, ll2, order1, order2,
                                                        pair_first, pair_second, pair_angle,
                                                        num_pairs, out, work, scratch);

@@ -221,6 +221,7 @@ struct DmatConstHost {
     int32_t p1, p2, mwords, dwords;
     int64_t list_doubles, work_doubles, cta_doubles;
     int max_grid;
+    int split;
 };
 int dmat_config(const pg_corr_params &p, const pg_dmat_params &d, int p1, int p2, int num_sms,
                 DmatConstHost &h);

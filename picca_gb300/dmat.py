@@ -31,14 +31,20 @@ _DRAW_BLOCK = 1 << 24
 
 def make_dmat_params(num_bins_r_par, num_bins_r_trans, coef_binning_model=1,
                      redshift_evolution=True, z_ref=2.25, alpha=2.9, alpha2=2.9,
-                     num_model_bins_r_par=None, num_model_bins_r_trans=None, row_capacity=0):
+                     num_model_bins_r_par=None, num_model_bins_r_trans=None, row_capacity=0,
+                     product="split_bf16"):
     """pg_dmat_params. The model bins default to coef_binning_model times the
     data bins (py/picca/bin/picca_dmat.py:366-369); row_capacity 0 keeps the
-    library's default chunking of a forest pair's bins."""
+    library's default chunking of a forest pair's bins; ``product`` selects
+    the arithmetic of the eta products: "split_bf16" (tensor cores, exact
+    digit products) or "fp64"."""
+    products = {"fp64": _native.PG_DMAT_FP64, "split_bf16": _native.PG_DMAT_SPLIT_BF16}
+    if product not in products:
+        raise ValueError(f"unknown product {product!r}")
     nmp = num_model_bins_r_par or int(num_bins_r_par * coef_binning_model)
     nmt = num_model_bins_r_trans or int(num_bins_r_trans * coef_binning_model)
     return DmatParamsC(int(nmp), int(nmt), int(bool(redshift_evolution)), int(row_capacity),
-                       float(z_ref), float(alpha), float(alpha2))
+                       products[product], 0, float(z_ref), float(alpha), float(alpha2))
 
 
 def _ranges(starts, ends):

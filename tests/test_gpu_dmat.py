@@ -10,10 +10,14 @@
   plates (same-half-plate vetoes), z cuts, redshift evolution, r-mu binning
   and a forced split of each forest pair's bins into chunks.
 
-Tolerance: the kernel regroups the reference's sums (the eta projections
-become a product of per-bin and per-pixel partial sums, added with
-atomics), so FP64 results differ from the oracle by rounding only:
-|got - want| <= 1e-9 |want| + 1e-11 max|want| per array.
+Both arithmetic forms of the eta products are checked: FP64 on the CUDA
+cores, and the tensor-core form (rows scaled by powers of two, 48-bit fixed
+point split into six 8-bit digits, exact digit products, error below 2^-46
+of the largest row x column product). Tolerance: the kernel regroups the
+reference's sums (the eta projections become a product of per-bin and
+per-pixel partial sums, added with atomics), so results differ from the
+oracle by rounding only: |got - want| <= 1e-9 |want| + 1e-11 max|want| per
+array.
 """
 
 import os
@@ -46,8 +50,10 @@ def close(got, want, rtol=1e-9, scale_tol=1e-11):
     return bool(np.all(err <= bound)), float(np.max(err) if err.size else 0.0)
 
 
-def test_forest_pair_cases_match_reference(cuda):
+@pytest.mark.parametrize("product", ["split_bf16", "fp64"])
+def test_forest_pair_cases_match_reference(cuda, product):
     from picca_gb300 import cf
+    cf.dmat_product = product
     f = golden("dmat_cases.npz")
     for k in range(int(f["num_cases"])):
         pre = f"dm{k}_"
@@ -76,7 +82,8 @@ def test_forest_pair_cases_match_reference(cuda):
             out["z_eff"], out["weight_eff"], bool(shp), int(p[5]), int(p[6]))
         for key, got in out.items():
             ok, err = close(got, f[pre + "out_" + key])
-            assert ok, (k, key, err)
+            assert ok, (product, k, key, err)
+    cf.dmat_product = "split_bf16"
 
 
 def test_cli_matches_golden_dmat(cuda, picca_inputs, tmp_path):
@@ -158,12 +165,13 @@ def test_synthetic_matches_oracle(cuda, case):
     params = pairs.make_params(rp_min, rp_max, rt_max, c["np"], c["nt"], ang_max,
                                z_min_pairs=zmin, z_max_pairs=zmax, rmu_binning=c["rmu"],
                                remove_same_half_plate_close_pairs=c["shp"])
-    for capacity in (0, 24):
+    for capacity, product in ((0, "split_bf16"), (24, "split_bf16"), (0, "fp64")):
         dparams = dmat.make_dmat_params(c["np"], c["nt"], coef_binning_model=c["coef"],
-                                        redshift_evolution=c["zevol"], row_capacity=capacity)
+                                        redshift_evolution=c["zevol"], row_capacity=capacity,
+                                        product=product)
         res = dmat.distortion_matrix(fs, None, params, dparams, c["reject"], nproc=c["nproc"])
         assert res["NPALL"] == npall and res["NPUSED"] == npused
         assert res["forest_pairs_used"] == npused
         for key in out:
             ok, err = close(res["raw"][key], out[key])
-            assert ok, (case, capacity, key, err)
+            assert ok, (case, capacity, product, key, err)
