@@ -49,12 +49,12 @@ constexpr int kTile = 32;   // GEMM output tile edge (data bins x model bins)
 constexpr int kSlab = 16;   // GEMM reduction step
 constexpr int kTilePad = kTile + 1;
 // Tensor-core form of the product (PG_DMAT_SPLIT_BF16): each FP64 row is
-// scaled by a power of two to |x| < 1, rounded to 48 fractional bits and
-// written as six signed 8-bit digits (exact in bf16). Products of digits
-// are exact in the FP32 accumulators of mma.sync m16n8k16; the 21 digit
-// pairs with p + q <= 5 (0-based) are summed per level p + q over 16
-// reduction steps (|sum| <= 2^21), moved into 32-bit integer level sums
-// (exact) and combined in FP64 at the end.
+// scaled by a power of two to |x| < 1/2, rounded to 48 fractional bits and
+// written as six signed digits of at most 128 in magnitude (exact in bf16).
+// Products of digits are exact in the FP32 accumulators of mma.sync
+// m16n8k16; the 21 digit pairs with p + q <= 5 (0-based) are summed per
+// level p + q over 32 reduction steps (|sum| < 2^22), moved into 32-bit
+// integer level sums (exact) and combined in FP64 at the end.
 constexpr int kSlices = 6;
 constexpr int kTcM = 32, kTcN = 32, kTcK = 32;
 constexpr int kTcRow = kTcK + 8;  // bf16 per staged row (pad: conflict-free fragments)
@@ -96,9 +96,9 @@ __host__ __device__ inline DmSmem dm_smem(int p1, int p2, int mwords, int dwords
     s.dbits = o; o += sizeof(uint32_t) * (size_t)dwords;
     s.dpref = o; o += sizeof(int32_t) * (size_t)dwords;
     o = dm_align(o, 16);
-    if (split) {
-        s.tile_a = o; o += sizeof(uint16_t) * kSlices * kTcM * kTcRow;
-        s.tile_b = o; o += sizeof(uint16_t) * kSlices * kTcN * kTcRow;
+    if (split) {  // two staging buffers per operand
+        s.tile_a = o; o += 2 * sizeof(uint16_t) * kSlices * kTcM * kTcRow;
+        s.tile_b = o; o += 2 * sizeof(uint16_t) * kSlices * kTcN * kTcRow;
     } else {
         s.tile_a = o; o += sizeof(double) * kSlab * kTilePad;
         s.tile_b = o; o += sizeof(double) * kSlab * kTilePad;
@@ -238,23 +238,48 @@ __device__ int dm_scan_bits(const uint32_t *bits, int32_t *pref, int words, int 
 // D = U E^T of one chunk on the tensor cores (see kSlices), added to the
 // global matrix: dmat[dlist[dl] * nm + mlist[ml]] += D[dl][ml]. U is
 // [dcc][kst], E is [mcc][kst] (FP64, zero-padded to kst, a multiple of 16).
+__device__ __forceinline__ void dm_ldsm4(uint32_t r[4], const uint16_t *p) {
+    const unsigned addr = (unsigned)__cvta_generic_to_shared(p);
+    asm volatile("ldmatrix.sync.aligned.m8n8.x4.shared.b16 {%0,%1,%2,%3}, [%4];\n"
+                 : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3])
+                 : "r"(addr));
+}
+
+// 16-byte asynchronous copy global -> shared; valid = false writes zeros.
+__device__ __forceinline__ void dm_cp16(uint16_t *dst, const uint16_t *src, bool valid) {
+    const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n"
+                 :
+                 : "r"(d), "l"(src), "r"(valid ? 16 : 0)
+                 : "memory");
+}
+
+__device__ __forceinline__ void dm_cp_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+__device__ __forceinline__ void dm_cp_wait_1() { asm volatile("cp.async.wait_group 1;\n" ::: "memory"); }
+__device__ __forceinline__ void dm_cp_wait_0() { asm volatile("cp.async.wait_group 0;\n" ::: "memory"); }
+
+// D = U E^T of one chunk on the tensor cores (see kSlices), added to the
+// global matrix: dmat[dlist[dl] * nm + mlist[ml]] += D[dl][ml]. U is
+// [dcc][kst], E is [mcc][kst] (FP64, zero-padded to kst, a multiple of 16).
+// sa / sb: two staging buffers of kSlices x 32 rows x kTcRow bf16 each.
 __device__ void dm_product_split(const double *U, const double *E, int dcc, int mcc, int kst,
                                  uint16_t *digits, int32_t *rexp, uint16_t *sa, uint16_t *sb,
                                  const int32_t *dlist, const int32_t *mlist, int nm,
                                  double *dmat) {
     const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
-    // row exponents and digits (a warp per row)
+    // row exponents and digits (a warp per row): rows are scaled to |x| < 1/2
+    // so every digit is at most 128 in magnitude
     for (int r = warp; r < dcc + mcc; r += kDmWarps) {
         const double *row = r < dcc ? U + (int64_t)r * kst : E + (int64_t)(r - dcc) * kst;
         double mx = 0.;
-        for (int k = lane; k < kst; k += 32) mx = fmax(mx, fabs(row[k]));
+        for (int k = lane; k < kst; k += 32) mx = fmax(mx, fabs(__ldcg(row + k)));
         for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
         const int ex = (int)((__double_as_longlong(mx) >> 52) & 0x7FF);
-        const int e = ex == 0 ? -1022 : ex - 1022;  // |x| <= mx < 2^e
+        const int e = (ex == 0 ? -1022 : ex - 1022) + 1;  // |x| <= mx < 2^(e - 1)
         if (lane == 0) rexp[r] = e;
         uint16_t *dst = digits + (int64_t)r * kSlices * kst;
         for (int k = lane; k < kst; k += 32) {
-            long long m = dm_fixed48(row[k], e);
+            long long m = dm_fixed48(__ldcg(row + k), e);
 #pragma unroll
             for (int p = 0; p < kSlices; ++p) {
                 const int sh = 8 * (kSlices - 1 - p);
@@ -267,19 +292,14 @@ __device__ void dm_product_split(const double *U, const double *E, int dcc, int 
     __syncthreads();
     const int group = lane >> 2, tig = lane & 3;
     const int wm = warp >> 2, wn = warp & 3;  // 2 x 4 warps, 16 x 8 each
+    constexpr int kParts = kTcK / 8;
+    constexpr int kOne = kSlices * kTcM * kParts;    // 16-byte copies per operand
+    constexpr int kBuf = kSlices * kTcM * kTcRow;    // bf16 per operand buffer
     for (int td = 0; td < dcc; td += kTcM) {
         for (int tm = 0; tm < mcc; tm += kTcN) {
-            uint32_t lev[kSlices][4];
-#pragma unroll
-            for (int l = 0; l < kSlices; ++l)
-#pragma unroll
-                for (int q = 0; q < 4; ++q) lev[l][q] = 0u;
-            uint32_t drains = 0;
-            for (int k0 = 0; k0 < kst; k0 += kTcK) {
-                // stage the digits of rows [td, td + 32) of U and [tm, tm + 32) of E:
-                // (slice, row, 8-element part) -> one 16-byte copy each
-                constexpr int kParts = kTcK / 8;
-                constexpr int kOne = kSlices * kTcM * kParts;
+            // stage the digits of rows [td, td + 32) of U and [tm, tm + 32) of
+            // E for reduction steps [k0, k0 + 32) into buffer b
+            auto stage = [&](int b, int k0) {
                 for (int e = tid; e < 2 * kOne; e += kDmBlock) {
                     const bool isa = e < kOne;
                     const int f = isa ? e : e - kOne;
@@ -288,43 +308,71 @@ __device__ void dm_product_split(const double *U, const double *E, int dcc, int 
                     const int p = f / (kParts * kTcM);
                     const int grow = (isa ? td : tm) + r;
                     const int kk = k0 + part * 8;
-                    uint4 v = make_uint4(0u, 0u, 0u, 0u);
-                    if (grow < (isa ? dcc : mcc) && kk < kst) {
-                        const int64_t src_row = isa ? grow : dcc + grow;
-                        v = *reinterpret_cast<const uint4 *>(
-                            digits + (src_row * kSlices + p) * (int64_t)kst + kk);
-                    }
-                    *reinterpret_cast<uint4 *>((isa ? sa : sb) + (p * kTcM + r) * kTcRow +
-                                               part * 8) = v;
+                    const bool valid = grow < (isa ? dcc : mcc) && kk < kst;
+                    const int64_t src_row = isa ? grow : dcc + grow;
+                    const uint16_t *src =
+                        valid ? digits + (src_row * kSlices + p) * (int64_t)kst + kk : digits;
+                    dm_cp16((isa ? sa : sb) + b * kBuf + (p * kTcM + r) * kTcRow + part * 8, src,
+                            valid);
+                }
+                dm_cp_commit();
+            };
+            uint32_t lev[kSlices][4];
+#pragma unroll
+            for (int l = 0; l < kSlices; ++l)
+#pragma unroll
+                for (int q = 0; q < 4; ++q) lev[l][q] = 0u;
+            uint32_t drains = 0;
+            stage(0, 0);
+            int b = 0;
+            for (int k0 = 0; k0 < kst; k0 += kTcK) {
+                if (k0 + kTcK < kst) {
+                    stage(b ^ 1, k0 + kTcK);
+                    dm_cp_wait_1();
+                } else {
+                    dm_cp_wait_0();
                 }
                 __syncthreads();
+                const uint16_t *A = sa + b * kBuf, *B = sb + b * kBuf;
+                // digit products: |digit| <= 128, so a level (p + q fixed, at
+                // most 6 pairs) summed over 32 reduction steps stays below
+                // 6 * 32 * 2^14 < 2^22 and is an exact FP32 integer
+                float acc[kSlices][4];
+#pragma unroll
+                for (int l = 0; l < kSlices; ++l)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) acc[l][q] = 0.f;
 #pragma unroll
                 for (int ks = 0; ks < kTcK; ks += 16) {
                     if (k0 + ks >= kst) break;
                     uint32_t af[kSlices][4], bf[kSlices][2];
 #pragma unroll
-                    for (int p = 0; p < kSlices; ++p) {
-                        const uint16_t *a0 = sa + (p * kTcM + wm * 16 + group) * kTcRow + ks + tig * 2;
-                        af[p][0] = *reinterpret_cast<const uint32_t *>(a0);
-                        af[p][1] = *reinterpret_cast<const uint32_t *>(a0 + 8 * kTcRow);
-                        af[p][2] = *reinterpret_cast<const uint32_t *>(a0 + 8);
-                        af[p][3] = *reinterpret_cast<const uint32_t *>(a0 + 8 * kTcRow + 8);
-                        const uint16_t *b0 = sb + (p * kTcN + wn * 8 + group) * kTcRow + ks + tig * 2;
-                        bf[p][0] = *reinterpret_cast<const uint32_t *>(b0);
-                        bf[p][1] = *reinterpret_cast<const uint32_t *>(b0 + 8);
+                    for (int p = 0; p < kSlices; ++p)
+                        dm_ldsm4(af[p], A + (p * kTcM + wm * 16 + (lane & 15)) * kTcRow + ks +
+                                            (lane >> 4) * 8);
+#pragma unroll
+                    for (int p = 0; p < kSlices; p += 2) {
+                        uint32_t t[4];
+                        dm_ldsm4(t, B + ((p + (lane >> 4)) * kTcN + wn * 8 + (lane & 7)) * kTcRow +
+                                        ks + ((lane >> 3) & 1) * 8);
+                        bf[p][0] = t[0];
+                        bf[p][1] = t[1];
+                        bf[p + 1][0] = t[2];
+                        bf[p + 1][1] = t[3];
                     }
 #pragma unroll
-                    for (int l = 0; l < kSlices; ++l) {
-                        float acc[4] = {0.f, 0.f, 0.f, 0.f};
+                    for (int l = 0; l < kSlices; ++l)
 #pragma unroll
-                        for (int p = 0; p <= l; ++p) dm_mma(acc, af[p], bf[l - p]);
-                        // exact integers |v| <= 2^21: bits of v + 1.5 * 2^23 carry v
-#pragma unroll
-                        for (int q = 0; q < 4; ++q) lev[l][q] += __float_as_uint(acc[q] + 12582912.f);
-                    }
-                    ++drains;
+                        for (int p = 0; p <= l; ++p) dm_mma(acc[l], af[p], bf[l - p]);
                 }
+                // bits of v + 1.5 * 2^23 carry the exact integer v (|v| < 2^22)
+#pragma unroll
+                for (int l = 0; l < kSlices; ++l)
+#pragma unroll
+                    for (int q = 0; q < 4; ++q) lev[l][q] += __float_as_uint(acc[l][q] + 12582912.f);
+                ++drains;
                 __syncthreads();
+                b ^= 1;
             }
             const uint32_t bias = drains * 0x4B400000u;
 #pragma unroll
@@ -730,6 +778,9 @@ __global__ void __launch_bounds__(kDmBlock, 2)
                 }
                 __syncthreads();
 
+                // Rows are accumulated with non-returning atomic adds (a row
+                // entry belongs to one thread, so they never contend) and read
+                // back through L2 (__ldcg) after the barrier.
                 // 2a. row sweep: a thread per pixel i of forest 1. Run sums are
                 // per-pixel factors of forest 2, scaled by those of pixel i at
                 // the flush (zfac = zf1 zf2, w12 = w1 w2, z = (z1 + z2) / 2,
@@ -768,8 +819,8 @@ __global__ void __launch_bounds__(kDmBlock, 2)
                         if (ml >= 0 && ml < mcc) {
                             if (ml != run_m) {
                                 if (run_m >= 0) {
-                                    E[(int64_t)run_m * kst + kU + i] -= __dmul_rn(zf1, e1);
-                                    if (ord2) E[(int64_t)run_m * kst + kV + i] -= __dmul_rn(zf1, e3);
+                                    atomicAdd(&E[(int64_t)run_m * kst + kU + i], -__dmul_rn(zf1, e1));
+                                    if (ord2) atomicAdd(&E[(int64_t)run_m * kst + kV + i], -__dmul_rn(zf1, e3));
                                 }
                                 run_m = ml;
                                 e1 = 0.;
@@ -783,8 +834,8 @@ __global__ void __launch_bounds__(kDmBlock, 2)
                             if (dl >= 0 && dl < dcc) {
                                 if (dl != run_d) {
                                     if (run_d >= 0) {
-                                        U[(int64_t)run_d * kst + kU + i] += __dmul_rn(w1, u);
-                                        if (ord2) U[(int64_t)run_d * kst + kV + i] += __dmul_rn(w1, v);
+                                        atomicAdd(&U[(int64_t)run_d * kst + kU + i], __dmul_rn(w1, u));
+                                        if (ord2) atomicAdd(&U[(int64_t)run_d * kst + kV + i], __dmul_rn(w1, v));
                                     }
                                     run_d = dl;
                                     u = 0.;
@@ -820,12 +871,12 @@ __global__ void __launch_bounds__(kDmBlock, 2)
                         }
                     }
                     if (run_m >= 0) {
-                        E[(int64_t)run_m * kst + kU + i] -= __dmul_rn(zf1, e1);
-                        if (ord2) E[(int64_t)run_m * kst + kV + i] -= __dmul_rn(zf1, e3);
+                        atomicAdd(&E[(int64_t)run_m * kst + kU + i], -__dmul_rn(zf1, e1));
+                        if (ord2) atomicAdd(&E[(int64_t)run_m * kst + kV + i], -__dmul_rn(zf1, e3));
                     }
                     if (run_d >= 0) {
-                        U[(int64_t)run_d * kst + kU + i] += __dmul_rn(w1, u);
-                        if (ord2) U[(int64_t)run_d * kst + kV + i] += __dmul_rn(w1, v);
+                        atomicAdd(&U[(int64_t)run_d * kst + kU + i], __dmul_rn(w1, u));
+                        if (ord2) atomicAdd(&U[(int64_t)run_d * kst + kV + i], __dmul_rn(w1, v));
                     }
                     if (run_k >= 0) flush_k();
                 }
@@ -847,8 +898,8 @@ __global__ void __launch_bounds__(kDmBlock, 2)
                         if (ml >= 0 && ml < mcc) {
                             if (ml != run_m) {
                                 if (run_m >= 0) {
-                                    E[(int64_t)run_m * kst + kX + j] -= __dmul_rn(zf2, e2);
-                                    if (ord1) E[(int64_t)run_m * kst + kY + j] -= __dmul_rn(zf2, e4);
+                                    atomicAdd(&E[(int64_t)run_m * kst + kX + j], -__dmul_rn(zf2, e2));
+                                    if (ord1) atomicAdd(&E[(int64_t)run_m * kst + kY + j], -__dmul_rn(zf2, e4));
                                 }
                                 run_m = ml;
                                 e2 = 0.;
@@ -862,8 +913,8 @@ __global__ void __launch_bounds__(kDmBlock, 2)
                             if (dl >= 0 && dl < dcc) {
                                 if (dl != run_d) {
                                     if (run_d >= 0) {
-                                        U[(int64_t)run_d * kst + kX + j] += __dmul_rn(w2, x);
-                                        if (ord1) U[(int64_t)run_d * kst + kY + j] += __dmul_rn(w2, y);
+                                        atomicAdd(&U[(int64_t)run_d * kst + kX + j], __dmul_rn(w2, x));
+                                        if (ord1) atomicAdd(&U[(int64_t)run_d * kst + kY + j], __dmul_rn(w2, y));
                                     }
                                     run_d = dl;
                                     x = 0.;
@@ -875,12 +926,12 @@ __global__ void __launch_bounds__(kDmBlock, 2)
                         }
                     }
                     if (run_m >= 0) {
-                        E[(int64_t)run_m * kst + kX + j] -= __dmul_rn(zf2, e2);
-                        if (ord1) E[(int64_t)run_m * kst + kY + j] -= __dmul_rn(zf2, e4);
+                        atomicAdd(&E[(int64_t)run_m * kst + kX + j], -__dmul_rn(zf2, e2));
+                        if (ord1) atomicAdd(&E[(int64_t)run_m * kst + kY + j], -__dmul_rn(zf2, e4));
                     }
                     if (run_d >= 0) {
-                        U[(int64_t)run_d * kst + kX + j] += __dmul_rn(w2, x);
-                        if (ord1) U[(int64_t)run_d * kst + kY + j] += __dmul_rn(w2, y);
+                        atomicAdd(&U[(int64_t)run_d * kst + kX + j], __dmul_rn(w2, x));
+                        if (ord1) atomicAdd(&U[(int64_t)run_d * kst + kY + j], __dmul_rn(w2, y));
                     }
                 }
                 __syncthreads();
@@ -893,23 +944,24 @@ __global__ void __launch_bounds__(kDmBlock, 2)
                         if (r < dcc) {
                             const double *row = U + (int64_t)r * kst;
                             for (int i = lane; i < n1; i += 32) {
-                                const double a = row[kU + i];
+                                const double a = __ldcg(row + kU + i);
                                 s0 += a;
                                 s2v += __dmul_rn(P1.dll[i], a);
-                                if (ord1 && ord2) s3 += __dmul_rn(P1.dll[i], row[kV + i]);
+                                if (ord1 && ord2) s3 += __dmul_rn(P1.dll[i], __ldcg(row + kV + i));
                             }
-                            for (int j = lane; j < n2; j += 32) s1v += __dmul_rn(P2.dll[j], row[kX + j]);
+                            for (int j = lane; j < n2; j += 32)
+                                s1v += __dmul_rn(P2.dll[j], __ldcg(row + kX + j));
                         } else {
                             const double *row = E + (int64_t)(r - dcc) * kst;
                             for (int i = lane; i < n1; i += 32) {
                                 const double a1 = __dmul_rn(P1.w[i], it.inv_sw1);
-                                const double e1 = row[kU + i];
+                                const double e1 = __ldcg(row + kU + i);
                                 s0 -= __dmul_rn(a1, e1);
-                                if (ord2) s1v -= __dmul_rn(a1, row[kV + i]);
+                                if (ord2) s1v -= __dmul_rn(a1, __ldcg(row + kV + i));
                                 if (ord1) {
                                     const double a7 = __dmul_rn(__dmul_rn(P1.w[i], P1.dll[i]), it.inv_q1);
                                     s2v -= __dmul_rn(a7, e1);
-                                    if (ord2) s3 -= __dmul_rn(a7, row[kV + i]);
+                                    if (ord2) s3 -= __dmul_rn(a7, __ldcg(row + kV + i));
                                 }
                             }
                         }
@@ -949,8 +1001,8 @@ __global__ void __launch_bounds__(kDmBlock, 2)
                         for (int k0 = 0; k0 < kst; k0 += kSlab) {
                             for (int e = tid; e < kTile * kSlab; e += kDmBlock) {
                                 const int rr = e / kSlab, kk = e % kSlab;
-                                ta[kk][rr] = (td + rr < dcc) ? U[(int64_t)(td + rr) * kst + k0 + kk] : 0.;
-                                tb[kk][rr] = (tm + rr < mcc) ? E[(int64_t)(tm + rr) * kst + k0 + kk] : 0.;
+                                ta[kk][rr] = (td + rr < dcc) ? __ldcg(U + (int64_t)(td + rr) * kst + k0 + kk) : 0.;
+                                tb[kk][rr] = (tm + rr < mcc) ? __ldcg(E + (int64_t)(tm + rr) * kst + k0 + kk) : 0.;
                             }
                             __syncthreads();
 #pragma unroll
