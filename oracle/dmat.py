@@ -1,7 +1,11 @@
-"""CPU oracle of picca's distortion matrix (TEST INFRASTRUCTURE ONLY).
+"""CPU oracle of picca's distortion matrices (TEST INFRASTRUCTURE ONLY).
 
 ``forest_pair`` drives the C restatement of
-``cf.compute_dmat_forest_pairs_fast`` (``dmat_oracle.c``, cf.py:519-887);
+``cf.compute_dmat_forest_pairs_fast`` (``dmat_oracle.c``, cf.py:519-887),
+``xforest`` that of ``xcf.compute_dmat_forest_pairs_fast`` (xcf.py:427-675)
+and ``xpipeline`` reproduces ``picca_xdmat.py`` (xcf.compute_dmat,
+py/picca/xcf.py:325-424, which skips forests without a kept neighbour
+before counting NPALL);
 ``pipeline`` reproduces ``picca_dmat.py`` for an auto-correlation
 (py/picca/bin/picca_dmat.py:21-38, :466-525 and cf.compute_dmat,
 py/picca/cf.py:390-517): healpix rows dealt to ``nproc`` chunks, NumPy's
@@ -62,6 +66,10 @@ def _lib():
             [_P(DmatParams)] + [d] * 10 + [ctypes.c_int64, ctypes.c_int64, ctypes.c_double,
                                            ctypes.c_double, ctypes.c_double, ctypes.c_int32,
                                            ctypes.c_int32, ctypes.c_int32] + [d] * 6)
+        lib.oracle_xdmat_forest.restype = None
+        lib.oracle_xdmat_forest.argtypes = (
+            [_P(DmatParams)] + [d] * 5 + [ctypes.c_int64] + [d] * 5 + [ctypes.c_int64,
+                                                                     ctypes.c_int32] + [d] * 6)
         lib._dmat_bound = True
     return lib
 
@@ -90,6 +98,17 @@ def forest_pair(params, ll1, ll2, r1, r2, m1, m2, z1, z2, w1, w2, zq1, zq2, ang,
                                                   "r_trans_eff", "z_eff", "weight_eff")])
 
 
+def xforest(params, ll1, r1, m1, z1, w1, r2, m2, z2, w2, ang, order1, outputs):
+    """Adds one forest and its kept objects to ``outputs``."""
+    a1 = [np.ascontiguousarray(a, dtype=np.float64) for a in (ll1, r1, m1, z1, w1)]
+    a2 = [np.ascontiguousarray(a, dtype=np.float64) for a in (r2, m2, z2, w2, ang)]
+    _lib().oracle_xdmat_forest(
+        ctypes.byref(params), *[_dp(a) for a in a1], len(a1[0]), *[_dp(a) for a in a2],
+        len(a2[0]), int(order1), *[_dp(outputs[k]) for k in ("weights_dmat", "dmat",
+                                                             "r_par_eff", "r_trans_eff",
+                                                             "z_eff", "weight_eff")])
+
+
 def selection(fs, offsets, nproc, reject):
     """Boolean mask over the neighbour list: the pairs picca_dmat.py keeps
     (rows dealt to nproc chunks, np.random.seed(first healpix of the chunk),
@@ -110,34 +129,75 @@ def selection(fs, offsets, nproc, reject):
     return mask, int(offsets[-1]), int(mask.sum())
 
 
-def pipeline(fs, params, ang_max, reject, nproc=1, order=1, redshift_evolution=True):
-    """picca_dmat.py on a ForestSet (auto-correlation). Returns the output
-    columns (WDM, DM, RP, RT, Z) and the pair counts."""
+def pipeline(fs, params, ang_max, reject, nproc=1, order=1, fs2=None):
+    """picca_dmat.py on a ForestSet (auto-correlation, or the cross with
+    ``fs2``). Returns the output columns (WDM, DM, RP, RT, Z) and the pair
+    counts."""
     oparams = cpu.make_params(params.r_par_min, params.r_par_max, params.r_trans_max,
                               params.num_bins_r_par, params.num_bins_r_trans)
-    offsets, index = cpu.neighbours(fs, fs, oparams, ang_max, auto_mode=1)
+    other = fs if fs2 is None else fs2
+    offsets, index = cpu.neighbours(fs, other, oparams, ang_max, auto_mode=int(fs2 is None))
     mask, npall, npused = selection(fs, offsets, nproc, reject)
     out = new_outputs(params)
-    po = np.asarray(fs.pix_offset)
+    po, po2 = np.asarray(fs.pix_offset), np.asarray(other.pix_offset)
     for f in range(fs.num):
         a0, a1 = po[f], po[f + 1]
         for k in range(int(offsets[f]), int(offsets[f + 1])):
             if not mask[k]:
                 continue
             g = int(index[k])
-            b0, b1 = po[g], po[g + 1]
+            b0, b1 = po2[g], po2[g + 1]
             ang = cpu.lib().oracle_angle(fs.x_cart[f], fs.y_cart[f], fs.z_cart[f], fs.ra[f],
-                                         fs.dec[f], fs.cos_dec[f], fs.x_cart[g], fs.y_cart[g],
-                                         fs.z_cart[g], fs.ra[g], fs.dec[g])
+                                         fs.dec[f], fs.cos_dec[f], other.x_cart[g],
+                                         other.y_cart[g], other.z_cart[g], other.ra[g],
+                                         other.dec[g])
             shp = params.remove_same_half_plate_close_pairs and (
-                fs.plate[f] == fs.plate[g]) and (
-                (fs.fiberid[f] <= 500 and fs.fiberid[g] <= 500) or
-                (fs.fiberid[f] > 500 and fs.fiberid[g] > 500))
-            forest_pair(params, fs.log_lambda[a0:a1], fs.log_lambda[b0:b1],
-                        fs.r_comov[a0:a1], fs.r_comov[b0:b1], fs.dist_m[a0:a1],
-                        fs.dist_m[b0:b1], fs.z[a0:a1], fs.z[b0:b1], fs.weights[a0:a1],
-                        fs.weights[b0:b1], fs.z_qso[f], fs.z_qso[g], ang, shp, order, order,
-                        out)
+                fs.plate[f] == other.plate[g]) and (
+                (fs.fiberid[f] <= 500 and other.fiberid[g] <= 500) or
+                (fs.fiberid[f] > 500 and other.fiberid[g] > 500))
+            forest_pair(params, fs.log_lambda[a0:a1], other.log_lambda[b0:b1],
+                        fs.r_comov[a0:a1], other.r_comov[b0:b1], fs.dist_m[a0:a1],
+                        other.dist_m[b0:b1], fs.z[a0:a1], other.z[b0:b1], fs.weights[a0:a1],
+                        other.weights[b0:b1], fs.z_qso[f], other.z_qso[g], ang, shp, order,
+                        order, out)
+    return normalise(out, params, npall, npused)
+
+
+def xselection(fs, offsets, nproc, reject):
+    """xcf.compute_dmat's draws (same generator use as ``selection``) and
+    its counts: forests without a kept neighbour add nothing to NPALL."""
+    mask, _, _ = selection(fs, offsets, nproc, reject)
+    npall = npused = 0
+    for f in range(fs.num):
+        k0, k1 = int(offsets[f]), int(offsets[f + 1])
+        used = int(mask[k0:k1].sum())
+        if used:
+            npall += k1 - k0
+            npused += used
+    return mask, npall, npused
+
+
+def xpipeline(fs, qs, params, ang_max, reject, nproc=1, order=1):
+    """picca_xdmat.py on a forest set and a quasar set."""
+    oparams = cpu.make_params(params.r_par_min, params.r_par_max, params.r_trans_max,
+                              params.num_bins_r_par, params.num_bins_r_trans)
+    offsets, index = cpu.neighbours(fs, qs, oparams, ang_max, auto_mode=0, xcf=True)
+    mask, npall, npused = xselection(fs, offsets, nproc, reject)
+    out = new_outputs(params)
+    po = np.asarray(fs.pix_offset)
+    for f in range(fs.num):
+        k0, k1 = int(offsets[f]), int(offsets[f + 1])
+        kept = [int(index[k]) for k in range(k0, k1) if mask[k]]
+        if not kept:
+            continue
+        ang = np.array([cpu.lib().oracle_angle(fs.x_cart[f], fs.y_cart[f], fs.z_cart[f],
+                                               fs.ra[f], fs.dec[f], fs.cos_dec[f],
+                                               qs.x_cart[g], qs.y_cart[g], qs.z_cart[g],
+                                               qs.ra[g], qs.dec[g]) for g in kept])
+        a = slice(po[f], po[f + 1])
+        xforest(params, fs.log_lambda[a], fs.r_comov[a], fs.dist_m[a], fs.z[a], fs.weights[a],
+                qs.obj_r_comov[kept], qs.obj_dist_m[kept], qs.z_qso[kept],
+                qs.obj_weight[kept], ang, order, out)
     return normalise(out, params, npall, npused)
 
 

@@ -39,6 +39,19 @@ CASES = {
 }
 
 
+# picca's golden distortion matrices (py/picca/tests/test_3_cor.py:318-347,
+# :489-520, :666-697, :858-1039): the correlation case whose flags they share,
+# plus the random rejection and no redshift evolution.
+DMAT_CASES = {"dmat": "cf", "dmat_zcuts": "cf_zcuts", "dmat_cross": "cf_cross",
+              "dmat_cross_zcuts": "cf_cross_zcuts", "xdmat": "xcf", "xdmat_zcuts": "xcf_zcuts"}
+DMAT_ARGS = ["--rej", "0.99", "--no-redshift-evolution"]
+
+
+def dmat_cli_args(case, base, out):
+    """Full command line of the picca_dmat / picca_xdmat drop-in."""
+    return cli_args(DMAT_CASES[case], base, out) + DMAT_ARGS
+
+
 def cli_args(case, base, out):
     """Full command line for the drop-in CLI."""
     spec = CASES[case]

@@ -14,6 +14,12 @@ Run once in a checkout that has the picca sources next to it
   command at ``py/picca/tests/test_3_cor.py:318-347``);
 * ``dmat_cases.npz``: inputs and outputs of picca's own
   ``cf.compute_dmat_forest_pairs_fast`` on forest pairs of the test data;
+* ``cor_dmat_zcuts.npz``, ``cor_dmat_cross.npz``, ``cor_dmat_cross_zcuts.npz``,
+  ``cor_xdmat.npz``, ``cor_xdmat_zcuts.npz``: picca's other golden distortion
+  matrices (``test_cor/*.fits.gz``, commands in py/picca/tests/test_3_cor.py);
+* ``xdmat_cases.npz``: inputs and outputs of picca's own
+  ``xcf.compute_dmat_forest_pairs_fast`` on forests of the test data and the
+  quasars around them;
 * ``pair_cases.npz``: inputs and outputs of picca's own
   ``cf.compute_xi_forest_pairs_fast`` and ``xcf.compute_xi_forest_pairs_fast``
   run here as plain Python (numba, healpy, fitsio, camb and iminuit replaced by
@@ -400,6 +406,85 @@ def _dmat_cases(reference_py, delta_dir, attributes):
     return case
 
 
+def _xdmat_cases(reference_py, delta_dir, attributes, catalogue):
+    """Inputs and outputs of picca's own xcf.compute_dmat_forest_pairs_fast
+    (run as plain Python) on forests of the test data with the quasars
+    around them."""
+    sys.dont_write_bytecode = True
+    _install_stand_ins()
+    if reference_py not in sys.path:
+        sys.path.insert(0, reference_py)
+    import picca.xcf as ref_xcf  # pylint: disable=import-outside-toplevel
+
+    cosmo = gb_constants.Cosmo(Om=0.315, verbose=False)
+    data, _, _, _ = gb_io.read_deltas(delta_dir, 16, 1215.67, 2.9, 2.25, cosmo,
+                                      delta_attributes=attributes)
+    objs, _ = gb_io.read_objects(catalogue, 16, 0, 10, 1.44, 2.25, cosmo)
+    deltas = [d for hp in sorted(data) for d in data[hp]]
+    quasars = [o for hp in sorted(objs) for o in objs[hp]]
+    rng = np.random.default_rng(20261205)
+    picks = []
+    for a in rng.permutation(len(deltas)):
+        d = deltas[a]
+        near = [o for o in quasars if o.thingid != d.thingid and
+                d.get_angle_between(o) < 0.02]
+        if len(near) >= 3:
+            picks.append((d, near[:12]))
+        if len(picks) >= 3:
+            break
+    variants = [
+        dict(name="xcf", np=30, nt=15, coef=1, zevol=False, order=1),
+        dict(name="xcf_zevol", np=30, nt=15, coef=1, zevol=True, order=1),
+        dict(name="xcf_coef2_order0", np=10, nt=8, coef=2, zevol=True, order=0),
+        dict(name="xcf_zcut", np=30, nt=15, coef=1, zevol=True, order=1, z_min_pairs=2.25,
+             z_max_pairs=2.6),
+    ]
+    out = {}
+    case = 0
+    for variant in variants:
+        for d, near in picks:
+            ref_xcf.r_par_min, ref_xcf.r_par_max, ref_xcf.r_trans_max = -60., 60., 60.
+            ref_xcf.num_bins_r_par, ref_xcf.num_bins_r_trans = variant["np"], variant["nt"]
+            ref_xcf.num_model_bins_r_par = variant["np"] * variant["coef"]
+            ref_xcf.num_model_bins_r_trans = variant["nt"] * variant["coef"]
+            ref_xcf.z_min_pairs = variant.get("z_min_pairs")
+            ref_xcf.z_max_pairs = variant.get("z_max_pairs")
+            ref_xcf.rmu_binning = False
+            ref_xcf.redshift_evolution_in_distortion_matrix = variant["zevol"]
+            ref_xcf.z_ref, ref_xcf.alpha, ref_xcf.alpha_obj = 2.25, 2.9, 1.44
+            nb = variant["np"] * variant["nt"]
+            nm = nb * variant["coef"] ** 2
+            arrays = dict(weights_dmat=np.zeros(nb), dmat=np.zeros(nb * nm),
+                          r_par_eff=np.zeros(nm), r_trans_eff=np.zeros(nm), z_eff=np.zeros(nm),
+                          weight_eff=np.zeros(nm))
+            ang = np.array([d.get_angle_between(o) for o in near])
+            r2 = np.array([o.r_comov for o in near])
+            m2 = np.array([o.dist_m for o in near])
+            w2 = np.array([o.weights for o in near])
+            z2 = np.array([o.z_qso for o in near])
+            ref_xcf.compute_dmat_forest_pairs_fast(
+                d.log_lambda, d.r_comov, d.dist_m, d.z, d.weights, r2, m2, z2, w2, ang,
+                arrays["weights_dmat"], arrays["dmat"], arrays["r_par_eff"],
+                arrays["r_trans_eff"], arrays["z_eff"], arrays["weight_eff"], variant["order"])
+            prefix = f"xd{case}_"
+            out[prefix + "params"] = np.array([
+                variant["np"], variant["nt"], variant["coef"], float(variant["zevol"]),
+                variant["order"],
+                np.nan if variant.get("z_min_pairs") is None else variant["z_min_pairs"],
+                np.nan if variant.get("z_max_pairs") is None else variant["z_max_pairs"]])
+            for key, val in (("ll1", d.log_lambda), ("r1", d.r_comov), ("m1", d.dist_m),
+                             ("z1", d.z), ("w1", d.weights), ("r2", r2), ("m2", m2),
+                             ("z2", z2), ("w2", w2), ("ang", ang)):
+                out[prefix + key] = np.asarray(val, dtype=float)
+            for key, val in arrays.items():
+                out[prefix + "out_" + key] = val
+            out[prefix + "name"] = np.asarray(variant["name"])
+            case += 1
+    out["num_cases"] = np.asarray(case)
+    np.savez_compressed(os.path.join(HERE, "xdmat_cases.npz"), **out)
+    return case
+
+
 def _continuum_cases(reference_py):
     """chi2 of picca's own LeastsSquaresContModel (least_squares_cont_model.py:
     65-197) on synthetic forests at several (zero_point, slope) points."""
@@ -466,8 +551,22 @@ def main(picca_root):
     ndm = _dmat_cases(os.path.join(picca_root, "py"),
                       os.path.join(tests, "test_delta", "Delta_LYA") + "/",
                       os.path.join(tests, "test_delta", "delta_attributes.fits.gz"))
+    extra_dmat(picca_root)
     print(f"wrote fixtures: {ncf} cf pair cases, {nxcf} xcf cases, {ncont} continuum cases, "
           f"{ndm} distortion-matrix cases")
+
+
+def extra_dmat(picca_root):
+    """The other golden distortion matrices (cf z cuts, the cross of two
+    delta sets, delta x quasar) and the xcf forest cases."""
+    tests = os.path.join(picca_root, "py", "picca", "tests", "data")
+    for case in ("dmat_zcuts", "dmat_cross", "dmat_cross_zcuts", "xdmat", "xdmat_zcuts"):
+        _convert_dmat(os.path.join(tests, "test_cor", case + ".fits.gz"),
+                      os.path.join(HERE, f"cor_{case}.npz"))
+    return _xdmat_cases(os.path.join(picca_root, "py"),
+                        os.path.join(tests, "test_delta", "Delta_LYA") + "/",
+                        os.path.join(tests, "test_delta", "delta_attributes.fits.gz"),
+                        os.path.join(tests, "test_delta", "cat.fits"))
 
 
 if __name__ == "__main__":
