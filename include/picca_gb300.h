@@ -24,6 +24,8 @@
  *                          py/picca/xcf.py:126-220, :223-322
  *  - pg_cf_dmat         <- cf.compute_dmat + cf.compute_dmat_forest_pairs_fast
  *                          py/picca/cf.py:390-517, :519-887
+ *  - pg_xcf_dmat        <- xcf.compute_dmat + xcf.compute_dmat_forest_pairs_fast
+ *                          py/picca/xcf.py:325-424, :427-675
  *  - pg_corr_params     <- the cf / xcf module globals set by
  *                          py/picca/bin/picca_cf.py:343-368 and
  *                          py/picca/bin/picca_xcf.py:351-373
@@ -396,6 +398,28 @@ int pg_cf_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_params
                const int32_t *pair_first, const int32_t *pair_second, const double *pair_angle,
                int64_t num_pairs, void *work, uint64_t work_bytes, const pg_dmat_sums *out,
                void *stream);
+
+/* Delta x quasar distortion matrix (py/picca/xcf.py:325-675,
+ * py/picca/bin/picca_xdmat.py). A work item q is forest item_forest[q] of
+ * `forests` with the quasars obj_index[item_start[q] .. item_start[q] +
+ * item_count[q]) of `objs` (at most PG_XDMAT_MAX_OBJECTS; a forest's kept
+ * quasars may be split over several items, their contributions add). The
+ * caller makes the random rejection and drops forests without a kept
+ * quasar (xcf.py:382-386). dparams->alpha2 is the quasars' redshift
+ * evolution (alpha_obj). obj_angle (optional, aligned with obj_index)
+ * overrides the angles computed from the unit vectors. r_par is signed;
+ * there is no half-plate veto and no velocity cut in the reference's
+ * kernel. */
+#define PG_XDMAT_MAX_OBJECTS 256
+int pg_xcf_dmat_work_bytes(pg_plan *plan, const pg_corr_params *params,
+                           const pg_dmat_params *dparams, int32_t max_pixels, int64_t max_ctas,
+                           uint64_t *bytes);
+int pg_xcf_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_params *dparams,
+                const pg_forest_set *forests, const pg_forest_set *objs, const double *log_lambda,
+                const int32_t *order, const int32_t *item_forest, const int32_t *item_start,
+                const int32_t *item_count, const int32_t *obj_index, const double *obj_angle,
+                int64_t num_items, void *work, uint64_t work_bytes, const pg_dmat_sums *out,
+                void *stream);
 
 #ifdef __cplusplus
 }

@@ -15,6 +15,7 @@ PG_MODE_FP64 = 0
 PG_MODE_FP32_GUARD = 1
 PG_DMAT_FP64 = 0
 PG_DMAT_SPLIT_BF16 = 1
+PG_XDMAT_MAX_OBJECTS = 256
 
 _P = ctypes.POINTER
 _c_double_p = ctypes.c_void_p  # device pointers are passed as integers
@@ -110,9 +111,17 @@ def lib():
     handle.pg_cf_dmat.argtypes += [ctypes.c_void_p] * 7 + [ctypes.c_int64, ctypes.c_void_p,
                                                            ctypes.c_uint64, _P(DmatSumsC),
                                                            ctypes.c_void_p]
+    handle.pg_xcf_dmat_work_bytes.argtypes = [
+        ctypes.c_void_p, _P(CorrParams), _P(DmatParamsC), ctypes.c_int32, ctypes.c_int64,
+        _P(ctypes.c_uint64)]
+    handle.pg_xcf_dmat.argtypes = [
+        ctypes.c_void_p, _P(CorrParams), _P(DmatParamsC), _P(ForestSetC), _P(ForestSetC)]
+    handle.pg_xcf_dmat.argtypes += [ctypes.c_void_p] * 7 + [ctypes.c_int64, ctypes.c_void_p,
+                                                            ctypes.c_uint64, _P(DmatSumsC),
+                                                            ctypes.c_void_p]
     for name in ("pg_plan_create", "pg_plan_destroy", "pg_plan_stats", "pg_cf_neighbours",
                  "pg_xcf_neighbours", "pg_cf_xi", "pg_xcf_xi", "pg_cf_dmat_work_bytes",
-                 "pg_cf_dmat"):
+                 "pg_cf_dmat", "pg_xcf_dmat_work_bytes", "pg_xcf_dmat"):
         getattr(handle, name).restype = ctypes.c_int
     _LIB = handle
     return handle

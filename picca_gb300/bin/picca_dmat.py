@@ -89,20 +89,21 @@ def parse_args(cmdargs=None):
     return parser.parse_args(cmdargs)
 
 
-def header_cards(args, num_pairs, num_pairs_used, blinding):
-    """Keywords of the DMAT HDU (py/picca/bin/picca_dmat.py:527-610; the
-    reference lists NPUSED, OMEGAM and OMEGAR twice, one card each)."""
+def header_cards(args, num_pairs, num_pairs_used, blinding, module=cf):
+    """Keywords of the DMAT HDU (py/picca/bin/picca_dmat.py:527-610 and
+    py/picca/bin/picca_xdmat.py, from the module globals of ``module``; the
+    references list NPUSED, OMEGAM and OMEGAR twice, one card each)."""
     return [
-        {"name": "RPMIN", "value": cf.r_par_min, "comment": "Minimum r-parallel [h^-1 Mpc]"},
-        {"name": "RPMAX", "value": cf.r_par_max, "comment": "Maximum r-parallel [h^-1 Mpc]"},
-        {"name": "RTMAX", "value": cf.r_trans_max, "comment": "Maximum r-transverse [h^-1 Mpc]"},
-        {"name": "NP", "value": cf.num_bins_r_par, "comment": "Number of bins in r-parallel"},
-        {"name": "NT", "value": cf.num_bins_r_trans, "comment": "Number of bins in r-transverse"},
+        {"name": "RPMIN", "value": module.r_par_min, "comment": "Minimum r-parallel [h^-1 Mpc]"},
+        {"name": "RPMAX", "value": module.r_par_max, "comment": "Maximum r-parallel [h^-1 Mpc]"},
+        {"name": "RTMAX", "value": module.r_trans_max, "comment": "Maximum r-transverse [h^-1 Mpc]"},
+        {"name": "NP", "value": module.num_bins_r_par, "comment": "Number of bins in r-parallel"},
+        {"name": "NT", "value": module.num_bins_r_trans, "comment": "Number of bins in r-transverse"},
         {"name": "COEFMOD", "value": args.coef_binning_model,
          "comment": "Coefficient for model binning"},
-        {"name": "ZMIN", "value": cf.z_min_pairs, "comment": "Minimum redshift of pairs"},
-        {"name": "ZMAX", "value": cf.z_max_pairs, "comment": "Maximum redshift of pairs"},
-        {"name": "REJ", "value": cf.reject, "comment": "Rejection factor"},
+        {"name": "ZMIN", "value": module.z_min_pairs, "comment": "Minimum redshift of pairs"},
+        {"name": "ZMAX", "value": module.z_max_pairs, "comment": "Maximum redshift of pairs"},
+        {"name": "REJ", "value": module.reject, "comment": "Rejection factor"},
         {"name": "NPALL", "value": int(num_pairs), "comment": "Number of pairs"},
         {"name": "NPUSED", "value": int(num_pairs_used), "comment": "Number of used pairs"},
         {"name": "OMEGAM", "value": args.fid_Om,
@@ -115,18 +116,19 @@ def header_cards(args, num_pairs, num_pairs_used, blinding):
          "comment": "Equation of state of dark energy of fiducial LambdaCDM cosmology"},
         {"name": "BLINDING", "value": blinding,
          "comment": "String specifying the blinding strategy"},
-        {"name": "RMU_BIN", "value": cf.rmu_binning, "comment": "True if binned in r, mu"},
+        {"name": "RMU_BIN", "value": module.rmu_binning, "comment": "True if binned in r, mu"},
     ]
 
 
-def write(path, result, args, blinding):
+def write(path, result, args, blinding, module=cf):
+    """The DMAT and ATTRI HDUs of picca_dmat.py / picca_xdmat.py."""
     dmat_name = "DM" if blinding == "none" else "DM_BLIND"
     dmat_hdu = {
         "columns": [result["WDM"], result["DM"]],
         "names": ["WDM", dmat_name],
         "comments": ["Sum of weight", "Distortion matrix"],
         "units": ["", ""],
-        "header": header_cards(args, result["NPALL"], result["NPUSED"], blinding),
+        "header": header_cards(args, result["NPALL"], result["NPUSED"], blinding, module),
         "extname": "DMAT",
     }
     attri = {

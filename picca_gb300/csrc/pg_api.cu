@@ -267,7 +267,7 @@ int pg_cf_dmat_work_bytes(pg_plan *plan, const pg_corr_params *params,
     if (rc) return rc;
     if ((rc = select_device(plan))) return rc;
     DmatConstHost h;
-    if ((rc = dmat_config(*params, *dparams, max_pixels1, max_pixels2, plan->num_sms, h)))
+    if ((rc = dmat_config(*params, *dparams, max_pixels1, max_pixels2, plan->num_sms, h, false)))
         return rc;
     if (max_ctas < 0) return PG_ERR_INVALID_ARGUMENT;
     const int64_t ctas = max_ctas > 0 ? std::min<int64_t>(max_ctas, h.max_grid) : h.max_grid;
@@ -299,7 +299,8 @@ int pg_cf_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_params
     if ((rc = reset_scratch(plan, st))) return rc;
     const pg_forest_set &other = s2 ? *s2 : *s1;
     DmatConstHost h;
-    if ((rc = dmat_config(*params, *dparams, s1->max_pixels, other.max_pixels, plan->num_sms, h)))
+    if ((rc = dmat_config(*params, *dparams, s1->max_pixels, other.max_pixels, plan->num_sms, h,
+                          false)))
         return rc;
     const uint64_t per_cta = (uint64_t)h.cta_doubles * sizeof(double);
     const uint64_t fit = work_bytes / per_cta;
@@ -419,6 +420,55 @@ int pg_mlp_features(pg_plan *plan, const pg_spectra *spectra, const pg_cont_mode
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     plan->last_stream = st;
     return launch_mlp_features(*spectra, *model, features, feat_stride, a0, plan->num_sms, st);
+}
+
+int pg_xcf_dmat_work_bytes(pg_plan *plan, const pg_corr_params *params,
+                           const pg_dmat_params *dparams, int32_t max_pixels, int64_t max_ctas,
+                           uint64_t *bytes) {
+    if (!plan || !bytes) return PG_ERR_INVALID_ARGUMENT;
+    int rc = validate_dmat(params, dparams);
+    if (rc) return rc;
+    if ((rc = select_device(plan))) return rc;
+    DmatConstHost h;
+    if ((rc = dmat_config(*params, *dparams, max_pixels, 0, plan->num_sms, h, true))) return rc;
+    if (max_ctas < 0) return PG_ERR_INVALID_ARGUMENT;
+    const int64_t ctas = max_ctas > 0 ? std::min<int64_t>(max_ctas, h.max_grid) : h.max_grid;
+    *bytes = (uint64_t)ctas * (uint64_t)h.cta_doubles * sizeof(double);
+    return PG_OK;
+}
+
+int pg_xcf_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_params *dparams,
+                const pg_forest_set *forests, const pg_forest_set *objs, const double *log_lambda,
+                const int32_t *order, const int32_t *item_forest, const int32_t *item_start,
+                const int32_t *item_count, const int32_t *obj_index, const double *obj_angle,
+                int64_t num_items, void *work, uint64_t work_bytes, const pg_dmat_sums *out,
+                void *stream) {
+    if (!plan || !forests || !objs || !out) return PG_ERR_INVALID_ARGUMENT;
+    int rc = validate_dmat(params, dparams);
+    if (rc) return rc;
+    if ((rc = validate_set(forests, true, false))) return rc;
+    if ((rc = validate_set(objs, false, objs->num > 0))) return rc;
+    if (!out->weights_dmat || !out->dmat || !out->r_par_eff || !out->r_trans_eff ||
+        !out->z_eff || !out->weight_eff)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (num_items < 0 || num_items > INT32_MAX) return PG_ERR_INVALID_ARGUMENT;
+    if (num_items > 0 && (!item_forest || !item_start || !item_count || !obj_index ||
+                          !log_lambda || !order || !work))
+        return PG_ERR_INVALID_ARGUMENT;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    if ((rc = reset_scratch(plan, st))) return rc;
+    DmatConstHost h;
+    if ((rc = dmat_config(*params, *dparams, forests->max_pixels, 0, plan->num_sms, h, true)))
+        return rc;
+    const uint64_t per_cta = (uint64_t)h.cta_doubles * sizeof(double);
+    const int grid = (int)std::min<uint64_t>((uint64_t)h.max_grid, work_bytes / per_cta);
+    if (num_items > 0 && grid < 1) return PG_ERR_INVALID_ARGUMENT;
+    if (reinterpret_cast<uintptr_t>(work) % 16) return PG_ERR_INVALID_ARGUMENT;
+    return launch_xcf_dmat(*params, *dparams, h, *forests, *objs, log_lambda, order, item_forest,
+                           item_start, item_count, obj_index, obj_angle, num_items,
+                           static_cast<double *>(work), grid, *out, scratch_of(plan), st);
 }
 
 }  // extern "C"

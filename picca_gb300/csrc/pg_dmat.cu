@@ -74,6 +74,7 @@ struct DmatConst {
     int64_t work_doubles;    // per-CTA scratch: U and E rows
     int64_t cta_doubles;     // list_doubles + work_doubles (+ digits and exponents)
     int32_t split;           // 1: tensor-core product (PG_DMAT_SPLIT_BF16)
+    int32_t xcf;             // 1: delta x quasar layout (forest, quasar slots)
 };
 
 // Shared-memory layout (bytes), identical on host and device.
@@ -83,12 +84,20 @@ struct DmSmem {
 
 __host__ __device__ inline size_t dm_align(size_t v, size_t a) { return (v + a - 1) / a * a; }
 
-__host__ __device__ inline DmSmem dm_smem(int p1, int p2, int mwords, int dwords, int split) {
+// Slot bytes per pixel: forest 1 of the auto-correlation (9 FP64 + 3 FP32
+// arrays), forest 2 and the forest of the cross (12 + 3), quasars (7 + 5).
+constexpr size_t kPix1Bytes = sizeof(double) * 9 + sizeof(float) * 3;
+constexpr size_t kPix2Bytes = sizeof(double) * 12 + sizeof(float) * 3;
+constexpr size_t kObjBytes = sizeof(double) * 7 + sizeof(float) * 5;
+constexpr int kXdObjects = PG_XDMAT_MAX_OBJECTS;  // quasars of one xcf work item
+
+__host__ __device__ inline DmSmem dm_smem(int p1, int p2, int mwords, int dwords, int split,
+                                          int xcf = 0) {
     DmSmem s;
     size_t o = 0;
-    s.f1 = o; o += (sizeof(double) * 9 + sizeof(float) * 3) * (size_t)p1;
+    s.f1 = o; o += (xcf ? kPix2Bytes : kPix1Bytes) * (size_t)p1;
     o = dm_align(o, 16);
-    s.f2 = o; o += (sizeof(double) * 12 + sizeof(float) * 3) * (size_t)p2;
+    s.f2 = o; o += (xcf ? kObjBytes : kPix2Bytes) * (size_t)p2;
     s.flags1 = o; o = dm_align(o + (size_t)p1, 8);
     s.flags2 = o; o = dm_align(o + (size_t)p2, 8);
     s.mbits = o; o += sizeof(uint32_t) * (size_t)mwords;
@@ -387,6 +396,59 @@ __device__ void dm_product_split(const double *U, const double *E, int dcc, int 
                 // v = sum_l lev_l 2^(-8 l); the level l product carries 2^(-8 (l + 2))
                 v = ldexp(v, rexp[dl] + rexp[dcc + ml] - 16);
                 if (v != 0.) atomicAdd(&dmat[(int64_t)dlist[dl] * nm + mlist[ml]], v);
+            }
+        }
+    }
+}
+
+// D = U E^T of one chunk in FP64 on the CUDA cores (32 x 32 tiles), added to
+// the global matrix like dm_product_split.
+__device__ void dm_product_fp64(const double *U, const double *E, int dcc, int mcc, int kst,
+                                double (*ta)[kTilePad], double (*tb)[kTilePad],
+                                const int32_t *dlist, const int32_t *mlist, int nm,
+                                double *dmat) {
+    const int tid = threadIdx.x;
+    const int tx = tid & 15, ty = tid >> 4;
+    for (int td = 0; td < dcc; td += kTile) {
+        for (int tm = 0; tm < mcc; tm += kTile) {
+            double acc[2][2];
+#pragma unroll
+            for (int a = 0; a < 2; ++a)
+#pragma unroll
+                for (int b2 = 0; b2 < 2; ++b2) acc[a][b2] = 0.;
+            for (int k0 = 0; k0 < kst; k0 += kSlab) {
+                for (int e = tid; e < kTile * kSlab; e += kDmBlock) {
+                    const int rr = e / kSlab, kk = e % kSlab;
+                    ta[kk][rr] = (td + rr < dcc) ? __ldcg(U + (int64_t)(td + rr) * kst + k0 + kk) : 0.;
+                    tb[kk][rr] = (tm + rr < mcc) ? __ldcg(E + (int64_t)(tm + rr) * kst + k0 + kk) : 0.;
+                }
+                __syncthreads();
+#pragma unroll
+                for (int kk = 0; kk < kSlab; ++kk) {
+                    double av[2], bv[2];
+#pragma unroll
+                    for (int a = 0; a < 2; ++a) av[a] = ta[kk][ty + 16 * a];
+#pragma unroll
+                    for (int b2 = 0; b2 < 2; ++b2) bv[b2] = tb[kk][tx + 16 * b2];
+#pragma unroll
+                    for (int a = 0; a < 2; ++a)
+#pragma unroll
+                        for (int b2 = 0; b2 < 2; ++b2)
+                            acc[a][b2] = __fma_rn(av[a], bv[b2], acc[a][b2]);
+                }
+                __syncthreads();
+            }
+#pragma unroll
+            for (int a = 0; a < 2; ++a) {
+                const int dl = td + ty + 16 * a;
+                if (dl >= dcc) continue;
+                const int64_t base = (int64_t)dlist[dl] * nm;
+#pragma unroll
+                for (int b2 = 0; b2 < 2; ++b2) {
+                    const int ml = tm + tx + 16 * b2;
+                    if (ml < mcc && acc[a][b2] != 0.)
+                        atomicAdd(&dmat[base + mlist[ml]], acc[a][b2]);
+                }
             }
         }
     }
@@ -984,56 +1046,426 @@ __global__ void __launch_bounds__(kDmBlock, 2)
                 if (tid == 0)
                     atomicAdd(&scratch->gemm_macs,
                               (unsigned long long)dcc * (unsigned long long)mcc * (kR + 4));
-                if (c.split) {
+                if (c.split)
                     dm_product_split(U, E, dcc, mcc, kst, digits, rexp, ta_raw, tb_raw,
                                      dlist + d0, mlist + m0, nm, out.dmat);
-                    __syncthreads();
+                else
+                    dm_product_fp64(U, E, dcc, mcc, kst, ta, tb, dlist + d0, mlist + m0, nm,
+                                    out.dmat);
+                __syncthreads();
+            }
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// Delta x quasar distortion matrix: xcf.compute_dmat (py/picca/xcf.py:325-424)
+// and xcf.compute_dmat_forest_pairs_fast (py/picca/xcf.py:427-675). A work
+// item is one forest with up to kXdObjects of its kept quasars. Only the
+// forest's continuum is projected out, so the product has the two kappa
+// blocks of the quasars: U = (sum_i w12, sum_i w12 dll1_i) per data bin and
+// E = -(eta2, eta4) per model bin; contributions of different quasars add,
+// so a forest's quasars may be split over items.
+
+// Per-quasar shared slots.
+struct DmObj {
+    double *r, *m, *z, *w, *zf, *cc, *ss;
+    float *rh, *rl, *mf, *ccf, *ssf;
+};
+
+__device__ __forceinline__ DmObj dm_obj(unsigned char *base, int n) {
+    DmObj x;
+    double *d = reinterpret_cast<double *>(base);
+    x.r = d; x.m = d + n; x.z = d + 2 * n; x.w = d + 3 * n; x.zf = d + 4 * n;
+    x.cc = d + 5 * n; x.ss = d + 6 * n;
+    float *f = reinterpret_cast<float *>(d + 7 * n);
+    x.rh = f; x.rl = f + n; x.mf = f + 2 * n; x.ccf = f + 3 * n; x.ssf = f + 4 * n;
+    return x;
+}
+
+// Decision of pixel i and quasar j: 0 outside, 1 inside (FP32 form), 2
+// inside (FP64 form, o.rp / o.rt / o.z set). r_par is signed.
+__device__ __forceinline__ int dm_decide_x(const DmatConst &c, const DmGuard &g, const DmPix &f,
+                                           const DmObj &q, int i, int j, DmPair &o) {
+    int st = 2;
+    if (!c.b.rmu) {
+        DmGuard gj = g;
+        gj.cc = q.ccf[j];
+        gj.ss = q.ssf[j];
+        st = dm_pair_f32(c, gj, f.rh[i], f.rl[i], f.mf[i], q.rh[j], q.rl[j], q.mf[j], false, o);
+    }
+    if (st == 0) return 0;
+    if (st == 2)
+        return dm_pair(c, f.r[i], f.m[i], f.z[i], q.r[j], q.m[j], q.z[j], q.cc[j], q.ss[j],
+                       false, o) ? 2 : 0;
+    o.zsel = true;
+    if (c.b.zmin_on || c.b.zmax_on) {
+        const double z = __dadd_rn(f.z[i], q.z[j]) / 2;
+        o.zsel = !((c.b.zmin_on && z < c.b.z_min) || (c.b.zmax_on && z > c.b.z_max));
+    }
+    return 1;
+}
+
+__global__ void __launch_bounds__(kDmBlock, 2)
+    xcf_dmat_kernel(DmatConst c, pg_forest_set fs, pg_forest_set qs, const double *ll,
+                    const int32_t *order, const int32_t *item_forest, const int32_t *item_start,
+                    const int32_t *item_count, const int32_t *obj_index,
+                    const double *obj_angle, int64_t num_items, pg_dmat_sums out, double *work,
+                    Scratch *scratch) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const DmSmem L = dm_smem(c.p1, c.p2, c.mwords, c.dwords, c.split, 1);
+    const DmPix F = dm_pix(smem + L.f1, c.p1, true);
+    const DmObj Q = dm_obj(smem + L.f2, c.p2);
+    uint32_t *mbits = reinterpret_cast<uint32_t *>(smem + L.mbits);
+    int32_t *mpref = reinterpret_cast<int32_t *>(smem + L.mpref);
+    uint32_t *dbits = reinterpret_cast<uint32_t *>(smem + L.dbits);
+    int32_t *dpref = reinterpret_cast<int32_t *>(smem + L.dpref);
+    double (*ta)[kTilePad] = reinterpret_cast<double (*)[kTilePad]>(smem + L.tile_a);
+    double (*tb)[kTilePad] = reinterpret_cast<double (*)[kTilePad]>(smem + L.tile_b);
+    uint16_t *ta_raw = reinterpret_cast<uint16_t *>(smem + L.tile_a);
+    uint16_t *tb_raw = reinterpret_cast<uint16_t *>(smem + L.tile_b);
+    __shared__ double red[kDmWarps];
+    __shared__ int red_int[kDmWarps];
+    __shared__ int s_item;
+    __shared__ int s_count;
+
+    const int tid = threadIdx.x;
+    const int nb = c.b.nbins, nm = c.nm;
+    double *cta = work + (int64_t)blockIdx.x * c.cta_doubles;
+    int32_t *dlist = reinterpret_cast<int32_t *>(cta);
+    int32_t *mlist = dlist + nb;
+    double *rows = cta + c.list_doubles;
+    uint16_t *digits = reinterpret_cast<uint16_t *>(rows + c.work_doubles);
+    int32_t *rexp = reinterpret_cast<int32_t *>(digits + (c.work_doubles * kSlices));
+
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(&scratch->work_counter, 1);
+        __syncthreads();
+        const int64_t q = s_item;
+        if (q >= num_items) break;
+        const int f = item_forest[q];
+        const int o0 = item_start[q];
+        const int n2 = item_count[q];
+        const int64_t p0 = fs.pix_offset[f];
+        const int n1 = (int)(fs.pix_offset[f + 1] - p0);
+        if (n1 > c.p1 || n2 > c.p2 || n2 < 0) {
+            if (tid == 0) report_error(scratch, PG_ERR_UNSUPPORTED, (int32_t)q);
+            __syncthreads();
+            continue;
+        }
+        const int ord1 = order[f] == 1;
+        // stage the forest and its quasars
+        double lmax = 0., lmmax = 0., lss = 0., lcc = 1.;
+        for (int t = tid; t < n1; t += kDmBlock) {
+            const double r = fs.r_comov[p0 + t], m = fs.dist_m[p0 + t];
+            F.r[t] = r;
+            F.m[t] = m;
+            F.z[t] = fs.z[p0 + t];
+            F.w[t] = fs.weights[p0 + t];
+            F.dll[t] = ll[p0 + t];
+            const float rh = (float)r;
+            F.rh[t] = rh;
+            F.rl[t] = (float)__dsub_rn(r, (double)rh);
+            F.mf[t] = (float)m;
+            lmax = fmax(lmax, fabs(r));
+            lmmax = fmax(lmmax, fabs(m));
+        }
+        for (int t = tid; t < n2; t += kDmBlock) {
+            const int g = obj_index[o0 + t];
+            const double r = qs.obj_r_comov[g], m = qs.obj_dist_m[g];
+            const double ang =
+                obj_angle ? obj_angle[o0 + t]
+                          : angle_between(fs.x_cart[f], fs.y_cart[f], fs.z_cart[f], fs.ra[f],
+                                          fs.dec[f], fs.cos_dec[f], qs.x_cart[g], qs.y_cart[g],
+                                          qs.z_cart[g], qs.ra[g], qs.dec[g]);
+            const double cc = cos(ang / 2), ss = sin(ang / 2);
+            Q.r[t] = r;
+            Q.m[t] = m;
+            Q.z[t] = qs.z_qso[g];
+            Q.w[t] = qs.obj_weight[g];
+            Q.cc[t] = cc;
+            Q.ss[t] = ss;
+            const float rh = (float)r;
+            Q.rh[t] = rh;
+            Q.rl[t] = (float)__dsub_rn(r, (double)rh);
+            Q.mf[t] = (float)m;
+            Q.ccf[t] = (float)cc;
+            Q.ssf[t] = (float)ss;
+            Q.zf[t] = c.redshift_evolution
+                          ? pow(__dadd_rn(1., Q.z[t]) / __dadd_rn(1., c.z_ref),
+                                __dsub_rn(c.alpha2, 1.))
+                          : 1.;
+            lmax = fmax(lmax, fabs(r));
+            lmmax = fmax(lmmax, fabs(m));
+            lss = fmax(lss, ss);
+            lcc = fmin(lcc, cc);
+        }
+        for (int t = tid; t < c.mwords; t += kDmBlock) mbits[t] = 0u;
+        for (int t = tid; t < c.dwords; t += kDmBlock) dbits[t] = 0u;
+        // guard bands as in the auto-correlation, with the extreme half-angles
+        double rmax, mmax, ssmax, ccmin;
+        {
+            for (int o = 16; o > 0; o >>= 1) {
+                lmax = fmax(lmax, __shfl_xor_sync(0xffffffffu, lmax, o));
+                lmmax = fmax(lmmax, __shfl_xor_sync(0xffffffffu, lmmax, o));
+                lss = fmax(lss, __shfl_xor_sync(0xffffffffu, lss, o));
+                lcc = fmin(lcc, __shfl_xor_sync(0xffffffffu, lcc, o));
+            }
+            double v[4] = {lmax, lmmax, lss, -lcc};
+            double res[4];
+            for (int k = 0; k < 4; ++k) {
+                __syncthreads();
+                if ((tid & 31) == 0) red[tid >> 5] = v[k];
+                __syncthreads();
+                double mx = -1e300;
+                for (int w = 0; w < kDmWarps; ++w) mx = fmax(mx, red[w]);
+                res[k] = mx;
+            }
+            rmax = res[0];
+            mmax = res[1];
+            ssmax = res[2];
+            ccmin = -res[3];
+        }
+        DmGuard gd;
+        {
+            const double u = 5.9604644775390625e-8;  // 2^-24
+            const double rlim = fmax(fabs(c.b.r_par_max), fabs(c.b.r_par_min));
+            const double gp = 2. * (2. * u * rmax + 3. * u * (rlim + 1.) / fmax(ccmin, 1e-6));
+            const double gt = 2. * (4. * u * mmax * ssmax + 2. * u * c.b.r_trans_max);
+            const double ey = 8. * u;
+            gd.cc = 1.f;
+            gd.ss = 0.f;
+            gd.gp = (float)gp;
+            gd.gt = (float)gt;
+            gd.gyp = (float)(gp * c.sp + ey * (c.b.np + 1));
+            gd.gymp = (float)(gp * c.smp + ey * (c.nmp + 1));
+            gd.gyt = (float)(gt * c.st + ey * (c.b.nt + 1));
+            gd.gymt = (float)(gt * c.smt + ey * (c.nmt + 1));
+        }
+        if (tid == 0) s_count = 0;
+        __syncthreads();
+
+        // 1. classification over (pixel, quasar)
+        {
+            int counted = 0;
+            for (int e = tid; e < n1 * n2; e += kDmBlock) {
+                const int j = e / n1, i = e - j * n1;
+                if (F.w[i] == 0. || Q.w[j] == 0.) continue;
+                DmPair o;
+                if (!dm_decide_x(c, gd, F, Q, i, j, o)) continue;
+                if (o.db < 0 || o.db >= nb || o.mb < 0 || o.mb >= nm) {
+                    report_error(scratch, PG_ERR_BIN_RANGE, o.mb);
                     continue;
                 }
-                const int tx = tid & 15, ty = tid >> 4;
-                for (int td = 0; td < dcc; td += kTile) {
-                    for (int tm = 0; tm < mcc; tm += kTile) {
-                        double acc[2][2];
-#pragma unroll
-                        for (int a = 0; a < 2; ++a)
-#pragma unroll
-                            for (int b2 = 0; b2 < 2; ++b2) acc[a][b2] = 0.;
-                        for (int k0 = 0; k0 < kst; k0 += kSlab) {
-                            for (int e = tid; e < kTile * kSlab; e += kDmBlock) {
-                                const int rr = e / kSlab, kk = e % kSlab;
-                                ta[kk][rr] = (td + rr < dcc) ? __ldcg(U + (int64_t)(td + rr) * kst + k0 + kk) : 0.;
-                                tb[kk][rr] = (tm + rr < mcc) ? __ldcg(E + (int64_t)(tm + rr) * kst + k0 + kk) : 0.;
+                ++counted;
+                const uint32_t mbit = 1u << (o.mb & 31);
+                if (!(mbits[o.mb >> 5] & mbit)) atomicOr(&mbits[o.mb >> 5], mbit);
+                if (o.zsel) {
+                    const uint32_t dbit = 1u << (o.db & 31);
+                    if (!(dbits[o.db >> 5] & dbit)) atomicOr(&dbits[o.db >> 5], dbit);
+                }
+            }
+            for (int o = 16; o > 0; o >>= 1) counted += __shfl_xor_sync(0xffffffffu, counted, o);
+            if ((tid & 31) == 0 && counted) atomicAdd(&s_count, counted);
+        }
+        __syncthreads();
+        if (s_count == 0) {
+            __syncthreads();
+            continue;
+        }
+        const int nmt = dm_scan_bits(mbits, mpref, c.mwords, red_int);
+        const int nbt = dm_scan_bits(dbits, dpref, c.dwords, red_int);
+        if (nbt == 0) {
+            __syncthreads();
+            continue;
+        }
+        if (tid == 0) atomicAdd(&scratch->work_items, 1ull);
+        for (int w = tid; w < c.mwords; w += kDmBlock) {
+            uint32_t bits = mbits[w];
+            int k = mpref[w];
+            while (bits) {
+                const int bit = __ffs(bits) - 1;
+                mlist[k++] = w * 32 + bit;
+                bits &= bits - 1u;
+            }
+        }
+        for (int w = tid; w < c.dwords; w += kDmBlock) {
+            uint32_t bits = dbits[w];
+            int k = dpref[w];
+            while (bits) {
+                const int bit = __ffs(bits) - 1;
+                dlist[k++] = w * 32 + bit;
+                bits &= bits - 1u;
+            }
+        }
+        // forest sums (py/picca/xcf.py:470-487) and per-pixel factors
+        double lw = 0., lsw = 0.;
+        for (int t = tid; t < n1; t += kDmBlock) {
+            lw += F.w[t];
+            lsw += __dmul_rn(F.dll[t], F.w[t]);
+        }
+        const double sw1 = dm_block_sum(lw, red);
+        const double sll1 = dm_block_sum(lsw, red);
+        const double mean1 = sll1 / sw1;
+        double q1 = 0.;
+        for (int t = tid; t < n1; t += kDmBlock) {
+            const double d = __dsub_rn(F.dll[t], mean1);
+            F.dll[t] = d;
+            q1 += __dmul_rn(F.w[t], __dmul_rn(d, d));
+            F.zf[t] = c.redshift_evolution
+                          ? pow(__dadd_rn(1., F.z[t]) / __dadd_rn(1., c.z_ref),
+                                __dsub_rn(c.alpha, 1.))
+                          : 1.;
+        }
+        const double swsll1 = dm_block_sum(q1, red);
+        if (ord1 && !(swsll1 != 0.)) {
+            if (tid == 0) report_error(scratch, PG_ERR_INVALID_ARGUMENT, (int32_t)q);
+            __syncthreads();
+            continue;
+        }
+        const double inv_sw1 = 1. / sw1, inv_q1 = 1. / swsll1;
+        for (int t = tid; t < n1; t += kDmBlock) {
+            const double wz = __dmul_rn(F.w[t], F.zf[t]);
+            F.a[t] = __dmul_rn(wz, inv_sw1);
+            F.b[t] = __dmul_rn(__dmul_rn(wz, F.dll[t]), inv_q1);
+            F.wd[t] = __dmul_rn(F.w[t], F.dll[t]);
+            F.wz[t] = wz;
+            F.wzz[t] = __dmul_rn(F.w[t], F.z[t]);
+            F.wm[t] = __dmul_rn(F.w[t], F.m[t]);
+        }
+        __syncthreads();
+
+        const int kX = 0, kY = n2;
+        const int kR = n2 + (ord1 ? n2 : 0);
+        const int kst = (int)dm_align((size_t)max(kR, 1), kSlab);
+        const int64_t cap = c.work_doubles / kst;
+        int dc = nbt, mc = nmt;
+        if ((int64_t)nbt + nmt > cap) {
+            dc = (int)min((int64_t)nbt, cap / 2);
+            mc = (int)(cap - dc);
+        }
+        // the sweep runs over (quasar, pixel segment): segs segments per quasar
+        const int segs = max(1, min(kDmBlock / max(n2, 1), (n1 + 7) / 8));
+        const int seg_len = (n1 + segs - 1) / segs;
+        for (int d0 = 0; d0 < nbt; d0 += dc) {
+            const int dcc = min(dc, nbt - d0);
+            for (int m0 = 0; m0 < nmt; m0 += mc) {
+                const int mcc = min(mc, nmt - m0);
+                const bool first = d0 == 0 && m0 == 0;
+                double *U = rows;
+                double *E = rows + (int64_t)dcc * kst;
+                {
+                    const int64_t n = (int64_t)(dcc + mcc) * kst / 2;
+                    double2 *pz = reinterpret_cast<double2 *>(rows);
+                    for (int64_t t = tid; t < n; t += kDmBlock) pz[t] = make_double2(0., 0.);
+                }
+                __syncthreads();
+                for (int e = tid; e < n2 * segs; e += kDmBlock) {
+                    const int j = e / segs, sg = e - j * segs;
+                    const int i0 = sg * seg_len, i1 = min(n1, i0 + seg_len);
+                    const double w2 = Q.w[j];
+                    if (w2 == 0.) continue;
+                    const double zf2 = Q.zf[j];
+                    int run_m = -1, run_d = -1;
+                    double e2 = 0., e4 = 0., x = 0., y = 0.;
+                    int64_t run_k = -1;
+                    int32_t k_db = 0, k_mb = 0;
+                    double k_dm = 0., k_w = 0., k_rp = 0., k_rt = 0., k_z = 0.;
+                    auto flush_k = [&]() {
+                        const double w2zf = __dmul_rn(w2, zf2);
+                        atomicAdd(&out.dmat[run_k], __dmul_rn(w2zf, k_dm));
+                        atomicAdd(&out.weights_dmat[k_db], __dmul_rn(w2, k_w));
+                        atomicAdd(&out.r_par_eff[k_mb], __dmul_rn(w2, k_rp));
+                        const double rt = c.b.rmu ? k_rt
+                                                  : __dmul_rn(__dadd_rn(k_rt,
+                                                                        __dmul_rn(Q.m[j], k_w)),
+                                                              Q.ss[j]);
+                        atomicAdd(&out.r_trans_eff[k_mb], __dmul_rn(w2, rt));
+                        atomicAdd(&out.z_eff[k_mb],
+                                  __dmul_rn(w2, __dmul_rn(0.5, __dadd_rn(k_z,
+                                                                         __dmul_rn(Q.z[j], k_w)))));
+                        atomicAdd(&out.weight_eff[k_mb], __dmul_rn(w2, k_w));
+                    };
+                    for (int i = i0; i < i1; ++i) {
+                        const double w1 = F.w[i];
+                        if (w1 == 0.) continue;
+                        DmPair o;
+                        const int st = dm_decide_x(c, gd, F, Q, i, j, o);
+                        if (!st) continue;
+                        if (o.db < 0 || o.db >= nb || o.mb < 0 || o.mb >= nm) continue;
+                        const int ml = dm_rank(mbits, mpref, o.mb) - m0;
+                        if (ml >= 0 && ml < mcc) {
+                            if (ml != run_m) {
+                                if (run_m >= 0) {
+                                    atomicAdd(&E[(int64_t)run_m * kst + kX + j], -__dmul_rn(zf2, e2));
+                                    if (ord1) atomicAdd(&E[(int64_t)run_m * kst + kY + j], -__dmul_rn(zf2, e4));
+                                }
+                                run_m = ml;
+                                e2 = 0.;
+                                e4 = 0.;
                             }
-                            __syncthreads();
-#pragma unroll
-                            for (int kk = 0; kk < kSlab; ++kk) {
-                                double av[2], bv[2];
-#pragma unroll
-                                for (int a = 0; a < 2; ++a) av[a] = ta[kk][ty + 16 * a];
-#pragma unroll
-                                for (int b2 = 0; b2 < 2; ++b2) bv[b2] = tb[kk][tx + 16 * b2];
-#pragma unroll
-                                for (int a = 0; a < 2; ++a)
-#pragma unroll
-                                    for (int b2 = 0; b2 < 2; ++b2)
-                                        acc[a][b2] = __fma_rn(av[a], bv[b2], acc[a][b2]);
-                            }
-                            __syncthreads();
+                            e2 += F.a[i];
+                            if (ord1) e4 += F.b[i];
                         }
-#pragma unroll
-                        for (int a = 0; a < 2; ++a) {
-                            const int dl = td + ty + 16 * a;
-                            if (dl >= dcc) continue;
-                            const int64_t base = (int64_t)dlist[d0 + dl] * nm;
-#pragma unroll
-                            for (int b2 = 0; b2 < 2; ++b2) {
-                                const int ml = tm + tx + 16 * b2;
-                                if (ml < mcc && acc[a][b2] != 0.)
-                                    atomicAdd(&out.dmat[base + mlist[m0 + ml]], acc[a][b2]);
+                        if (o.zsel) {
+                            const int dl = dm_rank(dbits, dpref, o.db) - d0;
+                            if (dl >= 0 && dl < dcc) {
+                                if (dl != run_d) {
+                                    if (run_d >= 0) {
+                                        atomicAdd(&U[(int64_t)run_d * kst + kX + j], __dmul_rn(w2, x));
+                                        if (ord1) atomicAdd(&U[(int64_t)run_d * kst + kY + j], __dmul_rn(w2, y));
+                                    }
+                                    run_d = dl;
+                                    x = 0.;
+                                    y = 0.;
+                                }
+                                x += w1;
+                                if (ord1) y += F.wd[i];
+                            }
+                            if (first) {
+                                const int64_t key = (int64_t)o.db * nm + o.mb;
+                                if (key != run_k) {
+                                    if (run_k >= 0) flush_k();
+                                    run_k = key;
+                                    k_db = o.db;
+                                    k_mb = o.mb;
+                                    k_dm = k_w = k_rp = k_rt = k_z = 0.;
+                                }
+                                k_dm += F.wz[i];
+                                k_w += w1;
+                                k_z += F.wzz[i];
+                                if (st == 2) {
+                                    k_rp += __dmul_rn(w1, o.rp);
+                                    if (c.b.rmu) k_rt += __dmul_rn(w1, o.rt);
+                                    else k_rt += F.wm[i];
+                                } else {
+                                    k_rp += __dmul_rn(w1, __dmul_rn(__dsub_rn(F.r[i], Q.r[j]),
+                                                                    Q.cc[j]));
+                                    k_rt += F.wm[i];
+                                }
                             }
                         }
                     }
+                    if (run_m >= 0) {
+                        atomicAdd(&E[(int64_t)run_m * kst + kX + j], -__dmul_rn(zf2, e2));
+                        if (ord1) atomicAdd(&E[(int64_t)run_m * kst + kY + j], -__dmul_rn(zf2, e4));
+                    }
+                    if (run_d >= 0) {
+                        atomicAdd(&U[(int64_t)run_d * kst + kX + j], __dmul_rn(w2, x));
+                        if (ord1) atomicAdd(&U[(int64_t)run_d * kst + kY + j], __dmul_rn(w2, y));
+                    }
+                    if (run_k >= 0) flush_k();
                 }
+                __syncthreads();
+                if (tid == 0)
+                    atomicAdd(&scratch->gemm_macs,
+                              (unsigned long long)dcc * (unsigned long long)mcc * kR);
+                if (c.split)
+                    dm_product_split(U, E, dcc, mcc, kst, digits, rexp, ta_raw, tb_raw,
+                                     dlist + d0, mlist + m0, nm, out.dmat);
+                else
+                    dm_product_fp64(U, E, dcc, mcc, kst, ta, tb, dlist + d0, mlist + m0, nm,
+                                    out.dmat);
                 __syncthreads();
             }
         }
@@ -1043,7 +1475,8 @@ __global__ void __launch_bounds__(kDmBlock, 2)
 }  // namespace
 
 int dmat_config(const pg_corr_params &p, const pg_dmat_params &d, int p1, int p2, int num_sms,
-                DmatConstHost &h) {
+                DmatConstHost &h, bool xcf) {
+    if (xcf) p2 = kXdObjects;
     if (d.num_model_bins_r_par <= 0 || d.num_model_bins_r_trans <= 0) return PG_ERR_INVALID_ARGUMENT;
     if (p1 <= 0 || p2 <= 0) return PG_ERR_INVALID_ARGUMENT;
     const int64_t nm = (int64_t)d.num_model_bins_r_par * d.num_model_bins_r_trans;
@@ -1052,14 +1485,15 @@ int dmat_config(const pg_corr_params &p, const pg_dmat_params &d, int p1, int p2
     const int mwords = (int)((nm + 31) / 32), dwords = (int)((nb + 31) / 32);
     if (d.product != PG_DMAT_FP64 && d.product != PG_DMAT_SPLIT_BF16) return PG_ERR_INVALID_ARGUMENT;
     const int split = d.product == PG_DMAT_SPLIT_BF16;
-    const DmSmem s = dm_smem(p1, p2, mwords, dwords, split);
+    const DmSmem s = dm_smem(p1, p2, mwords, dwords, split, xcf);
     if (s.total > 220 * 1024) return PG_ERR_UNSUPPORTED;
     h.smem = s.total;
     h.p1 = p1;
     h.p2 = p2;
     h.mwords = mwords;
     h.dwords = dwords;
-    const int64_t kcap = (int64_t)dm_align((size_t)2 * p1 + 2 * p2 + 4, kSlab);
+    const int64_t kcap = xcf ? (int64_t)dm_align((size_t)2 * p2, kSlab)
+                             : (int64_t)dm_align((size_t)2 * p1 + 2 * p2 + 4, kSlab);
     if (d.row_capacity < 0) return PG_ERR_INVALID_ARGUMENT;
     const int64_t wanted = d.row_capacity > 0 ? std::max<int64_t>(d.row_capacity, 2)
                                               : kDmatRowCapacity;
@@ -1070,11 +1504,13 @@ int dmat_config(const pg_corr_params &p, const pg_dmat_params &d, int p1, int p2
     const int64_t extra = split ? h.work_doubles * kSlices / 4 + h.work_doubles / 32 : 0;
     h.split = split;
     h.cta_doubles = (int64_t)dm_align((size_t)(h.list_doubles + h.work_doubles + extra), 32);
+    h.xcf = xcf;
     int occ = 0;
-    if (cudaFuncSetAttribute(cf_dmat_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)s.total) != cudaSuccess)
+    const void *fn = xcf ? (const void *)xcf_dmat_kernel : (const void *)cf_dmat_kernel;
+    if (cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)s.total) !=
+        cudaSuccess)
         return PG_ERR_CUDA;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, cf_dmat_kernel, kDmBlock, s.total) !=
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kDmBlock, s.total) !=
             cudaSuccess ||
         occ < 1)
         return PG_ERR_CUDA;
@@ -1082,13 +1518,7 @@ int dmat_config(const pg_corr_params &p, const pg_dmat_params &d, int p1, int p2
     return PG_OK;
 }
 
-int launch_cf_dmat(const pg_corr_params &p, const pg_dmat_params &d, const DmatConstHost &h,
-                   const pg_forest_set &s1, const pg_forest_set &s2, const double *ll1,
-                   const double *ll2, const int32_t *order1, const int32_t *order2,
-                   const int32_t *pair_first, const int32_t *pair_second,
-                   const double *pair_angle, int64_t num_pairs, double *work, int grid,
-                   const pg_dmat_sums &out, Scratch *scratch, cudaStream_t stream) {
-    if (num_pairs == 0) return PG_OK;
+static DmatConst dmat_const(const pg_corr_params &p, const pg_dmat_params &d, const DmatConstHost &h) {
     DmatConst c;
     c.b = make_binning(p);
     c.nmp = d.num_model_bins_r_par;
@@ -1120,9 +1550,39 @@ int launch_cf_dmat(const pg_corr_params &p, const pg_dmat_params &d, const DmatC
     c.work_doubles = h.work_doubles;
     c.cta_doubles = h.cta_doubles;
     c.split = h.split;
+    c.xcf = h.xcf;
+    return c;
+}
+
+int launch_cf_dmat(const pg_corr_params &p, const pg_dmat_params &d, const DmatConstHost &h,
+                   const pg_forest_set &s1, const pg_forest_set &s2, const double *ll1,
+                   const double *ll2, const int32_t *order1, const int32_t *order2,
+                   const int32_t *pair_first, const int32_t *pair_second,
+                   const double *pair_angle, int64_t num_pairs, double *work, int grid,
+                   const pg_dmat_sums &out, Scratch *scratch, cudaStream_t stream) {
+    if (num_pairs == 0) return PG_OK;
+    const DmatConst c = dmat_const(p, d, h);
     cf_dmat_kernel<<<grid, kDmBlock, h.smem, stream>>>(c, s1, s2, ll1, ll2, order1, order2,
                                                        pair_first, pair_second, pair_angle,
                                                        num_pairs, out, work, scratch);
+    return check_cuda(cudaGetLastError());
+}
+
+int launch_xcf_dmat(const pg_corr_params &p, const pg_dmat_params &d, const DmatConstHost &h,
+                    const pg_forest_set &forests, const pg_forest_set &objs, const double *ll,
+                    const int32_t *order, const int32_t *item_forest, const int32_t *item_start,
+                    const int32_t *item_count, const int32_t *obj_index,
+                    const double *obj_angle, int64_t num_items, double *work, int grid,
+                    const pg_dmat_sums &out, Scratch *scratch, cudaStream_t stream) {
+    if (num_items == 0) return PG_OK;
+    DmatConst c = dmat_const(p, d, h);
+    c.b.x_correlation = 1;  // r_par is signed in the cross-correlation
+    c.b.remove_shp = 0;
+    c.b.zerr_on = 0;
+    xcf_dmat_kernel<<<grid, kDmBlock, h.smem, stream>>>(c, forests, objs, ll, order, item_forest,
+                                                        item_start, item_count, obj_index,
+                                                        obj_angle, num_items, out, work,
+                                                        scratch);
     return check_cuda(cudaGetLastError());
 }
 

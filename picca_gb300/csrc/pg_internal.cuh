@@ -222,9 +222,18 @@ struct DmatConstHost {
     int64_t list_doubles, work_doubles, cta_doubles;
     int max_grid;
     int split;
+    int xcf;
 };
+// p1 / p2: pixel capacity of the two forests (cross: of the forest; the
+// quasar capacity of a work item is fixed).
 int dmat_config(const pg_corr_params &p, const pg_dmat_params &d, int p1, int p2, int num_sms,
-                DmatConstHost &h);
+                DmatConstHost &h, bool xcf);
+int launch_xcf_dmat(const pg_corr_params &p, const pg_dmat_params &d, const DmatConstHost &h,
+                    const pg_forest_set &forests, const pg_forest_set &objs, const double *ll,
+                    const int32_t *order, const int32_t *item_forest, const int32_t *item_start,
+                    const int32_t *item_count, const int32_t *obj_index,
+                    const double *obj_angle, int64_t num_items, double *work, int grid,
+                    const pg_dmat_sums &out, Scratch *scratch, cudaStream_t stream);
 int launch_cf_dmat(const pg_corr_params &p, const pg_dmat_params &d, const DmatConstHost &h,
                    const pg_forest_set &s1, const pg_forest_set &s2, const double *ll1,
                    const double *ll2, const int32_t *order1, const int32_t *order2,

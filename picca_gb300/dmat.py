@@ -235,3 +235,121 @@ def distortion_matrix(fs1, fs2, params, dparams, reject, nproc=1, engine=None, m
     result["forest_pairs_used"] = num_sel
     result["work_items"] = int(stats.work_items)
     return result
+
+
+# ---------------------------------------------------------------------------
+# Delta x quasar distortion matrix: xcf.compute_dmat (py/picca/xcf.py:325-424)
+# and picca_xdmat.py (py/picca/bin/picca_xdmat.py).
+
+def xcf_counts(nbr_offsets, mask):
+    """NPALL and NPUSED as xcf.compute_dmat counts them: a forest without a
+    kept quasar is skipped before its neighbours are counted
+    (py/picca/xcf.py:382-386)."""
+    offsets = np.asarray(nbr_offsets, dtype=np.int64)
+    csum = np.concatenate([[0], np.cumsum(mask, dtype=np.int64)])
+    kept = csum[offsets[1:]] - csum[offsets[:-1]]
+    counts = offsets[1:] - offsets[:-1]
+    return int(counts[kept > 0].sum()), int(kept.sum())
+
+
+def xcf_items(nbr_offsets, nbr_index, mask, npix, max_objects=_native.PG_XDMAT_MAX_OBJECTS):
+    """Work items of pg_xcf_dmat from the kept neighbours: (item_forest,
+    item_start, item_count, obj_index) with each forest's kept quasars in
+    chunks of at most max_objects, the costliest items first."""
+    offsets = np.asarray(nbr_offsets, dtype=np.int64)
+    kept = np.nonzero(mask)[0]
+    obj_index = np.asarray(nbr_index, dtype=np.int32)[kept]
+    forest = np.searchsorted(offsets, kept, side="right") - 1
+    if kept.size == 0:
+        z = np.zeros(0, dtype=np.int32)
+        return z, z, z, obj_index
+    starts = np.flatnonzero(np.r_[True, forest[1:] != forest[:-1]])
+    ends = np.r_[starts[1:], kept.size]
+    item_forest, item_start, item_count = [], [], []
+    for s0, s1 in zip(starts, ends):
+        for a in range(s0, s1, max_objects):
+            item_forest.append(forest[s0])
+            item_start.append(a)
+            item_count.append(min(max_objects, s1 - a))
+    item_forest = np.asarray(item_forest, dtype=np.int32)
+    item_start = np.asarray(item_start, dtype=np.int32)
+    item_count = np.asarray(item_count, dtype=np.int32)
+    cost = np.asarray(npix)[item_forest] * item_count
+    order = np.argsort(-cost, kind="stable")
+    return item_forest[order], item_start[order], item_count[order], obj_index
+
+
+class XDmatEngine(DmatEngine):
+    """Cross (delta x quasar) distortion-matrix sums on one CUDA device."""
+
+    def xwork_buffer(self, params, dparams, max_pixels, num_items):
+        nbytes = ctypes.c_uint64()
+        with torch.cuda.device(self.device):
+            check(_native.lib().pg_xcf_dmat_work_bytes(
+                self.engine.plan.handle, ctypes.byref(params), ctypes.byref(dparams),
+                int(max_pixels), int(num_items), ctypes.byref(nbytes)), "xdmat work size")
+        need = int(nbytes.value)
+        if self._work is None or self._work.numel() < need:
+            self._work = torch.empty(max(need, 16), dtype=torch.uint8, device=self.device)
+        return self._work
+
+    def xaccumulate(self, params, dparams, dev_forests, dev_objs, side, items, sums,
+                    angles=None):
+        """Launch pg_xcf_dmat; items = device int32 tensors (forest, start,
+        count, obj_index) and their number."""
+        item_forest, item_start, item_count, obj_index, num_items = items
+        work = self.xwork_buffer(params, dparams, dev_forests.max_pixels, max(num_items, 1))
+        out = DmatSumsC(*[sums[k].data_ptr() for k in ("weights_dmat", "dmat", "r_par_eff",
+                                                         "r_trans_eff", "z_eff", "weight_eff")])
+        with torch.cuda.device(self.device):
+            check(_native.lib().pg_xcf_dmat(
+                self.engine.plan.handle, ctypes.byref(params), ctypes.byref(dparams),
+                ctypes.byref(dev_forests.c), ctypes.byref(dev_objs.c), side[0].data_ptr(),
+                side[1].data_ptr(), item_forest.data_ptr(), item_start.data_ptr(),
+                item_count.data_ptr(), obj_index.data_ptr(),
+                angles.data_ptr() if angles is not None else None, int(num_items),
+                work.data_ptr(), int(work.numel()), ctypes.byref(out),
+                self.engine._stream()), "cross distortion matrix")
+        return sums
+
+    def device_items(self, item_forest, item_start, item_count, obj_index):
+        dev = self.device
+
+        def up(a):
+            a = np.asarray(a, dtype=np.int32)
+            return torch.from_numpy(a if a.size else np.zeros(1, dtype=np.int32)).to(dev)
+        return (up(item_forest), up(item_start), up(item_count), up(obj_index),
+                int(len(item_forest)))
+
+
+def cross_distortion_matrix(fs, qs, params, dparams, reject, nproc=1, engine=None, mask=None):
+    """picca_xdmat.py on a forest set and a quasar set: neighbours, the
+    random rejection of ``nproc`` chunks, the GPU sums and the
+    normalisation. Returns the normalised columns, the raw sums (host) and
+    run statistics."""
+    dm = engine if isinstance(engine, XDmatEngine) else XDmatEngine(engine)
+    pe = dm.engine
+    dev1 = _pairs.DeviceForests(fs, pe.device)
+    dev2 = _pairs.DeviceForests(qs, pe.device)
+    offsets, index, total = pe.neighbours(params, dev1, dev2, xcf=True)
+    offsets_h = offsets.cpu().numpy()
+    index_h = index.cpu().numpy()[:total]
+    if mask is None:
+        mask = selection_mask(fs.healpix_list, fs.row, offsets_h, nproc, reject)
+    npall, npused = xcf_counts(offsets_h, mask)
+    items = xcf_items(offsets_h, index_h, mask, dev1.npix)
+    if len(items[0]):
+        check_orders(fs, np.unique(items[0]))
+    ditems = dm.device_items(*items)
+    side = DmatEngine.side_arrays(dev1, pe.device)
+    sums = dm.alloc_sums(params, dparams)
+    dm.xaccumulate(params, dparams, dev1, dev2, side, ditems, sums)
+    stats = pe.stats()
+    raw = {k: v.cpu().numpy() for k, v in sums.items()}
+    result = normalise(raw, params, dparams, npall, npused)
+    result["raw"] = raw
+    result["work_items"] = int(stats.work_items)
+    result["items"] = int(ditems[4])
+    result["pixel_object_pairs"] = float(np.sum(dev1.npix[items[0]].astype(np.float64) *
+                                                items[2]))
+    return result

@@ -1,14 +1,16 @@
 """Drop-in replacement for the correlation part of ``picca.xcf``.
 
 Same module globals (py/picca/xcf.py:27-68) and functions ``fill_neighs``
-(:71-123), ``compute_xi`` (:126-220) and the 16-argument
-``compute_xi_forest_pairs_fast`` (:223-322), computed on the GPU. As in
-``picca_gb300.cf``, the first call runs every healpix in one launch
-(``compute_xi_all``) and later calls are served from that result.
+(:71-123), ``compute_xi`` (:126-220), the 16-argument
+``compute_xi_forest_pairs_fast`` (:223-322), ``compute_dmat`` (:325-424) and
+the 17-argument ``compute_dmat_forest_pairs_fast`` (:427-675), computed on
+the GPU. As in ``picca_gb300.cf``, the first call runs every healpix in one
+launch (``compute_xi_all``) and later calls are served from that result.
 """
 
 import numpy as np
 
+from . import dmat as _dmat
 from . import pairs as _pairs
 from .forests import ForestSet
 
@@ -46,9 +48,15 @@ cosmo = None
 rmu_binning = False
 ang_correlation = False
 
+# variables for distortion matrix
+redshift_evolution_in_distortion_matrix = True
+# arithmetic of the distortion-matrix eta products: "split_bf16" or "fp64"
+dmat_product = "split_bf16"
+
 precision = "fp32_guard"
 
-_cache = {"key": None, "result": None, "engine": None}
+_cache = {"key": None, "result": None, "engine": None, "dmat_engine": None, "nbr_key": None,
+          "nbr": None}
 
 
 def _mode():
@@ -180,3 +188,161 @@ def compute_xi_forest_pairs_fast(z1, r_comov1, dist_m1, weights1, delta1, z2, r_
     rebin_r_trans += rt
     rebin_z += zz
     rebin_num_pairs += nb
+
+
+def _dmat_params():
+    if num_model_bins_r_par is None or num_model_bins_r_trans is None:
+        raise ValueError("xcf.num_model_bins_r_par / num_model_bins_r_trans must be set "
+                         "before computing a distortion matrix")
+    return _dmat.make_dmat_params(
+        num_bins_r_par, num_bins_r_trans,
+        redshift_evolution=redshift_evolution_in_distortion_matrix,
+        z_ref=2.25 if z_ref is None else z_ref, alpha=2.9 if alpha is None else alpha,
+        alpha2=1.44 if alpha_obj is None else alpha_obj,
+        num_model_bins_r_par=num_model_bins_r_par,
+        num_model_bins_r_trans=num_model_bins_r_trans, product=dmat_product)
+
+
+def _dmat_engine():
+    if _cache["dmat_engine"] is None:
+        _cache["dmat_engine"] = _dmat.XDmatEngine(_engine())
+    return _cache["dmat_engine"]
+
+
+def _neighbour_state():
+    """Device forests, quasars and the quasar-neighbour CSR, cached."""
+    key = _state_key()
+    if _cache["nbr_key"] == key and _cache["nbr"] is not None:
+        return _cache["nbr"]
+    if data is None or objs is None:
+        raise ValueError("xcf.data and xcf.objs must be set")
+    if ang_correlation:
+        raise ValueError("the distortion matrix has no angular form")
+    engine = _engine()
+    fs = ForestSet.from_deltas(data)
+    qs = ForestSet.from_objects(objs)
+    dev1 = _pairs.DeviceForests(fs, engine.device)
+    dev2 = _pairs.DeviceForests(qs, engine.device)
+    offsets, index, total = engine.neighbours(_params(), dev1, dev2, xcf=True)
+    state = {"set1": fs, "set2": qs, "dev1": dev1, "dev2": dev2,
+             "offsets": offsets.cpu().numpy(), "index": index.cpu().numpy()[:total],
+             "total": total}
+    _cache["nbr_key"] = key
+    _cache["nbr"] = state
+    return state
+
+
+def _dmat_sums(state, mask):
+    engine = _dmat_engine()
+    items = _dmat.xcf_items(state["offsets"], state["index"], mask, state["dev1"].npix)
+    if len(items[0]):
+        _dmat.check_orders(state["set1"], np.unique(items[0]))
+    ditems = engine.device_items(*items)
+    side = _dmat.DmatEngine.side_arrays(state["dev1"], engine.device)
+    params, dparams = _params(), _dmat_params()
+    sums = engine.alloc_sums(params, dparams)
+    engine.xaccumulate(params, dparams, state["dev1"], state["dev2"], side, ditems, sums)
+    engine.engine.stats()
+    return {k: v.cpu().numpy() for k, v in sums.items()}
+
+
+def compute_dmat(healpixs):
+    """Raw cross distortion-matrix sums of ``healpixs``
+    (py/picca/xcf.py:325-424): ``np.random.rand(len(neighbours)) > reject``
+    from NumPy's global generator for every delta, forests without a kept
+    quasar skipped before counting; the kept pairs run on the GPU. Returns
+    ``(weights_dmat, dmat [nb, nm], r_par_eff, r_trans_eff, z_eff,
+    weight_eff, num_pairs, num_pairs_used)``."""
+    state = _neighbour_state()
+    fs = state["set1"]
+    offsets = state["offsets"]
+    firsts = np.searchsorted(fs.row, np.arange(len(fs.healpix_list)))
+    mask = np.zeros(int(state["total"]), dtype=bool)
+    num_pairs = 0
+    num_pairs_used = 0
+    for healpix in healpixs:
+        row = int(np.searchsorted(fs.healpix_list, healpix))
+        for k, delta in enumerate(data[healpix]):
+            if getattr(delta, "order", None) is None:
+                raise RuntimeError("Trying to compute the distortion matrix but order is not "
+                                   "defined for the deltas. Check previous warning to solve "
+                                   "this issue")
+            f = firsts[row] + k
+            start, end = int(offsets[f]), int(offsets[f + 1])
+            w = np.random.rand(end - start) > reject
+            if w.sum() == 0:
+                continue
+            num_pairs += end - start
+            num_pairs_used += int(w.sum())
+            mask[start:end] = w
+    raw = _dmat_sums(state, mask)
+    for healpix in healpixs:
+        for delta in data[healpix]:
+            if hasattr(delta, "neighbours"):
+                delta.neighbours = None
+    nb = num_bins_r_par * num_bins_r_trans
+    return (raw["weights_dmat"], raw["dmat"].reshape(nb, -1), raw["r_par_eff"],
+            raw["r_trans_eff"], raw["z_eff"], raw["weight_eff"], num_pairs, num_pairs_used)
+
+
+def compute_dmat_all(nproc):
+    """The whole picca_xdmat.py computation for ``nproc`` processes (random
+    rejection per chunk of healpix) in one GPU pass; normalised columns
+    (WDM, DM, RP, RT, Z) and NPALL / NPUSED."""
+    state = _neighbour_state()
+    fs = state["set1"]
+    _dmat.check_orders(fs, np.arange(fs.num))
+    mask = _dmat.selection_mask(fs.healpix_list, fs.row, state["offsets"], nproc, reject)
+    npall, npused = _dmat.xcf_counts(state["offsets"], mask)
+    raw = _dmat_sums(state, mask)
+    result = _dmat.normalise(raw, _params(), _dmat_params(), npall, npused)
+    result["raw"] = raw
+    return result
+
+
+def compute_dmat_forest_pairs_fast(log_lambda1, r_comov1, dist_m1, z1, weights1, r_comov2,
+                                   dist_m2, z2, weights2, ang, weights_dmat, dmat, r_par_eff,
+                                   r_trans_eff, z_eff, weight_eff, order1):
+    """One forest against quasar arrays, accumulated in place
+    (py/picca/xcf.py:427-445 signature)."""
+    import torch  # pylint: disable=import-outside-toplevel
+
+    n = len(z1)
+    m = len(z2)
+    if m == 0:
+        return
+    fs = ForestSet(
+        pix_offset=np.array([0, n], dtype=np.int64), z=np.asarray(z1, float),
+        r_comov=np.asarray(r_comov1, float), dist_m=np.asarray(dist_m1, float),
+        weights=np.asarray(weights1, float), delta=np.zeros(n),
+        log_lambda=np.asarray(log_lambda1, float), ra=np.zeros(1), dec=np.zeros(1),
+        x_cart=np.ones(1), y_cart=np.zeros(1), z_cart=np.zeros(1), cos_dec=np.ones(1),
+        z_qso=np.zeros(1), thingid=np.array([-1]), order=np.array([int(order1)]),
+        healpix=np.zeros(1, dtype=np.int64))
+    qs = ForestSet(
+        ra=np.zeros(m), dec=np.zeros(m), x_cart=np.ones(m), y_cart=np.zeros(m),
+        z_cart=np.zeros(m), cos_dec=np.ones(m), z_qso=np.asarray(z2, float),
+        obj_r_comov=np.asarray(r_comov2, float), obj_dist_m=np.asarray(dist_m2, float),
+        obj_weight=np.asarray(weights2, float), thingid=np.arange(m, dtype=np.int64),
+        healpix=np.zeros(m, dtype=np.int64))
+    engine = _dmat_engine()
+    dev = engine.device
+    dev1 = _pairs.DeviceForests(fs, dev)
+    dev2 = _pairs.DeviceForests(qs, dev)
+    params, dparams = _params(np.pi), _dmat_params()
+    side = _dmat.DmatEngine.side_arrays(dev1, dev)
+    nitem = (m + _dmat._native.PG_XDMAT_MAX_OBJECTS - 1) // _dmat._native.PG_XDMAT_MAX_OBJECTS
+    starts = np.arange(nitem) * _dmat._native.PG_XDMAT_MAX_OBJECTS
+    counts = np.minimum(m - starts, _dmat._native.PG_XDMAT_MAX_OBJECTS)
+    ditems = engine.device_items(np.zeros(nitem), starts, counts, np.arange(m))
+    angles = torch.tensor(np.asarray(ang, dtype=float).reshape(-1), dtype=torch.float64,
+                          device=dev)
+    sums = engine.alloc_sums(params, dparams)
+    engine.xaccumulate(params, dparams, dev1, dev2, side, ditems, sums, angles=angles)
+    engine.engine.stats()
+    weights_dmat += sums["weights_dmat"].cpu().numpy()
+    dmat += sums["dmat"].cpu().numpy().reshape(np.shape(dmat))
+    r_par_eff += sums["r_par_eff"].cpu().numpy()
+    r_trans_eff += sums["r_trans_eff"].cpu().numpy()
+    z_eff += sums["z_eff"].cpu().numpy()
+    weight_eff += sums["weight_eff"].cpu().numpy()
