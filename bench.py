@@ -316,6 +316,7 @@ def dmat_leg(args, fs, params, ang_max, cpu_seconds):
     torch.cuda.empty_cache()
     cpu_pairs, cpu_pix, cpu_desc, cores = dmat_cpu_sample(fs, params, dparams, (f_h, g_h),
                                                           cpu_seconds)
+    cross = xdmat_leg(args, fs, params, ang_max, engine)
     return {
         "metric": "distortion-matrix forest pairs per second",
         "value": nsel / kernel_s, "unit": "forest-pairs/s",
@@ -336,7 +337,61 @@ def dmat_leg(args, fs, params, ang_max, cpu_seconds):
         "cpu_baseline": {"value": cpu_pairs, "unit": "forest-pairs/s",
                          "pixel_pairs_per_s": cpu_pix, "cores": cores, "kind": "port",
                          "sample": cpu_desc},
+        "cross": cross,
     }
+
+
+def xdmat_leg(args, fs, params, ang_max, engine):
+    """Delta x quasar distortion matrix (picca_xdmat.py defaults: r_par -200
+    to 200, 100 x 50 bins, redshift evolution) of the same forests against
+    1.5 quasars per forest on the same area, random rejection
+    args.dmat_reject: one warm-up and one timed kernel launch."""
+    import torch
+
+    from picca_gb300 import dmat, pairs, synthetic
+    if args.config not in ("1", "2"):
+        return None
+    num, area, _, _ = CONFIGS[args.config]
+    half = 20.0 if area <= 4000 else 30.0
+    ra_r, dec_r = synthetic.band_for_area(area, half)
+    qs = synthetic.make_quasars(int(1.5 * num), 20261207, ra_r, dec_r)
+    xparams = dict(params, r_par_min=-200.0, num_bins_r_par=100)
+    cparams = pairs.make_params(ang_max=ang_max, x_correlation=True, **xparams)
+    dparams = dmat.make_dmat_params(100, 50, alpha2=1.44, product=args.dmat_product)
+    xeng = dmat.XDmatEngine(engine.engine)
+    pe = xeng.engine
+    dev1 = pairs.DeviceForests(fs, pe.device)
+    dev2 = pairs.DeviceForests(qs, pe.device)
+    offsets, index, total = pe.neighbours(cparams, dev1, dev2, xcf=True)
+    offsets_h = offsets.cpu().numpy()
+    mask = dmat.selection_mask(fs.healpix_list, fs.row, offsets_h, 1, args.dmat_reject)
+    items = dmat.xcf_items(offsets_h, index.cpu().numpy()[:total], mask, dev1.npix)
+    ditems = xeng.device_items(*items)
+    side = dmat.DmatEngine.side_arrays(dev1, pe.device)
+    stream = torch.cuda.current_stream()
+    times = []
+    for _ in range(2):
+        sums = xeng.alloc_sums(cparams, dparams)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        xeng.xaccumulate(cparams, dparams, dev1, dev2, side, ditems, sums)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+        pe.stats()
+    kept = int(mask.sum())
+    pix_obj = float(np.sum(dev1.npix[items[0]].astype(np.float64) * items[2]))
+    del dev1, dev2, sums, side, ditems
+    torch.cuda.empty_cache()
+    return {"metric": "cross distortion-matrix kept forest-quasar pairs per second",
+            "value": kept / times[-1], "unit": "forest-quasar-pairs/s",
+            "pixel_quasar_pairs_per_s": pix_obj / times[-1], "kernel_ms": times[-1] * 1e3,
+            "config": {"quasars": qs.num, "neighbour_pairs": int(total), "kept_pairs": kept,
+                       "work_items": int(len(items[0])),
+                       "bins": "100 x 50, r_par -200 to 200 Mpc/h"}}
+
 
 
 def continuum_leg(args, cpu_seconds):
