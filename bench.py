@@ -333,7 +333,11 @@ def dmat_leg(args, fs, params, ang_max, cpu_seconds):
         "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "gemm_macs": macs,
                      "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
-                     "achieved_counts": "2 x multiply-adds of the per-pair U E^T products"},
+                     "achieved_counts": "2 x multiply-adds of the per-pair U E^T products",
+                     "note": "the products are FP64-accurate (exact 8-bit digit products on "
+                             "the BF16 tensor cores unless --dmat-product fp64): frac above 1 "
+                             "is their rate over the native FP64 rate; the FP64 pipe (run "
+                             "sums) is the busiest unit in the ncu capture"},
         "cpu_baseline": {"value": cpu_pairs, "unit": "forest-pairs/s",
                          "pixel_pairs_per_s": cpu_pix, "cores": cores, "kind": "port",
                          "sample": cpu_desc},
