@@ -17,6 +17,8 @@ Run once in a checkout that has the picca sources next to it
 * ``cor_dmat_zcuts.npz``, ``cor_dmat_cross.npz``, ``cor_dmat_cross_zcuts.npz``,
   ``cor_xdmat.npz``, ``cor_xdmat_zcuts.npz``: picca's other golden distortion
   matrices (``test_cor/*.fits.gz``, commands in py/picca/tests/test_3_cor.py);
+* ``cor_metal_dmat.npz``: picca's golden metal distortion matrix
+  (``test_cor/metal_dmat.fits.gz``);
 * ``xdmat_cases.npz``: inputs and outputs of picca's own
   ``xcf.compute_dmat_forest_pairs_fast`` on forests of the test data and the
   quasars around them;
@@ -552,8 +554,31 @@ def main(picca_root):
                       os.path.join(tests, "test_delta", "Delta_LYA") + "/",
                       os.path.join(tests, "test_delta", "delta_attributes.fits.gz"))
     extra_dmat(picca_root)
+    extra_metal(picca_root)
     print(f"wrote fixtures: {ncf} cf pair cases, {nxcf} xcf cases, {ncont} continuum cases, "
           f"{ndm} distortion-matrix cases")
+
+
+def _convert_metal_dmat(src, out_path):
+    hdul = fitsio_lite.FITS(src)
+    attri = hdul["ATTRI"]
+    mdmat = hdul["MDMAT"]
+    out = {c: mdmat[c][:] for c in mdmat.get_colnames()}
+    out["NPALL"] = attri["NPALL"][:]
+    out["NPUSED"] = attri["NPUSED"][:]
+    out["ABS_IGM"] = np.asarray([str(x) for x in attri["ABS_IGM"][:]])
+    header = attri.read_header()
+    for key in ("RPMIN", "RPMAX", "RTMAX", "NP", "NT", "COEFMOD", "REJ", "ALPHAMET"):
+        out["hdr_" + key] = np.asarray(header[key])
+    np.savez_compressed(out_path, **out)
+
+
+def extra_metal(picca_root):
+    """picca's golden metal distortion matrix (test_cor/metal_dmat.fits.gz,
+    command at py/picca/tests/test_3_cor.py:351-382)."""
+    tests = os.path.join(picca_root, "py", "picca", "tests", "data")
+    _convert_metal_dmat(os.path.join(tests, "test_cor", "metal_dmat.fits.gz"),
+                        os.path.join(HERE, "cor_metal_dmat.npz"))
 
 
 def extra_dmat(picca_root):
