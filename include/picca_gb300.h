@@ -26,6 +26,7 @@
  *                          py/picca/cf.py:390-517, :519-887
  *  - pg_xcf_dmat        <- xcf.compute_dmat + xcf.compute_dmat_forest_pairs_fast
  *                          py/picca/xcf.py:325-424, :427-675
+ *  - pg_cf_metal_dmat   <- cf.compute_metal_dmat  py/picca/cf.py:890-1218
  *  - pg_corr_params     <- the cf / xcf module globals set by
  *                          py/picca/bin/picca_cf.py:343-368 and
  *                          py/picca/bin/picca_xcf.py:351-373
@@ -398,6 +399,30 @@ int pg_cf_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_params
                const int32_t *pair_first, const int32_t *pair_second, const double *pair_angle,
                int64_t num_pairs, void *work, uint64_t work_bytes, const pg_dmat_sums *out,
                void *stream);
+
+/* Metal distortion matrix (py/picca/cf.py:890-1218,
+ * py/picca/bin/picca_metal_dmat.py). The pixels of a set seen as absorber
+ * abs: distances and redshift at z_abs = 10^log_lambda / lambda_abs - 1,
+ * zfac = (1 + z_abs)^(alpha_abs - 1), and the pixel weight where z_abs is
+ * below the forest's quasar redshift, 0 elsewhere; arrays aligned with the
+ * set's pixel arrays. */
+typedef struct pg_metal_pixels {
+    const double *r_comov, *dist_m, *z, *zfac, *weights;
+} pg_metal_pixels;
+
+/* One pass of cf.compute_metal_dmat over the kept forest pairs
+ * (pair_first[q] of s1, pair_second[q] of s2; s2 NULL: auto): forest 1 seen
+ * as absorber abs1 (a1), forest 2 as abs2 (a2). zevol_den = (1 +
+ * z_ref)^(alpha_abs1 + alpha_abs2 - 2). The reference's swapped pass for two
+ * different absorbers is a second call with a1 / a2 built for abs2 / abs1.
+ * Sums are ACCUMULATED into out (FP64, the reference's un-normalised
+ * tuples). */
+int pg_cf_metal_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_params *dparams,
+                     double zevol_den, const pg_forest_set *s1, const pg_forest_set *s2,
+                     const pg_metal_pixels *a1, const pg_metal_pixels *a2,
+                     const int32_t *pair_first, const int32_t *pair_second,
+                     const double *pair_angle, int64_t num_pairs, const pg_dmat_sums *out,
+                     void *stream);
 
 /* Delta x quasar distortion matrix (py/picca/xcf.py:325-675,
  * py/picca/bin/picca_xdmat.py). A work item q is forest item_forest[q] of

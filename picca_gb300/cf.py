@@ -10,7 +10,9 @@ Same module globals (py/picca/cf.py:28-79) and the same functions:
 * ``compute_dmat(healpixs)`` returns the raw distortion-matrix sums of those
   healpix with the reference's random rejection (py/picca/cf.py:390-517),
   and ``compute_dmat_forest_pairs_fast(...)`` keeps the 22-argument signature
-  (py/picca/cf.py:519-887).
+  (py/picca/cf.py:519-887);
+* ``compute_metal_dmat(healpixs, abs_igm1, abs_igm2)`` returns the raw metal
+  distortion-matrix sums (py/picca/cf.py:890-1218).
 
 All pair arithmetic runs on the GPU through ``libpicca_gb300``. The first
 ``fill_neighs`` / ``compute_xi`` call computes the neighbour lists and the
@@ -402,3 +404,64 @@ def compute_dmat_forest_pairs_fast(log_lambda1, log_lambda2, r_comov1, r_comov2,
     r_trans_eff += sums["r_trans_eff"].cpu().numpy()
     z_eff += sums["z_eff"].cpu().numpy()
     weight_eff += sums["weight_eff"].cpu().numpy()
+
+
+def compute_metal_dmat(healpixs, abs_igm1="LYA", abs_igm2="SiIII(1207)"):
+    """Raw metal distortion-matrix sums of ``healpixs`` for the absorbers
+    (abs_igm1, abs_igm2) (py/picca/cf.py:890-1218): the random rejection
+    from NumPy's global generator as picca draws it, the direct and (for two
+    different absorbers) swapped passes on the GPU; module globals
+    ``cosmo``, ``alpha_abs`` and ``z_ref`` as picca_metal_dmat.py sets them.
+    Returns ``(weights_dmat, dmat [nb, nm], r_par_eff, r_trans_eff, z_eff,
+    weight_eff, num_pairs, num_pairs_used)``."""
+    from . import metal as _metal  # pylint: disable=import-outside-toplevel
+
+    if cosmo is None or alpha_abs is None:
+        raise ValueError("cf.cosmo and cf.alpha_abs must be set for the metal distortion "
+                         "matrix")
+    state = _neighbour_state()
+    fs1 = state["set1"]
+    if state["set2"] is not None:
+        raise NotImplementedError("the metal distortion matrix of two delta fields is not "
+                                  "supported")
+    offsets = state["offsets_host"]
+    firsts = np.searchsorted(fs1.row, np.arange(len(fs1.healpix_list)))
+    mask = np.zeros(int(state["total"]), dtype=bool)
+    num_pairs = num_pairs_used = 0
+    for healpix in healpixs:
+        row = int(np.searchsorted(fs1.healpix_list, healpix))
+        for k, _ in enumerate(data[healpix]):
+            f = firsts[row] + k
+            start, end = int(offsets[f]), int(offsets[f + 1])
+            w = np.random.rand(end - start) > reject
+            num_pairs += end - start
+            num_pairs_used += int(w.sum())
+            mask[start:end] = w
+    if _cache.get("metal_engine") is None:
+        _cache["metal_engine"] = _metal.MetalEngine(_engine())
+    engine = _cache["metal_engine"]
+    dev = state["dev1"]
+    first, second, num = engine.pair_list(dev, None, state["offsets"], state["index"], mask)
+    params = _params()
+    dparams = _dmat.make_dmat_params(num_bins_r_par, num_bins_r_trans,
+                                     num_model_bins_r_par=num_model_bins_r_par,
+                                     num_model_bins_r_trans=num_model_bins_r_trans)
+    zr = 2.25 if z_ref is None else z_ref
+    side1 = _metal.absorber_pixels(dev, cosmo, abs_igm1, alpha_abs[abs_igm1])
+    side2 = _metal.absorber_pixels(dev, cosmo, abs_igm2, alpha_abs[abs_igm2])
+    sums = engine.alloc_sums(params, dparams)
+    den = (1 + zr) ** (alpha_abs[abs_igm1] + alpha_abs[abs_igm2] - 2)
+    engine.run_pass(params, dparams, den, dev, None, side1, side2, first, second, num, sums)
+    if _metal.swapped_pass(abs_igm1, abs_igm2, x_correlation,
+                           lambda_abs2 is not None and lambda_abs == lambda_abs2):
+        engine.run_pass(params, dparams, den, dev, None, side2, side1, first, second, num,
+                        sums)
+    engine.engine.stats()
+    raw = {k: v.cpu().numpy() for k, v in sums.items()}
+    for healpix in healpixs:
+        for delta in data[healpix]:
+            if hasattr(delta, "neighbours"):
+                delta.neighbours = None
+    nb = num_bins_r_par * num_bins_r_trans
+    return (raw["weights_dmat"], raw["dmat"].reshape(nb, -1), raw["r_par_eff"],
+            raw["r_trans_eff"], raw["z_eff"], raw["weight_eff"], num_pairs, num_pairs_used)

@@ -471,4 +471,34 @@ int pg_xcf_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_param
                            static_cast<double *>(work), grid, *out, scratch_of(plan), st);
 }
 
+int pg_cf_metal_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_params *dparams,
+                     double zevol_den, const pg_forest_set *s1, const pg_forest_set *s2,
+                     const pg_metal_pixels *a1, const pg_metal_pixels *a2,
+                     const int32_t *pair_first, const int32_t *pair_second,
+                     const double *pair_angle, int64_t num_pairs, const pg_dmat_sums *out,
+                     void *stream) {
+    if (!plan || !s1 || !a1 || !a2 || !out) return PG_ERR_INVALID_ARGUMENT;
+    int rc = validate_dmat(params, dparams);
+    if (rc) return rc;
+    if ((rc = validate_set(s1, true, false))) return rc;
+    if (s2 && (rc = validate_set(s2, true, false))) return rc;
+    if (!out->weights_dmat || !out->dmat || !out->r_par_eff || !out->r_trans_eff ||
+        !out->z_eff || !out->weight_eff)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (num_pairs < 0 || num_pairs > INT32_MAX) return PG_ERR_INVALID_ARGUMENT;
+    if (!(zevol_den > 0) || !isfinite(zevol_den)) return PG_ERR_INVALID_ARGUMENT;
+    const pg_metal_pixels *sides[2] = {a1, a2};
+    for (const pg_metal_pixels *a : sides)
+        if (num_pairs > 0 && (!a->r_comov || !a->dist_m || !a->z || !a->zfac || !a->weights))
+            return PG_ERR_INVALID_ARGUMENT;
+    if (num_pairs > 0 && (!pair_first || !pair_second)) return PG_ERR_INVALID_ARGUMENT;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    if ((rc = reset_scratch(plan, st))) return rc;
+    return launch_metal_dmat(*params, *dparams, zevol_den, *s1, s2 ? *s2 : *s1, *a1, *a2,
+                             pair_first, pair_second, pair_angle, num_pairs, *out,
+                             scratch_of(plan), plan->num_sms, st);
+}
+
 }  // extern "C"

@@ -241,6 +241,13 @@ int launch_cf_dmat(const pg_corr_params &p, const pg_dmat_params &d, const DmatC
                    const double *pair_angle, int64_t num_pairs, double *work, int grid,
                    const pg_dmat_sums &out, Scratch *scratch, cudaStream_t stream);
 
+int launch_metal_dmat(const pg_corr_params &p, const pg_dmat_params &d, double zevol_den,
+                      const pg_forest_set &s1, const pg_forest_set &s2,
+                      const pg_metal_pixels &a1, const pg_metal_pixels &a2,
+                      const int32_t *pair_first, const int32_t *pair_second,
+                      const double *pair_angle, int64_t num_pairs, const pg_dmat_sums &out,
+                      Scratch *scratch, int num_sms, cudaStream_t stream);
+
 int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *start,
                     const int32_t *index, int64_t count, int max_iter, double tol, int mode,
                     const pg_cont_fit &out, Scratch *scratch, int num_sms, cudaStream_t stream);
