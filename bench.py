@@ -317,6 +317,7 @@ def dmat_leg(args, fs, params, ang_max, cpu_seconds):
     cpu_pairs, cpu_pix, cpu_desc, cores = dmat_cpu_sample(fs, params, dparams, (f_h, g_h),
                                                           cpu_seconds)
     cross = xdmat_leg(args, fs, params, ang_max, engine)
+    metals = metal_leg(args, fs, params, ang_max, engine, mask)
     return {
         "metric": "distortion-matrix forest pairs per second",
         "value": nsel / kernel_s, "unit": "forest-pairs/s",
@@ -342,7 +343,78 @@ def dmat_leg(args, fs, params, ang_max, cpu_seconds):
                          "pixel_pairs_per_s": cpu_pix, "cores": cores, "kind": "port",
                          "sample": cpu_desc},
         "cross": cross,
+        "metal": metals,
     }
+
+
+def metal_leg(args, fs, params, ang_max, engine, mask):
+    """Metal distortion matrix LYA x SiIII(1207) (picca_metal_dmat.py:
+    direct and swapped passes) over the same kept forest pairs: one warm-up
+    and one timed run of both passes (CUDA events), and the oracle (NumPy,
+    one core) on a sample of the kept pairs."""
+    import torch
+
+    from oracle import cpu as ocpu
+    from oracle import metal_dmat as omd
+    from picca_gb300 import constants, dmat, metal, pairs
+    cosmo = constants.Cosmo(Om=0.3147, verbose=False)
+    alpha = {"LYA": 2.9, "SiIII(1207)": 1.0}
+    cparams = pairs.make_params(ang_max=ang_max, **params)
+    dparams = dmat.make_dmat_params(params["num_bins_r_par"], params["num_bins_r_trans"])
+    meng = metal.MetalEngine(engine.engine)
+    pe = meng.engine
+    dev = pairs.DeviceForests(fs, pe.device)
+    offsets, index, _ = pe.neighbours(cparams, dev)
+    first, second, num = meng.pair_list(dev, None, offsets, index, mask)
+    side_l = metal.absorber_pixels(dev, cosmo, "LYA", alpha["LYA"])
+    side_s = metal.absorber_pixels(dev, cosmo, "SiIII(1207)", alpha["SiIII(1207)"])
+    den = (1 + 2.25) ** (alpha["LYA"] + alpha["SiIII(1207)"] - 2)
+    stream = torch.cuda.current_stream()
+    times = []
+    for _ in range(2):
+        sums = meng.alloc_sums(cparams, dparams)
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        meng.run_pass(cparams, dparams, den, dev, None, side_l, side_s, first, second, num, sums)
+        meng.run_pass(cparams, dparams, den, dev, None, side_s, side_l, first, second, num, sums)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+        pe.stats()
+    f_h, g_h = first.cpu().numpy()[:num], second.cpu().numpy()[:num]
+    npix = np.diff(fs.pix_offset)
+    pix_pairs = 2.0 * float(np.sum(npix[f_h].astype(np.float64) * npix[g_h]))
+    del dev, sums, side_l, side_s, first, second
+    torch.cuda.empty_cache()
+    # oracle sample
+    p = omd.MetalParams(params["r_par_min"], params["r_par_max"], params["r_trans_max"],
+                        params["num_bins_r_par"], params["num_bins_r_trans"], z_ref=2.25,
+                        alpha_abs=alpha)
+    out = omd.new_outputs(p)
+    po = np.asarray(fs.pix_offset)
+    rng = np.random.default_rng(3)
+    pick = rng.permutation(len(f_h))
+    n = 0
+    t0 = time.perf_counter()
+    while time.perf_counter() - t0 < min(args.cpu_seconds, 10.0) and n < len(pick):
+        f, g = int(f_h[pick[n]]), int(g_h[pick[n]])
+        ang = ocpu.lib().oracle_angle(fs.x_cart[f], fs.y_cart[f], fs.z_cart[f], fs.ra[f],
+                                      fs.dec[f], fs.cos_dec[f], fs.x_cart[g], fs.y_cart[g],
+                                      fs.z_cart[g], fs.ra[g], fs.dec[g])
+        side = lambda h: (fs.log_lambda[po[h]:po[h + 1]], fs.r_comov[po[h]:po[h + 1]],  # noqa
+                          fs.dist_m[po[h]:po[h + 1]], fs.weights[po[h]:po[h + 1]], fs.z_qso[h])
+        omd.forest_pair(p, cosmo, side(f), side(g), ang, False, "LYA", "SiIII(1207)", True, out)
+        n += 1
+    cpu_s = time.perf_counter() - t0
+    return {"metric": "metal distortion-matrix kept forest pairs per second (LYA x SiIII(1207), "
+                      "direct and swapped passes)",
+            "value": num / times[-1], "unit": "forest-pairs/s", "kernel_ms": times[-1] * 1e3,
+            "pixel_pairs_per_s": pix_pairs / times[-1], "dtype": "f64",
+            "cpu_baseline": {"value": n / cpu_s, "unit": "forest-pairs/s", "cores": 1,
+                             "kind": "port", "sample": f"{n} kept forest pairs, NumPy "
+                                                       f"restatement, {cpu_s:.1f} s"}}
 
 
 def xdmat_leg(args, fs, params, ang_max, engine):
