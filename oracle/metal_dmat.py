@@ -165,3 +165,94 @@ def normalise(out, p, npall, npused):
     w = wdm > 0
     dm[w, :] /= wdm[w, None]
     return {"RP": rp, "RT": rt, "Z": z, "DM": dm, "WDM": wdm, "NPALL": npall, "NPUSED": npused}
+
+
+def xforest(p, cosmo, f1, objs, angs, abs_name, out):
+    """xcf.compute_metal_dmat for one forest and its kept quasars
+    (py/picca/xcf.py:706-790); objs = (r_comov, dist_m, weights, z_qso)
+    arrays. Strict range tests and truncated bins as the reference."""
+    from picca_gb300 import constants
+    r1, m1, w1, ra1, ma1, za1 = _side(*f1[:4], f1[4], constants.ABSORBER_IGM[abs_name], cosmo)
+    if r1.size == 0:
+        return
+    zevol = ((1.0 + za1) / (1.0 + p.z_ref)) ** (p.alpha_abs[abs_name] - 1.0)
+    nm = p.nmp * p.nmt
+    for (r2, m2, w2, z2), ang in zip(zip(*objs), angs):
+        c, s = np.cos(ang / 2), np.sin(ang / 2)
+        r_par = (r1 - r2) * c
+        r_trans = (m1 + m2) * s
+        w12 = w1 * w2
+        ok = (r_par > p.r_par_min) & (r_par < p.r_par_max) & (r_trans < p.r_trans_max)
+        bp = ((r_par - p.r_par_min) / (p.r_par_max - p.r_par_min) * p.np).astype(int)
+        bt = (r_trans / p.r_trans_max * p.nt).astype(int)
+        bins = bt + p.nt * bp
+        h = np.bincount(bins[ok], weights=w12[ok])
+        out["weights_dmat"][: len(h)] += h
+        rp_abs = (ra1 - r2) * c
+        rt_abs = (ma1 + m2) * s
+        mp = ((rp_abs - p.r_par_min) / (p.r_par_max - p.r_par_min) * p.nmp).astype(int)
+        mt = (rt_abs / p.r_trans_max * p.nmt).astype(int)
+        mb = mt + p.nmt * mp
+        ok &= (rp_abs > p.r_par_min) & (rp_abs < p.r_par_max) & (rt_abs < p.r_trans_max)
+        wz = w12 * zevol
+        h = np.bincount(mb[ok] + nm * bins[ok], weights=wz[ok])
+        out["dmat"][: len(h)] += h
+        for key, vals in (("r_par_eff", rp_abs * wz), ("r_trans_eff", rt_abs * wz),
+                          ("z_eff", (za1 + z2) / 2 * wz), ("weight_eff", wz)):
+            h = np.bincount(mb[ok], weights=vals[ok])
+            out[key][: len(h)] += h
+
+
+def xselection(fs, offsets, nproc, reject, skip):
+    """The draws of xcf.compute_metal_dmat: a forest without a pixel below
+    its quasar redshift (``skip``) draws nothing and is not counted
+    (py/picca/xcf.py:722-727)."""
+    rows = np.arange(len(fs.healpix_list))
+    chunks = {}
+    for index, row in enumerate(rows):
+        chunks.setdefault(index % nproc, []).append(row)
+    mask = np.zeros(int(offsets[-1]), dtype=bool)
+    forest_rows = np.asarray(fs.row)
+    npall = npused = 0
+    for chunk in chunks.values():
+        rng = np.random.RandomState(int(fs.healpix_list[chunk[0]]))
+        for row in chunk:
+            for f in np.nonzero(forest_rows == row)[0]:
+                if skip[f]:
+                    continue
+                k0, k1 = int(offsets[f]), int(offsets[f + 1])
+                mask[k0:k1] = rng.rand(k1 - k0) > reject
+                npall += k1 - k0
+                npused += int(mask[k0:k1].sum())
+    return mask, npall, npused
+
+
+def xpipeline(fs, qs, cosmo, p, ang_max, reject, abs_igm, nproc=1):
+    """picca_metal_xdmat.py: per absorber the normalised matrices (keys
+    "QSO_" + absorber in the output file)."""
+    from picca_gb300 import constants
+    oparams = cpu.make_params(p.r_par_min, p.r_par_max, p.r_trans_max, p.np, p.nt)
+    offsets, index = cpu.neighbours(fs, qs, oparams, ang_max, auto_mode=0, xcf=True)
+    po = np.asarray(fs.pix_offset)
+    results = {}
+    for abs_name in abs_igm:
+        lam = constants.ABSORBER_IGM[abs_name]
+        skip = np.array([not np.any(10**fs.log_lambda[po[f]:po[f + 1]] / lam - 1 < fs.z_qso[f])
+                         for f in range(fs.num)])
+        mask, npall, npused = xselection(fs, offsets, nproc, reject, skip)
+        out = new_outputs(p)
+        for f in range(fs.num):
+            kept = [int(index[k]) for k in range(int(offsets[f]), int(offsets[f + 1]))
+                    if mask[k]]
+            if not kept:
+                continue
+            angs = [cpu.lib().oracle_angle(fs.x_cart[f], fs.y_cart[f], fs.z_cart[f], fs.ra[f],
+                                           fs.dec[f], fs.cos_dec[f], qs.x_cart[g], qs.y_cart[g],
+                                           qs.z_cart[g], qs.ra[g], qs.dec[g]) for g in kept]
+            sl = slice(po[f], po[f + 1])
+            xforest(p, cosmo, (fs.log_lambda[sl], fs.r_comov[sl], fs.dist_m[sl],
+                               fs.weights[sl], fs.z_qso[f]),
+                    (qs.obj_r_comov[kept], qs.obj_dist_m[kept], qs.obj_weight[kept],
+                     qs.z_qso[kept]), angs, abs_name, out)
+        results[abs_name] = normalise(out, p, npall, npused)
+    return results

@@ -17,8 +17,8 @@ Run once in a checkout that has the picca sources next to it
 * ``cor_dmat_zcuts.npz``, ``cor_dmat_cross.npz``, ``cor_dmat_cross_zcuts.npz``,
   ``cor_xdmat.npz``, ``cor_xdmat_zcuts.npz``: picca's other golden distortion
   matrices (``test_cor/*.fits.gz``, commands in py/picca/tests/test_3_cor.py);
-* ``cor_metal_dmat.npz``: picca's golden metal distortion matrix
-  (``test_cor/metal_dmat.fits.gz``);
+* ``cor_metal_dmat.npz``, ``cor_metal_xdmat.npz``: picca's golden metal
+  distortion matrices (``test_cor/metal_dmat.fits.gz``, ``metal_xdmat.fits.gz``);
 * ``xdmat_cases.npz``: inputs and outputs of picca's own
   ``xcf.compute_dmat_forest_pairs_fast`` on forests of the test data and the
   quasars around them;
@@ -569,16 +569,20 @@ def _convert_metal_dmat(src, out_path):
     out["ABS_IGM"] = np.asarray([str(x) for x in attri["ABS_IGM"][:]])
     header = attri.read_header()
     for key in ("RPMIN", "RPMAX", "RTMAX", "NP", "NT", "COEFMOD", "REJ", "ALPHAMET"):
-        out["hdr_" + key] = np.asarray(header[key])
+        if key in header:
+            out["hdr_" + key] = np.asarray(header[key])
     np.savez_compressed(out_path, **out)
 
 
 def extra_metal(picca_root):
-    """picca's golden metal distortion matrix (test_cor/metal_dmat.fits.gz,
-    command at py/picca/tests/test_3_cor.py:351-382)."""
+    """picca's golden metal distortion matrices (test_cor/metal_dmat.fits.gz
+    and metal_xdmat.fits.gz, commands at py/picca/tests/test_3_cor.py:351-382
+    and :700-729)."""
     tests = os.path.join(picca_root, "py", "picca", "tests", "data")
     _convert_metal_dmat(os.path.join(tests, "test_cor", "metal_dmat.fits.gz"),
                         os.path.join(HERE, "cor_metal_dmat.npz"))
+    _convert_metal_dmat(os.path.join(tests, "test_cor", "metal_xdmat.fits.gz"),
+                        os.path.join(HERE, "cor_metal_xdmat.npz"))
 
 
 def extra_dmat(picca_root):

@@ -47,3 +47,27 @@ def test_pipeline_matches_golden_metal_dmat(picca_inputs):
                                {key: want[f"{key}_{name}"] for key in ("RP", "RT", "Z", "DM",
                                                                         "WDM")},
                                names=("RP", "RT", "Z", "DM", "WDM"))
+
+
+def test_xpipeline_matches_golden_metal_xdmat(picca_inputs):
+    from picca_gb300 import constants, io, utils
+    from picca_gb300.forests import ForestSet
+    cosmo = constants.Cosmo(Om=0.315, verbose=False)
+    data, _, z_min, _ = io.read_deltas(
+        os.path.join(picca_inputs, "Delta_LYA") + "/", 16, constants.ABSORBER_IGM["LYA"], 2.9,
+        2.25, cosmo, delta_attributes=os.path.join(picca_inputs, "delta_attributes.fits.gz"))
+    objs, z_min2 = io.read_objects(os.path.join(picca_inputs, "cat.fits"), 16, 0, 10, 1.0, 2.25,
+                                   cosmo)
+    fs, qs = ForestSet.from_deltas(data), ForestSet.from_objects(objs)
+    params = omd.MetalParams(-60., 60., 60., 30, 15, z_ref=2.25, x_correlation=True,
+                             alpha_abs={"LYA": 2.9, "SiIII(1207)": 1.0})
+    ang_max = utils.compute_ang_max(cosmo, 60., z_min, z_min2)
+    got = omd.xpipeline(fs, qs, cosmo, params, ang_max, reject=0.99, abs_igm=["SiIII(1207)"])
+    want = golden("cor_metal_xdmat.npz")
+    assert [str(x) for x in want["ABS_IGM"]] == ["SiIII(1207)"]
+    g = got["SiIII(1207)"]
+    assert g["NPALL"] == int(want["NPALL"][0]) and g["NPUSED"] == int(want["NPUSED"][0])
+    compare_like_reference({k: g[k] for k in ("RP", "RT", "Z", "DM", "WDM")},
+                           {k: want[f"{k}_QSO_SiIII(1207)"] for k in ("RP", "RT", "Z", "DM",
+                                                                       "WDM")},
+                           names=("RP", "RT", "Z", "DM", "WDM"))
