@@ -27,6 +27,7 @@
  *  - pg_xcf_dmat        <- xcf.compute_dmat + xcf.compute_dmat_forest_pairs_fast
  *                          py/picca/xcf.py:325-424, :427-675
  *  - pg_cf_metal_dmat   <- cf.compute_metal_dmat  py/picca/cf.py:890-1218
+ *  - pg_xcf_metal_dmat  <- xcf.compute_metal_dmat py/picca/xcf.py:677-800
  *  - pg_corr_params     <- the cf / xcf module globals set by
  *                          py/picca/bin/picca_cf.py:343-368 and
  *                          py/picca/bin/picca_xcf.py:351-373
@@ -423,6 +424,20 @@ int pg_cf_metal_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_
                      const int32_t *pair_first, const int32_t *pair_second,
                      const double *pair_angle, int64_t num_pairs, const pg_dmat_sums *out,
                      void *stream);
+
+/* xcf.compute_metal_dmat (py/picca/xcf.py:677-800): the same pass with the
+ * quasars as one-pixel forests (quasar_pixels: a set whose pixel k is
+ * quasar k: r_comov, dist_m, weights and z the quasar's), a2 the quasars'
+ * values with zfac = 1, a1 the forests' pixels seen as the absorber with
+ * zfac = ((1 + z_abs) / (1 + z_ref))^(alpha_abs - 1) and zevol_den = 1.
+ * r_par is signed; pairs are kept by the reference's strict distance tests
+ * (r_par_min < r_par < r_par_max, r_trans < r_trans_max) for both bins. */
+int pg_xcf_metal_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_params *dparams,
+                      double zevol_den, const pg_forest_set *forests,
+                      const pg_forest_set *quasar_pixels, const pg_metal_pixels *a1,
+                      const pg_metal_pixels *a2, const int32_t *pair_first,
+                      const int32_t *pair_second, const double *pair_angle, int64_t num_pairs,
+                      const pg_dmat_sums *out, void *stream);
 
 /* Delta x quasar distortion matrix (py/picca/xcf.py:325-675,
  * py/picca/bin/picca_xdmat.py). A work item q is forest item_forest[q] of

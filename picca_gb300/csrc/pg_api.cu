@@ -471,12 +471,12 @@ int pg_xcf_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_param
                            static_cast<double *>(work), grid, *out, scratch_of(plan), st);
 }
 
-int pg_cf_metal_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_params *dparams,
-                     double zevol_den, const pg_forest_set *s1, const pg_forest_set *s2,
-                     const pg_metal_pixels *a1, const pg_metal_pixels *a2,
-                     const int32_t *pair_first, const int32_t *pair_second,
-                     const double *pair_angle, int64_t num_pairs, const pg_dmat_sums *out,
-                     void *stream) {
+static int metal_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_params *dparams,
+                      double zevol_den, const pg_forest_set *s1, const pg_forest_set *s2,
+                      const pg_metal_pixels *a1, const pg_metal_pixels *a2,
+                      const int32_t *pair_first, const int32_t *pair_second,
+                      const double *pair_angle, int64_t num_pairs, const pg_dmat_sums *out,
+                      void *stream, int cross) {
     if (!plan || !s1 || !a1 || !a2 || !out) return PG_ERR_INVALID_ARGUMENT;
     int rc = validate_dmat(params, dparams);
     if (rc) return rc;
@@ -498,7 +498,28 @@ int pg_cf_metal_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_
     if ((rc = reset_scratch(plan, st))) return rc;
     return launch_metal_dmat(*params, *dparams, zevol_den, *s1, s2 ? *s2 : *s1, *a1, *a2,
                              pair_first, pair_second, pair_angle, num_pairs, *out,
-                             scratch_of(plan), plan->num_sms, st);
+                             scratch_of(plan), plan->num_sms, st, cross != 0);
+}
+
+int pg_cf_metal_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_params *dparams,
+                     double zevol_den, const pg_forest_set *s1, const pg_forest_set *s2,
+                     const pg_metal_pixels *a1, const pg_metal_pixels *a2,
+                     const int32_t *pair_first, const int32_t *pair_second,
+                     const double *pair_angle, int64_t num_pairs, const pg_dmat_sums *out,
+                     void *stream) {
+    return metal_dmat(plan, params, dparams, zevol_den, s1, s2, a1, a2, pair_first, pair_second,
+                      pair_angle, num_pairs, out, stream, 0);
+}
+
+int pg_xcf_metal_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat_params *dparams,
+                      double zevol_den, const pg_forest_set *forests,
+                      const pg_forest_set *quasar_pixels, const pg_metal_pixels *a1,
+                      const pg_metal_pixels *a2, const int32_t *pair_first,
+                      const int32_t *pair_second, const double *pair_angle, int64_t num_pairs,
+                      const pg_dmat_sums *out, void *stream) {
+    if (!quasar_pixels) return PG_ERR_INVALID_ARGUMENT;
+    return metal_dmat(plan, params, dparams, zevol_den, forests, quasar_pixels, a1, a2,
+                      pair_first, pair_second, pair_angle, num_pairs, out, stream, 1);
 }
 
 }  // extern "C"

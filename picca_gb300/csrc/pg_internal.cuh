@@ -246,7 +246,7 @@ int launch_metal_dmat(const pg_corr_params &p, const pg_dmat_params &d, double z
                       const pg_metal_pixels &a1, const pg_metal_pixels &a2,
                       const int32_t *pair_first, const int32_t *pair_second,
                       const double *pair_angle, int64_t num_pairs, const pg_dmat_sums &out,
-                      Scratch *scratch, int num_sms, cudaStream_t stream);
+                      Scratch *scratch, int num_sms, cudaStream_t stream, bool xcf);
 
 int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *start,
                     const int32_t *index, int64_t count, int max_iter, double tol, int mode,

@@ -1,4 +1,6 @@
-// Metal distortion matrix: cf.compute_metal_dmat (py/picca/cf.py:890-1218).
+// Metal distortion matrices: cf.compute_metal_dmat (py/picca/cf.py:890-1218)
+// and, with the quasars as one-pixel forests, xcf.compute_metal_dmat
+// (py/picca/xcf.py:677-800).
 //
 // For every kept forest pair the reference bins all pixel pairs twice: with
 // the tracer's distances (data bin, r_par / r_trans of the delta files) and
@@ -27,6 +29,7 @@ struct MetalConst {
     int32_t nmp, nmt, nm;
     double inv_range, inv_rtmax;
     double inv_zevol_den;  // 1 / (1 + z_ref)^(alpha1 + alpha2 - 2)
+    int32_t xcf;           // delta x quasar rules (py/picca/xcf.py:735-770)
 };
 
 __device__ __forceinline__ double md_floor(double est, double num, double den, int32_t n) {
@@ -92,12 +95,19 @@ __global__ void __launch_bounds__(kMdBlock)
                 if (!c.b.x_correlation) rp = fabs(rp);
                 const double rt = __dmul_rn(__dadd_rn(m1, s2.dist_m[o2 + j]), ss);
                 if (shp && fabs(rp) < c.b.half_plate_cut) continue;  // weight set to 0
+                // the cross tests the distances (strict), the auto its bin indices
+                if (c.xcf && !(rp > c.b.r_par_min && rp < c.b.r_par_max &&
+                               rt < c.b.r_trans_max))
+                    continue;
                 const double xp = __dsub_rn(rp, c.b.r_par_min);
                 const double bp = md_floor(__dmul_rn(xp, c.inv_range), xp, c.b.r_par_range,
                                            c.b.np);
                 const double bt = md_floor(__dmul_rn(rt, c.inv_rtmax), rt, c.b.r_trans_max,
                                            c.b.nt);
-                if (!(bp < c.b.np && bt < c.b.nt && bp >= 0.)) continue;
+                if (!(bp < c.b.np && bt < c.b.nt && bp >= 0.)) {
+                    if (c.xcf) report_error(scratch, PG_ERR_BIN_RANGE, (int32_t)bp);
+                    continue;
+                }
                 const double w12 = __dmul_rn(w1, w2);
                 const int32_t b = (int32_t)bt + c.b.nt * (int32_t)bp;
                 if (b != run_b) {
@@ -110,12 +120,18 @@ __global__ void __launch_bounds__(kMdBlock)
                 double rpa = __dmul_rn(__dsub_rn(ra1, a2.r_comov[o2 + j]), cc);
                 if (!c.b.x_correlation) rpa = fabs(rpa);
                 const double rta = __dmul_rn(__dadd_rn(ma1, a2.dist_m[o2 + j]), ss);
+                if (c.xcf && !(rpa > c.b.r_par_min && rpa < c.b.r_par_max &&
+                               rta < c.b.r_trans_max))
+                    continue;
                 const double xm = __dsub_rn(rpa, c.b.r_par_min);
                 const double mp = md_floor(__dmul_rn(xm, c.inv_range), xm, c.b.r_par_range,
                                            c.nmp);
                 const double mt = md_floor(__dmul_rn(rta, c.inv_rtmax), rta, c.b.r_trans_max,
                                            c.nmt);
-                if (!(mp < c.nmp && mt < c.nmt && mp >= 0.)) continue;
+                if (!(mp < c.nmp && mt < c.nmt && mp >= 0.)) {
+                    if (c.xcf) report_error(scratch, PG_ERR_BIN_RANGE, (int32_t)mp);
+                    continue;
+                }
                 const int32_t mb = (int32_t)mt + c.nmt * (int32_t)mp;
                 const int64_t key = (int64_t)b * nm + mb;
                 if (key != run) {
@@ -145,7 +161,7 @@ int launch_metal_dmat(const pg_corr_params &p, const pg_dmat_params &d, double z
                       const pg_metal_pixels &a1, const pg_metal_pixels &a2,
                       const int32_t *pair_first, const int32_t *pair_second,
                       const double *pair_angle, int64_t num_pairs, const pg_dmat_sums &out,
-                      Scratch *scratch, int num_sms, cudaStream_t stream) {
+                      Scratch *scratch, int num_sms, cudaStream_t stream, bool xcf) {
     if (num_pairs == 0) return PG_OK;
     MetalConst c;
     c.b = make_binning(p);
@@ -155,6 +171,11 @@ int launch_metal_dmat(const pg_corr_params &p, const pg_dmat_params &d, double z
     c.inv_range = 1. / c.b.r_par_range;
     c.inv_rtmax = 1. / c.b.r_trans_max;
     c.inv_zevol_den = 1. / zevol_den;
+    c.xcf = xcf;
+    if (xcf) {  // r_par is signed and the cross has no half-plate veto
+        c.b.x_correlation = 1;
+        c.b.remove_shp = 0;
+    }
     int occ = 0;
     if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, metal_dmat_kernel, kMdBlock, 0) !=
             cudaSuccess ||

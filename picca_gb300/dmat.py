@@ -63,10 +63,12 @@ def chunk_rows(num_rows, nproc):
     return [np.arange(p, num_rows, nproc) for p in range(min(nproc, num_rows))]
 
 
-def selection_mask(healpix_list, forest_rows, nbr_offsets, nproc, reject):
+def selection_mask(healpix_list, forest_rows, nbr_offsets, nproc, reject, skip=None):
     """Boolean mask over the neighbour CSR of the pairs picca_dmat.py keeps
     when run with ``nproc`` processes. ``forest_rows`` must be
-    non-decreasing (forests grouped by healpix, as ForestSet stores them)."""
+    non-decreasing (forests grouped by healpix, as ForestSet stores them).
+    Forests flagged in ``skip`` draw nothing (xcf.compute_metal_dmat skips
+    forests without a usable pixel before drawing)."""
     forest_rows = np.asarray(forest_rows)
     offsets = np.asarray(nbr_offsets, dtype=np.int64)
     if forest_rows.size and np.any(np.diff(forest_rows) < 0):
@@ -78,7 +80,12 @@ def selection_mask(healpix_list, forest_rows, nbr_offsets, nproc, reject):
     mask = np.zeros(int(offsets[-1]) if offsets.size else 0, dtype=bool)
     for rows in chunk_rows(num_rows, max(int(nproc), 1)):
         rng = np.random.RandomState(int(healpix_list[rows[0]]))
-        positions = _ranges(offsets[first[rows]], offsets[last[rows]])
+        if skip is None:
+            positions = _ranges(offsets[first[rows]], offsets[last[rows]])
+        else:
+            forests = np.concatenate([np.arange(first[r], last[r]) for r in rows])
+            forests = forests[~np.asarray(skip)[forests]]
+            positions = _ranges(offsets[forests], offsets[forests + 1])
         for k in range(0, len(positions), _DRAW_BLOCK):
             part = positions[k:k + _DRAW_BLOCK]
             mask[part] = rng.rand(len(part)) > reject

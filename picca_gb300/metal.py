@@ -1,6 +1,7 @@
 """Metal distortion matrices on the GPU: cf.compute_metal_dmat
-(py/picca/cf.py:890-1218) and picca_metal_dmat.py
-(py/picca/bin/picca_metal_dmat.py:446-520).
+(py/picca/cf.py:890-1218) with picca_metal_dmat.py
+(py/picca/bin/picca_metal_dmat.py:446-520), and xcf.compute_metal_dmat
+(py/picca/xcf.py:677-800) with picca_metal_xdmat.py.
 
 Host side of ``pg_cf_metal_dmat``: the pixels of a forest set seen as an
 absorber (distances from the fiducial cosmology at z_abs = 10^log_lambda /
@@ -39,13 +40,17 @@ def _bind():
             ctypes.POINTER(MetalPixelsC), ctypes.POINTER(MetalPixelsC), ctypes.c_void_p,
             ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.POINTER(DmatSumsC),
             ctypes.c_void_p]
+        lib.pg_xcf_metal_dmat.restype = ctypes.c_int
+        lib.pg_xcf_metal_dmat.argtypes = lib.pg_cf_metal_dmat.argtypes
         lib._metal_bound = True
     return lib
 
 
-def absorber_pixels(dev, cosmo, abs_name, alpha):
+def absorber_pixels(dev, cosmo, abs_name, alpha, z_ref=None):
     """Pixels of a DeviceForests seen as absorber ``abs_name`` (aligned with
-    its compacted pixel arrays), as device tensors and their C struct."""
+    its compacted pixel arrays), as device tensors and their C struct.
+    zfac = (1 + z_abs)^(alpha - 1), or ((1 + z_abs) / (1 + z_ref))^(alpha - 1)
+    when ``z_ref`` is given (the cross's form, xcf.py:752-754)."""
     fs = dev.source
     weights = np.asarray(fs.weights, dtype=np.float64)
     keep = weights != 0
@@ -58,7 +63,8 @@ def absorber_pixels(dev, cosmo, abs_name, alpha):
         "r_comov": np.asarray(cosmo.get_r_comov(z_abs), dtype=np.float64),
         "dist_m": np.asarray(cosmo.get_dist_m(z_abs), dtype=np.float64),
         "z": z_abs,
-        "zfac": (1 + z_abs) ** (alpha - 1),
+        "zfac": ((1 + z_abs) ** (alpha - 1) if z_ref is None
+                 else ((1.0 + z_abs) / (1.0 + z_ref)) ** (alpha - 1.0)),
         "weights": np.where(z_abs < z_qso, w, 0.0),
     }
     tensors = {k: torch.from_numpy(np.ascontiguousarray(v if v.size else np.zeros(1)))
@@ -72,12 +78,13 @@ class MetalEngine(_dmat.DmatEngine):
     """Metal distortion-matrix passes on one CUDA device."""
 
     def run_pass(self, params, dparams, zevol_den, dev1, dev2, side1, side2, first, second,
-                 num_pairs, sums, angles=None):
+                 num_pairs, sums, angles=None, cross=False):
         lib = _bind()
+        entry = lib.pg_xcf_metal_dmat if cross else lib.pg_cf_metal_dmat
         out = DmatSumsC(*[sums[k].data_ptr() for k in ("weights_dmat", "dmat", "r_par_eff",
                                                          "r_trans_eff", "z_eff", "weight_eff")])
         with torch.cuda.device(self.device):
-            check(lib.pg_cf_metal_dmat(
+            check(entry(
                 self.engine.plan.handle, ctypes.byref(params), ctypes.byref(dparams),
                 float(zevol_den), ctypes.byref(dev1.c),
                 ctypes.byref(dev2.c) if dev2 is not None else None, ctypes.byref(side1[1]),
@@ -166,4 +173,79 @@ def metal_distortion_matrices(fs, params, dparams, cosmo, reject, abs_igm, alpha
         pe.stats()
         raw = {k: v.cpu().numpy() for k, v in sums.items()}
         results[f"{abs1}_{abs2}"] = normalise(raw, params, dparams, total, int(mask.sum()))
+    return results
+
+
+
+def quasar_pixel_set(qs):
+    """The quasars of a ForestSet as one-pixel forests (the second side of
+    pg_xcf_metal_dmat)."""
+    from .forests import ForestSet
+    n = qs.num
+    return ForestSet(
+        pix_offset=np.arange(n + 1, dtype=np.int64), z=np.asarray(qs.z_qso, float),
+        r_comov=np.asarray(qs.obj_r_comov, float), dist_m=np.asarray(qs.obj_dist_m, float),
+        weights=np.asarray(qs.obj_weight, float), delta=np.zeros(n), log_lambda=np.zeros(n),
+        ra=qs.ra, dec=qs.dec, x_cart=qs.x_cart, y_cart=qs.y_cart, z_cart=qs.z_cart,
+        cos_dec=qs.cos_dec, z_qso=qs.z_qso, thingid=qs.thingid, plate=qs.plate,
+        fiberid=qs.fiberid, healpix=qs.healpix, healpix_list=qs.healpix_list, row=qs.row)
+
+
+def quasar_side(dev_q):
+    """pg_metal_pixels of the one-pixel quasar forests: their own distances,
+    redshift and weight, zfac = 1."""
+    fs = dev_q.source
+    keep = np.asarray(fs.weights) != 0
+    arrays = {"r_comov": np.asarray(fs.r_comov, float)[keep],
+              "dist_m": np.asarray(fs.dist_m, float)[keep],
+              "z": np.asarray(fs.z, float)[keep], "zfac": np.ones(int(keep.sum())),
+              "weights": np.asarray(fs.weights, float)[keep]}
+    tensors = {k: torch.from_numpy(np.ascontiguousarray(v if v.size else np.zeros(1)))
+               .to(dev_q.device) for k, v in arrays.items()}
+    return tensors, MetalPixelsC(*[tensors[k].data_ptr() for k in ("r_comov", "dist_m", "z",
+                                                                    "zfac", "weights")])
+
+
+def forests_without_pixels(fs, abs_name):
+    """Forests with no pixel below their quasar redshift as ``abs_name``
+    (xcf.compute_metal_dmat skips them before drawing, xcf.py:713-727)."""
+    lam = constants.ABSORBER_IGM[abs_name]
+    npix = np.diff(np.asarray(fs.pix_offset))
+    z_abs = 10**np.asarray(fs.log_lambda, float) / lam - 1
+    below = (z_abs < np.repeat(np.asarray(fs.z_qso, float), npix)).astype(np.int64)
+    csum = np.concatenate([[0], np.cumsum(below)])
+    off = np.asarray(fs.pix_offset)
+    return (csum[off[1:]] - csum[off[:-1]]) == 0
+
+
+def cross_metal_distortion_matrices(fs, qs, params, dparams, cosmo, reject, abs_igm,
+                                    alpha_abs, z_ref=2.25, nproc=1, engine=None):
+    """picca_metal_xdmat.py on a forest set and a quasar set: for every
+    absorber, the normalised (RP, RT, Z, DM, WDM) and the pair counts."""
+    eng = engine if isinstance(engine, MetalEngine) else MetalEngine(engine)
+    pe = eng.engine
+    dev = _pairs.DeviceForests(fs, pe.device)
+    dev_objs = _pairs.DeviceForests(qs, pe.device)
+    offsets, index, total = pe.neighbours(params, dev, dev_objs, xcf=True)
+    offsets_h = offsets.cpu().numpy()
+    qpix = quasar_pixel_set(qs)
+    dev_q = _pairs.DeviceForests(qpix, pe.device)
+    qside = quasar_side(dev_q)
+    # quasars dropped by the compaction (zero weight) would change the
+    # indices of the one-pixel set; their pairs add nothing either way
+    results = {}
+    for abs_name in abs_igm:
+        skip = forests_without_pixels(fs, abs_name)
+        mask = _dmat.selection_mask(fs.healpix_list, fs.row, offsets_h, nproc, reject,
+                                    skip=skip)
+        counts = offsets_h[1:] - offsets_h[:-1]
+        npall = int(counts[~skip].sum())
+        first, second, num = eng.pair_list(dev, dev_q, offsets, index, mask)
+        side = absorber_pixels(dev, cosmo, abs_name, alpha_abs[abs_name], z_ref=z_ref)
+        sums = eng.alloc_sums(params, dparams)
+        eng.run_pass(params, dparams, 1.0, dev, dev_q, side, qside, first, second, num, sums,
+                     cross=True)
+        pe.stats()
+        raw = {k: v.cpu().numpy() for k, v in sums.items()}
+        results[abs_name] = normalise(raw, params, dparams, npall, int(mask.sum()))
     return results

@@ -2,9 +2,9 @@
 
 Same module globals (py/picca/xcf.py:27-68) and functions ``fill_neighs``
 (:71-123), ``compute_xi`` (:126-220), the 16-argument
-``compute_xi_forest_pairs_fast`` (:223-322), ``compute_dmat`` (:325-424) and
-the 17-argument ``compute_dmat_forest_pairs_fast`` (:427-675), computed on
-the GPU. As in ``picca_gb300.cf``, the first call runs every healpix in one
+``compute_xi_forest_pairs_fast`` (:223-322), ``compute_dmat`` (:325-424), the
+17-argument ``compute_dmat_forest_pairs_fast`` (:427-675) and
+``compute_metal_dmat`` (:677-800), computed on the GPU. As in ``picca_gb300.cf``, the first call runs every healpix in one
 launch (``compute_xi_all``) and later calls are served from that result.
 """
 
@@ -346,3 +346,63 @@ def compute_dmat_forest_pairs_fast(log_lambda1, r_comov1, dist_m1, z1, weights1,
     r_trans_eff += sums["r_trans_eff"].cpu().numpy()
     z_eff += sums["z_eff"].cpu().numpy()
     weight_eff += sums["weight_eff"].cpu().numpy()
+
+
+def compute_metal_dmat(healpixs, abs_igm="SiII(1526)"):
+    """Raw delta x quasar metal distortion-matrix sums of ``healpixs``
+    (py/picca/xcf.py:677-800): a forest without a pixel below its quasar
+    redshift as ``abs_igm`` is skipped before its draw; the others draw
+    ``np.random.rand(len(neighbours)) > reject`` from NumPy's global
+    generator; the kept pairs run on the GPU. Module globals ``cosmo``,
+    ``alpha_abs`` and ``z_ref`` as picca_metal_xdmat.py sets them."""
+    import torch  # pylint: disable=import-outside-toplevel
+
+    from . import metal as _metal  # pylint: disable=import-outside-toplevel
+    if cosmo is None or alpha_abs is None:
+        raise ValueError("xcf.cosmo and xcf.alpha_abs must be set for the metal distortion "
+                         "matrix")
+    state = _neighbour_state()
+    fs, qs = state["set1"], state["set2"]
+    offsets = state["offsets"]
+    skip = _metal.forests_without_pixels(fs, abs_igm)
+    firsts = np.searchsorted(fs.row, np.arange(len(fs.healpix_list)))
+    mask = np.zeros(int(state["total"]), dtype=bool)
+    num_pairs = num_pairs_used = 0
+    for healpix in healpixs:
+        row = int(np.searchsorted(fs.healpix_list, healpix))
+        for k, _ in enumerate(data[healpix]):
+            f = firsts[row] + k
+            if skip[f]:
+                continue
+            start, end = int(offsets[f]), int(offsets[f + 1])
+            w = np.random.rand(end - start) > reject
+            num_pairs += end - start
+            num_pairs_used += int(w.sum())
+            mask[start:end] = w
+    if _cache.get("metal_engine") is None:
+        _cache["metal_engine"] = _metal.MetalEngine(_engine())
+    engine = _cache["metal_engine"]
+    dev = state["dev1"]
+    dev_q = _pairs.DeviceForests(_metal.quasar_pixel_set(qs), engine.device)
+    off_d = torch.from_numpy(offsets).to(engine.device)
+    idx_d = torch.from_numpy(np.asarray(state["index"], dtype=np.int32)
+                             if state["total"] else np.zeros(1, np.int32)).to(engine.device)
+    first, second, num = engine.pair_list(dev, dev_q, off_d, idx_d, mask)
+    params = _params()
+    dparams = _dmat.make_dmat_params(num_bins_r_par, num_bins_r_trans,
+                                     num_model_bins_r_par=num_model_bins_r_par,
+                                     num_model_bins_r_trans=num_model_bins_r_trans)
+    zr = 2.25 if z_ref is None else z_ref
+    side = _metal.absorber_pixels(dev, cosmo, abs_igm, alpha_abs[abs_igm], z_ref=zr)
+    sums = engine.alloc_sums(params, dparams)
+    engine.run_pass(params, dparams, 1.0, dev, dev_q, side, _metal.quasar_side(dev_q), first,
+                    second, num, sums, cross=True)
+    engine.engine.stats()
+    raw = {k: v.cpu().numpy() for k, v in sums.items()}
+    for healpix in healpixs:
+        for delta in data[healpix]:
+            if hasattr(delta, "neighbours"):
+                delta.neighbours = None
+    nb = num_bins_r_par * num_bins_r_trans
+    return (raw["weights_dmat"], raw["dmat"].reshape(nb, -1), raw["r_par_eff"],
+            raw["r_trans_eff"], raw["z_eff"], raw["weight_eff"], num_pairs, num_pairs_used)

@@ -110,3 +110,48 @@ def test_synthetic_matches_oracle(cuda, unfold):
         for key in ("RP", "RT", "Z", "DM", "WDM"):
             ok, err = close(got[name][key], want[name][key])
             assert ok, (unfold, name, key, err)
+
+
+def test_cli_matches_golden_metal_xdmat(cuda, picca_inputs, tmp_path):
+    from picca_gb300 import fitsio_lite
+    from picca_gb300.bin import picca_metal_xdmat
+    out = str(tmp_path / "metal_xdmat.fits.gz")
+    picca_metal_xdmat.main([
+        "--in-dir", os.path.join(picca_inputs, "Delta_LYA") + "/",
+        "--drq", os.path.join(picca_inputs, "cat.fits"), "--out", out,
+        "--abs-igm", "SiIII(1207)", "--rp-min", "-60.0", "--rp-max", "+60.0",
+        "--rt-max", "+60.0", "--np", "30", "--nt", "15", "--rej", "0.99", "--nproc", "1",
+        "--z-evol-obj", "1.",
+        "--in-attributes", os.path.join(picca_inputs, "delta_attributes.fits.gz")])
+    want = golden("cor_metal_xdmat.npz")
+    with fitsio_lite.FITS(out) as h:
+        attri, mdmat = h["ATTRI"], h["MDMAT"]
+        assert np.array_equal(attri["NPALL"][:], want["NPALL"])
+        assert np.array_equal(attri["NPUSED"][:], want["NPUSED"])
+        name = "QSO_SiIII(1207)"
+        got = {k: mdmat[f"{k}_{name}"][:] for k in ("RP", "RT", "Z", "DM", "WDM")}
+        ref = {k: want[f"{k}_{name}"] for k in ("RP", "RT", "Z", "DM", "WDM")}
+        compare_like_reference(got, ref, names=("RP", "RT", "Z", "DM", "WDM"))
+
+
+def test_synthetic_xcf_matches_oracle(cuda):
+    from picca_gb300 import constants, dmat, metal, pairs, synthetic
+    fs = synthetic.make_forests(60, 31, (150.0, 152.5), (0.0, 2.5), max_pixels=400)
+    qs = synthetic.make_quasars(800, 32, (150.0, 152.5), (0.0, 2.5), z_lo=2.0, z_hi=3.6)
+    cosmo = constants.Cosmo(Om=0.3147, verbose=False)
+    metals = ["SiIII(1207)", "SiII(1527)"]
+    alpha = {"LYA": 2.9, "SiIII(1207)": 1.0, "SiII(1527)": 1.3}
+    p = omd.MetalParams(-60., 60., 60., 12, 10, coef_binning_model=2, x_correlation=True,
+                        z_ref=2.25, alpha_abs=alpha)
+    want = omd.xpipeline(fs, qs, cosmo, p, 0.03, reject=0.7, abs_igm=metals, nproc=3)
+    params = pairs.make_params(-60., 60., 60., 12, 10, 0.03, x_correlation=True)
+    dparams = dmat.make_dmat_params(12, 10, coef_binning_model=2)
+    got = metal.cross_metal_distortion_matrices(fs, qs, params, dparams, cosmo, 0.7, metals,
+                                                alpha, z_ref=2.25, nproc=3)
+    assert list(got) == list(want)
+    for name in want:
+        assert got[name]["NPALL"] == want[name]["NPALL"]
+        assert got[name]["NPUSED"] == want[name]["NPUSED"]
+        for key in ("RP", "RT", "Z", "DM", "WDM"):
+            ok, err = close(got[name][key], want[name][key])
+            assert ok, (name, key, err)
