@@ -119,22 +119,25 @@ def absorber_pairs(lambda_abs, abs_igm, lambda_abs2=None, abs_igm2=None):
     return out
 
 
-def pipeline(fs, cosmo, p, ang_max, reject, abs_igm, lambda_abs="LYA", nproc=1):
-    """picca_metal_dmat.py on a ForestSet (auto-correlation): per absorber
-    pair the normalised (RP, RT, Z, DM, WDM) and the pair counts."""
+def pipeline(fs, cosmo, p, ang_max, reject, abs_igm, lambda_abs="LYA", nproc=1, fs2=None):
+    """picca_metal_dmat.py on a ForestSet (auto-correlation, or the cross of
+    two delta fields with ``fs2`` and the same tracer on both sides): per
+    absorber pair the normalised (RP, RT, Z, DM, WDM) and the pair counts."""
+    other = fs if fs2 is None else fs2
     oparams = cpu.make_params(p.r_par_min, p.r_par_max, p.r_trans_max, p.np, p.nt)
-    offsets, index = cpu.neighbours(fs, fs, oparams, ang_max, auto_mode=1)
+    offsets, index = cpu.neighbours(fs, other, oparams, ang_max, auto_mode=int(fs2 is None))
     mask, npall, npused = odm.selection(fs, offsets, nproc, reject)
-    po = np.asarray(fs.pix_offset)
 
-    def forest(f):
+    def forest(s, f):
+        po = np.asarray(s.pix_offset)
         sl = slice(po[f], po[f + 1])
-        return (np.asarray(fs.log_lambda[sl]), np.asarray(fs.r_comov[sl]),
-                np.asarray(fs.dist_m[sl]), np.asarray(fs.weights[sl]), fs.z_qso[f])
+        return (np.asarray(s.log_lambda[sl]), np.asarray(s.r_comov[sl]),
+                np.asarray(s.dist_m[sl]), np.asarray(s.weights[sl]), s.z_qso[f])
 
     results = {}
     for abs1, abs2 in absorber_pairs(lambda_abs, abs_igm):
-        swapped = (not p.x_correlation) and abs1 != abs2
+        # cf.py:1088-1090 with cf.lambda_abs2 = cf.lambda_abs for two fields
+        swapped = (abs1 != abs2) if not p.x_correlation else fs2 is not None
         out = new_outputs(p)
         for f in range(fs.num):
             for k in range(int(offsets[f]), int(offsets[f + 1])):
@@ -142,11 +145,13 @@ def pipeline(fs, cosmo, p, ang_max, reject, abs_igm, lambda_abs="LYA", nproc=1):
                     continue
                 g = int(index[k])
                 ang = cpu.lib().oracle_angle(fs.x_cart[f], fs.y_cart[f], fs.z_cart[f], fs.ra[f],
-                                             fs.dec[f], fs.cos_dec[f], fs.x_cart[g],
-                                             fs.y_cart[g], fs.z_cart[g], fs.ra[g], fs.dec[g])
-                shp = p.shp and fs.plate[f] == fs.plate[g] and (
-                    (fs.fiberid[f] <= 500) == (fs.fiberid[g] <= 500))
-                forest_pair(p, cosmo, forest(f), forest(g), ang, shp, abs1, abs2, swapped, out)
+                                             fs.dec[f], fs.cos_dec[f], other.x_cart[g],
+                                             other.y_cart[g], other.z_cart[g], other.ra[g],
+                                             other.dec[g])
+                shp = p.shp and fs.plate[f] == other.plate[g] and (
+                    (fs.fiberid[f] <= 500) == (other.fiberid[g] <= 500))
+                forest_pair(p, cosmo, forest(fs, f), forest(other, g), ang, shp, abs1, abs2,
+                            swapped, out)
         results[f"{abs1}_{abs2}"] = normalise(out, p, npall, npused)
     return results
 

@@ -8,8 +8,9 @@ rejection per process chunk (the generator re-seeded per chunk for every
 absorber pair, so all pairs keep the same forest pairs), normalisation
 (:497-503) and FITS layout (HDU ``ATTRI`` with NPALL / NPUSED / ABS_IGM and
 the header keywords, HDU ``MDMAT`` with RP_ / RT_ / Z_ / DM_ / WDM_ columns per
-absorber pair). The cross of two delta fields (``--in-dir2``,
-``--lambda-abs2``) is not supported by this drop-in.
+absorber pair). The cross of two delta fields (``--in-dir2``) is supported
+with the same tracer on both sides; a different second tracer
+(``--lambda-abs2``) is not.
 """
 
 import argparse
@@ -144,8 +145,8 @@ def write(path, results, args, blinding):
 def main(cmdargs=None):
     """Compute the metal distortion matrices"""
     args = parse_args(cmdargs)
-    if args.in_dir2 or args.lambda_abs2:
-        raise NotImplementedError("the cross of two delta fields is not supported by this "
+    if args.lambda_abs2:
+        raise NotImplementedError("a second tracer (--lambda-abs2) is not supported by this "
                                   "drop-in")
     if args.nproc is None:
         args.nproc = max(cpu_count() // 2, 1)
@@ -159,10 +160,19 @@ def main(cmdargs=None):
     cf.reject = args.rej
     cf.lambda_abs = constants.ABSORBER_IGM[args.lambda_abs]
     cf.remove_same_half_plate_close_pairs = args.remove_same_half_plate_close_pairs
-    cf.x_correlation = bool(args.unfold_cf)
+    # picca sets x_correlation only for two delta fields (py/picca/bin/
+    # picca_metal_dmat.py:386-389)
+    cf.x_correlation = bool(args.in_dir2 and args.unfold_cf)
     cf.alpha_abs = {args.lambda_abs: cf.alpha}
     for name in args.abs_igm:
         cf.alpha_abs[name] = args.metal_alpha
+    if args.in_dir2:
+        cf.alpha2 = args.z_evol2
+        cf.lambda_abs2 = cf.lambda_abs
+        # picca stores alpha2 under the key None here (--lambda-abs2 unset),
+        # so the tracer keeps alpha (py/picca/bin/picca_metal_dmat.py:398)
+        for name in args.abs_igm2:
+            cf.alpha_abs[name] = args.metal_alpha
     blinding = io.read_blinding(args.in_dir)
     cf.cosmo = constants.Cosmo(Om=args.fid_Om, Or=args.fid_Or, Ok=args.fid_Ok, wl=args.fid_wl,
                                verbose=False)
@@ -176,8 +186,22 @@ def main(cmdargs=None):
     cf.num_data = num_data
     cf.ang_max = utils.compute_ang_max(cf.cosmo, cf.r_trans_max, z_min)
     userprint(f"done, npix = {len(data)}")
-    t1 = time.time()
     from picca_gb300.forests import ForestSet
+    fs2 = None
+    if args.in_dir2:
+        data2, num_data2, z_min2, _ = io.read_deltas(
+            args.in_dir2, cf.nside, cf.lambda_abs2, cf.alpha2, cf.z_ref, cf.cosmo,
+            max_num_spec=args.nspec, rebin_factor=args.rebin_factor,
+            z_min_qso=args.z_min_sources, z_max_qso=args.z_max_sources,
+            delta_attributes=args.in_attributes)
+        cf.data2 = data2
+        cf.num_data2 = num_data2
+        cf.ang_max = utils.compute_ang_max(cf.cosmo, cf.r_trans_max, z_min, z_min2)
+        fs2 = ForestSet.from_deltas(data2)
+        # without --lambda-abs2 the second list is the first one
+        # (py/picca/bin/picca_metal_dmat.py:449-451)
+        args.abs_igm2 = args.abs_igm
+    t1 = time.time()
     fs = ForestSet.from_deltas(data)
     params = pairs.make_params(cf.r_par_min, cf.r_par_max, cf.r_trans_max, cf.num_bins_r_par,
                                cf.num_bins_r_trans, cf.ang_max,
@@ -192,7 +216,8 @@ def main(cmdargs=None):
                 if (a1 == "LYA" and a2 in DEFAULT_SI_METALS) or (a1 == "CIV(eff)" and a1 == a2)]
     results = metal.metal_distortion_matrices(
         fs, params, dparams, cf.cosmo, cf.reject, args.abs_igm, cf.alpha_abs,
-        lambda_abs=args.lambda_abs, z_ref=cf.z_ref, nproc=args.nproc, only=only)
+        lambda_abs=args.lambda_abs, z_ref=cf.z_ref, nproc=args.nproc, only=only, fs2=fs2,
+        abs_igm2=args.abs_igm2 if fs2 is not None else None)
     userprint(f"picca_metal_dmat.py - Time computing all metal matrices : "
               f"{(time.time() - t1) / 60:.3f} minutes")
     write(args.out, results, args, blinding)

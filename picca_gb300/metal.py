@@ -138,37 +138,43 @@ def normalise(raw, params, dparams, npall, npused):
 
 def metal_distortion_matrices(fs, params, dparams, cosmo, reject, abs_igm, alpha_abs,
                               lambda_abs="LYA", z_ref=2.25, nproc=1, engine=None, mask=None,
-                              only=None):
-    """picca_metal_dmat.py (auto-correlation) on a ForestSet: for every
-    absorber pair (or the pairs in ``only``), the normalised (RP, RT, Z, DM,
-    WDM) and the pair counts. ``alpha_abs`` maps absorber names to their
+                              only=None, fs2=None, abs_igm2=None):
+    """picca_metal_dmat.py on a ForestSet (auto-correlation, or the cross
+    with a second field ``fs2`` of the same tracer): for every absorber pair
+    (or the pairs in ``only``), the normalised (RP, RT, Z, DM, WDM) and the
+    pair counts. ``alpha_abs`` maps absorber names to their
     redshift-evolution exponents."""
     eng = engine if isinstance(engine, MetalEngine) else MetalEngine(engine)
     pe = eng.engine
     dev = _pairs.DeviceForests(fs, pe.device)
-    offsets, index, total = pe.neighbours(params, dev, None)
+    dev2 = _pairs.DeviceForests(fs2, pe.device) if fs2 is not None else None
+    offsets, index, total = pe.neighbours(params, dev, dev2)
     offsets_h = offsets.cpu().numpy()
     if mask is None:
         mask = _dmat.selection_mask(fs.healpix_list, fs.row, offsets_h, nproc, reject)
-    first, second, num = eng.pair_list(dev, None, offsets, index, mask)
+    first, second, num = eng.pair_list(dev, dev2, offsets, index, mask)
     pixels = {}
 
-    def side(name):
-        if name not in pixels:
-            pixels[name] = absorber_pixels(dev, cosmo, name, alpha_abs[name])
-        return pixels[name]
+    def side(which, name):
+        key = (which, name)
+        if key not in pixels:
+            pixels[key] = absorber_pixels(dev if which == 1 or dev2 is None else dev2, cosmo,
+                                          name, alpha_abs[name])
+        return pixels[key]
 
     results = {}
-    for abs1, abs2 in absorber_pairs(lambda_abs, abs_igm):
+    pairs_list = absorber_pairs(lambda_abs, abs_igm, lambda_abs if fs2 is not None else None,
+                                abs_igm2)
+    for abs1, abs2 in pairs_list:
         if only is not None and (abs1, abs2) not in only:
             continue
         sums = eng.alloc_sums(params, dparams)
         den = (1 + z_ref) ** (alpha_abs[abs1] + alpha_abs[abs2] - 2)
-        eng.run_pass(params, dparams, den, dev, None, side(abs1), side(abs2), first, second,
-                     num, sums)
-        if swapped_pass(abs1, abs2, bool(params.x_correlation)):
+        eng.run_pass(params, dparams, den, dev, dev2, side(1, abs1), side(2, abs2), first,
+                     second, num, sums)
+        if swapped_pass(abs1, abs2, bool(params.x_correlation), same_tracer=fs2 is not None):
             den2 = (1 + z_ref) ** (alpha_abs[abs2] + alpha_abs[abs1] - 2)
-            eng.run_pass(params, dparams, den2, dev, None, side(abs2), side(abs1), first,
+            eng.run_pass(params, dparams, den2, dev, dev2, side(1, abs2), side(2, abs1), first,
                          second, num, sums)
         pe.stats()
         raw = {k: v.cpu().numpy() for k, v in sums.items()}

@@ -17,8 +17,10 @@ Run once in a checkout that has the picca sources next to it
 * ``cor_dmat_zcuts.npz``, ``cor_dmat_cross.npz``, ``cor_dmat_cross_zcuts.npz``,
   ``cor_xdmat.npz``, ``cor_xdmat_zcuts.npz``: picca's other golden distortion
   matrices (``test_cor/*.fits.gz``, commands in py/picca/tests/test_3_cor.py);
-* ``cor_metal_dmat.npz``, ``cor_metal_xdmat.npz``: picca's golden metal
-  distortion matrices (``test_cor/metal_dmat.fits.gz``, ``metal_xdmat.fits.gz``);
+* ``cor_metal_dmat.npz``, ``cor_metal_dmat_cross.npz``,
+  ``cor_metal_xdmat.npz``: picca's golden metal distortion matrices
+  (``test_cor/metal_dmat.fits.gz``, ``metal_dmat_cross.fits.gz``,
+  ``metal_xdmat.fits.gz``);
 * ``xdmat_cases.npz``: inputs and outputs of picca's own
   ``xcf.compute_dmat_forest_pairs_fast`` on forests of the test data and the
   quasars around them;
@@ -583,6 +585,8 @@ def extra_metal(picca_root):
                         os.path.join(HERE, "cor_metal_dmat.npz"))
     _convert_metal_dmat(os.path.join(tests, "test_cor", "metal_xdmat.fits.gz"),
                         os.path.join(HERE, "cor_metal_xdmat.npz"))
+    _convert_metal_dmat(os.path.join(tests, "test_cor", "metal_dmat_cross.fits.gz"),
+                        os.path.join(HERE, "cor_metal_dmat_cross.npz"))
 
 
 def extra_dmat(picca_root):

@@ -155,3 +155,26 @@ def test_synthetic_xcf_matches_oracle(cuda):
         for key in ("RP", "RT", "Z", "DM", "WDM"):
             ok, err = close(got[name][key], want[name][key])
             assert ok, (name, key, err)
+
+
+def test_cli_matches_golden_metal_dmat_cross(cuda, picca_inputs, tmp_path):
+    """py/picca/tests/test_3_cor.py:526-557."""
+    from picca_gb300 import fitsio_lite
+    from picca_gb300.bin import picca_metal_dmat
+    out = str(tmp_path / "metal_dmat_cross.fits.gz")
+    delta_dir = os.path.join(picca_inputs, "Delta_LYA") + "/"
+    picca_metal_dmat.main([
+        "--in-dir", delta_dir, "--in-dir2", delta_dir, "--out", out,
+        "--abs-igm", "SiIII(1207)", "--abs-igm2", "SiIII(1207)", "--rp-min", "-60.0",
+        "--rp-max", "+60.0", "--rt-max", "+60.0", "--np", "30", "--nt", "15", "--rej", "0.99",
+        "--nproc", "1", "--remove-same-half-plate-close-pairs", "--unfold-cf",
+        "--in-attributes", os.path.join(picca_inputs, "delta_attributes.fits.gz")])
+    want = golden("cor_metal_dmat_cross.npz")
+    with fitsio_lite.FITS(out) as h:
+        attri, mdmat = h["ATTRI"], h["MDMAT"]
+        assert np.array_equal(attri["NPALL"][:], want["NPALL"])
+        assert np.array_equal(attri["NPUSED"][:], want["NPUSED"])
+        for name in (str(x) for x in want["ABS_IGM"]):
+            got = {k: mdmat[f"{k}_{name}"][:] for k in ("RP", "RT", "Z", "DM", "WDM")}
+            ref = {k: want[f"{k}_{name}"] for k in ("RP", "RT", "Z", "DM", "WDM")}
+            compare_like_reference(got, ref, names=("RP", "RT", "Z", "DM", "WDM"))

@@ -71,3 +71,32 @@ def test_xpipeline_matches_golden_metal_xdmat(picca_inputs):
                            {k: want[f"{k}_QSO_SiIII(1207)"] for k in ("RP", "RT", "Z", "DM",
                                                                        "WDM")},
                            names=("RP", "RT", "Z", "DM", "WDM"))
+
+
+def test_pipeline_matches_golden_metal_dmat_cross(picca_inputs):
+    """py/picca/tests/test_3_cor.py:526-557: the same delta field twice,
+    SiIII(1207) on both, r_par unfolded, same-half-plate veto."""
+    from picca_gb300 import constants, io, utils
+    from picca_gb300.forests import ForestSet
+    cosmo = constants.Cosmo(Om=0.315, verbose=False)
+    sets = []
+    for _ in range(2):
+        data, _, z_min, _ = io.read_deltas(
+            os.path.join(picca_inputs, "Delta_LYA") + "/", 16, constants.ABSORBER_IGM["LYA"],
+            2.9, 2.25, cosmo,
+            delta_attributes=os.path.join(picca_inputs, "delta_attributes.fits.gz"))
+        sets.append(ForestSet.from_deltas(data))
+    params = omd.MetalParams(-60., 60., 60., 30, 15, x_correlation=True,
+                             remove_same_half_plate_close_pairs=True, z_ref=2.25,
+                             alpha_abs={"LYA": 2.9, "SiIII(1207)": 1.0})
+    ang_max = utils.compute_ang_max(cosmo, 60., z_min, z_min)
+    got = omd.pipeline(sets[0], cosmo, params, ang_max, reject=0.99, abs_igm=["SiIII(1207)"],
+                       fs2=sets[1])
+    want = golden("cor_metal_dmat_cross.npz")
+    for k, name in enumerate(str(x) for x in want["ABS_IGM"]):
+        g = got[name]
+        assert g["NPALL"] == int(want["NPALL"][k]) and g["NPUSED"] == int(want["NPUSED"][k])
+        compare_like_reference({key: g[key] for key in ("RP", "RT", "Z", "DM", "WDM")},
+                               {key: want[f"{key}_{name}"] for key in ("RP", "RT", "Z", "DM",
+                                                                        "WDM")},
+                               names=("RP", "RT", "Z", "DM", "WDM"))
