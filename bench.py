@@ -344,7 +344,77 @@ def dmat_leg(args, fs, params, ang_max, cpu_seconds):
                          "sample": cpu_desc},
         "cross": cross,
         "metal": metals,
+        "fast_metal": fast_metal_leg(args),
     }
+
+
+def fast_metal_leg(args):
+    """picca_fast_metal_dmat.py on a DESI-like stack (0.8 A pixels over
+    3600-5772 A, 2,716 pixels, synthetic weights), LYA and the four silicon
+    lines (14 absorber pairs), 50 x 50 bins, r 0-200 Mpc/h: the pair
+    histograms of all pairs timed with CUDA events, the whole computation
+    (side preparation, uploads, histograms, host epilogue) with the host
+    clock, and the NumPy oracle on one core for one pair."""
+    import torch
+
+    from oracle import fast_metal as ofm
+    from picca_gb300 import constants, fast_metal
+    cosmo = constants.Cosmo(Om=0.3147, verbose=False)
+    lam = 3600.0 + 0.8 * np.arange(2716)
+    log_lambda = np.log10(lam)
+    rng = np.random.default_rng(11)
+    weight = rng.uniform(10.0, 90.0, lam.size)
+    metals = ["SiII(1190)", "SiII(1193)", "SiIII(1207)", "SiII(1260)"]
+    alpha = {"LYA": 2.9, **{m: 1.0 for m in metals}}
+    A = constants.ABSORBER_IGM
+    pairs_ = fast_metal.absorber_pairs("LYA", metals)
+    engine = fast_metal.FastMetalEngine()
+
+    def sides(a1, a2, mod):
+        return (mod.stack_side(log_lambda, weight, A[a1], A["LYA"], alpha[a1] + 2.9, cosmo),
+                mod.stack_side(log_lambda, weight, A[a2], A["LYA"], alpha[a2] + 2.9, cosmo))
+
+    def run_all():
+        out = []
+        for a1, a2 in pairs_:
+            s1, s2 = sides(a1, a2, fast_metal)
+            out.append(fast_metal.fast_metal_matrix(s1, s2, 0.0, 200.0, 200.0, 50, 50, False,
+                                                    engine=engine))
+        return out
+
+    run_all()
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    run_all()
+    e2e_s = time.perf_counter() - t0
+    devs = [tuple(engine.upload(s) for s in sides(a1, a2, fast_metal)) for a1, a2 in pairs_]
+    stream = torch.cuda.current_stream()
+    times = []
+    for _ in range(3):
+        torch.cuda.synchronize()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for d1, d2 in devs:
+            engine.histograms_device(d1, d2, 0.0, 200.0, 50, 50, False)
+        e1.record(stream)
+        torch.cuda.synchronize()
+        times.append(e0.elapsed_time(e1) / 1e3)
+    kernel_s = min(times)
+    pix_pairs = float(len(pairs_)) * lam.size * lam.size
+    t0 = time.perf_counter()
+    s1, s2 = sides(*pairs_[0], ofm)
+    ofm.matrix(s1, s2, 0.0, 200.0, 200.0, 50, 50, False)
+    cpu_s = time.perf_counter() - t0
+    return {"metric": "fast metal distortion matrices: stack pixel pairs per second",
+            "value": pix_pairs / kernel_s, "unit": "pixel-pairs/s",
+            "kernel_ms": kernel_s * 1e3, "matrices": len(pairs_), "dtype": "f64",
+            "config": {"workload": "stack of 2,716 pixels (0.8 A, 3600-5772 A), LYA + 4 Si "
+                                   "lines = 14 absorber pairs, 50 x 50 bins, r 0-200 Mpc/h"},
+            "e2e": {"value": pix_pairs / e2e_s, "unit": "pixel-pairs/s", "seconds": e2e_s},
+            "cpu_baseline": {"value": lam.size * lam.size / cpu_s, "unit": "pixel-pairs/s",
+                             "cores": 1, "kind": "port",
+                             "sample": f"one absorber pair, NumPy restatement, {cpu_s:.2f} s"}}
 
 
 def metal_leg(args, fs, params, ang_max, engine, mask):

@@ -28,6 +28,9 @@
  *                          py/picca/xcf.py:325-424, :427-675
  *  - pg_cf_metal_dmat   <- cf.compute_metal_dmat  py/picca/cf.py:890-1218
  *  - pg_xcf_metal_dmat  <- xcf.compute_metal_dmat py/picca/xcf.py:677-800
+ *  - pg_fast_metal_dmat <- calc_fast_metal_dmat of
+ *                          py/picca/bin/picca_fast_metal_dmat.py:30-251 and
+ *                          py/picca/bin/picca_fast_metal_xdmat.py:28-215
  *  - pg_corr_params     <- the cf / xcf module globals set by
  *                          py/picca/bin/picca_cf.py:343-368 and
  *                          py/picca/bin/picca_xcf.py:351-373
@@ -438,6 +441,42 @@ int pg_xcf_metal_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat
                       const pg_metal_pixels *a2, const int32_t *pair_first,
                       const int32_t *pair_second, const double *pair_angle, int64_t num_pairs,
                       const pg_dmat_sums *out, void *stream);
+
+/* Fast metal distortion matrix (py/picca/bin/picca_fast_metal_dmat.py:30-251,
+ * py/picca/bin/picca_fast_metal_xdmat.py:28-215): every pair (i, j) of two
+ * pixel lists, side 1 the stacked deltas' wavelength grid, side 2 the same
+ * grid (auto) or the quasars' redshift histogram (cross). Per pixel: the
+ * comoving distance at the true absorber's redshift (r_in) and at the
+ * assumed one's (r_out), the true redshift and the weight with its
+ * redshift-evolution factor; a pair weighs weight_1 weight_2. */
+typedef struct pg_fast_metal_side {
+    const double *r_in, *r_out, *z_in, *weight;
+    int64_t num;
+} pg_fast_metal_side;
+
+/* r_par edges: r_par_min + ((r_par_max - r_par_min) / num_bins_r_par) k.
+ * num_ratio_bins: equal-width bins of the distance ratio (the reference
+ * uses 4 (num_bins_r_trans + 1)). signed_r_par 0 folds r_par (|r1 - r2|,
+ * the auto script), 1 keeps r1 - r2 (the cross script). near_r_par: the
+ * ratio histogram keeps pairs with |r_par_in| < near_r_par (20 Mpc/h). */
+typedef struct pg_fast_metal_params {
+    double r_par_min, r_par_max, near_r_par;
+    int32_t num_bins_r_par, num_ratio_bins, signed_r_par, reserved;
+} pg_fast_metal_params;
+
+/* Outputs (device, OVERWRITTEN): rp_dmat[num_bins_r_par^2] the histogram2d of
+ * (r_par_out, r_par_in) (row: output bin), ratio_weights / ratio_edges the
+ * ratio histogram and its edges (num_ratio_bins + 1, numpy's linspace over
+ * the ratio's range), out_weight / out_weight_rp / out_weight_z the sums of
+ * w, w r_par_out and w (z_in1 + z_in2) / 2 on the r_par_out bins. */
+typedef struct pg_fast_metal_sums {
+    double *rp_dmat, *ratio_weights, *ratio_edges;
+    double *out_weight, *out_weight_rp, *out_weight_z;
+} pg_fast_metal_sums;
+
+int pg_fast_metal_dmat(pg_plan *plan, const pg_fast_metal_params *params,
+                       const pg_fast_metal_side *s1, const pg_fast_metal_side *s2,
+                       const pg_fast_metal_sums *out, void *stream);
 
 /* Delta x quasar distortion matrix (py/picca/xcf.py:325-675,
  * py/picca/bin/picca_xdmat.py). A work item q is forest item_forest[q] of

@@ -522,4 +522,31 @@ int pg_xcf_metal_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat
                       pair_first, pair_second, pair_angle, num_pairs, out, stream, 1);
 }
 
+int pg_fast_metal_dmat(pg_plan *plan, const pg_fast_metal_params *params,
+                       const pg_fast_metal_side *s1, const pg_fast_metal_side *s2,
+                       const pg_fast_metal_sums *out, void *stream) {
+    if (!plan || !params || !s1 || !s2 || !out) return PG_ERR_INVALID_ARGUMENT;
+    const int np = params->num_bins_r_par, nr = params->num_ratio_bins;
+    if (np < 1 || nr < 1 || np > 4096 || nr > 65536) return PG_ERR_INVALID_ARGUMENT;
+    if (!(params->r_par_max > params->r_par_min) || !isfinite(params->r_par_min) ||
+        !isfinite(params->r_par_max) || !(params->near_r_par >= 0))
+        return PG_ERR_INVALID_ARGUMENT;
+    const pg_fast_metal_side *sides[2] = {s1, s2};
+    for (const pg_fast_metal_side *s : sides) {
+        if (s->num < 0 || s->num > INT32_MAX) return PG_ERR_INVALID_ARGUMENT;
+        if (s->num > 0 && (!s->r_in || !s->r_out || !s->z_in || !s->weight))
+            return PG_ERR_INVALID_ARGUMENT;
+    }
+    if (!out->rp_dmat || !out->ratio_weights || !out->ratio_edges || !out->out_weight ||
+        !out->out_weight_rp || !out->out_weight_z)
+        return PG_ERR_INVALID_ARGUMENT;
+    int rc;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    if ((rc = reset_scratch(plan, st))) return rc;
+    return launch_fast_metal(*params, *s1, *s2, *out, scratch_of(plan), plan->num_sms, st);
+}
+
 }  // extern "C"
+

@@ -31,6 +31,8 @@ struct Scratch {
     unsigned long long gemm_macs;      // distortion matrix: multiply-adds of the U E^T products
     // ordered-integer encodings of FP64 data ranges (guard-band inputs)
     unsigned long long r_min_key, r_max_key, d_max_key;
+    // fast metal matrix: range of the distance ratio (minimum as ~key)
+    unsigned long long ratio_lo_inv_key, ratio_hi_key;
 };
 
 // Map a double to an unsigned key with the same ordering (for atomicMin/Max).
@@ -247,6 +249,10 @@ int launch_metal_dmat(const pg_corr_params &p, const pg_dmat_params &d, double z
                       const int32_t *pair_first, const int32_t *pair_second,
                       const double *pair_angle, int64_t num_pairs, const pg_dmat_sums &out,
                       Scratch *scratch, int num_sms, cudaStream_t stream, bool xcf);
+
+int launch_fast_metal(const pg_fast_metal_params &p, const pg_fast_metal_side &a,
+                      const pg_fast_metal_side &b, const pg_fast_metal_sums &out,
+                      Scratch *scratch, int num_sms, cudaStream_t stream);
 
 int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *start,
                     const int32_t *index, int64_t count, int max_iter, double tol, int mode,

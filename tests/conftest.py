@@ -99,6 +99,16 @@ def write_attributes(path, order=1):
     return path
 
 
+def write_stack_attributes(path):
+    """Rebuild the STACK_DELTAS table of py/picca/tests/data/test_cor/
+    input_from_delta_extraction_lya_nodla/Log/delta_attributes.fits.gz."""
+    src = golden("stack_lya_nodla.npz")
+    cols = list(src)
+    fitsio_lite.write_fits(path, [{"columns": [src[c] for c in cols], "names": cols,
+                                   "extname": "STACK_DELTAS"}])
+    return path
+
+
 def write_catalogue(path):
     """Rebuild py/picca/tests/data/test_delta/cat.fits."""
     src = golden("cat.npz")

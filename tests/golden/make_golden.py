@@ -21,6 +21,11 @@ Run once in a checkout that has the picca sources next to it
   ``cor_metal_xdmat.npz``: picca's golden metal distortion matrices
   (``test_cor/metal_dmat.fits.gz``, ``metal_dmat_cross.fits.gz``,
   ``metal_xdmat.fits.gz``);
+* ``cor_fast_metal_dmat.npz``, ``cor_fast_metal_dmat_cross.npz``,
+  ``cor_fast_metal_xdmat.npz``: picca's golden fast metal distortion
+  matrices, and ``stack_lya_nodla.npz`` their input (the STACK_DELTAS table
+  of ``test_cor/input_from_delta_extraction_lya_nodla/Log/
+  delta_attributes.fits.gz``);
 * ``xdmat_cases.npz``: inputs and outputs of picca's own
   ``xcf.compute_dmat_forest_pairs_fast`` on forests of the test data and the
   quasars around them;
@@ -557,6 +562,7 @@ def main(picca_root):
                       os.path.join(tests, "test_delta", "delta_attributes.fits.gz"))
     extra_dmat(picca_root)
     extra_metal(picca_root)
+    extra_fast_metal(picca_root)
     print(f"wrote fixtures: {ncf} cf pair cases, {nxcf} xcf cases, {ncont} continuum cases, "
           f"{ndm} distortion-matrix cases")
 
@@ -587,6 +593,32 @@ def extra_metal(picca_root):
                         os.path.join(HERE, "cor_metal_xdmat.npz"))
     _convert_metal_dmat(os.path.join(tests, "test_cor", "metal_dmat_cross.fits.gz"),
                         os.path.join(HERE, "cor_metal_dmat_cross.npz"))
+
+
+def _convert_fast_metal(src, out_path):
+    hdul = fitsio_lite.FITS(src)
+    attri = hdul["ATTRI"]
+    mdmat = hdul["MDMAT"]
+    out = {c: mdmat[c][:] for c in mdmat.get_colnames()}
+    out["ABS_IGM"] = np.asarray([str(x) for x in attri["ABS_IGM"][:]])
+    np.savez_compressed(out_path, **out)
+
+
+def extra_fast_metal(picca_root):
+    """picca's golden fast metal distortion matrices (test_cor/
+    fast_metal_dmat.fits.gz, fast_metal_dmat_cross.fits.gz,
+    fast_metal_xdmat.fits.gz; commands at py/picca/tests/test_3_cor.py:384-409,
+    :562-589 and :731-757) and their input, the STACK_DELTAS table of
+    test_cor/input_from_delta_extraction_lya_nodla/Log/delta_attributes.fits.gz."""
+    tests = os.path.join(picca_root, "py", "picca", "tests", "data")
+    for case in ("fast_metal_dmat", "fast_metal_dmat_cross", "fast_metal_xdmat"):
+        _convert_fast_metal(os.path.join(tests, "test_cor", case + ".fits.gz"),
+                            os.path.join(HERE, f"cor_{case}.npz"))
+    stack = fitsio_lite.FITS(os.path.join(
+        tests, "test_cor", "input_from_delta_extraction_lya_nodla", "Log",
+        "delta_attributes.fits.gz"))["STACK_DELTAS"]
+    np.savez_compressed(os.path.join(HERE, "stack_lya_nodla.npz"),
+                        **{c: stack[c][:] for c in stack.get_colnames()})
 
 
 def extra_dmat(picca_root):
