@@ -28,6 +28,9 @@
  *                          py/picca/xcf.py:325-424, :427-675
  *  - pg_cf_metal_dmat   <- cf.compute_metal_dmat  py/picca/cf.py:890-1218
  *  - pg_xcf_metal_dmat  <- xcf.compute_metal_dmat py/picca/xcf.py:677-800
+ *  - pg_wick_xi_matrices, pg_cf_wick
+ *                       <- cf.compute_wick_terms + cf.compute_wickT123_pairs
+ *                          py/picca/cf.py:1328-1495, :1498-1626
  *  - pg_fast_metal_dmat <- calc_fast_metal_dmat of
  *                          py/picca/bin/picca_fast_metal_dmat.py:30-251 and
  *                          py/picca/bin/picca_fast_metal_xdmat.py:28-215
@@ -441,6 +444,48 @@ int pg_xcf_metal_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat
                       const pg_metal_pixels *a2, const int32_t *pair_first,
                       const int32_t *pair_second, const double *pair_angle, int64_t num_pairs,
                       const pg_dmat_sums *out, void *stream);
+
+/* Wick covariance of the auto-correlation, terms T1-T3
+ * (py/picca/cf.py:1328-1626, py/picca/bin/picca_wick.py). */
+
+/* Weighted 1D correlation matrix of each listed forest of `set`,
+ * X[i][k] = ((w_k w_i) xi) sqrt(v_k v_i) with xi = xi_values[m], m the
+ * number of xi_bounds below |log_lambda_k - log_lambda_i| (scipy's
+ * nearest-neighbour rule; xi_bounds[num_xi - 1] are the cell bounds of the
+ * num_xi tabulated offsets), and v the per-pixel 1D variance. Forest
+ * forests[q] is written row-major at arena + x_offsets[forests[q]]
+ * (n_f^2 doubles). The diagonal is written as 0 (no Wick term uses it). */
+int pg_wick_xi_matrices(pg_plan *plan, const pg_forest_set *set, const double *log_lambda,
+                        const double *variance, const double *xi_bounds,
+                        const double *xi_values, int32_t num_xi, const int32_t *forests,
+                        int64_t num_forests, const int64_t *x_offsets, double *arena,
+                        void *stream);
+
+/* Sums of cf.compute_wick_terms (device, ACCUMULATED into): weights_wick
+ * and num_pairs_wick [nb], t1 / t2 / t3 [nb * nb] (t1 only on its
+ * diagonal), nb = num_bins_r_par * num_bins_r_trans. */
+typedef struct pg_wick_sums {
+    double *weights_wick;
+    int64_t *num_pairs_wick;
+    double *t1, *t2, *t3;
+} pg_wick_sums;
+
+/* Terms T1-T3 of the forest pairs (pair_first[q] of s1, pair_second[q] of
+ * s2): zw1 / zw2 the per-pixel ((1 + z) / (1 + z_ref))^(alpha - 1) of each
+ * side, x_offsets / arena the matrices of pg_wick_xi_matrices. Uses
+ * params->r_par_min / r_par_max / r_trans_max / num_bins_* / x_correlation
+ * (the Wick pixel-pair range keeps r_par_min <= r_par < r_par_max,
+ * r_trans < r_trans_max). work: pg_cf_wick_work_bytes() bytes of device
+ * scratch (16-byte aligned); fewer bytes run fewer CTAs. Forests must have
+ * at most 65535 pixels. */
+int pg_cf_wick_work_bytes(pg_plan *plan, const pg_corr_params *params, int32_t max_pixels1,
+                          int32_t max_pixels2, int64_t max_ctas, uint64_t *bytes);
+int pg_cf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *s1,
+               const pg_forest_set *s2, const double *zw1, const double *zw2,
+               const int64_t *x_offsets1, const double *arena1, const int64_t *x_offsets2,
+               const double *arena2, const int32_t *pair_first, const int32_t *pair_second,
+               const double *pair_angle, int64_t num_pairs, void *work, uint64_t work_bytes,
+               const pg_wick_sums *out, void *stream);
 
 /* Fast metal distortion matrix (py/picca/bin/picca_fast_metal_dmat.py:30-251,
  * py/picca/bin/picca_fast_metal_xdmat.py:28-215): every pair (i, j) of two

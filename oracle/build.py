@@ -1,7 +1,7 @@
 """Build the CPU oracle shared library (test infrastructure only).
 
-``python oracle/build.py`` compiles ``oracle/pairs_oracle.c`` and
-``oracle/dmat_oracle.c`` into ``oracle/_build/liboracle.so`` with FMA
+``python oracle/build.py`` compiles ``oracle/pairs_oracle.c``,
+``oracle/dmat_oracle.c`` and ``oracle/wick_oracle.c`` into ``oracle/_build/liboracle.so`` with FMA
 contraction disabled, so the FP64 operation order is the one of picca's numba
 kernels.
 """
@@ -17,7 +17,7 @@ LIB = os.path.join(OUT_DIR, "liboracle.so")
 
 def build(force=False, quiet=True):
     """Compile the oracle if it is missing or older than its source."""
-    srcs = [os.path.join(HERE, name) for name in ("pairs_oracle.c", "dmat_oracle.c")]
+    srcs = [os.path.join(HERE, name) for name in ("pairs_oracle.c", "dmat_oracle.c", "wick_oracle.c")]
     if (not force and os.path.exists(LIB)
             and all(os.path.getmtime(LIB) >= os.path.getmtime(src) for src in srcs)):
         return LIB

@@ -522,6 +522,86 @@ int pg_xcf_metal_dmat(pg_plan *plan, const pg_corr_params *params, const pg_dmat
                       pair_first, pair_second, pair_angle, num_pairs, out, stream, 1);
 }
 
+int pg_wick_xi_matrices(pg_plan *plan, const pg_forest_set *set, const double *log_lambda,
+                        const double *variance, const double *xi_bounds,
+                        const double *xi_values, int32_t num_xi, const int32_t *forests,
+                        int64_t num_forests, const int64_t *x_offsets, double *arena,
+                        void *stream) {
+    if (!plan || !set || num_forests < 0 || num_xi < 1 || num_xi > 28000)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (num_forests > 0 && (!log_lambda || !variance || !xi_values || !forests ||
+                            !x_offsets || !arena || (num_xi > 1 && !xi_bounds)))
+        return PG_ERR_INVALID_ARGUMENT;
+    int rc = validate_set(set, true, false);
+    if (rc) return rc;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    return launch_wick_xmat(*set, log_lambda, variance, xi_bounds, xi_values, num_xi, forests,
+                            num_forests, x_offsets, arena, plan->num_sms, st);
+}
+
+static int wick_bins(const pg_corr_params *params, int *nb) {
+    if (!params || params->num_bins_r_par < 1 || params->num_bins_r_trans < 1 ||
+        !(params->r_par_max > params->r_par_min) || !(params->r_trans_max > 0))
+        return PG_ERR_INVALID_ARGUMENT;
+    const int64_t n = (int64_t)params->num_bins_r_par * params->num_bins_r_trans;
+    if (n > 6000) return PG_ERR_UNSUPPORTED;
+    *nb = (int)n;
+    return PG_OK;
+}
+
+int pg_cf_wick_work_bytes(pg_plan *plan, const pg_corr_params *params, int32_t max_pixels1,
+                          int32_t max_pixels2, int64_t max_ctas, uint64_t *bytes) {
+    if (!plan || !bytes || max_pixels1 < 1 || max_pixels2 < 1 || max_pixels1 > 65535 ||
+        max_pixels2 > 65535)
+        return PG_ERR_INVALID_ARGUMENT;
+    int nb = 0, grid = 0;
+    int rc = wick_bins(params, &nb);
+    if (rc) return rc;
+    if ((rc = select_device(plan))) return rc;
+    if ((rc = wick_t123_grid(nb, plan->num_sms, &grid))) return rc;
+    if (max_ctas > 0) grid = (int)std::min<int64_t>(grid, max_ctas);
+    *bytes = (uint64_t)grid * (uint64_t)max_pixels1 * (uint64_t)max_pixels2 * sizeof(uint32_t);
+    return PG_OK;
+}
+
+int pg_cf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *s1,
+               const pg_forest_set *s2, const double *zw1, const double *zw2,
+               const int64_t *x_offsets1, const double *arena1, const int64_t *x_offsets2,
+               const double *arena2, const int32_t *pair_first, const int32_t *pair_second,
+               const double *pair_angle, int64_t num_pairs, void *work, uint64_t work_bytes,
+               const pg_wick_sums *out, void *stream) {
+    if (!plan || !s1 || !out) return PG_ERR_INVALID_ARGUMENT;
+    int nb = 0, rc = wick_bins(params, &nb);
+    if (rc) return rc;
+    const pg_forest_set *t = s2 ? s2 : s1;
+    if ((rc = validate_set(s1, true, false)) || (rc = validate_set(t, true, false))) return rc;
+    if (num_pairs < 0 || num_pairs > INT32_MAX) return PG_ERR_INVALID_ARGUMENT;
+    if (s1->max_pixels < 1 || t->max_pixels < 1 || s1->max_pixels > 65535 ||
+        t->max_pixels > 65535)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (!out->weights_wick || !out->num_pairs_wick || !out->t1 || !out->t2 || !out->t3)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (num_pairs > 0 && (!zw1 || !zw2 || !x_offsets1 || !arena1 || !x_offsets2 || !arena2 ||
+                          !pair_first || !pair_second || !work))
+        return PG_ERR_INVALID_ARGUMENT;
+    if (reinterpret_cast<uintptr_t>(work) % 16) return PG_ERR_INVALID_ARGUMENT;
+    if ((rc = select_device(plan))) return rc;
+    int grid = 0;
+    if ((rc = wick_t123_grid(nb, plan->num_sms, &grid))) return rc;
+    const int64_t cap = (int64_t)s1->max_pixels * t->max_pixels;
+    grid = (int)std::min<uint64_t>((uint64_t)grid, work_bytes / ((uint64_t)cap * 4));
+    if (num_pairs > 0 && grid < 1) return PG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    if ((rc = reset_scratch(plan, st))) return rc;
+    return launch_wick_t123(*params, *s1, *t, zw1, zw2, x_offsets1, arena1, x_offsets2, arena2,
+                            pair_first, pair_second, pair_angle, num_pairs,
+                            static_cast<uint32_t *>(work), cap, grid, *out, scratch_of(plan), st);
+}
+
+
 int pg_fast_metal_dmat(pg_plan *plan, const pg_fast_metal_params *params,
                        const pg_fast_metal_side *s1, const pg_fast_metal_side *s2,
                        const pg_fast_metal_sums *out, void *stream) {

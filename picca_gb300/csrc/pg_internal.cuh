@@ -250,6 +250,19 @@ int launch_metal_dmat(const pg_corr_params &p, const pg_dmat_params &d, double z
                       const double *pair_angle, int64_t num_pairs, const pg_dmat_sums &out,
                       Scratch *scratch, int num_sms, cudaStream_t stream, bool xcf);
 
+int launch_wick_xmat(const pg_forest_set &s, const double *log_lambda, const double *variance,
+                     const double *bounds, const double *values, int32_t num_values,
+                     const int32_t *forests, int64_t num_forests, const int64_t *x_offsets,
+                     double *arena, int num_sms, cudaStream_t stream);
+int wick_t123_grid(int nb, int num_sms, int *grid);
+int launch_wick_t123(const pg_corr_params &p, const pg_forest_set &s1, const pg_forest_set &s2,
+                     const double *zw1, const double *zw2, const int64_t *xo1,
+                     const double *xa1, const int64_t *xo2, const double *xa2,
+                     const int32_t *pair_first, const int32_t *pair_second,
+                     const double *pair_angle, int64_t num_pairs, uint32_t *work,
+                     int64_t cap, int grid, const pg_wick_sums &out, Scratch *scratch,
+                     cudaStream_t stream);
+
 int launch_fast_metal(const pg_fast_metal_params &p, const pg_fast_metal_side &a,
                       const pg_fast_metal_side &b, const pg_fast_metal_sums &out,
                       Scratch *scratch, int num_sms, cudaStream_t stream);

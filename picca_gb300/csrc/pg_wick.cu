@@ -1,0 +1,325 @@
+// Wick covariance of the auto-correlation, terms T1-T3:
+// cf.compute_wick_terms + cf.compute_wickT123_pairs (py/picca/cf.py:
+// 1328-1495, :1498-1626).
+//
+// For a forest pair the reference lists the pixel pairs inside the r_par /
+// r_trans range with their bin, then visits every pair of listed pixel
+// pairs (a, b): a shared pixel of forest 1 adds X2[j_a, j_b] w1 zw1 to T2, a
+// shared pixel of forest 2 adds X1[i_a, i_b] w2 zw2 to T2, and otherwise
+// X1[i_a, i_b] X2[j_a, j_b] goes to T3, in the cell (bin a, bin b) and its
+// mirror. X is the weighted 1D correlation of a forest's own pixels,
+// (w w^T) xi_1d(|dlog_lambda|) sqrt(v v^T). This is O(K^2) in the K listed
+// pixel pairs of a forest pair.
+//
+// Two kernels:
+//  * wick_xmat_kernel: X of each listed forest, once, into an arena (the
+//    reference recomputes it for every pair). The diagonal is stored as 0:
+//    no term uses it, and a zero there lets T3 run without branches. xi_1d
+//    is scipy's nearest-neighbour rule (count of cell bounds below |dll|).
+//  * wick_t123_kernel: one CTA per forest pair (persistent). It counts the
+//    listed pixel pairs per bin in shared memory (with WALL, NB and the
+//    diagonal T1), sorts them by bin into a per-CTA list (counting sort),
+//    then every warp takes 32 pixel pairs a of one bin P and sweeps all b
+//    in bin order: lanes read X1[i_b][i_a] and X2[j_b][j_a] (rows of the
+//    symmetric matrices, so the 32 lanes touch one or two cache lines),
+//    one FP64 FMA per (a, b) for T3 and predicated FMAs for the shared-pixel
+//    T2 terms, and at each end of a bin Q the warp reduces and adds the
+//    (P, Q) cell to the output with one atomic.
+// All arithmetic is FP64; the sums differ from the reference's only in
+// summation order.
+#include <algorithm>
+
+#include "pg_internal.cuh"
+
+namespace pg {
+namespace {
+
+constexpr int kWkBlock = 256;
+constexpr int kWkWarps = kWkBlock / 32;
+constexpr int kXmBlock = 256;
+
+struct WickConst {
+    double r_par_min, r_par_max, r_trans_max, range;
+    int32_t np, nt, nb, x_correlation;
+    int64_t cap;  // list entries per CTA
+};
+
+__global__ void __launch_bounds__(kXmBlock)
+    wick_xmat_kernel(pg_forest_set s, const double *log_lambda, const double *variance,
+                     const double *bounds, const double *values, int32_t num_values,
+                     const int32_t *forests, int64_t num_forests, const int64_t *x_offsets,
+                     double *arena) {
+    extern __shared__ double xm_bounds[];
+    for (int k = threadIdx.x; k < num_values - 1; k += kXmBlock) xm_bounds[k] = bounds[k];
+    __syncthreads();
+    for (int64_t q = blockIdx.x; q < num_forests; q += gridDim.x) {
+        const int f = forests[q];
+        const int64_t o = s.pix_offset[f];
+        const int n = (int)(s.pix_offset[f + 1] - o);
+        double *x = arena + x_offsets[f];
+        for (int64_t t = threadIdx.x; t < (int64_t)n * n; t += kXmBlock) {
+            const int i = (int)(t / n), k = (int)(t - (int64_t)i * n);
+            if (i == k) {
+                x[t] = 0.;
+                continue;
+            }
+            const double d = fabs(log_lambda[o + k] - log_lambda[o + i]);
+            // searchsorted(bounds, d, 'left'): number of bounds below d
+            int lo = 0, hi = num_values - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi) >> 1;
+                if (xm_bounds[mid] < d)
+                    lo = mid + 1;
+                else
+                    hi = mid;
+            }
+            const double wi = s.weights[o + i], wk = s.weights[o + k];
+            const double vi = variance[o + i], vk = variance[o + k];
+            x[t] = ((wk * wi) * values[lo]) * sqrt(vk * vi);
+        }
+    }
+}
+
+struct WickSmem {
+    int32_t *count;   // [nb] listed pixel pairs per bin, then the write cursor
+    int32_t *start;   // [nb + 1] bin starts in the list
+    int32_t *nonempty;  // [nb] bins with pixel pairs, ascending
+    int32_t *task_start;  // [nb + 1] first 32-pair task of each nonempty bin
+    int32_t *npairs;  // [nb]
+    double *wall, *t1;  // [nb]
+    int32_t *scalars;  // num nonempty, num tasks, task counter
+};
+
+__device__ __forceinline__ WickSmem wick_smem(void *base, int nb) {
+    WickSmem m;
+    double *d = static_cast<double *>(base);
+    m.wall = d;
+    m.t1 = d + nb;
+    int32_t *p = reinterpret_cast<int32_t *>(d + 2 * nb);
+    m.count = p;
+    m.start = p + nb;
+    m.nonempty = m.start + nb + 1;
+    m.task_start = m.nonempty + nb;
+    m.npairs = m.task_start + nb + 1;
+    m.scalars = m.npairs + nb;
+    return m;
+}
+
+// Bin of the pixel pair (i, j), or -1 outside the range (cf.py:1561-1594).
+__device__ __forceinline__ int wick_bin(const WickConst &c, double r1, double r2, double cc,
+                                        double ss) {
+    double r_par = __dmul_rn(__dsub_rn(r1, r2), cc);
+    if (!c.x_correlation) r_par = fabs(r_par);
+    const double r_trans = __dmul_rn(__dadd_rn(r1, r2), ss);
+    if (!(r_par < c.r_par_max && r_trans < c.r_trans_max && r_par >= c.r_par_min)) return -1;
+    const int bp = (int)__dmul_rn(__ddiv_rn(__dsub_rn(r_par, c.r_par_min), c.range), (double)c.np);
+    const int bt = (int)__dmul_rn(__ddiv_rn(r_trans, c.r_trans_max), (double)c.nt);
+    return bt + c.nt * bp;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+    for (int off = 16; off > 0; off >>= 1) v += __shfl_down_sync(0xffffffffu, v, off);
+    return v;
+}
+
+__global__ void __launch_bounds__(kWkBlock)
+    wick_t123_kernel(WickConst c, pg_forest_set s1, pg_forest_set s2, const double *zw1,
+                     const double *zw2, const int64_t *xo1, const double *xa1,
+                     const int64_t *xo2, const double *xa2, const int32_t *pair_first,
+                     const int32_t *pair_second, const double *pair_angle, int64_t num_pairs,
+                     uint32_t *work, pg_wick_sums out, Scratch *scratch) {
+    extern __shared__ double wk_smem[];
+    __shared__ int s_item;
+    const int nb = c.nb, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    WickSmem m = wick_smem(wk_smem, nb);
+    uint32_t *list = work + (int64_t)blockIdx.x * c.cap;
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(&scratch->work_counter, 1);
+        for (int k = tid; k < nb; k += kWkBlock) {
+            m.count[k] = 0;
+            m.npairs[k] = 0;
+            m.wall[k] = 0.;
+            m.t1[k] = 0.;
+        }
+        __syncthreads();
+        const int64_t q = s_item;
+        if (q >= num_pairs) break;
+        const int f = pair_first[q], g = pair_second[q];
+        const double ang = pair_angle ? pair_angle[q]
+                                      : angle_between(s1.x_cart[f], s1.y_cart[f], s1.z_cart[f],
+                                                      s1.ra[f], s1.dec[f], s1.cos_dec[f],
+                                                      s2.x_cart[g], s2.y_cart[g], s2.z_cart[g],
+                                                      s2.ra[g], s2.dec[g]);
+        const double cc = cos(ang / 2), ss = sin(ang / 2);
+        const int64_t o1 = s1.pix_offset[f], o2 = s2.pix_offset[g];
+        const int n1 = (int)(s1.pix_offset[f + 1] - o1), n2 = (int)(s2.pix_offset[g + 1] - o2);
+        const int64_t grid = (int64_t)n1 * n2;
+        if (grid > c.cap) {
+            if (tid == 0) report_error(scratch, PG_ERR_INVALID_ARGUMENT, (int32_t)q);
+            __syncthreads();
+            continue;
+        }
+        if (tid == 0) atomicAdd(&scratch->work_items, 1ull);
+        // pass 1: counts, WALL, NB and T1 per bin
+        for (int64_t t = tid; t < grid; t += kWkBlock) {
+            const int j = (int)(t / n1), i = (int)(t - (int64_t)j * n1);
+            const int b = wick_bin(c, s1.r_comov[o1 + i], s2.r_comov[o2 + j], cc, ss);
+            if (b < 0) continue;
+            const double w12 = __dmul_rn(s1.weights[o1 + i], s2.weights[o2 + j]);
+            atomicAdd(&m.count[b], 1);
+            atomicAdd(&m.npairs[b], 1);
+            atomicAdd(&m.wall[b], w12);
+            atomicAdd(&m.t1[b], __dmul_rn(w12, __dmul_rn(zw1[o1 + i], zw2[o2 + j])));
+        }
+        __syncthreads();
+        if (tid == 0) {
+            int run = 0, nz = 0, tasks = 0;
+            for (int b = 0; b < nb; ++b) {
+                const int n = m.count[b];
+                m.start[b] = run;
+                m.count[b] = run;  // write cursor
+                if (n) {
+                    m.nonempty[nz] = b;
+                    m.task_start[nz] = tasks;
+                    tasks += (n + 31) >> 5;
+                    ++nz;
+                }
+                run += n;
+            }
+            m.start[nb] = run;
+            m.task_start[nz] = tasks;
+            m.scalars[0] = nz;
+            m.scalars[1] = tasks;
+            m.scalars[2] = 0;
+        }
+        __syncthreads();
+        const int nz = m.scalars[0], num_tasks = m.scalars[1];
+        // pass 2: list of (i, j) sorted by bin
+        for (int64_t t = tid; t < grid; t += kWkBlock) {
+            const int j = (int)(t / n1), i = (int)(t - (int64_t)j * n1);
+            const int b = wick_bin(c, s1.r_comov[o1 + i], s2.r_comov[o2 + j], cc, ss);
+            if (b < 0) continue;
+            list[atomicAdd(&m.count[b], 1)] = (uint32_t)i | ((uint32_t)j << 16);
+        }
+        for (int k = tid; k < nz; k += kWkBlock) {
+            const int b = m.nonempty[k];
+            atomicAdd(&out.weights_wick[b], m.wall[b]);
+            atomicAdd(reinterpret_cast<unsigned long long *>(&out.num_pairs_wick[b]),
+                      (unsigned long long)m.npairs[b]);
+            atomicAdd(&out.t1[(int64_t)b * nb + b], m.t1[b]);
+        }
+        __syncthreads();
+        const int num_listed = m.start[nb];
+        const double *x1 = xa1 + xo1[f], *x2 = xa2 + xo2[g];
+        for (;;) {
+            int task = 0;
+            if (lane == 0) task = atomicAdd(&m.scalars[2], 1);
+            task = __shfl_sync(0xffffffffu, task, 0);
+            if (task >= num_tasks) break;
+            // the nonempty bin holding this task
+            int lo = 0, hi = nz - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (m.task_start[mid] <= task)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            const int bin_p = m.nonempty[lo];
+            const int a = m.start[bin_p] + ((task - m.task_start[lo]) << 5) + lane;
+            const bool valid = a < m.start[bin_p + 1];
+            const uint32_t ua = valid ? list[a] : 0u;
+            const int ia = (int)(ua & 0xffffu), ja = (int)(ua >> 16);
+            const double c1a = valid ? __dmul_rn(s1.weights[o1 + ia], zw1[o1 + ia]) : 0.;
+            const double c2a = valid ? __dmul_rn(s2.weights[o2 + ja], zw2[o2 + ja]) : 0.;
+            double acc3 = 0., acc2 = 0.;
+            int kq = 0;
+            int end = m.start[m.nonempty[0] + 1];
+            for (int b = 0; b < num_listed; ++b) {
+                const uint32_t ub = list[b];
+                const int ib = (int)(ub & 0xffffu), jb = (int)(ub >> 16);
+                const double v1 = x1[(int64_t)ib * n1 + ia];
+                const double v2 = x2[(int64_t)jb * n2 + ja];
+                acc3 = fma(v1, v2, acc3);
+                if (ia == ib) acc2 = fma(v2, c1a, acc2);
+                if (ja == jb) acc2 = fma(v1, c2a, acc2);
+                if (b + 1 == end) {
+                    const double r3 = warp_sum(valid ? acc3 : 0.);
+                    const double r2 = warp_sum(valid ? acc2 : 0.);
+                    if (lane == 0) {
+                        const int64_t cell = (int64_t)bin_p * nb + m.nonempty[kq];
+                        if (r3 != 0.) atomicAdd(&out.t3[cell], r3);
+                        if (r2 != 0.) atomicAdd(&out.t2[cell], r2);
+                    }
+                    acc3 = acc2 = 0.;
+                    if (++kq < nz) end = m.start[m.nonempty[kq] + 1];
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
+}  // namespace
+
+int wick_xmat_smem(int num_values) { return (int)(sizeof(double) * std::max(1, num_values - 1)); }
+
+int launch_wick_xmat(const pg_forest_set &s, const double *log_lambda, const double *variance,
+                     const double *bounds, const double *values, int32_t num_values,
+                     const int32_t *forests, int64_t num_forests, const int64_t *x_offsets,
+                     double *arena, int num_sms, cudaStream_t stream) {
+    if (num_forests == 0) return PG_OK;
+    const int smem = wick_xmat_smem(num_values);
+    cudaError_t err = cudaFuncSetAttribute(
+        wick_xmat_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    if (err != cudaSuccess) return check_cuda(err);
+    const int64_t grid = std::min<int64_t>((int64_t)num_sms * 8, num_forests);
+    wick_xmat_kernel<<<(int)grid, kXmBlock, smem, stream>>>(s, log_lambda, variance, bounds,
+                                                            values, num_values, forests,
+                                                            num_forests, x_offsets, arena);
+    return check_cuda(cudaGetLastError());
+}
+
+size_t wick_t123_smem(int nb) {
+    return (size_t)2 * nb * sizeof(double) + ((size_t)5 * nb + 2 + 3) * sizeof(int32_t);
+}
+
+int wick_t123_grid(int nb, int num_sms, int *grid) {
+    const size_t smem = wick_t123_smem(nb);
+    cudaError_t err = cudaFuncSetAttribute(
+        wick_t123_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return check_cuda(err);
+    int occ = 0;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, wick_t123_kernel, kWkBlock, smem);
+    if (err != cudaSuccess || occ < 1) return PG_ERR_CUDA;
+    *grid = num_sms * occ;
+    return PG_OK;
+}
+
+int launch_wick_t123(const pg_corr_params &p, const pg_forest_set &s1, const pg_forest_set &s2,
+                     const double *zw1, const double *zw2, const int64_t *xo1,
+                     const double *xa1, const int64_t *xo2, const double *xa2,
+                     const int32_t *pair_first, const int32_t *pair_second,
+                     const double *pair_angle, int64_t num_pairs, uint32_t *work,
+                     int64_t cap, int grid, const pg_wick_sums &out, Scratch *scratch,
+                     cudaStream_t stream) {
+    if (num_pairs == 0) return PG_OK;
+    WickConst c;
+    c.r_par_min = p.r_par_min;
+    c.r_par_max = p.r_par_max;
+    c.r_trans_max = p.r_trans_max;
+    c.range = p.r_par_max - p.r_par_min;
+    c.np = p.num_bins_r_par;
+    c.nt = p.num_bins_r_trans;
+    c.nb = c.np * c.nt;
+    c.x_correlation = p.x_correlation;
+    c.cap = cap;
+    const size_t smem = wick_t123_smem(c.nb);
+    const int64_t blocks = std::min<int64_t>(grid, num_pairs);
+    wick_t123_kernel<<<(int)blocks, kWkBlock, smem, stream>>>(
+        c, s1, s2, zw1, zw2, xo1, xa1, xo2, xa2, pair_first, pair_second, pair_angle, num_pairs,
+        work, out, scratch);
+    return check_cuda(cudaGetLastError());
+}
+
+}  // namespace pg

@@ -1,0 +1,280 @@
+"""Wick covariance of the auto-correlation on the GPU: cf.compute_wick_terms
+with cf.compute_wickT123_pairs (py/picca/cf.py:1328-1626) and picca_wick.py
+(py/picca/bin/picca_wick.py:392-540).
+
+Host side of ``pg_wick_xi_matrices`` / ``pg_cf_wick``: the 1D variance and
+1D correlation of the pixels of one forest from a picca_cf1d.py table
+(nearest tabulated point, as scipy's interp1d in the reference), the random
+draw per forest, the forest pairs (every neighbour of a kept forest), the
+per-pixel redshift-evolution factors, and the normalisation. The weighted 1D
+correlation matrix of each forest in a pair is built once on the device; the
+O(K^2) sum over pairs of pixel pairs runs in ``csrc/pg_wick.cu``.
+
+Diagrams 4 and 5 (picca_wick.py --max-diagram > 3) and the two-field form
+(--in-dir2 / --lambda-abs2) are not provided: the reference's own code for
+them does not run (compute_wickT45_pairs indexes the 1-3 pixel pairs with
+the 1-2 bins, and the second field's relabelling loop renames the first
+field), and picca_wick.py's default is --max-diagram 3, where T4-T6 are 0.
+"""
+
+import ctypes
+
+import numpy as np
+import torch
+
+from . import _native
+from . import pairs as _pairs
+from ._native import check
+
+_P = ctypes.POINTER
+
+
+class WickSumsC(ctypes.Structure):
+    _fields_ = [("weights_wick", ctypes.c_void_p), ("num_pairs_wick", ctypes.c_void_p),
+                ("t1", ctypes.c_void_p), ("t2", ctypes.c_void_p), ("t3", ctypes.c_void_p)]
+
+
+def _bind():
+    lib = _native.lib()
+    if not getattr(lib, "_wick_bound", False):
+        vp, i64, i32 = ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32
+        lib.pg_wick_xi_matrices.restype = ctypes.c_int
+        lib.pg_wick_xi_matrices.argtypes = [vp, _P(_native.ForestSetC), vp, vp, vp, vp, i32, vp,
+                                            i64, vp, vp, vp]
+        lib.pg_cf_wick_work_bytes.restype = ctypes.c_int
+        lib.pg_cf_wick_work_bytes.argtypes = [vp, _P(_native.CorrParams), i32, i32, i64,
+                                              _P(ctypes.c_uint64)]
+        lib.pg_cf_wick.restype = ctypes.c_int
+        lib.pg_cf_wick.argtypes = [vp, _P(_native.CorrParams), _P(_native.ForestSetC),
+                                   _P(_native.ForestSetC), vp, vp, vp, vp, vp, vp, vp, vp, vp,
+                                   i64, vp, ctypes.c_uint64, _P(WickSumsC), vp]
+        lib._wick_bound = True
+    return lib
+
+
+def read_cf1d(path):
+    """HDU 1 of a picca_cf1d.py file: LLMIN, DLL and the v1d / nv1d / c1d /
+    nb1d columns (py/picca/bin/picca_wick.py:392-421)."""
+    from . import fitsio_lite
+    hdu = fitsio_lite.FITS(path)[1]
+    header = hdu.read_header()
+    out = {k: np.asarray(hdu[k][:]) for k in ("v1d", "nv1d", "c1d", "nb1d")}
+    out["LLMIN"], out["DLL"] = float(header["LLMIN"]), float(header["DLL"])
+    return out
+
+
+class OneDTables:
+    """The reference's nearest-point interpolants of a picca_cf1d.py table:
+    the variance at a pixel's log_lambda (evaluated here on the host), and
+    the 1D correlation at |dlog_lambda| as cell bounds and values for the
+    device (scipy interp1d kind="nearest": the value of the point whose
+    cell, bounded by the midpoints x[k] / 2 + x[k + 1] / 2, holds the
+    argument; ties go to the lower point; beyond the ends, the end points)."""
+
+    def __init__(self, cf1d):
+        log_lambda = cf1d["LLMIN"] + cf1d["DLL"] * np.arange(len(cf1d["v1d"]))
+        kv = np.asarray(cf1d["nv1d"]) > 0
+        self.var_x = log_lambda[kv]
+        self.var_y = np.asarray(cf1d["v1d"], dtype=np.float64)[kv]
+        kx = np.asarray(cf1d["nb1d"]) > 0
+        self.xi_x = (log_lambda - cf1d["LLMIN"])[kx]
+        self.xi_y = np.ascontiguousarray(np.asarray(cf1d["c1d"], dtype=np.float64)[kx])
+        if self.var_x.size == 0 or self.xi_x.size == 0:
+            raise ValueError("empty 1D correlation table")
+        self.xi_bounds = np.ascontiguousarray(self._bounds(self.xi_x))
+        self.var_bounds = self._bounds(self.var_x)
+
+    @staticmethod
+    def _bounds(x):
+        half = x / 2.0
+        return half[1:] + half[:-1]
+
+    def variance(self, log_lambda):
+        idx = np.searchsorted(self.var_bounds, log_lambda, side="left")
+        return self.var_y[np.clip(idx, 0, self.var_y.size - 1)]
+
+
+def selection(fs, nproc, reject):
+    """Kept forests of cf.compute_wick_terms (py/picca/cf.py:1376-1380 with
+    picca_wick.py:20-37, 498-512): healpix rows dealt to nproc chunks, the
+    generator seeded with the chunk's first healpix, one rand(len(forests))
+    draw per healpix. Returns (keep, npall, npused)."""
+    keep = np.zeros(fs.num, dtype=bool)
+    rows = np.asarray(fs.row)
+    members = {}
+    for f, row in enumerate(rows):
+        members.setdefault(int(row), []).append(f)
+    chunks = {}
+    for index in range(len(fs.healpix_list)):
+        chunks.setdefault(index % nproc, []).append(index)
+    npall = npused = 0
+    for chunk in chunks.values():
+        rng = np.random.RandomState(int(fs.healpix_list[chunk[0]]))
+        for row in chunk:
+            forests = members.get(row, [])
+            draw = rng.rand(len(forests)) > reject
+            keep[forests] = draw
+            npall += len(forests)
+            npused += int(draw.sum())
+    return keep, npall, npused
+
+
+class WickEngine:
+    """Wick terms T1-T3 on one CUDA device."""
+
+    def __init__(self, engine=None, device=None):
+        self.engine = engine or _pairs.PairEngine(device)
+        self.device = self.engine.device
+        self._work = None
+
+    def _stream(self):
+        return self.engine._stream()
+
+    def xi_matrices(self, dev, tables, forests):
+        """Arena of the weighted 1D correlation matrices of ``forests``
+        (indices into dev's set) and the per-forest offsets into it."""
+        lib = _bind()
+        fs = dev.source
+        npix = np.asarray(dev.npix, dtype=np.int64)
+        offsets = np.zeros(max(fs.num, 1), dtype=np.int64)
+        forests = np.unique(np.asarray(forests, dtype=np.int64))
+        sizes = npix[forests] ** 2
+        offsets[forests] = np.concatenate([[0], np.cumsum(sizes)[:-1]]) if forests.size else []
+        total = int(sizes.sum()) if forests.size else 0
+        ll = np.asarray(fs.log_lambda, dtype=np.float64)
+        var = tables.variance(ll) if ll.size else np.zeros(1)
+        dvc = self.device
+        t = {"ll": torch.from_numpy(np.ascontiguousarray(ll if ll.size else np.zeros(1))).to(dvc),
+             "var": torch.from_numpy(np.ascontiguousarray(var)).to(dvc),
+             "bounds": torch.from_numpy(tables.xi_bounds if tables.xi_bounds.size
+                                        else np.zeros(1)).to(dvc),
+             "values": torch.from_numpy(tables.xi_y).to(dvc),
+             "forests": torch.from_numpy(forests.astype(np.int32) if forests.size
+                                         else np.zeros(1, dtype=np.int32)).to(dvc),
+             "offsets": torch.from_numpy(offsets).to(dvc)}
+        arena = torch.empty(max(total, 1), dtype=torch.float64, device=dvc)
+        with torch.cuda.device(dvc):
+            check(lib.pg_wick_xi_matrices(
+                self.engine.plan.handle, ctypes.byref(dev.c), t["ll"].data_ptr(),
+                t["var"].data_ptr(), t["bounds"].data_ptr(), t["values"].data_ptr(),
+                int(tables.xi_y.size), t["forests"].data_ptr(), int(forests.size),
+                t["offsets"].data_ptr(), arena.data_ptr(), self._stream()), "Wick xi matrices")
+        return arena, t["offsets"], t
+
+    def alloc_sums(self, nb):
+        dvc = self.device
+        return {"weights_wick": torch.zeros(nb, dtype=torch.float64, device=dvc),
+                "num_pairs_wick": torch.zeros(nb, dtype=torch.int64, device=dvc),
+                "t1": torch.zeros(nb * nb, dtype=torch.float64, device=dvc),
+                "t2": torch.zeros(nb * nb, dtype=torch.float64, device=dvc),
+                "t3": torch.zeros(nb * nb, dtype=torch.float64, device=dvc)}
+
+    def work_buffer(self, params, max_pixels1, max_pixels2, num_pairs):
+        lib = _bind()
+        nbytes = ctypes.c_uint64()
+        with torch.cuda.device(self.device):
+            check(lib.pg_cf_wick_work_bytes(self.engine.plan.handle, ctypes.byref(params),
+                                            int(max_pixels1), int(max_pixels2), int(num_pairs),
+                                            ctypes.byref(nbytes)), "Wick work size")
+        need = int(nbytes.value)
+        if self._work is None or self._work.numel() < need:
+            self._work = torch.empty(max(need, 16), dtype=torch.uint8, device=self.device)
+        return self._work
+
+    def accumulate(self, params, dev, zw1, zw2, xo, xa, first, second, num_pairs, sums,
+                   angles=None):
+        """Launch pg_cf_wick (asynchronous on the current stream)."""
+        lib = _bind()
+        work = self.work_buffer(params, dev.max_pixels, dev.max_pixels, max(int(num_pairs), 1))
+        out = WickSumsC(*[sums[k].data_ptr() for k in ("weights_wick", "num_pairs_wick", "t1",
+                                                       "t2", "t3")])
+        with torch.cuda.device(self.device):
+            check(lib.pg_cf_wick(
+                self.engine.plan.handle, ctypes.byref(params), ctypes.byref(dev.c), None,
+                zw1.data_ptr(), zw2.data_ptr(), xo.data_ptr(), xa.data_ptr(), xo.data_ptr(),
+                xa.data_ptr(), first.data_ptr(), second.data_ptr(),
+                angles.data_ptr() if angles is not None else None, int(num_pairs),
+                work.data_ptr(), int(work.numel()), ctypes.byref(out), self._stream()),
+                "Wick terms")
+        return sums
+
+    def stats(self):
+        return self.engine.stats()
+
+
+def forest_pairs(dev, offsets, index, mask):
+    """(first, second) device lists of the neighbour entries in ``mask``,
+    longest pixel grids first (a better balance of the persistent CTAs)."""
+    total = int(mask.size)
+    device = dev.device
+    if total == 0 or not mask.any():
+        z = torch.zeros(1, dtype=torch.int32, device=device)
+        return z, z, 0
+    k = torch.nonzero(torch.from_numpy(mask).to(device)).flatten()
+    first = torch.searchsorted(offsets, k, right=True) - 1
+    second = index[:total][k].long()
+    npix = torch.from_numpy(np.asarray(dev.npix, dtype=np.int64)).to(device)
+    order = torch.argsort(npix[first] * npix[second], descending=True, stable=True)
+    return (first[order].to(torch.int32).contiguous(),
+            second[order].to(torch.int32).contiguous(), int(k.numel()))
+
+
+def evolution(z, z_ref, alpha):
+    """((1 + z) / (1 + z_ref))^(alpha - 1) per pixel (cf.py:1545-1546)."""
+    return ((1 + np.asarray(z, dtype=np.float64)) / (1 + z_ref)) ** (alpha - 1)
+
+
+def normalise(raw, npall, npused):
+    """py/picca/bin/picca_wick.py:515-540: every term divided by
+    WALL WALL^T where positive and scaled by NPUSED / NPALL; T4-T6 are 0."""
+    nb = raw["weights_wick"].size
+    weights = raw["weights_wick"] * raw["weights_wick"][:, None]
+    w = weights > 0.0
+    out = {"WALL": raw["weights_wick"].copy(), "NB": raw["num_pairs_wick"].copy()}
+    for key in ("t1", "t2", "t3"):
+        t = raw[key].reshape(nb, nb).copy()
+        t[w] /= weights[w]
+        t *= 1.0 * npused / npall
+        out[key.upper()] = t
+    for key in ("T4", "T5", "T6"):
+        out[key] = np.zeros((nb, nb))
+    out["CO"] = out["T1"] + out["T2"] + out["T3"] + out["T4"] + out["T5"] + out["T6"]
+    out["NPALL"], out["NPUSED"] = int(npall), int(npused)
+    return out
+
+
+def wick_covariance(fs, params, cf1d, reject, nproc=1, z_ref=2.25, alpha=2.9, alpha2=None,
+                    engine=None, return_raw=False):
+    """picca_wick.py for one delta field (auto-correlation, --max-diagram 3)
+    on a ForestSet: the normalised COV columns (CO, WALL, NB, T1-T6) and
+    NPALL / NPUSED."""
+    alpha2 = alpha if alpha2 is None else alpha2
+    engine = engine or WickEngine()
+    pe = engine.engine
+    tables = OneDTables(cf1d)
+    dev = _pairs.DeviceForests(fs, pe.device, compact=False)
+    offsets, index, _ = pe.neighbours(params, dev)
+    keep, npall, npused = selection(fs, nproc, reject)
+    off_h = offsets.cpu().numpy()
+    mask = np.repeat(keep, np.diff(off_h))
+    first, second, num = forest_pairs(dev, offsets, index, mask)
+    nb = params.num_bins_r_par * params.num_bins_r_trans
+    sums = engine.alloc_sums(nb)
+    if num:
+        used = np.unique(np.concatenate([first[:num].cpu().numpy(),
+                                         second[:num].cpu().numpy()]))
+        xa, xo, _keep_alive = engine.xi_matrices(dev, tables, used)
+        z = np.asarray(fs.z, dtype=np.float64)
+        zw1 = torch.from_numpy(np.ascontiguousarray(evolution(z, z_ref, alpha)
+                                                    if z.size else np.zeros(1))).to(pe.device)
+        zw2 = torch.from_numpy(np.ascontiguousarray(evolution(z, z_ref, alpha2)
+                                                    if z.size else np.zeros(1))).to(pe.device)
+        engine.accumulate(params, dev, zw1, zw2, xo, xa, first, second, num, sums)
+        stats = engine.stats()
+        if stats.status != 0:
+            raise _native.NativeError(f"Wick kernel reported status {stats.status}")
+    raw = {k: v.cpu().numpy() for k, v in sums.items()}
+    out = normalise(raw, npall, npused)
+    if return_raw:
+        out["raw"] = raw
+    return out
