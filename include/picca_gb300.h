@@ -31,6 +31,8 @@
  *  - pg_wick_xi_matrices, pg_cf_wick
  *                       <- cf.compute_wick_terms + cf.compute_wickT123_pairs
  *                          py/picca/cf.py:1328-1495, :1498-1626
+ *  - pg_xcf_wick        <- xcf.compute_wick_terms + xcf.compute_wickT1234_pairs
+ *                          py/picca/xcf.py:838-1008, :1220-1351
  *  - pg_fast_metal_dmat <- calc_fast_metal_dmat of
  *                          py/picca/bin/picca_fast_metal_dmat.py:30-251 and
  *                          py/picca/bin/picca_fast_metal_xdmat.py:28-215
@@ -461,13 +463,14 @@ int pg_wick_xi_matrices(pg_plan *plan, const pg_forest_set *set, const double *l
                         int64_t num_forests, const int64_t *x_offsets, double *arena,
                         void *stream);
 
-/* Sums of cf.compute_wick_terms (device, ACCUMULATED into): weights_wick
- * and num_pairs_wick [nb], t1 / t2 / t3 [nb * nb] (t1 only on its
- * diagonal), nb = num_bins_r_par * num_bins_r_trans. */
+/* Sums of cf.compute_wick_terms / xcf.compute_wick_terms (device,
+ * ACCUMULATED into): weights_wick and num_pairs_wick [nb], t1 .. t4
+ * [nb * nb] (t1 only on its diagonal; t4 only for the cross, may be NULL
+ * for pg_cf_wick), nb = num_bins_r_par * num_bins_r_trans. */
 typedef struct pg_wick_sums {
     double *weights_wick;
     int64_t *num_pairs_wick;
-    double *t1, *t2, *t3;
+    double *t1, *t2, *t3, *t4;
 } pg_wick_sums;
 
 /* Terms T1-T3 of the forest pairs (pair_first[q] of s1, pair_second[q] of
@@ -486,6 +489,27 @@ int pg_cf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set 
                const double *arena2, const int32_t *pair_first, const int32_t *pair_second,
                const double *pair_angle, int64_t num_pairs, void *work, uint64_t work_bytes,
                const pg_wick_sums *out, void *stream);
+
+/* Terms T1-T4 of the delta x quasar Wick covariance. A work item q is
+ * forest item_forest[q] of `forests` with its neighbouring quasars
+ * obj_index[item_start[q] .. item_start[q] + item_count[q]) of `objs`
+ * (obj_angle, optional and aligned with obj_index, overrides the angles
+ * from the unit vectors). zw1: per pixel of `forests`
+ * ((1 + z) / (1 + z_ref))^(alpha - 1); zw_obj: per object
+ * ((1 + z_qso) / (1 + z_ref))^(alpha_obj - 1); the objects' weights and
+ * comoving distances are objs->obj_weight / obj_r_comov. r_par is signed and
+ * a pair is kept when r_par_min <= r_par < r_par_max, r_trans <
+ * r_trans_max. work: pg_xcf_wick_work_bytes() bytes (16-byte aligned) for
+ * forests of at most max_pixels pixels and items of at most max_quasars
+ * quasars (both at most 65535). */
+int pg_xcf_wick_work_bytes(pg_plan *plan, const pg_corr_params *params, int32_t max_pixels,
+                           int32_t max_quasars, int64_t max_ctas, uint64_t *bytes);
+int pg_xcf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *forests,
+                const pg_forest_set *objs, const double *zw1, const double *zw_obj,
+                const int64_t *x_offsets, const double *arena, const int32_t *item_forest,
+                const int32_t *item_start, const int32_t *item_count, const int32_t *obj_index,
+                const double *obj_angle, int64_t num_items, int32_t max_quasars, void *work,
+                uint64_t work_bytes, const pg_wick_sums *out, void *stream);
 
 /* Fast metal distortion matrix (py/picca/bin/picca_fast_metal_dmat.py:30-251,
  * py/picca/bin/picca_fast_metal_xdmat.py:28-215): every pair (i, j) of two

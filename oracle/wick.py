@@ -43,6 +43,11 @@ def _lib():
     lib = cpu.lib()
     if not getattr(lib, "_wick_bound", False):
         d = _P(ctypes.c_double)
+        lib.oracle_xwick_t1234.restype = None
+        lib.oracle_xwick_t1234.argtypes = (
+            [_P(WickParams)] + [d] * 4 + [ctypes.c_int64] + [d] * 4 + [ctypes.c_int64, d,
+                                                                     _P(ctypes.c_int64)]
+            + [d] * 4)
         lib.oracle_wick_t123.restype = None
         lib.oracle_wick_t123.argtypes = (
             [_P(WickParams)] + [d] * 4 + [ctypes.c_int64] + [d] * 4 + [ctypes.c_int64,
@@ -150,18 +155,64 @@ def pipeline(fs, p, ang_max, cf1d, reject, nproc=1, z_ref=2.25, alpha=2.9, alpha
     return res
 
 
-def normalise(out, npall, npused):
-    """picca_wick.py:515-540."""
+def xforest(p, r1, w1, zw1, x1, rq, wq, zwq, ang, out):
+    """compute_wickT1234_pairs for one forest and its quasars."""
+    a1 = [np.ascontiguousarray(a, dtype=np.float64) for a in (r1, w1, zw1, x1)]
+    a2 = [np.ascontiguousarray(a, dtype=np.float64) for a in (rq, wq, zwq, ang)]
+    _lib().oracle_xwick_t1234(ctypes.byref(p), *[_dp(a) for a in a1], len(a1[0]),
+                              *[_dp(a) for a in a2], len(a2[0]), _dp(out["weights_wick"]),
+                              out["num_pairs_wick"].ctypes.data_as(_P(ctypes.c_int64)),
+                              _dp(out["t1"]), _dp(out["t2"]), _dp(out["t3"]), _dp(out["t4"]))
+
+
+def xpipeline(fs, qs, p, ang_max, cf1d, reject, nproc=1, z_ref=2.25, alpha=2.9, alpha_obj=1.44,
+              return_raw=False):
+    """picca_xwick.py (py/picca/bin/picca_xwick.py:447-520) with
+    xcf.compute_wick_terms (py/picca/xcf.py:838-1008) on a forest set and a
+    quasar set, --max-diagram 4 (the default): T1-T4."""
+    oparams = cpu.make_params(p.r_par_min, p.r_par_max, p.r_trans_max, p.num_bins_r_par,
+                              p.num_bins_r_trans)
+    offsets, index = cpu.neighbours(fs, qs, oparams, ang_max, auto_mode=0, xcf=True)
+    keep, npall, npused = selection(fs, nproc, reject)
+    variance, xi = interpolants(cf1d)
+    po = np.asarray(fs.pix_offset)
+    out = new_outputs(p)
+    out["t4"] = np.zeros_like(out["t1"])
+    for f in np.nonzero(keep)[0]:
+        nbrs = [int(index[k]) for k in range(int(offsets[f]), int(offsets[f + 1]))]
+        if not nbrs:
+            continue
+        sl = slice(po[f], po[f + 1])
+        ll, w1, z1 = fs.log_lambda[sl], fs.weights[sl], fs.z[sl]
+        x1 = weighted_xi_1d(ll, w1, variance, xi)
+        zw1 = ((1 + z1) / (1 + z_ref)) ** (alpha - 1)
+        ang = np.array([cpu.lib().oracle_angle(fs.x_cart[f], fs.y_cart[f], fs.z_cart[f],
+                                               fs.ra[f], fs.dec[f], fs.cos_dec[f],
+                                               qs.x_cart[g], qs.y_cart[g], qs.z_cart[g],
+                                               qs.ra[g], qs.dec[g]) for g in nbrs])
+        zq = qs.z_qso[nbrs]
+        zwq = ((1 + zq) / (1 + z_ref)) ** (alpha_obj - 1)
+        xforest(p, fs.r_comov[sl], w1, zw1, x1, qs.obj_r_comov[nbrs], qs.obj_weight[nbrs], zwq,
+                ang, out)
+    res = normalise(out, npall, npused, terms=("t1", "t2", "t3", "t4"))
+    if return_raw:
+        res["raw"] = out
+    return res
+
+
+def normalise(out, npall, npused, terms=("t1", "t2", "t3")):
+    """picca_wick.py:515-540 (picca_xwick.py:487-506 with T4)."""
     weights = out["weights_wick"] * out["weights_wick"][:, None]
     w = weights > 0.0
     res = {"WALL": out["weights_wick"].copy(), "NB": out["num_pairs_wick"].copy()}
-    for key in ("t1", "t2", "t3"):
+    for key in terms:
         t = out[key].copy()
         t[w] /= weights[w]
         t *= 1.0 * npused / npall
         res[key.upper()] = t
-    for key in ("T4", "T5", "T6"):
-        res[key] = np.zeros_like(res["T1"])
+    for key in ("T2", "T3", "T4", "T5", "T6"):
+        if key not in res:
+            res[key] = np.zeros_like(res["T1"])
     res["CO"] = res["T1"] + res["T2"] + res["T3"] + res["T4"] + res["T5"] + res["T6"]
     res["NPALL"], res["NPUSED"] = npall, npused
     return res

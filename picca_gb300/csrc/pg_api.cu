@@ -602,6 +602,61 @@ int pg_cf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set 
 }
 
 
+int pg_xcf_wick_work_bytes(pg_plan *plan, const pg_corr_params *params, int32_t max_pixels,
+                           int32_t max_quasars, int64_t max_ctas, uint64_t *bytes) {
+    if (!plan || !bytes || max_pixels < 1 || max_quasars < 1 || max_pixels > 65535 ||
+        max_quasars > 65535)
+        return PG_ERR_INVALID_ARGUMENT;
+    int nb = 0, grid = 0;
+    int rc = wick_bins(params, &nb);
+    if (rc) return rc;
+    if ((rc = select_device(plan))) return rc;
+    if ((rc = xwick_grid(nb, plan->num_sms, &grid))) return rc;
+    if (max_ctas > 0) grid = (int)std::min<int64_t>(grid, max_ctas);
+    *bytes = (uint64_t)grid *
+             (uint64_t)xwick_cta_bytes((int64_t)max_pixels * max_quasars, max_quasars);
+    return PG_OK;
+}
+
+int pg_xcf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *forests,
+                const pg_forest_set *objs, const double *zw1, const double *zw_obj,
+                const int64_t *x_offsets, const double *arena, const int32_t *item_forest,
+                const int32_t *item_start, const int32_t *item_count, const int32_t *obj_index,
+                const double *obj_angle, int64_t num_items, int32_t max_quasars, void *work,
+                uint64_t work_bytes, const pg_wick_sums *out, void *stream) {
+    if (!plan || !forests || !objs || !out) return PG_ERR_INVALID_ARGUMENT;
+    int nb = 0, rc = wick_bins(params, &nb);
+    if (rc) return rc;
+    if ((rc = validate_set(forests, true, false)) || (rc = validate_set(objs, false, true)))
+        return rc;
+    if (num_items < 0 || num_items > INT32_MAX) return PG_ERR_INVALID_ARGUMENT;
+    if (forests->max_pixels < 1 || forests->max_pixels > 65535 || max_quasars < 1 ||
+        max_quasars > 65535)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (!out->weights_wick || !out->num_pairs_wick || !out->t1 || !out->t2 || !out->t3 ||
+        !out->t4)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (num_items > 0 && (!zw1 || !zw_obj || !x_offsets || !arena || !item_forest ||
+                          !item_start || !item_count || !obj_index || !work))
+        return PG_ERR_INVALID_ARGUMENT;
+    if (reinterpret_cast<uintptr_t>(work) % 16) return PG_ERR_INVALID_ARGUMENT;
+    if ((rc = select_device(plan))) return rc;
+    int grid = 0;
+    if ((rc = xwick_grid(nb, plan->num_sms, &grid))) return rc;
+    const int64_t cap = (int64_t)forests->max_pixels * max_quasars;
+    const uint64_t per_cta = (uint64_t)xwick_cta_bytes(cap, max_quasars);
+    grid = (int)std::min<uint64_t>((uint64_t)grid, work_bytes / per_cta);
+    if (num_items > 0 && grid < 1) return PG_ERR_INVALID_ARGUMENT;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    if ((rc = reset_scratch(plan, st))) return rc;
+    return launch_xwick(*params, *forests, *objs, zw1, zw_obj, x_offsets, arena, item_forest,
+                        item_start, item_count, obj_index, obj_angle, num_items,
+                        static_cast<char *>(work), cap, max_quasars, grid, *out,
+                        scratch_of(plan), st);
+}
+
+
 int pg_fast_metal_dmat(pg_plan *plan, const pg_fast_metal_params *params,
                        const pg_fast_metal_side *s1, const pg_fast_metal_side *s2,
                        const pg_fast_metal_sums *out, void *stream) {

@@ -263,6 +263,15 @@ int launch_wick_t123(const pg_corr_params &p, const pg_forest_set &s1, const pg_
                      int64_t cap, int grid, const pg_wick_sums &out, Scratch *scratch,
                      cudaStream_t stream);
 
+int64_t xwick_cta_bytes(int64_t cap, int64_t max_quasars);
+int xwick_grid(int nb, int num_sms, int *grid);
+int launch_xwick(const pg_corr_params &p, const pg_forest_set &forests, const pg_forest_set &objs,
+                 const double *zw1, const double *zw_obj, const int64_t *xo, const double *xa,
+                 const int32_t *item_forest, const int32_t *item_start, const int32_t *item_count,
+                 const int32_t *obj_index, const double *obj_angle, int64_t num_items,
+                 char *work, int64_t cap, int64_t max_quasars, int grid,
+                 const pg_wick_sums &out, Scratch *scratch, cudaStream_t stream);
+
 int launch_fast_metal(const pg_fast_metal_params &p, const pg_fast_metal_side &a,
                       const pg_fast_metal_side &b, const pg_fast_metal_sums &out,
                       Scratch *scratch, int num_sms, cudaStream_t stream);

@@ -1,6 +1,8 @@
 // Wick covariance of the auto-correlation, terms T1-T3:
 // cf.compute_wick_terms + cf.compute_wickT123_pairs (py/picca/cf.py:
-// 1328-1495, :1498-1626).
+// 1328-1495, :1498-1626), and of the delta x quasar cross-correlation,
+// terms T1-T4: xcf.compute_wick_terms + xcf.compute_wickT1234_pairs
+// (py/picca/xcf.py:838-1008, :1220-1351).
 //
 // For a forest pair the reference lists the pixel pairs inside the r_par /
 // r_trans range with their bin, then visits every pair of listed pixel
@@ -25,6 +27,12 @@
 //    one FP64 FMA per (a, b) for T3 and predicated FMAs for the shared-pixel
 //    T2 terms, and at each end of a bin Q the warp reduces and adds the
 //    (P, Q) cell to the output with one atomic.
+//  * xwick_kernel: the cross. A work item is one forest with its
+//    neighbouring quasars (each with its own angle); the listed pairs are
+//    (pixel, quasar). T2 (same quasar) and T4 (different quasars) are both
+//    X1[i_a, i_b] zw_a zw_b: the sweep keeps the sum over all b and the
+//    same-quasar part, T4 is their difference; T3 (same pixel) sums
+//    w12_b and is scaled by w12_a / w1 zw1 at the flush.
 // All arithmetic is FP64; the sums differ from the reference's only in
 // summation order.
 #include <algorithm>
@@ -260,6 +268,182 @@ __global__ void __launch_bounds__(kWkBlock)
     }
 }
 
+struct XWickConst {
+    double r_par_min, r_par_max, r_trans_max, range;
+    int32_t np, nt, nb, pad;
+    int64_t cap, max_quasars;
+};
+
+// Bin of a (pixel, quasar) pair, or -1 (xcf.py:1282-1316, r_par signed).
+__device__ __forceinline__ int xwick_bin(const XWickConst &c, double r1, double r2, double cc,
+                                         double ss) {
+    const double r_par = __dmul_rn(__dsub_rn(r1, r2), cc);
+    const double r_trans = __dmul_rn(__dadd_rn(r1, r2), ss);
+    if (!(r_par < c.r_par_max && r_trans < c.r_trans_max && r_par >= c.r_par_min)) return -1;
+    const int bp = (int)__dmul_rn(__ddiv_rn(__dsub_rn(r_par, c.r_par_min), c.range), (double)c.np);
+    const int bt = (int)__dmul_rn(__ddiv_rn(r_trans, c.r_trans_max), (double)c.nt);
+    return bt + c.nt * bp;
+}
+
+__global__ void __launch_bounds__(kWkBlock)
+    xwick_kernel(XWickConst c, pg_forest_set forests, pg_forest_set objs, const double *zw1,
+                 const double *zw_obj, const int64_t *xo, const double *xa,
+                 const int32_t *item_forest, const int32_t *item_start,
+                 const int32_t *item_count, const int32_t *obj_index, const double *obj_angle,
+                 int64_t num_items, char *work, int64_t cta_bytes, pg_wick_sums out,
+                 Scratch *scratch) {
+    extern __shared__ double wk_smem[];
+    __shared__ int s_item;
+    const int nb = c.nb, tid = threadIdx.x, lane = tid & 31;
+    WickSmem m = wick_smem(wk_smem, nb);
+    char *base = work + (int64_t)blockIdx.x * cta_bytes;
+    double *zql = reinterpret_cast<double *>(base);                  // [cap]
+    double *q_cos = zql + c.cap, *q_sin = q_cos + c.max_quasars;       // [max_quasars]
+    double *q_r = q_sin + c.max_quasars, *q_w = q_r + c.max_quasars, *q_zw = q_w + c.max_quasars;
+    uint32_t *list = reinterpret_cast<uint32_t *>(q_zw + c.max_quasars);  // [cap]
+    for (;;) {
+        if (tid == 0) s_item = atomicAdd(&scratch->work_counter, 1);
+        for (int k = tid; k < nb; k += kWkBlock) {
+            m.count[k] = 0;
+            m.npairs[k] = 0;
+            m.wall[k] = 0.;
+            m.t1[k] = 0.;
+        }
+        __syncthreads();
+        const int64_t q = s_item;
+        if (q >= num_items) break;
+        const int f = item_forest[q];
+        const int32_t q0 = item_start[q], nq = item_count[q];
+        const int64_t o1 = forests.pix_offset[f];
+        const int n1 = (int)(forests.pix_offset[f + 1] - o1);
+        const int64_t grid = (int64_t)n1 * nq;
+        if (nq > c.max_quasars || grid > c.cap) {
+            if (tid == 0) report_error(scratch, PG_ERR_INVALID_ARGUMENT, (int32_t)q);
+            __syncthreads();
+            continue;
+        }
+        if (tid == 0) atomicAdd(&scratch->work_items, 1ull);
+        for (int k = tid; k < nq; k += kWkBlock) {
+            const int g = obj_index[q0 + k];
+            const double ang =
+                obj_angle ? obj_angle[q0 + k]
+                          : angle_between(forests.x_cart[f], forests.y_cart[f], forests.z_cart[f],
+                                          forests.ra[f], forests.dec[f], forests.cos_dec[f],
+                                          objs.x_cart[g], objs.y_cart[g], objs.z_cart[g],
+                                          objs.ra[g], objs.dec[g]);
+            q_cos[k] = cos(ang / 2);
+            q_sin[k] = sin(ang / 2);
+            q_r[k] = objs.obj_r_comov[g];
+            q_w[k] = objs.obj_weight[g];
+            q_zw[k] = zw_obj[g];
+        }
+        __syncthreads();
+        // pass 1: counts, WALL, NB and T1 = w12^2 / w1 zw1 per bin
+        for (int64_t t = tid; t < grid; t += kWkBlock) {
+            const int j = (int)(t / n1), i = (int)(t - (int64_t)j * n1);
+            const int b = xwick_bin(c, forests.r_comov[o1 + i], q_r[j], q_cos[j], q_sin[j]);
+            if (b < 0) continue;
+            const double w1 = forests.weights[o1 + i];
+            const double w12 = __dmul_rn(w1, q_w[j]);
+            atomicAdd(&m.count[b], 1);
+            atomicAdd(&m.npairs[b], 1);
+            atomicAdd(&m.wall[b], w12);
+            atomicAdd(&m.t1[b], __dmul_rn(__ddiv_rn(__dmul_rn(w12, w12), w1), zw1[o1 + i]));
+        }
+        __syncthreads();
+        if (tid == 0) {
+            int run = 0, nz = 0, tasks = 0;
+            for (int b = 0; b < nb; ++b) {
+                const int n = m.count[b];
+                m.start[b] = run;
+                m.count[b] = run;
+                if (n) {
+                    m.nonempty[nz] = b;
+                    m.task_start[nz] = tasks;
+                    tasks += (n + 31) >> 5;
+                    ++nz;
+                }
+                run += n;
+            }
+            m.start[nb] = run;
+            m.task_start[nz] = tasks;
+            m.scalars[0] = nz;
+            m.scalars[1] = tasks;
+            m.scalars[2] = 0;
+        }
+        __syncthreads();
+        const int nz = m.scalars[0], num_tasks = m.scalars[1];
+        for (int64_t t = tid; t < grid; t += kWkBlock) {
+            const int j = (int)(t / n1), i = (int)(t - (int64_t)j * n1);
+            const int b = xwick_bin(c, forests.r_comov[o1 + i], q_r[j], q_cos[j], q_sin[j]);
+            if (b < 0) continue;
+            const int pos = atomicAdd(&m.count[b], 1);
+            list[pos] = (uint32_t)i | ((uint32_t)j << 16);
+            zql[pos] = q_zw[j];
+        }
+        for (int k = tid; k < nz; k += kWkBlock) {
+            const int b = m.nonempty[k];
+            atomicAdd(&out.weights_wick[b], m.wall[b]);
+            atomicAdd(reinterpret_cast<unsigned long long *>(&out.num_pairs_wick[b]),
+                      (unsigned long long)m.npairs[b]);
+            atomicAdd(&out.t1[(int64_t)b * nb + b], m.t1[b]);
+        }
+        __syncthreads();
+        const int num_listed = m.start[nb];
+        const double *x1 = xa + xo[f];
+        for (;;) {
+            int task = 0;
+            if (lane == 0) task = atomicAdd(&m.scalars[2], 1);
+            task = __shfl_sync(0xffffffffu, task, 0);
+            if (task >= num_tasks) break;
+            int lo = 0, hi = nz - 1;
+            while (lo < hi) {
+                const int mid = (lo + hi + 1) >> 1;
+                if (m.task_start[mid] <= task)
+                    lo = mid;
+                else
+                    hi = mid - 1;
+            }
+            const int bin_p = m.nonempty[lo];
+            const int a = m.start[bin_p] + ((task - m.task_start[lo]) << 5) + lane;
+            const bool valid = a < m.start[bin_p + 1];
+            const uint32_t ua = valid ? list[a] : 0u;
+            const int ia = (int)(ua & 0xffffu), ja = (int)(ua >> 16);
+            const double w1a = forests.weights[o1 + ia];
+            const double zwa = valid ? q_zw[ja] : 0.;
+            // T3 scale: w12_a / w1 zw1 (xcf.py:1335-1341)
+            const double c3a =
+                valid ? __dmul_rn(__ddiv_rn(__dmul_rn(w1a, q_w[ja]), w1a), zw1[o1 + ia]) : 0.;
+            double acc_all = 0., acc2 = 0., acc3 = 0.;
+            int kq = 0;
+            int end = m.start[m.nonempty[0] + 1];
+            for (int b = 0; b < num_listed; ++b) {
+                const uint32_t ub = list[b];
+                const int ib = (int)(ub & 0xffffu), jb = (int)(ub >> 16);
+                const double v1 = x1[(int64_t)ib * n1 + ia];
+                const double zb = zql[b];
+                acc_all = fma(v1, zb, acc_all);
+                if (ja == jb) acc2 = fma(v1, zb, acc2);
+                if (ia == ib && ja != jb) acc3 += __dmul_rn(forests.weights[o1 + ib], q_w[jb]);
+                if (b + 1 == end) {
+                    const double r2 = warp_sum(valid ? zwa * acc2 : 0.);
+                    const double r4 = warp_sum(valid ? zwa * (acc_all - acc2) : 0.);
+                    const double r3 = warp_sum(valid ? c3a * acc3 : 0.);
+                    if (lane == 0) {
+                        const int64_t cell = (int64_t)bin_p * nb + m.nonempty[kq];
+                        if (r2 != 0.) atomicAdd(&out.t2[cell], r2);
+                        if (r3 != 0.) atomicAdd(&out.t3[cell], r3);
+                        if (r4 != 0.) atomicAdd(&out.t4[cell], r4);
+                    }
+                    acc_all = acc2 = acc3 = 0.;
+                    if (++kq < nz) end = m.start[m.nonempty[kq] + 1];
+                }
+            }
+        }
+        __syncthreads();
+    }
+}
+
 }  // namespace
 
 int wick_xmat_smem(int num_values) { return (int)(sizeof(double) * std::max(1, num_values - 1)); }
@@ -319,6 +503,54 @@ int launch_wick_t123(const pg_corr_params &p, const pg_forest_set &s1, const pg_
     wick_t123_kernel<<<(int)blocks, kWkBlock, smem, stream>>>(
         c, s1, s2, zw1, zw2, xo1, xa1, xo2, xa2, pair_first, pair_second, pair_angle, num_pairs,
         work, out, scratch);
+    return check_cuda(cudaGetLastError());
+}
+
+}  // namespace pg
+
+namespace pg {
+
+int64_t xwick_cta_bytes(int64_t cap, int64_t max_quasars) {
+    const int64_t bytes = cap * (int64_t)sizeof(double) + 5 * max_quasars * (int64_t)sizeof(double) +
+                          cap * (int64_t)sizeof(uint32_t);
+    return (bytes + 255) & ~(int64_t)255;
+}
+
+int xwick_grid(int nb, int num_sms, int *grid) {
+    const size_t smem = wick_t123_smem(nb);
+    cudaError_t err = cudaFuncSetAttribute(
+        xwick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return check_cuda(err);
+    int occ = 0;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, xwick_kernel, kWkBlock, smem);
+    if (err != cudaSuccess || occ < 1) return PG_ERR_CUDA;
+    *grid = num_sms * occ;
+    return PG_OK;
+}
+
+int launch_xwick(const pg_corr_params &p, const pg_forest_set &forests, const pg_forest_set &objs,
+                 const double *zw1, const double *zw_obj, const int64_t *xo, const double *xa,
+                 const int32_t *item_forest, const int32_t *item_start, const int32_t *item_count,
+                 const int32_t *obj_index, const double *obj_angle, int64_t num_items,
+                 char *work, int64_t cap, int64_t max_quasars, int grid,
+                 const pg_wick_sums &out, Scratch *scratch, cudaStream_t stream) {
+    if (num_items == 0) return PG_OK;
+    XWickConst c;
+    c.r_par_min = p.r_par_min;
+    c.r_par_max = p.r_par_max;
+    c.r_trans_max = p.r_trans_max;
+    c.range = p.r_par_max - p.r_par_min;
+    c.np = p.num_bins_r_par;
+    c.nt = p.num_bins_r_trans;
+    c.nb = c.np * c.nt;
+    c.pad = 0;
+    c.cap = cap;
+    c.max_quasars = max_quasars;
+    const size_t smem = wick_t123_smem(c.nb);
+    const int64_t blocks = std::min<int64_t>(grid, num_items);
+    xwick_kernel<<<(int)blocks, kWkBlock, smem, stream>>>(
+        c, forests, objs, zw1, zw_obj, xo, xa, item_forest, item_start, item_count, obj_index,
+        obj_angle, num_items, work, xwick_cta_bytes(cap, max_quasars), out, scratch);
     return check_cuda(cudaGetLastError());
 }
 

@@ -29,9 +29,11 @@ from ._native import check
 _P = ctypes.POINTER
 
 
+SUM_KEYS = ("weights_wick", "num_pairs_wick", "t1", "t2", "t3", "t4")
+
+
 class WickSumsC(ctypes.Structure):
-    _fields_ = [("weights_wick", ctypes.c_void_p), ("num_pairs_wick", ctypes.c_void_p),
-                ("t1", ctypes.c_void_p), ("t2", ctypes.c_void_p), ("t3", ctypes.c_void_p)]
+    _fields_ = [(k, ctypes.c_void_p) for k in SUM_KEYS]
 
 
 def _bind():
@@ -48,6 +50,12 @@ def _bind():
         lib.pg_cf_wick.argtypes = [vp, _P(_native.CorrParams), _P(_native.ForestSetC),
                                    _P(_native.ForestSetC), vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                    i64, vp, ctypes.c_uint64, _P(WickSumsC), vp]
+        lib.pg_xcf_wick_work_bytes.restype = ctypes.c_int
+        lib.pg_xcf_wick_work_bytes.argtypes = lib.pg_cf_wick_work_bytes.argtypes
+        lib.pg_xcf_wick.restype = ctypes.c_int
+        lib.pg_xcf_wick.argtypes = [vp, _P(_native.CorrParams), _P(_native.ForestSetC),
+                                    _P(_native.ForestSetC), vp, vp, vp, vp, vp, vp, vp, vp, vp,
+                                    i64, i32, vp, ctypes.c_uint64, _P(WickSumsC), vp]
         lib._wick_bound = True
     return lib
 
@@ -161,13 +169,17 @@ class WickEngine:
                 t["offsets"].data_ptr(), arena.data_ptr(), self._stream()), "Wick xi matrices")
         return arena, t["offsets"], t
 
-    def alloc_sums(self, nb):
+    def alloc_sums(self, nb, cross=False):
         dvc = self.device
-        return {"weights_wick": torch.zeros(nb, dtype=torch.float64, device=dvc),
-                "num_pairs_wick": torch.zeros(nb, dtype=torch.int64, device=dvc),
-                "t1": torch.zeros(nb * nb, dtype=torch.float64, device=dvc),
-                "t2": torch.zeros(nb * nb, dtype=torch.float64, device=dvc),
-                "t3": torch.zeros(nb * nb, dtype=torch.float64, device=dvc)}
+        out = {"weights_wick": torch.zeros(nb, dtype=torch.float64, device=dvc),
+               "num_pairs_wick": torch.zeros(nb, dtype=torch.int64, device=dvc)}
+        for key in ("t1", "t2", "t3") + (("t4",) if cross else ()):
+            out[key] = torch.zeros(nb * nb, dtype=torch.float64, device=dvc)
+        return out
+
+    @staticmethod
+    def _sums_struct(sums):
+        return WickSumsC(*[sums[k].data_ptr() if k in sums else None for k in SUM_KEYS])
 
     def work_buffer(self, params, max_pixels1, max_pixels2, num_pairs):
         lib = _bind()
@@ -186,8 +198,7 @@ class WickEngine:
         """Launch pg_cf_wick (asynchronous on the current stream)."""
         lib = _bind()
         work = self.work_buffer(params, dev.max_pixels, dev.max_pixels, max(int(num_pairs), 1))
-        out = WickSumsC(*[sums[k].data_ptr() for k in ("weights_wick", "num_pairs_wick", "t1",
-                                                       "t2", "t3")])
+        out = self._sums_struct(sums)
         with torch.cuda.device(self.device):
             check(lib.pg_cf_wick(
                 self.engine.plan.handle, ctypes.byref(params), ctypes.byref(dev.c), None,
@@ -196,6 +207,29 @@ class WickEngine:
                 angles.data_ptr() if angles is not None else None, int(num_pairs),
                 work.data_ptr(), int(work.numel()), ctypes.byref(out), self._stream()),
                 "Wick terms")
+        return sums
+
+    def accumulate_cross(self, params, dev, qdev, zw1, zw_obj, xo, xa, items, sums):
+        """Launch pg_xcf_wick on work items (forest, first neighbour,
+        neighbour count) of the neighbour index (asynchronous)."""
+        lib = _bind()
+        item_forest, item_start, item_count, obj_index, num_items, max_quasars = items
+        nbytes = ctypes.c_uint64()
+        with torch.cuda.device(self.device):
+            check(lib.pg_xcf_wick_work_bytes(self.engine.plan.handle, ctypes.byref(params),
+                                             int(dev.max_pixels), int(max_quasars),
+                                             int(num_items), ctypes.byref(nbytes)),
+                  "cross Wick work size")
+            need = int(nbytes.value)
+            if self._work is None or self._work.numel() < need:
+                self._work = torch.empty(max(need, 16), dtype=torch.uint8, device=self.device)
+            check(lib.pg_xcf_wick(
+                self.engine.plan.handle, ctypes.byref(params), ctypes.byref(dev.c),
+                ctypes.byref(qdev.c), zw1.data_ptr(), zw_obj.data_ptr(), xo.data_ptr(),
+                xa.data_ptr(), item_forest.data_ptr(), item_start.data_ptr(),
+                item_count.data_ptr(), obj_index.data_ptr(), None, int(num_items),
+                int(max_quasars), self._work.data_ptr(), int(self._work.numel()),
+                ctypes.byref(self._sums_struct(sums)), self._stream()), "cross Wick terms")
         return sums
 
     def stats(self):
@@ -225,19 +259,23 @@ def evolution(z, z_ref, alpha):
 
 
 def normalise(raw, npall, npused):
-    """py/picca/bin/picca_wick.py:515-540: every term divided by
-    WALL WALL^T where positive and scaled by NPUSED / NPALL; T4-T6 are 0."""
+    """py/picca/bin/picca_wick.py:515-540 (picca_xwick.py:487-506): every
+    term divided by WALL WALL^T where positive and scaled by NPUSED / NPALL;
+    the terms not computed are 0."""
     nb = raw["weights_wick"].size
     weights = raw["weights_wick"] * raw["weights_wick"][:, None]
     w = weights > 0.0
     out = {"WALL": raw["weights_wick"].copy(), "NB": raw["num_pairs_wick"].copy()}
-    for key in ("t1", "t2", "t3"):
+    for key in ("t1", "t2", "t3", "t4"):
+        if key not in raw:
+            continue
         t = raw[key].reshape(nb, nb).copy()
         t[w] /= weights[w]
         t *= 1.0 * npused / npall
         out[key.upper()] = t
     for key in ("T4", "T5", "T6"):
-        out[key] = np.zeros((nb, nb))
+        if key not in out:
+            out[key] = np.zeros((nb, nb))
     out["CO"] = out["T1"] + out["T2"] + out["T3"] + out["T4"] + out["T5"] + out["T6"]
     out["NPALL"], out["NPUSED"] = int(npall), int(npused)
     return out
@@ -273,6 +311,53 @@ def wick_covariance(fs, params, cf1d, reject, nproc=1, z_ref=2.25, alpha=2.9, al
         stats = engine.stats()
         if stats.status != 0:
             raise _native.NativeError(f"Wick kernel reported status {stats.status}")
+    raw = {k: v.cpu().numpy() for k, v in sums.items()}
+    out = normalise(raw, npall, npused)
+    if return_raw:
+        out["raw"] = raw
+    return out
+
+
+def cross_wick_covariance(fs, qs, params, cf1d, reject, nproc=1, z_ref=2.25, alpha=2.9,
+                          alpha_obj=1.44, engine=None, return_raw=False):
+    """picca_xwick.py (py/picca/bin/picca_xwick.py:447-520, --max-diagram 4,
+    the default) on a forest set and a quasar set: the normalised COV
+    columns (CO, WALL, NB, T1-T6, T5 = T6 = 0) and NPALL / NPUSED. Every
+    neighbouring quasar of a kept forest enters (no per-pair draw)."""
+    engine = engine or WickEngine()
+    pe = engine.engine
+    tables = OneDTables(cf1d)
+    dev = _pairs.DeviceForests(fs, pe.device, compact=False)
+    qdev = _pairs.DeviceForests(qs, pe.device)
+    offsets, index, total = pe.neighbours(params, dev, qdev, xcf=True)
+    keep, npall, npused = selection(fs, nproc, reject)
+    off_h = offsets.cpu().numpy()
+    counts = np.diff(off_h)
+    forests = np.nonzero(keep & (counts > 0))[0]
+    nb = params.num_bins_r_par * params.num_bins_r_trans
+    sums = engine.alloc_sums(nb, cross=True)
+    if forests.size:
+        if total >= 2**31 or counts[forests].max() > 65535:
+            raise _native.NativeError("too many forest-quasar neighbours for the cross Wick "
+                                      "kernel")
+        order = np.argsort(-(np.asarray(dev.npix)[forests] * counts[forests]), kind="stable")
+        forests = forests[order]
+        dvc = pe.device
+        items = (torch.from_numpy(forests.astype(np.int32)).to(dvc),
+                 torch.from_numpy(off_h[forests].astype(np.int32)).to(dvc),
+                 torch.from_numpy(counts[forests].astype(np.int32)).to(dvc),
+                 index, int(forests.size), int(counts[forests].max()))
+        xa, xo, _keep_alive = engine.xi_matrices(dev, tables, forests)
+        z = np.asarray(fs.z, dtype=np.float64)
+        zw1 = torch.from_numpy(np.ascontiguousarray(evolution(z, z_ref, alpha)
+                                                    if z.size else np.zeros(1))).to(dvc)
+        zq = np.asarray(qs.z_qso, dtype=np.float64)
+        zw_obj = torch.from_numpy(np.ascontiguousarray(evolution(zq, z_ref, alpha_obj)
+                                                       if zq.size else np.zeros(1))).to(dvc)
+        engine.accumulate_cross(params, dev, qdev, zw1, zw_obj, xo, xa, items, sums)
+        stats = engine.stats()
+        if stats.status != 0:
+            raise _native.NativeError(f"cross Wick kernel reported status {stats.status}")
     raw = {k: v.cpu().numpy() for k, v in sums.items()}
     out = normalise(raw, npall, npused)
     if return_raw:

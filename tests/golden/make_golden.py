@@ -26,8 +26,9 @@ Run once in a checkout that has the picca sources next to it
   matrices, and ``stack_lya_nodla.npz`` their input (the STACK_DELTAS table
   of ``test_cor/input_from_delta_extraction_lya_nodla/Log/
   delta_attributes.fits.gz``);
-* ``cor_wick.npz`` and ``cf1d.npz``: picca's golden Wick covariance
-  (``test_cor/wick.fits.gz``) and its 1D-correlation input
+* ``cor_wick.npz``, ``cor_xwick.npz`` and ``cf1d.npz``: picca's golden Wick
+  covariances (``test_cor/wick.fits.gz``, ``xwick.fits.gz``) and their
+  1D-correlation input
   (``test_cor/cf1d.fits.gz``);
 * ``xdmat_cases.npz``: inputs and outputs of picca's own
   ``xcf.compute_dmat_forest_pairs_fast`` on forests of the test data and the
@@ -626,21 +627,23 @@ def extra_fast_metal(picca_root):
 
 
 def extra_wick(picca_root):
-    """picca's golden Wick covariance (test_cor/wick.fits.gz, command at
-    py/picca/tests/test_3_cor.py:412-441) and its 1D-correlation input
-    (test_cor/cf1d.fits.gz, HDU 1DCOR)."""
+    """picca's golden Wick covariances (test_cor/wick.fits.gz and
+    xwick.fits.gz, commands at py/picca/tests/test_3_cor.py:412-441 and
+    :759-791) and their 1D-correlation input (test_cor/cf1d.fits.gz, HDU
+    1DCOR)."""
     tests = os.path.join(picca_root, "py", "picca", "tests", "data", "test_cor")
     hdu = fitsio_lite.FITS(os.path.join(tests, "cf1d.fits.gz"))[1]
     header = hdu.read_header()
     out = {c: hdu[c][:] for c in hdu.get_colnames()}
     out["LLMIN"], out["DLL"] = np.asarray(header["LLMIN"]), np.asarray(header["DLL"])
     np.savez_compressed(os.path.join(HERE, "cf1d.npz"), **out)
-    cov = fitsio_lite.FITS(os.path.join(tests, "wick.fits.gz"))["COV"]
-    header = cov.read_header()
-    out = {c: cov[c][:] for c in cov.get_colnames()}
-    for key in ("NPALL", "NPUSED"):
-        out["hdr_" + key] = np.asarray(header[key])
-    np.savez_compressed(os.path.join(HERE, "cor_wick.npz"), **out)
+    for case in ("wick", "xwick"):
+        cov = fitsio_lite.FITS(os.path.join(tests, case + ".fits.gz"))["COV"]
+        header = cov.read_header()
+        out = {c: cov[c][:] for c in cov.get_colnames()}
+        for key in ("NPALL", "NPUSED"):
+            out["hdr_" + key] = np.asarray(header[key])
+        np.savez_compressed(os.path.join(HERE, f"cor_{case}.npz"), **out)
 
 
 def extra_dmat(picca_root):

@@ -116,3 +116,65 @@ def test_synthetic_matches_oracle(cuda, unfold, rp_min, rp_max, np_, nt, reject)
         close(raw_g[key].reshape(nb, nb), raw_w[key])
     for key in ("CO", "T1", "T2", "T3"):
         close(got[key], want[key])
+
+
+def write_cf1d(path):
+    from picca_gb300 import fitsio_lite
+    cf1d = golden("cf1d.npz")
+    fitsio_lite.write_fits(path, [{
+        "columns": [cf1d[k] for k in ("v1d", "wv1d", "nv1d", "c1d", "nc1d", "nb1d")],
+        "names": ["v1d", "wv1d", "nv1d", "c1d", "nc1d", "nb1d"], "extname": "1DCOR",
+        "header": [{"name": "LLMIN", "value": float(cf1d["LLMIN"])},
+                   {"name": "DLL", "value": float(cf1d["DLL"])}]}])
+    return path
+
+
+def test_cli_matches_golden_xwick(cuda, tmp_path):
+    from conftest import write_catalogue
+    from picca_gb300 import fitsio_lite
+    from picca_gb300.bin import picca_xwick
+    base = str(tmp_path)
+    write_delta_dir(os.path.join(base, "Delta_LYA"))
+    write_attributes(os.path.join(base, "attributes.fits.gz"))
+    write_catalogue(os.path.join(base, "cat.fits"))
+    out = os.path.join(base, "xwick.fits.gz")
+    picca_xwick.main(["--in-dir", os.path.join(base, "Delta_LYA") + "/",
+                      "--drq", os.path.join(base, "cat.fits"), "--out", out,
+                      "--cf1d", write_cf1d(os.path.join(base, "cf1d.fits.gz")),
+                      "--rp-min", "-60.0", "--rp-max", "+60.0", "--rt-max", "+60.0",
+                      "--np", "30", "--nt", "15", "--rej", "0.99", "--nproc", "1",
+                      "--z-evol-obj", "1.",
+                      "--in-attributes", os.path.join(base, "attributes.fits.gz")])
+    want = golden("cor_xwick.npz")
+    with fitsio_lite.FITS(out) as h:
+        cov = h["COV"]
+        header = cov.read_header()
+        got = {c: cov[c][:] for c in cov.get_colnames()}
+    assert int(header["NPALL"]) == int(want["hdr_NPALL"])
+    assert int(header["NPUSED"]) == int(want["hdr_NPUSED"])
+    compare_like_reference(got, want, names=tuple(got))
+
+
+@pytest.mark.parametrize("np_,nt,rp,reject", [(30, 15, 60.0, 0.5), (100, 50, 200.0, 0.9)])
+def test_synthetic_cross_matches_oracle(cuda, np_, nt, rp, reject):
+    from picca_gb300 import constants, pairs, synthetic as syn, utils, wick
+    fs = synthetic(60, 17, 200)
+    qs = syn.make_quasars(900, 18, (150.0, 152.0), (0.0, 2.0), z_lo=2.0, z_hi=3.6)
+    cf1d = golden("cf1d.npz")
+    cosmo = constants.Cosmo(Om=0.3147, verbose=False)
+    ang_max = utils.compute_ang_max(cosmo, rp, 2.0, 2.0)
+    p = ow.make_params(-rp, rp, rp, np_, nt, x_correlation=True)
+    want = ow.xpipeline(fs, qs, p, ang_max, cf1d, reject, nproc=2, alpha_obj=1.44,
+                        return_raw=True)
+    params = pairs.make_params(-rp, rp, rp, np_, nt, ang_max, x_correlation=True)
+    got = wick.cross_wick_covariance(fs, qs, params, cf1d, reject, nproc=2, alpha_obj=1.44,
+                                     return_raw=True)
+    assert (got["NPALL"], got["NPUSED"]) == (want["NPALL"], want["NPUSED"])
+    assert want["NB"].sum() > 0
+    assert np.array_equal(got["NB"], want["NB"])
+    nb = np_ * nt
+    close(got["raw"]["weights_wick"], want["raw"]["weights_wick"])
+    for key in ("t1", "t2", "t3", "t4"):
+        close(got["raw"][key].reshape(nb, nb), want["raw"][key])
+    for key in ("CO", "T1", "T2", "T3", "T4"):
+        close(got[key], want[key])

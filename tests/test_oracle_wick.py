@@ -63,3 +63,22 @@ def test_one_d_tables_match_scipy():
     d = np.concatenate([d, tables.xi_bounds, tables.xi_x])
     idx = np.clip(np.searchsorted(tables.xi_bounds, d, side="left"), 0, tables.xi_y.size - 1)
     assert np.array_equal(tables.xi_y[idx], xi(d))
+
+
+def test_oracle_matches_golden_xwick(test_forests, tmp_path):
+    from conftest import write_catalogue
+    fs, _ = test_forests
+    path = os.path.join(tmp_path, "cat.fits")
+    write_catalogue(path)
+    cosmo = constants.Cosmo(Om=0.315, verbose=False)
+    objs, z_min2 = io.read_objects(path, 16, 0, 10, 1.0, 2.25, cosmo)
+    qs = ForestSet.from_objects(objs)
+    z_min = float(np.min(fs.z))
+    ang_max = utils.compute_ang_max(cosmo, 60.0, z_min, z_min2)
+    got = ow.xpipeline(fs, qs, ow.make_params(-60.0, 60.0, 60.0, 30, 15, x_correlation=True),
+                       ang_max, golden("cf1d.npz"), 0.99, nproc=1, alpha_obj=1.0)
+    want = golden("cor_xwick.npz")
+    assert got["NPALL"] == int(want["hdr_NPALL"])
+    assert got["NPUSED"] == int(want["hdr_NPUSED"])
+    compare_like_reference(got, want, names=("CO", "WALL", "NB", "T1", "T2", "T3", "T4", "T5",
+                                             "T6"))
