@@ -72,6 +72,10 @@ def parse():
                    help="run only the distortion-matrix leg on --config (prints its JSON)")
     p.add_argument("--dmat-product", choices=["split_bf16", "fp64"], default="split_bf16",
                    help="arithmetic of the eta products in the distortion-matrix leg")
+    p.add_argument("--wick-reject", type=float, default=0.99995,
+                   help="forest rejection of the Wick covariance legs")
+    p.add_argument("--wick-only", action="store_true",
+                   help="run only the Wick covariance legs (one JSON line)")
     p.add_argument("--continuum-correlation", type=int, default=50_000,
                    help="forests whose plain- and learned-fit deltas are correlated (0 skips)")
     return p.parse_args()
@@ -487,6 +491,196 @@ def metal_leg(args, fs, params, ang_max, engine, mask):
                                                        f"restatement, {cpu_s:.1f} s"}}
 
 
+def synthetic_cf1d():
+    """A picca_cf1d.py table for the Wick legs: 1,000 offsets of 3e-4 in
+    log10(lambda) from 3600 A, unit correlation at zero offset and a small
+    anticorrelation decaying with the offset, variance 0.05-0.15."""
+    k = np.arange(1000)
+    c1d = np.where(k == 0, 1.0, -0.015 * np.exp(-k / 40.0))
+    v1d = 0.1 + 0.05 * np.sin(k / 60.0)
+    ones = np.ones(k.size, dtype=np.int64)
+    return {"LLMIN": float(np.log10(3600.0)), "DLL": 3e-4, "v1d": v1d, "nv1d": ones,
+            "c1d": c1d, "nb1d": ones}
+
+
+def wick_cpu_sample(fs, qs, cparams, pairs_or_items, cf1d, seconds, cross=False):
+    """The oracle's C restatement of compute_wickT123_pairs (auto) or
+    compute_wickT1234_pairs (cross) on a bounded sample of the same work, on
+    every host core (threads: the ctypes call releases the GIL). Returns
+    (work units/s, sample description, threads)."""
+    from concurrent.futures import ThreadPoolExecutor
+
+    from oracle import cpu as ocpu
+    from oracle import wick as ow
+    cores = os.cpu_count() or 1
+    p = ow.make_params(cparams.r_par_min, cparams.r_par_max, cparams.r_trans_max,
+                       cparams.num_bins_r_par, cparams.num_bins_r_trans,
+                       x_correlation=bool(cparams.x_correlation))
+    variance, xi = ow.interpolants(cf1d)
+    po = np.asarray(fs.pix_offset)
+    zw = ((1 + np.asarray(fs.z)) / 3.25) ** 1.9
+
+    def xmat(f):
+        sl = slice(po[f], po[f + 1])
+        return ow.weighted_xi_1d(fs.log_lambda[sl], fs.weights[sl], variance, xi)
+
+    def angle(f, g, other):
+        return ocpu.lib().oracle_angle(fs.x_cart[f], fs.y_cart[f], fs.z_cart[f], fs.ra[f],
+                                       fs.dec[f], fs.cos_dec[f], other.x_cart[g],
+                                       other.y_cart[g], other.z_cart[g], other.ra[g],
+                                       other.dec[g])
+
+    def work(unit):
+        out = ow.new_outputs(p)
+        out["t4"] = np.zeros_like(out["t1"])
+        if cross:
+            f, nbrs = unit
+            sl = slice(po[f], po[f + 1])
+            zq = qs.z_qso[nbrs]
+            ow.xforest(p, fs.r_comov[sl], fs.weights[sl], zw[sl], xmat(f), qs.obj_r_comov[nbrs],
+                       qs.obj_weight[nbrs], ((1 + zq) / 3.25) ** 0.44,
+                       np.array([angle(f, g, qs) for g in nbrs]), out)
+        else:
+            f, g = unit
+            a, b = slice(po[f], po[f + 1]), slice(po[g], po[g + 1])
+            ow.forest_pair(p, fs.r_comov[a], fs.weights[a], zw[a], xmat(f), fs.r_comov[b],
+                           fs.weights[b], zw[b], xmat(g), angle(f, g, fs), out)
+        return int(out["num_pairs_wick"].sum())
+
+    rng = np.random.default_rng(5)
+    units = list(pairs_or_items)
+    order = rng.permutation(len(units))
+    n = 0
+    listed = []
+    t0 = time.perf_counter()
+    with ThreadPoolExecutor(cores) as ex:
+        while time.perf_counter() - t0 < seconds and n < len(order):
+            pick = [units[i] for i in order[n:n + cores]]
+            listed += list(ex.map(work, pick))
+            n += len(pick)
+    elapsed = time.perf_counter() - t0
+    pairs2 = float(np.sum(np.square(np.asarray(listed, dtype=np.float64))))
+    what = "forests with their quasars" if cross else "forest pairs"
+    return (n / elapsed, pairs2 / elapsed,
+            f"{n} {what} of the same selection (random), C restatement, {elapsed:.1f} s",
+            cores)
+
+
+def wick_leg(args, fs, params, ang_max):
+    """Wick covariance (picca_wick.py T1-T3, picca_xwick.py T1-T4) of the
+    bench forests, forests kept with probability 1 - args.wick_reject: the
+    drop-in call timed end to end (host clock), the Wick kernel alone
+    (CUDA events), its FP64 rate against the measured DGEMM peak (one FMA
+    per pair of listed pixel pairs), and the C oracle on the host cores."""
+    import torch
+
+    from picca_gb300 import pairs, synthetic, wick
+    cf1d = synthetic_cf1d()
+    out = {"reject": args.wick_reject, "cf1d": "synthetic (1,000 offsets of 3e-4)"}
+    peak = fp64_peak_tflops()
+    for name in ("auto", "cross"):
+        if name == "cross":
+            num, area, _, _ = CONFIGS[args.config]
+            half = 20.0 if area <= 4000 else 30.0
+            ra_r, dec_r = synthetic.band_for_area(area, half)
+            qs = synthetic.make_quasars(int(1.5 * num), 20261207, ra_r, dec_r)
+            cparams = pairs.make_params(ang_max=ang_max, x_correlation=True,
+                                        **dict(params, r_par_min=-200.0, num_bins_r_par=100))
+        else:
+            qs = None
+            cparams = pairs.make_params(ang_max=ang_max, **params)
+        engine = wick.WickEngine()
+        run = (lambda: wick.cross_wick_covariance(fs, qs, cparams, cf1d, args.wick_reject,
+                                                  engine=engine)) if qs is not None else \
+            (lambda: wick.wick_covariance(fs, cparams, cf1d, args.wick_reject, engine=engine))
+        run()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        res = run()
+        e2e_s = time.perf_counter() - t0
+        # the kernel alone, on the same work
+        pe = engine.engine
+        tables = wick.OneDTables(cf1d)
+        dev = pairs.DeviceForests(fs, pe.device, compact=False)
+        keep, _, _ = wick.selection(fs, 1, args.wick_reject)
+        stream = torch.cuda.current_stream()
+        nb = cparams.num_bins_r_par * cparams.num_bins_r_trans
+        z = np.asarray(fs.z, dtype=np.float64)
+        zw1 = torch.from_numpy(wick.evolution(z, 2.25, 2.9)).to(pe.device)
+        if qs is None:
+            offsets, index, _ = pe.neighbours(cparams, dev)
+            mask = np.repeat(keep, np.diff(offsets.cpu().numpy()))
+            first, second, num = wick.forest_pairs(dev, offsets, index, mask)
+            if num == 0:
+                out[name] = None
+                continue
+            used = np.unique(np.concatenate([first[:num].cpu().numpy(),
+                                             second[:num].cpu().numpy()]))
+            xa, xo, _alive = engine.xi_matrices(dev, tables, used)
+            plan = engine.plan_pairs(dev, first, second, num)
+            launch = lambda sums: engine.launch_pairs(cparams, dev, zw1, zw1, xo, xa, plan,  # noqa
+                                                      sums)
+            units = list(zip(first[:num].cpu().numpy(), second[:num].cpu().numpy()))
+            work_units = num
+        else:
+            qdev = pairs.DeviceForests(qs, pe.device)
+            offsets, index, total = pe.neighbours(cparams, dev, qdev, xcf=True)
+            off_h = offsets.cpu().numpy()
+            counts = np.diff(off_h)
+            forests = np.nonzero(keep & (counts > 0))[0]
+            if forests.size == 0:
+                out[name] = None
+                continue
+            items = (torch.from_numpy(forests.astype(np.int32)).to(pe.device),
+                     torch.from_numpy(off_h[forests].astype(np.int32)).to(pe.device),
+                     torch.from_numpy(counts[forests].astype(np.int32)).to(pe.device),
+                     index, int(forests.size), int(counts[forests].max()))
+            xa, xo, _alive = engine.xi_matrices(dev, tables, forests)
+            zq = torch.from_numpy(wick.evolution(qs.z_qso, 2.25, 1.44)).to(pe.device)
+            plan = engine.plan_items(dev, items)
+            launch = lambda sums: engine.launch_items(cparams, dev, qdev, zw1, zq, xo, xa,  # noqa
+                                                      plan, sums)
+            idx_h = index.cpu().numpy()
+            units = [(int(f), idx_h[off_h[f]:off_h[f + 1]]) for f in forests]
+            work_units = int(forests.size)
+        times = []
+        for _ in range(2):
+            sums = engine.alloc_sums(nb, cross=qs is not None)
+            torch.cuda.synchronize()
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            launch(sums)
+            e1.record(stream)
+            torch.cuda.synchronize()
+            times.append(e0.elapsed_time(e1) / 1e3)
+            stats = engine.stats()
+        kernel_s = times[-1]
+        pairs2 = float(stats.visited_pairs)
+        achieved = 2.0 * pairs2 / kernel_s / 1e12
+        cpu_units, cpu_pairs2, desc, cores = wick_cpu_sample(
+            fs, qs, cparams, units, cf1d, min(args.cpu_seconds, 15.0), cross=qs is not None)
+        unit = "forests/s" if qs is not None else "forest-pairs/s"
+        out[name] = {
+            "metric": ("cross " if qs is not None else "") + "Wick covariance work per second",
+            "value": work_units / kernel_s, "unit": unit,
+            "pairs_of_pixel_pairs_per_s": pairs2 / kernel_s, "kernel_ms": kernel_s * 1e3,
+            "work": {"units": work_units, "pairs_of_pixel_pairs": pairs2,
+                     "bins": f"{cparams.num_bins_r_par} x {cparams.num_bins_r_trans}",
+                     "npused": res["NPUSED"], "npall": res["NPALL"]},
+            "e2e": {"value": work_units / e2e_s, "unit": unit, "seconds": e2e_s},
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": peak,
+                         "unit": "TFLOP/s", "frac": achieved / peak,
+                         "peak_source": "cuBLAS DGEMM 4096^3 measured in this run",
+                         "achieved_counts": "2 flops (one FMA) per pair of listed pixel pairs"},
+            "cpu_baseline": {"value": cpu_units, "unit": unit,
+                             "pairs_of_pixel_pairs_per_s": cpu_pairs2, "cores": cores,
+                             "kind": "port", "sample": desc}}
+        del engine, dev
+        torch.cuda.empty_cache()
+    return out
+
+
 def xdmat_leg(args, fs, params, ang_max, engine):
     """Delta x quasar distortion matrix (picca_xdmat.py defaults: r_par -200
     to 200, 100 x 50 bins, redshift evolution) of the same forests against
@@ -793,6 +987,10 @@ def run_ours(args):
         torch.cuda.synchronize()
 
     fs, params, ang_max = make_workload(args.config)
+    if args.wick_only:
+        if rank == 0:
+            print(json.dumps(wick_leg(args, fs, params, ang_max)), flush=True)
+        return
     if args.dmat_only:
         if rank == 0:
             print(json.dumps(dmat_leg(args, fs, params, ang_max, args.cpu_seconds)), flush=True)
@@ -956,6 +1154,8 @@ def run_ours(args):
     torch.cuda.empty_cache()
     dm = dmat_leg(args, fs, params, ang_max, args.cpu_seconds)
     print("dmat leg: " + json.dumps(dm), file=sys.stderr, flush=True)
+    wk = wick_leg(args, fs, params, ang_max)
+    print("wick leg: " + json.dumps(wk), file=sys.stderr, flush=True)
     cont = continuum_leg(args, args.cpu_seconds)
     cfg2 = config2_leg(args) if args.config2 else None
     print("continuum leg: " + json.dumps(cont), file=sys.stderr, flush=True)
@@ -991,6 +1191,7 @@ def run_ours(args):
                          "kind": "port", "sample": cpu_desc},
         "continuum": cont,
         "dmat": dm,
+        "wick": wk,
     }
     if cfg2 is not None:
         line["config2"] = cfg2

@@ -478,17 +478,21 @@ typedef struct pg_wick_sums {
  * side, x_offsets / arena the matrices of pg_wick_xi_matrices. Uses
  * params->r_par_min / r_par_max / r_trans_max / num_bins_* / x_correlation
  * (the Wick pixel-pair range keeps r_par_min <= r_par < r_par_max,
- * r_trans < r_trans_max). work: pg_cf_wick_work_bytes() bytes of device
+ * r_trans < r_trans_max). A costly pair may be listed several times as
+ * slices: entry q then does slice unit_slice[q] of unit_slices[q] (both
+ * optional: NULL = one slice per entry); every slice of a pair must be
+ * listed exactly once. work: pg_cf_wick_work_bytes() bytes of device
  * scratch (16-byte aligned); fewer bytes run fewer CTAs. Forests must have
- * at most 65535 pixels. */
+ * at most 32767 pixels. */
 int pg_cf_wick_work_bytes(pg_plan *plan, const pg_corr_params *params, int32_t max_pixels1,
                           int32_t max_pixels2, int64_t max_ctas, uint64_t *bytes);
 int pg_cf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *s1,
                const pg_forest_set *s2, const double *zw1, const double *zw2,
                const int64_t *x_offsets1, const double *arena1, const int64_t *x_offsets2,
                const double *arena2, const int32_t *pair_first, const int32_t *pair_second,
-               const double *pair_angle, int64_t num_pairs, void *work, uint64_t work_bytes,
-               const pg_wick_sums *out, void *stream);
+               const double *pair_angle, const int32_t *unit_slice, const int32_t *unit_slices,
+               int64_t num_pairs, void *work, uint64_t work_bytes, const pg_wick_sums *out,
+               void *stream);
 
 /* Terms T1-T4 of the delta x quasar Wick covariance. A work item q is
  * forest item_forest[q] of `forests` with its neighbouring quasars
@@ -499,17 +503,19 @@ int pg_cf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set 
  * ((1 + z_qso) / (1 + z_ref))^(alpha_obj - 1); the objects' weights and
  * comoving distances are objs->obj_weight / obj_r_comov. r_par is signed and
  * a pair is kept when r_par_min <= r_par < r_par_max, r_trans <
- * r_trans_max. work: pg_xcf_wick_work_bytes() bytes (16-byte aligned) for
- * forests of at most max_pixels pixels and items of at most max_quasars
- * quasars (both at most 65535). */
+ * r_trans_max. unit_slice / unit_slices cut costly items into slices as
+ * for pg_cf_wick. work: pg_xcf_wick_work_bytes() bytes (16-byte aligned)
+ * for forests of at most max_pixels pixels (at most 32767) and items of at
+ * most max_quasars quasars (at most 65535). */
 int pg_xcf_wick_work_bytes(pg_plan *plan, const pg_corr_params *params, int32_t max_pixels,
                            int32_t max_quasars, int64_t max_ctas, uint64_t *bytes);
 int pg_xcf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *forests,
                 const pg_forest_set *objs, const double *zw1, const double *zw_obj,
                 const int64_t *x_offsets, const double *arena, const int32_t *item_forest,
                 const int32_t *item_start, const int32_t *item_count, const int32_t *obj_index,
-                const double *obj_angle, int64_t num_items, int32_t max_quasars, void *work,
-                uint64_t work_bytes, const pg_wick_sums *out, void *stream);
+                const double *obj_angle, const int32_t *unit_slice, const int32_t *unit_slices,
+                int64_t num_items, int32_t max_quasars, void *work, uint64_t work_bytes,
+                const pg_wick_sums *out, void *stream);
 
 /* Fast metal distortion matrix (py/picca/bin/picca_fast_metal_dmat.py:30-251,
  * py/picca/bin/picca_fast_metal_xdmat.py:28-215): every pair (i, j) of two

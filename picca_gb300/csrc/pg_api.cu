@@ -553,8 +553,8 @@ static int wick_bins(const pg_corr_params *params, int *nb) {
 
 int pg_cf_wick_work_bytes(pg_plan *plan, const pg_corr_params *params, int32_t max_pixels1,
                           int32_t max_pixels2, int64_t max_ctas, uint64_t *bytes) {
-    if (!plan || !bytes || max_pixels1 < 1 || max_pixels2 < 1 || max_pixels1 > 65535 ||
-        max_pixels2 > 65535)
+    if (!plan || !bytes || max_pixels1 < 1 || max_pixels2 < 1 || max_pixels1 > 32767 ||
+        max_pixels2 > 32767)
         return PG_ERR_INVALID_ARGUMENT;
     int nb = 0, grid = 0;
     int rc = wick_bins(params, &nb);
@@ -570,17 +570,19 @@ int pg_cf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set 
                const pg_forest_set *s2, const double *zw1, const double *zw2,
                const int64_t *x_offsets1, const double *arena1, const int64_t *x_offsets2,
                const double *arena2, const int32_t *pair_first, const int32_t *pair_second,
-               const double *pair_angle, int64_t num_pairs, void *work, uint64_t work_bytes,
-               const pg_wick_sums *out, void *stream) {
+               const double *pair_angle, const int32_t *unit_slice, const int32_t *unit_slices,
+               int64_t num_pairs, void *work, uint64_t work_bytes, const pg_wick_sums *out,
+               void *stream) {
     if (!plan || !s1 || !out) return PG_ERR_INVALID_ARGUMENT;
     int nb = 0, rc = wick_bins(params, &nb);
     if (rc) return rc;
     const pg_forest_set *t = s2 ? s2 : s1;
     if ((rc = validate_set(s1, true, false)) || (rc = validate_set(t, true, false))) return rc;
     if (num_pairs < 0 || num_pairs > INT32_MAX) return PG_ERR_INVALID_ARGUMENT;
-    if (s1->max_pixels < 1 || t->max_pixels < 1 || s1->max_pixels > 65535 ||
-        t->max_pixels > 65535)
+    if (s1->max_pixels < 1 || t->max_pixels < 1 || s1->max_pixels > 32767 ||
+        t->max_pixels > 32767)
         return PG_ERR_INVALID_ARGUMENT;
+    if ((unit_slice == nullptr) != (unit_slices == nullptr)) return PG_ERR_INVALID_ARGUMENT;
     if (!out->weights_wick || !out->num_pairs_wick || !out->t1 || !out->t2 || !out->t3)
         return PG_ERR_INVALID_ARGUMENT;
     if (num_pairs > 0 && (!zw1 || !zw2 || !x_offsets1 || !arena1 || !x_offsets2 || !arena2 ||
@@ -597,14 +599,14 @@ int pg_cf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set 
     plan->last_stream = st;
     if ((rc = reset_scratch(plan, st))) return rc;
     return launch_wick_t123(*params, *s1, *t, zw1, zw2, x_offsets1, arena1, x_offsets2, arena2,
-                            pair_first, pair_second, pair_angle, num_pairs,
+                            pair_first, pair_second, pair_angle, unit_slice, unit_slices, num_pairs,
                             static_cast<uint32_t *>(work), cap, grid, *out, scratch_of(plan), st);
 }
 
 
 int pg_xcf_wick_work_bytes(pg_plan *plan, const pg_corr_params *params, int32_t max_pixels,
                            int32_t max_quasars, int64_t max_ctas, uint64_t *bytes) {
-    if (!plan || !bytes || max_pixels < 1 || max_quasars < 1 || max_pixels > 65535 ||
+    if (!plan || !bytes || max_pixels < 1 || max_quasars < 1 || max_pixels > 32767 ||
         max_quasars > 65535)
         return PG_ERR_INVALID_ARGUMENT;
     int nb = 0, grid = 0;
@@ -622,17 +624,19 @@ int pg_xcf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set
                 const pg_forest_set *objs, const double *zw1, const double *zw_obj,
                 const int64_t *x_offsets, const double *arena, const int32_t *item_forest,
                 const int32_t *item_start, const int32_t *item_count, const int32_t *obj_index,
-                const double *obj_angle, int64_t num_items, int32_t max_quasars, void *work,
-                uint64_t work_bytes, const pg_wick_sums *out, void *stream) {
+                const double *obj_angle, const int32_t *unit_slice, const int32_t *unit_slices,
+                int64_t num_items, int32_t max_quasars, void *work, uint64_t work_bytes,
+                const pg_wick_sums *out, void *stream) {
     if (!plan || !forests || !objs || !out) return PG_ERR_INVALID_ARGUMENT;
     int nb = 0, rc = wick_bins(params, &nb);
     if (rc) return rc;
     if ((rc = validate_set(forests, true, false)) || (rc = validate_set(objs, false, true)))
         return rc;
     if (num_items < 0 || num_items > INT32_MAX) return PG_ERR_INVALID_ARGUMENT;
-    if (forests->max_pixels < 1 || forests->max_pixels > 65535 || max_quasars < 1 ||
+    if (forests->max_pixels < 1 || forests->max_pixels > 32767 || max_quasars < 1 ||
         max_quasars > 65535)
         return PG_ERR_INVALID_ARGUMENT;
+    if ((unit_slice == nullptr) != (unit_slices == nullptr)) return PG_ERR_INVALID_ARGUMENT;
     if (!out->weights_wick || !out->num_pairs_wick || !out->t1 || !out->t2 || !out->t3 ||
         !out->t4)
         return PG_ERR_INVALID_ARGUMENT;
@@ -651,8 +655,8 @@ int pg_xcf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set
     plan->last_stream = st;
     if ((rc = reset_scratch(plan, st))) return rc;
     return launch_xwick(*params, *forests, *objs, zw1, zw_obj, x_offsets, arena, item_forest,
-                        item_start, item_count, obj_index, obj_angle, num_items,
-                        static_cast<char *>(work), cap, max_quasars, grid, *out,
+                        item_start, item_count, obj_index, obj_angle, unit_slice, unit_slices,
+                        num_items, static_cast<char *>(work), cap, max_quasars, grid, *out,
                         scratch_of(plan), st);
 }
 

@@ -259,7 +259,8 @@ int launch_wick_t123(const pg_corr_params &p, const pg_forest_set &s1, const pg_
                      const double *zw1, const double *zw2, const int64_t *xo1,
                      const double *xa1, const int64_t *xo2, const double *xa2,
                      const int32_t *pair_first, const int32_t *pair_second,
-                     const double *pair_angle, int64_t num_pairs, uint32_t *work,
+                     const double *pair_angle, const int32_t *unit_slice,
+                     const int32_t *unit_slices, int64_t num_pairs, uint32_t *work,
                      int64_t cap, int grid, const pg_wick_sums &out, Scratch *scratch,
                      cudaStream_t stream);
 
@@ -268,9 +269,10 @@ int xwick_grid(int nb, int num_sms, int *grid);
 int launch_xwick(const pg_corr_params &p, const pg_forest_set &forests, const pg_forest_set &objs,
                  const double *zw1, const double *zw_obj, const int64_t *xo, const double *xa,
                  const int32_t *item_forest, const int32_t *item_start, const int32_t *item_count,
-                 const int32_t *obj_index, const double *obj_angle, int64_t num_items,
-                 char *work, int64_t cap, int64_t max_quasars, int grid,
-                 const pg_wick_sums &out, Scratch *scratch, cudaStream_t stream);
+                 const int32_t *obj_index, const double *obj_angle, const int32_t *unit_slice,
+                 const int32_t *unit_slices, int64_t num_items, char *work, int64_t cap,
+                 int64_t max_quasars, int grid, const pg_wick_sums &out, Scratch *scratch,
+                 cudaStream_t stream);
 
 int launch_fast_metal(const pg_fast_metal_params &p, const pg_fast_metal_side &a,
                       const pg_fast_metal_side &b, const pg_fast_metal_sums &out,

@@ -42,9 +42,26 @@
 namespace pg {
 namespace {
 
-constexpr int kWkBlock = 256;
-constexpr int kWkWarps = kWkBlock / 32;
+constexpr int kWkBlock = 512;   // auto: two CTAs per SM up to 2,500 bins
+constexpr int kXwBlock = 1024;  // cross: one CTA per SM at 5,000 bins
 constexpr int kXmBlock = 256;
+constexpr int kWkBatch = 4;  // pixel pairs b whose loads are in flight together
+// Listed pixel pair: i in bits 0-14, j in bits 15-30, bit 31 marks the last
+// pair of its bin.
+constexpr uint32_t kWkEnd = 0x80000000u;
+
+__device__ __forceinline__ uint32_t wick_pack(int i, int j, bool last) {
+    return (uint32_t)i | ((uint32_t)j << 15) | (last ? kWkEnd : 0u);
+}
+__device__ __forceinline__ int wick_i(uint32_t u) { return (int)(u & 0x7fffu); }
+__device__ __forceinline__ int wick_j(uint32_t u) { return (int)((u >> 15) & 0xffffu); }
+
+// Next 32-pair task of this CTA (a warp-wide counter in shared memory).
+__device__ __forceinline__ int wick_next_task(int32_t *counter, int lane) {
+    int t = 0;
+    if (lane == 0) t = atomicAdd(counter, 1);
+    return __shfl_sync(0xffffffffu, t, 0);
+}
 
 struct WickConst {
     double r_par_min, r_par_max, r_trans_max, range;
@@ -88,11 +105,16 @@ __global__ void __launch_bounds__(kXmBlock)
     }
 }
 
+// A work unit may be cut into slices run by different CTAs: each CTA lists
+// the unit's pixel pairs itself (the order inside a bin differs from CTA to
+// CTA), so a slice owns whole bins P (every slice-th nonempty bin) and
+// sweeps all b for them.
 struct WickSmem {
     int32_t *count;   // [nb] listed pixel pairs per bin, then the write cursor
     int32_t *start;   // [nb + 1] bin starts in the list
     int32_t *nonempty;  // [nb] bins with pixel pairs, ascending
-    int32_t *task_start;  // [nb + 1] first 32-pair task of each nonempty bin
+    int32_t *own;     // [nb] nonempty bins of this slice
+    int32_t *task_start;  // [nb + 1] first 32-pair task of each owned bin
     int32_t *npairs;  // [nb]
     double *wall, *t1;  // [nb]
     int32_t *scalars;  // num nonempty, num tasks, task counter
@@ -107,7 +129,8 @@ __device__ __forceinline__ WickSmem wick_smem(void *base, int nb) {
     m.count = p;
     m.start = p + nb;
     m.nonempty = m.start + nb + 1;
-    m.task_start = m.nonempty + nb;
+    m.own = m.nonempty + nb;
+    m.task_start = m.own + nb;
     m.npairs = m.task_start + nb + 1;
     m.scalars = m.npairs + nb;
     return m;
@@ -134,11 +157,12 @@ __global__ void __launch_bounds__(kWkBlock)
     wick_t123_kernel(WickConst c, pg_forest_set s1, pg_forest_set s2, const double *zw1,
                      const double *zw2, const int64_t *xo1, const double *xa1,
                      const int64_t *xo2, const double *xa2, const int32_t *pair_first,
-                     const int32_t *pair_second, const double *pair_angle, int64_t num_pairs,
+                     const int32_t *pair_second, const double *pair_angle,
+                     const int32_t *unit_slice, const int32_t *unit_slices, int64_t num_pairs,
                      uint32_t *work, pg_wick_sums out, Scratch *scratch) {
     extern __shared__ double wk_smem[];
     __shared__ int s_item;
-    const int nb = c.nb, tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const int nb = c.nb, tid = threadIdx.x, lane = tid & 31;
     WickSmem m = wick_smem(wk_smem, nb);
     uint32_t *list = work + (int64_t)blockIdx.x * c.cap;
     for (;;) {
@@ -153,6 +177,7 @@ __global__ void __launch_bounds__(kWkBlock)
         const int64_t q = s_item;
         if (q >= num_pairs) break;
         const int f = pair_first[q], g = pair_second[q];
+        const int slice = unit_slice ? unit_slice[q] : 0, slices = unit_slices ? unit_slices[q] : 1;
         const double ang = pair_angle ? pair_angle[q]
                                       : angle_between(s1.x_cart[f], s1.y_cart[f], s1.z_cart[f],
                                                       s1.ra[f], s1.dec[f], s1.cos_dec[f],
@@ -167,7 +192,7 @@ __global__ void __launch_bounds__(kWkBlock)
             __syncthreads();
             continue;
         }
-        if (tid == 0) atomicAdd(&scratch->work_items, 1ull);
+        if (tid == 0 && slice == 0) atomicAdd(&scratch->work_items, 1ull);
         // pass 1: counts, WALL, NB and T1 per bin
         for (int64_t t = tid; t < grid; t += kWkBlock) {
             const int j = (int)(t / n1), i = (int)(t - (int64_t)j * n1);
@@ -181,24 +206,33 @@ __global__ void __launch_bounds__(kWkBlock)
         }
         __syncthreads();
         if (tid == 0) {
-            int run = 0, nz = 0, tasks = 0;
+            int run = 0, nz = 0, owned = 0, tasks = 0;
             for (int b = 0; b < nb; ++b) {
                 const int n = m.count[b];
                 m.start[b] = run;
                 m.count[b] = run;  // write cursor
                 if (n) {
+                    if (nz % slices == slice) {
+                        m.own[owned] = b;
+                        m.task_start[owned] = tasks;
+                        tasks += (n + 31) >> 5;
+                        ++owned;
+                    }
                     m.nonempty[nz] = b;
-                    m.task_start[nz] = tasks;
-                    tasks += (n + 31) >> 5;
                     ++nz;
                 }
                 run += n;
             }
             m.start[nb] = run;
-            m.task_start[nz] = tasks;
+            m.task_start[owned] = tasks;
+            m.scalars[3] = owned;
             m.scalars[0] = nz;
             m.scalars[1] = tasks;
             m.scalars[2] = 0;
+            // (a, b) pairs of listed pixel pairs the sweep evaluates
+            if (slice == 0)
+                atomicAdd(&scratch->visited_pairs,
+                          (unsigned long long)run * (unsigned long long)run);
         }
         __syncthreads();
         const int nz = m.scalars[0], num_tasks = m.scalars[1];
@@ -207,9 +241,10 @@ __global__ void __launch_bounds__(kWkBlock)
             const int j = (int)(t / n1), i = (int)(t - (int64_t)j * n1);
             const int b = wick_bin(c, s1.r_comov[o1 + i], s2.r_comov[o2 + j], cc, ss);
             if (b < 0) continue;
-            list[atomicAdd(&m.count[b], 1)] = (uint32_t)i | ((uint32_t)j << 16);
+            const int pos = atomicAdd(&m.count[b], 1);
+            list[pos] = wick_pack(i, j, pos == m.start[b + 1] - 1);
         }
-        for (int k = tid; k < nz; k += kWkBlock) {
+        for (int k = tid; k < nz && slice == 0; k += kWkBlock) {
             const int b = m.nonempty[k];
             atomicAdd(&out.weights_wick[b], m.wall[b]);
             atomicAdd(reinterpret_cast<unsigned long long *>(&out.num_pairs_wick[b]),
@@ -218,14 +253,13 @@ __global__ void __launch_bounds__(kWkBlock)
         }
         __syncthreads();
         const int num_listed = m.start[nb];
-        const double *x1 = xa1 + xo1[f], *x2 = xa2 + xo2[g];
+        const double *__restrict__ x1 = xa1 + xo1[f];
+        const double *__restrict__ x2 = xa2 + xo2[g];
         for (;;) {
-            int task = 0;
-            if (lane == 0) task = atomicAdd(&m.scalars[2], 1);
-            task = __shfl_sync(0xffffffffu, task, 0);
+            const int task = wick_next_task(&m.scalars[2], lane);
             if (task >= num_tasks) break;
             // the nonempty bin holding this task
-            int lo = 0, hi = nz - 1;
+            int lo = 0, hi = m.scalars[3] - 1;
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
                 if (m.task_start[mid] <= task)
@@ -233,34 +267,50 @@ __global__ void __launch_bounds__(kWkBlock)
                 else
                     hi = mid - 1;
             }
-            const int bin_p = m.nonempty[lo];
+            const int bin_p = m.own[lo];
             const int a = m.start[bin_p] + ((task - m.task_start[lo]) << 5) + lane;
             const bool valid = a < m.start[bin_p + 1];
             const uint32_t ua = valid ? list[a] : 0u;
-            const int ia = (int)(ua & 0xffffu), ja = (int)(ua >> 16);
+            const int ia = wick_i(ua), ja = wick_j(ua);
             const double c1a = valid ? __dmul_rn(s1.weights[o1 + ia], zw1[o1 + ia]) : 0.;
             const double c2a = valid ? __dmul_rn(s2.weights[o2 + ja], zw2[o2 + ja]) : 0.;
             double acc3 = 0., acc2 = 0.;
             int kq = 0;
-            int end = m.start[m.nonempty[0] + 1];
-            for (int b = 0; b < num_listed; ++b) {
-                const uint32_t ub = list[b];
-                const int ib = (int)(ub & 0xffffu), jb = (int)(ub >> 16);
-                const double v1 = x1[(int64_t)ib * n1 + ia];
-                const double v2 = x2[(int64_t)jb * n2 + ja];
-                acc3 = fma(v1, v2, acc3);
-                if (ia == ib) acc2 = fma(v2, c1a, acc2);
-                if (ja == jb) acc2 = fma(v1, c2a, acc2);
-                if (b + 1 == end) {
-                    const double r3 = warp_sum(valid ? acc3 : 0.);
-                    const double r2 = warp_sum(valid ? acc2 : 0.);
-                    if (lane == 0) {
-                        const int64_t cell = (int64_t)bin_p * nb + m.nonempty[kq];
-                        if (r3 != 0.) atomicAdd(&out.t3[cell], r3);
-                        if (r2 != 0.) atomicAdd(&out.t2[cell], r2);
+            for (int b0 = 0; b0 < num_listed; b0 += 32) {
+                const int nbatch = min(32, num_listed - b0);
+                const uint32_t mine = lane < nbatch ? list[b0 + lane] : 0u;
+                for (int k = 0; k < nbatch; k += kWkBatch) {
+                    uint32_t ub[kWkBatch];
+                    double v1[kWkBatch], v2[kWkBatch];
+#pragma unroll
+                    for (int r = 0; r < kWkBatch; ++r) {
+                        ub[r] = __shfl_sync(0xffffffffu, mine, (k + r) & 31);
+                        v1[r] = __ldg(x1 + (int64_t)wick_i(ub[r]) * n1 + ia);
+                        v2[r] = __ldg(x2 + (int64_t)wick_j(ub[r]) * n2 + ja);
                     }
-                    acc3 = acc2 = 0.;
-                    if (++kq < nz) end = m.start[m.nonempty[kq] + 1];
+#pragma unroll
+                    for (int r = 0; r < kWkBatch; ++r) {
+                        if (k + r >= nbatch) break;
+                        acc3 = fma(v1[r], v2[r], acc3);
+                        // shared-pixel T2 terms: rare, so vote first (a predicated
+                        // FP64 FMA still takes the FP64 pipe for the whole warp)
+                        const bool same_i = ia == wick_i(ub[r]), same_j = ja == wick_j(ub[r]);
+                        if (__any_sync(0xffffffffu, same_i || same_j)) {
+                            if (same_i) acc2 = fma(v2[r], c1a, acc2);
+                            if (same_j) acc2 = fma(v1[r], c2a, acc2);
+                        }
+                        if (ub[r] & kWkEnd) {
+                            const double r3 = warp_sum(valid ? acc3 : 0.);
+                            const double r2 = warp_sum(valid ? acc2 : 0.);
+                            if (lane == 0) {
+                                const int64_t cell = (int64_t)bin_p * nb + m.nonempty[kq];
+                                if (r3 != 0.) atomicAdd(&out.t3[cell], r3);
+                                if (r2 != 0.) atomicAdd(&out.t2[cell], r2);
+                            }
+                            acc3 = acc2 = 0.;
+                            ++kq;
+                        }
+                    }
                 }
             }
         }
@@ -285,13 +335,13 @@ __device__ __forceinline__ int xwick_bin(const XWickConst &c, double r1, double 
     return bt + c.nt * bp;
 }
 
-__global__ void __launch_bounds__(kWkBlock)
+__global__ void __launch_bounds__(kXwBlock)
     xwick_kernel(XWickConst c, pg_forest_set forests, pg_forest_set objs, const double *zw1,
                  const double *zw_obj, const int64_t *xo, const double *xa,
                  const int32_t *item_forest, const int32_t *item_start,
                  const int32_t *item_count, const int32_t *obj_index, const double *obj_angle,
-                 int64_t num_items, char *work, int64_t cta_bytes, pg_wick_sums out,
-                 Scratch *scratch) {
+                 const int32_t *unit_slice, const int32_t *unit_slices, int64_t num_items,
+                 char *work, int64_t cta_bytes, pg_wick_sums out, Scratch *scratch) {
     extern __shared__ double wk_smem[];
     __shared__ int s_item;
     const int nb = c.nb, tid = threadIdx.x, lane = tid & 31;
@@ -303,7 +353,7 @@ __global__ void __launch_bounds__(kWkBlock)
     uint32_t *list = reinterpret_cast<uint32_t *>(q_zw + c.max_quasars);  // [cap]
     for (;;) {
         if (tid == 0) s_item = atomicAdd(&scratch->work_counter, 1);
-        for (int k = tid; k < nb; k += kWkBlock) {
+        for (int k = tid; k < nb; k += kXwBlock) {
             m.count[k] = 0;
             m.npairs[k] = 0;
             m.wall[k] = 0.;
@@ -314,6 +364,7 @@ __global__ void __launch_bounds__(kWkBlock)
         if (q >= num_items) break;
         const int f = item_forest[q];
         const int32_t q0 = item_start[q], nq = item_count[q];
+        const int slice = unit_slice ? unit_slice[q] : 0, slices = unit_slices ? unit_slices[q] : 1;
         const int64_t o1 = forests.pix_offset[f];
         const int n1 = (int)(forests.pix_offset[f + 1] - o1);
         const int64_t grid = (int64_t)n1 * nq;
@@ -322,8 +373,8 @@ __global__ void __launch_bounds__(kWkBlock)
             __syncthreads();
             continue;
         }
-        if (tid == 0) atomicAdd(&scratch->work_items, 1ull);
-        for (int k = tid; k < nq; k += kWkBlock) {
+        if (tid == 0 && slice == 0) atomicAdd(&scratch->work_items, 1ull);
+        for (int k = tid; k < nq; k += kXwBlock) {
             const int g = obj_index[q0 + k];
             const double ang =
                 obj_angle ? obj_angle[q0 + k]
@@ -339,7 +390,7 @@ __global__ void __launch_bounds__(kWkBlock)
         }
         __syncthreads();
         // pass 1: counts, WALL, NB and T1 = w12^2 / w1 zw1 per bin
-        for (int64_t t = tid; t < grid; t += kWkBlock) {
+        for (int64_t t = tid; t < grid; t += kXwBlock) {
             const int j = (int)(t / n1), i = (int)(t - (int64_t)j * n1);
             const int b = xwick_bin(c, forests.r_comov[o1 + i], q_r[j], q_cos[j], q_sin[j]);
             if (b < 0) continue;
@@ -352,36 +403,45 @@ __global__ void __launch_bounds__(kWkBlock)
         }
         __syncthreads();
         if (tid == 0) {
-            int run = 0, nz = 0, tasks = 0;
+            int run = 0, nz = 0, owned = 0, tasks = 0;
             for (int b = 0; b < nb; ++b) {
                 const int n = m.count[b];
                 m.start[b] = run;
                 m.count[b] = run;
                 if (n) {
+                    if (nz % slices == slice) {
+                        m.own[owned] = b;
+                        m.task_start[owned] = tasks;
+                        tasks += (n + 31) >> 5;
+                        ++owned;
+                    }
                     m.nonempty[nz] = b;
-                    m.task_start[nz] = tasks;
-                    tasks += (n + 31) >> 5;
                     ++nz;
                 }
                 run += n;
             }
             m.start[nb] = run;
-            m.task_start[nz] = tasks;
+            m.task_start[owned] = tasks;
+            m.scalars[3] = owned;
             m.scalars[0] = nz;
             m.scalars[1] = tasks;
             m.scalars[2] = 0;
+            // (a, b) pairs of listed pixel pairs the sweep evaluates
+            if (slice == 0)
+                atomicAdd(&scratch->visited_pairs,
+                          (unsigned long long)run * (unsigned long long)run);
         }
         __syncthreads();
         const int nz = m.scalars[0], num_tasks = m.scalars[1];
-        for (int64_t t = tid; t < grid; t += kWkBlock) {
+        for (int64_t t = tid; t < grid; t += kXwBlock) {
             const int j = (int)(t / n1), i = (int)(t - (int64_t)j * n1);
             const int b = xwick_bin(c, forests.r_comov[o1 + i], q_r[j], q_cos[j], q_sin[j]);
             if (b < 0) continue;
             const int pos = atomicAdd(&m.count[b], 1);
-            list[pos] = (uint32_t)i | ((uint32_t)j << 16);
+            list[pos] = wick_pack(i, j, pos == m.start[b + 1] - 1);
             zql[pos] = q_zw[j];
         }
-        for (int k = tid; k < nz; k += kWkBlock) {
+        for (int k = tid; k < nz && slice == 0; k += kXwBlock) {
             const int b = m.nonempty[k];
             atomicAdd(&out.weights_wick[b], m.wall[b]);
             atomicAdd(reinterpret_cast<unsigned long long *>(&out.num_pairs_wick[b]),
@@ -390,13 +450,11 @@ __global__ void __launch_bounds__(kWkBlock)
         }
         __syncthreads();
         const int num_listed = m.start[nb];
-        const double *x1 = xa + xo[f];
+        const double *__restrict__ x1 = xa + xo[f];
         for (;;) {
-            int task = 0;
-            if (lane == 0) task = atomicAdd(&m.scalars[2], 1);
-            task = __shfl_sync(0xffffffffu, task, 0);
+            const int task = wick_next_task(&m.scalars[2], lane);
             if (task >= num_tasks) break;
-            int lo = 0, hi = nz - 1;
+            int lo = 0, hi = m.scalars[3] - 1;
             while (lo < hi) {
                 const int mid = (lo + hi + 1) >> 1;
                 if (m.task_start[mid] <= task)
@@ -404,11 +462,11 @@ __global__ void __launch_bounds__(kWkBlock)
                 else
                     hi = mid - 1;
             }
-            const int bin_p = m.nonempty[lo];
+            const int bin_p = m.own[lo];
             const int a = m.start[bin_p] + ((task - m.task_start[lo]) << 5) + lane;
             const bool valid = a < m.start[bin_p + 1];
             const uint32_t ua = valid ? list[a] : 0u;
-            const int ia = (int)(ua & 0xffffu), ja = (int)(ua >> 16);
+            const int ia = wick_i(ua), ja = wick_j(ua);
             const double w1a = forests.weights[o1 + ia];
             const double zwa = valid ? q_zw[ja] : 0.;
             // T3 scale: w12_a / w1 zw1 (xcf.py:1335-1341)
@@ -416,27 +474,43 @@ __global__ void __launch_bounds__(kWkBlock)
                 valid ? __dmul_rn(__ddiv_rn(__dmul_rn(w1a, q_w[ja]), w1a), zw1[o1 + ia]) : 0.;
             double acc_all = 0., acc2 = 0., acc3 = 0.;
             int kq = 0;
-            int end = m.start[m.nonempty[0] + 1];
-            for (int b = 0; b < num_listed; ++b) {
-                const uint32_t ub = list[b];
-                const int ib = (int)(ub & 0xffffu), jb = (int)(ub >> 16);
-                const double v1 = x1[(int64_t)ib * n1 + ia];
-                const double zb = zql[b];
-                acc_all = fma(v1, zb, acc_all);
-                if (ja == jb) acc2 = fma(v1, zb, acc2);
-                if (ia == ib && ja != jb) acc3 += __dmul_rn(forests.weights[o1 + ib], q_w[jb]);
-                if (b + 1 == end) {
-                    const double r2 = warp_sum(valid ? zwa * acc2 : 0.);
-                    const double r4 = warp_sum(valid ? zwa * (acc_all - acc2) : 0.);
-                    const double r3 = warp_sum(valid ? c3a * acc3 : 0.);
-                    if (lane == 0) {
-                        const int64_t cell = (int64_t)bin_p * nb + m.nonempty[kq];
-                        if (r2 != 0.) atomicAdd(&out.t2[cell], r2);
-                        if (r3 != 0.) atomicAdd(&out.t3[cell], r3);
-                        if (r4 != 0.) atomicAdd(&out.t4[cell], r4);
+            for (int b0 = 0; b0 < num_listed; b0 += 32) {
+                const int nbatch = min(32, num_listed - b0);
+                const uint32_t mine = lane < nbatch ? list[b0 + lane] : 0u;
+                const double zmine = lane < nbatch ? zql[b0 + lane] : 0.;
+                for (int k = 0; k < nbatch; k += kWkBatch) {
+                    uint32_t ub[kWkBatch];
+                    double v1[kWkBatch], zb[kWkBatch];
+#pragma unroll
+                    for (int r = 0; r < kWkBatch; ++r) {
+                        ub[r] = __shfl_sync(0xffffffffu, mine, (k + r) & 31);
+                        zb[r] = __shfl_sync(0xffffffffu, zmine, (k + r) & 31);
+                        v1[r] = __ldg(x1 + (int64_t)wick_i(ub[r]) * n1 + ia);
                     }
-                    acc_all = acc2 = acc3 = 0.;
-                    if (++kq < nz) end = m.start[m.nonempty[kq] + 1];
+#pragma unroll
+                    for (int r = 0; r < kWkBatch; ++r) {
+                        if (k + r >= nbatch) break;
+                        const int ib = wick_i(ub[r]), jb = wick_j(ub[r]);
+                        acc_all = fma(v1[r], zb[r], acc_all);
+                        const bool same_j = ja == jb, same_i = ia == ib && !same_j;
+                        if (__any_sync(0xffffffffu, same_i || same_j)) {
+                            if (same_j) acc2 = fma(v1[r], zb[r], acc2);
+                            if (same_i) acc3 += __dmul_rn(forests.weights[o1 + ib], q_w[jb]);
+                        }
+                        if (ub[r] & kWkEnd) {
+                            const double r2 = warp_sum(valid ? zwa * acc2 : 0.);
+                            const double r4 = warp_sum(valid ? zwa * (acc_all - acc2) : 0.);
+                            const double r3 = warp_sum(valid ? c3a * acc3 : 0.);
+                            if (lane == 0) {
+                                const int64_t cell = (int64_t)bin_p * nb + m.nonempty[kq];
+                                if (r2 != 0.) atomicAdd(&out.t2[cell], r2);
+                                if (r3 != 0.) atomicAdd(&out.t3[cell], r3);
+                                if (r4 != 0.) atomicAdd(&out.t4[cell], r4);
+                            }
+                            acc_all = acc2 = acc3 = 0.;
+                            ++kq;
+                        }
+                    }
                 }
             }
         }
@@ -465,7 +539,7 @@ int launch_wick_xmat(const pg_forest_set &s, const double *log_lambda, const dou
 }
 
 size_t wick_t123_smem(int nb) {
-    return (size_t)2 * nb * sizeof(double) + ((size_t)5 * nb + 2 + 3) * sizeof(int32_t);
+    return (size_t)2 * nb * sizeof(double) + ((size_t)6 * nb + 2 + 4) * sizeof(int32_t);
 }
 
 int wick_t123_grid(int nb, int num_sms, int *grid) {
@@ -484,7 +558,8 @@ int launch_wick_t123(const pg_corr_params &p, const pg_forest_set &s1, const pg_
                      const double *zw1, const double *zw2, const int64_t *xo1,
                      const double *xa1, const int64_t *xo2, const double *xa2,
                      const int32_t *pair_first, const int32_t *pair_second,
-                     const double *pair_angle, int64_t num_pairs, uint32_t *work,
+                     const double *pair_angle, const int32_t *unit_slice,
+                     const int32_t *unit_slices, int64_t num_pairs, uint32_t *work,
                      int64_t cap, int grid, const pg_wick_sums &out, Scratch *scratch,
                      cudaStream_t stream) {
     if (num_pairs == 0) return PG_OK;
@@ -501,8 +576,8 @@ int launch_wick_t123(const pg_corr_params &p, const pg_forest_set &s1, const pg_
     const size_t smem = wick_t123_smem(c.nb);
     const int64_t blocks = std::min<int64_t>(grid, num_pairs);
     wick_t123_kernel<<<(int)blocks, kWkBlock, smem, stream>>>(
-        c, s1, s2, zw1, zw2, xo1, xa1, xo2, xa2, pair_first, pair_second, pair_angle, num_pairs,
-        work, out, scratch);
+        c, s1, s2, zw1, zw2, xo1, xa1, xo2, xa2, pair_first, pair_second, pair_angle, unit_slice,
+        unit_slices, num_pairs, work, out, scratch);
     return check_cuda(cudaGetLastError());
 }
 
@@ -522,7 +597,7 @@ int xwick_grid(int nb, int num_sms, int *grid) {
         xwick_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return check_cuda(err);
     int occ = 0;
-    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, xwick_kernel, kWkBlock, smem);
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, xwick_kernel, kXwBlock, smem);
     if (err != cudaSuccess || occ < 1) return PG_ERR_CUDA;
     *grid = num_sms * occ;
     return PG_OK;
@@ -531,9 +606,10 @@ int xwick_grid(int nb, int num_sms, int *grid) {
 int launch_xwick(const pg_corr_params &p, const pg_forest_set &forests, const pg_forest_set &objs,
                  const double *zw1, const double *zw_obj, const int64_t *xo, const double *xa,
                  const int32_t *item_forest, const int32_t *item_start, const int32_t *item_count,
-                 const int32_t *obj_index, const double *obj_angle, int64_t num_items,
-                 char *work, int64_t cap, int64_t max_quasars, int grid,
-                 const pg_wick_sums &out, Scratch *scratch, cudaStream_t stream) {
+                 const int32_t *obj_index, const double *obj_angle, const int32_t *unit_slice,
+                 const int32_t *unit_slices, int64_t num_items, char *work, int64_t cap,
+                 int64_t max_quasars, int grid, const pg_wick_sums &out, Scratch *scratch,
+                 cudaStream_t stream) {
     if (num_items == 0) return PG_OK;
     XWickConst c;
     c.r_par_min = p.r_par_min;
@@ -548,9 +624,10 @@ int launch_xwick(const pg_corr_params &p, const pg_forest_set &forests, const pg
     c.max_quasars = max_quasars;
     const size_t smem = wick_t123_smem(c.nb);
     const int64_t blocks = std::min<int64_t>(grid, num_items);
-    xwick_kernel<<<(int)blocks, kWkBlock, smem, stream>>>(
+    xwick_kernel<<<(int)blocks, kXwBlock, smem, stream>>>(
         c, forests, objs, zw1, zw_obj, xo, xa, item_forest, item_start, item_count, obj_index,
-        obj_angle, num_items, work, xwick_cta_bytes(cap, max_quasars), out, scratch);
+        obj_angle, unit_slice, unit_slices, num_items, work, xwick_cta_bytes(cap, max_quasars),
+        out, scratch);
     return check_cuda(cudaGetLastError());
 }
 

@@ -49,13 +49,13 @@ def _bind():
         lib.pg_cf_wick.restype = ctypes.c_int
         lib.pg_cf_wick.argtypes = [vp, _P(_native.CorrParams), _P(_native.ForestSetC),
                                    _P(_native.ForestSetC), vp, vp, vp, vp, vp, vp, vp, vp, vp,
-                                   i64, vp, ctypes.c_uint64, _P(WickSumsC), vp]
+                                   vp, vp, i64, vp, ctypes.c_uint64, _P(WickSumsC), vp]
         lib.pg_xcf_wick_work_bytes.restype = ctypes.c_int
         lib.pg_xcf_wick_work_bytes.argtypes = lib.pg_cf_wick_work_bytes.argtypes
         lib.pg_xcf_wick.restype = ctypes.c_int
         lib.pg_xcf_wick.argtypes = [vp, _P(_native.CorrParams), _P(_native.ForestSetC),
                                     _P(_native.ForestSetC), vp, vp, vp, vp, vp, vp, vp, vp, vp,
-                                    i64, i32, vp, ctypes.c_uint64, _P(WickSumsC), vp]
+                                    vp, vp, i64, i32, vp, ctypes.c_uint64, _P(WickSumsC), vp]
         lib._wick_bound = True
     return lib
 
@@ -193,32 +193,62 @@ class WickEngine:
             self._work = torch.empty(max(need, 16), dtype=torch.uint8, device=self.device)
         return self._work
 
-    def accumulate(self, params, dev, zw1, zw2, xo, xa, first, second, num_pairs, sums,
-                   angles=None):
-        """Launch pg_cf_wick (asynchronous on the current stream)."""
+    def plan_pairs(self, dev, first, second, num_pairs, angles=None):
+        """Work units of pg_cf_wick: the forest pairs, costly ones cut into
+        slices (``slice_units``), as device arrays."""
+        npix = torch.from_numpy(np.asarray(dev.npix, dtype=np.int64)).to(self.device)
+        num_pairs = int(num_pairs)
+        cost = (npix[first[:num_pairs].long()] * npix[second[:num_pairs].long()]).cpu().numpy()
+        unit, sl, sls = slice_units(cost)
+        u = torch.from_numpy(unit).to(self.device)
+        return {"first": first[u].contiguous(), "second": second[u].contiguous(),
+                "angles": angles[u].contiguous() if angles is not None else None,
+                "slice": torch.from_numpy(sl).to(self.device),
+                "slices": torch.from_numpy(sls).to(self.device), "num": int(unit.size)}
+
+    def launch_pairs(self, params, dev, zw1, zw2, xo, xa, units, sums):
+        """Launch pg_cf_wick on planned units (asynchronous, current stream)."""
         lib = _bind()
-        work = self.work_buffer(params, dev.max_pixels, dev.max_pixels, max(int(num_pairs), 1))
-        out = self._sums_struct(sums)
+        work = self.work_buffer(params, dev.max_pixels, dev.max_pixels, max(units["num"], 1))
+        angles = units["angles"]
         with torch.cuda.device(self.device):
             check(lib.pg_cf_wick(
                 self.engine.plan.handle, ctypes.byref(params), ctypes.byref(dev.c), None,
                 zw1.data_ptr(), zw2.data_ptr(), xo.data_ptr(), xa.data_ptr(), xo.data_ptr(),
-                xa.data_ptr(), first.data_ptr(), second.data_ptr(),
-                angles.data_ptr() if angles is not None else None, int(num_pairs),
-                work.data_ptr(), int(work.numel()), ctypes.byref(out), self._stream()),
-                "Wick terms")
+                xa.data_ptr(), units["first"].data_ptr(), units["second"].data_ptr(),
+                angles.data_ptr() if angles is not None else None, units["slice"].data_ptr(),
+                units["slices"].data_ptr(), units["num"], work.data_ptr(), int(work.numel()),
+                ctypes.byref(self._sums_struct(sums)), self._stream()), "Wick terms")
         return sums
 
-    def accumulate_cross(self, params, dev, qdev, zw1, zw_obj, xo, xa, items, sums):
-        """Launch pg_xcf_wick on work items (forest, first neighbour,
-        neighbour count) of the neighbour index (asynchronous)."""
-        lib = _bind()
+    def accumulate(self, params, dev, zw1, zw2, xo, xa, first, second, num_pairs, sums,
+                   angles=None):
+        """Plan and launch pg_cf_wick for the forest pairs."""
+        units = self.plan_pairs(dev, first, second, num_pairs, angles)
+        return self.launch_pairs(params, dev, zw1, zw2, xo, xa, units, sums)
+
+    def plan_items(self, dev, items):
+        """Work units of pg_xcf_wick (forest, first neighbour, neighbour
+        count), costly items cut into slices, as device arrays."""
         item_forest, item_start, item_count, obj_index, num_items, max_quasars = items
+        npix = torch.from_numpy(np.asarray(dev.npix, dtype=np.int64)).to(self.device)
+        cost = (npix[item_forest[:num_items].long()] * item_count[:num_items].long()).cpu().numpy()
+        unit, sl, sls = slice_units(cost)
+        u = torch.from_numpy(unit).to(self.device)
+        return {"forest": item_forest[u].contiguous(), "start": item_start[u].contiguous(),
+                "count": item_count[u].contiguous(), "index": obj_index,
+                "slice": torch.from_numpy(sl).to(self.device),
+                "slices": torch.from_numpy(sls).to(self.device), "num": int(unit.size),
+                "max_quasars": int(max_quasars)}
+
+    def launch_items(self, params, dev, qdev, zw1, zw_obj, xo, xa, units, sums):
+        """Launch pg_xcf_wick on planned units (asynchronous, current stream)."""
+        lib = _bind()
         nbytes = ctypes.c_uint64()
         with torch.cuda.device(self.device):
             check(lib.pg_xcf_wick_work_bytes(self.engine.plan.handle, ctypes.byref(params),
-                                             int(dev.max_pixels), int(max_quasars),
-                                             int(num_items), ctypes.byref(nbytes)),
+                                             int(dev.max_pixels), units["max_quasars"],
+                                             max(units["num"], 1), ctypes.byref(nbytes)),
                   "cross Wick work size")
             need = int(nbytes.value)
             if self._work is None or self._work.numel() < need:
@@ -226,14 +256,41 @@ class WickEngine:
             check(lib.pg_xcf_wick(
                 self.engine.plan.handle, ctypes.byref(params), ctypes.byref(dev.c),
                 ctypes.byref(qdev.c), zw1.data_ptr(), zw_obj.data_ptr(), xo.data_ptr(),
-                xa.data_ptr(), item_forest.data_ptr(), item_start.data_ptr(),
-                item_count.data_ptr(), obj_index.data_ptr(), None, int(num_items),
-                int(max_quasars), self._work.data_ptr(), int(self._work.numel()),
+                xa.data_ptr(), units["forest"].data_ptr(), units["start"].data_ptr(),
+                units["count"].data_ptr(), units["index"].data_ptr(), None,
+                units["slice"].data_ptr(), units["slices"].data_ptr(), units["num"],
+                units["max_quasars"], self._work.data_ptr(), int(self._work.numel()),
                 ctypes.byref(self._sums_struct(sums)), self._stream()), "cross Wick terms")
         return sums
 
+    def accumulate_cross(self, params, dev, qdev, zw1, zw_obj, xo, xa, items, sums):
+        """Plan and launch pg_xcf_wick for work items (forest, first
+        neighbour, neighbour count) of the neighbour index."""
+        units = self.plan_items(dev, items)
+        return self.launch_items(params, dev, qdev, zw1, zw_obj, xo, xa, units, sums)
+
     def stats(self):
         return self.engine.stats()
+
+
+#: pairs of listed pixel pairs per slice the host aims at when it cuts a
+#: costly work unit (the sweep of one unit is one CTA's)
+SLICE_TARGET = 2.0e9
+MAX_SLICES = 128
+
+
+def slice_units(cost):
+    """Cut work units into slices by their bound on the sweep, (pixel pairs
+    of the unit)^2: returns (unit index, slice, slices) per entry, costliest
+    slices first."""
+    cost = np.asarray(cost, dtype=np.float64)
+    slices = np.clip(np.ceil(cost * cost / SLICE_TARGET), 1, MAX_SLICES).astype(np.int64)
+    unit = np.repeat(np.arange(cost.size, dtype=np.int64), slices)
+    start = np.concatenate([[0], np.cumsum(slices)[:-1]]) if cost.size else np.zeros(0, np.int64)
+    sl = np.arange(unit.size, dtype=np.int64) - np.repeat(start, slices)
+    per = (cost * cost / slices)[unit]
+    order = np.argsort(-per, kind="stable")
+    return (unit[order], sl[order].astype(np.int32), slices[unit][order].astype(np.int32))
 
 
 def forest_pairs(dev, offsets, index, mask):

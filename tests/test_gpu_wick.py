@@ -91,13 +91,17 @@ def test_xi_matrices_bitwise(cuda):
         assert np.array_equal(got, want)
 
 
-@pytest.mark.parametrize("unfold,rp_min,rp_max,np_,nt,reject", [
-    (False, 0.0, 60.0, 15, 15, 0.6),
-    (True, -60.0, 60.0, 30, 15, 0.6),
-    (False, 0.0, 200.0, 50, 50, 0.9),
+@pytest.mark.parametrize("unfold,rp_min,rp_max,np_,nt,reject,target", [
+    (False, 0.0, 60.0, 15, 15, 0.6, None),
+    (True, -60.0, 60.0, 30, 15, 0.6, None),
+    (False, 0.0, 200.0, 50, 50, 0.9, None),
+    (False, 0.0, 200.0, 50, 50, 0.9, 1e5),  # every pair cut into many slices
 ])
-def test_synthetic_matches_oracle(cuda, unfold, rp_min, rp_max, np_, nt, reject):
+def test_synthetic_matches_oracle(cuda, monkeypatch, unfold, rp_min, rp_max, np_, nt, reject,
+                                  target):
     from picca_gb300 import constants, pairs, utils, wick
+    if target is not None:
+        monkeypatch.setattr(wick, "SLICE_TARGET", target)
     fs = synthetic(70, 13, 220)
     cf1d = golden("cf1d.npz")
     cosmo = constants.Cosmo(Om=0.3147, verbose=False)
@@ -155,9 +159,13 @@ def test_cli_matches_golden_xwick(cuda, tmp_path):
     compare_like_reference(got, want, names=tuple(got))
 
 
-@pytest.mark.parametrize("np_,nt,rp,reject", [(30, 15, 60.0, 0.5), (100, 50, 200.0, 0.9)])
-def test_synthetic_cross_matches_oracle(cuda, np_, nt, rp, reject):
+@pytest.mark.parametrize("np_,nt,rp,reject,target", [(30, 15, 60.0, 0.5, None),
+                                                     (100, 50, 200.0, 0.9, None),
+                                                     (100, 50, 200.0, 0.9, 1e5)])
+def test_synthetic_cross_matches_oracle(cuda, monkeypatch, np_, nt, rp, reject, target):
     from picca_gb300 import constants, pairs, synthetic as syn, utils, wick
+    if target is not None:
+        monkeypatch.setattr(wick, "SLICE_TARGET", target)
     fs = synthetic(60, 17, 200)
     qs = syn.make_quasars(900, 18, (150.0, 152.0), (0.0, 2.0), z_lo=2.0, z_hi=3.6)
     cf1d = golden("cf1d.npz")
