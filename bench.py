@@ -581,9 +581,12 @@ def wick_leg(args, fs, params, ang_max):
     for name in ("auto", "cross"):
         if name == "cross":
             num, area, _, _ = CONFIGS[args.config]
-            half = 20.0 if area <= 4000 else 30.0
-            ra_r, dec_r = synthetic.band_for_area(area, half)
-            qs = synthetic.make_quasars(int(1.5 * num), 20261207, ra_r, dec_r)
+            if area is None:  # the patch of the CPU-runnable case
+                ra_r = tuple(np.degrees([np.min(fs.ra), np.max(fs.ra)]))
+                dec_r = tuple(np.degrees([np.min(fs.dec), np.max(fs.dec)]))
+            else:
+                ra_r, dec_r = synthetic.band_for_area(area, 20.0 if area <= 4000 else 30.0)
+            qs = synthetic.make_quasars(int(1.5 * fs.num), 20261207, ra_r, dec_r)
             cparams = pairs.make_params(ang_max=ang_max, x_correlation=True,
                                         **dict(params, r_par_min=-200.0, num_bins_r_par=100))
         else:

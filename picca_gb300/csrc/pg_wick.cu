@@ -279,6 +279,20 @@ __global__ void __launch_bounds__(kWkBlock)
             for (int b0 = 0; b0 < num_listed; b0 += 32) {
                 const int nbatch = min(32, num_listed - b0);
                 const uint32_t mine = lane < nbatch ? list[b0 + lane] : 0u;
+                // b of this batch that share a pixel with some lane: their T2
+                // terms are added after the branch-free T3 sweep (a predicated
+                // FP64 FMA would take the FP64 pipe for the whole warp)
+                uint32_t pending = 0u;
+                auto drain = [&]() {
+                    while (pending) {
+                        const int k = __ffs(pending) - 1;
+                        pending &= pending - 1u;
+                        const uint32_t u = __shfl_sync(0xffffffffu, mine, k);
+                        const int ib = wick_i(u), jb = wick_j(u);
+                        if (ia == ib) acc2 = fma(__ldg(x2 + (int64_t)jb * n2 + ja), c1a, acc2);
+                        if (ja == jb) acc2 = fma(__ldg(x1 + (int64_t)ib * n1 + ia), c2a, acc2);
+                    }
+                };
                 for (int k = 0; k < nbatch; k += kWkBatch) {
                     uint32_t ub[kWkBatch];
                     double v1[kWkBatch], v2[kWkBatch];
@@ -292,14 +306,10 @@ __global__ void __launch_bounds__(kWkBlock)
                     for (int r = 0; r < kWkBatch; ++r) {
                         if (k + r >= nbatch) break;
                         acc3 = fma(v1[r], v2[r], acc3);
-                        // shared-pixel T2 terms: rare, so vote first (a predicated
-                        // FP64 FMA still takes the FP64 pipe for the whole warp)
-                        const bool same_i = ia == wick_i(ub[r]), same_j = ja == wick_j(ub[r]);
-                        if (__any_sync(0xffffffffu, same_i || same_j)) {
-                            if (same_i) acc2 = fma(v2[r], c1a, acc2);
-                            if (same_j) acc2 = fma(v1[r], c2a, acc2);
-                        }
+                        const bool shared = ia == wick_i(ub[r]) || ja == wick_j(ub[r]);
+                        if (__any_sync(0xffffffffu, shared)) pending |= 1u << (k + r);
                         if (ub[r] & kWkEnd) {
+                            drain();
                             const double r3 = warp_sum(valid ? acc3 : 0.);
                             const double r2 = warp_sum(valid ? acc2 : 0.);
                             if (lane == 0) {
@@ -312,6 +322,7 @@ __global__ void __launch_bounds__(kWkBlock)
                         }
                     }
                 }
+                drain();
             }
         }
         __syncthreads();
@@ -478,6 +489,22 @@ __global__ void __launch_bounds__(kXwBlock)
                 const int nbatch = min(32, num_listed - b0);
                 const uint32_t mine = lane < nbatch ? list[b0 + lane] : 0u;
                 const double zmine = lane < nbatch ? zql[b0 + lane] : 0.;
+                // b sharing the quasar (T2) or the pixel (T3) with some lane,
+                // added after the branch-free sweep
+                uint32_t pending = 0u;
+                auto drain = [&]() {
+                    while (pending) {
+                        const int k = __ffs(pending) - 1;
+                        pending &= pending - 1u;
+                        const uint32_t u = __shfl_sync(0xffffffffu, mine, k);
+                        const double z = __shfl_sync(0xffffffffu, zmine, k);
+                        const int ib = wick_i(u), jb = wick_j(u);
+                        if (ja == jb)
+                            acc2 = fma(__ldg(x1 + (int64_t)ib * n1 + ia), z, acc2);
+                        else if (ia == ib)
+                            acc3 += __dmul_rn(forests.weights[o1 + ib], q_w[jb]);
+                    }
+                };
                 for (int k = 0; k < nbatch; k += kWkBatch) {
                     uint32_t ub[kWkBatch];
                     double v1[kWkBatch], zb[kWkBatch];
@@ -490,14 +517,11 @@ __global__ void __launch_bounds__(kXwBlock)
 #pragma unroll
                     for (int r = 0; r < kWkBatch; ++r) {
                         if (k + r >= nbatch) break;
-                        const int ib = wick_i(ub[r]), jb = wick_j(ub[r]);
                         acc_all = fma(v1[r], zb[r], acc_all);
-                        const bool same_j = ja == jb, same_i = ia == ib && !same_j;
-                        if (__any_sync(0xffffffffu, same_i || same_j)) {
-                            if (same_j) acc2 = fma(v1[r], zb[r], acc2);
-                            if (same_i) acc3 += __dmul_rn(forests.weights[o1 + ib], q_w[jb]);
-                        }
+                        const bool shared = ja == wick_j(ub[r]) || ia == wick_i(ub[r]);
+                        if (__any_sync(0xffffffffu, shared)) pending |= 1u << (k + r);
                         if (ub[r] & kWkEnd) {
+                            drain();
                             const double r2 = warp_sum(valid ? zwa * acc2 : 0.);
                             const double r4 = warp_sum(valid ? zwa * (acc_all - acc2) : 0.);
                             const double r3 = warp_sum(valid ? c3a * acc3 : 0.);
@@ -512,6 +536,7 @@ __global__ void __launch_bounds__(kXwBlock)
                         }
                     }
                 }
+                drain();
             }
         }
         __syncthreads();
