@@ -491,6 +491,59 @@ def metal_leg(args, fs, params, ang_max, engine, mask):
                                                        f"restatement, {cpu_s:.1f} s"}}
 
 
+def delta_io_leg(fs, num=20_000, per_file=1_000):
+    """Delta-file reading (io.read_deltas: parse, z, distances, weights,
+    projection) of the first ``num`` bench forests written as picca delta
+    files (one BINTABLE per line of sight, gzip, ``per_file`` per file):
+    the native parser and projection against the per-object readers, wall
+    clock, all host threads for the native path."""
+    import shutil
+    import tempfile
+
+    from picca_gb300 import constants, fitsio_lite, io
+    num = min(num, fs.num)
+    base = tempfile.mkdtemp(prefix="deltas_")
+    po = np.asarray(fs.pix_offset)
+    os.makedirs(os.path.join(base, "Delta"))
+    try:
+        for k in range(0, num, per_file):
+            tables = []
+            for f in range(k, min(k + per_file, num)):
+                sl = slice(po[f], po[f + 1])
+                tables.append({
+                    "columns": [fs.log_lambda[sl], fs.delta[sl], fs.weights[sl],
+                                np.ones(po[f + 1] - po[f])],
+                    "names": ["LOGLAM", "DELTA", "WEIGHT", "CONT"], "extname": str(f),
+                    "header": [{"name": "RA", "value": float(fs.ra[f])},
+                               {"name": "DEC", "value": float(fs.dec[f])},
+                               {"name": "Z", "value": float(fs.z_qso[f])},
+                               {"name": "THING_ID", "value": int(f)},
+                               {"name": "PLATE", "value": 1}, {"name": "MJD", "value": 1},
+                               {"name": "FIBERID", "value": f % 1000 + 1}]})
+            fitsio_lite.write_fits(os.path.join(base, "Delta", f"delta-{k // per_file}.fits.gz"),
+                                   tables)
+        attr = os.path.join(base, "attributes.fits.gz")
+        fitsio_lite.write_fits(attr, [{"columns": [np.zeros(1, dtype=np.int64)],
+                                       "names": ["LOS_ID"], "extname": "FIT_METADATA",
+                                       "header": [{"name": "FITORDER", "value": 1}]}])
+        cosmo = constants.Cosmo(Om=0.3147, verbose=False)
+        times = {}
+        for native in (True, False):
+            t0 = time.perf_counter()
+            _, n, _, _ = io.read_deltas(os.path.join(base, "Delta") + "/", 16,
+                                        constants.ABSORBER_IGM["LYA"], 2.9, 2.25, cosmo,
+                                        delta_attributes=attr, native=native)
+            times[native] = time.perf_counter() - t0
+    finally:
+        shutil.rmtree(base, ignore_errors=True)
+    return {"metric": "delta files read per second (parse, z, distances, weights, projection)",
+            "value": n / times[True], "unit": "forests/s", "forests": n,
+            "files": (n + per_file - 1) // per_file, "threads": os.cpu_count(),
+            "cpu_baseline": {"value": n / times[False], "unit": "forests/s", "cores": 1,
+                             "kind": "port", "sample": "the same files through the "
+                             "per-object readers (io.read_deltas(native=False))"}}
+
+
 def synthetic_cf1d():
     """A picca_cf1d.py table for the Wick legs: 1,000 offsets of 3e-4 in
     log10(lambda) from 3600 A, unit correlation at zero offset and a small
@@ -1159,6 +1212,8 @@ def run_ours(args):
     print("dmat leg: " + json.dumps(dm), file=sys.stderr, flush=True)
     wk = wick_leg(args, fs, params, ang_max)
     print("wick leg: " + json.dumps(wk), file=sys.stderr, flush=True)
+    dio = delta_io_leg(fs)
+    print("delta io leg: " + json.dumps(dio), file=sys.stderr, flush=True)
     cont = continuum_leg(args, args.cpu_seconds)
     cfg2 = config2_leg(args) if args.config2 else None
     print("continuum leg: " + json.dumps(cont), file=sys.stderr, flush=True)
@@ -1195,6 +1250,7 @@ def run_ours(args):
         "continuum": cont,
         "dmat": dm,
         "wick": wk,
+        "delta_io": dio,
     }
     if cfg2 is not None:
         line["config2"] = cfg2

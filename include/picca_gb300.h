@@ -33,6 +33,9 @@
  *                          py/picca/cf.py:1328-1495, :1498-1626
  *  - pg_xcf_wick        <- xcf.compute_wick_terms + xcf.compute_wickT1234_pairs
  *                          py/picca/xcf.py:838-1008, :1220-1351
+ *  - pg_read_delta_file <- io.read_delta_file + Delta.from_fitsio / from_image
+ *                          py/picca/io.py:333-380, py/picca/data.py:376-620
+ *  - pg_project_deltas  <- Delta.project            py/picca/data.py:622-655
  *  - pg_fast_metal_dmat <- calc_fast_metal_dmat of
  *                          py/picca/bin/picca_fast_metal_dmat.py:30-251 and
  *                          py/picca/bin/picca_fast_metal_xdmat.py:28-215
@@ -516,6 +519,35 @@ int pg_xcf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set
                 const double *obj_angle, const int32_t *unit_slice, const int32_t *unit_slices,
                 int64_t num_items, int32_t max_quasars, void *work, uint64_t work_bytes,
                 const pg_wick_sums *out, void *stream);
+
+/* Delta files (HOST memory; no device, no plan). pg_read_delta_file parses
+ * one delta file, given its bytes (already gunzipped), in either layout: a
+ * BINTABLE per line of sight (kept when z_min_qso < Z < z_max_qso) or the
+ * image layout with a METADATA table (kept when z_min_qso <= Z <= z_max_qso,
+ * pixels with weight > 0). Two passes: with out->los_id == NULL it only sets
+ * num_los / num_pixels; then, with every array allocated, it fills them.
+ * wave holds LOGLAM, or LAMBDA when wave_is_lambda (the caller takes log10).
+ * DELTA_BLIND is read when the file is blinded. */
+typedef struct pg_delta_arrays {
+    int64_t num_los, num_pixels;   /* out */
+    int32_t format;                /* out: 0 one table per line of sight, 1 image */
+    int32_t wave_is_lambda;        /* out */
+    int64_t *los_id, *plate, *mjd, *fiberid;  /* [num_los] */
+    double *ra, *dec, *z_qso;                 /* [num_los] */
+    int64_t *pix_offset;                      /* [num_los + 1] */
+    double *wave, *delta, *weights, *cont;    /* [num_pixels] */
+} pg_delta_arrays;
+
+int pg_read_delta_file(const uint8_t *bytes, int64_t size, double z_min_qso, double z_max_qso,
+                       pg_delta_arrays *out);
+
+/* Delta.project of every line of sight (host arrays, in place): the
+ * weighted mean of delta and, for order 1, its weighted linear trend in
+ * log_lambda removed, with NumPy's summation order (bit-identical to the
+ * reference). order[f] is 0 or 1; threads host threads. */
+int pg_project_deltas(int64_t num_los, const int64_t *pix_offset, const double *log_lambda,
+                      const double *weights, double *delta, const int32_t *order,
+                      int32_t threads);
 
 /* Fast metal distortion matrix (py/picca/bin/picca_fast_metal_dmat.py:30-251,
  * py/picca/bin/picca_fast_metal_xdmat.py:28-215): every pair (i, j) of two

@@ -1,8 +1,9 @@
 """Build ``libpicca_gb300.so`` (the C-ABI CUDA library) in-tree.
 
 Every translation unit under ``csrc/`` is compiled for sm_103a only, in
-parallel, with ``-fmad=false`` (FP64 expressions keep picca's operation
-order; the FP32 kernels ask for fused multiply-adds explicitly) and linked
+parallel, with ``-fmad=false`` and the host compiler's ``-ffp-contract=off``
+(FP64 expressions keep picca's operation order on the device and in the host
+code; the FP32 kernels ask for fused multiply-adds explicitly) and linked
 with ``-shared``. ``python -m picca_gb300.build_ext`` rebuilds.
 """
 
@@ -17,7 +18,7 @@ BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(HERE, "libpicca_gb300.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "-Xcompiler", "-fPIC",
-              "--expt-relaxed-constexpr"]
+              "-Xcompiler", "-ffp-contract=off", "--expt-relaxed-constexpr"]
 
 
 def _nvcc():
@@ -65,7 +66,8 @@ def build(force=False, verbose=False, ptxas_info=False):
             if err.strip():
                 print(err)
     tmp = LIB + f".tmp{os.getpid()}"
-    cmd = [nvcc, *ARCH, "-shared", "-cudart", "static", "-o", tmp] + [o for o, _ in results]
+    cmd = [nvcc, *ARCH, "-shared", "-cudart", "static", "-o", tmp] + [o for o, _ in results] + [
+        "-lpthread"]
     res = subprocess.run(cmd, capture_output=True, text=True)
     if res.returncode != 0:
         raise RuntimeError(f"link failed:\n{res.stderr}")

@@ -661,6 +661,28 @@ int pg_xcf_wick(pg_plan *plan, const pg_corr_params *params, const pg_forest_set
 }
 
 
+int pg_read_delta_file(const uint8_t *bytes, int64_t size, double z_min_qso, double z_max_qso,
+                       pg_delta_arrays *out) {
+    if (!bytes || size < 0 || !out) return PG_ERR_INVALID_ARGUMENT;
+    if (out->los_id && (!out->plate || !out->mjd || !out->fiberid || !out->ra || !out->dec ||
+                        !out->z_qso || !out->pix_offset || !out->wave || !out->delta ||
+                        !out->weights || !out->cont))
+        return PG_ERR_INVALID_ARGUMENT;
+    return read_delta_file(bytes, size, z_min_qso, z_max_qso, out);
+}
+
+int pg_project_deltas(int64_t num_los, const int64_t *pix_offset, const double *log_lambda,
+                      const double *weights, double *delta, const int32_t *order,
+                      int32_t threads) {
+    if (num_los < 0) return PG_ERR_INVALID_ARGUMENT;
+    if (num_los > 0 && (!pix_offset || !log_lambda || !weights || !delta || !order))
+        return PG_ERR_INVALID_ARGUMENT;
+    for (int64_t f = 0; f < num_los; ++f)
+        if ((order[f] != 0 && order[f] != 1) || pix_offset[f + 1] < pix_offset[f])
+            return PG_ERR_INVALID_ARGUMENT;
+    return project_deltas(num_los, pix_offset, log_lambda, weights, delta, order, threads);
+}
+
 int pg_fast_metal_dmat(pg_plan *plan, const pg_fast_metal_params *params,
                        const pg_fast_metal_side *s1, const pg_fast_metal_side *s2,
                        const pg_fast_metal_sums *out, void *stream) {

@@ -274,6 +274,11 @@ int launch_xwick(const pg_corr_params &p, const pg_forest_set &forests, const pg
                  int64_t max_quasars, int grid, const pg_wick_sums &out, Scratch *scratch,
                  cudaStream_t stream);
 
+int read_delta_file(const uint8_t *buf, int64_t size, double z_min, double z_max,
+                    pg_delta_arrays *out);
+int project_deltas(int64_t num_los, const int64_t *pix_offset, const double *log_lambda,
+                   const double *weights, double *delta, const int32_t *order, int threads);
+
 int launch_fast_metal(const pg_fast_metal_params &p, const pg_fast_metal_side &a,
                       const pg_fast_metal_side &b, const pg_fast_metal_sums &out,
                       Scratch *scratch, int num_sms, cudaStream_t stream);

@@ -1,0 +1,151 @@
+"""Native reading of delta files (``pg_read_delta_file``, ``pg_project_deltas``).
+
+``io.read_deltas`` (py/picca/io.py:383-512) reads every file with fitsio,
+builds one ``Delta`` per line of sight (py/picca/data.py:376-620) and then,
+forest by forest, computes z, the comoving distances, the redshift evolution
+of the weights and the projection. Here each file's bytes go to the C parser
+(files in parallel threads; gunzip and the parser release the GIL), the
+per-pixel quantities are computed once over the concatenated pixel arrays
+(the same elementwise NumPy expressions), the projection runs in the native
+library with NumPy's summation order, and the ``Delta`` objects are views
+into those arrays. The result is bit-identical to the per-object path
+(``tests/test_deltaio.py``).
+"""
+
+import ctypes
+import gzip
+import os
+from concurrent.futures import ThreadPoolExecutor
+
+import numpy as np
+
+from . import _native
+from .data import Delta
+
+_P = ctypes.POINTER
+
+
+class DeltaArraysC(ctypes.Structure):
+    _fields_ = [("num_los", ctypes.c_int64), ("num_pixels", ctypes.c_int64),
+                ("format", ctypes.c_int32), ("wave_is_lambda", ctypes.c_int32)] + [
+        (k, ctypes.c_void_p) for k in ("los_id", "plate", "mjd", "fiberid", "ra", "dec", "z_qso",
+                                       "pix_offset", "wave", "delta", "weights", "cont")]
+
+
+LOS_KEYS = {"los_id": np.int64, "plate": np.int64, "mjd": np.int64, "fiberid": np.int64,
+            "ra": np.float64, "dec": np.float64, "z_qso": np.float64}
+PIX_KEYS = ("wave", "delta", "weights", "cont")
+
+
+def _bind():
+    lib = _native.lib()
+    if not getattr(lib, "_deltaio_bound", False):
+        lib.pg_read_delta_file.restype = ctypes.c_int
+        lib.pg_read_delta_file.argtypes = [ctypes.c_void_p, ctypes.c_int64, ctypes.c_double,
+                                           ctypes.c_double, _P(DeltaArraysC)]
+        lib.pg_project_deltas.restype = ctypes.c_int
+        lib.pg_project_deltas.argtypes = [ctypes.c_int64, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                          ctypes.c_int32]
+        lib._deltaio_bound = True
+    return lib
+
+
+def file_bytes(path):
+    """A delta file's bytes, gunzipped when they carry the gzip magic."""
+    with open(path, "rb") as handle:
+        raw = handle.read()
+    return gzip.decompress(raw) if raw[:2] == b"\x1f\x8b" else raw
+
+
+def read_file(path, z_min_qso=0.0, z_max_qso=10.0):
+    """One delta file as arrays: per line of sight (los_id, plate, mjd,
+    fiberid, ra, dec, z_qso, pix_offset) and per pixel (log_lambda, delta,
+    weights, cont)."""
+    lib = _bind()
+    raw = file_bytes(path)
+    buf = np.frombuffer(raw, dtype=np.uint8)
+    out = DeltaArraysC()
+    _native.check(lib.pg_read_delta_file(buf.ctypes.data, buf.size, float(z_min_qso),
+                                         float(z_max_qso), ctypes.byref(out)),
+                  f"delta file {path}")
+    nlos, npix = int(out.num_los), int(out.num_pixels)
+    arrays = {k: np.zeros(max(nlos, 1), dtype=t) for k, t in LOS_KEYS.items()}
+    arrays["pix_offset"] = np.zeros(nlos + 1, dtype=np.int64)
+    for k in PIX_KEYS:
+        arrays[k] = np.zeros(max(npix, 1), dtype=np.float64)
+    for k, v in arrays.items():
+        setattr(out, k, v.ctypes.data)
+    _native.check(lib.pg_read_delta_file(buf.ctypes.data, buf.size, float(z_min_qso),
+                                         float(z_max_qso), ctypes.byref(out)),
+                  f"delta file {path}")
+    for k in LOS_KEYS:
+        arrays[k] = arrays[k][:nlos]
+    for k in PIX_KEYS:
+        arrays[k] = arrays[k][:npix]
+    arrays["log_lambda"] = np.log10(arrays["wave"]) if out.wave_is_lambda else arrays["wave"]
+    arrays["image"] = bool(out.format)
+    return arrays
+
+
+def project(pix_offset, log_lambda, weights, delta, order, threads=None):
+    """Delta.project of every line of sight, in place (native, NumPy's
+    summation order)."""
+    lib = _bind()
+    num = int(len(pix_offset) - 1)
+    order = np.ascontiguousarray(order, dtype=np.int32)
+    threads = threads or min(32, os.cpu_count() or 1)
+    _native.check(lib.pg_project_deltas(num, pix_offset.ctypes.data, log_lambda.ctypes.data,
+                                        weights.ctypes.data, delta.ctypes.data, order.ctypes.data,
+                                        int(threads)), "delta projection")
+
+
+def read_files(files, z_min_qso=0.0, z_max_qso=10.0, max_num_spec=None, threads=None):
+    """The files' arrays concatenated in file order (reading stops after the
+    file that passes max_num_spec lines of sight, as io.read_deltas does)."""
+    threads = threads or min(16, os.cpu_count() or 1)
+    parts = []
+    num = 0
+    with ThreadPoolExecutor(threads) as pool:
+        step = max(threads, 1)
+        for i in range(0, len(files), step):
+            for part in pool.map(lambda f: read_file(f, z_min_qso, z_max_qso),
+                                 files[i:i + step]):
+                parts.append(part)
+                num += len(part["ra"])
+                if max_num_spec is not None and num > max_num_spec:
+                    break
+            if max_num_spec is not None and num > max_num_spec:
+                break
+    out = {}
+    for k in list(LOS_KEYS) + ["log_lambda", "delta", "weights", "cont"]:
+        out[k] = (np.concatenate([p[k] for p in parts]) if parts
+                  else np.zeros(0, dtype=LOS_KEYS.get(k, np.float64)))
+    counts = np.concatenate([np.diff(p["pix_offset"]) for p in parts]) if parts else \
+        np.zeros(0, dtype=np.int64)
+    if max_num_spec is not None and len(counts) > max_num_spec:
+        counts = counts[:max_num_spec]
+        for k in LOS_KEYS:
+            out[k] = out[k][:max_num_spec]
+        npix = int(counts.sum())
+        for k in ("log_lambda", "delta", "weights", "cont"):
+            out[k] = out[k][:npix]
+    out["pix_offset"] = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    return out
+
+
+def make_deltas(arrays, order):
+    """Delta objects whose pixel arrays are views into ``arrays``."""
+    po = arrays["pix_offset"]
+    deltas = []
+    for f in range(len(po) - 1):
+        sl = slice(po[f], po[f + 1])
+        d = Delta(int(arrays["los_id"][f]), float(arrays["ra"][f]), float(arrays["dec"][f]),
+                  float(arrays["z_qso"][f]), int(arrays["plate"][f]), int(arrays["mjd"][f]),
+                  int(arrays["fiberid"][f]), arrays["log_lambda"][sl], arrays["weights"][sl],
+                  arrays["cont"][sl], arrays["delta"][sl], order)
+        for key in ("z", "r_comov", "dist_m"):
+            if key in arrays:
+                setattr(d, key, arrays[key][sl])
+        deltas.append(d)
+    return deltas

@@ -90,15 +90,20 @@ def read_delta_file(filename, z_min_qso=0, z_max_qso=10, rebin_factor=None,
 def read_deltas(in_dir, nside, lambda_abs, alpha, z_ref, cosmo,
                 max_num_spec=None, no_project=False, nproc=None,
                 rebin_factor=None, z_min_qso=0, z_max_qso=10,
-                delta_attributes=None):
+                delta_attributes=None, native=True):
     """Read deltas, compute z, r_comov, dist_m, evolve weights and project.
 
     Same contract as py/picca/io.py:383-512: returns (data, num_data, z_min,
-    z_max) with ``data = {healpix: [Delta, ...]}``.
+    z_max) with ``data = {healpix: [Delta, ...]}``. ``native`` (default)
+    parses the files and projects the deltas in the native library
+    (``picca_gb300.deltaio``, bit-identical); rebinning uses the per-object
+    readers below.
     """
-    del nproc
     files = _list_delta_files(in_dir)
     order = find_order(in_dir, delta_attributes)
+    if native and rebin_factor is None:
+        return _read_deltas_native(files, in_dir, nside, lambda_abs, alpha, z_ref, cosmo,
+                                   max_num_spec, no_project, nproc, z_min_qso, z_max_qso, order)
     deltas = []
     num_data = 0
     for filename in files:
@@ -173,6 +178,43 @@ def read_drq(drq_filename, z_min=0, z_max=10., keep_bal=False, bi_max=None,
     out["DEC"] = np.radians(out["DEC"])
     out["_obj_id_name"] = obj_id_name
     return out
+
+
+def _read_deltas_native(files, in_dir, nside, lambda_abs, alpha, z_ref, cosmo, max_num_spec,
+                        no_project, nproc, z_min_qso, z_max_qso, order):
+    """read_deltas through the native parser and projection: the per-pixel
+    expressions of the per-object path, evaluated once over all pixels."""
+    from . import deltaio
+    arrays = deltaio.read_files(files, z_min_qso, z_max_qso, max_num_spec,
+                                threads=nproc if nproc else None)
+    num_data = len(arrays["ra"])
+    ra, dec = arrays["ra"], arrays["dec"]
+    healpixs = ang2pix_ring(nside, np.pi / 2. - dec, ra)
+    if np.size(healpixs) == 0:
+        raise AssertionError(f"ERROR: No data in {in_dir}")
+    log_lambda = arrays["log_lambda"]
+    z = 10**log_lambda / lambda_abs - 1.
+    z_min = 10**log_lambda[0] / lambda_abs - 1.
+    z_max = 0.
+    if z.size:
+        z_min = min(z_min, z.min())
+        z_max = max(z_max, z.max())
+    arrays["z"] = z
+    if cosmo is not None:
+        arrays["r_comov"] = cosmo.get_r_comov(z)
+        arrays["dist_m"] = cosmo.get_dist_m(z)
+    arrays["weights"] *= ((1 + z) / (1 + z_ref))**(alpha - 1)
+    if not no_project:
+        if order is None:
+            raise RuntimeError(
+                "Trying to project but order is not defined for the deltas. "
+                "Check previous warning to solve this issue")
+        deltaio.project(arrays["pix_offset"], log_lambda, arrays["weights"], arrays["delta"],
+                        np.full(num_data, int(order), dtype=np.int32))
+    data = {}
+    for delta, healpix in zip(deltaio.make_deltas(arrays, order), np.atleast_1d(healpixs)):
+        data.setdefault(int(healpix), []).append(delta)
+    return data, num_data, z_min, z_max
 
 
 def read_objects(filename, nside, z_min, z_max, alpha, z_ref, cosmo,
