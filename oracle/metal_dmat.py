@@ -119,10 +119,13 @@ def absorber_pairs(lambda_abs, abs_igm, lambda_abs2=None, abs_igm2=None):
     return out
 
 
-def pipeline(fs, cosmo, p, ang_max, reject, abs_igm, lambda_abs="LYA", nproc=1, fs2=None):
+def pipeline(fs, cosmo, p, ang_max, reject, abs_igm, lambda_abs="LYA", nproc=1, fs2=None,
+             lambda_abs2=None, abs_igm2=None):
     """picca_metal_dmat.py on a ForestSet (auto-correlation, or the cross of
-    two delta fields with ``fs2`` and the same tracer on both sides): per
-    absorber pair the normalised (RP, RT, Z, DM, WDM) and the pair counts."""
+    two delta fields with ``fs2``: the same tracer on both sides, or a
+    second tracer ``lambda_abs2`` with its absorbers ``abs_igm2``, whose
+    distances ``fs2`` already carries): per absorber pair the normalised
+    (RP, RT, Z, DM, WDM) and the pair counts."""
     other = fs if fs2 is None else fs2
     oparams = cpu.make_params(p.r_par_min, p.r_par_max, p.r_trans_max, p.np, p.nt)
     offsets, index = cpu.neighbours(fs, other, oparams, ang_max, auto_mode=int(fs2 is None))
@@ -135,9 +138,12 @@ def pipeline(fs, cosmo, p, ang_max, reject, abs_igm, lambda_abs="LYA", nproc=1, 
                 np.asarray(s.dist_m[sl]), np.asarray(s.weights[sl]), s.z_qso[f])
 
     results = {}
-    for abs1, abs2 in absorber_pairs(lambda_abs, abs_igm):
-        # cf.py:1088-1090 with cf.lambda_abs2 = cf.lambda_abs for two fields
-        swapped = (abs1 != abs2) if not p.x_correlation else fs2 is not None
+    same_tracer = lambda_abs2 is None or lambda_abs2 == lambda_abs
+    for abs1, abs2 in absorber_pairs(lambda_abs, abs_igm, lambda_abs2,
+                                     abs_igm2 if lambda_abs2 is not None else None):
+        # cf.py:1088-1090: the swapped pass for two different absorbers in the
+        # folded auto-correlation, or two fields of the same tracer
+        swapped = (abs1 != abs2) if not p.x_correlation else (fs2 is not None and same_tracer)
         out = new_outputs(p)
         for f in range(fs.num):
             for k in range(int(offsets[f]), int(offsets[f + 1])):

@@ -8,9 +8,9 @@ rejection per process chunk (the generator re-seeded per chunk for every
 absorber pair, so all pairs keep the same forest pairs), normalisation
 (:497-503) and FITS layout (HDU ``ATTRI`` with NPALL / NPUSED / ABS_IGM and
 the header keywords, HDU ``MDMAT`` with RP_ / RT_ / Z_ / DM_ / WDM_ columns per
-absorber pair). The cross of two delta fields (``--in-dir2``) is supported
-with the same tracer on both sides; a different second tracer
-(``--lambda-abs2``) is not.
+absorber pair). A second delta field (``--in-dir2``) and a second tracer
+(``--lambda-abs2``, with its absorbers ``--abs-igm2``) are read as the
+reference does (py/picca/bin/picca_metal_dmat.py:389-421).
 """
 
 import argparse
@@ -145,9 +145,6 @@ def write(path, results, args, blinding):
 def main(cmdargs=None):
     """Compute the metal distortion matrices"""
     args = parse_args(cmdargs)
-    if args.lambda_abs2:
-        raise NotImplementedError("a second tracer (--lambda-abs2) is not supported by this "
-                                  "drop-in")
     if args.nproc is None:
         args.nproc = max(cpu_count() // 2, 1)
     cf.r_par_max, cf.r_par_min, cf.r_trans_max = args.rp_max, args.rp_min, args.rt_max
@@ -160,17 +157,22 @@ def main(cmdargs=None):
     cf.reject = args.rej
     cf.lambda_abs = constants.ABSORBER_IGM[args.lambda_abs]
     cf.remove_same_half_plate_close_pairs = args.remove_same_half_plate_close_pairs
-    # picca sets x_correlation only for two delta fields (py/picca/bin/
-    # picca_metal_dmat.py:386-389)
-    cf.x_correlation = bool(args.in_dir2 and args.unfold_cf)
+    # picca sets x_correlation only for a second field or tracer
+    # (py/picca/bin/picca_metal_dmat.py:389-401)
+    two_fields = bool(args.in_dir2 or args.lambda_abs2)
+    cf.x_correlation = bool(two_fields and (args.lambda_abs2 or args.unfold_cf))
     cf.alpha_abs = {args.lambda_abs: cf.alpha}
     for name in args.abs_igm:
         cf.alpha_abs[name] = args.metal_alpha
-    if args.in_dir2:
+    if two_fields:
         cf.alpha2 = args.z_evol2
-        cf.lambda_abs2 = cf.lambda_abs
-        # picca stores alpha2 under the key None here (--lambda-abs2 unset),
-        # so the tracer keeps alpha (py/picca/bin/picca_metal_dmat.py:398)
+        if args.in_dir2 is None:
+            args.in_dir2 = args.in_dir
+        cf.lambda_abs2 = (constants.ABSORBER_IGM[args.lambda_abs2] if args.lambda_abs2
+                          else cf.lambda_abs)
+        # without --lambda-abs2 picca stores alpha2 under the key None, so the
+        # tracer keeps alpha (py/picca/bin/picca_metal_dmat.py:399)
+        cf.alpha_abs[args.lambda_abs2] = cf.alpha2
         for name in args.abs_igm2:
             cf.alpha_abs[name] = args.metal_alpha
     blinding = io.read_blinding(args.in_dir)
@@ -198,8 +200,10 @@ def main(cmdargs=None):
         cf.num_data2 = num_data2
         cf.ang_max = utils.compute_ang_max(cf.cosmo, cf.r_trans_max, z_min, z_min2)
         fs2 = ForestSet.from_deltas(data2)
-        # without --lambda-abs2 the second list is the first one
-        # (py/picca/bin/picca_metal_dmat.py:449-451)
+    lambda_abs2 = args.lambda_abs2
+    if args.lambda_abs2 is None:
+        # the second list is then the first one (py/picca/bin/picca_metal_dmat.py:449-451)
+        args.lambda_abs2 = args.lambda_abs
         args.abs_igm2 = args.abs_igm
     t1 = time.time()
     fs = ForestSet.from_deltas(data)
@@ -212,12 +216,13 @@ def main(cmdargs=None):
                                            coef_binning_model=args.coef_binning_model)
     only = None
     if args.fast_metals:
-        only = [(a1, a2) for a1, a2 in metal.absorber_pairs(args.lambda_abs, args.abs_igm)
+        only = [(a1, a2) for a1, a2 in metal.absorber_pairs(args.lambda_abs, args.abs_igm,
+                                                            args.lambda_abs2, args.abs_igm2)
                 if (a1 == "LYA" and a2 in DEFAULT_SI_METALS) or (a1 == "CIV(eff)" and a1 == a2)]
     results = metal.metal_distortion_matrices(
         fs, params, dparams, cf.cosmo, cf.reject, args.abs_igm, cf.alpha_abs,
         lambda_abs=args.lambda_abs, z_ref=cf.z_ref, nproc=args.nproc, only=only, fs2=fs2,
-        abs_igm2=args.abs_igm2 if fs2 is not None else None)
+        abs_igm2=args.abs_igm2 if fs2 is not None else None, lambda_abs2=lambda_abs2)
     userprint(f"picca_metal_dmat.py - Time computing all metal matrices : "
               f"{(time.time() - t1) / 60:.3f} minutes")
     write(args.out, results, args, blinding)

@@ -138,12 +138,13 @@ def normalise(raw, params, dparams, npall, npused):
 
 def metal_distortion_matrices(fs, params, dparams, cosmo, reject, abs_igm, alpha_abs,
                               lambda_abs="LYA", z_ref=2.25, nproc=1, engine=None, mask=None,
-                              only=None, fs2=None, abs_igm2=None):
+                              only=None, fs2=None, abs_igm2=None, lambda_abs2=None):
     """picca_metal_dmat.py on a ForestSet (auto-correlation, or the cross
-    with a second field ``fs2`` of the same tracer): for every absorber pair
-    (or the pairs in ``only``), the normalised (RP, RT, Z, DM, WDM) and the
-    pair counts. ``alpha_abs`` maps absorber names to their
-    redshift-evolution exponents."""
+    with a second field ``fs2``: of the same tracer, or of a second tracer
+    ``lambda_abs2`` with its absorbers ``abs_igm2``, fs2's distances being
+    that tracer's): for every absorber pair (or the pairs in ``only``), the
+    normalised (RP, RT, Z, DM, WDM) and the pair counts. ``alpha_abs`` maps
+    absorber names to their redshift-evolution exponents."""
     eng = engine if isinstance(engine, MetalEngine) else MetalEngine(engine)
     pe = eng.engine
     dev = _pairs.DeviceForests(fs, pe.device)
@@ -163,7 +164,9 @@ def metal_distortion_matrices(fs, params, dparams, cosmo, reject, abs_igm, alpha
         return pixels[key]
 
     results = {}
-    pairs_list = absorber_pairs(lambda_abs, abs_igm, lambda_abs if fs2 is not None else None,
+    same_tracer = fs2 is not None and (lambda_abs2 is None or lambda_abs2 == lambda_abs)
+    pairs_list = absorber_pairs(lambda_abs, abs_igm,
+                                (lambda_abs2 or lambda_abs) if fs2 is not None else None,
                                 abs_igm2)
     for abs1, abs2 in pairs_list:
         if only is not None and (abs1, abs2) not in only:
@@ -172,7 +175,7 @@ def metal_distortion_matrices(fs, params, dparams, cosmo, reject, abs_igm, alpha
         den = (1 + z_ref) ** (alpha_abs[abs1] + alpha_abs[abs2] - 2)
         eng.run_pass(params, dparams, den, dev, dev2, side(1, abs1), side(2, abs2), first,
                      second, num, sums)
-        if swapped_pass(abs1, abs2, bool(params.x_correlation), same_tracer=fs2 is not None):
+        if swapped_pass(abs1, abs2, bool(params.x_correlation), same_tracer=same_tracer):
             den2 = (1 + z_ref) ** (alpha_abs[abs2] + alpha_abs[abs1] - 2)
             eng.run_pass(params, dparams, den2, dev, dev2, side(1, abs2), side(2, abs1), first,
                          second, num, sums)

@@ -178,3 +178,49 @@ def test_cli_matches_golden_metal_dmat_cross(cuda, picca_inputs, tmp_path):
             got = {k: mdmat[f"{k}_{name}"][:] for k in ("RP", "RT", "Z", "DM", "WDM")}
             ref = {k: want[f"{k}_{name}"] for k in ("RP", "RT", "Z", "DM", "WDM")}
             compare_like_reference(got, ref, names=("RP", "RT", "Z", "DM", "WDM"))
+
+
+def test_second_tracer_matches_oracle(cuda):
+    """picca_metal_dmat.py with --lambda-abs2: the second field's distances are
+    those of its own tracer (here LYB), every absorber of the first list is
+    paired with every one of the second, r_par is unfolded and no swapped
+    pass is made (py/picca/bin/picca_metal_dmat.py:389-470,
+    py/picca/cf.py:1088-1090)."""
+    from picca_gb300 import constants, dmat, metal, pairs, synthetic
+    cosmo = constants.Cosmo(Om=0.3147, verbose=False)
+    # the first field: LYA forests of quasars at z 3.5-4; the second: forests
+    # moved to 0.85 of their wavelengths (rest frame 884-1020 A, below LYB)
+    # of quasars at z 3.8-4.6, so that both overlap in observed wavelength
+    fs = synthetic.make_forests(60, 31, (150.0, 152.5), (0.0, 2.5), z_lo=3.5, z_hi=4.0,
+                                max_pixels=400)
+    fs2 = synthetic.make_forests(60, 32, (150.0, 152.5), (0.0, 2.5), z_lo=3.8, z_hi=4.6,
+                                 max_pixels=400, thingid_start=10_000)
+    fs2.log_lambda = np.asarray(fs2.log_lambda) + np.log10(0.85)
+    # the second field as LYB forests: z and distances of that tracer
+    lam2 = constants.ABSORBER_IGM["LYB"]
+    z2 = 10**np.asarray(fs2.log_lambda) / lam2 - 1.0
+    fs2.z = z2
+    fs2.r_comov = cosmo.get_r_comov(z2)
+    fs2.dist_m = cosmo.get_dist_m(z2)
+    alpha = {"LYA": 2.9, "LYB": 2.9, "SiIII(1207)": 1.0, "SiII(1260)": 1.0}
+    p = omd.MetalParams(-60.0, 60.0, 60.0, 12, 10, coef_binning_model=1, x_correlation=True,
+                        z_ref=2.25, alpha_abs=alpha)
+    ang_max = 0.03
+    want = omd.pipeline(fs, cosmo, p, ang_max, 0.7, ["SiIII(1207)"], nproc=2, fs2=fs2,
+                        lambda_abs2="LYB", abs_igm2=["SiII(1260)"])
+    params = pairs.make_params(-60.0, 60.0, 60.0, 12, 10, ang_max, x_correlation=True)
+    dparams = dmat.make_dmat_params(12, 10)
+    got = metal.metal_distortion_matrices(fs, params, dparams, cosmo, 0.7, ["SiIII(1207)"],
+                                          alpha, z_ref=2.25, nproc=2, fs2=fs2,
+                                          abs_igm2=["SiII(1260)"], lambda_abs2="LYB")
+    # the tracer pair itself (LYA_LYB) is the correlation, not a metal matrix
+    assert sorted(got) == sorted(want) == sorted(
+        ["LYA_SiII(1260)", "SiIII(1207)_LYB", "SiIII(1207)_SiII(1260)"])
+    assert np.abs(want["SiIII(1207)_LYB"]["DM"]).sum() > 0
+    for name in want:
+        assert got[name]["NPALL"] == want[name]["NPALL"]
+        assert got[name]["NPUSED"] == want[name]["NPUSED"]
+        assert want[name]["WDM"].sum() > 0
+        for key in ("WDM", "DM", "RP", "RT", "Z"):
+            ok, err = close(got[name][key], want[name][key])
+            assert ok, (name, key, err)
