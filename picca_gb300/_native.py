@@ -16,6 +16,7 @@ PG_MODE_FP32_GUARD = 1
 PG_DMAT_FP64 = 0
 PG_DMAT_SPLIT_BF16 = 1
 PG_XDMAT_MAX_OBJECTS = 256
+PG_ERR_UNSUPPORTED = -6
 
 _P = ctypes.POINTER
 _c_double_p = ctypes.c_void_p  # device pointers are passed as integers
@@ -128,10 +129,12 @@ def lib():
 
 
 def check(status, what):
-    """Raise NativeError for a nonzero status."""
+    """Raise NativeError (with the status in ``.status``) for a nonzero status."""
     if status != PG_OK:
         msg = lib().pg_strerror(status).decode()
-        raise NativeError(f"{what} failed: {msg} (status {status})")
+        err = NativeError(f"{what} failed: {msg} (status {status})")
+        err.status = status
+        raise err
 
 
 class Plan:

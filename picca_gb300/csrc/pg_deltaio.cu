@@ -357,6 +357,10 @@ int read_delta_file(const uint8_t *buf, int64_t size, double z_min, double z_max
         if (!thing) cid = column(cols, "LOS_ID");
         if (!cz || !cra || !cdec || !cid || (thing && (!cpl || !cmj || !cfb)))
             return PG_ERR_INVALID_ARGUMENT;
+        // identifiers stored as text (coadded SDSS plates "3655-3657") are
+        // left to the per-object reader
+        for (const Column *c : {cid, cpl, cmj, cfb})
+            if (c && (c->type == 'A' || c->repeat != 1)) return PG_ERR_UNSUPPORTED;
         const uint8_t *mrow0 = buf + meta->data_offset;
         const int eb = it[1] == 'D' ? 8 : 4;
         const int lb = lt == 'D' ? 8 : 4;

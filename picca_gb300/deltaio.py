@@ -149,3 +149,77 @@ def make_deltas(arrays, order):
                 setattr(d, key, arrays[key][sl])
         deltas.append(d)
     return deltas
+
+
+def write_deltas(out_dir, arrays, log_lambda_grid, grid_index, save_format="ImageHDU",
+                 wave_solution="log", blinding="none", flux_units="10**-17 erg/(s cm2 Angstrom)"):
+    """Delta files of delta_extraction (py/picca/delta_extraction/data.py:62-265):
+    one ``delta-{healpix}.fits.gz`` per healpix under ``out_dir/Delta``.
+
+    ``arrays``: per line of sight ``los_id``, ``ra``, ``dec``, ``z_qso``,
+    ``healpix`` (and optionally ``mean_snr``), ``pix_offset``, and per pixel
+    ``delta``, ``weights``, ``cont``; ``grid_index`` places each pixel on
+    ``log_lambda_grid``. ``ImageHDU``: LAMBDA, METADATA (LOS_ID, RA, DEC, Z,
+    MEANSNR; BLINDING), DELTA (DELTA_BLIND when blinded), WEIGHT and CONT
+    images over the grid, NaN outside each forest. ``BinTableHDU``: one table
+    per line of sight (LAMBDA or LOGLAM, DELTA, WEIGHT, CONT; header LOS_ID,
+    RA, DEC, Z, BLINDING). Returns the paths written."""
+    from . import fitsio_lite
+    os.makedirs(os.path.join(out_dir, "Delta"), exist_ok=True)
+    po = np.asarray(arrays["pix_offset"], dtype=np.int64)
+    healpix = np.asarray(arrays["healpix"], dtype=np.int64)
+    grid = np.asarray(log_lambda_grid, dtype=np.float64)
+    index = np.asarray(grid_index, dtype=np.int64)
+    mean_snr = np.asarray(arrays.get("mean_snr", np.zeros(len(healpix))), dtype=np.float64)
+    delta_name = "DELTA" if blinding == "none" else "DELTA_BLIND"
+    paths = []
+    for hp in np.unique(healpix):
+        members = np.nonzero(healpix == hp)[0]
+        path = os.path.join(out_dir, "Delta", f"delta-{int(hp)}.fits.gz")
+        if save_format == "ImageHDU":
+            shape = (members.size, grid.size)
+            images = {k: np.full(shape, np.nan) for k in ("delta", "weights", "cont")}
+            for row, f in enumerate(members):
+                sl = slice(po[f], po[f + 1])
+                for k in images:
+                    images[k][row, index[sl]] = arrays[k][sl]
+            step = [{"name": "DELTA_LOG_LAMBDA", "value": round(grid[1] - grid[0], 2)}] \
+                if wave_solution == "log" else \
+                [{"name": "DELTA_LAMBDA", "value": round(10**grid[1] - 10**grid[0], 2)}]
+            meta = {"columns": [np.asarray(arrays["los_id"])[members].astype(np.int64),
+                                np.asarray(arrays["ra"])[members],
+                                np.asarray(arrays["dec"])[members],
+                                np.asarray(arrays["z_qso"])[members], mean_snr[members]],
+                    "names": ["LOS_ID", "RA", "DEC", "Z", "MEANSNR"],
+                    "header": [{"name": "BLINDING", "value": blinding}],
+                    "extname": "METADATA"}
+            fitsio_lite.write_hdus(path, [
+                ("image", "LAMBDA", 10**grid,
+                 [{"name": "BUNIT", "value": "Angstrom"},
+                  {"name": "WAVE_SOLUTION", "value": wave_solution}] + step),
+                ("table", meta),
+                ("image", delta_name, images["delta"], [{"name": "BUNIT", "value": ""}]),
+                ("image", "WEIGHT", images["weights"], []),
+                ("image", "CONT", images["cont"], [{"name": "BUNIT", "value": flux_units}])])
+        elif save_format == "BinTableHDU":
+            tables = []
+            for f in members:
+                sl = slice(po[f], po[f + 1])
+                wave = 10**grid[index[sl]] if wave_solution == "lin" else grid[index[sl]]
+                tables.append({
+                    "columns": [wave, arrays["delta"][sl], arrays["weights"][sl],
+                                arrays["cont"][sl]],
+                    "names": ["LAMBDA" if wave_solution == "lin" else "LOGLAM", delta_name,
+                              "WEIGHT", "CONT"],
+                    "extname": str(int(arrays["los_id"][f])),
+                    "header": [{"name": "LOS_ID", "value": int(arrays["los_id"][f])},
+                               {"name": "RA", "value": float(arrays["ra"][f])},
+                               {"name": "DEC", "value": float(arrays["dec"][f])},
+                               {"name": "Z", "value": float(arrays["z_qso"][f])},
+                               {"name": "MEANSNR", "value": float(mean_snr[f])},
+                               {"name": "BLINDING", "value": blinding}]})
+            fitsio_lite.write_fits(path, tables)
+        else:
+            raise ValueError(f"Invalid format {save_format}; expected ImageHDU or BinTableHDU")
+        paths.append(path)
+    return paths

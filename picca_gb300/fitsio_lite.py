@@ -364,6 +364,91 @@ def _column_spec(values):
     raise FITSError(f"cannot write column of dtype {arr.dtype}")
 
 
+def _primary_bytes(records=None):
+    return _header_bytes([
+        _card("SIMPLE", True, "file does conform to FITS standard"),
+        _card("BITPIX", 8, "number of bits per data pixel"),
+        _card("NAXIS", 0, "number of data axes"),
+        _card("EXTEND", True, "FITS dataset may contain extensions"),
+    ] + [_card(r["name"], r["value"], r.get("comment", "")) for r in (records or [])])
+
+
+def _table_bytes(table):
+    columns = table["columns"]
+    names = table["names"]
+    units = table.get("units") or [""] * len(names)
+    comments = table.get("comments") or [""] * len(names)
+    nrows = len(np.asarray(columns[0]))
+    specs = []
+    row_fields = []
+    for col, name in zip(columns, names):
+        arr = np.asarray(col)
+        if arr.shape[0] != nrows:
+            raise FITSError("columns must share their first dimension")
+        code, conv, width = _column_spec(arr)
+        repeat = int(np.prod(arr.shape[1:])) if arr.ndim > 1 else 1
+        if code == "A":
+            tform = f"{width}A"
+            field_dtype = conv.dtype
+        else:
+            tform = f"{repeat}{code}" if repeat != 1 else code
+            field_dtype = conv.dtype if repeat == 1 else (conv.dtype, (repeat,))
+        specs.append((name, tform))
+        row_fields.append((name, conv.reshape(nrows, -1) if repeat != 1 else conv,
+                           field_dtype))
+    dtype = np.dtype([(n, d) for n, _, d in row_fields])
+    rec = np.zeros(nrows, dtype=dtype)
+    for name, conv, _ in row_fields:
+        rec[name] = conv
+    cards = [
+        _card("XTENSION", "BINTABLE", "binary table extension"),
+        _card("BITPIX", 8, "8-bit bytes"),
+        _card("NAXIS", 2, "2-dimensional binary table"),
+        _card("NAXIS1", dtype.itemsize, "width of table in bytes"),
+        _card("NAXIS2", nrows, "number of rows in table"),
+        _card("PCOUNT", 0, "size of special data area"),
+        _card("GCOUNT", 1, "one data group (required keyword)"),
+        _card("TFIELDS", len(specs), "number of fields in each row"),
+    ]
+    for index, ((name, tform), unit, comment) in enumerate(
+            zip(specs, units, comments), start=1):
+        cards.append(_card(f"TTYPE{index}", name, comment or f"label for field {index}"))
+        cards.append(_card(f"TFORM{index}", tform, "data format of field"))
+        if unit:
+            cards.append(_card(f"TUNIT{index}", unit, "physical unit of field"))
+    if table.get("extname"):
+        cards.append(_card("EXTNAME", table["extname"], "name of this binary table extension"))
+    for record in table.get("header") or []:
+        cards.append(_card(record["name"], record["value"], record.get("comment", "")))
+    return _header_bytes(cards) + _pad_data(rec.tobytes())
+
+
+def _image_bytes(extname, arr, records):
+    arr = np.asarray(arr)
+    if arr.dtype.kind == "f":
+        bitpix, data = -64, arr.astype(">f8")
+    else:
+        bitpix, data = 64, arr.astype(">i8")
+    cards = [
+        _card("XTENSION", "IMAGE", "Image extension"),
+        _card("BITPIX", bitpix, "data type"),
+        _card("NAXIS", arr.ndim, "number of axes"),
+    ]
+    for axis, dim in enumerate(reversed(arr.shape), start=1):
+        cards.append(_card(f"NAXIS{axis}", dim))
+    cards += [_card("PCOUNT", 0), _card("GCOUNT", 1), _card("EXTNAME", extname)]
+    for record in records or []:
+        cards.append(_card(record["name"], record["value"], record.get("comment", "")))
+    return _header_bytes(cards) + _pad_data(data.tobytes())
+
+
+def _write_payload(path, payload):
+    if str(path).endswith(".gz"):
+        payload = gzip.compress(payload, compresslevel=4)
+    with open(path, "wb") as handle:
+        handle.write(payload)
+
+
 def write_fits(path, tables, clobber=True):
     """Write a primary HDU followed by one BINTABLE per entry of ``tables``.
 
@@ -376,66 +461,24 @@ def write_fits(path, tables, clobber=True):
     if os.path.exists(path) and not clobber:
         raise FITSError(f"{path} exists")
     out = io.BytesIO()
-    out.write(_header_bytes([
-        _card("SIMPLE", True, "file does conform to FITS standard"),
-        _card("BITPIX", 8, "number of bits per data pixel"),
-        _card("NAXIS", 0, "number of data axes"),
-        _card("EXTEND", True, "FITS dataset may contain extensions"),
-    ]))
+    out.write(_primary_bytes())
     for table in tables:
-        columns = table["columns"]
-        names = table["names"]
-        units = table.get("units") or [""] * len(names)
-        comments = table.get("comments") or [""] * len(names)
-        nrows = len(np.asarray(columns[0]))
-        specs = []
-        row_fields = []
-        for col, name in zip(columns, names):
-            arr = np.asarray(col)
-            if arr.shape[0] != nrows:
-                raise FITSError("columns must share their first dimension")
-            code, conv, width = _column_spec(arr)
-            repeat = int(np.prod(arr.shape[1:])) if arr.ndim > 1 else 1
-            if code == "A":
-                tform = f"{width}A"
-                field_dtype = conv.dtype
-            else:
-                tform = f"{repeat}{code}" if repeat != 1 else code
-                field_dtype = conv.dtype if repeat == 1 else (conv.dtype, (repeat,))
-            specs.append((name, tform))
-            row_fields.append((name, conv.reshape(nrows, -1) if repeat != 1 else conv,
-                               field_dtype))
-        dtype = np.dtype([(n, d) for n, _, d in row_fields])
-        rec = np.zeros(nrows, dtype=dtype)
-        for name, conv, _ in row_fields:
-            rec[name] = conv
-        cards = [
-            _card("XTENSION", "BINTABLE", "binary table extension"),
-            _card("BITPIX", 8, "8-bit bytes"),
-            _card("NAXIS", 2, "2-dimensional binary table"),
-            _card("NAXIS1", dtype.itemsize, "width of table in bytes"),
-            _card("NAXIS2", nrows, "number of rows in table"),
-            _card("PCOUNT", 0, "size of special data area"),
-            _card("GCOUNT", 1, "one data group (required keyword)"),
-            _card("TFIELDS", len(specs), "number of fields in each row"),
-        ]
-        for index, ((name, tform), unit, comment) in enumerate(
-                zip(specs, units, comments), start=1):
-            cards.append(_card(f"TTYPE{index}", name, comment or f"label for field {index}"))
-            cards.append(_card(f"TFORM{index}", tform, "data format of field"))
-            if unit:
-                cards.append(_card(f"TUNIT{index}", unit, "physical unit of field"))
-        if table.get("extname"):
-            cards.append(_card("EXTNAME", table["extname"], "name of this binary table extension"))
-        for record in table.get("header") or []:
-            cards.append(_card(record["name"], record["value"], record.get("comment", "")))
-        out.write(_header_bytes(cards))
-        out.write(_pad_data(rec.tobytes()))
-    payload = out.getvalue()
-    if str(path).endswith(".gz"):
-        payload = gzip.compress(payload, compresslevel=4)
-    with open(path, "wb") as handle:
-        handle.write(payload)
+        out.write(_table_bytes(table))
+    _write_payload(path, out.getvalue())
+
+
+def write_hdus(path, hdus, primary_header=None):
+    """Write a primary HDU and a mix of extensions: each entry of ``hdus`` is
+    ``("image", extname, array, header records)`` or ``("table", table)``
+    with ``table`` as for :func:`write_fits`."""
+    out = io.BytesIO()
+    out.write(_primary_bytes(primary_header))
+    for entry in hdus:
+        if entry[0] == "image":
+            out.write(_image_bytes(*entry[1:]))
+        else:
+            out.write(_table_bytes(entry[1]))
+    _write_payload(path, out.getvalue())
 
 
 def write_image_hdus(path, images, primary_header=None):
@@ -444,33 +487,4 @@ def write_image_hdus(path, images, primary_header=None):
     ``images`` is a list of (extname, array, header records). Arrays are
     written big-endian as float64 (BITPIX -64) or int64 (BITPIX 64).
     """
-    out = io.BytesIO()
-    out.write(_header_bytes([
-        _card("SIMPLE", True, "file does conform to FITS standard"),
-        _card("BITPIX", 8, "number of bits per data pixel"),
-        _card("NAXIS", 0, "number of data axes"),
-        _card("EXTEND", True, "FITS dataset may contain extensions"),
-    ] + [_card(r["name"], r["value"], r.get("comment", "")) for r in (primary_header or [])]))
-    for extname, arr, records in images:
-        arr = np.asarray(arr)
-        if arr.dtype.kind == "f":
-            bitpix, data = -64, arr.astype(">f8")
-        else:
-            bitpix, data = 64, arr.astype(">i8")
-        cards = [
-            _card("XTENSION", "IMAGE", "Image extension"),
-            _card("BITPIX", bitpix, "data type"),
-            _card("NAXIS", arr.ndim, "number of axes"),
-        ]
-        for axis, dim in enumerate(reversed(arr.shape), start=1):
-            cards.append(_card(f"NAXIS{axis}", dim))
-        cards += [_card("PCOUNT", 0), _card("GCOUNT", 1), _card("EXTNAME", extname)]
-        for record in records or []:
-            cards.append(_card(record["name"], record["value"], record.get("comment", "")))
-        out.write(_header_bytes(cards))
-        out.write(_pad_data(data.tobytes()))
-    payload = out.getvalue()
-    if str(path).endswith(".gz"):
-        payload = gzip.compress(payload, compresslevel=4)
-    with open(path, "wb") as handle:
-        handle.write(payload)
+    write_hdus(path, [("image",) + tuple(entry) for entry in images], primary_header)

@@ -102,8 +102,15 @@ def read_deltas(in_dir, nside, lambda_abs, alpha, z_ref, cosmo,
     files = _list_delta_files(in_dir)
     order = find_order(in_dir, delta_attributes)
     if native and rebin_factor is None:
-        return _read_deltas_native(files, in_dir, nside, lambda_abs, alpha, z_ref, cosmo,
-                                   max_num_spec, no_project, nproc, z_min_qso, z_max_qso, order)
+        from ._native import NativeError, PG_ERR_UNSUPPORTED
+        try:
+            return _read_deltas_native(files, in_dir, nside, lambda_abs, alpha, z_ref, cosmo,
+                                       max_num_spec, no_project, nproc, z_min_qso, z_max_qso,
+                                       order)
+        except NativeError as err:
+            if getattr(err, "status", None) != PG_ERR_UNSUPPORTED:
+                raise
+            # a layout the native parser leaves to the per-object readers
     deltas = []
     num_data = 0
     for filename in files:

@@ -75,3 +75,82 @@ def test_projection_orders_and_sizes():
                         d[sl].copy(), order)
             obj.project()
             assert np.array_equal(got[sl], obj.delta), (order, sizes[f])
+
+
+@pytest.mark.parametrize("save_format,wave", [("ImageHDU", "log"), ("ImageHDU", "lin"),
+                                              ("BinTableHDU", "log"), ("BinTableHDU", "lin")])
+def test_writer_round_trip(tmp_path, save_format, wave):
+    """delta_extraction's delta files (py/picca/delta_extraction/data.py:62-265)
+    written by deltaio.write_deltas and read back by both readers: every
+    forest, pixel and value recovered."""
+    from picca_gb300 import deltaio
+    rng = np.random.default_rng(7)
+    grid = (3.5563 + 3e-4 * np.arange(900)) if wave == "log" else \
+        np.log10(3600.0 + 0.8 * np.arange(900))
+    nf = 40
+    starts = rng.integers(0, 500, nf)
+    lengths = rng.integers(30, 380, nf)
+    index = np.concatenate([np.arange(s, s + n) for s, n in zip(starts, lengths)])
+    po = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    n = int(po[-1])
+    arrays = {"los_id": np.arange(100, 100 + nf), "ra": rng.uniform(0, 0.1, nf),
+              "dec": rng.uniform(0, 0.1, nf), "z_qso": rng.uniform(2.2, 3.4, nf),
+              "healpix": rng.integers(0, 3, nf), "pix_offset": po,
+              "delta": rng.normal(0, 0.3, n), "weights": rng.uniform(0.5, 3.0, n),
+              "cont": rng.uniform(1.0, 2.0, n)}
+    deltaio.write_deltas(str(tmp_path), arrays, grid, index, save_format=save_format,
+                         wave_solution=wave)
+    files = sorted(str(p) for p in (tmp_path / "Delta").iterdir())
+    got = deltaio.read_files(files)
+    # forests come back grouped by healpix file, in file order
+    order = np.concatenate([np.nonzero(arrays["healpix"] == hp)[0]
+                            for hp in sorted(np.unique(arrays["healpix"]),
+                                             key=lambda h: f"delta-{h}.fits.gz")])
+    assert np.array_equal(got["los_id"], arrays["los_id"][order])
+    for key in ("ra", "dec", "z_qso"):
+        assert np.array_equal(got[key], arrays[key][order])
+    want_ll = np.concatenate([grid[index[po[f]:po[f + 1]]] for f in order])
+    if wave == "lin":  # stored as wavelength, read back as log10 of it
+        want_ll = np.log10(10**want_ll)
+    assert np.array_equal(got["log_lambda"], want_ll)
+    for key in ("delta", "weights", "cont"):
+        want = np.concatenate([arrays[key][po[f]:po[f + 1]] for f in order])
+        assert np.array_equal(got[key], want)
+    # the per-object readers see the same files
+    per_object = [d for path in files for d in io.read_delta_file(path)]
+    assert [d.los_id for d in per_object] == list(got["los_id"])
+    assert np.array_equal(np.concatenate([d.delta for d in per_object]), got["delta"])
+
+
+def test_text_identifiers_use_per_object_reader(tmp_path):
+    """Image files whose METADATA keeps coadded SDSS identifiers as text
+    (PLATE '3655-3657', py/picca/delta_extraction/astronomical_objects/
+    sdss_forest.py:144-161) are left to the per-object readers."""
+    from picca_gb300 import _native, deltaio, fitsio_lite
+    rng = np.random.default_rng(3)
+    grid = 3.5563 + 3e-4 * np.arange(200)
+    nf = 5
+    inside = rng.random((nf, 200)) < 0.7
+    img = {k: np.where(inside, rng.uniform(0.5, 1.5, (nf, 200)), np.nan)
+           for k in ("DELTA", "WEIGHT", "CONT")}
+    meta = {"columns": [np.arange(nf, dtype=np.int64) + 7, rng.uniform(0, 0.1, nf),
+                        rng.uniform(0, 0.1, nf), rng.uniform(2.2, 3.0, nf),
+                        np.array([b"3655-3657"] * nf), np.array([b"55240-55244"] * nf),
+                        np.array([b"0012-0300"] * nf)],
+            "names": ["THING_ID", "RA", "DEC", "Z", "PLATE", "MJD", "FIBERID"],
+            "header": [{"name": "BLINDING", "value": "none"}], "extname": "METADATA"}
+    os.makedirs(tmp_path / "Delta")
+    path = str(tmp_path / "Delta" / "delta-1.fits.gz")
+    fitsio_lite.write_hdus(path, [("image", "LAMBDA", 10**grid, []), ("table", meta)]
+                           + [("image", k, v, []) for k, v in img.items()])
+    with pytest.raises(_native.NativeError) as info:
+        deltaio.read_file(path)
+    assert info.value.status == _native.PG_ERR_UNSUPPORTED
+    cosmo = constants.Cosmo(Om=0.315, verbose=False)
+    args = (str(tmp_path / "Delta") + "/", 16, constants.ABSORBER_IGM["LYA"], 2.9, 2.25, cosmo)
+    got = io.read_deltas(*args, no_project=True, native=True)
+    want = io.read_deltas(*args, no_project=True, native=False)
+    assert got[1] == want[1] == nf
+    for hp in want[0]:
+        for a, b in zip(got[0][hp], want[0][hp]):
+            assert np.array_equal(a.delta, b.delta) and a.plate == b.plate
