@@ -9,7 +9,7 @@ host API (pinned host arrays uploaded, rows read back, every step).
 
 Default workload: the 100k-forest auto-correlation on 2,000 deg^2 (50 x 50
 bins, r_par and r_trans 0-200 Mpc/h, precision form); ``--config 2`` runs the
-400k-forest survey on 8,000 deg^2. ``--impl reference``
+400k-forest survey on 8,000 deg^2 and ``--config 0`` the 1,000-forest patch. ``--impl reference``
 times the CPU oracle (FP64 C restatement of picca's numba kernel, OpenMP over
 all host cores) on a bounded sample of the same workload.
 """
@@ -30,14 +30,14 @@ sys.path.insert(0, HERE)
 
 CONFIGS = {
     # name: (num forests, area deg^2, grid, description)
-    "0": (1000, None, "log", "1,000 forests in a 4.5x4.5 deg patch (config 0)"),
-    "1": (100_000, 2000.0, "log", "100k forests on 2,000 deg^2 (config 1)"),
-    "1lin": (100_000, 2000.0, "lin", "100k forests on 2,000 deg^2, 0.8 A grid (config 1 lin)"),
-    "2": (400_000, 8000.0, "log", "400k forests on 8,000 deg^2 (config 2)"),
+    "0": (1000, None, "log", "1,000 forests in a 4.5x4.5 deg patch"),
+    "1": (100_000, 2000.0, "log", "100k forests on 2,000 deg^2"),
+    "1lin": (100_000, 2000.0, "lin", "100k forests on 2,000 deg^2, 0.8 A grid"),
+    "2": (400_000, 8000.0, "log", "400k forests on 8,000 deg^2"),
 }
 METRIC = "cf pixel-pairs/s at stated FP64-oracle error; continuum fits/s plain vs learned"
 # DRAM bytes (read + write) of the pair kernel per candidate pixel pair, from
-# one ncu capture on 1,000 random work items of config 1 (5.533 GB read +
+# one ncu capture on 1,000 random work items of the 100k-forest survey (5.533 GB read +
 # 0.114 GB written for 2.628e10 candidate pairs; see profiles/); the roofline
 # entry scales it to the launch by the candidate pairs processed
 PAIR_DRAM_BYTES_PER_CANDIDATE = (5.532826e9 + 0.113620e9) / 26284549581
@@ -56,14 +56,14 @@ def parse():
     p.add_argument("--cpu-seconds", type=float, default=15.0,
                    help="target CPU time of the oracle sample")
     p.add_argument("--continuum-forests", type=int, default=400_000,
-                   help="raw forests of the continuum-fit leg (configs 3/4); 0 skips it")
+                   help="raw forests of the continuum-fit leg; 0 skips it")
     p.add_argument("--continuum-train", type=int, default=200_000,
                    help="raw forests (separate seed) the warm-start network is trained on")
     p.add_argument("--continuum-iterations", type=int, default=5)
     p.add_argument("--profile-items", type=int, default=0,
                    help="profiling aid: run the pair kernel once on this many randomly chosen "
                         "work items of the workload and exit (no timing, no JSON line)")
-    p.add_argument("--config2", action="store_true",
+    p.add_argument("--large-survey", action="store_true",
                    help="also run the 400k-forest auto and 600k-quasar cross correlations")
     p.add_argument("--dmat-reject", type=float, default=0.99,
                    help="random rejection of the distortion-matrix leg (picca_dmat.py --rej); "
@@ -85,9 +85,9 @@ def make_workload(cfg):
     from picca_gb300 import synthetic
     num, area, grid, _ = CONFIGS[cfg]
     if area is None:
-        fs = synthetic.config0()
+        fs = synthetic.patch_forests()
     else:
-        fs = synthetic.config_area(num, area, seed=20261203, grid=grid)
+        fs = synthetic.survey_band(num, area, seed=20261203, grid=grid)
     params = dict(r_par_min=0.0, r_par_max=200.0, r_trans_max=200.0, num_bins_r_par=50,
                   num_bins_r_trans=50)
     ang_max = synthetic.correlation_ang_max(200.0, float(fs.z.min()))
@@ -791,7 +791,7 @@ def xdmat_leg(args, fs, params, ang_max, engine):
 
 
 def continuum_leg(args, cpu_seconds):
-    """Configs 3 and 4: the plain batched Dr16 fit and the learned warm start.
+    """The plain batched Dr16 fit and the learned warm start.
 
     A fit is one forest in one outer iteration. Both legs run the same
     number of iterations of the whole Dr16 loop (fits, GPU histograms, host
@@ -823,7 +823,7 @@ def continuum_leg(args, cpu_seconds):
         eng = continuum.Dr16Gpu(small.grid, num_iterations=2, fit_mode=mode)
         eng.run(continuum.DeviceSpectra(small, eng.device))
 
-    # plain leg (config 3): FP32 per-pixel terms, FP64 2x2 Newton solve;
+    # plain leg: FP32 per-pixel terms, FP64 2x2 Newton solve;
     # fit kernel time measured separately
     eng_p = continuum.Dr16Gpu(eval_raw.grid, num_iterations=iters, fit_mode=mixed)
     spectra = continuum.DeviceSpectra(eval_raw, eng_p.device)
@@ -867,7 +867,7 @@ def continuum_leg(args, cpu_seconds):
     num_samples = int(feats.shape[0])
     del feats, targs, train
 
-    # learned leg (config 4) on the same evaluation forests
+    # learned leg on the same evaluation forests
     eng_w = continuum.Dr16Gpu(eval_raw.grid, num_iterations=iters, fit_mode=mixed)
     (warm_fit, stats), warm_s = timed_loop(lambda: learned.run_warm(eng_w, spectra, net))
     warm = continuum.fit_results_to_host(warm_fit)
@@ -878,7 +878,7 @@ def continuum_leg(args, cpu_seconds):
     # chi2 sums terms of both signs: relative to max(|chi2|, ndata)
     dchi = (np.abs(warm["chi2"] - plain["chi2"]) /
             np.maximum(np.abs(plain["chi2"]), plain["ndata"]))[ok]
-    # config 4 end to end: the deltas of both fits feed the auto-correlation
+    # learned warm start end to end: the deltas of both fits feed the auto-correlation
     # (50k forests of a contiguous stretch of the survey band)
     e2e_corr = None
     if args.continuum_correlation > 0:
@@ -934,8 +934,8 @@ def continuum_leg(args, cpu_seconds):
     }
 
 
-def config2_leg(args):
-    """Config 2: the 400k-forest auto-correlation on 8,000 deg^2 and the
+def large_survey_leg(args):
+    """The 400k-forest auto-correlation on 8,000 deg^2 and the
     cross-correlation with 600k quasars on the same band (r_par -200..200 in
     100 bins x r_trans 0..200 in 50), both in the precision form; each kernel
     timed once after a warm-up run, with its error against the plain FP64
@@ -943,7 +943,7 @@ def config2_leg(args):
     import torch
 
     from picca_gb300 import pairs, synthetic
-    fs = synthetic.config_area(400_000, 8000.0, seed=20261206)
+    fs = synthetic.survey_band(400_000, 8000.0, seed=20261206)
     ra_r, dec_r = synthetic.band_for_area(8000.0, 30.0)
     qs = synthetic.make_quasars(600_000, 20261207, ra_r, dec_r)
     ang_max = synthetic.correlation_ang_max(200.0, float(fs.z.min()))
@@ -1215,7 +1215,7 @@ def run_ours(args):
     dio = delta_io_leg(fs)
     print("delta io leg: " + json.dumps(dio), file=sys.stderr, flush=True)
     cont = continuum_leg(args, args.cpu_seconds)
-    cfg2 = config2_leg(args) if args.config2 else None
+    cfg2 = large_survey_leg(args) if args.large_survey else None
     print("continuum leg: " + json.dumps(cont), file=sys.stderr, flush=True)
     line = {
         "metric": METRIC, "value": value, "unit": "pixel-pairs/s", "n_gpus": world,
@@ -1253,7 +1253,7 @@ def run_ours(args):
         "delta_io": dio,
     }
     if cfg2 is not None:
-        line["config2"] = cfg2
+        line["large_survey"] = cfg2
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -143,15 +143,15 @@ def make_quasars(num, seed, ra_range_deg, dec_range_deg, z_lo=2.1, z_hi=4.0, z_l
         healpix=healpix)
 
 
-# The benchmark configurations -------------------------------------------------
-def config0(seed=20261203):
+# The benchmark workloads ------------------------------------------------------
+def patch_forests(seed=20261203):
     """1,000 forests in a 4.5 x 4.5 deg patch, z_qso ~ U(2.1, 3.5)."""
     return make_forests(1000, seed, (150.0, 154.5), (0.0, 4.5), 2.1, 3.5, "uniform")
 
 
-def config_area(num, area_deg2, seed, grid="log", half_height=None):
+def survey_band(num, area_deg2, seed, grid="log", half_height=None):
     """``num`` forests on a band of ``area_deg2`` with z_qso ~ (1+z)^-2 on
-    [2.1, 4.0] (configs 1 and 2: 100k on 2,000 deg^2, 400k on 8,000 deg^2)."""
+    [2.1, 4.0] (the benchmark surveys: 100k on 2,000 deg^2, 400k on 8,000 deg^2)."""
     if half_height is None:
         half_height = 20.0 if area_deg2 <= 4000 else 30.0
     ra_r, dec_r = band_for_area(area_deg2, half_height)

@@ -59,7 +59,7 @@ class RawForests:
 
 def make_raw_forests(num, seed, grid=None, z_lo=2.1, z_hi=4.0, z_law="inv2", area_deg2=8000.0,
                      nside=16, min_pixels=50):
-    """Generate ``num`` raw forests (config 3 / 4 inputs)."""
+    """Generate ``num`` raw forests (the continuum-fit inputs)."""
     grid = grid or Grid()
     rng = np.random.default_rng(seed)
     ll0 = grid.log_lambda_grid[0]
