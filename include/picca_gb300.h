@@ -31,7 +31,8 @@
  *  - pg_wick_xi_matrices, pg_cf_wick
  *                       <- cf.compute_wick_terms + cf.compute_wickT123_pairs
  *                          py/picca/cf.py:1328-1495, :1498-1626
- *  - pg_xcf_wick        <- xcf.compute_wick_terms + xcf.compute_wickT1234_pairs
+ *  - pg_xcf_wick, pg_xcf_wick_factored
+ *                       <- xcf.compute_wick_terms + xcf.compute_wickT1234_pairs
  *                          py/picca/xcf.py:838-1008, :1220-1351
  *  - pg_read_delta_file <- io.read_delta_file + Delta.from_fitsio / from_image
  *                          py/picca/io.py:333-380, py/picca/data.py:376-620
@@ -548,6 +549,26 @@ int pg_read_delta_file(const uint8_t *bytes, int64_t size, double z_min_qso, dou
 int pg_project_deltas(int64_t num_los, const int64_t *pix_offset, const double *log_lambda,
                       const double *weights, double *delta, const int32_t *order,
                       int32_t threads);
+
+/* The same terms T1-T4 by factorisation, without the sweep over pairs of
+ * listed pairs: T2 + T4 = U^T X1 U and T3 = W^T diag(zw1 / w1) W over the
+ * forest's nonempty bins (U: per pixel and bin, the sum of the quasars'
+ * zw_obj; W: of w1 w_obj), as FP64 GEMMs, with the same-quasar part T2
+ * summed directly and T4 = U^T X1 U - T2. Same arguments as pg_xcf_wick
+ * (item arrays on the device; no slices). Items run one after another on
+ * `stream`, and the call waits for each item's bin count. work:
+ * pg_xcf_wick_factored_work_bytes() bytes (4 max_pixels nb + 3 nb^2
+ * doubles, nb = np nt). */
+int pg_xcf_wick_factored_work_bytes(pg_plan *plan, const pg_corr_params *params,
+                                    int32_t max_pixels, int32_t max_quasars, uint64_t *bytes);
+int pg_xcf_wick_factored(pg_plan *plan, const pg_corr_params *params,
+                         const pg_forest_set *forests, const pg_forest_set *objs,
+                         const double *zw1, const double *zw_obj, const int64_t *x_offsets,
+                         const double *arena, const int32_t *item_forest,
+                         const int32_t *item_start, const int32_t *item_count,
+                         const int32_t *obj_index, const double *obj_angle, int64_t num_items,
+                         int32_t max_quasars, void *work, uint64_t work_bytes,
+                         const pg_wick_sums *out, void *stream);
 
 /* Fast metal distortion matrix (py/picca/bin/picca_fast_metal_dmat.py:30-251,
  * py/picca/bin/picca_fast_metal_xdmat.py:28-215): every pair (i, j) of two

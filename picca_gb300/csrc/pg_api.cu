@@ -1,4 +1,5 @@
 // C-ABI entry points of libpicca_gb300 (declared in include/picca_gb300.h).
+#include <vector>
 #include <stdlib.h>
 
 #include <algorithm>
@@ -681,6 +682,71 @@ int pg_project_deltas(int64_t num_los, const int64_t *pix_offset, const double *
         if ((order[f] != 0 && order[f] != 1) || pix_offset[f + 1] < pix_offset[f])
             return PG_ERR_INVALID_ARGUMENT;
     return project_deltas(num_los, pix_offset, log_lambda, weights, delta, order, threads);
+}
+
+int pg_xcf_wick_factored_work_bytes(pg_plan *plan, const pg_corr_params *params,
+                                    int32_t max_pixels, int32_t max_quasars, uint64_t *bytes) {
+    if (!plan || !bytes || max_pixels < 1 || max_quasars < 1) return PG_ERR_INVALID_ARGUMENT;
+    int nb = 0;
+    int rc = wick_bins(params, &nb);
+    if (rc) return rc;
+    *bytes = xwick_factored_bytes(nb, max_pixels, max_quasars);
+    return PG_OK;
+}
+
+int pg_xcf_wick_factored(pg_plan *plan, const pg_corr_params *params,
+                         const pg_forest_set *forests, const pg_forest_set *objs,
+                         const double *zw1, const double *zw_obj, const int64_t *x_offsets,
+                         const double *arena, const int32_t *item_forest,
+                         const int32_t *item_start, const int32_t *item_count,
+                         const int32_t *obj_index, const double *obj_angle, int64_t num_items,
+                         int32_t max_quasars, void *work, uint64_t work_bytes,
+                         const pg_wick_sums *out, void *stream) {
+    if (!plan || !forests || !objs || !out) return PG_ERR_INVALID_ARGUMENT;
+    int nb = 0, rc = wick_bins(params, &nb);
+    if (rc) return rc;
+    if ((rc = validate_set(forests, true, false)) || (rc = validate_set(objs, false, true)))
+        return rc;
+    if (num_items < 0 || max_quasars < 1 || forests->max_pixels < 1)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (!out->weights_wick || !out->num_pairs_wick || !out->t1 || !out->t2 || !out->t3 ||
+        !out->t4)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (num_items == 0) return PG_OK;
+    if (!zw1 || !zw_obj || !x_offsets || !arena || !item_forest || !item_start || !item_count ||
+        !obj_index || !work)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (reinterpret_cast<uintptr_t>(work) % 256) return PG_ERR_INVALID_ARGUMENT;
+    if (work_bytes < xwick_factored_bytes(nb, forests->max_pixels, max_quasars))
+        return PG_ERR_INVALID_ARGUMENT;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    // the host loop needs the items, the forests' pixel offsets and the arena offsets
+    std::vector<int32_t> hf(num_items), hs(num_items), hc(num_items);
+    std::vector<int64_t> po(forests->num + 1), xo(forests->num);
+    cudaError_t err = cudaMemcpyAsync(hf.data(), item_forest, 4 * num_items,
+                                      cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(hs.data(), item_start, 4 * num_items, cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(hc.data(), item_count, 4 * num_items, cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(po.data(), forests->pix_offset, 8 * po.size(),
+                              cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess)
+        err = cudaMemcpyAsync(xo.data(), x_offsets, 8 * xo.size(), cudaMemcpyDeviceToHost, st);
+    if (err == cudaSuccess) err = cudaStreamSynchronize(st);
+    if (err != cudaSuccess) return check_cuda(err);
+    if ((rc = reset_scratch(plan, st))) return rc;
+    for (int64_t q = 0; q < num_items; ++q)
+        if (hf[q] < 0 || hf[q] >= forests->num || hc[q] > max_quasars || hc[q] < 0 ||
+            po[hf[q] + 1] - po[hf[q]] > forests->max_pixels)
+            return PG_ERR_INVALID_ARGUMENT;
+    return run_xwick_factored(*params, *forests, *objs, zw1, zw_obj, xo.data(), arena, hf.data(),
+                              hs.data(), hc.data(), obj_index, obj_angle, num_items, po.data(),
+                              forests->max_pixels, max_quasars, static_cast<char *>(work), *out,
+                              scratch_of(plan), plan->num_sms, st);
 }
 
 int pg_fast_metal_dmat(pg_plan *plan, const pg_fast_metal_params *params,

@@ -279,6 +279,16 @@ int read_delta_file(const uint8_t *buf, int64_t size, double z_min, double z_max
 int project_deltas(int64_t num_los, const int64_t *pix_offset, const double *log_lambda,
                    const double *weights, double *delta, const int32_t *order, int threads);
 
+uint64_t xwick_factored_bytes(int nb, int max_pixels, int max_quasars);
+int run_xwick_factored(const pg_corr_params &p, const pg_forest_set &forests,
+                       const pg_forest_set &objs, const double *zw1, const double *zw_obj,
+                       const int64_t *xo_host, const double *xa, const int32_t *item_forest,
+                       const int32_t *item_start, const int32_t *item_count,
+                       const int32_t *obj_index, const double *obj_angle, int64_t num_items,
+                       const int64_t *pix_offset_host, int max_pixels, int max_quasars,
+                       char *work, const pg_wick_sums &out, Scratch *scratch, int num_sms,
+                       cudaStream_t st);
+
 int launch_fast_metal(const pg_fast_metal_params &p, const pg_fast_metal_side &a,
                       const pg_fast_metal_side &b, const pg_fast_metal_sums &out,
                       Scratch *scratch, int num_sms, cudaStream_t stream);

@@ -145,6 +145,9 @@ __device__ __forceinline__ int wick_bin(const WickConst &c, double r1, double r2
     if (!(r_par < c.r_par_max && r_trans < c.r_trans_max && r_par >= c.r_par_min)) return -1;
     const int bp = (int)__dmul_rn(__ddiv_rn(__dsub_rn(r_par, c.r_par_min), c.range), (double)c.np);
     const int bt = (int)__dmul_rn(__ddiv_rn(r_trans, c.r_trans_max), (double)c.nt);
+    // a quotient that rounds up to 1 would index past the last bin (the
+    // reference writes out of bounds there); such a pair is dropped
+    if (bp >= c.np || bt >= c.nt) return -1;
     return bt + c.nt * bp;
 }
 
@@ -343,6 +346,9 @@ __device__ __forceinline__ int xwick_bin(const XWickConst &c, double r1, double 
     if (!(r_par < c.r_par_max && r_trans < c.r_trans_max && r_par >= c.r_par_min)) return -1;
     const int bp = (int)__dmul_rn(__ddiv_rn(__dsub_rn(r_par, c.r_par_min), c.range), (double)c.np);
     const int bt = (int)__dmul_rn(__ddiv_rn(r_trans, c.r_trans_max), (double)c.nt);
+    // a quotient that rounds up to 1 would index past the last bin (the
+    // reference writes out of bounds there); such a pair is dropped
+    if (bp >= c.np || bt >= c.nt) return -1;
     return bt + c.nt * bp;
 }
 

@@ -56,6 +56,14 @@ def _bind():
         lib.pg_xcf_wick.argtypes = [vp, _P(_native.CorrParams), _P(_native.ForestSetC),
                                     _P(_native.ForestSetC), vp, vp, vp, vp, vp, vp, vp, vp, vp,
                                     vp, vp, i64, i32, vp, ctypes.c_uint64, _P(WickSumsC), vp]
+        lib.pg_xcf_wick_factored_work_bytes.restype = ctypes.c_int
+        lib.pg_xcf_wick_factored_work_bytes.argtypes = [vp, _P(_native.CorrParams), i32, i32,
+                                                        _P(ctypes.c_uint64)]
+        lib.pg_xcf_wick_factored.restype = ctypes.c_int
+        lib.pg_xcf_wick_factored.argtypes = [vp, _P(_native.CorrParams), _P(_native.ForestSetC),
+                                             _P(_native.ForestSetC), vp, vp, vp, vp, vp, vp, vp,
+                                             vp, vp, i64, i32, vp, ctypes.c_uint64,
+                                             _P(WickSumsC), vp]
         lib._wick_bound = True
     return lib
 
@@ -263,6 +271,29 @@ class WickEngine:
                 ctypes.byref(self._sums_struct(sums)), self._stream()), "cross Wick terms")
         return sums
 
+    def launch_items_factored(self, params, dev, qdev, zw1, zw_obj, xo, xa, items, sums):
+        """pg_xcf_wick_factored on work items (forest, first neighbour,
+        neighbour count): T2 + T4 and T3 as FP64 GEMMs over each forest's
+        nonempty bins (the call waits for each item's bin count)."""
+        lib = _bind()
+        item_forest, item_start, item_count, obj_index, num_items, max_quasars = items
+        nbytes = ctypes.c_uint64()
+        with torch.cuda.device(self.device):
+            check(lib.pg_xcf_wick_factored_work_bytes(
+                self.engine.plan.handle, ctypes.byref(params), int(dev.max_pixels),
+                int(max_quasars), ctypes.byref(nbytes)), "cross Wick work size")
+            need = int(nbytes.value)
+            if self._work is None or self._work.numel() < need:
+                self._work = torch.empty(max(need, 16), dtype=torch.uint8, device=self.device)
+            check(lib.pg_xcf_wick_factored(
+                self.engine.plan.handle, ctypes.byref(params), ctypes.byref(dev.c),
+                ctypes.byref(qdev.c), zw1.data_ptr(), zw_obj.data_ptr(), xo.data_ptr(),
+                xa.data_ptr(), item_forest.data_ptr(), item_start.data_ptr(),
+                item_count.data_ptr(), obj_index.data_ptr(), None, int(num_items),
+                int(max_quasars), self._work.data_ptr(), int(self._work.numel()),
+                ctypes.byref(self._sums_struct(sums)), self._stream()), "cross Wick terms")
+        return sums
+
     def accumulate_cross(self, params, dev, qdev, zw1, zw_obj, xo, xa, items, sums):
         """Plan and launch pg_xcf_wick for work items (forest, first
         neighbour, neighbour count) of the neighbour index."""
@@ -376,11 +407,14 @@ def wick_covariance(fs, params, cf1d, reject, nproc=1, z_ref=2.25, alpha=2.9, al
 
 
 def cross_wick_covariance(fs, qs, params, cf1d, reject, nproc=1, z_ref=2.25, alpha=2.9,
-                          alpha_obj=1.44, engine=None, return_raw=False):
+                          alpha_obj=1.44, engine=None, return_raw=False, method="factored"):
     """picca_xwick.py (py/picca/bin/picca_xwick.py:447-520, --max-diagram 4,
     the default) on a forest set and a quasar set: the normalised COV
     columns (CO, WALL, NB, T1-T6, T5 = T6 = 0) and NPALL / NPUSED. Every
-    neighbouring quasar of a kept forest enters (no per-pair draw)."""
+    neighbouring quasar of a kept forest enters (no per-pair draw).
+    ``method``: "factored" (GEMMs over each forest's bins,
+    pg_xcf_wick_factored) or "sweep" (all pairs of listed pairs,
+    pg_xcf_wick)."""
     engine = engine or WickEngine()
     pe = engine.engine
     tables = OneDTables(cf1d)
@@ -411,7 +445,12 @@ def cross_wick_covariance(fs, qs, params, cf1d, reject, nproc=1, z_ref=2.25, alp
         zq = np.asarray(qs.z_qso, dtype=np.float64)
         zw_obj = torch.from_numpy(np.ascontiguousarray(evolution(zq, z_ref, alpha_obj)
                                                        if zq.size else np.zeros(1))).to(dvc)
-        engine.accumulate_cross(params, dev, qdev, zw1, zw_obj, xo, xa, items, sums)
+        if method == "factored":
+            engine.launch_items_factored(params, dev, qdev, zw1, zw_obj, xo, xa, items, sums)
+        elif method == "sweep":
+            engine.accumulate_cross(params, dev, qdev, zw1, zw_obj, xo, xa, items, sums)
+        else:
+            raise ValueError(f"unknown method {method}")
         stats = engine.stats()
         if stats.status != 0:
             raise _native.NativeError(f"cross Wick kernel reported status {stats.status}")

@@ -159,10 +159,11 @@ def test_cli_matches_golden_xwick(cuda, tmp_path):
     compare_like_reference(got, want, names=tuple(got))
 
 
-@pytest.mark.parametrize("np_,nt,rp,reject,target", [(30, 15, 60.0, 0.5, None),
-                                                     (100, 50, 200.0, 0.9, None),
-                                                     (100, 50, 200.0, 0.9, 1e5)])
-def test_synthetic_cross_matches_oracle(cuda, monkeypatch, np_, nt, rp, reject, target):
+@pytest.mark.parametrize("np_,nt,rp,reject,target,method", [
+    (30, 15, 60.0, 0.5, None, "sweep"), (100, 50, 200.0, 0.9, None, "sweep"),
+    (100, 50, 200.0, 0.9, 1e5, "sweep"), (30, 15, 60.0, 0.5, None, "factored"),
+    (100, 50, 200.0, 0.9, None, "factored")])
+def test_synthetic_cross_matches_oracle(cuda, monkeypatch, np_, nt, rp, reject, target, method):
     from picca_gb300 import constants, pairs, synthetic as syn, utils, wick
     if target is not None:
         monkeypatch.setattr(wick, "SLICE_TARGET", target)
@@ -176,7 +177,7 @@ def test_synthetic_cross_matches_oracle(cuda, monkeypatch, np_, nt, rp, reject, 
                         return_raw=True)
     params = pairs.make_params(-rp, rp, rp, np_, nt, ang_max, x_correlation=True)
     got = wick.cross_wick_covariance(fs, qs, params, cf1d, reject, nproc=2, alpha_obj=1.44,
-                                     return_raw=True)
+                                     return_raw=True, method=method)
     assert (got["NPALL"], got["NPUSED"]) == (want["NPALL"], want["NPUSED"])
     assert want["NB"].sum() > 0
     assert np.array_equal(got["NB"], want["NB"])
