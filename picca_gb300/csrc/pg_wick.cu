@@ -278,6 +278,7 @@ __global__ void __launch_bounds__(kWkBlock)
             const double c1a = valid ? __dmul_rn(s1.weights[o1 + ia], zw1[o1 + ia]) : 0.;
             const double c2a = valid ? __dmul_rn(s2.weights[o2 + ja], zw2[o2 + ja]) : 0.;
             double acc3 = 0., acc2 = 0.;
+            bool have2 = false;  // warp-uniform: acc2 got terms since the last flush
             int kq = 0;
             for (int b0 = 0; b0 < num_listed; b0 += 32) {
                 const int nbatch = min(32, num_listed - b0);
@@ -287,6 +288,7 @@ __global__ void __launch_bounds__(kWkBlock)
                 // FP64 FMA would take the FP64 pipe for the whole warp)
                 uint32_t pending = 0u;
                 auto drain = [&]() {
+                    if (pending) have2 = true;
                     while (pending) {
                         const int k = __ffs(pending) - 1;
                         pending &= pending - 1u;
@@ -313,14 +315,17 @@ __global__ void __launch_bounds__(kWkBlock)
                         if (__any_sync(0xffffffffu, shared)) pending |= 1u << (k + r);
                         if (ub[r] & kWkEnd) {
                             drain();
+                            // the reduction's additions run on the FP64 pipe
+                            // too: T2's only when this bin had shared pixels
                             const double r3 = warp_sum(valid ? acc3 : 0.);
-                            const double r2 = warp_sum(valid ? acc2 : 0.);
+                            const double r2 = have2 ? warp_sum(valid ? acc2 : 0.) : 0.;
                             if (lane == 0) {
                                 const int64_t cell = (int64_t)bin_p * nb + m.nonempty[kq];
                                 if (r3 != 0.) atomicAdd(&out.t3[cell], r3);
                                 if (r2 != 0.) atomicAdd(&out.t2[cell], r2);
                             }
                             acc3 = acc2 = 0.;
+                            have2 = false;
                             ++kq;
                         }
                     }
