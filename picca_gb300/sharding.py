@@ -8,7 +8,10 @@ neighbours, and the full result is the union of disjoint rows. Nothing is
 reduced; :func:`gather_rows` only assembles the rows for the output file.
 
 Rows are dealt out longest-first to the least-loaded rank (LPT), with the
-number of candidate pixel pairs of a row as its cost.
+number of candidate pixel pairs of a row as its cost. The distortion, metal
+and Wick matrices are sums over kept forest pairs instead of rows: the same
+split of the kept forests by healpix applies, and :func:`reduce_sums` adds
+the ranks' un-normalised sums once at the end.
 """
 
 import numpy as np
@@ -59,6 +62,28 @@ def gather_rows(arrays, rows, num_rows, group=None):
         mask[rows] = True
         t = t.clone()
         t[torch.as_tensor(~mask)] = 0
+        dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
+        out.append(t.numpy())
+    return out
+
+
+def reduce_sums(arrays, group=None):
+    """Total of per-rank partial sums on every rank (torch.distributed
+    all_reduce, SUM; any backend). The distortion matrices, the metal
+    matrices and the Wick terms are sums over kept forest pairs rather than
+    per-healpix rows (py/picca/bin/picca_dmat.py:487-494,
+    py/picca/bin/picca_wick.py:515-530 add the process chunks' tuples), so
+    splitting the kept forests over ranks needs one reduction of the
+    un-normalised sums at the end; the random draws are made identically on
+    every rank before the split, so the kept pairs are the single-process
+    ones."""
+    import torch
+    import torch.distributed as dist
+    out = []
+    for arr in arrays:
+        t = torch.as_tensor(np.ascontiguousarray(arr)).clone()
+        if t.dtype not in (torch.float64, torch.int64):
+            raise TypeError("sums are float64 or int64")
         dist.all_reduce(t, op=dist.ReduceOp.SUM, group=group)
         out.append(t.numpy())
     return out

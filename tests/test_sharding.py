@@ -81,3 +81,85 @@ def test_assignment_covers_every_row_once():
     assert np.array_equal(rows, np.arange(6))
     loads = [cost[o].sum() for o in owned]
     assert max(loads) - min(loads) <= cost.max()
+
+
+def _wick_workload():
+    from picca_gb300 import synthetic
+    from oracle import wick as ow
+    fs = synthetic.make_forests(120, 9, (150.0, 152.0), (0.0, 2.0), 2.1, 3.5, "uniform",
+                                max_pixels=160)
+    ang_max = synthetic.correlation_ang_max(60.0, float(fs.z.min()))
+    return fs, ow.make_params(0.0, 60.0, 60.0, 15, 15), ang_max
+
+
+def _wick_partial(fs, p, ang_max, forests_subset):
+    """The oracle's raw Wick sums over the kept forests in ``forests_subset``
+    (the per-forest draws made exactly as a single process makes them)."""
+    from conftest import golden
+    from oracle import cpu
+    from oracle import wick as ow
+    offsets, index = cpu.neighbours(fs, fs, cpu.make_params(0.0, 60.0, 60.0, 15, 15), ang_max,
+                                    auto_mode=1)
+    keep, npall, npused = ow.selection(fs, 2, 0.6)
+    variance, xi = ow.interpolants(golden("cf1d.npz"))
+    po = np.asarray(fs.pix_offset)
+    out = ow.new_outputs(p)
+
+    def forest(f):
+        sl = slice(po[f], po[f + 1])
+        return (fs.r_comov[sl], fs.weights[sl], ((1 + fs.z[sl]) / 3.25) ** 1.9,
+                ow.weighted_xi_1d(fs.log_lambda[sl], fs.weights[sl], variance, xi))
+
+    for f in np.nonzero(keep)[0]:
+        if f not in forests_subset:
+            continue
+        r1, w1, zw1, x1 = forest(f)
+        for k in range(int(offsets[f]), int(offsets[f + 1])):
+            g = int(index[k])
+            r2, w2, zw2, x2 = forest(g)
+            ang = cpu.lib().oracle_angle(fs.x_cart[f], fs.y_cart[f], fs.z_cart[f], fs.ra[f],
+                                         fs.dec[f], fs.cos_dec[f], fs.x_cart[g], fs.y_cart[g],
+                                         fs.z_cart[g], fs.ra[g], fs.dec[g])
+            ow.forest_pair(p, r1, w1, zw1, x1, r2, w2, zw2, x2, ang, out)
+    return out, npall, npused
+
+
+def _rank_wick(rank, world, port, out_path):
+    import sys
+    import torch.distributed as dist
+    from picca_gb300 import sharding
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    os.environ["MASTER_ADDR"] = "127.0.0.1"
+    os.environ["MASTER_PORT"] = str(port)
+    dist.init_process_group("gloo", rank=rank, world_size=world)
+    fs, p, ang_max = _wick_workload()
+    owned = sharding.assign_rows(sharding.row_costs(len(fs.healpix_list), fs.row,
+                                                    np.diff(fs.pix_offset)), world)
+    mine = set(int(f) for f in sharding.shard_forests(fs.row, owned[rank]))
+    raw, _, _ = _wick_partial(fs, p, ang_max, mine)
+    keys = ("weights_wick", "num_pairs_wick", "t1", "t2", "t3")
+    total = sharding.reduce_sums([raw[k] for k in keys])
+    if rank == 0:
+        np.savez(out_path, **dict(zip(keys, total)))
+    dist.barrier()
+    dist.destroy_process_group()
+
+
+def test_two_rank_wick_sums_equal_single_process(tmp_path):
+    """Kept forests split by healpix over two gloo ranks, partial Wick sums
+    reduced: the single-process sums (NB exact, FP64 sums to rounding)."""
+    import socket
+    import torch.multiprocessing as mp
+    with socket.socket() as s:
+        s.bind(("127.0.0.1", 0))
+        port = s.getsockname()[1]
+    out = str(tmp_path / "wick.npz")
+    mp.start_processes(_rank_wick, args=(2, port, out), nprocs=2, start_method="spawn")
+    fs, p, ang_max = _wick_workload()
+    ref, _, _ = _wick_partial(fs, p, ang_max, set(range(fs.num)))
+    got = np.load(out)
+    assert ref["num_pairs_wick"].sum() > 0
+    assert np.array_equal(got["num_pairs_wick"], ref["num_pairs_wick"])
+    for key in ("weights_wick", "t1", "t2", "t3"):
+        scale = np.abs(ref[key]).max()
+        assert np.all(np.abs(got[key] - ref[key]) <= 1e-12 * np.abs(ref[key]) + 1e-14 * scale)
