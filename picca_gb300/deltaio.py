@@ -13,8 +13,8 @@ into those arrays. The result is bit-identical to the per-object path
 """
 
 import ctypes
-import gzip
 import os
+import zlib
 from concurrent.futures import ThreadPoolExecutor
 
 import numpy as np
@@ -51,11 +51,23 @@ def _bind():
     return lib
 
 
+def gunzip(raw):
+    """Every gzip member of ``raw`` inflated (zlib checks each member's CRC
+    in C, without the GIL)."""
+    parts = []
+    while raw[:2] == b"\x1f\x8b":
+        d = zlib.decompressobj(wbits=31)
+        parts.append(d.decompress(raw))
+        parts.append(d.flush())
+        raw = d.unused_data
+    return b"".join(parts)
+
+
 def file_bytes(path):
     """A delta file's bytes, gunzipped when they carry the gzip magic."""
     with open(path, "rb") as handle:
         raw = handle.read()
-    return gzip.decompress(raw) if raw[:2] == b"\x1f\x8b" else raw
+    return gunzip(raw) if raw[:2] == b"\x1f\x8b" else raw
 
 
 def read_file(path, z_min_qso=0.0, z_max_qso=10.0):
@@ -135,18 +147,34 @@ def read_files(files, z_min_qso=0.0, z_max_qso=10.0, max_num_spec=None, threads=
 
 
 def make_deltas(arrays, order):
-    """Delta objects whose pixel arrays are views into ``arrays``."""
+    """Delta objects whose pixel arrays are views into ``arrays``. The
+    per-object trigonometry of QSO.__init__ (py/picca/data.py:60-104) is
+    evaluated once over all lines of sight (the same NumPy expressions,
+    elementwise), and the objects are filled without calling __init__."""
     po = arrays["pix_offset"]
+    num = len(po) - 1
+    ra, dec = arrays["ra"][:num], arrays["dec"][:num]
+    cos_ra, sin_ra = np.cos(ra), np.sin(ra)
+    cos_dec, sin_dec = np.cos(dec), np.sin(dec)
+    x_cart, y_cart = cos_ra * cos_dec, sin_ra * cos_dec
+    pix = {k: arrays[k] for k in ("z", "r_comov", "dist_m") if k in arrays}
     deltas = []
-    for f in range(len(po) - 1):
+    for f in range(num):
         sl = slice(po[f], po[f + 1])
-        d = Delta(int(arrays["los_id"][f]), float(arrays["ra"][f]), float(arrays["dec"][f]),
-                  float(arrays["z_qso"][f]), int(arrays["plate"][f]), int(arrays["mjd"][f]),
-                  int(arrays["fiberid"][f]), arrays["log_lambda"][sl], arrays["weights"][sl],
-                  arrays["cont"][sl], arrays["delta"][sl], order)
-        for key in ("z", "r_comov", "dist_m"):
-            if key in arrays:
-                setattr(d, key, arrays[key][sl])
+        los_id = int(arrays["los_id"][f])
+        d = Delta.__new__(Delta)
+        d.__dict__.update({
+            "ra": float(ra[f]), "dec": float(dec[f]), "plate": int(arrays["plate"][f]),
+            "mjd": int(arrays["mjd"][f]), "fiberid": int(arrays["fiberid"][f]),
+            "x_cart": x_cart[f], "y_cart": y_cart[f], "z_cart": sin_dec[f],
+            "cos_dec": cos_dec[f], "z_qso": float(arrays["z_qso"][f]), "los_id": los_id,
+            "thingid": los_id, "weight": None, "weights": arrays["weights"][sl],
+            "log_lambda": arrays["log_lambda"][sl], "cont": arrays["cont"][sl],
+            "delta": arrays["delta"][sl], "order": order, "ivar": None,
+            "exposures_diff": None, "mean_snr": None, "mean_reso": None, "mean_z": None,
+            "z": None, "r_comov": None, "dist_m": None, "neighbours": None, "fname": None})
+        for key, values in pix.items():
+            d.__dict__[key] = values[sl]
         deltas.append(d)
     return deltas
 
