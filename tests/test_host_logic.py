@@ -1,0 +1,64 @@
+"""Host-side logic of the newer rows (no GPU): how costly Wick work units
+are cut into slices, the absorber pairs of the fast metal script, and
+blinded delta files through both readers."""
+
+import os
+
+import numpy as np
+
+from picca_gb300 import constants, io
+
+
+def test_slice_units_cover_each_unit_once():
+    from picca_gb300 import wick
+    cost = np.array([10.0, 3.0e5, 4.5e4, 1.0, 8.0e4])
+    unit, sl, sls = wick.slice_units(cost)
+    for u in range(cost.size):
+        mine = np.nonzero(unit == u)[0]
+        assert mine.size == sls[mine[0]]
+        assert np.array_equal(np.sort(sl[mine]), np.arange(mine.size))
+    per = (cost * cost / np.clip(np.ceil(cost * cost / wick.SLICE_TARGET), 1,
+                                 wick.MAX_SLICES))[unit]
+    assert np.all(np.diff(per) <= 0)  # costliest slices first
+    assert sls.max() <= wick.MAX_SLICES
+
+
+def test_fast_metal_relevant_pairs():
+    from picca_gb300 import fast_metal
+    metals = ["SiII(1190)", "SiIII(1207)", "CIV(eff)", "SiII(1526)"]
+    pairs = fast_metal.absorber_pairs("LYA", metals, relevant=True)
+    # LYA with the four DEFAULT_SI_METALS present, and CIV(eff) with itself
+    # (py/picca/bin/picca_fast_metal_dmat.py:15, :571-575)
+    assert pairs == [("LYA", "SiII(1190)"), ("LYA", "SiIII(1207)"), ("CIV(eff)", "CIV(eff)")]
+    assert len(fast_metal.absorber_pairs("LYA", metals)) == 14
+
+
+def test_blinded_files_read_the_same(tmp_path):
+    from picca_gb300 import deltaio
+    rng = np.random.default_rng(8)
+    grid = 3.5563 + 3e-4 * np.arange(300)
+    nf = 12
+    lengths = rng.integers(40, 200, nf)
+    starts = rng.integers(0, 100, nf)
+    index = np.concatenate([np.arange(s, s + n) for s, n in zip(starts, lengths)])
+    po = np.concatenate([[0], np.cumsum(lengths)]).astype(np.int64)
+    n = int(po[-1])
+    arrays = {"los_id": np.arange(nf) + 40, "ra": rng.uniform(0, 0.05, nf),
+              "dec": rng.uniform(0, 0.05, nf), "z_qso": rng.uniform(2.3, 3.0, nf),
+              "healpix": np.zeros(nf, dtype=np.int64), "pix_offset": po,
+              "delta": rng.normal(0, 0.3, n), "weights": rng.uniform(0.5, 3.0, n),
+              "cont": rng.uniform(1.0, 2.0, n)}
+    cosmo = constants.Cosmo(Om=0.315, verbose=False)
+    for layout in ("ImageHDU", "BinTableHDU"):
+        out = tmp_path / layout
+        deltaio.write_deltas(str(out), arrays, grid, index, save_format=layout,
+                             blinding="desi_y1")
+        assert io.read_blinding(str(out / "Delta")) == "desi_y1"
+        args = (str(out / "Delta") + "/", 16, constants.ABSORBER_IGM["LYA"], 2.9, 2.25, cosmo)
+        got = io.read_deltas(*args, no_project=True, native=True)
+        want = io.read_deltas(*args, no_project=True, native=False)
+        assert got[1] == want[1] == nf
+        for hp in want[0]:
+            for a, b in zip(got[0][hp], want[0][hp]):
+                assert np.array_equal(a.delta, b.delta) and np.array_equal(a.weights, b.weights)
+        assert not os.path.exists(out / "Delta" / "delta-1.fits.gz")
