@@ -112,6 +112,27 @@ def project(pix_offset, log_lambda, weights, delta, order, threads=None):
                                         int(threads)), "delta projection")
 
 
+def per_pixel(func, arrays, threads=None, chunk=1 << 18):
+    """``func(*arrays)`` for an elementwise ``func`` of equal-length 1-D
+    arrays, evaluated on contiguous chunks in a thread pool (NumPy ufuncs and
+    ``np.interp`` release the GIL). Elementwise means chunking changes no
+    value: the result equals the one-call result bit for bit."""
+    n = len(arrays[0])
+    threads = threads or min(16, os.cpu_count() or 1)
+    if n <= chunk or threads == 1:
+        return np.asarray(func(*arrays), dtype=np.float64)
+    out = np.empty(n, dtype=np.float64)
+    edges = list(range(0, n, chunk)) + [n]
+
+    def run(k):
+        sl = slice(edges[k], edges[k + 1])
+        out[sl] = func(*(a[sl] for a in arrays))
+
+    with ThreadPoolExecutor(threads) as pool:
+        list(pool.map(run, range(len(edges) - 1)))
+    return out
+
+
 def read_files(files, z_min_qso=0.0, z_max_qso=10.0, max_num_spec=None, threads=None):
     """The files' arrays concatenated in file order (reading stops after the
     file that passes max_num_spec lines of sight, as io.read_deltas does)."""
@@ -119,7 +140,9 @@ def read_files(files, z_min_qso=0.0, z_max_qso=10.0, max_num_spec=None, threads=
     parts = []
     num = 0
     with ThreadPoolExecutor(threads) as pool:
-        step = max(threads, 1)
+        # without a cap every file is read: one queue keeps all threads busy;
+        # with one, files go in waves so that reading stops near the cap
+        step = len(files) if max_num_spec is None else max(threads, 1)
         for i in range(0, len(files), step):
             for part in pool.map(lambda f: read_file(f, z_min_qso, z_max_qso),
                                  files[i:i + step]):
@@ -157,24 +180,30 @@ def make_deltas(arrays, order):
     cos_ra, sin_ra = np.cos(ra), np.sin(ra)
     cos_dec, sin_dec = np.cos(dec), np.sin(dec)
     x_cart, y_cart = cos_ra * cos_dec, sin_ra * cos_dec
-    pix = {k: arrays[k] for k in ("z", "r_comov", "dist_m") if k in arrays}
+    pix = [(k, arrays[k]) for k in ("z", "r_comov", "dist_m") if k in arrays]
+    pix += [(k, arrays[k]) for k in ("weights", "log_lambda", "cont", "delta")]
+    # Python scalars and offsets as lists: one conversion per array instead
+    # of one NumPy scalar access per line of sight
+    bounds = po.tolist()
+    ra_l, dec_l, z_qso_l = ra.tolist(), dec.tolist(), arrays["z_qso"][:num].tolist()
+    plate_l, mjd_l = arrays["plate"][:num].tolist(), arrays["mjd"][:num].tolist()
+    fiber_l, los_l = arrays["fiberid"][:num].tolist(), arrays["los_id"][:num].tolist()
     deltas = []
     for f in range(num):
-        sl = slice(po[f], po[f + 1])
-        los_id = int(arrays["los_id"][f])
+        lo, hi = bounds[f], bounds[f + 1]
+        los_id = los_l[f]
         d = Delta.__new__(Delta)
-        d.__dict__.update({
-            "ra": float(ra[f]), "dec": float(dec[f]), "plate": int(arrays["plate"][f]),
-            "mjd": int(arrays["mjd"][f]), "fiberid": int(arrays["fiberid"][f]),
+        fields = {
+            "ra": ra_l[f], "dec": dec_l[f], "plate": plate_l[f],
+            "mjd": mjd_l[f], "fiberid": fiber_l[f],
             "x_cart": x_cart[f], "y_cart": y_cart[f], "z_cart": sin_dec[f],
-            "cos_dec": cos_dec[f], "z_qso": float(arrays["z_qso"][f]), "los_id": los_id,
-            "thingid": los_id, "weight": None, "weights": arrays["weights"][sl],
-            "log_lambda": arrays["log_lambda"][sl], "cont": arrays["cont"][sl],
-            "delta": arrays["delta"][sl], "order": order, "ivar": None,
+            "cos_dec": cos_dec[f], "z_qso": z_qso_l[f], "los_id": los_id,
+            "thingid": los_id, "weight": None, "order": order, "ivar": None,
             "exposures_diff": None, "mean_snr": None, "mean_reso": None, "mean_z": None,
-            "z": None, "r_comov": None, "dist_m": None, "neighbours": None, "fname": None})
-        for key, values in pix.items():
-            d.__dict__[key] = values[sl]
+            "z": None, "r_comov": None, "dist_m": None, "neighbours": None, "fname": None}
+        for key, values in pix:
+            fields[key] = values[lo:hi]
+        d.__dict__.update(fields)
         deltas.append(d)
     return deltas
 

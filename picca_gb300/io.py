@@ -200,7 +200,8 @@ def _read_deltas_native(files, in_dir, nside, lambda_abs, alpha, z_ref, cosmo, m
     if np.size(healpixs) == 0:
         raise AssertionError(f"ERROR: No data in {in_dir}")
     log_lambda = arrays["log_lambda"]
-    z = 10**log_lambda / lambda_abs - 1.
+    threads = nproc if nproc else None
+    z = deltaio.per_pixel(lambda ll: 10**ll / lambda_abs - 1., [log_lambda], threads)
     z_min = 10**log_lambda[0] / lambda_abs - 1.
     z_max = 0.
     if z.size:
@@ -208,9 +209,10 @@ def _read_deltas_native(files, in_dir, nside, lambda_abs, alpha, z_ref, cosmo, m
         z_max = max(z_max, z.max())
     arrays["z"] = z
     if cosmo is not None:
-        arrays["r_comov"] = cosmo.get_r_comov(z)
-        arrays["dist_m"] = cosmo.get_dist_m(z)
-    arrays["weights"] *= ((1 + z) / (1 + z_ref))**(alpha - 1)
+        arrays["r_comov"] = deltaio.per_pixel(cosmo.get_r_comov, [z], threads)
+        arrays["dist_m"] = deltaio.per_pixel(cosmo.get_dist_m, [z], threads)
+    arrays["weights"] = deltaio.per_pixel(
+        lambda w, zz: w * ((1 + zz) / (1 + z_ref))**(alpha - 1), [arrays["weights"], z], threads)
     if not no_project:
         if order is None:
             raise RuntimeError(

@@ -62,3 +62,19 @@ def test_blinded_files_read_the_same(tmp_path):
             for a, b in zip(got[0][hp], want[0][hp]):
                 assert np.array_equal(a.delta, b.delta) and np.array_equal(a.weights, b.weights)
         assert not os.path.exists(out / "Delta" / "delta-1.fits.gz")
+
+
+def test_per_pixel_chunks_match_one_call():
+    from picca_gb300 import deltaio
+    rng = np.random.default_rng(3)
+    ll = np.sort(rng.uniform(3.55, 3.75, 100_003))
+    w = rng.uniform(0.1, 5.0, ll.size)
+    cosmo = constants.Cosmo(Om=0.315, verbose=False)
+    z = 10**ll / 1215.67 - 1.
+    for chunk in (999, 4096):  # odd chunk: unaligned chunk starts
+        zc = deltaio.per_pixel(lambda a: 10**a / 1215.67 - 1., [ll], threads=4, chunk=chunk)
+        assert np.array_equal(zc, z)
+        assert np.array_equal(deltaio.per_pixel(cosmo.get_r_comov, [z], 4, chunk),
+                              cosmo.get_r_comov(z))
+        got = deltaio.per_pixel(lambda a, b: a * ((1 + b) / 3.25)**2.8, [w, z], 4, chunk)
+        assert np.array_equal(got, w * ((1 + z) / 3.25)**2.8)
