@@ -181,7 +181,16 @@ def _parse_header(raw, pos):
             if name == "END":
                 done = True
                 break
-            if card[8:10] == "= ":
+            if name == "HIERARCH" and "=" in card[9:]:
+                # ESO HIERARCH convention (cfitsio writes keywords longer than
+                # eight characters this way): "HIERARCH NAME = value / comment"
+                key, rest = card[9:].split("=", 1)
+                value_text, comment = _split_value_comment(rest)
+                value = _parse_value(value_text)
+                name = key.strip()
+                header[name] = value
+                header.record_list.append({"name": name, "value": value, "comment": comment})
+            elif card[8:10] == "= ":
                 value_text, comment = _split_value_comment(card[10:])
                 value = _parse_value(value_text)
                 header[name] = value
@@ -325,6 +334,8 @@ def _format_value(value):
 def _card(name, value=None, comment=""):
     if name in ("COMMENT", "HISTORY", ""):
         card = f"{name:<8}{str(value or '')}"
+    elif len(name) > 8:
+        card = f"HIERARCH {name} = {_format_value(value).strip()}"
     else:
         card = f"{name:<8}= {_format_value(value)}"
         if comment:

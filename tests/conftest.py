@@ -66,7 +66,9 @@ def write_image_dir(out_dir):
         meta_cols = [k for k in src if k.startswith(f"f{index}_META_")]
         path = os.path.join(out_dir, str(name))
         # image HDUs then a METADATA table: write both with the lite writers
-        images = [("LAMBDA", src[f"f{index}_LAMBDA"], [])]
+        lam_cards = [{"name": k.split("_HDR_", 1)[1], "value": src[k].item()}
+                     for k in src if k.startswith(f"f{index}_HDR_")]
+        images = [("LAMBDA", src[f"f{index}_LAMBDA"], lam_cards)]
         for key in ("DELTA", "WEIGHT", "CONT"):
             images.append((key, src[f"f{index}_{key}"], []))
         tmp_img = path + ".img"

@@ -1,5 +1,5 @@
 """The golden correlation cases of picca's own test-suite
-(py/picca/tests/test_3_cor.py:229-316, :458-488, :636-664, :791-1002), as
+(py/picca/tests/test_3_cor.py:229-316 including the rebinned image case, :458-488, :636-664, :791-1002), as
 (command-line arguments, host-side preparation) pairs shared by the oracle
 and GPU parity tests."""
 
@@ -25,6 +25,9 @@ CASES = {
         "--z-max-pairs", "2.3", "--z-min-sources", "2.3", "--z-max-sources", "2.5"]),
     "cf_image": dict(kind="cf", in_dir="Delta_LYA_image", args=[
         "--rp-min", "0.0", "--rp-max", "60.0", "--rt-max", "60.0", "--np", "15", "--nt", "15"]),
+    "cf_image_rebinned": dict(kind="cf", in_dir="Delta_LYA_image", args=[
+        "--rp-min", "0.0", "--rp-max", "60.0", "--rt-max", "60.0", "--np", "15", "--nt", "15",
+        "--rebin-factor", "3"]),
     "cf_image_zcuts": dict(kind="cf", in_dir="Delta_LYA_image", args=[
         "--rp-min", "0.0", "--rp-max", "60.0", "--rt-max", "60.0", "--np", "15", "--nt", "15",
         "--z-min-pairs", "2.25", "--z-max-pairs", "2.3", "--z-min-sources", "2.3",
@@ -86,7 +89,8 @@ def prepare(case, base):
         remove_same_half_plate_close_pairs="--remove-same-half-plate-close-pairs" in args)
     data, _, z_min, z_max = io.read_deltas(
         os.path.join(base, spec["in_dir"]) + "/", 16, constants.ABSORBER_IGM["LYA"], 2.9, 2.25,
-        cosmo, z_min_qso=z_min_src, z_max_qso=z_max_src, delta_attributes=attributes)
+        cosmo, z_min_qso=z_min_src, z_max_qso=z_max_src, delta_attributes=attributes,
+        rebin_factor=_opt(args, "--rebin-factor", None, int))
     if spec["kind"] == "cf":
         ang_max = utils.compute_ang_max(cosmo, params["r_trans_max"], z_min)
         set2 = None

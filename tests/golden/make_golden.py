@@ -88,6 +88,10 @@ def _convert_image_dir(src_dir, out_path):
         hdul = fitsio_lite.FITS(os.path.join(src_dir, name))
         meta = hdul["METADATA"]
         out[f"f{index}_LAMBDA"] = hdul["LAMBDA"][:]
+        lam_header = hdul["LAMBDA"].read_header()
+        for key in ("WAVE_SOLUTION", "DELTA_LAMBDA", "DELTA_LOG_LAMBDA"):
+            if key in lam_header:
+                out[f"f{index}_HDR_{key}"] = np.asarray(lam_header[key])
         for key in ("DELTA", "WEIGHT", "CONT"):
             out[f"f{index}_{key}"] = np.asarray(hdul[key].read(), dtype=float)
         for col in meta.get_colnames():
@@ -552,7 +556,7 @@ def main(picca_root):
                        os.path.join(HERE, "delta_lya_image.npz"))
     _convert_cat(os.path.join(tests, "test_delta", "cat.fits"), os.path.join(HERE, "cat.npz"))
     for case in ("cf", "cf_zcuts", "cf_cross", "cf_cross_zcuts", "cf_image",
-                 "cf_image_zcuts", "xcf", "xcf_zcuts"):
+                 "cf_image_rebinned", "cf_image_zcuts", "xcf", "xcf_zcuts"):
         _convert_cor(os.path.join(tests, "test_cor", case + ".fits.gz"),
                      os.path.join(HERE, f"cor_{case}.npz"))
     ncf, nxcf = _pair_cases(os.path.join(picca_root, "py"),
@@ -644,6 +648,17 @@ def extra_wick(picca_root):
         for key in ("NPALL", "NPUSED"):
             out["hdr_" + key] = np.asarray(header[key])
         np.savez_compressed(os.path.join(HERE, f"cor_{case}.npz"), **out)
+
+
+def extra_rebin(picca_root):
+    """The image-layout inputs with their LAMBDA header cards (WAVE_SOLUTION,
+    DELTA_LAMBDA: HIERARCH keywords), and picca's rebinned image-layout
+    correlation (py/picca/tests/test_3_cor.py:288-316)."""
+    tests = os.path.join(picca_root, "py", "picca", "tests", "data")
+    _convert_image_dir(os.path.join(tests, "test_delta", "Delta_LYA_image"),
+                       os.path.join(HERE, "delta_lya_image.npz"))
+    _convert_cor(os.path.join(tests, "test_cor", "cf_image_rebinned.fits.gz"),
+                 os.path.join(HERE, "cor_cf_image_rebinned.npz"))
 
 
 def extra_dmat(picca_root):
