@@ -70,10 +70,12 @@ def file_bytes(path):
     return gunzip(raw) if raw[:2] == b"\x1f\x8b" else raw
 
 
-def read_file(path, z_min_qso=0.0, z_max_qso=10.0):
+def read_file(path, z_min_qso=0.0, z_max_qso=10.0, rebin_factor=None):
     """One delta file as arrays: per line of sight (los_id, plate, mjd,
     fiberid, ra, dec, z_qso, pix_offset) and per pixel (log_lambda, delta,
-    weights, cont)."""
+    weights, cont). With ``rebin_factor`` the forests are rebinned as
+    py/picca/io.py:362-376 does (``rebin_arrays``); ``cont`` keeps the
+    original pixels, at ``cont_offset``."""
     lib = _bind()
     raw = file_bytes(path)
     buf = np.frombuffer(raw, dtype=np.uint8)
@@ -97,7 +99,76 @@ def read_file(path, z_min_qso=0.0, z_max_qso=10.0):
         arrays[k] = arrays[k][:npix]
     arrays["log_lambda"] = np.log10(arrays["wave"]) if out.wave_is_lambda else arrays["wave"]
     arrays["image"] = bool(out.format)
+    if rebin_factor is not None:
+        from . import fitsio_lite
+        headers = fitsio_lite.hdu_headers(raw)
+        card = headers[1]
+        if out.format:
+            card = next(h for h in headers if str(h.get("EXTNAME", "")).strip() == "LAMBDA")
+        if card["WAVE_SOLUTION"] != "lin":
+            raise ValueError("Delta rebinning only implemented for linear lambda bins")
+        arrays["cont_offset"] = arrays["pix_offset"]
+        (arrays["pix_offset"], arrays["log_lambda"], arrays["delta"],
+         arrays["weights"]) = rebin_arrays(arrays["pix_offset"], arrays["log_lambda"],
+                                           arrays["delta"], arrays["weights"], rebin_factor,
+                                           card["DELTA_LAMBDA"])
     return arrays
+
+
+def rebin_arrays(pix_offset, log_lambda, delta, weights, factor, dwave):
+    """Delta.rebin (py/picca/data.py:657-686) of every forest at once: the
+    wavelength bins of each forest start half a pixel below its bluest pixel
+    and are ``factor`` pixels wide; a pixel goes to the bin that
+    searchsorted(edges, wave) names, bins 1 .. num_bins - 1 are kept, and
+    those with weight are returned (weighted mean delta, summed weight, bin
+    centre). Every expression is the per-forest one evaluated elementwise,
+    and the bin sums are one bincount over all forests, which adds each
+    bin's pixels in the same order as the per-forest bincount: the result
+    is bit-identical to rebinning the forests one by one."""
+    po = np.asarray(pix_offset, dtype=np.int64)
+    n = np.diff(po)
+    nf = n.size
+    if nf == 0:
+        return po, log_lambda, delta, weights
+    if np.any(n == 0):
+        raise ValueError("zero-size array to reduction operation minimum which has no identity")
+    wave = 10**log_lambda
+    first, last = po[:-1], po[1:] - 1
+    start = np.minimum.reduceat(wave, first) - dwave / 2
+    num_bins = np.ceil(((wave[last] - wave[first]) / dwave + 1) / factor)
+    nb = num_bins.astype(np.int64)
+    eo = np.concatenate([[0], np.cumsum(nb)])
+    k = (np.arange(eo[-1]) - np.repeat(eo[:-1], nb)).astype(np.float64)
+    edges = k * dwave * factor + np.repeat(start, nb)
+    # searchsorted(edges, wave) per forest: the number of edges below each
+    # pixel, from a guess corrected against the edges themselves
+    fpix = np.repeat(np.arange(nf), n)
+    base, top = eo[fpix], nb[fpix]
+    idx = np.clip(np.floor((wave - start[fpix]) / (dwave * factor)).astype(np.int64) + 1, 0, top)
+    for _ in range(64):
+        down = (idx > 0) & (edges[base + np.maximum(idx - 1, 0)] >= wave)
+        up = (idx < top) & (edges[base + np.minimum(idx, top - 1)] < wave)
+        if not (down.any() or up.any()):
+            break
+        idx += up.astype(np.int64) - down.astype(np.int64)
+    else:
+        raise RuntimeError("rebinning: bin search did not settle")
+    seg = np.concatenate([[0], np.cumsum(nb + 1)])
+    gid = seg[fpix] + idx
+    binned_delta = np.bincount(gid, weights=delta * weights, minlength=seg[-1])
+    binned_weight = np.bincount(gid, weights=weights, minlength=seg[-1])
+    # bins 1 .. nb-1 of each forest, and the centres of those bins
+    local = np.arange(seg[-1]) - np.repeat(seg[:-1], nb + 1)
+    owner = np.repeat(np.arange(nf), nb + 1)
+    inner = (local >= 1) & (local <= nb[owner] - 1)
+    binned_delta, binned_weight = binned_delta[inner], binned_weight[inner]
+    right = eo[owner[inner]] + local[inner]
+    new_wave = (edges[right] + edges[right - 1]) / 2
+    mask = binned_weight != 0
+    binned_delta[mask] /= binned_weight[mask]
+    counts = np.bincount(owner[inner][mask], minlength=nf)
+    new_po = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    return new_po, np.log10(new_wave[mask]), binned_delta[mask], binned_weight[mask]
 
 
 def project(pix_offset, log_lambda, weights, delta, order, threads=None):
@@ -133,7 +204,8 @@ def per_pixel(func, arrays, threads=None, chunk=1 << 18):
     return out
 
 
-def read_files(files, z_min_qso=0.0, z_max_qso=10.0, max_num_spec=None, threads=None):
+def read_files(files, z_min_qso=0.0, z_max_qso=10.0, max_num_spec=None, threads=None,
+               rebin_factor=None):
     """The files' arrays concatenated in file order (reading stops after the
     file that passes max_num_spec lines of sight, as io.read_deltas does)."""
     threads = threads or min(16, os.cpu_count() or 1)
@@ -144,7 +216,7 @@ def read_files(files, z_min_qso=0.0, z_max_qso=10.0, max_num_spec=None, threads=
         # with one, files go in waves so that reading stops near the cap
         step = len(files) if max_num_spec is None else max(threads, 1)
         for i in range(0, len(files), step):
-            for part in pool.map(lambda f: read_file(f, z_min_qso, z_max_qso),
+            for part in pool.map(lambda f: read_file(f, z_min_qso, z_max_qso, rebin_factor),
                                  files[i:i + step]):
                 parts.append(part)
                 num += len(part["ra"])
@@ -158,14 +230,22 @@ def read_files(files, z_min_qso=0.0, z_max_qso=10.0, max_num_spec=None, threads=
                   else np.zeros(0, dtype=LOS_KEYS.get(k, np.float64)))
     counts = np.concatenate([np.diff(p["pix_offset"]) for p in parts]) if parts else \
         np.zeros(0, dtype=np.int64)
+    # cont keeps the pixels as read when the forests were rebinned
+    cont_key = "cont_offset" if rebin_factor is not None else "pix_offset"
+    cont_counts = np.concatenate([np.diff(p[cont_key]) for p in parts]) if parts else \
+        np.zeros(0, dtype=np.int64)
     if max_num_spec is not None and len(counts) > max_num_spec:
         counts = counts[:max_num_spec]
+        cont_counts = cont_counts[:max_num_spec]
         for k in LOS_KEYS:
             out[k] = out[k][:max_num_spec]
         npix = int(counts.sum())
-        for k in ("log_lambda", "delta", "weights", "cont"):
+        for k in ("log_lambda", "delta", "weights"):
             out[k] = out[k][:npix]
+        out["cont"] = out["cont"][:int(cont_counts.sum())]
     out["pix_offset"] = np.concatenate([[0], np.cumsum(counts)]).astype(np.int64)
+    if rebin_factor is not None:
+        out["cont_offset"] = np.concatenate([[0], np.cumsum(cont_counts)]).astype(np.int64)
     return out
 
 
@@ -181,10 +261,11 @@ def make_deltas(arrays, order):
     cos_dec, sin_dec = np.cos(dec), np.sin(dec)
     x_cart, y_cart = cos_ra * cos_dec, sin_ra * cos_dec
     pix = [(k, arrays[k]) for k in ("z", "r_comov", "dist_m") if k in arrays]
-    pix += [(k, arrays[k]) for k in ("weights", "log_lambda", "cont", "delta")]
+    pix += [(k, arrays[k]) for k in ("weights", "log_lambda", "delta")]
     # Python scalars and offsets as lists: one conversion per array instead
     # of one NumPy scalar access per line of sight
     bounds = po.tolist()
+    cont, cont_bounds = arrays["cont"], arrays.get("cont_offset", po).tolist()
     ra_l, dec_l, z_qso_l = ra.tolist(), dec.tolist(), arrays["z_qso"][:num].tolist()
     plate_l, mjd_l = arrays["plate"][:num].tolist(), arrays["mjd"][:num].tolist()
     fiber_l, los_l = arrays["fiberid"][:num].tolist(), arrays["los_id"][:num].tolist()
@@ -203,6 +284,7 @@ def make_deltas(arrays, order):
             "z": None, "r_comov": None, "dist_m": None, "neighbours": None, "fname": None}
         for key, values in pix:
             fields[key] = values[lo:hi]
+        fields["cont"] = cont[cont_bounds[f]:cont_bounds[f + 1]]
         d.__dict__.update(fields)
         deltas.append(d)
     return deltas

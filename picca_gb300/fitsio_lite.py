@@ -228,6 +228,25 @@ def _bintable_dtype(header):
     return np.dtype(fields)
 
 
+def hdu_headers(raw):
+    """The header of every HDU of an uncompressed FITS byte string, without
+    reading any data."""
+    pos = 0
+    headers = []
+    while pos < len(raw) and raw[pos:pos + BLOCK].strip(b"\x00 "):
+        header, pos = _parse_header(raw, pos)
+        naxis = header["NAXIS"]
+        nbytes = 0
+        if naxis > 0:
+            nbytes = abs(header["BITPIX"]) // 8
+            for i in range(1, naxis + 1):
+                nbytes *= header[f"NAXIS{i}"]
+        nbytes += header.get("PCOUNT", 0) or 0
+        headers.append(header)
+        pos += (nbytes + BLOCK - 1) // BLOCK * BLOCK
+    return headers
+
+
 def read_hdus(path):
     """Read every HDU of a (possibly gzip-compressed) FITS file."""
     raw = _read_raw(path)

@@ -95,18 +95,18 @@ def read_deltas(in_dir, nside, lambda_abs, alpha, z_ref, cosmo,
 
     Same contract as py/picca/io.py:383-512: returns (data, num_data, z_min,
     z_max) with ``data = {healpix: [Delta, ...]}``. ``native`` (default)
-    parses the files and projects the deltas in the native library
-    (``picca_gb300.deltaio``, bit-identical); rebinning uses the per-object
-    readers below.
+    parses, rebins and projects the deltas in the native library and
+    vectorised NumPy (``picca_gb300.deltaio``, bit-identical to the
+    per-object readers below).
     """
     files = _list_delta_files(in_dir)
     order = find_order(in_dir, delta_attributes)
-    if native and rebin_factor is None:
+    if native:
         from ._native import NativeError, PG_ERR_UNSUPPORTED
         try:
             return _read_deltas_native(files, in_dir, nside, lambda_abs, alpha, z_ref, cosmo,
                                        max_num_spec, no_project, nproc, z_min_qso, z_max_qso,
-                                       order)
+                                       order, rebin_factor)
         except NativeError as err:
             if getattr(err, "status", None) != PG_ERR_UNSUPPORTED:
                 raise
@@ -188,12 +188,12 @@ def read_drq(drq_filename, z_min=0, z_max=10., keep_bal=False, bi_max=None,
 
 
 def _read_deltas_native(files, in_dir, nside, lambda_abs, alpha, z_ref, cosmo, max_num_spec,
-                        no_project, nproc, z_min_qso, z_max_qso, order):
+                        no_project, nproc, z_min_qso, z_max_qso, order, rebin_factor=None):
     """read_deltas through the native parser and projection: the per-pixel
     expressions of the per-object path, evaluated once over all pixels."""
     from . import deltaio
     arrays = deltaio.read_files(files, z_min_qso, z_max_qso, max_num_spec,
-                                threads=nproc if nproc else None)
+                                threads=nproc if nproc else None, rebin_factor=rebin_factor)
     num_data = len(arrays["ra"])
     ra, dec = arrays["ra"], arrays["dec"]
     healpixs = ang2pix_ring(nside, np.pi / 2. - dec, ra)

@@ -154,3 +154,47 @@ def test_text_identifiers_use_per_object_reader(tmp_path):
     for hp in want[0]:
         for a, b in zip(got[0][hp], want[0][hp]):
             assert np.array_equal(a.delta, b.delta) and a.plate == b.plate
+
+
+@pytest.mark.parametrize("kwargs", [{"rebin_factor": 3}, {"rebin_factor": 2, "max_num_spec": 300},
+                                    {"rebin_factor": 5, "no_project": True}])
+def test_native_rebinning_matches_per_object(dirs, kwargs):
+    """--rebin-factor on the image layout (linear wavelength grid)."""
+    attr = os.path.join(dirs, "attr1.fits.gz")
+    cosmo = constants.Cosmo(Om=0.315, verbose=False)
+    args = (os.path.join(dirs, "Delta_LYA_image") + "/", 16, constants.ABSORBER_IGM["LYA"], 2.9,
+            2.25, cosmo)
+    got = io.read_deltas(*args, delta_attributes=attr, native=True, **kwargs)
+    want = io.read_deltas(*args, delta_attributes=attr, native=False, **kwargs)
+    assert got[1] == want[1] and got[2] == want[2] and got[3] == want[3]
+    same_sets(ForestSet.from_deltas(got[0]), ForestSet.from_deltas(want[0]))
+    for hp in want[0]:
+        for a, b in zip(got[0][hp], want[0][hp]):
+            assert np.array_equal(a.cont, b.cont)
+
+
+def test_rebin_arrays_matches_delta_rebin():
+    from picca_gb300 import deltaio
+    from picca_gb300.data import Delta
+    rng = np.random.default_rng(12)
+    sizes = [1, 2, 3, 7, 40, 333, 600]
+    lls, ws, ds = [], [], []
+    for n in sizes:
+        start = 3600.0 + 0.8 * rng.integers(0, 500)
+        pix = np.sort(rng.choice(np.arange(3 * n), n, replace=False))  # gaps
+        lls.append(np.log10(start + 0.8 * pix))
+        w = rng.uniform(0.1, 3.0, n)
+        w[rng.random(n) < 0.2] = 0.0  # bins whose pixels all have no weight
+        ws.append(w)
+        ds.append(rng.normal(0, 0.3, n))
+    po = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    for factor in (1, 2, 3, 4):
+        new_po, ll, d, w = deltaio.rebin_arrays(po, np.concatenate(lls), np.concatenate(ds),
+                                                np.concatenate(ws), factor, 0.8)
+        for f in range(len(sizes)):
+            obj = Delta(1, 0.1, 0.2, 2.5, 1, 1, 1, lls[f].copy(), ws[f].copy(), None,
+                        ds[f].copy(), 1)
+            obj.rebin(factor, dwave=0.8)
+            sl = slice(new_po[f], new_po[f + 1])
+            assert np.array_equal(ll[sl], obj.log_lambda), (factor, sizes[f])
+            assert np.array_equal(d[sl], obj.delta) and np.array_equal(w[sl], obj.weights)
