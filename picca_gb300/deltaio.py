@@ -302,7 +302,10 @@ def write_deltas(out_dir, arrays, log_lambda_grid, grid_index, save_format="Imag
     MEANSNR; BLINDING), DELTA (DELTA_BLIND when blinded), WEIGHT and CONT
     images over the grid, NaN outside each forest. ``BinTableHDU``: one table
     per line of sight (LAMBDA or LOGLAM, DELTA, WEIGHT, CONT; header LOS_ID,
-    RA, DEC, Z, BLINDING). Returns the paths written."""
+    RA, DEC, Z, MEANSNR, BLINDING, WAVE_SOLUTION and the pixel step, as
+    Forest.get_header writes them,
+    py/picca/delta_extraction/astronomical_objects/forest.py:551-610).
+    Returns the paths written."""
     from . import fitsio_lite
     os.makedirs(os.path.join(out_dir, "Delta"), exist_ok=True)
     po = np.asarray(arrays["pix_offset"], dtype=np.int64)
@@ -311,6 +314,9 @@ def write_deltas(out_dir, arrays, log_lambda_grid, grid_index, save_format="Imag
     index = np.asarray(grid_index, dtype=np.int64)
     mean_snr = np.asarray(arrays.get("mean_snr", np.zeros(len(healpix))), dtype=np.float64)
     delta_name = "DELTA" if blinding == "none" else "DELTA_BLIND"
+    step = [{"name": "DELTA_LOG_LAMBDA", "value": round(grid[1] - grid[0], 2)}] \
+        if wave_solution == "log" else \
+        [{"name": "DELTA_LAMBDA", "value": round(10**grid[1] - 10**grid[0], 2)}]
     paths = []
     for hp in np.unique(healpix):
         members = np.nonzero(healpix == hp)[0]
@@ -322,9 +328,6 @@ def write_deltas(out_dir, arrays, log_lambda_grid, grid_index, save_format="Imag
                 sl = slice(po[f], po[f + 1])
                 for k in images:
                     images[k][row, index[sl]] = arrays[k][sl]
-            step = [{"name": "DELTA_LOG_LAMBDA", "value": round(grid[1] - grid[0], 2)}] \
-                if wave_solution == "log" else \
-                [{"name": "DELTA_LAMBDA", "value": round(10**grid[1] - 10**grid[0], 2)}]
             meta = {"columns": [np.asarray(arrays["los_id"])[members].astype(np.int64),
                                 np.asarray(arrays["ra"])[members],
                                 np.asarray(arrays["dec"])[members],
@@ -356,7 +359,8 @@ def write_deltas(out_dir, arrays, log_lambda_grid, grid_index, save_format="Imag
                                {"name": "DEC", "value": float(arrays["dec"][f])},
                                {"name": "Z", "value": float(arrays["z_qso"][f])},
                                {"name": "MEANSNR", "value": float(mean_snr[f])},
-                               {"name": "BLINDING", "value": blinding}]})
+                               {"name": "BLINDING", "value": blinding},
+                               {"name": "WAVE_SOLUTION", "value": wave_solution}] + step})
             fitsio_lite.write_fits(path, tables)
         else:
             raise ValueError(f"Invalid format {save_format}; expected ImageHDU or BinTableHDU")

@@ -120,6 +120,17 @@ def test_writer_round_trip(tmp_path, save_format, wave):
     per_object = [d for path in files for d in io.read_delta_file(path)]
     assert [d.los_id for d in per_object] == list(got["los_id"])
     assert np.array_equal(np.concatenate([d.delta for d in per_object]), got["delta"])
+    # rebinning reads WAVE_SOLUTION / DELTA_LAMBDA (HIERARCH cards) back
+    if wave == "lin":
+        rebinned = deltaio.read_files(files, rebin_factor=3)
+        per_object = [d for path in files for d in io.read_delta_file(path, rebin_factor=3)]
+        for key in ("log_lambda", "delta", "weights"):
+            assert np.array_equal(np.concatenate([getattr(d, key) for d in per_object]),
+                                  rebinned[key]), key
+        assert rebinned["log_lambda"].size < got["log_lambda"].size
+    else:
+        with pytest.raises(ValueError):
+            deltaio.read_files(files, rebin_factor=3)
 
 
 def test_text_identifiers_use_per_object_reader(tmp_path):
