@@ -209,3 +209,29 @@ def test_rebin_arrays_matches_delta_rebin():
             sl = slice(new_po[f], new_po[f + 1])
             assert np.array_equal(ll[sl], obj.log_lambda), (factor, sizes[f])
             assert np.array_equal(d[sl], obj.delta) and np.array_equal(w[sl], obj.weights)
+
+
+def test_rebin_arrays_jittered_wavelengths():
+    """Pixels off the nominal grid (up to half a pixel), so that many fall
+    next to a bin edge: the bin search must agree with searchsorted."""
+    from picca_gb300 import deltaio
+    from picca_gb300.data import Delta
+    rng = np.random.default_rng(21)
+    sizes = rng.integers(1, 300, 60)
+    lls, ws, ds = [], [], []
+    for n in sizes:
+        wave = 3700.0 + 0.8 * np.arange(n) + rng.uniform(-0.45, 0.45, n) * 0.8
+        lls.append(np.log10(np.sort(wave)))
+        ws.append(rng.uniform(0.1, 3.0, n))
+        ds.append(rng.normal(0, 0.3, n))
+    po = np.concatenate([[0], np.cumsum(sizes)]).astype(np.int64)
+    for factor in (1, 2, 7):
+        new_po, ll, d, w = deltaio.rebin_arrays(po, np.concatenate(lls), np.concatenate(ds),
+                                                np.concatenate(ws), factor, 0.8)
+        for f in range(len(sizes)):
+            obj = Delta(1, 0.1, 0.2, 2.5, 1, 1, 1, lls[f].copy(), ws[f].copy(), None,
+                        ds[f].copy(), 1)
+            obj.rebin(factor, dwave=0.8)
+            sl = slice(new_po[f], new_po[f + 1])
+            assert np.array_equal(ll[sl], obj.log_lambda), (factor, f)
+            assert np.array_equal(d[sl], obj.delta) and np.array_equal(w[sl], obj.weights)
