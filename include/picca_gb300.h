@@ -179,8 +179,10 @@ int pg_xcf_xi(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *
  * (held by every GPU that loads the library until exit). All calls on a
  * device share that array: calls that overlap on the GPU race and give
  * wrong results. The first call with a device current looks up the
- * array's address and should come before any stream capture. The call
- * synchronises `stream` and returns the kernel's device-side status;
+ * array's address (once per device). The call is synchronous: it
+ * synchronises `stream` and copies the kernel's device-side status back
+ * with a blocking cudaMemcpy, so it must not be called while `stream` (or
+ * any stream) is being captured into a CUDA graph. Returns that status;
  * PG_ERR_UNSUPPORTED if the scratch would not fit in the array. */
 #define PG_STATIC_SCRATCH_BYTES 4096
 int pg_cf_xi_static(const pg_corr_params *params, const pg_forest_set *s1,

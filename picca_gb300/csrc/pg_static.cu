@@ -21,8 +21,9 @@
 //    stream are safe: this function synchronises the stream before it
 //    returns;
 //  - its device address is looked up once per device by the first call made
-//    with that device current (cudaGetSymbolAddress); that first call should
-//    come before any stream capture.
+//    with that device current (cudaGetSymbolAddress).
+// The call is synchronous (stream synchronise, then a blocking copy of the
+// status word), so it cannot be issued inside a CUDA graph capture.
 #include <mutex>
 
 #include "pg_internal.cuh"

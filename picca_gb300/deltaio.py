@@ -290,6 +290,25 @@ def make_deltas(arrays, order):
     return deltas
 
 
+def pixel_step_records(grid, wave_solution):
+    """Header records of the pixel step for the two delta layouts.
+
+    The image layout rounds the step to two decimals
+    (py/picca/delta_extraction/data.py:97-108); the table layout writes it
+    unrounded (Forest.get_header,
+    py/picca/delta_extraction/astronomical_objects/forest.py:580-601), and
+    the rebinning of the reader takes it from there. Returns
+    (image records, table records)."""
+    grid = np.asarray(grid, dtype=np.float64)
+    if wave_solution == "log":
+        name, value = "DELTA_LOG_LAMBDA", grid[1] - grid[0]
+    elif wave_solution == "lin":
+        name, value = "DELTA_LAMBDA", 10**grid[1] - 10**grid[0]
+    else:
+        raise ValueError(f"Invalid wave_solution {wave_solution}; expected 'lin' or 'log'")
+    return [{"name": name, "value": round(float(value), 2)}], [{"name": name, "value": float(value)}]
+
+
 def write_deltas(out_dir, arrays, log_lambda_grid, grid_index, save_format="ImageHDU",
                  wave_solution="log", blinding="none", flux_units="10**-17 erg/(s cm2 Angstrom)"):
     """Delta files of delta_extraction (py/picca/delta_extraction/data.py:62-265):
@@ -314,9 +333,7 @@ def write_deltas(out_dir, arrays, log_lambda_grid, grid_index, save_format="Imag
     index = np.asarray(grid_index, dtype=np.int64)
     mean_snr = np.asarray(arrays.get("mean_snr", np.zeros(len(healpix))), dtype=np.float64)
     delta_name = "DELTA" if blinding == "none" else "DELTA_BLIND"
-    step = [{"name": "DELTA_LOG_LAMBDA", "value": round(grid[1] - grid[0], 2)}] \
-        if wave_solution == "log" else \
-        [{"name": "DELTA_LAMBDA", "value": round(10**grid[1] - 10**grid[0], 2)}]
+    step_image, step_table = pixel_step_records(grid, wave_solution)
     paths = []
     for hp in np.unique(healpix):
         members = np.nonzero(healpix == hp)[0]
@@ -338,7 +355,7 @@ def write_deltas(out_dir, arrays, log_lambda_grid, grid_index, save_format="Imag
             fitsio_lite.write_hdus(path, [
                 ("image", "LAMBDA", 10**grid,
                  [{"name": "BUNIT", "value": "Angstrom"},
-                  {"name": "WAVE_SOLUTION", "value": wave_solution}] + step),
+                  {"name": "WAVE_SOLUTION", "value": wave_solution}] + step_image),
                 ("table", meta),
                 ("image", delta_name, images["delta"], [{"name": "BUNIT", "value": ""}]),
                 ("image", "WEIGHT", images["weights"], []),
@@ -360,7 +377,7 @@ def write_deltas(out_dir, arrays, log_lambda_grid, grid_index, save_format="Imag
                                {"name": "Z", "value": float(arrays["z_qso"][f])},
                                {"name": "MEANSNR", "value": float(mean_snr[f])},
                                {"name": "BLINDING", "value": blinding},
-                               {"name": "WAVE_SOLUTION", "value": wave_solution}] + step})
+                               {"name": "WAVE_SOLUTION", "value": wave_solution}] + step_table})
             fitsio_lite.write_fits(path, tables)
         else:
             raise ValueError(f"Invalid format {save_format}; expected ImageHDU or BinTableHDU")

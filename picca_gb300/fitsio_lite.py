@@ -355,6 +355,12 @@ def _card(name, value=None, comment=""):
         card = f"{name:<8}{str(value or '')}"
     elif len(name) > 8:
         card = f"HIERARCH {name} = {_format_value(value).strip()}"
+        if len(card) > CARD:
+            raise ValueError(f"HIERARCH card for {name!r} needs {len(card)} characters "
+                             f"(a card holds {CARD})")
+        if comment and len(card) + 3 + len(comment) <= CARD:
+            card += f" / {comment}"
+        return card.ljust(CARD)
     else:
         card = f"{name:<8}= {_format_value(value)}"
         if comment:

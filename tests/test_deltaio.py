@@ -101,6 +101,18 @@ def test_writer_round_trip(tmp_path, save_format, wave):
     deltaio.write_deltas(str(tmp_path), arrays, grid, index, save_format=save_format,
                          wave_solution=wave)
     files = sorted(str(p) for p in (tmp_path / "Delta").iterdir())
+    # the pixel step as picca writes it: unrounded in the table layout
+    # (Forest.get_header, delta_extraction/astronomical_objects/forest.py:580-601),
+    # rounded to two decimals in the image layout (delta_extraction/data.py:97-108)
+    from picca_gb300 import fitsio_lite
+    exact = (grid[1] - grid[0]) if wave == "log" else (10**grid[1] - 10**grid[0])
+    key = "DELTA_LOG_LAMBDA" if wave == "log" else "DELTA_LAMBDA"
+    headers = fitsio_lite.hdu_headers(deltaio.file_bytes(files[0]))
+    step_header = headers[1]
+    if save_format == "ImageHDU":
+        step_header = next(h for h in headers if str(h.get("EXTNAME", "")).strip() == "LAMBDA")
+    assert step_header[key] == (round(exact, 2) if save_format == "ImageHDU" else exact)
+    assert step_header["WAVE_SOLUTION"] == wave
     got = deltaio.read_files(files)
     # forests come back grouped by healpix file, in file order
     order = np.concatenate([np.nonzero(arrays["healpix"] == hp)[0]
@@ -235,3 +247,21 @@ def test_rebin_arrays_jittered_wavelengths():
             sl = slice(new_po[f], new_po[f + 1])
             assert np.array_equal(ll[sl], obj.log_lambda), (factor, f)
             assert np.array_equal(d[sl], obj.delta) and np.array_equal(w[sl], obj.weights)
+
+
+def test_hierarch_cards():
+    """Keywords longer than eight characters are written as HIERARCH cards:
+    the comment is kept when the card has room for it, and a card that
+    cannot hold its value is refused instead of being cut."""
+    from picca_gb300 import fitsio_lite
+    card = fitsio_lite._card("DELTA_LAMBDA", 0.7999999999997272, "pixel step")
+    assert len(card) == 80
+    assert card.rstrip().endswith("/ pixel step")
+    header, _ = fitsio_lite._parse_header(fitsio_lite._header_bytes([card]), 0)
+    assert header["DELTA_LAMBDA"] == 0.7999999999997272
+    long_text = "x" * 60
+    with pytest.raises(ValueError):
+        fitsio_lite._card("A_VERY_LONG_KEYWORD", long_text)
+    # a comment that does not fit is dropped, the value is kept whole
+    card = fitsio_lite._card("WAVE_SOLUTION", "lin", "c" * 70)
+    assert "'lin" in card and "/" not in card
