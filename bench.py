@@ -5,13 +5,18 @@ lists of every forest + pair accumulation into per-healpix rows (the work of
 ``cf.fill_neighs`` + ``cf.compute_xi`` over every healpix,
 py/picca/bin/picca_cf.py:452-458). ``value`` is candidate pixel pairs per
 second with inputs resident in HBM; ``e2e`` is the same through the public
-host API (pinned host arrays uploaded, rows read back, every step).
+drop-in ``cf.compute_xi_all`` from host ``Delta`` objects (packing, pinned
+upload, neighbours, pairs, rows and neighbour lists back), every e2e step.
 
-Default workload: the 100k-forest auto-correlation on 2,000 deg^2 (50 x 50
-bins, r_par and r_trans 0-200 Mpc/h, precision form); ``--config 2`` runs the
-400k-forest survey on 8,000 deg^2 and ``--config 0`` the 1,000-forest patch. ``--impl reference``
-times the CPU oracle (FP64 C restatement of picca's numba kernel, OpenMP over
-all host cores) on a bounded sample of the same workload.
+Default workload: the 400k-forest auto-correlation on 8,000 deg^2 (50 x 50
+bins, r_par and r_trans 0-200 Mpc/h, precision form), with the
+cross-correlation of the same forests against 600k quasars (100 x 50 bins,
+r_par -200 to 200) as the ``xcf`` object and the Dr16 continuum fit (plain
+and learned warm start, 400k raw forests) as the ``continuum`` object.
+``--config 1`` / ``1lin`` run the 100k-forest survey (log or 0.8 A linear
+grid), ``--config 0`` the 1,000-forest patch. ``--impl reference`` times the
+CPU oracle (FP64 C restatement of picca's numba kernel, OpenMP over all host
+cores) on a bounded sample of the same workload.
 """
 
 import argparse
@@ -37,10 +42,11 @@ CONFIGS = {
 }
 METRIC = "cf pixel-pairs/s at stated FP64-oracle error; continuum fits/s plain vs learned"
 # DRAM bytes (read + write) of the pair kernel per candidate pixel pair, from
-# one ncu capture on 1,000 random work items of the 100k-forest survey (5.533 GB read +
-# 0.114 GB written for 2.628e10 candidate pairs; see profiles/); the roofline
-# entry scales it to the launch by the candidate pairs processed
-PAIR_DRAM_BYTES_PER_CANDIDATE = (5.532826e9 + 0.113620e9) / 26284549581
+# an ncu capture of the kernel on a sample of work items (profiles/); the
+# roofline entry scales it to the launch by the candidate pairs processed.
+# None until the diagonal-sweep kernel has been captured.
+PAIR_DRAM_BYTES_PER_CANDIDATE = None
+PAIR_TRAFFIC_SOURCE = "not captured for this kernel yet"
 
 
 def parse():
@@ -49,7 +55,7 @@ def parse():
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=3)
     p.add_argument("--impl", choices=["ours", "reference"], default="ours")
-    p.add_argument("--config", default="1", choices=sorted(CONFIGS))
+    p.add_argument("--config", default="2", choices=sorted(CONFIGS))
     p.add_argument("--precision", choices=["fp32_guard", "fp64"], default="fp32_guard")
     p.add_argument("--check-fraction", type=float, default=0.01,
                    help="fraction of work items re-run in FP64 for the error report")
@@ -63,8 +69,11 @@ def parse():
     p.add_argument("--profile-items", type=int, default=0,
                    help="profiling aid: run the pair kernel once on this many randomly chosen "
                         "work items of the workload and exit (no timing, no JSON line)")
-    p.add_argument("--large-survey", action="store_true",
-                   help="also run the 400k-forest auto and 600k-quasar cross correlations")
+    p.add_argument("--legs", default="xcf,continuum",
+                   help="comma-separated extra legs: xcf, continuum, dmat, wick, delta_io "
+                        "(dmat and wick also run alone with --dmat-only / --wick-only)")
+    p.add_argument("--e2e-steps", type=int, default=2,
+                   help="steps of the end-to-end leg through cf.compute_xi_all")
     p.add_argument("--dmat-reject", type=float, default=0.99,
                    help="random rejection of the distortion-matrix leg (picca_dmat.py --rej); "
                         "a value >= 1 skips the leg")
@@ -938,66 +947,194 @@ def continuum_leg(args, cpu_seconds):
     }
 
 
-def large_survey_leg(args):
-    """The 400k-forest auto-correlation on 8,000 deg^2 and the
-    cross-correlation with 600k quasars on the same band (r_par -200..200 in
-    100 bins x r_trans 0..200 in 50), both in the precision form; each kernel
-    timed once after a warm-up run, with its error against the plain FP64
-    kernel on 0.5% of the work items."""
+def survey_quasars(cfg, fs):
+    """Quasar catalogue of a workload: 600k on the 8,000 deg^2 band (75 per
+    deg^2, the forests' z law), 1.5 per forest otherwise, same area."""
+    from picca_gb300 import synthetic
+    num, area, _, _ = CONFIGS[cfg]
+    if area is None:  # the patch of the CPU-runnable case
+        ra_r = tuple(np.degrees([np.min(fs.ra), np.max(fs.ra)]))
+        dec_r = tuple(np.degrees([np.min(fs.dec), np.max(fs.dec)]))
+    else:
+        ra_r, dec_r = synthetic.band_for_area(area, 20.0 if area <= 4000 else 30.0)
+    return synthetic.make_quasars(int(1.5 * num), 20261207, ra_r, dec_r)
+
+
+def xcf_cpu_sample(fs, qs, p_or, ang_max, seconds):
+    """The CPU oracle's xcf (neighbours + pixel-quasar pairs) on a bounded
+    random sample of forests with all their quasars, on every host core.
+    Returns (candidate pixel-quasar pairs/s, description, threads)."""
+    from oracle import cpu as oracle
+    rng = np.random.default_rng(11)
+    cores = os.cpu_count() or 1
+    npix = np.diff(fs.pix_offset)
+    per_forest = float(np.mean(npix)) * 2500.0
+    n = int(max(cores, min(fs.num, seconds * 1.5e8 * cores / per_forest)))
+    sample = np.sort(rng.choice(fs.num, size=min(n, fs.num), replace=False))
+    sub = fs.take(sample)
+    t0 = time.perf_counter()
+    offsets, index = oracle.neighbours(sub, qs, p_or, ang_max, auto_mode=0, xcf=True)
+    oracle.rows(sub, qs, p_or, offsets, index, xcf=True)
+    elapsed = time.perf_counter() - t0
+    cand = int((npix[sample] * np.diff(offsets)).sum())
+    return cand / elapsed, (f"{len(sample)} random forests with all their quasars, C "
+                            f"restatement of xcf.compute_xi_forest_pairs_fast; {elapsed:.1f} s"), cores
+
+
+def xcf_leg(args, fs, ang_max, steps, warmup):
+    """The delta x quasar cross-correlation of the same forests (picca_xcf.py:
+    r_par -200 to 200 in 100 bins x r_trans 0-200 in 50), precision form: a
+    step is quasar neighbours + pixel-quasar pairs of the whole survey. Per
+    bin error against the plain FP64 kernel on 1% of the forests, FP32
+    roofline of the pair kernel, and the CPU oracle on a sample."""
     import torch
 
-    from picca_gb300 import pairs, synthetic
-    fs = synthetic.survey_band(400_000, 8000.0, seed=20261206)
-    ra_r, dec_r = synthetic.band_for_area(8000.0, 30.0)
-    qs = synthetic.make_quasars(600_000, 20261207, ra_r, dec_r)
-    ang_max = synthetic.correlation_ang_max(200.0, float(fs.z.min()))
+    from oracle import cpu as oracle
+    from picca_gb300 import pairs
+    qs = survey_quasars(args.config, fs)
+    kw = dict(r_par_min=-200.0, r_par_max=200.0, r_trans_max=200.0, num_bins_r_par=100,
+              num_bins_r_trans=50)
+    params = pairs.make_params(ang_max=ang_max, x_correlation=True, **kw)
+    engine = pairs.PairEngine()
+    d1 = pairs.DeviceForests(fs, engine.device)
+    d2 = pairs.DeviceForests(qs, engine.device)
+    nrows, nbins = len(fs.healpix_list), 5000
     stream = torch.cuda.current_stream()
-    out = {}
-    for name, xcf in (("auto", False), ("xcf", True)):
-        kw = (dict(r_par_min=-200.0, r_par_max=200.0, r_trans_max=200.0, num_bins_r_par=100,
-                   num_bins_r_trans=50, x_correlation=True) if xcf else
-              dict(r_par_min=0.0, r_par_max=200.0, r_trans_max=200.0, num_bins_r_par=50,
-                   num_bins_r_trans=50))
-        params = pairs.make_params(ang_max=ang_max, **kw)
-        engine = pairs.PairEngine()
-        d1 = pairs.DeviceForests(fs, engine.device)
-        d2 = pairs.DeviceForests(qs, engine.device) if xcf else None
-        offsets, index, total = engine.neighbours(params, d1, d2, xcf=xcf)
-        order, num_work, cand = engine.work_order(d1, d2, offsets, index, total, xcf=xcf)
-        nbins = kw["num_bins_r_par"] * kw["num_bins_r_trans"]
-        times = []
-        for _ in range(2):
-            rows = engine.alloc_rows(len(fs.healpix_list), nbins)
-            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-            e0.record(stream)
-            engine.accumulate(params, d1, d2, offsets, index, order, num_work, rows,
-                              pairs.MODE_FP32_GUARD, xcf=xcf)
-            e1.record(stream)
-            torch.cuda.synchronize()
-            times.append(e0.elapsed_time(e1) / 1e3)
-        n_check = max(1, num_work // 200)
-        sub = order[:num_work][torch.randperm(num_work, device=order.device)[:n_check]]
-        sub = sub.contiguous()
-        r32 = engine.alloc_rows(len(fs.healpix_list), nbins)
-        r64 = engine.alloc_rows(len(fs.healpix_list), nbins)
-        engine.accumulate(params, d1, d2, offsets, index, sub, n_check, r32,
-                          pairs.MODE_FP32_GUARD, xcf=xcf)
-        engine.accumulate(params, d1, d2, offsets, index, sub, n_check, r64, pairs.MODE_FP64,
-                          xcf=xcf)
-        torch.cuda.synchronize()
-        a = [r.cpu().numpy() for r in r32]
-        b = [r.cpu().numpy() for r in r64]
-        nz = b[0] > 0
-        out[name] = {
-            "forests": fs.num, "quasars": qs.num if xcf else None, "bins": nbins,
-            "candidate_pairs": int(cand), "kernel_s": times[-1],
-            "pairs_per_s": cand / times[-1], "nb_identical_on_sample": bool(
-                np.array_equal(a[5], b[5])),
-            "we_max_rel_on_sample": float(np.max(np.abs(a[0][nz] - b[0][nz]) / b[0][nz]))
-            if nz.any() else None}
-        del engine, d1, d2, offsets, index, order, rows, r32, r64
-        torch.cuda.empty_cache()
+
+    def step(kern=None):
+        offsets, index, total = engine.neighbours(params, d1, d2, xcf=True)
+        order, num_work, cand = engine.work_order(d1, d2, offsets, index, total, xcf=True)
+        rows = engine.alloc_rows(nrows, nbins)
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        engine.accumulate(params, d1, d2, offsets, index, order, num_work, rows,
+                          pairs.MODE_FP32_GUARD, xcf=True)
+        e1.record(stream)
+        if kern is not None:
+            kern.append((e0, e1))
+        return rows, cand, (offsets, index, order, num_work)
+
+    for _ in range(warmup):
+        step()
+    torch.cuda.synchronize()
+    kern = []
+    t0 = torch.cuda.Event(enable_timing=True)
+    t1 = torch.cuda.Event(enable_timing=True)
+    t0.record(stream)
+    for _ in range(steps):
+        rows, cand, work = step(kern)
+    t1.record(stream)
+    torch.cuda.synchronize()
+    elapsed = t0.elapsed_time(t1) / 1e3
+    kmean = float(np.mean([a.elapsed_time(b) / 1e3 for a, b in kern]))
+    accepted = int(rows[5].sum().item())
+    check = precision_check(engine, params, d1, d2, work, nrows, nbins, args.check_fraction,
+                            xcf=True)
+    pk, source = peaks()
+    sms = torch.cuda.get_device_properties(0).multi_processor_count
+    fp32_peak = sms * 128 * 2 * pk.get("sm_max_mhz", 2070.0) * 1e6 / 1e12
+    flops = 10.0 * cand + 9.0 * accepted
+    p_or = oracle.make_params(**kw, x_correlation=True)
+    cpu_val, cpu_desc, cores = xcf_cpu_sample(fs, qs, p_or, ang_max, min(args.cpu_seconds, 10.0))
+    out = {
+        "metric": "xcf candidate pixel-quasar pairs per second (precision form)",
+        "value": cand * steps / elapsed, "unit": "pixel-quasar-pairs/s",
+        "steps": steps, "warmup": warmup, "ms_per_step": elapsed / steps * 1e3,
+        "config": {"workload": f"{fs.num} forests x {qs.num} quasars, r_par -200 to 200 "
+                               "(100 bins) x r_trans 0-200 (50 bins) Mpc/h",
+                   "candidate_pixel_quasar_pairs_per_step": int(cand),
+                   "accepted_pairs_per_step": accepted},
+        "roofline": {"bound": "fp32", "achieved": flops / kmean / 1e12, "peak": fp32_peak,
+                     "unit": "TFLOP/s", "frac": flops / kmean / 1e12 / fp32_peak,
+                     "traffic": None, "kernel_ms": kmean * 1e3,
+                     "peak_source": f"SMs x 128 FP32 lanes x 2 x sm_max_mhz ({source} peaks file)"},
+        "precision_check_vs_fp64_kernel": check,
+        "cpu_baseline": {"value": cpu_val, "unit": "pixel-quasar-pairs/s", "cores": cores,
+                         "kind": "port", "sample": cpu_desc},
+    }
+    del engine, d1, d2
+    torch.cuda.empty_cache()
     return out
+
+
+def precision_check(engine, params, d1, d2, work, nrows, nbins, fraction, xcf=False):
+    """The precision form against the plain all-FP64 kernel on a random
+    `fraction` of the work items: pair counts, per-bin relative errors of
+    xi, the weights and the r_par / r_trans / z sums (bins with pairs), and
+    both kernels' rates on the sample."""
+    import torch
+
+    from picca_gb300 import pairs
+    offsets, index, order, num_work = work
+    n_check = max(1, int(num_work * fraction))
+    gen = torch.Generator(device=order.device).manual_seed(3)
+    sub = order[:num_work][torch.randperm(num_work, device=order.device,
+                                          generator=gen)[:n_check]].contiguous()
+    sample_cand = int(engine.last_cost[sub.long()].sum().item())
+    stream = torch.cuda.current_stream()
+    r32 = engine.alloc_rows(nrows, nbins)
+    r64 = engine.alloc_rows(nrows, nbins)
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+    ev[0].record(stream)
+    engine.accumulate(params, d1, d2, offsets, index, sub, n_check, r32, pairs.MODE_FP32_GUARD,
+                      xcf=xcf)
+    ev[1].record(stream)
+    ev[2].record(stream)
+    engine.accumulate(params, d1, d2, offsets, index, sub, n_check, r64, pairs.MODE_FP64, xcf=xcf)
+    ev[3].record(stream)
+    torch.cuda.synchronize()
+    fast_s = ev[0].elapsed_time(ev[1]) / 1e3
+    fp64_s = ev[2].elapsed_time(ev[3]) / 1e3
+    a = [r.cpu().numpy() for r in r32]
+    b = [r.cpu().numpy() for r in r64]
+    has = b[5] > 0
+
+    def rel(k):
+        return np.abs(a[k][has] - b[k][has]) / np.maximum(np.abs(b[k][has]), 1e-300)
+
+    def norm_abs(k):  # the normalised mean (sum / weights): r_par, r_trans in Mpc/h, z
+        return np.abs(a[k][has] / a[0][has] - b[k][has] / b[0][has])
+
+    xi = rel(1)
+    xi_n = np.abs(a[1][has] / a[0][has] - b[1][has] / b[0][has]) / np.maximum(
+        np.abs(b[1][has] / b[0][has]), 1e-300)
+    return {
+        "work_items_checked": int(n_check), "bins_with_pairs": int(has.sum()),
+        "nb_identical": bool(np.array_equal(a[5], b[5])),
+        "xi_max_rel": float(xi.max()), "xi_p99_rel": float(np.percentile(xi, 99)),
+        "xi_median_rel": float(np.median(xi)),
+        "xi_normalised_max_rel": float(xi_n.max()),
+        "we_max_rel": float(rel(0).max()), "we_p99_rel": float(np.percentile(rel(0), 99)),
+        "r_par_max_abs_mpc": float(norm_abs(2).max()),
+        "r_trans_max_abs_mpc": float(norm_abs(3).max()), "z_max_abs": float(norm_abs(4).max()),
+        "sample_candidate_pixel_pairs": sample_cand,
+        "precision_form_pairs_per_s_on_sample": sample_cand / fast_s,
+        "plain_fp64_kernel_pairs_per_s_on_sample": sample_cand / fp64_s,
+        "precision_form_over_fp64_kernel": fp64_s / fast_s,
+    }
+
+
+def delta_dict(fs):
+    """{healpix: [Delta]} of a ForestSet (what picca_cf.py holds after
+    reading the delta files): objects whose pixel arrays are views into the
+    set's arrays, in the set's order."""
+    from picca_gb300 import deltaio
+    arrays = {"pix_offset": np.asarray(fs.pix_offset), "ra": fs.ra, "dec": fs.dec,
+              "z_qso": fs.z_qso, "plate": fs.plate, "mjd": np.zeros(fs.num, dtype=np.int64),
+              "fiberid": fs.fiberid, "los_id": fs.thingid, "z": fs.z, "r_comov": fs.r_comov,
+              "dist_m": fs.dist_m, "weights": fs.weights, "log_lambda": fs.log_lambda,
+              "delta": fs.delta, "cont": np.ones(fs.num_pixels)}
+    deltas = deltaio.make_deltas(arrays, 1)
+    out = {}
+    for hp, d in zip(np.asarray(fs.healpix).tolist(), deltas):
+        out.setdefault(hp, []).append(d)
+    return out
+
+
+def reference_step_seconds(args):
+    """CPU time of one reference step: the whole --steps/--warmup run stays
+    within a few minutes."""
+    return float(min(args.cpu_seconds, max(2.0, 150.0 / max(args.steps, 1))))
 
 
 def run_reference(args):
@@ -1005,12 +1142,13 @@ def run_reference(args):
     if rank != 0:
         return
     fs, params, ang_max = make_workload(args.config)
+    seconds = reference_step_seconds(args)
     vals = []
     for _ in range(args.warmup):
-        cpu_sample(fs, params, ang_max, min(5.0, args.cpu_seconds), args.config)
+        cpu_sample(fs, params, ang_max, min(2.0, seconds), args.config)
     desc, cores = "", 1
     for _ in range(args.steps):
-        v, desc, cores = cpu_sample(fs, params, ang_max, args.cpu_seconds, args.config)
+        v, desc, cores = cpu_sample(fs, params, ang_max, seconds, args.config)
         vals.append(v)
     value = float(np.median(vals))
     line = {
@@ -1018,14 +1156,19 @@ def run_reference(args):
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
         "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": CONFIGS[args.config][3], "bins": "50x50",
+        "config": {"workload": workload_name(args.config), "bins": "50x50",
                    "r_par": "0-200", "r_trans": "0-200"},
         "cpu_baseline": {"value": value, "unit": "pixel-pairs/s", "cores": cores,
-                         "kind": "port", "sample": desc},
+                         "kind": "port", "sample": desc + " (median over steps)"},
         "e2e": {"value": value, "unit": "pixel-pairs/s", "h2d_bytes_per_step": 0,
                 "d2h_bytes_per_step": 0},
     }
     print(json.dumps(line), flush=True)
+
+
+def workload_name(cfg):
+    return (CONFIGS[cfg][3] + ", auto-correlation 50x50 bins, r_par 0-200, r_trans 0-200 "
+            "Mpc/h")
 
 
 def run_ours(args):
@@ -1055,6 +1198,7 @@ def run_ours(args):
         if rank == 0:
             print(json.dumps(dmat_leg(args, fs, params, ang_max, args.cpu_seconds)), flush=True)
         return
+    legs = set(x for x in args.legs.split(",") if x)
     mode = pairs.MODE_FP32_GUARD if args.precision == "fp32_guard" else pairs.MODE_FP64
     cparams = pairs.make_params(ang_max=ang_max, **params)
     engine = pairs.PairEngine()
@@ -1085,12 +1229,7 @@ def run_ours(args):
         n = min(args.profile_items, num_work)
         sub = order[:num_work][torch.randperm(num_work, device=order.device,
                                               generator=gen)[:n]].contiguous()
-        npix = torch.diff(dev.tensors["pix_offset"])
-        sub_l = sub.long()
-        cand = 0
-        for f in sub_l.tolist():
-            nb = index[offsets[f]:offsets[f + 1]].long()
-            cand += int(npix[f].item()) * int(npix[nb].sum().item())
+        cand = int(engine.last_cost[sub.long()].sum().item())
         rows = engine.alloc_rows(num_rows, nbins)
         engine.accumulate(cparams, dev, None, offsets, index, sub, n, rows, mode)
         torch.cuda.synchronize()
@@ -1126,80 +1265,59 @@ def run_ours(args):
         elapsed = float(t.item())
     pairs_per_step = cands[0]
     value = pairs_per_step * args.steps * world / elapsed
+    accepted = int(rows[5].sum().item())
 
-    # end to end through the host API: pinned upload, compute, rows back
+    # FP64 error report on a sample of work items (plain FP64 kernel vs ours)
+    check = {}
+    if mode != pairs.MODE_FP64 and args.check_fraction > 0:
+        check = precision_check(engine, cparams, dev, None, work, num_rows, nbins,
+                                args.check_fraction)
+    offsets_w = index_w = order_w = None
+    del work, rows, offsets_w, index_w, order_w
+    num_pixels, resident_bytes = int(dev.num_pixels), int(dev.h2d_bytes)
+    del dev, packed
+    torch.cuda.empty_cache()
+
+    # end to end through the drop-in cf module: {healpix: [Delta]} on the
+    # host -> packing, pinned upload, neighbours, pairs, rows and neighbour
+    # lists back, every step
+    from picca_gb300 import cf as cfmod
+    data = delta_dict(fs)
+    cfmod.data, cfmod.data2 = data, None
+    cfmod.r_par_min, cfmod.r_par_max = params["r_par_min"], params["r_par_max"]
+    cfmod.r_trans_max = params["r_trans_max"]
+    cfmod.num_bins_r_par, cfmod.num_bins_r_trans = params["num_bins_r_par"], params["num_bins_r_trans"]
+    cfmod.z_min_pairs = cfmod.z_max_pairs = cfmod.zerr_cut_deg = cfmod.zerr_cut_kms = None
+    cfmod.ang_max, cfmod.nside = ang_max, 16
+    cfmod.x_correlation = cfmod.rmu_binning = cfmod.ang_correlation = False
+    cfmod.remove_same_half_plate_close_pairs = False
+    cfmod.precision = args.precision
     barrier()
-    e2e_t0 = time.perf_counter()
+    e2e_steps = max(1, args.e2e_steps)
     h2d = d2h = 0
-    for _ in range(args.steps):
-        dev_e = pairs.DeviceForests(fs, engine.device, packed=packed)
-        rows_e, _, _, _ = step(device_forests=dev_e)
-        host_rows = [r.cpu() for r in rows_e]
-        h2d = dev_e.h2d_bytes
-        d2h = sum(int(r.numel() * r.element_size()) for r in host_rows)
+    e2e_t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        cfmod._cache["key"] = None
+        cfmod._cache["result"] = None
+        res_e = cfmod.compute_xi_all()
+        h2d, d2h = res_e["h2d_bytes"], res_e["d2h_bytes"]
     torch.cuda.synchronize()
     e2e_elapsed = time.perf_counter() - e2e_t0
+    e2e_cand = res_e["candidate_pairs"]
+    e2e_nb_same = None
+    del res_e
+    cfmod._cache["result"] = None
+    cfmod.data = None
+    del data
     if world > 1:
         t = torch.tensor([e2e_elapsed], device="cuda")
         dist.all_reduce(t, op=dist.ReduceOp.MAX)
         e2e_elapsed = float(t.item())
-    e2e_value = pairs_per_step * args.steps * world / e2e_elapsed
-
-    # FP64 error report on a sample of work items (plain FP64 kernel vs ours)
-    offsets, index, order, num_work = work
-    n_check = max(1, int(num_work * args.check_fraction))
-    check = {}
-    if n_check > 0 and mode != pairs.MODE_FP64:
-        sub_order = order[:num_work][torch.randperm(num_work, device=order.device)[:n_check]]
-        sub_order = sub_order.contiguous()
-        r32 = engine.alloc_rows(num_rows, nbins)
-        r64 = engine.alloc_rows(num_rows, nbins)
-        sample_cand = int(engine.last_cost[sub_order.long()].sum().item())
-        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
-        ev[0].record(stream)
-        engine.accumulate(cparams, dev, None, offsets, index, sub_order, n_check, r32, mode)
-        ev[1].record(stream)
-        ev[2].record(stream)
-        engine.accumulate(cparams, dev, None, offsets, index, sub_order, n_check, r64,
-                          pairs.MODE_FP64)
-        ev[3].record(stream)
-        torch.cuda.synchronize()
-        fast_s = ev[0].elapsed_time(ev[1]) / 1e3
-        fp64_s = ev[2].elapsed_time(ev[3]) / 1e3
-        # the scale of xi's rounding: sum of |delta1 w1 delta2 w2| per bin (FP64 kernel on |delta|)
-        packed_abs = dict(packed)
-        packed_abs["delta"] = np.abs(np.asarray(packed["delta"]))
-        dev_abs = pairs.DeviceForests(fs, engine.device, packed=packed_abs)
-        rabs = engine.alloc_rows(num_rows, nbins)
-        engine.accumulate(cparams, dev_abs, None, offsets, index, sub_order, n_check, rabs,
-                          pairs.MODE_FP64)
-        torch.cuda.synchronize()
-        a = [r.cpu().numpy() for r in r32]
-        b = [r.cpu().numpy() for r in r64]
-        abs_sum = rabs[1].cpu().numpy()
-        del dev_abs, rabs, packed_abs
-        nz = b[0] > 0
-        rel_we = np.abs(a[0][nz] - b[0][nz]) / b[0][nz]
-        rel_xi = np.abs(a[1][nz] - b[1][nz]) / np.maximum(np.abs(b[1][nz]), 1e-300)
-        err_abs = np.abs(a[1][nz] - b[1][nz]) / np.maximum(abs_sum[nz], 1e-300)
-        xi_sum = np.abs(a[1].sum() - b[1].sum()) / abs(b[1].sum())
-        check = {
-            "work_items_checked": int(n_check), "nb_identical": bool(np.array_equal(a[5], b[5])),
-            "we_max_rel": float(rel_we.max()), "we_median_rel": float(np.median(rel_we)),
-            "xi_err_over_abs_sum_max": float(err_abs.max()),
-            "xi_err_over_abs_sum_median": float(np.median(err_abs)),
-            "xi_median_rel": float(np.median(rel_xi)),
-            "xi_p99_rel": float(np.percentile(rel_xi, 99)),
-            "xi_total_rel": float(xi_sum),
-            "sample_candidate_pixel_pairs": sample_cand,
-            "precision_form_pairs_per_s_on_sample": sample_cand / fast_s,
-            "plain_fp64_kernel_pairs_per_s_on_sample": sample_cand / fp64_s,
-        }
+    e2e_value = e2e_cand * e2e_steps * world / e2e_elapsed
 
     # roofline of the pair kernel (FP32 CUDA-core bound)
     pk, source = peaks()
     sms = torch.cuda.get_device_properties(0).multi_processor_count
-    accepted = int(rows[5].sum().item())
     flops = 10.0 * pairs_per_step + 9.0 * accepted
     kmean = float(np.mean(kernel_s))
     achieved = flops / kmean / 1e12
@@ -1209,55 +1327,56 @@ def run_ours(args):
     if rank != 0:
         return
     cpu_val, cpu_desc, cores = cpu_sample(fs, params, ang_max, args.cpu_seconds, args.config)
-    num_pixels, resident_bytes = int(dev.num_pixels), int(dev.h2d_bytes)
-    del dev, packed, engine
+    del engine
     torch.cuda.empty_cache()
-    dm = dmat_leg(args, fs, params, ang_max, args.cpu_seconds)
-    print("dmat leg: " + json.dumps(dm), file=sys.stderr, flush=True)
-    wk = wick_leg(args, fs, params, ang_max)
-    print("wick leg: " + json.dumps(wk), file=sys.stderr, flush=True)
-    dio = delta_io_leg(fs)
-    print("delta io leg: " + json.dumps(dio), file=sys.stderr, flush=True)
-    cont = continuum_leg(args, args.cpu_seconds)
-    cfg2 = large_survey_leg(args) if args.large_survey else None
-    print("continuum leg: " + json.dumps(cont), file=sys.stderr, flush=True)
+    extra = {}
+    if "xcf" in legs:
+        extra["xcf"] = xcf_leg(args, fs, ang_max, min(args.steps, 5), min(args.warmup, 2))
+        print("xcf leg: " + json.dumps(extra["xcf"]), file=sys.stderr, flush=True)
+    if "dmat" in legs:
+        extra["dmat"] = dmat_leg(args, fs, params, ang_max, args.cpu_seconds)
+        print("dmat leg: " + json.dumps(extra["dmat"]), file=sys.stderr, flush=True)
+    if "wick" in legs:
+        extra["wick"] = wick_leg(args, fs, params, ang_max)
+        print("wick leg: " + json.dumps(extra["wick"]), file=sys.stderr, flush=True)
+    if "delta_io" in legs:
+        extra["delta_io"] = delta_io_leg(fs)
+        print("delta io leg: " + json.dumps(extra["delta_io"]), file=sys.stderr, flush=True)
+    if "continuum" in legs:
+        extra["continuum"] = continuum_leg(args, args.cpu_seconds)
+        print("continuum leg: " + json.dumps(extra["continuum"]), file=sys.stderr, flush=True)
     line = {
         "metric": METRIC, "value": value, "unit": "pixel-pairs/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": elapsed / args.steps * 1e3,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64guard"
         if mode != pairs.MODE_FP64 else "f64", "data": "synthetic",
-        "config": {"workload": CONFIGS[args.config][3] + ", auto-correlation 50x50 bins, "
-                   "r_par 0-200, r_trans 0-200 Mpc/h", "forests": fs.num,
+        "config": {"workload": workload_name(args.config), "forests": fs.num,
                    "pixels": num_pixels, "forest_pairs": int(total),
                    "candidate_pixel_pairs_per_step": int(pairs_per_step),
                    "accepted_pixel_pairs_per_step": accepted, "precision": args.precision,
                    "l2": "inputs larger than L2 (%.1f GB resident)" % (resident_bytes / 1e9),
                    "parallelism": f"replicas x{world}"},
         "e2e": {"value": e2e_value, "unit": "pixel-pairs/s", "h2d_bytes_per_step": int(h2d),
-                "d2h_bytes_per_step": int(d2h)},
+                "d2h_bytes_per_step": int(d2h), "steps": e2e_steps,
+                "path": "cf.compute_xi_all from {healpix: [Delta]} host objects (packing, "
+                        "pinned upload, neighbours, pairs, rows and neighbour lists back)"},
         "gpu_launches": launches_per_step * args.steps,
         "roofline": {"bound": "fp32", "achieved": achieved, "peak": fp32_peak,
                      "unit": "TFLOP/s", "frac": achieved / fp32_peak,
                      "traffic": PAIR_DRAM_BYTES_PER_CANDIDATE * pairs_per_step
-                     if args.config in ("1", "2") else None,
-                     "traffic_source": "ncu capture of 1,000 config-1 work items, scaled by "
-                                       "candidate pairs",
+                     if PAIR_DRAM_BYTES_PER_CANDIDATE else None,
+                     "traffic_source": PAIR_TRAFFIC_SOURCE,
                      "kernel_ms": kmean * 1e3,
                      "peak_source": f"SMs x 128 FP32 lanes x 2 x sm_max_mhz ({source} peaks file)",
                      "flops_per_launch": flops},
         "precision_check_vs_fp64_kernel": check,
         "rechecked_pairs_last_step": int(stats.rechecked_pairs),
-        "evaluated_pixel_pair_slots_last_step": int(stats.visited_pairs),
+        "evaluated_pixel_pairs_last_step": int(stats.visited_pairs),
         "clocks": clocks,
         "cpu_baseline": {"value": cpu_val, "unit": "pixel-pairs/s", "cores": cores,
                          "kind": "port", "sample": cpu_desc},
-        "continuum": cont,
-        "dmat": dm,
-        "wick": wk,
-        "delta_io": dio,
     }
-    if cfg2 is not None:
-        line["large_survey"] = cfg2
+    line.update(extra)
     print(json.dumps(line), flush=True)
     if world > 1:
         dist.destroy_process_group()

@@ -18,6 +18,9 @@
  * Reference interfaces replaced (picca v9.21.0):
  *  - pg_cf_neighbours   <- cf.fill_neighs            py/picca/cf.py:82-135
  *  - pg_xcf_neighbours  <- xcf.fill_neighs           py/picca/xcf.py:71-123
+ *  - pg_cf_neighbours_grouped / pg_xcf_neighbours_grouped <- the same, with
+ *                          the query_disc candidate healpix (cf.py:105-122,
+ *                          xcf.py:92-101) as groups of the sorted sets
  *  - pg_cf_xi           <- cf.compute_xi + cf.compute_xi_forest_pairs_fast
  *                          py/picca/cf.py:138-247, :250-387
  *  - pg_xcf_xi          <- xcf.compute_xi + xcf.compute_xi_forest_pairs_fast
@@ -121,8 +124,9 @@ typedef struct pg_run_stats {
     int64_t work_items;         /* work items processed                        */
     int64_t gemm_macs;          /* pg_cf_dmat: multiply-adds of the per-pair
                                    products of the eta terms               */
-    int64_t visited_pairs;      /* FP32_GUARD cf: pixel-pair slots evaluated
-                                   (after the per-block pixel windows)         */
+    int64_t visited_pairs;      /* FP32_GUARD cf: lane steps of the diagonal
+                                   sweeps (pixel pairs evaluated, idle lanes
+                                   included)                                   */
 } pg_run_stats;
 
 typedef struct pg_plan pg_plan;
@@ -153,6 +157,38 @@ int pg_cf_neighbours(pg_plan *plan, const pg_corr_params *params, const pg_fores
 int pg_xcf_neighbours(pg_plan *plan, const pg_corr_params *params,
                       const pg_forest_set *forests, const pg_forest_set *objs,
                       int64_t *counts, const int64_t *offsets, int32_t *index, void *stream);
+
+/* Groups of two forest sets for the grouped neighbour search (the
+ * healpix-by-healpix candidate selection of cf.fill_neighs, cf.py:105-122,
+ * which asks healpy.query_disc for the healpix near each forest). The
+ * query set's objects are grouped into consecutive ranges; blocks
+ * [block_first[b], block_end[b]) (at most 256 queries each) all belong to
+ * group block_group[b] and every query belongs to exactly one block. The
+ * other set's group g holds objects [start2[g], start2[g+1]) (start2
+ * non-decreasing). cand_groups[cand_offsets[G] .. cand_offsets[G+1]) lists,
+ * in increasing order, every group of the other set that can hold a
+ * neighbour of a query of group G (a superset is fine: each object is still
+ * tested exactly). All arrays are device pointers. */
+typedef struct pg_nbr_groups {
+    int32_t num_groups1, num_groups2, num_blocks, reserved;
+    const int64_t *start2;        /* [num_groups2 + 1] */
+    const int32_t *cand_offsets;  /* [num_groups1 + 1] */
+    const int32_t *cand_groups;   /* [cand_offsets[num_groups1]] */
+    const int32_t *block_group;   /* [num_blocks] */
+    const int64_t *block_first;   /* [num_blocks] */
+    const int64_t *block_end;     /* [num_blocks] */
+} pg_nbr_groups;
+
+/* pg_cf_neighbours / pg_xcf_neighbours restricted to candidate groups (same
+ * protocol, same results and order when the groups cover every neighbour). */
+int pg_cf_neighbours_grouped(pg_plan *plan, const pg_corr_params *params,
+                             const pg_forest_set *s1, const pg_forest_set *s2,
+                             const pg_nbr_groups *groups, int64_t *counts,
+                             const int64_t *offsets, int32_t *index, void *stream);
+int pg_xcf_neighbours_grouped(pg_plan *plan, const pg_corr_params *params,
+                              const pg_forest_set *forests, const pg_forest_set *objs,
+                              const pg_nbr_groups *groups, int64_t *counts,
+                              const int64_t *offsets, int32_t *index, void *stream);
 
 /* Accumulate the pair sums of forests s1[work_order[k]] (k < num_work; NULL
  * work_order: 0..num_work-1) with their neighbours in s2 (NULL: s1) into

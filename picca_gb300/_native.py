@@ -52,6 +52,14 @@ class ForestSetC(ctypes.Structure):
                 + [("num_rows", ctypes.c_int32), ("max_pixels", ctypes.c_int32)])
 
 
+class NbrGroupsC(ctypes.Structure):
+    _fields_ = ([("num_groups1", ctypes.c_int32), ("num_groups2", ctypes.c_int32),
+                 ("num_blocks", ctypes.c_int32), ("reserved", ctypes.c_int32)]
+                + [(name, ctypes.c_void_p) for name in
+                   ("start2", "cand_offsets", "cand_groups", "block_group", "block_first",
+                    "block_end")])
+
+
 class XiRowsC(ctypes.Structure):
     _fields_ = [(name, ctypes.c_void_p) for name in
                 ("weights", "xi", "r_par", "r_trans", "z", "num_pairs")]
@@ -99,6 +107,10 @@ def lib():
         ctypes.c_void_p, _P(CorrParams), _P(ForestSetC), _P(ForestSetC), ctypes.c_void_p,
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
     handle.pg_xcf_neighbours.argtypes = handle.pg_cf_neighbours.argtypes
+    handle.pg_cf_neighbours_grouped.argtypes = [
+        ctypes.c_void_p, _P(CorrParams), _P(ForestSetC), _P(ForestSetC), _P(NbrGroupsC),
+        ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+    handle.pg_xcf_neighbours_grouped.argtypes = handle.pg_cf_neighbours_grouped.argtypes
     handle.pg_cf_xi.argtypes = [
         ctypes.c_void_p, _P(CorrParams), _P(ForestSetC), _P(ForestSetC), ctypes.c_void_p,
         ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64, ctypes.c_int32,
@@ -121,7 +133,7 @@ def lib():
                                                             ctypes.c_uint64, _P(DmatSumsC),
                                                             ctypes.c_void_p]
     for name in ("pg_plan_create", "pg_plan_destroy", "pg_plan_stats", "pg_cf_neighbours",
-                 "pg_xcf_neighbours", "pg_cf_xi", "pg_xcf_xi", "pg_cf_dmat_work_bytes",
+                 "pg_xcf_neighbours", "pg_cf_neighbours_grouped", "pg_xcf_neighbours_grouped", "pg_cf_xi", "pg_xcf_xi", "pg_cf_dmat_work_bytes",
                  "pg_cf_dmat", "pg_xcf_dmat_work_bytes", "pg_xcf_dmat"):
         getattr(handle, name).restype = ctypes.c_int
     _LIB = handle

@@ -135,7 +135,7 @@ def compute_xi_all():
     _check_fiberids(fs1)
     if fs2 is not None:
         _check_fiberids(fs2)
-    res = _pairs.correlate(fs1, fs2, _params(), mode=_mode(), engine=_engine())
+    res = _pairs.correlate(fs1, fs2, _params(), mode=_mode(), engine=_engine(), pinned=True)
     we, xi, rp, rt, zz, nb = res["raw"]
     xi_n, rp_n, rt_n, zz_n = _pairs.normalise(we, xi, rp, rt, zz)
     index = res["index"].cpu().numpy()[: res["num_pairs_forest"]]
@@ -145,7 +145,8 @@ def compute_xi_all():
         "r_trans": rt_n, "z": zz_n, "num_pairs": nb, "raw": res["raw"],
         "candidate_pairs": res["candidate_pairs"], "rechecked_pairs": res["rechecked_pairs"],
         "forest_pairs": res["num_pairs_forest"], "nbr_offsets": offsets, "nbr_index": index,
-        "set1": fs1, "set2": fs2,
+        "set1": fs1, "set2": fs2, "h2d_bytes": res["h2d_bytes"],
+        "d2h_bytes": sum(int(a.nbytes) for a in res["raw"]) + int(offsets.nbytes) + int(index.nbytes),
     }
     _cache["key"] = key
     _cache["result"] = result

@@ -169,8 +169,8 @@ int pg_cf_neighbours(pg_plan *plan, const pg_corr_params *params, const pg_fores
     if ((rc = select_device(plan))) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     plan->last_stream = st;
-    return launch_cf_neighbours(*params, *s1, s2 ? *s2 : *s1, s2 == nullptr, counts, offsets,
-                                index, st);
+    return launch_cf_neighbours(*params, *s1, s2 ? *s2 : *s1, s2 == nullptr, nullptr, counts,
+                                offsets, index, st);
 }
 
 int pg_xcf_neighbours(pg_plan *plan, const pg_corr_params *params,
@@ -187,7 +187,55 @@ int pg_xcf_neighbours(pg_plan *plan, const pg_corr_params *params,
     if ((rc = select_device(plan))) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     plan->last_stream = st;
-    return launch_xcf_neighbours(*params, *forests, *objs, counts, offsets, index, st);
+    return launch_xcf_neighbours(*params, *forests, *objs, nullptr, counts, offsets, index, st);
+}
+
+static int validate_groups(const pg_nbr_groups *g) {
+    if (!g || g->num_groups1 < 0 || g->num_groups2 < 0 || g->num_blocks < 0)
+        return PG_ERR_INVALID_ARGUMENT;
+    if (g->num_blocks > 0 &&
+        (!g->start2 || !g->cand_offsets || !g->cand_groups || !g->block_group ||
+         !g->block_first || !g->block_end))
+        return PG_ERR_INVALID_ARGUMENT;
+    return PG_OK;
+}
+
+int pg_cf_neighbours_grouped(pg_plan *plan, const pg_corr_params *params,
+                             const pg_forest_set *s1, const pg_forest_set *s2,
+                             const pg_nbr_groups *groups, int64_t *counts,
+                             const int64_t *offsets, int32_t *index, void *stream) {
+    if (!plan) return PG_ERR_INVALID_ARGUMENT;
+    int rc = validate_params(params);
+    if (rc) return rc;
+    if ((rc = validate_set(s1, false, false))) return rc;
+    if (s2 && (rc = validate_set(s2, false, false))) return rc;
+    if ((rc = validate_groups(groups))) return rc;
+    if (offsets == nullptr && counts == nullptr) return PG_ERR_INVALID_ARGUMENT;
+    if (offsets != nullptr && index == nullptr) return PG_ERR_INVALID_ARGUMENT;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    return launch_cf_neighbours(*params, *s1, s2 ? *s2 : *s1, s2 == nullptr, groups, counts,
+                                offsets, index, st);
+}
+
+int pg_xcf_neighbours_grouped(pg_plan *plan, const pg_corr_params *params,
+                              const pg_forest_set *forests, const pg_forest_set *objs,
+                              const pg_nbr_groups *groups, int64_t *counts,
+                              const int64_t *offsets, int32_t *index, void *stream) {
+    if (!plan || !forests || !objs) return PG_ERR_INVALID_ARGUMENT;
+    int rc = validate_params(params);
+    if (rc) return rc;
+    if ((rc = validate_set(forests, false, false))) return rc;
+    if ((rc = validate_set(objs, false, objs->num > 0))) return rc;
+    if (forests->num > 0 && (!forests->r_first || !forests->r_last)) return PG_ERR_INVALID_ARGUMENT;
+    if ((rc = validate_groups(groups))) return rc;
+    if (offsets == nullptr && counts == nullptr) return PG_ERR_INVALID_ARGUMENT;
+    if (offsets != nullptr && index == nullptr) return PG_ERR_INVALID_ARGUMENT;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    return launch_xcf_neighbours(*params, *forests, *objs, groups, counts, offsets, index, st);
 }
 
 int pg_cf_xi(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *s1,

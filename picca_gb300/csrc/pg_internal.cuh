@@ -187,11 +187,12 @@ int check_cuda(cudaError_t err);
 
 // Launchers implemented in the kernel translation units.
 int launch_cf_neighbours(const pg_corr_params &p, const pg_forest_set &s1, const pg_forest_set &s2,
-                         bool auto_mode, int64_t *counts, const int64_t *offsets, int32_t *index,
-                         cudaStream_t stream);
+                         bool auto_mode, const pg_nbr_groups *groups, int64_t *counts,
+                         const int64_t *offsets, int32_t *index, cudaStream_t stream);
 int launch_xcf_neighbours(const pg_corr_params &p, const pg_forest_set &forests,
-                          const pg_forest_set &objs, int64_t *counts, const int64_t *offsets,
-                          int32_t *index, cudaStream_t stream);
+                          const pg_forest_set &objs, const pg_nbr_groups *groups,
+                          int64_t *counts, const int64_t *offsets, int32_t *index,
+                          cudaStream_t stream);
 int launch_cf_xi_fp64(const Binning &b, const pg_forest_set &s1, const pg_forest_set &s2,
                       const int64_t *nbr_offsets, const int32_t *nbr_index, const double *nbr_angle,
                       const int32_t *work_order, int64_t num_work, const pg_xi_rows &out,

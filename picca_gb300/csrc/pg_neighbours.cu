@@ -33,6 +33,74 @@ struct NbrArgs {
     int32_t zerr_on, precut_on;
 };
 
+// One query against one candidate g of the other set (after the FP32
+// prefilter): thingid, exact FP64 angle with the reference's formula, and
+// the mode's filters. True when g is a neighbour.
+struct Query {
+    double x, y, z, ra, dec, cosdec, zq, rfirst, rlast;
+    int64_t id;
+};
+
+template <int MODE>
+__device__ __forceinline__ bool is_neighbour(const NbrArgs &a, const Query &q, int64_t g) {
+    if (a.id2[g] == q.id) return false;
+    const double ang = angle_between(q.x, q.y, q.z, q.ra, q.dec, q.cosdec, a.x2[g], a.y2[g],
+                                     a.z2[g], a.ra2[g], a.dec2[g]);
+    if (!(ang < a.ang_max)) return false;
+    if (MODE == 1 && !(q.ra > a.ra2[g])) return false;
+    if (MODE == 2) {
+        if (a.zerr_on) {
+            const double ang_deg = __dmul_rn(180.0 / kPi, ang);
+            const double zq = a.zq2[g];
+            const double z_qq = __dmul_rn(0.5, __dadd_rn(q.zq, zq));
+            double dv = fabs(__dsub_rn(q.zq, zq)) / __dadd_rn(1.0, z_qq);
+            dv = __dmul_rn(dv, kSpeedLight);
+            if (ang_deg < a.zerr_deg && dv < a.zerr_kms) return false;
+        }
+        if (a.precut_on) {
+            const double c = cos(ang / 2.);
+            const double robj = a.robj2[g];
+            if (!(__dmul_rn(__dsub_rn(q.rfirst, robj), c) < a.r_par_max_f)) return false;
+            if (!(__dmul_rn(__dsub_rn(q.rlast, robj), c) > a.r_par_min_f)) return false;
+        }
+    }
+    return true;
+}
+
+template <int MODE>
+__device__ __forceinline__ Query load_query(const NbrArgs &a, int64_t f, bool active) {
+    Query q{0, 0, 0, 0, 0, 1, 0, 0, 0, 0};
+    if (active) {
+        q.x = a.x1[f]; q.y = a.y1[f]; q.z = a.z1[f];
+        q.ra = a.ra1[f]; q.dec = a.dec1[f]; q.cosdec = a.cosdec1[f];
+        q.id = a.id1[f];
+        if (MODE == 2) {
+            q.zq = a.zq1[f];
+            q.rfirst = a.rfirst1[f];
+            q.rlast = a.rlast1[f];
+        }
+    }
+    return q;
+}
+
+// Tests the query against objects [t0, t0 + tn) staged in the tile (FP32 unit
+// vectors); appends neighbours in increasing index order.
+template <int MODE>
+__device__ __forceinline__ void scan_tile(const NbrArgs &a, const Query &q, float fx, float fy,
+                                          float fz, const float4 *tile, int64_t t0, int tn,
+                                          int64_t out, const int64_t *offsets, int32_t *index,
+                                          int64_t &n) {
+    for (int k = 0; k < tn; ++k) {
+        const float4 t = tile[k];
+        const float dot = __fmaf_rn(fz, t.z, __fmaf_rn(fy, t.y, fx * t.x));
+        if (dot <= a.dot_threshold) continue;
+        const int64_t g = t0 + k;
+        if (!is_neighbour<MODE>(a, q, g)) continue;
+        if (offsets) index[out + n] = (int32_t)g;
+        ++n;
+    }
+}
+
 template <int MODE>  // 0: cf cross (two sets), 1: cf auto, 2: xcf
 __global__ void __launch_bounds__(kNbrBlock) neighbours_kernel(NbrArgs a, int64_t *counts,
                                                                 const int64_t *offsets,
@@ -40,19 +108,8 @@ __global__ void __launch_bounds__(kNbrBlock) neighbours_kernel(NbrArgs a, int64_
     __shared__ float4 tile[kNbrTile];
     const int64_t f = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     const bool active = f < a.n1;
-    double qx = 0, qy = 0, qz = 0, qra = 0, qdec = 0, qcos = 1, qzq = 0, qrf = 0, qrl = 0;
-    int64_t qid = 0;
-    if (active) {
-        qx = a.x1[f]; qy = a.y1[f]; qz = a.z1[f];
-        qra = a.ra1[f]; qdec = a.dec1[f]; qcos = a.cosdec1[f];
-        qid = a.id1[f];
-        if (MODE == 2) {
-            qzq = a.zq1[f];
-            qrf = a.rfirst1[f];
-            qrl = a.rlast1[f];
-        }
-    }
-    const float fx = (float)qx, fy = (float)qy, fz = (float)qz;
+    const Query q = load_query<MODE>(a, f, active);
+    const float fx = (float)q.x, fy = (float)q.y, fz = (float)q.z;
     int64_t n = 0;
     const int64_t out = (active && offsets) ? offsets[f] : 0;
     for (int64_t t0 = 0; t0 < a.n2; t0 += kNbrTile) {
@@ -63,34 +120,38 @@ __global__ void __launch_bounds__(kNbrBlock) neighbours_kernel(NbrArgs a, int64_
         }
         __syncthreads();
         if (!active) continue;
-        for (int k = 0; k < tn; ++k) {
-            const float4 t = tile[k];
-            const float dot = __fmaf_rn(fz, t.z, __fmaf_rn(fy, t.y, fx * t.x));
-            if (dot <= a.dot_threshold) continue;
-            const int64_t g = t0 + k;
-            if (a.id2[g] == qid) continue;
-            const double ang = angle_between(qx, qy, qz, qra, qdec, qcos, a.x2[g], a.y2[g],
-                                             a.z2[g], a.ra2[g], a.dec2[g]);
-            if (!(ang < a.ang_max)) continue;
-            if (MODE == 1 && !(qra > a.ra2[g])) continue;
-            if (MODE == 2) {
-                if (a.zerr_on) {
-                    const double ang_deg = __dmul_rn(180.0 / kPi, ang);
-                    const double zq = a.zq2[g];
-                    const double z_qq = __dmul_rn(0.5, __dadd_rn(qzq, zq));
-                    double dv = fabs(__dsub_rn(qzq, zq)) / __dadd_rn(1.0, z_qq);
-                    dv = __dmul_rn(dv, kSpeedLight);
-                    if (ang_deg < a.zerr_deg && dv < a.zerr_kms) continue;
-                }
-                if (a.precut_on) {
-                    const double c = cos(ang / 2.);
-                    const double robj = a.robj2[g];
-                    if (!(__dmul_rn(__dsub_rn(qrf, robj), c) < a.r_par_max_f)) continue;
-                    if (!(__dmul_rn(__dsub_rn(qrl, robj), c) > a.r_par_min_f)) continue;
-                }
-            }
-            if (offsets) index[out + n] = (int32_t)g;
-            ++n;
+        scan_tile<MODE>(a, q, fx, fy, fz, tile, t0, tn, out, offsets, index, n);
+    }
+    if (active && !offsets) counts[f] = n;
+}
+
+// Grouped search: a block takes up to kNbrBlock queries of one group of the
+// query set and scans only the candidate groups of the other set (object
+// ranges, ascending), so neighbours still come out in increasing index
+// order. The candidate lists are a superset (bounding caps), the tests per
+// object are those of the brute-force kernel.
+template <int MODE>
+__global__ void __launch_bounds__(kNbrBlock) neighbours_grouped_kernel(
+    NbrArgs a, pg_nbr_groups gr, int64_t *counts, const int64_t *offsets, int32_t *index) {
+    __shared__ float4 tile[kNbrTile];
+    const int grp = gr.block_group[blockIdx.x];
+    const int64_t f = gr.block_first[blockIdx.x] + threadIdx.x;
+    const bool active = f < gr.block_end[blockIdx.x];
+    const Query q = load_query<MODE>(a, f, active);
+    const float fx = (float)q.x, fy = (float)q.y, fz = (float)q.z;
+    int64_t n = 0;
+    const int64_t out = (active && offsets) ? offsets[f] : 0;
+    for (int c = gr.cand_offsets[grp]; c < gr.cand_offsets[grp + 1]; ++c) {
+        const int g2 = gr.cand_groups[c];
+        const int64_t lo = gr.start2[g2], hi = gr.start2[g2 + 1];
+        for (int64_t t0 = lo; t0 < hi; t0 += kNbrTile) {
+            const int tn = (int)min((int64_t)kNbrTile, hi - t0);
+            __syncthreads();
+            for (int k = threadIdx.x; k < tn; k += blockDim.x)
+                tile[k] = make_float4((float)a.x2[t0 + k], (float)a.y2[t0 + k],
+                                      (float)a.z2[t0 + k], 0.f);
+            __syncthreads();
+            if (active) scan_tile<MODE>(a, q, fx, fy, fz, tile, t0, tn, out, offsets, index, n);
         }
     }
     if (active && !offsets) counts[f] = n;
@@ -105,8 +166,8 @@ float dot_threshold(double ang_max) {
 }  // namespace
 
 int launch_cf_neighbours(const pg_corr_params &p, const pg_forest_set &s1, const pg_forest_set &s2,
-                         bool auto_mode, int64_t *counts, const int64_t *offsets, int32_t *index,
-                         cudaStream_t stream) {
+                         bool auto_mode, const pg_nbr_groups *groups, int64_t *counts,
+                         const int64_t *offsets, int32_t *index, cudaStream_t stream) {
     NbrArgs a{};
     a.n1 = s1.num;
     a.x1 = s1.x_cart; a.y1 = s1.y_cart; a.z1 = s1.z_cart;
@@ -117,6 +178,17 @@ int launch_cf_neighbours(const pg_corr_params &p, const pg_forest_set &s1, const
     a.ang_max = p.ang_max;
     a.dot_threshold = dot_threshold(p.ang_max);
     if (a.n1 == 0) return PG_OK;
+    if (groups) {
+        if (groups->num_blocks <= 0) return PG_OK;
+        const dim3 grid((unsigned)groups->num_blocks);
+        if (auto_mode)
+            neighbours_grouped_kernel<1><<<grid, kNbrBlock, 0, stream>>>(a, *groups, counts,
+                                                                         offsets, index);
+        else
+            neighbours_grouped_kernel<0><<<grid, kNbrBlock, 0, stream>>>(a, *groups, counts,
+                                                                         offsets, index);
+        return check_cuda(cudaGetLastError());
+    }
     const dim3 grid((unsigned)((a.n1 + kNbrBlock - 1) / kNbrBlock));
     if (auto_mode)
         neighbours_kernel<1><<<grid, kNbrBlock, 0, stream>>>(a, counts, offsets, index);
@@ -126,8 +198,9 @@ int launch_cf_neighbours(const pg_corr_params &p, const pg_forest_set &s1, const
 }
 
 int launch_xcf_neighbours(const pg_corr_params &p, const pg_forest_set &forests,
-                          const pg_forest_set &objs, int64_t *counts, const int64_t *offsets,
-                          int32_t *index, cudaStream_t stream) {
+                          const pg_forest_set &objs, const pg_nbr_groups *groups,
+                          int64_t *counts, const int64_t *offsets, int32_t *index,
+                          cudaStream_t stream) {
     NbrArgs a{};
     a.n1 = forests.num;
     a.x1 = forests.x_cart; a.y1 = forests.y_cart; a.z1 = forests.z_cart;
@@ -148,6 +221,12 @@ int launch_xcf_neighbours(const pg_corr_params &p, const pg_forest_set &forests,
     a.r_par_max_f = p.r_par_max * f;
     a.r_par_min_f = p.r_par_min * f;
     if (a.n1 == 0) return PG_OK;
+    if (groups) {
+        if (groups->num_blocks <= 0) return PG_OK;
+        neighbours_grouped_kernel<2><<<(unsigned)groups->num_blocks, kNbrBlock, 0, stream>>>(
+            a, *groups, counts, offsets, index);
+        return check_cuda(cudaGetLastError());
+    }
     const dim3 grid((unsigned)((a.n1 + kNbrBlock - 1) / kNbrBlock));
     neighbours_kernel<2><<<grid, kNbrBlock, 0, stream>>>(a, counts, offsets, index);
     return check_cuda(cudaGetLastError());

@@ -1,17 +1,22 @@
 // Precision-form pair accumulation: FP32 geometry with an FP64 bin-edge
-// guard, compensated FP32 shared-memory block sums, FP64 rows.
+// guard, double-float xi terms, compensated FP32 shared-memory block sums,
+// FP64 rows.
 //
 // Persistent structure: one work item = one forest of set 1 with all its
 // neighbours; the forest-1 pixels are staged in shared memory, warps take
 // neighbour forests dynamically, and each lane holds P consecutive forest-2
-// pixels in registers while it loops over the forest-1 pixels. For every
-// pixel pair the kernel evaluates, in FP32,
-//     p   = cp*((r1h - r2h) + (r1l - r2l))   (= r_par * np/(r_par_max - r_par_min))
-//     x'  = |p| - (r_par_min*inv_p + 1/2)   (p itself for signed, cross correlations)
-//     xt' = st*d1 + (st*d2 - 1/2)           (= r_trans * nt/r_trans_max - 1/2)
-// with cp = cos(theta/2) * inv_p, st = sin(theta/2) * inv_t, and the comoving
-// distance carried as an FP32 pair r = rh + rl, so that r1 - r2 is exact to
-// ~1e-7 of itself (not of r). The bin index of py/picca/cf.py:372-376 is
+// pixels in registers while it loops over the forest-1 pixels.
+//
+// Geometry. Comoving distances are taken relative to R, the distance of the
+// middle pixel of forest 1 (one FP64 subtraction per pixel, exact), and
+// rounded to FP32: rho = r - R, |rho| of the order of a forest's length
+// rather than of r (~4000 Mpc/h). Per forest pair and forest-2 pixel the
+// lane holds nB = -cp*rho2 (cp = cos(theta/2) * inv_p), so that for every
+// pixel pair one FFMA gives
+//     p   = cp*rho1 + nB                 (= r_par * np/(r_par_max - r_par_min))
+//     x'  = |p| - (r_par_min*inv_p + 1/2)  (p itself for signed, cross correlations)
+//     xt' = st*d1 + (st*d2 - 1/2)         (= r_trans * nt/r_trans_max - 1/2)
+// with st = sin(theta/2) * inv_t. The bin index of py/picca/cf.py:372-376 is
 // floor(x) = round(x'), taken with one round-to-nearest add of 1.5 * 2^23:
 // y = x' + 1.5*2^23 is an integer for |x'| < 2^22, so round(x') is the bit
 // pattern of y minus that of 1.5*2^23 and f = x' - (y - 1.5*2^23), in
@@ -20,21 +25,32 @@
 // of the half-plate r_par cut or the z-pair cuts, is queued and re-decided
 // in FP64 with the reference's operation order (cf_pair_bin /
 // xcf_pair_bin), so every accepted pair, bin index and pair count equals
-// the FP64 reference. g exceeds the worst-case FP32 error (make_fast_const).
+// the FP64 reference. g exceeds the worst-case FP32 error; its r_par part
+// grows with the largest |rho1| of the work item (make_fast_const, and the
+// per-item band computed after staging).
 // Forest-2 slots past the end of the forest or with zero weight carry
-// r = t = z = 1e30 (and cp = 1 for quasars), which lands far outside every
+// nB = t = z = 1e30 (and cp = 1 for quasars), which lands far outside every
 // bin, edge and cut, so such a slot is neither accepted nor queued.
+//
+// xi terms. delta*w of every pixel is formed in FP64 and carried as an FP32
+// pair (hi, lo) with hi + lo = delta*w to 2^-48. The product of two such
+// pairs is hi1*hi2 (rounded) plus a low part: the exact rounding error of
+// hi1*hi2 (one FMA) and the cross terms hi1*lo2 + lo1*hi2; the lost lo1*lo2
+// is below 2^-48 of the term. Runs of accepted pairs of one lane in one bin
+// sum the high parts with Knuth's TwoSum, its error going to the run's low
+// part, so a run reaches the histogram as (hi, lo) with an error of order
+// 2^-46 of its terms.
 //
 // Sums: per-CTA FP32 shared-memory histograms of xi, w, p*w, x_tr*w,
 // (z1+z2)*w and an int32 count. xi (products of signed deltas, strongly
 // cancelling) and w (the normalisation) are summed error-free: the atomic add
-// returns the previous value, Knuth's TwoSum recovers the exact rounding
-// error of the add and a second histogram collects it. Accepted pairs first
-// go to a per-warp ring, and the warp applies them 32 at a time, so the
-// eight atomic adds of a pair run with every lane active instead of in the
-// divergent branch of each pair. After each work item the histograms are
-// added to the FP64 rows and mapped back to picca's units (r_par =
-// p/inv_p, r_trans = x_tr/inv_t, z = (z1+z2)/2).
+// returns the previous value, TwoSum recovers the exact rounding error of
+// the add and a second histogram collects it together with the run's low
+// part. Accepted pairs first go to a per-warp ring, and the warp applies
+// them 32 at a time, so the eight atomic adds of a pair run with every lane
+// active instead of in the divergent branch of each pair. After each work
+// item the histograms are added to the FP64 rows and mapped back to picca's
+// units (r_par = p/inv_p, r_trans = x_tr/inv_t, z = (z1+z2)/2).
 #include <type_traits>
 
 #include "pg_internal.cuh"
@@ -44,10 +60,12 @@ namespace {
 
 constexpr float kMagic = 12582912.0f;        // 1.5 * 2^23
 constexpr unsigned kMagicBits = 0x4B400000u;  // bits of 1.5 * 2^23
-constexpr float kFar = 1e30f;                 // r and t of an empty slot
-constexpr int kQueue = 256;                   // FP64 recheck entries per warp
-constexpr int kAccQ = 128;                    // accepted-pair ring per warp
-constexpr int kCfP = 4;                       // forest-2 pixels per lane (full passes)
+constexpr float kFar = 1e30f;                 // nB, t and z of an empty slot
+constexpr int kQueue = 256;                   // FP64 recheck entries per warp (cross)
+constexpr int kCfQueue = 128;                 // FP64 recheck entries per warp (auto)
+constexpr int kAccQ = 64;                     // run ring per warp (<= 31 + 32 entries held)
+constexpr int kChunk = 128;                   // forest-2 pixels staged per warp at a time
+constexpr int kRunMax = 64;                   // pairs summed in FP32 registers per run
 constexpr int kXcfP = 2;                      // quasars per lane per pass
 constexpr int kCfBlock = 768;
 constexpr int kXcfBlock = 512;
@@ -55,9 +73,9 @@ constexpr int kXcfBlock = 512;
 struct FastConst {
     double inv_p, inv_t;
     float pc;               // r_par_min * inv_p + 1/2
-    float low_clamp;        // -1/2 + 2 g_par (auto-correlation with r_par_min = 0)
-    float h_par, h_tr;      // 1/2 - g: |f| above this is near an edge
-    float guard_v;          // half-plate cut guard (in units of p)
+    float g0_par;           // guard band of x' without the |rho1| term
+    float g_rho;            // guard band of x' per unit of the work item's max |rho1|
+    float h_tr;             // 1/2 - g_tr: |f| above this is near an r_trans edge
     float guard_z;          // guard on z1 + z2
     float zmin2, zmax2;     // 2 z_min, 2 z_max
     unsigned np, nt;
@@ -67,18 +85,36 @@ struct FastConst {
                             // the lower edge of bin 0 can never be crossed
 };
 
+// Guard of the r_par coordinate of one work item (see make_fast_const).
+struct ParGuard {
+    float h_par;      // 1/2 - g
+    float low_clamp;  // -1/2 + 2 g (auto-correlation with r_par_min = 0)
+    float guard_v;    // half-plate cut guard (in units of p)
+};
+
+__device__ __forceinline__ ParGuard par_guard(const FastConst *fcp, float max_rho) {
+    float g = fcp->g0_par + fcp->g_rho * max_rho;
+    if (!(g < 0.05f)) g = 0.05f;  // absurd bin counts: almost everything is re-decided
+    ParGuard pg;
+    pg.h_par = 0.5f - g;
+    pg.low_clamp = -0.5f + 2.f * g;
+    pg.guard_v = g;
+    return pg;
+}
+
 // ---------------------------------------------------------------------------
 // shared-memory histograms: H_COUNT float arrays of stride hstride
 // ---------------------------------------------------------------------------
 enum { H_XI = 0, H_XIL, H_WE, H_WEL, H_PW, H_TW, H_ZW, H_NB, H_COUNT };
 
-// One pair into the histograms. xi and w are compensated: the atomic add
-// returns the previous value, Knuth's TwoSum of it and the term gives the
-// exact rounding error of the add, which goes to the error histogram. The two
-// adds whose previous value is needed go first, so that their round trips
-// overlap the four plain adds.
-__device__ __forceinline__ void hist_add(float *h, int hs, unsigned bin, float xi, float w,
-                                         float pw, float tw, float zw, int count) {
+// One run of pairs into the histograms. xi (given as hi + lo) and w are
+// compensated: the atomic add returns the previous value, Knuth's TwoSum of
+// it and the term gives the exact rounding error of the add, which goes to
+// the error histogram together with xi's low part. The two adds whose
+// previous value is needed go first, so that their round trips overlap the
+// four plain adds.
+__device__ __forceinline__ void hist_add(float *h, int hs, unsigned bin, float xi, float xil,
+                                         float w, float pw, float tw, float zw, int count) {
     float *hx = h + bin;
     const float oxi = atomicAdd(hx + H_XI * hs, xi);
     const float owe = atomicAdd(hx + H_WE * hs, w);
@@ -87,7 +123,7 @@ __device__ __forceinline__ void hist_add(float *h, int hs, unsigned bin, float x
     atomicAdd(hx + H_ZW * hs, zw);
     atomicAdd(reinterpret_cast<int *>(hx + H_NB * hs), count);
     float sum = oxi + xi, bb = sum - oxi;
-    atomicAdd(hx + H_XIL * hs, (oxi - (sum - bb)) + (xi - bb));
+    atomicAdd(hx + H_XIL * hs, ((oxi - (sum - bb)) + (xi - bb)) + xil);
     sum = owe + w;
     bb = sum - owe;
     atomicAdd(hx + H_WEL * hs, (owe - (sum - bb)) + (w - bb));
@@ -117,9 +153,14 @@ __device__ __forceinline__ void zero_all(float *h, int n) {
     for (int b = threadIdx.x; b < n; b += blockDim.x) h[b] = 0.f;
 }
 
-__device__ __forceinline__ int next_item(Scratch *scratch, int *slot) {
+// Next work item of the persistent CTA; also clears the work item's
+// max |rho1| (written by the staging loop after the second barrier).
+__device__ __forceinline__ int next_item(Scratch *scratch, int *slot, unsigned *max_rho_bits) {
     __syncthreads();
-    if (threadIdx.x == 0) *slot = atomicAdd(&scratch->work_counter, 1);
+    if (threadIdx.x == 0) {
+        *slot = atomicAdd(&scratch->work_counter, 1);
+        *max_rho_bits = 0u;
+    }
     __syncthreads();
     return *slot;
 }
@@ -132,6 +173,28 @@ __device__ __forceinline__ float weight32(double w) {
     return f;
 }
 
+// x as an FP32 pair hi + lo (equal to x to about 2^-48 of |x|).
+__device__ __forceinline__ float2 split2(double x) {
+    const float hi = (float)x;
+    return make_float2(hi, (float)(x - (double)hi));
+}
+
+// (ah + al) * (bh + bl) = ph + pl: ph the rounded product of the high
+// parts, pl its exact rounding error (one FMA) plus the cross terms.
+__device__ __forceinline__ void two_prod(float ah, float al, float bh, float bl, float &ph,
+                                         float &pl) {
+    ph = __fmul_rn(ah, bh);
+    pl = __fmaf_rn(ah, bl, __fmaf_rn(al, bh, __fmaf_rn(ah, bh, -ph)));
+}
+
+// s + x with TwoSum: s becomes the rounded sum, its exact error goes to lo.
+__device__ __forceinline__ void two_sum_into(float &s, float &lo, float x) {
+    const float t = s + x;
+    const float bb = t - s;
+    lo += (s - (t - bb)) + (x - bb);
+    s = t;
+}
+
 // round(x) (as unsigned; negative results wrap to large values) and the
 // remainder x - round(x) in [-1/2, 1/2].
 __device__ __forceinline__ unsigned round_rem(float x, float &rem) {
@@ -141,6 +204,9 @@ __device__ __forceinline__ unsigned round_rem(float x, float &rem) {
 }
 
 // Shared-memory layout of both kernels (offsets in bytes from the start).
+// p1: float4 (rho, dist_m, z, w) per forest-1 pixel; p2: float2 (delta*w as
+// hi, lo); acc0 / acc1: float4 pairs of the accepted-pair rings; queue: the
+// FP64 re-decision entries.
 struct SmemLayout {
     size_t cells, p1, p2, acc0, acc1, queue, total;
 };
@@ -154,9 +220,33 @@ __host__ __device__ inline SmemLayout smem_layout(int nbins, int max_pix1, int n
     l.p2 = l.p1 + mp * 16;
     l.acc0 = l.p2 + mp * 8;
     l.acc1 = l.acc0 + (acc_queue ? (size_t)nwarps * kAccQ * 16 : 0);
-    l.queue = l.acc1 + (acc_queue ? (size_t)nwarps * kAccQ * 8 : 0);
+    l.queue = l.acc1 + (acc_queue ? (size_t)nwarps * kAccQ * 16 : 0);
     l.total = l.queue + (size_t)nwarps * kQueue * 4;
     return l;
+}
+
+// Stages a forest of set 1 (n1 pixels from a0) in shared memory relative to
+// r_ref and records its largest |rho| in *max_rho_bits (a non-negative
+// float's bits order as unsigned). Returns whether rho and dist_m are
+// non-decreasing along the forest (block-wide, after a barrier).
+__device__ __forceinline__ bool stage_forest1(const pg_forest_set &s1, int64_t a0, int n1,
+                                              double r_ref, float4 *p1, float2 *p2,
+                                              unsigned *max_rho_bits) {
+    bool ordered = true;
+    float local_max = 0.f;
+    for (int i = threadIdx.x; i < n1; i += blockDim.x) {
+        const double w = s1.weights[a0 + i];
+        const float rho = (float)(s1.r_comov[a0 + i] - r_ref);
+        const float d = (float)s1.dist_m[a0 + i];
+        p1[i] = make_float4(rho, d, (float)s1.z[a0 + i], weight32(w));
+        p2[i] = split2(s1.delta[a0 + i] * w);
+        local_max = fmaxf(local_max, fabsf(rho));
+        if (i + 1 < n1)
+            ordered &= (float)(s1.r_comov[a0 + i + 1] - r_ref) >= rho &&
+                       (float)s1.dist_m[a0 + i + 1] >= d;
+    }
+    if (local_max > 0.f) atomicMax(max_rho_bits, __float_as_uint(local_max));
+    return __syncthreads_and(ordered) != 0;
 }
 
 // ---------------------------------------------------------------------------
@@ -191,87 +281,104 @@ __device__ __forceinline__ void cf_drain(const Binning &b, const FastConst *__re
         }
         const double w1 = s1.weights[ia], w2 = s2.weights[jb];
         const float w12 = weight32(w1) * weight32(w2);
-        const float dw12 = (float)(s1.delta[ia] * w1) * (float)(s2.delta[jb] * w2);
+        // delta_times_weight1 * delta_times_weight2 (py/picca/cf.py:367-369)
+        const float2 dw12 = split2((s1.delta[ia] * w1) * (s2.delta[jb] * w2));
         const float pv = (float)(r_par * inv_p);
         const float tv = (float)(r_trans * inv_t);
         const float zs = (float)z1 + (float)z2;
-        hist_add(h, fcp->hstride, (unsigned)bin, dw12, w12, pv * w12, tv * w12, zs * w12, 1);
+        hist_add(h, fcp->hstride, (unsigned)bin, dw12.x, dw12.y, w12, pv * w12, tv * w12,
+                 zs * w12, 1);
     }
     if (lane == 0) atomicAdd(&scratch->rechecked_pairs, (unsigned long long)count);
     __syncwarp();
 }
 
-// Applies n (<= 32) queued entries starting at ring position head. An entry
-// is a run of accepted pairs of one lane in one bin (consecutive forest-2
-// pixels against one forest-1 pixel): {sum dw1 dw2, sum w1 w2, sum p w,
-// sum x_tr w} and {sum (z1 + z2) w, bin * 8 + pairs}.
+// Applies n (<= 32) ring entries starting at position head. An entry is a
+// run of accepted pairs of one lane in one bin (consecutive pairs of one
+// diagonal): {sum dw1 dw2 (hi, lo), sum w1 w2, sum p w} and {sum x_tr w,
+// sum (z1 + z2) w, bin, pairs}.
 template <bool FULL>
-__device__ __forceinline__ void apply_accepted(const float4 *acc0, const float2 *acc1, int head,
-                                               int n, float *h, int hs) {
+__device__ __forceinline__ void apply_runs(const float4 *acc0, const float4 *acc1, int head,
+                                           int n, float *h, int hs) {
     __syncwarp();
     const int lane = threadIdx.x & 31;
     if (FULL || lane < n) {  // FULL: n = 32, no divergence
         const int e = (head + lane) & (kAccQ - 1);
         const float4 v = acc0[e];
-        const float2 u = acc1[e];
-        const unsigned key = __float_as_uint(u.y);
-        hist_add(h, hs, key >> 3, v.x, v.y, v.z, v.w, u.x, (int)(key & 7u));
+        const float4 u = acc1[e];
+        hist_add(h, hs, __float_as_uint(u.z), v.x, v.y, v.z, v.w, u.x, u.y,
+                 (int)__float_as_uint(u.w));
     }
     __syncwarp();
 }
 
-// Number of leading forest-1 pixels whose field (0: r, 1: dist_m) is below v
-// (UPPER: not above v), for pixels in increasing order of that field.
-template <int FIELD, bool UPPER>
-__device__ __forceinline__ int count_below(const float4 *p1, int n, float v) {
+// Number of leading entries of a non-increasing sequence x[0..n) (the .x
+// field of the staged forest-2 records) above v (OR_EQUAL: not below v).
+template <bool OR_EQUAL>
+__device__ __forceinline__ int count_leading(const float4 *x, int n, float v) {
     int lo = 0, hi = n;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        const float4 q = p1[mid];
-        const float x = FIELD == 0 ? q.x : q.z;
-        if (UPPER ? x <= v : x < v) lo = mid + 1;
+        const float y = x[mid].x;
+        if (OR_EQUAL ? y >= v : y > v) lo = mid + 1;
         else hi = mid;
     }
     return lo;
 }
 
-// Forest-1 pixel range [i_lo, i_hi) that can pair with this warp's
-// forest-2 block, for forest-1 pixels in increasing r and dist_m. Pairs
-// outside it have x = p - pmin more than one bin outside [0, np] (r1 beyond
-// the block's r range +- the offsets) or x_tr' = st d1 + t above nt + 1
-// (d1 beyond (nt + 1 - min t) / st); their FP32 values are then far from
-// every bin and edge, so the FP32 test would reject them without queueing.
-template <int P>
-__device__ __forceinline__ void window(const float4 *p1, int n1, const float (&rh)[P],
-                                       const float (&t)[P], float st, float lo_off,
-                                       float hi_off, float t_end, int &i_lo, int &i_hi) {
-    float rmin = kFar, rmax = -kFar, tmin = kFar;
-#pragma unroll
-    for (int p = 0; p < P; ++p) {
-        if (rh[p] < 0.5f * kFar) {
-            rmin = fminf(rmin, rh[p]);
-            rmax = fmaxf(rmax, rh[p]);
-            tmin = fminf(tmin, t[p]);
-        }
-    }
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-        rmin = fminf(rmin, __shfl_xor_sync(0xffffffffu, rmin, o));
-        rmax = fmaxf(rmax, __shfl_xor_sync(0xffffffffu, rmax, o));
-        tmin = fminf(tmin, __shfl_xor_sync(0xffffffffu, tmin, o));
-    }
-    i_lo = count_below<0, false>(p1, n1, rmin + lo_off);
-    i_hi = count_below<0, true>(p1, n1, rmax + hi_off);
-    if (st > 0.f) {
-        const int it_end = count_below<1, false>(p1, n1, (t_end - tmin) / st);
-        if (it_end < i_hi) i_hi = it_end;
-    }
+// Shared-memory layout of the auto-correlation kernel (byte offsets):
+// block histograms; forest 1 as float4 (rho, dist_m, z, w) and float2
+// (delta*w hi, lo); then per warp the staged forest-2 chunk as float4 (nB,
+// t, z, w) and float2 (delta*w hi, lo), the run ring (two float4 per entry),
+// the FP64 re-decision queue and the forest-1 zerr veto bits.
+struct CfSmem {
+    size_t cells, p1, p1x, warps, per_warp, buf, bufx, acc0, acc1, queue, veto, total;
+};
+
+__host__ __device__ inline CfSmem cf_smem(int nbins, int max_pix1, int nwarps) {
+    CfSmem l;
+    const size_t mp = (size_t)((max_pix1 + 1) & ~1);
+    l.cells = 0;
+    l.p1 = (size_t)((nbins + 3) & ~3) * H_COUNT * 4;
+    l.p1x = l.p1 + mp * 16;
+    l.warps = l.p1x + mp * 8;
+    l.buf = 0;
+    l.bufx = l.buf + (size_t)kChunk * 16;
+    l.acc0 = l.bufx + (size_t)kChunk * 8;
+    l.acc1 = l.acc0 + (size_t)kAccQ * 16;
+    l.queue = l.acc1 + (size_t)kAccQ * 16;
+    l.veto = l.queue + (size_t)kCfQueue * 4;
+    l.per_warp = (l.veto + ((mp + 31) / 32) * 4 + 15) & ~(size_t)15;
+    l.total = l.warps + (size_t)nwarps * l.per_warp;
+    return l;
 }
 
+// The auto-correlation (and the correlation of two delta fields) as sweeps
+// along diagonals. For a forest pair the pixel pairs (i, j) with j - i = d
+// form diagonal d; along it r1 - r2 and d1 + d2 change slowly (pixels on the
+// same wavelength grid), so consecutive pairs of a diagonal share their bin
+// for tens of steps. A lane owns one diagonal of a group of 32 consecutive
+// ones and steps i with the others (forest-1 pixel i is a broadcast read of
+// shared memory, forest-2 pixel i + d a read of the warp's staged chunk),
+// summing consecutive accepted pairs of one bin in registers (a run); a run
+// goes to the block histogram only when its bin changes, through a ring
+// that applies 32 runs with every lane active.
+//
+// Work skipped, every skip exact: forest 2 is staged in chunks of kChunk
+// pixels; per chunk, binary searches give for every forest-1 pixel i the
+// forest-2 pixels whose p = cp*rho1 + nB lies within one bin of the
+// accepted r_par range, hence the band of diagonals [D_lo, D_hi) holding
+// every such pair (requires rho non-decreasing along both forests, checked;
+// otherwise every diagonal is swept). Along a diagonal x_tr' = st d1 + t is
+// non-decreasing (d non-decreasing, checked), so a binary search ends each
+// lane's sweep at the first pair with x_tr' >= nt + 1. Skipped pairs are at
+// least one bin outside the accepted ranges, so the reference rejects them
+// too.
+//
 // EXTRA: half-plate veto, z-pair cuts or zerr cut may be active.
 // LOWX: auto-correlation with r_par_min = 0 (lower edge of bin 0 exempt).
 template <bool AUTO, bool EXTRA, bool LOWX>
-__global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
+__global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
     const __grid_constant__ Binning b, const FastConst *__restrict__ fcp,
     const __grid_constant__ pg_forest_set s1, const __grid_constant__ pg_forest_set s2,
     const int64_t *__restrict__ nbr_offsets, const int32_t *__restrict__ nbr_index,
@@ -279,71 +386,69 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
     int64_t num_work, const __grid_constant__ pg_xi_rows out, Scratch *scratch, int max_pix1) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int item_slot;
+    __shared__ unsigned max_rho_bits;
     __shared__ long long nbr_next;
-    // state read only off the hot loop lives in shared memory, which keeps
-    // the registers for the pixel pairs (and 24 warps per SM resident)
     __shared__ double f1_geom[7];  // x, y, z, ra, dec, cos dec, z_qso of forest 1
     __shared__ CfPairCtx pair_ctx[kCfBlock / 32];
-    __shared__ unsigned long long visited[kCfBlock / 32];  // forest-1 pixel steps per warp
+    __shared__ unsigned long long visited[kCfBlock / 32];  // pair steps swept per warp
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
     const unsigned lt_mask = (1u << lane) - 1u;
     const int nbins = fcp->nbins;
     const double inv_p = fcp->inv_p, inv_t = fcp->inv_t;
-    const float pc = fcp->pc, low_clamp = fcp->low_clamp;
+    const float pc = fcp->pc;
     const float pmin_f = fcp->pc - 0.5f;
-    const float h_par = fcp->h_par, h_tr = fcp->h_tr;
+    const float h_tr = fcp->h_tr;
     const unsigned np = fcp->np, nt = fcp->nt;
-    const float t_end = (float)nt + 1.f;  // x_tr' above this: rejected with a bin of margin
+    const float t_end = (float)nt + 1.f;  // x_tr' at or above this: rejected, a bin of margin
+    // accepted range of p with one bin of margin each side: x = p - pmin in
+    // [-1, np + 1]; |p| <= np + 1 for auto-correlations
+    const float p_lo = AUTO ? -(float)(np + 1u) : pmin_f - 1.f;
+    const float p_hi = AUTO ? (float)(np + 1u) : pmin_f + (float)np + 1.f;
     const int hs = fcp->hstride;
-    const SmemLayout L = smem_layout(nbins, max_pix1, nwarps, true);
+    const CfSmem L = cf_smem(nbins, max_pix1, nwarps);
     float *h = reinterpret_cast<float *>(smem + L.cells);
-    float4 *p1 = reinterpret_cast<float4 *>(smem + L.p1);
-    float2 *p2 = reinterpret_cast<float2 *>(smem + L.p2);
-    float4 *acc0 = reinterpret_cast<float4 *>(smem + L.acc0) + warp * kAccQ;
-    float2 *acc1 = reinterpret_cast<float2 *>(smem + L.acc1) + warp * kAccQ;
-    uint32_t *queue = reinterpret_cast<uint32_t *>(smem + L.queue) + warp * kQueue;
+    const float4 *p1 = reinterpret_cast<const float4 *>(smem + L.p1);
+    const float2 *p1x = reinterpret_cast<const float2 *>(smem + L.p1x);
+    unsigned char *wbase = smem + L.warps + (size_t)warp * L.per_warp;
+    float4 *buf = reinterpret_cast<float4 *>(wbase + L.buf);
+    float2 *bufx = reinterpret_cast<float2 *>(wbase + L.bufx);
+    float4 *acc0 = reinterpret_cast<float4 *>(wbase + L.acc0);
+    float4 *acc1 = reinterpret_cast<float4 *>(wbase + L.acc1);
+    uint32_t *queue = reinterpret_cast<uint32_t *>(wbase + L.queue);
+    uint32_t *veto1 = reinterpret_cast<uint32_t *>(wbase + L.veto);
     zero_all(h, H_COUNT * hs);
     CfPairCtx &ctx = pair_ctx[warp];
     if (lane == 0) visited[warp] = 0ull;
 
     for (;;) {
-        const int item = next_item(scratch, &item_slot);
+        const int item = next_item(scratch, &item_slot, &max_rho_bits);
         if (item >= num_work) break;
         const int64_t f1 = work_order ? work_order[item] : item;
         const int32_t row = s1.row[f1];
         const int64_t a0 = s1.pix_offset[f1];
         const int64_t n1_64 = s1.pix_offset[f1 + 1] - a0;
-        if (n1_64 > max_pix1 || n1_64 > 65535) {
-            if (threadIdx.x == 0) report_error(scratch, PG_ERR_UNSUPPORTED, (int32_t)f1);
+        if (n1_64 > max_pix1 || n1_64 > 65535 || n1_64 < 1) {
+            if (threadIdx.x == 0 && n1_64 > 0) report_error(scratch, PG_ERR_UNSUPPORTED, (int32_t)f1);
             continue;
         }
         const int n1 = (int)n1_64;
-        // stage forest 1 in FP32: r as (hi, lo), dist_m, z; (w, delta*w)
-        bool ordered = true;
-        for (int i = threadIdx.x; i < n1; i += blockDim.x) {
-            const double w = s1.weights[a0 + i];
-            const double r = s1.r_comov[a0 + i];
-            const float rh = (float)r;
-            p1[i] = make_float4(rh, (float)(r - (double)rh), (float)s1.dist_m[a0 + i],
-                                (float)s1.z[a0 + i]);
-            p2[i] = make_float2(weight32(w), (float)(s1.delta[a0 + i] * w));
-            if (i + 1 < n1)
-                ordered &= (float)s1.r_comov[a0 + i + 1] >= rh &&
-                           (float)s1.dist_m[a0 + i + 1] >= (float)s1.dist_m[a0 + i];
-        }
-        // forest-1 pixels in increasing distance: each forest-2 block only
-        // visits the forest-1 pixels that can pair with it (see below)
+        // forest 1 in FP32 relative to the distance of its middle pixel
+        const double r_ref = s1.r_comov[a0 + n1 / 2];
         if (threadIdx.x == 0) {
             f1_geom[0] = s1.x_cart[f1]; f1_geom[1] = s1.y_cart[f1]; f1_geom[2] = s1.z_cart[f1];
             f1_geom[3] = s1.ra[f1]; f1_geom[4] = s1.dec[f1]; f1_geom[5] = s1.cos_dec[f1];
             f1_geom[6] = s1.z_qso[f1];
             nbr_next = nbr_offsets[f1];
         }
-        const bool sorted1 = __syncthreads_and(ordered) != 0;
+        const bool sorted1 = stage_forest1(s1, a0, n1, r_ref, const_cast<float4 *>(p1),
+                                           const_cast<float2 *>(p1x), &max_rho_bits);
+        const ParGuard pg = par_guard(fcp, __uint_as_float(max_rho_bits));
+        const float h_par = pg.h_par, low_clamp = pg.low_clamp;
         const int64_t k1 = nbr_offsets[f1 + 1];
-        int head = 0, tail = 0;  // accepted-pair ring of this warp (warp-uniform)
+        int head = 0, tail = 0;  // run ring of this warp (warp-uniform)
+        int qn = 0;              // FP64 re-decision queue of this warp
         for (;;) {
             // warps take neighbour forests dynamically (balances uneven lengths)
             int64_t k = 0;
@@ -373,6 +478,10 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                 }
                 zerr_pair = b.zerr_on && (ang < b.zerr_ang);
             }
+            if (qn) {  // the queue holds the previous pair's entries
+                cf_drain(b, fcp, s1, s2, ctx, queue, qn, h, scratch);
+                qn = 0;
+            }
             __syncwarp();
             if (lane == 0) {
                 ctx.a0 = a0;
@@ -383,105 +492,132 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                 ctx.shp = shp;
                 ctx.zq2 = EXTRA ? s2.z_qso[g] : 0.;
             }
+            if (EXTRA && zerr_pair) {
+                // forest-1 pixels vetoed against quasar 2 (py/picca/cf.py:321-328)
+                const double zq2 = s2.z_qso[g];
+                for (int i0 = 0; i0 < n1; i0 += 32) {
+                    const int i = i0 + lane;
+                    const bool v = i < n1 && zerr_veto(s1.z[a0 + i], zq2, b.zerr_kms);
+                    const unsigned m = __ballot_sync(0xffffffffu, v);
+                    if (lane == 0) veto1[i0 >> 5] = m;
+                }
+            }
             __syncwarp();
             const float cp = (float)(chalf * inv_p);
             const float st = (float)(shalf * inv_t);
-            // r1 - r2 limits of pairs that can land in a bin, one bin of margin
-            // each side: x = p - pmin in [-1, np + 1], |p| for auto-correlations
-            const float lo_off = AUTO ? -(float)(np + 1u) / cp : (pmin_f - 1.f) / cp;
-            const float hi_off = AUTO ? (float)(np + 1u) / cp : (pmin_f + (float)np + 1.f) / cp;
-            int qn = 0;
-            // One pass over forest-2 pixels [jb, jb + 32 P): lane l holds pixels
-            // jb + P l + p, p < P. The forest is covered with P = 4 passes and
-            // a last pass of P = 2 or 1 for a short remainder, so that few
-            // slots are empty.
-            auto pass = [&](auto p_const, const int jb) {
-              constexpr int P = decltype(p_const)::value;
-              // The FP64 re-decision queue is drained between passes over the
-              // forest-1 pixels, outside the pixel loop, so that its FP64 code
-              // does not hold registers in the loop; a pass stops early when
-              // one more pixel could overflow the queue, and the next pass
-              // reloads the forest-2 slots and resumes at that pixel.
-              int i_next = -1, i_end = n1;
-              for (;;) {
-                // lane owns pixels jb + kCfP*lane + p (consecutive pixels, so the
-                // lanes of a warp mostly fall in different r_par bins)
-                float rh[P], rl[P], t[P], zv[P], wv[P], dv[P];
-                bool any = false;
-#pragma unroll
-                for (int p = 0; p < P; ++p) {
-                    const int j = jb + P * lane + p;
-                    rh[p] = kFar; rl[p] = 0.f; t[p] = kFar; zv[p] = kFar; wv[p] = 0.f; dv[p] = 0.f;
-                    if (j < n2) {
-                        const int64_t jj = b0 + j;
-                        const double w2 = s2.weights[jj];
-                        bool ok = w2 != 0;
-                        if (EXTRA && zerr_pair && ok)
-                            ok = !zerr_veto(s2.z[jj], f1_geom[6], b.zerr_kms);
-                        if (ok) {
-                            any = true;
-                            const double r = s2.r_comov[jj];
-                            rh[p] = (float)r;
-                            rl[p] = (float)(r - (double)rh[p]);
-                            t[p] = st * (float)s2.dist_m[jj] - 0.5f;
-                            zv[p] = (float)s2.z[jj];
-                            wv[p] = weight32(w2);
-                            dv[p] = (float)(s2.delta[jj] * w2);
+            for (int jc = 0; jc < n2; jc += kChunk) {
+                const int jn = min(kChunk, n2 - jc);
+                // stage the chunk: nB = -cp rho2, t = st d2 - 1/2; a pixel
+                // without weight or vetoed against quasar 1 gets w = 0 (and
+                // t = kFar), which removes its pairs in the sweep
+                bool ordered2 = true, valid2 = true;
+                __syncwarp();
+                for (int jl = lane; jl < jn; jl += 32) {
+                    const int64_t jj = b0 + jc + jl;
+                    const double w2 = s2.weights[jj];
+                    bool ok = w2 != 0;
+                    if (EXTRA && zerr_pair && ok)
+                        ok = !zerr_veto(s2.z[jj], f1_geom[6], b.zerr_kms);
+                    const float rho2 = (float)(s2.r_comov[jj] - r_ref);
+                    const float d2 = (float)s2.dist_m[jj];
+                    buf[jl] = make_float4(-__fmul_rn(cp, rho2),
+                                          ok ? __fmaf_rn(st, d2, -0.5f) : kFar,
+                                          (float)s2.z[jj], ok ? weight32(w2) : 0.f);
+                    bufx[jl] = split2(s2.delta[jj] * w2);
+                    valid2 &= ok;
+                    if (jl + 1 < jn)
+                        ordered2 &= (float)(s2.r_comov[jj + 1] - r_ref) >= rho2 &&
+                                    (float)s2.dist_m[jj + 1] >= d2;
+                }
+                ordered2 = __all_sync(0xffffffffu, ordered2);
+                valid2 = __all_sync(0xffffffffu, valid2);
+                __syncwarp();
+                // the band of diagonals [d_lo, d_hi) holding every pair within
+                // one bin of the accepted r_par range
+                int d_lo = jc - (n1 - 1), d_hi = jc + jn;
+                if (sorted1 && ordered2) {
+                    int lo = INT_MAX, hi = INT_MIN;
+                    for (int i = lane; i < n1; i += 32) {
+                        const float a = __fmul_rn(cp, p1[i].x);
+                        const int j1 = count_leading<false>(buf, jn, p_hi - a);
+                        const int j2 = count_leading<true>(buf, jn, p_lo - a);
+                        if (j1 < j2) {
+                            lo = min(lo, jc + j1 - i);
+                            hi = max(hi, jc + j2 - i);
                         }
                     }
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        lo = min(lo, __shfl_xor_sync(0xffffffffu, lo, o));
+                        hi = max(hi, __shfl_xor_sync(0xffffffffu, hi, o));
+                    }
+                    d_lo = lo;
+                    d_hi = hi;
                 }
-                if (!__any_sync(0xffffffffu, any)) break;
-                if (i_next < 0) {
-                    int i_lo = 0, i_hi = n1;
-                    if (sorted1)
-                        window<P>(p1, n1, rh, t, st, lo_off, hi_off, t_end, i_lo, i_hi);
-                    i_next = i_lo;
-                    i_end = i_hi;
-                }
-                int i = i_next;
-
-                for (; i < i_end; ++i) {
-                    if (qn > kQueue - 32 * P) break;  // drain first (below)
-                    const float2 qw = p2[i];
-                    const float4 q = p1[i];
-                    if (qw.x == 0.f) continue;  // zero-weight pixel (warp-uniform)
-                    if (EXTRA && zerr_pair && zerr_veto(s1.z[a0 + i], ctx.zq2, b.zerr_kms))
-                        continue;
-                    const float ui = st * q.z;
-                    unsigned near_mask = 0;
-                    // Accepted pairs of this lane's consecutive slots that fall in
-                    // the same bin are summed in registers (a run) and go to the
-                    // ring as one entry, which halves the shared-memory atomics.
-                    unsigned run_bin = 0u;
+                // along a diagonal x_tr' is non-decreasing: trim at t_end
+                const bool t_trim = sorted1 && ordered2 && valid2 && st > 0.f;
+                for (int d0 = d_lo; d0 < d_hi; d0 += 32) {
+                    const int d = d0 + lane;
+                    // this lane's pairs: j = i + d in the chunk, i in forest 1
+                    int ia = max(0, jc - d), ib = min(n1, jc + jn - d);
+                    if (d >= d_hi) ib = ia;
+                    const int joff = d - jc;  // chunk index of pixel i's partner
+                    if (t_trim && ia < ib) {
+                        int lo = ia, hi = ib;
+                        while (lo < hi) {
+                            const int mid = (lo + hi) >> 1;
+                            const float x = __fmaf_rn(st, p1[mid].y, buf[mid + joff].y);
+                            if (x < t_end) lo = mid + 1;
+                            else hi = mid;
+                        }
+                        ib = lo;
+                    }
+                    int g_lo = ia < ib ? ia : INT_MAX, g_hi = ia < ib ? ib : INT_MIN;
+#pragma unroll
+                    for (int o = 16; o > 0; o >>= 1) {
+                        g_lo = min(g_lo, __shfl_xor_sync(0xffffffffu, g_lo, o));
+                        g_hi = max(g_hi, __shfl_xor_sync(0xffffffffu, g_hi, o));
+                    }
+                    if (g_lo >= g_hi) continue;
+                    if (lane == 0) visited[warp] += (unsigned long long)(g_hi - g_lo) * 32u;
+                    // the lane's run: bin, pairs and sums
+                    unsigned run_bin = 0xFFFFFFFFu;
                     int run_n = 0;
-                    float r_xi = 0.f, r_w = 0.f, r_pw = 0.f, r_tw = 0.f, r_zw = 0.f;
+                    float r_xi = 0.f, r_xil = 0.f, r_w = 0.f, r_pw = 0.f, r_tw = 0.f, r_zw = 0.f;
                     // stores the runs of the lanes in `flag` into the ring
                     auto store_runs = [&](bool flag) {
                         const unsigned m = __ballot_sync(0xffffffffu, flag);
                         const int pos = (tail + __popc(m & lt_mask)) & (kAccQ - 1);
                         if (flag) {
-                            acc0[pos] = make_float4(r_xi, r_w, r_pw, r_tw);
-                            acc1[pos] = make_float2(r_zw, __uint_as_float((run_bin << 3) |
-                                                                          (unsigned)run_n));
+                            acc0[pos] = make_float4(r_xi, r_xil, r_w, r_pw);
+                            acc1[pos] = make_float4(r_tw, r_zw, __uint_as_float(run_bin),
+                                                    __uint_as_float((unsigned)run_n));
                         }
                         tail += __popc(m);
                     };
-#pragma unroll
-                    for (int p = 0; p < P; ++p) {
-                        const float pp = cp * ((q.x - rh[p]) + (q.y - rl[p]));
+                    for (int i = g_lo; i < g_hi; ++i) {
+                        bool in = (i >= ia) & (i < ib);
+                        if (EXTRA && zerr_pair) in &= ((veto1[i >> 5] >> (i & 31)) & 1u) == 0u;
+                        const int jl = in ? i + joff : 0;
+                        const float4 q1 = p1[i];
+                        const float4 q2 = buf[jl];
+                        const float pp = __fmaf_rn(cp, q1.x, q2.x);
                         const float v = fabsf(pp);
                         const float pv = AUTO ? v : pp;
                         const float xp = LOWX ? fmaxf(pv - pc, low_clamp) : pv - pc;
-                        const float xt = ui + t[p];
+                        const float xt = __fmaf_rn(st, q1.y, q2.y);
                         float fp, ft;
                         const unsigned ip = round_rem(xp, fp);
                         const unsigned it = round_rem(xt, ft);
+                        // a pixel without weight or vetoed (w staged as 0) pairs with
+                        // nothing: neither accepted nor queued for re-decision
+                        in &= (q1.w != 0.f) & (q2.w != 0.f);
                         bool near = (fabsf(fp) > h_par) | (fabsf(ft) > h_tr);
                         bool ok = (ip < np) & (it < nt);
-                        const float zs = q.w + zv[p];
+                        const float zs = q1.z + q2.z;
                         if (EXTRA) {
                             if (shp) {
-                                near |= fabsf(v - 1.f) < fcp->guard_v;
+                                near |= fabsf(v - 1.f) < pg.guard_v;
                                 ok &= !(v < 1.f);
                             }
                             if (b.zmin_on) {
@@ -493,80 +629,61 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_fast_kernel(
                                 ok &= !(zs > fcp->zmax2);
                             }
                         }
-                        near_mask |= (unsigned)near << p;
-                        const bool acc = ok & !near;
+                        near &= in;
+                        const bool acc = in & ok & !near;
                         const unsigned bin = ip * nt + it;
-                        const bool extend = acc & (run_n > 0) & (bin == run_bin);
-                        // a pair that starts a new run stores the previous one
-                        store_runs(acc & (run_n > 0) & !extend);
-                        if (acc) {
-                            if (!extend) {
-                                run_bin = bin;
+                        const bool brk = acc & ((bin != run_bin) | (run_n >= kRunMax));
+                        const bool flush = brk & (run_n > 0);
+                        if (__any_sync(0xffffffffu, flush)) {
+                            store_runs(flush);
+                            if (flush) {
                                 run_n = 0;
-                                r_xi = r_w = r_pw = r_tw = r_zw = 0.f;
+                                r_xi = r_xil = r_w = r_pw = r_tw = r_zw = 0.f;
                             }
-                            const float w12 = qw.x * wv[p];
-                            r_xi += qw.y * dv[p];
+                        }
+                        if (brk) run_bin = bin;
+                        if (acc) {
+                            const float2 x1 = p1x[i];
+                            const float2 x2 = bufx[jl];
+                            const float w12 = q1.w * q2.w;
+                            float th, tl;
+                            two_prod(x1.x, x1.y, x2.x, x2.y, th, tl);
+                            two_sum_into(r_xi, r_xil, th);
+                            r_xil += tl;
                             r_w += w12;
-                            r_pw += pv * w12;
-                            r_tw += (xt + 0.5f) * w12;
-                            r_zw += zs * w12;
+                            r_pw = __fmaf_rn(pv, w12, r_pw);
+                            r_tw = __fmaf_rn(xt + 0.5f, w12, r_tw);
+                            r_zw = __fmaf_rn(zs, w12, r_zw);
                             ++run_n;
                         }
-                        if (p & 1) {
-                            // at most 64 entries since the last check: the ring
-                            // (kAccQ = 128 > 31 + 64) never overflows
-                            while (tail - head >= 32) {
-                                apply_accepted<true>(acc0, acc1, head, 32, h, hs);
-                                head += 32;
+                        if (__any_sync(0xffffffffu, near)) {
+                            // rare path: queue the pairs near an edge for FP64 re-decision
+                            if (qn > kCfQueue - 32) {
+                                cf_drain(b, fcp, s1, s2, ctx, queue, qn, h, scratch);
+                                if (lane == 0) atomicAdd(&scratch->recheck_overflows, 1ull);
+                                qn = 0;
                             }
+                            const unsigned nmask = __ballot_sync(0xffffffffu, near);
+                            if (near)
+                                queue[qn + __popc(nmask & lt_mask)] =
+                                    ((uint32_t)i << 16) | (uint32_t)(i + d);
+                            qn += __popc(nmask);
+                        }
+                        if (tail - head >= 32) {
+                            apply_runs<true>(acc0, acc1, head, 32, h, hs);
+                            head += 32;
                         }
                     }
                     store_runs(run_n > 0);
                     while (tail - head >= 32) {
-                        apply_accepted<true>(acc0, acc1, head, 32, h, hs);
+                        apply_runs<true>(acc0, acc1, head, 32, h, hs);
                         head += 32;
                     }
-                    if (__any_sync(0xffffffffu, near_mask != 0)) {
-                        // rare path: queue the pairs near an edge for FP64 re-decision
-#pragma unroll
-                        for (int p = 0; p < P; ++p) {
-                            const bool near = (near_mask >> p) & 1u;
-                            const unsigned nmask = __ballot_sync(0xffffffffu, near);
-                            if (!nmask) continue;
-                            const int cnt = __popc(nmask);
-                            if (near) {
-                                const int pos = qn + __popc(nmask & lt_mask);
-                                queue[pos] = ((uint32_t)i << 16) | (uint32_t)(jb + P * lane + p);
-                            }
-                            qn += cnt;
-                        }
-                    }
-                }
-                if (lane == 0) visited[warp] += (unsigned long long)(i - i_next) * (32u * P);
-                if (i >= i_end) break;
-                cf_drain(b, fcp, s1, s2, ctx, queue, qn, h, scratch);
-                if (lane == 0) atomicAdd(&scratch->recheck_overflows, 1ull);
-                qn = 0;
-                i_next = i;
-              }
-            };
-            for (int jb = 0; jb < n2;) {
-                const int rem = n2 - jb;
-                if (rem > 64) {
-                    pass(std::integral_constant<int, 4>{}, jb);
-                    jb += 128;
-                } else if (rem > 32) {
-                    pass(std::integral_constant<int, 2>{}, jb);
-                    jb += 64;
-                } else {
-                    pass(std::integral_constant<int, 1>{}, jb);
-                    jb += 32;
                 }
             }
-            if (qn) cf_drain(b, fcp, s1, s2, ctx, queue, qn, h, scratch);
         }
-        if (tail != head) apply_accepted<false>(acc0, acc1, head, tail - head, h, hs);
+        if (qn) cf_drain(b, fcp, s1, s2, ctx, queue, qn, h, scratch);
+        if (tail != head) apply_runs<false>(acc0, acc1, head, tail - head, h, hs);
         __syncthreads();
         flush_rows(h, *fcp, out, row);
         if (threadIdx.x == 0) atomicAdd(&scratch->work_items, 1ull);
@@ -612,11 +729,12 @@ __device__ __forceinline__ void xcf_drain(const Binning &b, const FastConst *__r
         }
         const double w1 = fs.weights[ia], wq = objs.obj_weight[g];
         const float w12 = weight32(w1) * weight32(wq);
-        const float dw = (float)(fs.delta[ia] * w1) * weight32(wq);
+        // delta1[i] * weights1[i] * weights2[j] (py/picca/xcf.py:308)
+        const float2 dw = split2(fs.delta[ia] * w1 * wq);
         const float pv = (float)(r_par * inv_p);
         const float tv = (float)(r_trans * inv_t);
         const float zs = (float)z1 + (float)zq;
-        hist_add(h, fcp->hstride, (unsigned)bin, dw, w12, pv * w12, tv * w12, zs * w12, 1);
+        hist_add(h, fcp->hstride, (unsigned)bin, dw.x, dw.y, w12, pv * w12, tv * w12, zs * w12, 1);
     }
     __syncwarp();
 }
@@ -630,6 +748,7 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
     int64_t num_work, const __grid_constant__ pg_xi_rows out, Scratch *scratch, int max_pix1) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ int item_slot;
+    __shared__ unsigned max_rho_bits;
     const int lane = threadIdx.x & 31;
     const int warp = threadIdx.x >> 5;
     const int nwarps = blockDim.x >> 5;
@@ -637,7 +756,7 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
     const int nbins = fcp->nbins;
     const double inv_p = fcp->inv_p, inv_t = fcp->inv_t;
     const float pc = fcp->pc;
-    const float h_par = fcp->h_par, h_tr = fcp->h_tr;
+    const float h_tr = fcp->h_tr;
     const unsigned np = fcp->np, nt = fcp->nt;
     const int hs = fcp->hstride;
     const SmemLayout L = smem_layout(nbins, max_pix1, nwarps, false);
@@ -649,7 +768,7 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
     unsigned long long rechecks = 0, overflows = 0;
 
     for (;;) {
-        const int item = next_item(scratch, &item_slot);
+        const int item = next_item(scratch, &item_slot, &max_rho_bits);
         if (item >= num_work) break;
         const int64_t f = work_order ? work_order[item] : item;
         const int32_t row = fs.row[f];
@@ -657,32 +776,27 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
         ctx.a0 = fs.pix_offset[f];
         const int64_t n1_64 = fs.pix_offset[f + 1] - ctx.a0;
         const int64_t nq_64 = nbr_offsets[f + 1] - nbr_offsets[f];
-        if (n1_64 > max_pix1 || n1_64 > 65535 || nq_64 > 65535) {
-            if (threadIdx.x == 0) report_error(scratch, PG_ERR_UNSUPPORTED, (int32_t)f);
+        if (n1_64 > max_pix1 || n1_64 > 65535 || nq_64 > 65535 || n1_64 < 1) {
+            if (threadIdx.x == 0 && n1_64 > 0) report_error(scratch, PG_ERR_UNSUPPORTED, (int32_t)f);
             continue;
         }
         const int n1 = (int)n1_64;
-        for (int i = threadIdx.x; i < n1; i += blockDim.x) {
-            const double w = fs.weights[ctx.a0 + i];
-            const double r = fs.r_comov[ctx.a0 + i];
-            const float rh = (float)r;
-            p1[i] = make_float4(rh, (float)(r - (double)rh), (float)fs.dist_m[ctx.a0 + i],
-                                (float)fs.z[ctx.a0 + i]);
-            p2[i] = make_float2(weight32(w), (float)(fs.delta[ctx.a0 + i] * w));
-        }
-        __syncthreads();
+        const double r_ref = fs.r_comov[ctx.a0 + n1 / 2];
+        stage_forest1(fs, ctx.a0, n1, r_ref, p1, p2, &max_rho_bits);
+        const ParGuard pg = par_guard(fcp, __uint_as_float(max_rho_bits));
+        const float h_par = pg.h_par;
         ctx.x1 = fs.x_cart[f]; ctx.y1 = fs.y_cart[f]; ctx.zc1 = fs.z_cart[f];
         ctx.ra1 = fs.ra[f]; ctx.dec1 = fs.dec[f]; ctx.cd1 = fs.cos_dec[f];
         ctx.k0 = nbr_offsets[f];
         const int nq = (int)nq_64;
         for (int kb = warp * 32 * kXcfP; kb < nq; kb += nwarps * 32 * kXcfP) {
-            float cp[kXcfP], st[kXcfP], rh[kXcfP], rl[kXcfP], t[kXcfP], zv[kXcfP], wv[kXcfP];
+            float cp[kXcfP], st[kXcfP], nb[kXcfP], t[kXcfP], zv[kXcfP], wvh[kXcfP], wvl[kXcfP];
             bool any = false;
 #pragma unroll
             for (int p = 0; p < kXcfP; ++p) {
                 const int kk = kb + lane + 32 * p;
-                cp[p] = 1.f; st[p] = 0.f; rh[p] = kFar; rl[p] = 0.f; t[p] = kFar; zv[p] = kFar;
-                wv[p] = 0.f;
+                cp[p] = 1.f; st[p] = 0.f; nb[p] = kFar; t[p] = kFar; zv[p] = kFar;
+                wvh[p] = 0.f; wvl[p] = 0.f;
                 if (kk < nq) {
                     const int64_t g = nbr_index[ctx.k0 + kk];
                     const double wq = objs.obj_weight[g];
@@ -695,32 +809,32 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
                                                       objs.z_cart[g], objs.ra[g], objs.dec[g]);
                         cp[p] = (float)(cos(ang / 2) * inv_p);
                         st[p] = (float)(sin(ang / 2) * inv_t);
-                        const double r = objs.obj_r_comov[g];
-                        rh[p] = (float)r;
-                        rl[p] = (float)(r - (double)rh[p]);
-                        t[p] = st[p] * (float)objs.obj_dist_m[g] - 0.5f;
+                        const float rho_q = (float)(objs.obj_r_comov[g] - r_ref);
+                        nb[p] = -__fmul_rn(cp[p], rho_q);
+                        t[p] = __fmaf_rn(st[p], (float)objs.obj_dist_m[g], -0.5f);
                         zv[p] = (float)objs.z_qso[g];
-                        wv[p] = weight32(wq);
+                        wvh[p] = weight32(wq);
+                        wvl[p] = (float)(wq - (double)wvh[p]);
                     }
                 }
             }
             if (!__any_sync(0xffffffffu, any)) continue;
             int qn = 0;
             for (int i = 0; i < n1; ++i) {
-                const float2 qw = p2[i];
-                if (qw.x == 0.f) continue;
                 const float4 q = p1[i];
+                if (q.w == 0.f) continue;
+                const float2 qd = p2[i];
                 unsigned near_mask = 0;
 #pragma unroll
                 for (int p = 0; p < kXcfP; ++p) {
-                    const float pv = cp[p] * ((q.x - rh[p]) + (q.y - rl[p]));
-                    const float xt = __fmaf_rn(st[p], q.z, t[p]);
+                    const float pv = __fmaf_rn(cp[p], q.x, nb[p]);
+                    const float xt = __fmaf_rn(st[p], q.y, t[p]);
                     float fp, ft;
                     const unsigned ip = round_rem(pv - pc, fp);
                     const unsigned it = round_rem(xt, ft);
                     bool near = (fabsf(fp) > h_par) | (fabsf(ft) > h_tr);
                     bool ok = (ip < np) & (it < nt);
-                    const float zs = q.w + zv[p];
+                    const float zs = q.z + zv[p];
                     if (EXTRA) {
                         if (b.zmin_on) {
                             near |= fabsf(zs - fcp->zmin2) < fcp->guard_z;
@@ -733,9 +847,11 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
                     }
                     near_mask |= (unsigned)near << p;
                     if (ok & !near) {
-                        const float w12 = qw.x * wv[p];
+                        const float w12 = q.w * wvh[p];
                         const unsigned bin = ip * nt + it;
-                        hist_add(h, hs, bin, qw.y * wv[p], w12, pv * w12, (xt + 0.5f) * w12,
+                        float th, tl;
+                        two_prod(qd.x, qd.y, wvh[p], wvl[p], th, tl);
+                        hist_add(h, hs, bin, th, tl, w12, pv * w12, (xt + 0.5f) * w12,
                                  zs * w12, 1);
                     }
                 }
@@ -776,23 +892,27 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
     }
 }
 
-// Guard bands. Let u = 2^-24. r is carried as rh + rl with |r - rh - rl|
-// <= u^2 r (negligible), so r1 - r2 = (r1h - r2h) + (r1l - r2l) is formed
-// with two roundings of size u |r1 - r2| and u |r1l - r2l|; the product with
-// cp (itself rounded, relative u), the rounding of pc = pmin + 1/2 and the
-// subtraction add u |p|, u (|pmin| + 1/2) and u |x'|. Altogether the FP32 x'
-// is within 6 u (|x| + |pmin| + 1) of the exact x - 1/2. For x_tr the FP32
-// rounding of d1 and d2 (relative u), of st, of the two products, of the
-// shift by 1/2 and of the sum give <= 6 u (|x_tr| + 1). round(x') and the
-// remainder are exact (the magic-number add rounds to an integer and the
-// subtraction is exact). Only pairs whose exact x lies in [-1, n + 1] matter
-// (the others are rejected either way), so with a factor > 2 of margin
-//   g = 16 u (n + |pmin| + 2) + 1e-6.
-// The reference's own FP64 evaluation is within 1e-12 of the exact value,
-// far inside these bands. With r_par_min = 0 in an auto-correlation x = |p|
-// >= 0 and the lower edge of bin 0 cannot be crossed: x' is clamped from
-// below at -1/2 + 2g, which keeps pairs with |p| < 2g (same-wavelength pixels
-// give p = 0 exactly) in bin 0 without flagging them.
+// Guard bands. Let u = 2^-24 (the unit roundoff of FP32). For r_par: rho1
+// and rho2 are the FP64 differences r - R (exact) rounded to FP32 (errors
+// u|rho1|, u|rho2|); cp carries a relative error u, nB = -cp*rho2 another
+// u|cp rho2|, and the FMA p = cp*rho1 + nB rounds once (u|p|). For a pair
+// whose exact x lies in [-1, n + 1] (the others are rejected either way),
+// |rho2| <= |rho1| + (n + 1)/cp, so p is within 4u(n + 1) + 3u cp|rho1| of
+// the exact value; the rounding of pc = pmin + 1/2 and of the subtraction add
+// u(|pmin| + 1/2) and u|x'|. With cp <= inv_p and a factor 2 of margin
+//   g_par = 16 u (n + |pmin| + 2) + 8 u inv_p max|rho1| + 1e-6,
+// the last term taken per work item (R is the middle pixel of forest 1, so
+// max|rho1| is about half the forest's length). For x_tr the FP32 rounding
+// of d1 and d2 (relative u), of st, of t = st*d2 - 1/2 (one FMA) and of the
+// FMA st*d1 + t give <= 6u(|x_tr| + 1), and
+//   g_tr = 16 u (n + 2) + 1e-6.
+// round(x') and the remainder are exact (the magic-number add rounds to an
+// integer and the subtraction is exact). The reference's own FP64 evaluation
+// is within 1e-12 of the exact value, far inside these bands. With
+// r_par_min = 0 in an auto-correlation x = |p| >= 0 and the lower edge of bin
+// 0 cannot be crossed: x' is clamped from below at -1/2 + 2g, which keeps
+// pairs with |p| < 2g (same-wavelength pixels give p = 0 exactly) in bin 0
+// without flagging them.
 FastConst make_fast_const(const Binning &b) {
     FastConst fc{};
     const double u = 1.0 / 16777216.0;
@@ -800,14 +920,11 @@ FastConst make_fast_const(const Binning &b) {
     fc.inv_t = (double)b.nt / b.r_trans_max;
     const double pmin = b.r_par_min * fc.inv_p;
     fc.pc = (float)(pmin + 0.5);
-    double g_par = 16 * u * (b.np + fabs(pmin) + 2) + 1e-6;
+    fc.g0_par = (float)(16 * u * (b.np + fabs(pmin) + 2) + 1e-6);
+    fc.g_rho = (float)(8 * u * fc.inv_p);
     double g_tr = 16 * u * (b.nt + 2) + 1e-6;
-    if (!(g_par < 0.05)) g_par = 0.05;  // absurd bin counts: almost everything is re-decided
     if (!(g_tr < 0.05)) g_tr = 0.05;
-    fc.h_par = (float)(0.5 - g_par);
     fc.h_tr = (float)(0.5 - g_tr);
-    fc.low_clamp = (float)(-0.5 + 2 * g_par);
-    fc.guard_v = (float)g_par;
     fc.guard_z = 1e-5f;  // z1 + z2 < 20: FP32 error below 5e-6
     fc.zmin2 = (float)(2 * b.z_min);
     fc.zmax2 = (float)(2 * b.z_max);
@@ -855,12 +972,11 @@ int launch_cf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &s1,
     if (num_work <= 0) return PG_OK;
     FastConst *fc = static_cast<FastConst *>(fast_const);
     const int max_pix1 = s1.max_pixels;
-    // as many warps (up to kCfBlock / 32) as the per-warp queues leave room for
+    // as many warps (up to kCfBlock / 32) as shared memory leaves room for
     int nwarps = kCfBlock / 32;
-    while (nwarps > 1 && smem_layout(b.nbins, max_pix1, nwarps, true).total > 227 * 1024)
-        --nwarps;
+    while (nwarps > 1 && cf_smem(b.nbins, max_pix1, nwarps).total > 227 * 1024) --nwarps;
     const int block = nwarps * 32;
-    const size_t smem = smem_layout(b.nbins, max_pix1, nwarps, true).total;
+    const size_t smem = cf_smem(b.nbins, max_pix1, nwarps).total;
     if (smem > 227 * 1024) return PG_ERR_UNSUPPORTED;
     (void)ang_max;
     int rc = prepare_fast(b, fc, stream);
@@ -870,9 +986,9 @@ int launch_cf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &s1,
     const bool lowx = autoc && b.r_par_min == 0.0;
     int grid = 0;
 #define PG_LAUNCH_CF(A, E, L)                                                                  \
-    rc = persistent_grid(cf_xi_fast_kernel<A, E, L>, block, smem, num_sms, num_work, &grid);   \
+    rc = persistent_grid(cf_xi_diag_kernel<A, E, L>, block, smem, num_sms, num_work, &grid);   \
     if (rc) return rc;                                                                         \
-    cf_xi_fast_kernel<A, E, L><<<grid, block, smem, stream>>>(b, fc, s1, s2, nbr_offsets,      \
+    cf_xi_diag_kernel<A, E, L><<<grid, block, smem, stream>>>(b, fc, s1, s2, nbr_offsets,      \
                                                               nbr_index, nbr_angle,            \
                                                               work_order, num_work, out,       \
                                                               scratch, max_pix1);

@@ -17,7 +17,7 @@ import numpy as np
 import torch
 
 from . import _native
-from ._native import CorrParams, ForestSetC, XiRowsC, check
+from ._native import CorrParams, ForestSetC, NbrGroupsC, XiRowsC, check
 
 MODE_FP64 = _native.PG_MODE_FP64
 MODE_FP32_GUARD = _native.PG_MODE_FP32_GUARD
@@ -132,6 +132,69 @@ def pack_host(fs, compact=True, pinned=False):
     return host
 
 
+def _group_bounds(row):
+    """Start offsets of the runs of equal values of a non-decreasing array
+    (None when it is not sorted)."""
+    row = np.asarray(row)
+    if row.size == 0:
+        return np.zeros(1, dtype=np.int64)
+    if np.any(np.diff(row) < 0):
+        return None
+    change = np.nonzero(np.diff(row))[0] + 1
+    return np.concatenate([[0], change, [row.size]]).astype(np.int64)
+
+
+def _caps(host, bounds):
+    """Bounding cap of every group: centre (normalised sum of the members'
+    unit vectors) and radius (largest angle from the centre to a member)."""
+    x, y, z = (np.asarray(host[k], dtype=np.float64) for k in ("x_cart", "y_cart", "z_cart"))
+    starts = bounds[:-1]
+    sx, sy, sz = (np.add.reduceat(v, starts) for v in (x, y, z))
+    norm = np.sqrt(sx * sx + sy * sy + sz * sz)
+    safe = np.where(norm > 0, norm, 1.0)
+    cx, cy, cz = sx / safe, sy / safe, sz / safe
+    gid = np.repeat(np.arange(starts.size), np.diff(bounds))
+    ang = np.arccos(np.clip(x * cx[gid] + y * cy[gid] + z * cz[gid], -1.0, 1.0))
+    radius = np.maximum.reduceat(ang, starts)
+    radius = np.where(norm > 0, radius, np.pi)
+    return np.stack([cx, cy, cz], axis=1), radius
+
+
+def neighbour_groups(host1, host2, num1, num2, ang_max, block=256):
+    """Groups for pg_*_neighbours_grouped: the healpix rows of both sets
+    (objects are stored sorted by healpix) with, per row of the query set,
+    every row of the other set whose bounding cap comes within ang_max of
+    the row's cap (triangle inequality: a superset of the rows that can hold
+    a neighbour, the role of healpy.query_disc in cf.fill_neighs,
+    py/picca/cf.py:105-122). Returns host arrays, or None when a set is not
+    sorted by row (the brute-force search is then used)."""
+    if num1 == 0 or num2 == 0:
+        return None
+    b1 = _group_bounds(np.asarray(host1["row"])[:num1])
+    b2 = _group_bounds(np.asarray(host2["row"])[:num2])
+    if b1 is None or b2 is None:
+        return None
+    c1, r1 = _caps({k: np.asarray(host1[k])[:num1] for k in ("x_cart", "y_cart", "z_cart")}, b1)
+    c2, r2 = _caps({k: np.asarray(host2[k])[:num2] for k in ("x_cart", "y_cart", "z_cart")}, b2)
+    sep = np.arccos(np.clip(c1 @ c2.T, -1.0, 1.0))
+    reach = float(ang_max) + r1[:, None] + r2[None, :] + 1e-6
+    cand = sep <= reach
+    cand_offsets = np.zeros(b1.size, dtype=np.int32)
+    np.cumsum(cand.sum(axis=1), out=cand_offsets[1:])
+    cand_groups = np.nonzero(cand)[1].astype(np.int32)  # row-major: ascending per group
+    sizes = np.diff(b1)
+    nblk = (sizes + block - 1) // block
+    block_group = np.repeat(np.arange(b1.size - 1, dtype=np.int32), nblk)
+    first_of_group = np.repeat(b1[:-1], nblk)
+    k = np.arange(block_group.size) - np.repeat(np.concatenate([[0], np.cumsum(nblk)[:-1]]), nblk)
+    block_first = (first_of_group + k * block).astype(np.int64)
+    block_end = np.minimum(block_first + block, np.repeat(b1[1:], nblk)).astype(np.int64)
+    return {"start2": b2, "cand_offsets": cand_offsets,
+            "cand_groups": cand_groups if cand_groups.size else np.zeros(1, dtype=np.int32),
+            "block_group": block_group, "block_first": block_first, "block_end": block_end,
+            "num_groups1": b1.size - 1, "num_groups2": b2.size - 1}
+
+
 class PairEngine:
     """Neighbour search + pair accumulation on one CUDA device."""
 
@@ -145,13 +208,46 @@ class PairEngine:
     def _stream(self):
         return ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
 
-    def neighbours(self, params, dev1, dev2=None, xcf=False):
-        """Neighbour CSR (offsets int64 [n1+1], index int32) on the device."""
+    def groups(self, params, dev1, dev2=None):
+        """Device copy of the grouped-search structure of (dev1, dev2), cached
+        per pair of sets and ang_max; None when a set is not sorted by row."""
+        other = dev2 if dev2 is not None else dev1
+        key = (id(dev1), id(other), float(params.ang_max))
+        cache = getattr(self, "_groups_cache", None)
+        if cache is not None and cache[0] == key:
+            return cache[1]
+        host = neighbour_groups(dev1.host, other.host, dev1.num, other.num, params.ang_max)
+        if host is None:
+            out = None
+        else:
+            tensors = {k: torch.from_numpy(np.ascontiguousarray(v)).to(self.device)
+                       for k, v in host.items() if isinstance(v, np.ndarray)}
+            c = NbrGroupsC(int(host["num_groups1"]), int(host["num_groups2"]),
+                           int(host["block_group"].size), 0,
+                           *[tensors[k].data_ptr() for k in
+                             ("start2", "cand_offsets", "cand_groups", "block_group",
+                              "block_first", "block_end")])
+            out = (c, tensors, (dev1, other))  # keeps the sets alive with the key
+        self._groups_cache = (key, out)
+        return out
+
+    def neighbours(self, params, dev1, dev2=None, xcf=False, grouped=True):
+        """Neighbour CSR (offsets int64 [n1+1], index int32) on the device.
+        With ``grouped`` (the default) only candidate healpix rows are
+        scanned (``neighbour_groups``); the lists are the same."""
         lib = _native.lib()
         n1 = dev1.num
         counts = torch.zeros(max(n1, 1), dtype=torch.int64, device=self.device)
         s2 = ctypes.byref(dev2.c) if dev2 is not None else None
-        func = lib.pg_xcf_neighbours if xcf else lib.pg_cf_neighbours
+        groups = self.groups(params, dev1, dev2) if grouped else None
+        if groups is not None:
+            gfunc = lib.pg_xcf_neighbours_grouped if xcf else lib.pg_cf_neighbours_grouped
+            gref = ctypes.byref(groups[0])
+
+            def func(plan, par, d1, d2, cnt, off, idx, stream):
+                return gfunc(plan, par, d1, d2, gref, cnt, off, idx, stream)
+        else:
+            func = lib.pg_xcf_neighbours if xcf else lib.pg_cf_neighbours
         with torch.cuda.device(self.device):
             check(func(self.plan.handle, ctypes.byref(params), ctypes.byref(dev1.c), s2,
                        counts.data_ptr(), None, None, self._stream()), "neighbour count")
@@ -236,12 +332,15 @@ def normalise(we, xi, rp, rt, zz):
     return xi, rp, rt, zz
 
 
-def correlate(fs1, fs2, params, mode=MODE_FP64, xcf=False, engine=None, device=None):
+def correlate(fs1, fs2, params, mode=MODE_FP64, xcf=False, engine=None, device=None,
+              pinned=False):
     """Whole correlation of ForestSets: returns a dict with per-row raw
-    sums, normalised rows and run statistics (host numpy arrays)."""
+    sums, normalised rows and run statistics (host numpy arrays). With
+    ``pinned`` the host arrays are staged in page-locked memory and uploaded
+    asynchronously."""
     engine = engine or PairEngine(device)
-    dev1 = DeviceForests(fs1, engine.device)
-    dev2 = DeviceForests(fs2, engine.device) if fs2 is not None else None
+    dev1 = DeviceForests(fs1, engine.device, pinned=pinned)
+    dev2 = DeviceForests(fs2, engine.device, pinned=pinned) if fs2 is not None else None
     nbins = params.num_bins_r_par * params.num_bins_r_trans
     num_rows = len(fs1.healpix_list)
     offsets, index, total = engine.neighbours(params, dev1, dev2, xcf=xcf)
@@ -250,7 +349,8 @@ def correlate(fs1, fs2, params, mode=MODE_FP64, xcf=False, engine=None, device=N
     engine.accumulate(params, dev1, dev2, offsets, index, order, num_work, rows, mode, xcf=xcf)
     stats = engine.stats()
     we, xi, rp, rt, zz, nb = rows_to_numpy(rows, max(num_rows, 1), nbins)
-    return {"raw": (we, xi, rp, rt, zz, nb), "num_rows": num_rows, "nbins": nbins,
+    h2d = dev1.h2d_bytes + (dev2.h2d_bytes if dev2 is not None else 0)
+    return {"raw": (we, xi, rp, rt, zz, nb), "num_rows": num_rows, "nbins": nbins, "h2d_bytes": h2d,
             "num_pairs_forest": total, "candidate_pairs": candidates,
             "rechecked_pairs": int(stats.rechecked_pairs), "work_items": int(stats.work_items),
             "visited_pairs": int(stats.visited_pairs),

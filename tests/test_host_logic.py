@@ -78,3 +78,41 @@ def test_per_pixel_chunks_match_one_call():
                               cosmo.get_r_comov(z))
         got = deltaio.per_pixel(lambda a, b: a * ((1 + b) / 3.25)**2.8, [w, z], 4, chunk)
         assert np.array_equal(got, w * ((1 + z) / 3.25)**2.8)
+
+
+def test_neighbour_groups_cover_every_neighbour():
+    """The grouped neighbour search scans, for each healpix row of the
+    query set, only the candidate rows of neighbour_groups: every pair of
+    objects closer than ang_max must fall in a candidate row pair, and the
+    block list must cover every query exactly once (within one row)."""
+    import torch  # noqa: F401  (pairs imports torch)
+    from picca_gb300 import pairs, synthetic
+    fs = synthetic.make_forests(3000, 5, (140.0, 170.0), (-10.0, 20.0), 2.1, 3.5, "uniform")
+    qs = synthetic.make_quasars(2500, 6, (140.0, 170.0), (-10.0, 20.0))
+    ang_max = synthetic.correlation_ang_max(200.0, float(fs.z.min()))
+    for other in (fs, qs):
+        h1 = pairs.DeviceForests._host_arrays(fs, True)
+        h2 = pairs.DeviceForests._host_arrays(other, True)
+        g = pairs.neighbour_groups(h1, h2, fs.num, other.num, ang_max, block=64)
+        assert g is not None
+        row1 = np.asarray(h1["row"])
+        start2 = g["start2"]
+        grp2 = np.searchsorted(start2, np.arange(other.num), side="right") - 1
+        v1 = np.stack([h1["x_cart"], h1["y_cart"], h1["z_cart"]], axis=1)
+        v2 = np.stack([h2["x_cart"], h2["y_cart"], h2["z_cart"]], axis=1)
+        ang = np.arccos(np.clip(v1 @ v2.T, -1, 1))
+        i, j = np.nonzero(ang < ang_max * 1.001)
+        # group index of set 1 = rank of its row run
+        grp1 = np.searchsorted(np.unique(row1), row1)
+        for a, b in zip(grp1[i], grp2[j]):
+            lo, hi = g["cand_offsets"][a], g["cand_offsets"][a + 1]
+            assert b in g["cand_groups"][lo:hi]
+        for a in range(g["num_groups1"]):
+            c = g["cand_groups"][g["cand_offsets"][a]:g["cand_offsets"][a + 1]]
+            assert np.all(np.diff(c) > 0)
+        covered = np.zeros(fs.num, dtype=int)
+        for grp, first, end in zip(g["block_group"], g["block_first"], g["block_end"]):
+            assert 0 < end - first <= 64
+            covered[first:end] += 1
+            assert np.all(grp1[first:end] == grp)
+        assert np.all(covered == 1)
