@@ -311,7 +311,9 @@ typedef struct pg_cont_stacks {
  * chi2 of the continuum model. start (optional, [2*num], device) gives a
  * warm start (zero_point, slope) per forest; NULL starts from the
  * ivar-weighted mean flux and slope 0 (utils.py:92-94). Iterations stop
- * when the step is below tol * max(1, |a|, |b|) or after max_iter. */
+ * when the step is below tol * max(1, |a|, |b|) or after max_iter. With a
+ * start and max_iter == 0 nothing is fitted: the continuum, chi2 and status
+ * are evaluated at the given (zero_point, slope). */
 int pg_cont_fit_batch(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
                 const double *start, int32_t max_iter, double tol, int32_t mode,
                 const pg_cont_fit *out, void *stream);

@@ -331,6 +331,11 @@ class Dr16Oracle:
                                         kind="cubic")
             self.get_fudge = interp1d(self.var_grid[w], fudge[w], fill_value="extrapolate",
                                       kind="cubic")
+        self.update_stack(sums)
+
+    def update_stack(self, sums):
+        """compute_delta_stack's normalisation (expected_flux.py:226-236)."""
+        grid = self.grid
         stack = sums["s_num"].copy()
         w = sums["s_w"] > 0
         stack[w] /= sums["s_w"][w]
@@ -338,12 +343,17 @@ class Dr16Oracle:
                                         fill_value="extrapolate")
 
     def run(self, raw):
-        """All iterations; returns the last (continua, fit parameters)."""
+        """All iterations; returns the last (continua, fit parameters). As in
+        compute_expected_flux (dr16_expected_flux.py:426-449) the delta stack
+        is computed after the variance functions are updated, so its weights
+        use the new ones."""
         conts = params = None
         for iteration in range(self.num_iterations):
             conts, params = self.fit_all(raw)
             last = iteration == self.num_iterations - 1
             self.update(self.stacks(raw, conts), last)
+            if not last:
+                self.update_stack(self.stacks(raw, conts))
         return conts, params
 
     def deltas(self, raw, conts):

@@ -161,8 +161,13 @@ class Dr16Gpu:
             self.plan = _native.Plan()
         _bind()
         rest = grid.log_lambda_rest_frame_grid
-        self.log_lambda_var_func_grid = np.linspace(grid.log_lambda_grid[0],
-                                                    grid.log_lambda_grid[-1], num_bins_variance)
+        # _initialize_variance_wavelength_array (expected_flux.py:122-142)
+        if getattr(grid, "wave_solution", "log") == "lin":
+            self.log_lambda_var_func_grid = np.log10(np.linspace(
+                10**grid.log_lambda_grid[0], 10**grid.log_lambda_grid[-1], num_bins_variance))
+        else:
+            self.log_lambda_var_func_grid = np.linspace(
+                grid.log_lambda_grid[0], grid.log_lambda_grid[-1], num_bins_variance)
         # initial interpolators (dr16_expected_flux.py:198-286, expected_flux.py:95-113)
         self.mean_cont_x = rest.copy()
         self.mean_cont_y = np.ones_like(rest)
@@ -259,8 +264,8 @@ class Dr16Gpu:
                 self.plan.handle, ctypes.byref(spectra.c), ctypes.byref(model), start_ptr,
                 None if index is None else index.data_ptr(),
                 n if index is None else int(index.numel()),
-                int(max_iter or self.max_iter), float(self.tol), mode, ctypes.byref(fit_c),
-                self._stream()), "continuum fit")
+                int(self.max_iter if max_iter is None else max_iter), float(self.tol), mode,
+                ctypes.byref(fit_c), self._stream()), "continuum fit")
             if mode == FIT_MIXED:
                 # forests whose optimum the FP32 terms cannot place to 1e-7:
                 # FP64 Newton from the mixed solution
@@ -338,18 +343,9 @@ class Dr16Gpu:
         """Variance statistics and the (eta, var_lss, fudge) fits
         (least_squares_var_stats.py:183-198, dr16_expected_flux.py:531-617)."""
         nvb = self.num_bins_variance
-        var_delta = sums["v_d2"].copy()
-        mean_delta = sums["v_mean"].copy()
-        var2_delta = sums["v_d4"].copy()
-        num_pixels = sums["v_np"]
-        num_qso = sums["v_nq"]
-        w = num_pixels > 0
-        var_delta[w] /= num_pixels[w]
-        mean_delta[w] /= num_pixels[w]
-        var_delta -= mean_delta**2
-        var2_delta[w] /= num_pixels[w]
-        var2_delta -= var_delta**2
-        var2_delta[w] /= num_pixels[w]
+        stats = normalise_var_stats(sums)
+        var_delta, var2_delta = stats["var_delta"], stats["var2_delta"]
+        num_pixels, num_qso = stats["num_pixels"], stats["num_qso"]
         var_pipe_values = 10**(VAR_PIPE_MIN + ((np.arange(NUM_VAR_BINS) + .5) *
                                                (VAR_PIPE_MAX - VAR_PIPE_MIN) / NUM_VAR_BINS))
         eta = interp1d(self.var_x, self.eta, kind="cubic", fill_value="extrapolate")(
@@ -387,6 +383,24 @@ class Dr16Gpu:
         self.stack_y = stack[w]
         self.stack_weight = weight[w]
 
+    def update_model(self, spectra, fit, last):
+        """The updates of one iteration after the fits, in the reference's
+        order (dr16_expected_flux.py:426-449): mean continuum and variance
+        statistics from the weights of the current variance functions, then
+        (except after the last iteration) the new mean continuum and variance
+        functions, then the delta stack with the weights of the NEW variance
+        functions (compute_delta_stack runs after compute_var_stats)."""
+        refit = (not last) and self.fit_functions
+        sums = self._stacks(spectra, fit, mean_cont=not last, var_stats=refit,
+                            delta_stack=not refit)
+        if not last:
+            self.update_mean_cont(sums)
+            if self.fit_functions:
+                self.update_var_functions(sums)
+                sums = self._stacks(spectra, fit, mean_cont=False, var_stats=False,
+                                    delta_stack=True)
+        self.update_stack(sums)
+
     def run(self, spectra, start=None, mode=None, on_iteration=None):
         """The Dr16 outer loop. ``start`` optionally warm-starts every
         iteration's fit (e.g. with learned (a, b)); ``on_iteration(iteration,
@@ -395,14 +409,7 @@ class Dr16Gpu:
         fit = None
         for iteration in range(self.num_iterations):
             fit = self.fit(spectra, start=start, mode=mode)
-            last = iteration == self.num_iterations - 1
-            sums = self._stacks(spectra, fit, mean_cont=not last,
-                                var_stats=(not last) and self.fit_functions, delta_stack=True)
-            if not last:
-                self.update_mean_cont(sums)
-                if self.fit_functions:
-                    self.update_var_functions(sums)
-            self.update_stack(sums)
+            self.update_model(spectra, fit, iteration == self.num_iterations - 1)
             self.history.append({"iteration": iteration,
                                  "iterations_mean": float(fit["iterations"].float().mean()),
                                  "accepted": int((fit["status"] == 0).sum())})
@@ -425,6 +432,25 @@ class Dr16Gpu:
         torch.cuda.synchronize(dev)
         del keep
         return delta, weights
+
+
+def normalise_var_stats(sums):
+    """The normalisation of the variance statistics
+    (LeastsSquaresVarStats.initialize_delta_arrays,
+    least_squares_var_stats.py:176-184) applied to the bin sums."""
+    var_delta = sums["v_d2"].copy()
+    mean_delta = sums["v_mean"].copy()
+    var2_delta = sums["v_d4"].copy()
+    num_pixels = sums["v_np"]
+    w = num_pixels > 0
+    var_delta[w] /= num_pixels[w]
+    mean_delta[w] /= num_pixels[w]
+    var_delta -= mean_delta**2
+    var2_delta[w] /= num_pixels[w]
+    var2_delta -= var_delta**2
+    var2_delta[w] /= num_pixels[w]
+    return {"var_delta": var_delta, "var2_delta": var2_delta, "mean_delta": mean_delta,
+            "num_pixels": num_pixels, "num_qso": sums["v_nq"]}
 
 
 def fit_var_bin(var_delta, var2_delta, num_qso, var_pipe_values, min_num_qso, limit_eta,

@@ -408,7 +408,8 @@ int pg_cont_fit_select(pg_plan *plan, const pg_spectra *spectra, const pg_cont_m
     if ((rc = validate_spectra(spectra)) || (rc = validate_model(model)) ||
         (rc = validate_fit(out, false)))
         return rc;
-    if (max_iter < 1 || !(tol > 0) || (mode != PG_FIT_FP64 && mode != PG_FIT_MIXED))
+    if (max_iter < 0 || (max_iter == 0 && !start) || !(tol > 0) ||
+        (mode != PG_FIT_FP64 && mode != PG_FIT_MIXED))
         return PG_ERR_INVALID_ARGUMENT;
     if ((rc = select_device(plan))) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);

@@ -228,7 +228,8 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_kernel(
         double s[6];
         eval_all<T>(px, a, b, const_w, s);
         int it = 0;
-        bool converged = false;
+        // max_iter == 0 with a start: evaluate the model at the given (a, b)
+        bool converged = max_iter == 0 && start != nullptr;
         for (; it < max_iter; ++it) {
             double da, db;
             if (m.order == 0) {
@@ -511,7 +512,9 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
         float s[6];
         eval_all_f(px, ah, bh, const_w, s);
         int it = 0;
-        bool converged = false;
+        // max_iter == 0 with a start: evaluate the model at the given (a, b)
+        const bool evaluate_only = max_iter == 0 && start != nullptr;
+        bool converged = evaluate_only;
         for (; it < max_iter; ++it) {
             // Newton step. The 2x2 determinant and numerators are formed in
             // FP64 from the FP32 sums (products of two FP32 numbers are exact
@@ -622,7 +625,7 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
         // rms(g)): large when the data barely separate a from b (a forest
         // covering a short stretch of the rest-frame window)
         bool refine = false;
-        if (lane == 0 && converged) {
+        if (lane == 0 && converged && !evaluate_only) {
             const float ua = 8.f * 5.96e-8f * sqrtf(ga_abs);
             const float ub = 8.f * 5.96e-8f * sqrtf(gb_abs);
             const float ref = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));

@@ -67,7 +67,7 @@ constexpr int kAccQ = 64;                     // run ring per warp (<= 31 + 32 e
 constexpr int kChunk = 128;                   // forest-2 pixels staged per warp at a time
 constexpr int kRunMax = 64;                   // pairs summed in FP32 registers per run
 constexpr int kXcfP = 2;                      // quasars per lane per pass
-constexpr int kCfBlock = 768;
+constexpr int kCfBlock = 640;
 constexpr int kXcfBlock = 512;
 
 struct FastConst {
@@ -203,10 +203,9 @@ __device__ __forceinline__ unsigned round_rem(float x, float &rem) {
     return __float_as_uint(y) - kMagicBits;
 }
 
-// Shared-memory layout of both kernels (offsets in bytes from the start).
-// p1: float4 (rho, dist_m, z, w) per forest-1 pixel; p2: float2 (delta*w as
-// hi, lo); acc0 / acc1: float4 pairs of the accepted-pair rings; queue: the
-// FP64 re-decision entries.
+// Shared-memory layout of the cross-correlation kernel (byte offsets from
+// the start). p1: float4 (rho, dist_m, z, w) per forest pixel; p2: float4
+// (delta*w hi, lo, rho lo, 0); queue: the FP64 re-decision entries.
 struct SmemLayout {
     size_t cells, p1, p2, acc0, acc1, queue, total;
 };
@@ -218,7 +217,7 @@ __host__ __device__ inline SmemLayout smem_layout(int nbins, int max_pix1, int n
     l.cells = 0;
     l.p1 = l.cells + (size_t)((nbins + 3) & ~3) * H_COUNT * 4;
     l.p2 = l.p1 + mp * 16;
-    l.acc0 = l.p2 + mp * 8;
+    l.acc0 = l.p2 + mp * 16;
     l.acc1 = l.acc0 + (acc_queue ? (size_t)nwarps * kAccQ * 16 : 0);
     l.queue = l.acc1 + (acc_queue ? (size_t)nwarps * kAccQ * 16 : 0);
     l.total = l.queue + (size_t)nwarps * kQueue * 4;
@@ -226,20 +225,24 @@ __host__ __device__ inline SmemLayout smem_layout(int nbins, int max_pix1, int n
 }
 
 // Stages a forest of set 1 (n1 pixels from a0) in shared memory relative to
-// r_ref and records its largest |rho| in *max_rho_bits (a non-negative
-// float's bits order as unsigned). Returns whether rho and dist_m are
-// non-decreasing along the forest (block-wide, after a barrier).
+// r_ref: p1 = (rho, dist_m, z, w), p2 = (delta*w hi, lo, rho lo, 0) with
+// rho + rho lo = r - r_ref to 2^-48 (the low part sharpens the r_par that is
+// summed, not the bin decision). Records the largest |rho| in *max_rho_bits
+// (a non-negative float's bits order as unsigned). Returns whether rho and
+// dist_m are non-decreasing along the forest (block-wide, after a barrier).
 __device__ __forceinline__ bool stage_forest1(const pg_forest_set &s1, int64_t a0, int n1,
-                                              double r_ref, float4 *p1, float2 *p2,
+                                              double r_ref, float4 *p1, float4 *p2,
                                               unsigned *max_rho_bits) {
     bool ordered = true;
     float local_max = 0.f;
     for (int i = threadIdx.x; i < n1; i += blockDim.x) {
         const double w = s1.weights[a0 + i];
-        const float rho = (float)(s1.r_comov[a0 + i] - r_ref);
+        const double rho_d = s1.r_comov[a0 + i] - r_ref;
+        const float rho = (float)rho_d;
         const float d = (float)s1.dist_m[a0 + i];
         p1[i] = make_float4(rho, d, (float)s1.z[a0 + i], weight32(w));
-        p2[i] = split2(s1.delta[a0 + i] * w);
+        const float2 dw = split2(s1.delta[a0 + i] * w);
+        p2[i] = make_float4(dw.x, dw.y, (float)(rho_d - (double)rho), 0.f);
         local_max = fmaxf(local_max, fabsf(rho));
         if (i + 1 < n1)
             ordered &= (float)(s1.r_comov[a0 + i + 1] - r_ref) >= rho &&
@@ -327,10 +330,11 @@ __device__ __forceinline__ int count_leading(const float4 *x, int n, float v) {
 }
 
 // Shared-memory layout of the auto-correlation kernel (byte offsets):
-// block histograms; forest 1 as float4 (rho, dist_m, z, w) and float2
-// (delta*w hi, lo); then per warp the staged forest-2 chunk as float4 (nB,
-// t, z, w) and float2 (delta*w hi, lo), the run ring (two float4 per entry),
-// the FP64 re-decision queue and the forest-1 zerr veto bits.
+// block histograms; forest 1 as float4 (rho, dist_m, z, w) and float4
+// (delta*w hi, lo, rho lo, 0); then per warp the staged forest-2 chunk as
+// float4 (nB, t, z, w) and float4 (delta*w hi, lo, nB lo, 0), the run ring
+// (two float4 per entry), the FP64 re-decision queue and the forest-1 zerr
+// veto bits.
 struct CfSmem {
     size_t cells, p1, p1x, warps, per_warp, buf, bufx, acc0, acc1, queue, veto, total;
 };
@@ -341,10 +345,10 @@ __host__ __device__ inline CfSmem cf_smem(int nbins, int max_pix1, int nwarps) {
     l.cells = 0;
     l.p1 = (size_t)((nbins + 3) & ~3) * H_COUNT * 4;
     l.p1x = l.p1 + mp * 16;
-    l.warps = l.p1x + mp * 8;
+    l.warps = l.p1x + mp * 16;
     l.buf = 0;
     l.bufx = l.buf + (size_t)kChunk * 16;
-    l.acc0 = l.bufx + (size_t)kChunk * 8;
+    l.acc0 = l.bufx + (size_t)kChunk * 16;
     l.acc1 = l.acc0 + (size_t)kAccQ * 16;
     l.queue = l.acc1 + (size_t)kAccQ * 16;
     l.veto = l.queue + (size_t)kCfQueue * 4;
@@ -410,10 +414,10 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
     const CfSmem L = cf_smem(nbins, max_pix1, nwarps);
     float *h = reinterpret_cast<float *>(smem + L.cells);
     const float4 *p1 = reinterpret_cast<const float4 *>(smem + L.p1);
-    const float2 *p1x = reinterpret_cast<const float2 *>(smem + L.p1x);
+    const float4 *p1x = reinterpret_cast<const float4 *>(smem + L.p1x);
     unsigned char *wbase = smem + L.warps + (size_t)warp * L.per_warp;
     float4 *buf = reinterpret_cast<float4 *>(wbase + L.buf);
-    float2 *bufx = reinterpret_cast<float2 *>(wbase + L.bufx);
+    float4 *bufx = reinterpret_cast<float4 *>(wbase + L.bufx);
     float4 *acc0 = reinterpret_cast<float4 *>(wbase + L.acc0);
     float4 *acc1 = reinterpret_cast<float4 *>(wbase + L.acc1);
     uint32_t *queue = reinterpret_cast<uint32_t *>(wbase + L.queue);
@@ -443,7 +447,7 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
             nbr_next = nbr_offsets[f1];
         }
         const bool sorted1 = stage_forest1(s1, a0, n1, r_ref, const_cast<float4 *>(p1),
-                                           const_cast<float2 *>(p1x), &max_rho_bits);
+                                           const_cast<float4 *>(p1x), &max_rho_bits);
         const ParGuard pg = par_guard(fcp, __uint_as_float(max_rho_bits));
         const float h_par = pg.h_par, low_clamp = pg.low_clamp;
         const int64_t k1 = nbr_offsets[f1 + 1];
@@ -518,12 +522,17 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                     bool ok = w2 != 0;
                     if (EXTRA && zerr_pair && ok)
                         ok = !zerr_veto(s2.z[jj], f1_geom[6], b.zerr_kms);
-                    const float rho2 = (float)(s2.r_comov[jj] - r_ref);
+                    const double rho2_d = s2.r_comov[jj] - r_ref;
+                    const float rho2 = (float)rho2_d;
                     const float d2 = (float)s2.dist_m[jj];
-                    buf[jl] = make_float4(-__fmul_rn(cp, rho2),
-                                          ok ? __fmaf_rn(st, d2, -0.5f) : kFar,
+                    // nB = -cp rho2 as hi + lo (exact to 2^-48): hi decides,
+                    // hi + lo enters the summed r_par
+                    const double nb_d = -((double)cp * rho2_d);
+                    const float nb_h = -__fmul_rn(cp, rho2);
+                    buf[jl] = make_float4(nb_h, ok ? __fmaf_rn(st, d2, -0.5f) : kFar,
                                           (float)s2.z[jj], ok ? weight32(w2) : 0.f);
-                    bufx[jl] = split2(s2.delta[jj] * w2);
+                    const float2 dw = split2(s2.delta[jj] * w2);
+                    bufx[jl] = make_float4(dw.x, dw.y, (float)(nb_d - (double)nb_h), 0.f);
                     valid2 &= ok;
                     if (jl + 1 < jn)
                         ordered2 &= (float)(s2.r_comov[jj + 1] - r_ref) >= rho2 &&
@@ -643,15 +652,18 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                         }
                         if (brk) run_bin = bin;
                         if (acc) {
-                            const float2 x1 = p1x[i];
-                            const float2 x2 = bufx[jl];
+                            const float4 x1 = p1x[i];
+                            const float4 x2 = bufx[jl];
                             const float w12 = q1.w * q2.w;
                             float th, tl;
                             two_prod(x1.x, x1.y, x2.x, x2.y, th, tl);
                             two_sum_into(r_xi, r_xil, th);
                             r_xil += tl;
                             r_w += w12;
-                            r_pw = __fmaf_rn(pv, w12, r_pw);
+                            // r_par (bin units) from the hi + lo distances:
+                            // relative precision for the summed r_par
+                            const float pp_s = pp + __fmaf_rn(cp, x1.z, x2.z);
+                            r_pw = __fmaf_rn(AUTO ? fabsf(pp_s) : pp_s, w12, r_pw);
                             r_tw = __fmaf_rn(xt + 0.5f, w12, r_tw);
                             r_zw = __fmaf_rn(zs, w12, r_zw);
                             ++run_n;
@@ -762,7 +774,7 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
     const SmemLayout L = smem_layout(nbins, max_pix1, nwarps, false);
     float *h = reinterpret_cast<float *>(smem + L.cells);
     float4 *p1 = reinterpret_cast<float4 *>(smem + L.p1);
-    float2 *p2 = reinterpret_cast<float2 *>(smem + L.p2);
+    float4 *p2 = reinterpret_cast<float4 *>(smem + L.p2);
     uint32_t *queue = reinterpret_cast<uint32_t *>(smem + L.queue) + warp * kQueue;
     zero_all(h, H_COUNT * hs);
     unsigned long long rechecks = 0, overflows = 0;
@@ -790,12 +802,13 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
         ctx.k0 = nbr_offsets[f];
         const int nq = (int)nq_64;
         for (int kb = warp * 32 * kXcfP; kb < nq; kb += nwarps * 32 * kXcfP) {
-            float cp[kXcfP], st[kXcfP], nb[kXcfP], t[kXcfP], zv[kXcfP], wvh[kXcfP], wvl[kXcfP];
+            float cp[kXcfP], st[kXcfP], nb[kXcfP], nbl[kXcfP], t[kXcfP], zv[kXcfP], wvh[kXcfP],
+                wvl[kXcfP];
             bool any = false;
 #pragma unroll
             for (int p = 0; p < kXcfP; ++p) {
                 const int kk = kb + lane + 32 * p;
-                cp[p] = 1.f; st[p] = 0.f; nb[p] = kFar; t[p] = kFar; zv[p] = kFar;
+                cp[p] = 1.f; st[p] = 0.f; nb[p] = kFar; nbl[p] = 0.f; t[p] = kFar; zv[p] = kFar;
                 wvh[p] = 0.f; wvl[p] = 0.f;
                 if (kk < nq) {
                     const int64_t g = nbr_index[ctx.k0 + kk];
@@ -809,8 +822,10 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
                                                       objs.z_cart[g], objs.ra[g], objs.dec[g]);
                         cp[p] = (float)(cos(ang / 2) * inv_p);
                         st[p] = (float)(sin(ang / 2) * inv_t);
-                        const float rho_q = (float)(objs.obj_r_comov[g] - r_ref);
+                        const double rho_d = objs.obj_r_comov[g] - r_ref;
+                        const float rho_q = (float)rho_d;
                         nb[p] = -__fmul_rn(cp[p], rho_q);
+                        nbl[p] = (float)(-((double)cp[p] * rho_d) - (double)nb[p]);
                         t[p] = __fmaf_rn(st[p], (float)objs.obj_dist_m[g], -0.5f);
                         zv[p] = (float)objs.z_qso[g];
                         wvh[p] = weight32(wq);
@@ -823,7 +838,7 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
             for (int i = 0; i < n1; ++i) {
                 const float4 q = p1[i];
                 if (q.w == 0.f) continue;
-                const float2 qd = p2[i];
+                const float4 qd = p2[i];
                 unsigned near_mask = 0;
 #pragma unroll
                 for (int p = 0; p < kXcfP; ++p) {
@@ -851,7 +866,9 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
                         const unsigned bin = ip * nt + it;
                         float th, tl;
                         two_prod(qd.x, qd.y, wvh[p], wvl[p], th, tl);
-                        hist_add(h, hs, bin, th, tl, w12, pv * w12, (xt + 0.5f) * w12,
+                        // summed r_par from the hi + lo distances
+                        const float pv_s = pv + __fmaf_rn(cp[p], qd.z, nbl[p]);
+                        hist_add(h, hs, bin, th, tl, w12, pv_s * w12, (xt + 0.5f) * w12,
                                  zs * w12, 1);
                     }
                 }

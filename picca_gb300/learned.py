@@ -249,14 +249,7 @@ def collect_training(engine, spectra):
         t, ok = targets_from_fit(fit, a0)
         feats.append(feat[ok])
         targs.append(t[ok])
-        last = iteration == engine.num_iterations - 1
-        sums = engine._stacks(spectra, fit, mean_cont=not last,
-                              var_stats=(not last) and engine.fit_functions, delta_stack=True)
-        if not last:
-            engine.update_mean_cont(sums)
-            if engine.fit_functions:
-                engine.update_var_functions(sums)
-        engine.update_stack(sums)
+        engine.update_model(spectra, fit, iteration == engine.num_iterations - 1)
         del keep
     return torch.cat(feats), torch.cat(targs), fit
 
@@ -268,14 +261,7 @@ def run_warm(engine, spectra, mlp, warm_max_iter=8, mode=None):
     fit = None
     for iteration in range(engine.num_iterations):
         fit, _, fallback = warm_fit(engine, spectra, mlp, warm_max_iter=warm_max_iter, mode=mode)
-        last = iteration == engine.num_iterations - 1
-        sums = engine._stacks(spectra, fit, mean_cont=not last,
-                              var_stats=(not last) and engine.fit_functions, delta_stack=True)
-        if not last:
-            engine.update_mean_cont(sums)
-            if engine.fit_functions:
-                engine.update_var_functions(sums)
-        engine.update_stack(sums)
+        engine.update_model(spectra, fit, iteration == engine.num_iterations - 1)
         stats.append({"fallback": int(fallback.sum().item()),
                       "iterations_mean": float(fit["iterations"].float().mean().item())})
     return fit, stats

@@ -2,7 +2,9 @@
 
 Each forest is observed on picca's log-lambda grid (step 3e-4, observed
 3600-5500 Angstrom, rest frame 1040-1200 Angstrom; the Dr16 defaults of
-py/picca/delta_extraction/data.py:44-50). The flux is
+py/picca/delta_extraction/data.py:44-50) or on the linear grid of DESI
+(``wave_solution="lin"``, step 0.8 Angstrom, the rest-frame step equal to
+it, data.py:402-410). The flux is
 
     f = A * C(lambda_rf) * (1 + s * (x - 1/2)) * F + noise,
 
@@ -26,15 +28,43 @@ LINES = (1033.8, 1073.0, 1123.0)
 
 
 class Grid:
-    """Observed and rest-frame log-lambda grids (Forest class variables)."""
+    """Observed and rest-frame wavelength grids (the Forest class variables
+    of Forest.set_class_variables,
+    py/picca/delta_extraction/astronomical_objects/forest.py:694-748):
+    evenly spaced in log10(lambda) (``wave_solution="log"``, steps in
+    log10 Angstrom) or in lambda (``"lin"``, steps in Angstrom)."""
 
     def __init__(self, lambda_min=3600.0, lambda_max=5500.0, lambda_min_rest=1040.0,
-                 lambda_max_rest=1200.0, step=3e-4):
+                 lambda_max_rest=1200.0, step=3e-4, wave_solution="log", step_rest=None):
         self.step = step
-        self.log_lambda_grid = np.arange(np.log10(lambda_min), np.log10(lambda_max) + step / 2,
-                                         step)
-        self.log_lambda_rest_frame_grid = np.arange(np.log10(lambda_min_rest),
-                                                    np.log10(lambda_max_rest) + step / 2, step)
+        self.step_rest = step if step_rest is None else step_rest
+        self.wave_solution = wave_solution
+        self.lambda_min = lambda_min
+        if wave_solution == "log":
+            self.log_lambda_grid = np.arange(np.log10(lambda_min),
+                                             np.log10(lambda_max) + step / 2, step)
+            self.log_lambda_rest_frame_grid = np.arange(
+                np.log10(lambda_min_rest), np.log10(lambda_max_rest) + self.step_rest / 2,
+                self.step_rest)
+        elif wave_solution == "lin":
+            self.log_lambda_grid = np.log10(np.arange(lambda_min, lambda_max + step / 2, step))
+            self.log_lambda_rest_frame_grid = np.log10(
+                np.arange(lambda_min_rest, lambda_max_rest + self.step_rest / 2, self.step_rest))
+        else:
+            raise ValueError(f"wave_solution must be 'log' or 'lin', got {wave_solution!r}")
+
+    @property
+    def is_lin(self):
+        return self.wave_solution == "lin"
+
+    def find_bins(self, values, grid_array):
+        """find_bins_log / find_bins_lin (py/picca/delta_extraction/utils.py:139-186)."""
+        if self.is_lin:
+            aux = 10**grid_array[0]
+            step = 10**grid_array[1] - aux
+            return ((10**values - aux) / step + 0.5).astype(np.int64)
+        step = grid_array[1] - grid_array[0]
+        return ((values - grid_array[0]) / step + 0.5).astype(np.int64)
 
 
 class RawForests:
@@ -69,8 +99,13 @@ def make_raw_forests(num, seed, grid=None, z_lo=2.1, z_hi=4.0, z_law="inv2", are
                         grid.log_lambda_rest_frame_grid[0] + np.log10(1 + zq))
         hi = np.minimum(grid.log_lambda_grid[-1],
                         grid.log_lambda_rest_frame_grid[-1] + np.log10(1 + zq))
-        first = np.ceil((lo - ll0) / grid.step - 1e-9).astype(np.int64)
-        last = np.floor((hi - ll0) / grid.step + 1e-9).astype(np.int64)
+        if grid.is_lin:
+            lam0 = grid.lambda_min
+            first = np.ceil((10**lo - lam0) / grid.step - 1e-9).astype(np.int64)
+            last = np.floor((10**hi - lam0) / grid.step + 1e-9).astype(np.int64)
+        else:
+            first = np.ceil((lo - ll0) / grid.step - 1e-9).astype(np.int64)
+            last = np.floor((hi - ll0) / grid.step + 1e-9).astype(np.int64)
         return first, np.maximum(last - first + 1, 0)
 
     # forests shorter than the minimum are rejected as the reader does
@@ -86,7 +121,10 @@ def make_raw_forests(num, seed, grid=None, z_lo=2.1, z_hi=4.0, z_law="inv2", are
     total = int(offset[-1])
     fid = np.repeat(np.arange(num), npix)
     k = k0[fid] + (np.arange(total) - offset[fid])
-    log_lambda = ll0 + k * grid.step
+    if grid.is_lin:
+        log_lambda = np.log10(grid.lambda_min + k * grid.step)
+    else:
+        log_lambda = ll0 + k * grid.step
     lam = 10**log_lambda
     lam_rf = lam / (1 + z_qso[fid])
     cont = (lam_rf / 1100.0) ** -1.5

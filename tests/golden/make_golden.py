@@ -117,6 +117,65 @@ def _convert_cor(src, out_path):
     np.savez_compressed(out_path, **out)
 
 
+class _LimitDict(dict):
+    def __missing__(self, key):
+        return None
+
+
+class _MinuitStandIn:
+    """Stand-in for iminuit.Minuit in the fixture runs (iminuit is not
+    installed; no iminuit code is involved): ``migrad`` minimises the
+    reference's own cost function with SciPy (Nelder-Mead, then L-BFGS-B from
+    its result, limits as bounds, fixed parameters held), ``valid`` reports
+    SciPy's success, ``fval`` is the cost at the result."""
+
+    def __init__(self, fcn, *args, name=None, **start):
+        import inspect
+        self.fcn = fcn
+        if name is None:
+            name = [p for p in inspect.signature(fcn).parameters]
+        self.names = list(name)
+        self.values = {n: float(start[n]) for n in self.names}
+        self.errors = {}
+        self.limits = _LimitDict()
+        self.fixed = {}
+        self.errordef = 1.0
+        self.print_level = 0
+        self.valid = False
+        self.fval = None
+
+    def _cost(self, free, x):
+        vals = dict(self.values)
+        vals.update(zip(free, x))
+        return float(self.fcn(*[vals[n] for n in self.names]))
+
+    def migrad(self):
+        from scipy.optimize import minimize
+        free = [n for n in self.names if not self.fixed.get(n, False)]
+        x0 = np.array([self.values[n] for n in free])
+        bounds = []
+        for n in free:
+            lim = self.limits[n]
+            lo, hi = (None, None) if lim is None else lim
+            bounds.append((-np.inf if lo is None else lo, np.inf if hi is None else hi))
+        x0 = np.clip(x0, [b[0] for b in bounds], [b[1] for b in bounds])
+        cost = lambda x: self._cost(free, x)  # noqa: E731
+        with np.errstate(all="ignore"):
+            res = minimize(cost, x0, method="Nelder-Mead", bounds=bounds,
+                           options={"xatol": 1e-13, "fatol": 1e-13, "maxiter": 20000,
+                                    "maxfev": 40000})
+            res2 = minimize(cost, res.x, method="L-BFGS-B", bounds=bounds,
+                            options={"ftol": 1e-15, "gtol": 1e-12, "maxiter": 2000})
+        best = res2 if res2.fun <= res.fun else res
+        for n, v in zip(free, best.x):
+            self.values[n] = float(v)
+        self.fval = self._cost(free, best.x)
+        self.valid = bool(np.isfinite(self.fval) and (res.success or res2.success))
+
+    def hesse(self):
+        return None
+
+
 def _install_stand_ins():
     """Stand-ins for the reference's third-party imports (no code of those
     projects is involved; the pair functions need none of them)."""
@@ -131,6 +190,9 @@ def _install_stand_ins():
     numba.jit = njit
     numba.int32 = np.int32
     numba.prange = range
+    numba_types = types.ModuleType("numba.types")
+    numba_types.bool_ = np.bool_
+    numba.types = numba_types
     healpy = types.ModuleType("healpy")
     healpy.query_disc = lambda nside, vec, radius, inclusive=True: np.arange(12 * nside * nside)
     healpy.ang2pix = lambda nside, theta, phi: ang2pix_ring(nside, theta, phi)
@@ -139,8 +201,9 @@ def _install_stand_ins():
     camb = types.ModuleType("camb")
     iminuit = types.ModuleType("iminuit")
     iminuit.util = types.SimpleNamespace(IMinuitWarning=Warning)
-    for name, mod in (("numba", numba), ("healpy", healpy), ("fitsio", fitsio),
-                      ("camb", camb), ("iminuit", iminuit)):
+    iminuit.Minuit = _MinuitStandIn
+    for name, mod in (("numba", numba), ("numba.types", numba_types), ("healpy", healpy),
+                      ("fitsio", fitsio), ("camb", camb), ("iminuit", iminuit)):
         sys.modules[name] = mod
 
 
@@ -548,6 +611,146 @@ def _continuum_cases(reference_py):
     return raw.num
 
 
+def _continuum_loop_cases(reference_py, wave_solution, num, seed, iterations=3):
+    """picca's own Dr16 continuum loop on synthetic raw forests:
+    Dr16ExpectedFlux.compute_expected_flux (dr16_expected_flux.py:380-464)
+    run as plain Python, with iminuit replaced by _MinuitStandIn, recording
+    at every iteration (where the reference saves its iteration files) the
+    fit of every forest (zero point, slope, chi2, ndata, reason), the mean
+    continuum (_compute_mean_cont, expected_flux.py:256-308), the variance
+    statistics of LeastsSquaresVarStats (least_squares_var_stats.py:134-198)
+    with the fitted eta / var_lss / fudge, and the delta stack
+    (compute_delta_stack, expected_flux.py:190-236); then populate_los_ids
+    (dr16_expected_flux.py:706-740) and compute_forest_weights (:466-488),
+    and find_bins_log / find_bins_lin (delta_extraction/utils.py:139-186) on
+    the pixels. Written to continuum_loop_<wave_solution>.npz."""
+    sys.dont_write_bytecode = True
+    _install_stand_ins()
+    if reference_py not in sys.path:
+        sys.path.insert(0, reference_py)
+    import logging  # pylint: disable=import-outside-toplevel
+    from scipy.interpolate import interp1d  # pylint: disable=import-outside-toplevel
+    from picca.delta_extraction.astronomical_objects.forest import Forest  # noqa: E501 pylint: disable=import-outside-toplevel
+    import picca.delta_extraction.expected_fluxes.dr16_expected_flux as ref_dr16  # noqa: E501 pylint: disable=import-outside-toplevel
+    from picca.delta_extraction import utils as ref_utils  # noqa: E501 pylint: disable=import-outside-toplevel
+    from picca_gb300 import synthetic_spectra
+
+    step = 3e-4 if wave_solution == "log" else 0.8
+    grid = synthetic_spectra.Grid(step=step, wave_solution=wave_solution)
+    Forest.set_class_variables(3600.0, 5500.0, 1040.0, 1200.0, step, step, wave_solution,
+                               "10**-17 erg/(s cm2 Angstrom)")
+    assert np.array_equal(Forest.log_lambda_grid, grid.log_lambda_grid)
+    assert np.array_equal(Forest.log_lambda_rest_frame_grid, grid.log_lambda_rest_frame_grid)
+    raw = synthetic_spectra.make_raw_forests(num, seed, grid=grid)
+    rng = np.random.default_rng(seed + 1)
+    forests = []
+    for k in range(raw.num):
+        ll, fl, iv, tc = raw.forest(k)
+        iv = iv.copy()
+        iv[rng.random(len(iv)) < 0.03] = 0.0  # masked pixels
+        forests.append(types.SimpleNamespace(
+            log_lambda=ll.copy(), flux=fl.copy(), ivar=iv, transmission_correction=tc.copy(),
+            z=float(raw.z_qso[k]), los_id=int(raw.los_id[k]), continuum=None,
+            bad_continuum_reason=None))
+
+    class _Log:
+        def __getattr__(self, name):
+            return lambda *a, **k: None
+
+    flux = ref_dr16.Dr16ExpectedFlux.__new__(ref_dr16.Dr16ExpectedFlux)
+    flux.logger = _Log()
+    flux.los_ids = {}
+    flux.num_bins_variance = 20
+    flux.num_processors = 1
+    flux.num_iterations = iterations
+    flux.order = 1
+    flux.use_constant_weight = False
+    flux.use_ivar_as_weight = False
+    flux.force_stack_delta_to_zero = True
+    flux.var_lss_mod = 1.0
+    flux.limit_eta = (0.5, 1.5)
+    flux.limit_var_lss = (0.0, 0.3)
+    flux.min_num_qso_in_fit = 5
+    flux.continuum_fit_parameters = None
+    flux.fit_variance_functions = []
+    flux.out_dir = None
+    flux._initialize_variance_wavelength_array()
+    flux._initialize_mean_continuum_arrays()
+    flux._initialize_variance_functions()
+    out = {"wave_solution": np.asarray(wave_solution), "num_iterations": np.asarray(iterations),
+           "min_num_qso_in_fit": np.asarray(5),
+           "pix_offset": np.concatenate([[0], np.cumsum([len(f.flux) for f in forests])]),
+           "log_lambda": np.concatenate([f.log_lambda for f in forests]),
+           "flux": np.concatenate([f.flux for f in forests]),
+           "ivar": np.concatenate([f.ivar for f in forests]),
+           "transmission_correction": np.concatenate([f.transmission_correction
+                                                      for f in forests]),
+           "z_qso": np.array([f.z for f in forests]),
+           "los_id": np.array([f.los_id for f in forests]),
+           "log_lambda_var_func_grid": flux.log_lambda_var_func_grid.copy(),
+           "log_lambda_grid": grid.log_lambda_grid,
+           "log_lambda_rest_frame_grid": grid.log_lambda_rest_frame_grid}
+    var_stats = []
+    original = ref_dr16.LeastsSquaresVarStats
+
+    def recording_var_stats(*args, **kwargs):
+        obj = original(*args, **kwargs)
+        var_stats.append(obj)
+        return obj
+
+    ref_dr16.LeastsSquaresVarStats = recording_var_stats
+    snapshots = []
+
+    def save_iteration_step(iteration):
+        it = len(snapshots)
+        pre = f"it{it}_"
+        params = np.array([flux.continuum_fit_parameters[f.los_id] for f in forests])
+        snap = {pre + "zero_point": params[:, 0], pre + "slope": params[:, 1],
+                pre + "chi2": params[:, 2], pre + "ndata": params[:, 3],
+                pre + "bad": np.array([f.bad_continuum_reason is not None for f in forests]),
+                pre + "stack_x": np.asarray(flux.get_stack_delta.x),
+                pre + "stack_y": np.asarray(flux.get_stack_delta.y)}
+        if it < iterations - 1:
+            snap[pre + "mean_cont_x"] = np.asarray(flux.get_mean_cont.x)
+            snap[pre + "mean_cont_y"] = np.asarray(flux.get_mean_cont.y)
+            snap[pre + "mean_cont_weight"] = np.asarray(flux.get_mean_cont_weight.y)
+            vs = var_stats[-1]
+            snap[pre + "var_delta"] = vs.var_delta
+            snap[pre + "var2_delta"] = vs.var2_delta
+            snap[pre + "num_pixels"] = vs.num_pixels
+            snap[pre + "num_qso"] = vs.num_qso
+            snap[pre + "eta"] = flux.get_eta(flux.log_lambda_var_func_grid)
+            snap[pre + "var_lss"] = flux.get_var_lss(flux.log_lambda_var_func_grid)
+            snap[pre + "fudge"] = flux.get_fudge(flux.log_lambda_var_func_grid)
+            snap[pre + "var_x"] = np.asarray(flux.get_eta.x)
+        snapshots.append(snap)
+
+    flux.save_iteration_step = save_iteration_step
+    logging.disable(logging.CRITICAL)
+    flux.compute_expected_flux(forests)
+    ref_dr16.LeastsSquaresVarStats = original
+    for snap in snapshots:
+        out.update(snap)
+    good = [f for f in forests if f.bad_continuum_reason is None]
+    out["los_good"] = np.array([f.los_id for f in good])
+    out["los_mean_expected_flux"] = np.concatenate(
+        [flux.los_ids[f.los_id]["mean expected flux"] for f in good])
+    out["los_weights"] = np.concatenate([flux.los_ids[f.los_id]["weights"] for f in good])
+    out["los_continuum"] = np.concatenate([flux.los_ids[f.los_id]["continuum"] for f in good])
+    # the weights of the last iteration's continua (compute_forest_weights)
+    out["forest_weights"] = np.concatenate([flux.compute_forest_weights(f, f.continuum)
+                                            for f in good])
+    # find_bins on the observed and rest-frame grids
+    finder = ref_utils.find_bins_log if wave_solution == "log" else ref_utils.find_bins_lin
+    out["bins_obs"] = finder(out["log_lambda"], grid.log_lambda_grid)
+    zpix = np.repeat(out["z_qso"], np.diff(out["pix_offset"]))
+    out["bins_rest"] = finder(out["log_lambda"] - np.log10(1 + zpix),
+                              grid.log_lambda_rest_frame_grid)
+    out["bins_var"] = finder(out["log_lambda"], flux.log_lambda_var_func_grid)
+    np.savez_compressed(os.path.join(HERE, f"continuum_loop_{wave_solution}.npz"), **out)
+    return len(good)
+
+
 def main(picca_root):
     tests = os.path.join(picca_root, "py", "picca", "tests", "data")
     _convert_delta_dir(os.path.join(tests, "test_delta", "Delta_LYA"),
@@ -563,6 +766,8 @@ def main(picca_root):
                             os.path.join(tests, "test_delta", "Delta_LYA") + "/",
                             os.path.join(tests, "test_delta", "delta_attributes.fits.gz"))
     ncont = _continuum_cases(os.path.join(picca_root, "py"))
+    for wave, num, seed in (("log", 240, 606), ("lin", 80, 707)):
+        _continuum_loop_cases(os.path.join(picca_root, "py"), wave, num, seed)
     _convert_dmat(os.path.join(tests, "test_cor", "dmat.fits.gz"),
                   os.path.join(HERE, "cor_dmat.npz"))
     ndm = _dmat_cases(os.path.join(picca_root, "py"),
@@ -675,4 +880,6 @@ def extra_dmat(picca_root):
 
 
 if __name__ == "__main__":
-    main(sys.argv[1] if len(sys.argv) > 1 else "/root/reference")
+    if len(sys.argv) != 2:
+        sys.exit("usage: python tests/golden/make_golden.py /path/to/picca")
+    main(sys.argv[1])

@@ -12,6 +12,7 @@
 """
 
 import numpy as np
+import pytest
 from scipy.optimize import minimize
 
 from conftest import golden
@@ -86,3 +87,19 @@ def test_var_stats_solver_minimises_reference_objective():
                        bounds=[(0.5, 1.5), (0., 0.3), (0, None)],
                        options={"ftol": 1e-15, "gtol": 1e-12, "maxiter": 10000})
         assert best <= res.fun * (1 + 1e-9) + 1e-12
+
+
+@pytest.mark.parametrize("wave", ["log", "lin"])
+def test_find_bins_match_reference(wave):
+    """find_bins_log / find_bins_lin of the host code on the fixture's pixels
+    (observed, rest-frame and variance grids) equal picca's."""
+    from picca_gb300 import synthetic_spectra
+    f = golden(f"continuum_loop_{wave}.npz")
+    grid = synthetic_spectra.Grid(step=3e-4 if wave == "log" else 0.8, wave_solution=wave)
+    zpix = np.repeat(f["z_qso"], np.diff(f["pix_offset"]))
+    ll = f["log_lambda"]
+    np.testing.assert_array_equal(grid.find_bins(ll, grid.log_lambda_grid), f["bins_obs"])
+    np.testing.assert_array_equal(
+        grid.find_bins(ll - np.log10(1 + zpix), grid.log_lambda_rest_frame_grid), f["bins_rest"])
+    np.testing.assert_array_equal(grid.find_bins(ll, f["log_lambda_var_func_grid"]),
+                                  f["bins_var"])
