@@ -301,6 +301,11 @@ typedef struct pg_cont_stacks {
     int32_t obs_bins;
     double obs_grid0, obs_step;
     double *stack_num, *stack_weight;
+    /* 0: grids evenly spaced in log10(lambda), grid0 / step in log10
+     * Angstrom (find_bins_log); 1: evenly spaced in lambda, grid0 = lambda of
+     * the first node and step in Angstrom (find_bins_lin, bin of 10**x),
+     * delta_extraction/utils.py:139-186 */
+    int32_t wave_lin;
 } pg_cont_stacks;
 
 #define PG_FIT_FP64 0        /* per-pixel chi2 terms in FP64                   */

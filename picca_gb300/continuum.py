@@ -72,7 +72,8 @@ class ContStacksC(ctypes.Structure):
         ("var_delta4", ctypes.c_void_p), ("var_npix", ctypes.c_void_p),
         ("var_nqso", ctypes.c_void_p), ("obs_bins", ctypes.c_int32),
         ("obs_grid0", ctypes.c_double), ("obs_step", ctypes.c_double),
-        ("stack_num", ctypes.c_void_p), ("stack_weight", ctypes.c_void_p)]
+        ("stack_num", ctypes.c_void_p), ("stack_weight", ctypes.c_void_p),
+        ("wave_lin", ctypes.c_int32)]
 
 
 def _bind():
@@ -293,15 +294,22 @@ class Dr16Gpu:
             ("v_d4", nvar), ("v_np", nvar), ("v_nq", nvar), ("s_num", len(obs)),
             ("s_w", len(obs)))}
         st = ContStacksC()
+        lin = getattr(grid, "wave_solution", "log") == "lin"
+        st.wave_lin = int(lin)
+
+        def origin_step(g):
+            # find_bins_lin works on lambda, find_bins_log on log10(lambda)
+            if lin:
+                return float(10**g[0]), float(10**g[1] - 10**g[0])
+            return float(g[0]), float(g[1] - g[0])
+
         st.rest_bins = len(rest)
-        st.rest_grid0 = float(rest[0])
-        st.rest_step = float(rest[1] - rest[0])
+        st.rest_grid0, st.rest_step = origin_step(rest)
         if mean_cont:
             st.mean_cont_num = bufs["mc_num"].data_ptr()
             st.mean_cont_weight = bufs["mc_w"].data_ptr()
         st.var_lambda_bins = self.num_bins_variance
-        st.var_grid0 = float(self.log_lambda_var_func_grid[0])
-        st.var_step = float(self.log_lambda_var_func_grid[1] - self.log_lambda_var_func_grid[0])
+        st.var_grid0, st.var_step = origin_step(self.log_lambda_var_func_grid)
         if var_stats:
             st.var_mean = bufs["v_mean"].data_ptr()
             st.var_delta2 = bufs["v_d2"].data_ptr()
@@ -309,8 +317,7 @@ class Dr16Gpu:
             st.var_npix = bufs["v_np"].data_ptr()
             st.var_nqso = bufs["v_nq"].data_ptr()
         st.obs_bins = len(obs)
-        st.obs_grid0 = float(obs[0])
-        st.obs_step = float(obs[1] - obs[0])
+        st.obs_grid0, st.obs_step = origin_step(obs)
         if delta_stack:
             st.stack_num = bufs["s_num"].data_ptr()
             st.stack_weight = bufs["s_w"].data_ptr()
@@ -453,6 +460,49 @@ def normalise_var_stats(sums):
             "num_pixels": num_pixels, "num_qso": sums["v_nq"]}
 
 
+def _faces(limit_eta, limit_var_lss):
+    """Every face of the box eta x var_lss x fudge' (fudge' >= 0): for each
+    variable None (free) or the bound it is held at."""
+    out = []
+    for e in (None, limit_eta[0], limit_eta[1]):
+        for v in (None, limit_var_lss[0], limit_var_lss[1]):
+            for f in (None, 0.0):
+                out.append((e, v, f))
+    return out
+
+
+def box_lsq3(mat, rhs, limit_eta, limit_var_lss):
+    """Exact minimiser of ||mat x - rhs||^2 over eta in limit_eta, var_lss in
+    limit_var_lss, fudge' >= 0 (three columns). The objective is convex, so
+    its minimum over the box is the least-squares solution of one face (the
+    free variables solved with the others held at their bounds) that lies in
+    the box; every face is solved and the best feasible one kept. Returns
+    None when a face's system is rank deficient (the caller then uses an
+    iterative bounded solver)."""
+    gram = mat.T @ mat
+    mty = mat.T @ rhs
+    best, best_val = None, np.inf
+    lo = np.array([limit_eta[0], limit_var_lss[0], 0.0])
+    hi = np.array([limit_eta[1], limit_var_lss[1], np.inf])
+    for face in _faces(limit_eta, limit_var_lss):
+        x = np.array([0.0 if b is None else b for b in face])
+        free = [k for k in range(3) if face[k] is None]
+        if free:
+            fixed = [k for k in range(3) if face[k] is not None]
+            sub = gram[np.ix_(free, free)]
+            if np.linalg.matrix_rank(sub) < len(free):
+                return None
+            r = mty[free] - (gram[np.ix_(free, fixed)] @ x[fixed] if fixed else 0.0)
+            x[free] = np.linalg.solve(sub, r)
+            if np.any(x[free] < lo[free] - 1e-15) or np.any(x[free] > hi[free] + 1e-15):
+                continue
+        res = mat @ x - rhs
+        val = float(res @ res)
+        if val < best_val:
+            best, best_val = x, val
+    return best
+
+
 def fit_var_bin(var_delta, var2_delta, num_qso, var_pipe_values, min_num_qso, limit_eta,
                 limit_var_lss, start):
     """(eta, var_lss, fudge) of one wavelength bin. The chi2 of
@@ -466,6 +516,9 @@ def fit_var_bin(var_delta, var2_delta, num_qso, var_pipe_values, min_num_qso, li
     wgt = 1.0 / np.sqrt(var2_delta[sel])
     mat = np.stack([var_pipe_values[sel], np.ones(sel.sum()),
                     FUDGE_REF / var_pipe_values[sel]], axis=1) * wgt[:, None]
+    exact = box_lsq3(mat, var_delta[sel] * wgt, limit_eta, limit_var_lss)
+    if exact is not None:
+        return float(exact[0]), float(exact[1]), float(exact[2]) * FUDGE_REF
     res = lsq_linear(mat, var_delta[sel] * wgt,
                      bounds=([limit_eta[0], limit_var_lss[0], 0.0],
                              [limit_eta[1], limit_var_lss[1], np.inf]),

@@ -161,9 +161,9 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_kernel(
         const int64_t f = index ? (int64_t)index[w] : w;
         const int64_t off = sp.pix_offset[f];
         const int64_t n64 = sp.pix_offset[f + 1] - off;
-        if (n64 > 32 * kContK || n64 <= 0) {
+        if (n64 > 32 * kContK) continue;  // a long forest: cont_fit_long_kernel
+        if (n64 <= 0) {
             if (lane == 0) {
-                if (n64 > 32 * kContK) report_error(scratch, PG_ERR_UNSUPPORTED, (int32_t)f);
                 out.zero_point[f] = NAN;
                 out.slope[f] = NAN;
                 out.chi2[f] = NAN;
@@ -310,6 +310,213 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_kernel(
 }
 
 // ---------------------------------------------------------------------------
+// Long forests (more than 32 * kContK pixels, up to 32 * kLongK: the linear
+// 0.8 Angstrom grid reaches about 1,000 pixels). Same fit as cont_fit_kernel
+// in FP64 (damped Newton with Armijo backtracking, the same status codes),
+// with the per-pixel terms in the warp's shared-memory slab instead of
+// registers: term t of pixel k*32 + lane at slab[t * 32 * kLongK + k * 32 +
+// lane] (consecutive lanes, consecutive banks). Forests of at most
+// 32 * kContK pixels are left to the register kernels.
+// ---------------------------------------------------------------------------
+constexpr int kLongK = 32;
+constexpr int kLongWarps = 4;  // 4 x 48 KB slabs per block
+
+__device__ __forceinline__ void long_terms(const double *slab, unsigned valid, int nk, double a,
+                                           double b, bool const_w, double s[6]) {
+    const int lane = threadIdx.x & 31;
+    double val = 0, ga = 0, gb = 0, haa = 0, hab = 0, hbb = 0;
+    constexpr int S = 32 * kLongK;
+    for (int k = 0; k < nk; ++k) {
+        if (!((valid >> k) & 1u)) continue;
+        const int e = k * 32 + lane;
+        const double ja = slab[e], jb = slab[S + e], fl = slab[2 * S + e];
+        const double q = slab[3 * S + e], vl = slab[4 * S + e], fi = slab[5 * S + e];
+        const double c = a * ja + b * jb;
+        const double c2 = c * c;
+        const double d = q + vl * c2 + fi * c2 * c2;
+        const double dd = 2. * vl * c + 4. * fi * c2 * c;
+        const double d2d = 2. * vl + 12. * fi * c2;
+        const double r = fl - c;
+        const double id = 1. / d;
+        const double rid = r * id;
+        const double ddid = dd * id;
+        val += r * rid + (const_w ? 0. : log(d));
+        const double g = -2. * rid - rid * rid * dd + ddid;
+        const double h = 2. * id + 4. * rid * ddid + 2. * rid * rid * dd * ddid - rid * rid * d2d +
+                         d2d * id - ddid * ddid;
+        ga += g * ja;
+        gb += g * jb;
+        haa += h * ja * ja;
+        hab += h * ja * jb;
+        hbb += h * jb * jb;
+    }
+    s[0] = warp_sum(val); s[1] = warp_sum(ga); s[2] = warp_sum(gb);
+    s[3] = warp_sum(haa); s[4] = warp_sum(hab); s[5] = warp_sum(hbb);
+}
+
+__global__ void __launch_bounds__(32 * kLongWarps) cont_fit_long_kernel(
+    const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
+    const double *__restrict__ start, const int32_t *__restrict__ index, int64_t count,
+    int max_iter, double tol, const __grid_constant__ pg_cont_fit out, Scratch *scratch) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    double *slab = reinterpret_cast<double *>(smem) + (size_t)(threadIdx.x >> 5) * 6 * 32 * kLongK;
+    constexpr int S = 32 * kLongK;
+    const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    const bool const_w = m.use_constant_weight != 0;
+    for (int64_t w = warp_global; w < count; w += nwarps) {
+        const int64_t f = index ? (int64_t)index[w] : w;
+        const int64_t off = sp.pix_offset[f];
+        const int64_t n64 = sp.pix_offset[f + 1] - off;
+        if (n64 <= 32 * kContK) continue;  // the register kernels' forests
+        if (n64 > 32 * kLongK) {
+            if (lane == 0) {
+                report_error(scratch, PG_ERR_UNSUPPORTED, (int32_t)f);
+                out.zero_point[f] = NAN;
+                out.slope[f] = NAN;
+                out.chi2[f] = NAN;
+                out.ndata[f] = 0;
+                out.status[f] = 1;
+                out.iterations[f] = 0;
+            }
+            continue;
+        }
+        const int n = (int)n64;
+        const int nk = (n + 31) / 32;
+        const double zp1 = log10(1 + sp.z_qso[f]);
+        const double ll_min = m.log_lambda_rest_min + zp1;
+        const double ll_max = m.log_lambda_rest_max + zp1;
+        unsigned valid = 0;
+        double sfi = 0., si = 0.;
+        __syncwarp();
+        for (int k = 0; k < nk; ++k) {
+            const int p = lane + 32 * k;
+            const int e = k * 32 + lane;
+            double ja = 0, jb = 0, fl = 0, q = 0, vl = 0, fi = 0;
+            if (p < n) {
+                const double ll = sp.log_lambda[off + p];
+                fl = sp.flux[off + p];
+                const double iv = sp.ivar[off + p];
+                sfi += fl * iv;
+                si += iv;
+                if (iv > 0) {
+                    const ModelEval ev = eval_model(m, ll, zp1, sp.transmission_correction[off + p]);
+                    const double x = (ll - ll_min) / (ll_max - ll_min);
+                    ja = ev.mc;
+                    jb = x * ev.mc;
+                    q = const_w ? 1. : ev.eta / iv;
+                    vl = const_w ? 0. : ev.var_lss;
+                    fi = const_w ? 0. : ev.fudge * iv;
+                    valid |= 1u << k;
+                }
+            }
+            slab[e] = ja; slab[S + e] = jb; slab[2 * S + e] = fl;
+            slab[3 * S + e] = q; slab[4 * S + e] = vl; slab[5 * S + e] = fi;
+        }
+        __syncwarp();
+        sfi = warp_sum(sfi);
+        si = warp_sum(si);
+        const double a0 = sfi / si;  // utils.py:92
+        int nd = 0;
+        for (int k = 0; k < nk; ++k) {
+            if ((valid >> k) & 1u) {
+                const int e = k * 32 + lane;
+                const double c = a0 * slab[e];
+                const double d = slab[3 * S + e] + slab[4 * S + e] * c * c +
+                                 slab[5 * S + e] * c * c * c * c;
+                nd += (d > 0.) ? 1 : 0;
+            }
+        }
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) nd += __shfl_xor_sync(0xffffffffu, nd, o);
+        double a = a0, b = 0.;
+        if (start) {
+            a = start[2 * f];
+            b = m.order == 0 ? 0. : start[2 * f + 1];
+        }
+        double s[6];
+        long_terms(slab, valid, nk, a, b, const_w, s);
+        int it = 0;
+        bool converged = max_iter == 0 && start != nullptr;
+        for (; it < max_iter; ++it) {
+            double da, db;
+            if (m.order == 0) {
+                da = s[3] > 0 ? -s[1] / s[3] : -s[1];
+                db = 0.;
+            } else {
+                const double det = s[3] * s[5] - s[4] * s[4];
+                if (det > 0 && s[3] > 0) {
+                    da = -(s[5] * s[1] - s[4] * s[2]) / det;
+                    db = -(s[3] * s[2] - s[4] * s[1]) / det;
+                } else {
+                    const double scale = fmax(fabs(s[3]), fabs(s[5]));
+                    da = -s[1] / (scale > 0 ? scale : 1.);
+                    db = -s[2] / (scale > 0 ? scale : 1.);
+                }
+                if (da * s[1] + db * s[2] >= 0) {  // not a descent direction
+                    const double scale = fmax(fabs(s[3]), fabs(s[5]));
+                    da = -s[1] / (scale > 0 ? scale : 1.);
+                    db = -s[2] / (scale > 0 ? scale : 1.);
+                }
+            }
+            const double slope_dir = da * s[1] + db * s[2];
+            double t = 1.;
+            double trial[6];
+            bool accepted = false;
+            for (int ls = 0; ls < 40; ++ls) {
+                long_terms(slab, valid, nk, a + t * da, b + t * db, const_w, trial);
+                if (isfinite(trial[0]) && trial[0] <= s[0] + 1e-4 * t * slope_dir) {
+                    accepted = true;
+                    break;
+                }
+                t *= 0.5;
+            }
+            if (!accepted) {
+                converged = fabs(s[1]) + fabs(s[2]) < 1e-6 * fmax(1., fabs(s[0]));
+                break;
+            }
+            a += t * da;
+            b += t * db;
+#pragma unroll
+            for (int k = 0; k < 6; ++k) s[k] = trial[k];
+            if (fabs(t * da) < tol * fmax(1., fmax(fabs(a), fabs(b))) &&
+                fabs(t * db) < tol * fmax(1., fmax(fabs(a), fabs(b)))) {
+                converged = true;
+                ++it;
+                break;
+            }
+        }
+        double fin[6];
+        long_terms(slab, valid, nk, a, b, const_w, fin);
+        bool negative = false, all_zero = true;
+        for (int p = lane; p < n; p += 32) {
+            const double ll = sp.log_lambda[off + p];
+            const double mc = interp_linear(m.mean_cont_x, m.mean_cont_y, m.num_mean_cont,
+                                            ll - zp1) * sp.transmission_correction[off + p];
+            const double line = b * (ll - ll_min) / (ll_max - ll_min) + a;
+            const double c = line * mc;
+            if (out.continuum) out.continuum[off + p] = c;
+            negative |= c < 0;
+            all_zero &= c == 0;
+        }
+        negative = __any_sync(0xffffffffu, negative);
+        all_zero = __all_sync(0xffffffffu, all_zero);
+        if (lane == 0) {
+            int status = converged ? 0 : 1;
+            if (negative) status = 2;
+            if (all_zero) status = 3;
+            out.zero_point[f] = status == 0 ? a : NAN;
+            out.slope[f] = status == 0 ? b : NAN;
+            out.chi2[f] = status == 0 ? fin[0] : NAN;
+            out.ndata[f] = nd;
+            out.status[f] = status;
+            out.iterations[f] = it;
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
 // Mixed-precision fit (PG_FIT_MIXED): FP32 per-pixel terms, FP32 lane and
 // warp sums, FP64 2x2 Newton solve. GB300 executes FP64 at 1/64 of the FP32
 // rate, so the per-pixel work avoids FP64 except for the three differences
@@ -428,9 +635,9 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
         const int64_t f = index ? (int64_t)index[w] : w;
         const int64_t off = sp.pix_offset[f];
         const int64_t n64 = sp.pix_offset[f + 1] - off;
-        if (n64 > 32 * kContK || n64 <= 0) {
+        if (n64 > 32 * kContK) continue;  // a long forest: cont_fit_long_kernel
+        if (n64 <= 0) {
             if (lane == 0) {
-                if (n64 > 32 * kContK) report_error(scratch, PG_ERR_UNSUPPORTED, (int32_t)f);
                 out.zero_point[f] = NAN;
                 out.slope[f] = NAN;
                 out.chi2[f] = NAN;
@@ -691,22 +898,87 @@ __device__ __forceinline__ double forest_weight(const pg_cont_model &m, double l
     return 1.0 / (eta * var_pipe + m.var_lss_mod * vlss + fudge / var_pipe);
 }
 
-__global__ void __launch_bounds__(kContBlock) cont_stacks_kernel(
+// find_bins_log / find_bins_lin (delta_extraction/utils.py:139-186): the
+// nearest node of an evenly spaced grid in log10(lambda) (grid0, step in
+// log10 Angstrom) or in lambda (grid0, step in Angstrom; the value's lambda is
+// 10**x). The int conversion truncates toward zero, as astype(int64) does.
+__device__ __forceinline__ int64_t find_bin(double x, double grid0, double step, int lin) {
+    if (lin) return (int64_t)((pow(10.0, x) - grid0) / step + 0.5);
+    return (int64_t)((x - grid0) / step + 0.5);
+}
+
+// Histograms of one Dr16 iteration. A persistent block per SM (one warp per
+// forest, pixels across lanes) accumulates the rest-frame mean continuum, the
+// observed-frame stack and the variance statistics in shared-memory FP64
+// histograms and adds them to the global sums once at the end: 400k forests
+// add to a few thousand bins, and global atomics from every warp would
+// contend on them. The variance functions (three cubic pieces on the same
+// breakpoints, staged in shared memory) are evaluated with one interval
+// search per pixel, and the forest weight once per pixel.
+constexpr int kStackBlock = 512;
+
+__host__ __device__ inline size_t stack_smem_doubles(const pg_cont_stacks &st, int m) {
+    const int nvar = st.var_lambda_bins * kVarBins;
+    return (size_t)2 * st.rest_bins + (size_t)2 * st.obs_bins + (size_t)5 * nvar + (m + 1) +
+           (size_t)12 * m;
+}
+
+// eta, var_lss and fudge at v: one search (searchsorted right, the end
+// pieces extrapolated) and the three cubics as eval_ppoly evaluates them.
+__device__ __forceinline__ void var_funcs(const double *brk, const double *coef, int m, double v,
+                                          double &eta, double &vlss, double &fudge) {
+    int lo = 0, hi = m + 1;
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (brk[mid] <= v) lo = mid + 1;
+        else hi = mid;
+    }
+    int i = lo - 1;
+    i = i < 0 ? 0 : (i > m - 1 ? m - 1 : i);
+    const double dx = v - brk[i];
+    const double *c = coef;
+    eta = ((c[i] * dx + c[m + i]) * dx + c[2 * m + i]) * dx + c[3 * m + i];
+    c += 4 * m;
+    vlss = ((c[i] * dx + c[m + i]) * dx + c[2 * m + i]) * dx + c[3 * m + i];
+    c += 4 * m;
+    fudge = ((c[i] * dx + c[m + i]) * dx + c[2 * m + i]) * dx + c[3 * m + i];
+}
+
+__global__ void __launch_bounds__(kStackBlock) cont_stacks_kernel(
     const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
     const __grid_constant__ pg_cont_fit fit, const __grid_constant__ pg_cont_stacks st,
     Scratch *scratch) {
-    __shared__ uint32_t seen[kContBlock / 32][64];  // per-warp bitmap of var bins (<= 2048)
+    extern __shared__ __align__(16) unsigned char smem_raw[];
+    __shared__ uint32_t seen[kStackBlock / 32][64];  // per-warp bitmap of var bins (<= 2048)
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
+    const int nvar = st.var_lambda_bins * kVarBins;
+    const int mi = m.use_constant_weight ? 0 : m.num_var_intervals;
+    double *base = reinterpret_cast<double *>(smem_raw);
+    double *mc_num = base, *mc_w = mc_num + st.rest_bins;
+    double *s_num = mc_w + st.rest_bins, *s_w = s_num + st.obs_bins;
+    double *v_mean = s_w + st.obs_bins, *v_d2 = v_mean + nvar, *v_d4 = v_d2 + nvar;
+    double *v_np = v_d4 + nvar, *v_nq = v_np + nvar;
+    double *brk = v_nq + nvar, *coef = brk + (mi + 1);
+    const int nhist = 2 * st.rest_bins + 2 * st.obs_bins + 5 * nvar;
+    for (int k = threadIdx.x; k < nhist; k += blockDim.x) base[k] = 0.;
+    for (int k = threadIdx.x; k <= mi && mi > 0; k += blockDim.x) brk[k] = m.var_breaks[k];
+    for (int k = threadIdx.x; k < 4 * mi; k += blockDim.x) {
+        coef[k] = m.eta_coef[k];
+        coef[4 * mi + k] = m.var_lss_coef[k];
+        coef[8 * mi + k] = m.fudge_coef[k];
+    }
+    __syncthreads();
     const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const int nvar = st.var_lambda_bins * kVarBins;
+    const bool do_mc = st.mean_cont_num != nullptr;
+    const bool do_stack = st.stack_num != nullptr;
+    const bool do_var = st.var_mean != nullptr && nvar <= 2048;
     for (int64_t f = warp_global; f < sp.num; f += nwarps) {
         if (fit.status[f] != 0) continue;
         const int64_t off = sp.pix_offset[f];
         const int64_t n = sp.pix_offset[f + 1] - off;
         const double zp1 = log10(1 + sp.z_qso[f]);
-        const bool do_var = st.var_mean != nullptr && nvar <= 2048;
         if (do_var) {
             for (int k = lane; k < 64; k += 32) seen[wib][k] = 0u;
             __syncwarp();
@@ -715,27 +987,35 @@ __global__ void __launch_bounds__(kContBlock) cont_stacks_kernel(
             const double ll = sp.log_lambda[off + p], fl = sp.flux[off + p];
             const double iv = sp.ivar[off + p];
             const double cont = fit.continuum[off + p];
-            if (st.mean_cont_num) {
-                // _compute_mean_cont: (f / (C + 1e-16)) * w binned in the rest frame
-                const double w = forest_weight(m, ll, iv, cont);
-                const int64_t bin = (int64_t)((ll - zp1 - st.rest_grid0) / st.rest_step + 0.5);
-                if (bin >= 0 && bin < st.rest_bins) {
-                    atomicAdd(&st.mean_cont_num[bin], fl / (cont + 1e-16) * w);
-                    atomicAdd(&st.mean_cont_weight[bin], w);
-                } else {
-                    report_error(scratch, PG_ERR_BIN_RANGE, (int32_t)bin);
+            if (do_mc || do_stack) {
+                // compute_forest_weights (dr16_expected_flux.py:466-488)
+                double w = 0.;
+                if (iv > 0) {
+                    const double var_pipe = 1. / iv / (cont * cont);
+                    double eta = 0., vlss = 1., fudge = 0.;
+                    if (mi > 0) var_funcs(brk, coef, mi, ll, eta, vlss, fudge);
+                    w = 1.0 / (eta * var_pipe + m.var_lss_mod * vlss + fudge / var_pipe);
                 }
-            }
-            if (st.stack_num) {
-                // compute_delta_stack: delta = f / C where ivar > 0
-                const double w = forest_weight(m, ll, iv, cont);
-                const double delta = iv > 0 ? fl / cont : 0.;
-                const int64_t bin = (int64_t)((ll - st.obs_grid0) / st.obs_step + 0.5);
-                if (bin >= 0 && bin < st.obs_bins) {
-                    atomicAdd(&st.stack_num[bin], delta * w);
-                    atomicAdd(&st.stack_weight[bin], w);
-                } else {
-                    report_error(scratch, PG_ERR_BIN_RANGE, (int32_t)bin);
+                if (do_mc) {
+                    // _compute_mean_cont: (f / (C + 1e-16)) * w binned in the rest frame
+                    const int64_t bin = find_bin(ll - zp1, st.rest_grid0, st.rest_step, st.wave_lin);
+                    if (bin >= 0 && bin < st.rest_bins) {
+                        atomicAdd(&mc_num[bin], fl / (cont + 1e-16) * w);
+                        atomicAdd(&mc_w[bin], w);
+                    } else {
+                        report_error(scratch, PG_ERR_BIN_RANGE, (int32_t)bin);
+                    }
+                }
+                if (do_stack) {
+                    // compute_delta_stack: delta = f / C where ivar > 0
+                    const double delta = iv > 0 ? fl / cont : 0.;
+                    const int64_t bin = find_bin(ll, st.obs_grid0, st.obs_step, st.wave_lin);
+                    if (bin >= 0 && bin < st.obs_bins) {
+                        atomicAdd(&s_num[bin], delta * w);
+                        atomicAdd(&s_w[bin], w);
+                    } else {
+                        report_error(scratch, PG_ERR_BIN_RANGE, (int32_t)bin);
+                    }
                 }
             }
             if (do_var && iv > 0) {
@@ -744,15 +1024,15 @@ __global__ void __launch_bounds__(kContBlock) cont_stacks_kernel(
                 const double lv = log10(var_pipe);
                 if (lv > kVarPipeMin && lv < kVarPipeMax) {
                     const int vbin = (int)((lv - kVarPipeMin) / (kVarPipeMax - kVarPipeMin) * kVarBins);
-                    const int64_t lbin = (int64_t)((ll - st.var_grid0) / st.var_step + 0.5);
+                    const int64_t lbin = find_bin(ll, st.var_grid0, st.var_step, st.wave_lin);
                     const int64_t bin = vbin + (int64_t)kVarBins * lbin;
                     if (bin >= 0 && bin < nvar) {
                         const double delta = fl / cont - 1;
                         const double d2 = delta * delta;
-                        atomicAdd(&st.var_mean[bin], delta);
-                        atomicAdd(&st.var_delta2[bin], d2);
-                        atomicAdd(&st.var_delta4[bin], d2 * d2);
-                        atomicAdd(&st.var_npix[bin], 1.0);
+                        atomicAdd(&v_mean[bin], delta);
+                        atomicAdd(&v_d2[bin], d2);
+                        atomicAdd(&v_d4[bin], d2 * d2);
+                        atomicAdd(&v_np[bin], 1.0);
                         atomicOr(&seen[wib][bin >> 5], 1u << (bin & 31));
                     } else {
                         report_error(scratch, PG_ERR_BIN_RANGE, (int32_t)bin);
@@ -767,11 +1047,29 @@ __global__ void __launch_bounds__(kContBlock) cont_stacks_kernel(
                 while (bits) {
                     const int bit = __ffs(bits) - 1;
                     bits &= bits - 1;
-                    atomicAdd(&st.var_nqso[k * 32 + bit], 1.0);
+                    atomicAdd(&v_nq[k * 32 + bit], 1.0);
                 }
             }
             __syncwarp();
         }
+    }
+    __syncthreads();
+    // one add per nonzero bin and block
+    auto flush = [&](double *dst, const double *src, int count) {
+        if (!dst) return;
+        for (int k = threadIdx.x; k < count; k += blockDim.x)
+            if (src[k] != 0.) atomicAdd(&dst[k], src[k]);
+    };
+    flush(st.mean_cont_num, mc_num, st.rest_bins);
+    flush(st.mean_cont_weight, mc_w, st.rest_bins);
+    flush(st.stack_num, s_num, st.obs_bins);
+    flush(st.stack_weight, s_w, st.obs_bins);
+    if (do_var) {
+        flush(st.var_mean, v_mean, nvar);
+        flush(st.var_delta2, v_d2, nvar);
+        flush(st.var_delta4, v_d4, nvar);
+        flush(st.var_npix, v_np, nvar);
+        flush(st.var_nqso, v_nq, nvar);
     }
 }
 
@@ -804,15 +1102,21 @@ __global__ void __launch_bounds__(kContBlock) cont_deltas_kernel(
 constexpr int kFeatBins = 64;
 
 // Warm-start network inputs (see pg_mlp_features in include/picca_gb300.h).
+// FP32 per pixel (the features are rounded to BF16): the mean continuum is
+// interpolated from the shared-memory tables of the mixed fit, with the
+// rest-frame coordinate's close-operand differences formed in FP64.
 __global__ void __launch_bounds__(kContBlock) mlp_features_kernel(
     const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
     __nv_bfloat16 *__restrict__ feat, int stride, double *__restrict__ a0_out) {
+    extern __shared__ __align__(16) unsigned char smem[];
     __shared__ float sums[kContBlock / 32][2][kFeatBins];
+    const MixedTables tab = load_tables(m, smem);
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
-    const double span = m.log_lambda_rest_max - m.log_lambda_rest_min;
+    const float bins_per_span =
+        (float)(kFeatBins / (m.log_lambda_rest_max - m.log_lambda_rest_min));
     for (int64_t f = warp_global; f < sp.num; f += nwarps) {
         for (int k = lane; k < kFeatBins; k += 32) {
             sums[wib][0][k] = 0.f;
@@ -821,46 +1125,50 @@ __global__ void __launch_bounds__(kContBlock) mlp_features_kernel(
         __syncwarp();
         const int64_t off = sp.pix_offset[f];
         const int64_t n = sp.pix_offset[f + 1] - off;
-        const double zp1 = log10(1 + sp.z_qso[f]);
-        double sfi = 0., si = 0., snr = 0., cnt = 0.;
+        double zp1 = 0.;
+        if (lane == 0) zp1 = log10(1 + sp.z_qso[f]);
+        zp1 = __shfl_sync(0xffffffffu, zp1, 0);
+        const double rest0 = zp1 + m.log_lambda_rest_min;
+        float sfi = 0.f, si = 0.f, snr = 0.f, cnt = 0.f;
         for (int64_t p = lane; p < n; p += 32) {
-            const double ll = sp.log_lambda[off + p], fl = sp.flux[off + p];
-            const double iv = sp.ivar[off + p];
+            const double ll = sp.log_lambda[off + p];
+            const float fl = (float)sp.flux[off + p];
+            const float iv = (float)sp.ivar[off + p];
             sfi += fl * iv;
             si += iv;
-            if (iv > 0) {
-                snr += fl * sqrt(iv);
-                cnt += 1.;
-                const double mc = interp_linear(m.mean_cont_x, m.mean_cont_y, m.num_mean_cont,
-                                                ll - zp1) * sp.transmission_correction[off + p];
-                int bin = (int)floor((ll - zp1 - m.log_lambda_rest_min) / span * kFeatBins);
+            if (iv > 0.f) {
+                snr += fl * sqrtf(iv);
+                cnt += 1.f;
+                const float mc =
+                    interp_mc(tab, ll - zp1) * (float)sp.transmission_correction[off + p];
+                int bin = (int)floorf((float)(ll - rest0) * bins_per_span);
                 bin = bin < 0 ? 0 : (bin >= kFeatBins ? kFeatBins - 1 : bin);
-                if (mc != 0.) {
-                    atomicAdd(&sums[wib][0][bin], (float)(fl / mc * iv));
-                    atomicAdd(&sums[wib][1][bin], (float)iv);
+                if (mc != 0.f) {
+                    atomicAdd(&sums[wib][0][bin], fl / mc * iv);
+                    atomicAdd(&sums[wib][1][bin], iv);
                 }
             }
         }
-        sfi = warp_sum(sfi);
-        si = warp_sum(si);
-        snr = warp_sum(snr);
-        cnt = warp_sum(cnt);
+        sfi = warp_sum_f(sfi);
+        si = warp_sum_f(si);
+        snr = warp_sum_f(snr);
+        cnt = warp_sum_f(cnt);
         __syncwarp();
-        const double a0 = si > 0 ? sfi / si : 0.;
+        const float a0 = si > 0.f ? sfi / si : 0.f;
         __nv_bfloat16 *row = feat + f * (int64_t)stride;
         for (int k = lane; k < stride; k += 32) {
             float v = 0.f;
             if (k < kFeatBins) {
                 const float w = sums[wib][1][k];
-                v = (w > 0.f && a0 != 0.) ? (float)(sums[wib][0][k] / w / a0) - 1.f : 0.f;
+                v = (w > 0.f && a0 != 0.f) ? sums[wib][0][k] / w / a0 - 1.f : 0.f;
             } else if (k == kFeatBins) {
                 v = (float)(sp.z_qso[f] - 3.0);
             } else if (k == kFeatBins + 1) {
-                v = (float)log(fmax(cnt > 0 ? snr / cnt : 0., 1e-3));
+                v = logf(fmaxf(cnt > 0.f ? snr / cnt : 0.f, 1e-3f));
             }
             row[k] = __float2bfloat16(v);
         }
-        if (lane == 0) a0_out[f] = a0;
+        if (lane == 0) a0_out[f] = (double)a0;
         __syncwarp();
     }
 }
@@ -892,6 +1200,18 @@ int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *
         cont_fit_kernel<double><<<blocks, kContBlock, 0, stream>>>(sp, m, start, index, count,
                                                                     max_iter, tol, out, scratch);
     }
+    cudaError_t err = cudaGetLastError();
+    if (err != cudaSuccess) return check_cuda(err);
+    // forests longer than the register kernels hold (the linear grid), in FP64
+    const size_t long_smem = (size_t)kLongWarps * 6 * 32 * kLongK * sizeof(double);
+    err = cudaFuncSetAttribute(cont_fit_long_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                               (int)long_smem);
+    if (err != cudaSuccess) return check_cuda(err);
+    int64_t long_blocks = (count + kLongWarps - 1) / kLongWarps;
+    if (long_blocks > (int64_t)num_sms * 8) long_blocks = (int64_t)num_sms * 8;
+    cont_fit_long_kernel<<<(unsigned)(long_blocks < 1 ? 1 : long_blocks), 32 * kLongWarps,
+                           long_smem, stream>>>(sp, m, start, index, count, max_iter, tol, out,
+                                                scratch);
     return check_cuda(cudaGetLastError());
 }
 
@@ -900,15 +1220,28 @@ int launch_cont_stacks(const pg_spectra &sp, const pg_cont_model &m, const pg_co
                        cudaStream_t stream) {
     if (sp.num <= 0) return PG_OK;
     if (st.var_mean && st.var_lambda_bins * kVarBins > 2048) return PG_ERR_UNSUPPORTED;
-    cont_stacks_kernel<<<blocks_for(sp.num, num_sms), kContBlock, 0, stream>>>(sp, m, fit, st,
-                                                                               scratch);
+    const int mi = m.use_constant_weight ? 0 : m.num_var_intervals;
+    const size_t smem = stack_smem_doubles(st, mi) * sizeof(double);
+    if (smem > 200 * 1024) return PG_ERR_UNSUPPORTED;
+    cudaError_t err = cudaFuncSetAttribute(cont_stacks_kernel,
+                                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return check_cuda(err);
+    int64_t blocks = (sp.num + kStackBlock / 32 - 1) / (kStackBlock / 32);
+    if (blocks > num_sms) blocks = num_sms;
+    cont_stacks_kernel<<<(unsigned)(blocks < 1 ? 1 : blocks), kStackBlock, smem, stream>>>(
+        sp, m, fit, st, scratch);
     return check_cuda(cudaGetLastError());
 }
 
 int launch_mlp_features(const pg_spectra &sp, const pg_cont_model &m, uint16_t *features,
                         int stride, double *a0, int num_sms, cudaStream_t stream) {
     if (sp.num <= 0) return PG_OK;
-    mlp_features_kernel<<<blocks_for(sp.num, num_sms), kContBlock, 0, stream>>>(
+    const size_t smem = mixed_smem_bytes(m.num_mean_cont, m.num_var_intervals);
+    if (smem > 200 * 1024) return PG_ERR_UNSUPPORTED;
+    cudaError_t err = cudaFuncSetAttribute(
+        mlp_features_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return check_cuda(err);
+    mlp_features_kernel<<<blocks_for(sp.num, num_sms), kContBlock, smem, stream>>>(
         sp, m, reinterpret_cast<__nv_bfloat16 *>(features), stride, a0);
     return check_cuda(cudaGetLastError());
 }

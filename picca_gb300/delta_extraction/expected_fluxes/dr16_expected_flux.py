@@ -27,9 +27,12 @@ Forests are any objects with picca's ``Forest`` attributes ``los_id``,
 picca itself is importable, from ``Forest``. Differences from the
 reference: the continuum minimiser is a damped Newton method on the same
 chi2 (the reference uses iminuit's MIGRAD), the variance functions are
-fitted by exact bounded linear least squares (the same chi2), only the
-logarithmic wavelength solution and a one-dimensional mean continuum are
-supported, and Pk1d forests' ``ivar`` entry is not produced.
+fitted by exact bounded linear least squares (the same chi2), only a
+one-dimensional mean continuum is supported, and Pk1d forests' ``ivar``
+entry is not produced. Both wavelength solutions are supported: on the
+linear grid the bins follow find_bins_lin and the variance functions' grid
+is linear in lambda (expected_flux.py:122-142); forests longer than 224
+pixels are fitted with FP64 per-pixel terms held in shared memory.
 """
 
 import logging
@@ -146,8 +149,8 @@ class Dr16ExpectedFlux(_Base):
             raise ExpectedFluxError("'use constant weight' and 'use ivar as weight' "
                                     "are mutually exclusive")
         self.grid = grid if grid is not None else _forest_class_grid()
-        if getattr(self.grid, "wave_solution", "log") != "log":
-            raise ExpectedFluxError("only the logarithmic wavelength solution is supported")
+        if getattr(self.grid, "wave_solution", "log") not in ("log", "lin"):
+            raise ExpectedFluxError("Forest.wave_solution must be 'lin' or 'log'")
         self.gpu = gpu_continuum.Dr16Gpu(
             self.grid, num_iterations=self.num_iterations, order=self.order,
             limit_eta=self.limit_eta, limit_var_lss=self.limit_var_lss,

@@ -125,9 +125,19 @@ class _LimitDict(dict):
 class _MinuitStandIn:
     """Stand-in for iminuit.Minuit in the fixture runs (iminuit is not
     installed; no iminuit code is involved): ``migrad`` minimises the
-    reference's own cost function with SciPy (Nelder-Mead, then L-BFGS-B from
-    its result, limits as bounds, fixed parameters held), ``valid`` reports
-    SciPy's success, ``fval`` is the cost at the result."""
+    reference's own cost function with SciPy, the parameters scaled by the
+    step sizes iminuit is given (``errors``), limits as bounds, fixed
+    parameters held. The continuum fit (zero point, slope) uses local
+    searches from the start only (L-BFGS-B and a small Nelder-Mead simplex,
+    each polished from the better result): picca's continuum chi2 is
+    unbounded below where a pixel's noise model crosses zero (picca drops
+    log w for w <= 0), away from the start. The variance fit (eta, var_lss,
+    fudge) is a convex quadratic whose fudge column is scaled very
+    differently from the others; Powell's method is added there. ``valid``
+    reports SciPy's success and a cost of normal size: a chi2 of order 1e8
+    or more means the search ended on that singular region, where MIGRAD's
+    outcome is undefined, and the fit is reported as not converged;
+    ``fval`` is the cost at the result."""
 
     def __init__(self, fcn, *args, name=None, **start):
         import inspect
@@ -159,18 +169,45 @@ class _MinuitStandIn:
             lo, hi = (None, None) if lim is None else lim
             bounds.append((-np.inf if lo is None else lo, np.inf if hi is None else hi))
         x0 = np.clip(x0, [b[0] for b in bounds], [b[1] for b in bounds])
-        cost = lambda x: self._cost(free, x)  # noqa: E731
+        step = np.array([abs(self.errors.get(n, 0.0)) or max(abs(v), 1.0)
+                         for n, v in zip(free, x0)])
+        sb = [(lo / sc if np.isfinite(lo) else -np.inf, hi / sc if np.isfinite(hi) else np.inf)
+              for (lo, hi), sc in zip(bounds, step)]
+        cost = lambda y: self._cost(free, y * step)  # noqa: E731
+        y0 = x0 / step
+        local = "fudge" not in self.names
+        methods = [("L-BFGS-B", {"ftol": 1e-15, "gtol": 1e-12, "maxiter": 5000}),
+                   ("Nelder-Mead", {"xatol": 1e-13, "fatol": 1e-13, "maxiter": 20000,
+                                    "maxfev": 40000})]
+        if not local:
+            methods.append(("Powell", {"xtol": 1e-13, "ftol": 1e-15, "maxiter": 20000}))
+
+        def run(method, opts, y):
+            if method == "Nelder-Mead":
+                opts = dict(opts, initial_simplex=np.vstack([y, y + 0.05 * np.eye(len(y))]))
+            return minimize(cost, y, method=method, bounds=sb, options=opts)
+
+        def value(r):
+            return r.fun if np.isfinite(r.fun) else np.inf
+
         with np.errstate(all="ignore"):
-            res = minimize(cost, x0, method="Nelder-Mead", bounds=bounds,
-                           options={"xatol": 1e-13, "fatol": 1e-13, "maxiter": 20000,
-                                    "maxfev": 40000})
-            res2 = minimize(cost, res.x, method="L-BFGS-B", bounds=bounds,
-                            options={"ftol": 1e-15, "gtol": 1e-12, "maxiter": 2000})
-        best = res2 if res2.fun <= res.fun else res
-        for n, v in zip(free, best.x):
+            results = [run(m, o, y0) for m, o in methods]
+            best = min(results, key=value)
+            for _ in range(3):  # polish from the best point
+                for method, opts in methods:
+                    if method == "Nelder-Mead":
+                        opts = dict(opts, initial_simplex=np.vstack(
+                            [best.x, best.x + 1e-3 * np.eye(len(best.x))]))
+                        res = minimize(cost, best.x, method=method, bounds=sb, options=opts)
+                    else:
+                        res = run(method, opts, best.x)
+                    if value(res) < value(best):
+                        best = res
+        for n, v in zip(free, best.x * step):
             self.values[n] = float(v)
-        self.fval = self._cost(free, best.x)
-        self.valid = bool(np.isfinite(self.fval) and (res.success or res2.success))
+        self.fval = self._cost(free, best.x * step)
+        self.valid = bool(np.isfinite(self.fval) and abs(self.fval) < 1e8 and
+                          any(r.success for r in results))
 
     def hesse(self):
         return None

@@ -98,7 +98,7 @@ def _set_state(eng, f, it):
     eng.fudge = f[pre + "fudge"][nodes].copy()
 
 
-@pytest.mark.parametrize("wave", ["log"])
+@pytest.mark.parametrize("wave", ["log", "lin"])
 def test_dr16_loop_matches_reference_functions(cuda, wave):
     from picca_gb300 import continuum
     f = golden(f"continuum_loop_{wave}.npz")
@@ -132,9 +132,9 @@ def test_dr16_loop_matches_reference_functions(cuda, wave):
             nodes = np.isin(f["log_lambda_var_func_grid"], f[pre + "var_x"])
             np.testing.assert_allclose(eng.eta, f[pre + "eta"][nodes], rtol=0, atol=2e-5)
             np.testing.assert_allclose(eng.var_lss, f[pre + "var_lss"][nodes], rtol=0, atol=2e-5)
-            np.testing.assert_allclose(eng.fudge / continuum.FUDGE_REF,
-                                       f[pre + "fudge"][nodes] / continuum.FUDGE_REF,
-                                       rtol=0, atol=2e-5)
+            fudge_ref = f[pre + "fudge"][nodes] / continuum.FUDGE_REF
+            assert np.all(np.abs(eng.fudge / continuum.FUDGE_REF - fudge_ref) <=
+                          2e-5 * np.maximum(1.0, np.abs(fudge_ref))), it
             _set_state(eng, f, it)
         # the delta stack, with the variance functions of this iteration's end
         sums = eng._stacks(spectra, fit, mean_cont=False, var_stats=False, delta_stack=True)
@@ -154,7 +154,7 @@ def test_dr16_loop_matches_reference_functions(cuda, wave):
     np.testing.assert_allclose(delta[sel][w], want, rtol=1e-10, atol=1e-12)
 
 
-@pytest.mark.parametrize("wave", ["log"])
+@pytest.mark.parametrize("wave", ["log", "lin"])
 @pytest.mark.parametrize("mode", ["fp64", "mixed"])
 def test_newton_fit_matches_reference_minimum(cuda, wave, mode):
     """The GPU Newton fit from picca's starting point at the reference's
@@ -175,7 +175,11 @@ def test_newton_fit_matches_reference_minimum(cuda, wave, mode):
         assert np.max(np.abs(fit["zero_point"][good] - a) / scale) < 1e-4, it
         assert np.max(np.abs(fit["slope"][good] - b) / scale) < 1e-4, it
         chi_scale = np.maximum(np.abs(f[pre + "chi2"][good]), f[pre + "ndata"][good])
-        assert np.all(fit["chi2"][good] - f[pre + "chi2"][good] <= 1e-6 * chi_scale), it
+        excess = (fit["chi2"][good] - f[pre + "chi2"][good]) / chi_scale
+        k = int(np.argmax(excess))
+        assert excess[k] <= 1e-6, (it, k, fit["chi2"][good][k], f[pre + "chi2"][good][k],
+                                   fit["zero_point"][good][k], a[k], fit["slope"][good][k], b[k],
+                                   fit["iterations"][good][k])
         if it + 1 < int(f["num_iterations"]):
             _set_state(eng, f, it)
         eng.stack_x, eng.stack_y = f[pre + "stack_x"], f[pre + "stack_y"]

@@ -157,9 +157,10 @@ def test_cli_matches_golden(cuda, picca_inputs, tmp_path, case, precision):
     compare_like_reference(got, want)
 
 
-def _synthetic_sets(seed=7, num=600, xcf=False):
+def _synthetic_sets(seed=7, num=600, xcf=False, grid="log"):
     from picca_gb300 import synthetic
-    fs = synthetic.make_forests(num, seed, (150.0, 156.0), (0.0, 6.0), 2.1, 3.5, "uniform")
+    fs = synthetic.make_forests(num, seed, (150.0, 156.0), (0.0, 6.0), 2.1, 3.5, "uniform",
+                                grid=grid)
     if xcf:
         qs = synthetic.make_quasars(int(num * 1.5), seed + 1, (150.0, 156.0), (0.0, 6.0))
         return fs, qs
@@ -167,11 +168,17 @@ def _synthetic_sets(seed=7, num=600, xcf=False):
 
 
 @pytest.mark.parametrize("precision", MODES)
-@pytest.mark.parametrize("variant", ["auto", "cross", "auto_cuts"])
+@pytest.mark.parametrize("variant", ["auto", "cross", "auto_cuts", "auto_lin"])
 def test_cf_gpu_matches_oracle_synthetic(cuda, precision, variant):
+    """``auto_lin``: forests on the DESI-like linear grid (0.8 Angstrom,
+    150-600 pixels), which the pair kernel stages in several chunks."""
     from oracle import cpu as oracle
     from picca_gb300 import pairs, synthetic
-    fs, _ = _synthetic_sets()
+    fs, _ = _synthetic_sets(grid="lin" if variant == "auto_lin" else "log",
+                            num=300 if variant == "auto_lin" else 600)
+    if variant == "auto_lin":
+        npix = np.diff(fs.pix_offset)
+        assert npix.max() > 400 and npix.min() >= 150
     fs2 = None
     kwargs = dict(r_par_min=0.0, r_par_max=200.0, r_trans_max=200.0, num_bins_r_par=50,
                   num_bins_r_trans=50)
@@ -200,10 +207,11 @@ def test_cf_gpu_matches_oracle_synthetic(cuda, precision, variant):
 
 
 @pytest.mark.parametrize("precision", MODES)
-def test_xcf_gpu_matches_oracle_synthetic(cuda, precision):
+@pytest.mark.parametrize("grid", ["log", "lin"])
+def test_xcf_gpu_matches_oracle_synthetic(cuda, precision, grid):
     from oracle import cpu as oracle
     from picca_gb300 import pairs, synthetic
-    fs, qs = _synthetic_sets(xcf=True)
+    fs, qs = _synthetic_sets(xcf=True, grid=grid, num=600 if grid == "log" else 300)
     kwargs = dict(r_par_min=-200.0, r_par_max=200.0, r_trans_max=200.0, num_bins_r_par=100,
                   num_bins_r_trans=50)
     ang_max = synthetic.correlation_ang_max(200.0, float(fs.z.min()))

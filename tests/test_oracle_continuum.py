@@ -103,3 +103,28 @@ def test_find_bins_match_reference(wave):
         grid.find_bins(ll - np.log10(1 + zpix), grid.log_lambda_rest_frame_grid), f["bins_rest"])
     np.testing.assert_array_equal(grid.find_bins(ll, f["log_lambda_var_func_grid"]),
                                   f["bins_var"])
+
+
+def test_box_lsq3_matches_bounded_least_squares():
+    """The exact face-enumeration solver of the (eta, var_lss, fudge) fits
+    (continuum.box_lsq3) equals scipy's bounded least squares (BVLS) on
+    random problems with and without active bounds."""
+    from scipy.optimize import lsq_linear
+    from picca_gb300 import continuum
+    rng = np.random.default_rng(3)
+    var_pipe = 10**rng.uniform(-5, 0.3, 40)
+    for trial in range(200):
+        n = int(rng.integers(3, 40))
+        v = var_pipe[:n]
+        mat = np.stack([v, np.ones(n), 1e-7 / v], axis=1) * rng.uniform(0.5, 2, n)[:, None]
+        truth = np.array([rng.uniform(0.2, 1.8), rng.uniform(-0.1, 0.4), rng.uniform(-1, 3)])
+        rhs = mat @ truth + rng.normal(0, 0.05, n) * np.abs(mat @ truth).mean()
+        got = continuum.box_lsq3(mat, rhs, (0.5, 1.5), (0.0, 0.3))
+        want = lsq_linear(mat, rhs, bounds=([0.5, 0.0, 0.0], [1.5, 0.3, np.inf]),
+                          method="bvls", tol=1e-14).x
+        if got is None:
+            continue
+        f_got = np.sum((mat @ got - rhs) ** 2)
+        f_want = np.sum((mat @ want - rhs) ** 2)
+        assert f_got <= f_want * (1 + 1e-10) + 1e-300, trial
+        np.testing.assert_allclose(got, want, rtol=1e-6, atol=1e-9)
