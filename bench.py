@@ -916,6 +916,46 @@ def continuum_leg(args, cpu_seconds):
                     "xi_rms_diff_over_rms_xi": float(np.sqrt(np.mean((xis[1] - xis[0])**2)) /
                                                      np.sqrt(np.mean(xis[0]**2)))}
 
+    # the fit stage alone, plain vs learned, on the same model state at every
+    # iteration (the loop advances with the plain fit): each stage is timed
+    # with CUDA events, best of three, and the learned stage includes the
+    # features, the network, the certified fit and the plain re-fit of the
+    # forests that were not certified
+    eng_c = continuum.Dr16Gpu(eval_raw.grid, num_iterations=iters, fit_mode=mixed)
+    per_iter = []
+    for iteration in range(iters):
+        best_p, best_w = np.inf, np.inf
+        for _ in range(3):
+            fp, tp = timed_loop(lambda: eng_c.fit(spectra))
+            (fw, _, fb), tw = timed_loop(lambda: learned.warm_fit(eng_c, spectra, net))
+            best_p, best_w = min(best_p, tp), min(best_w, tw)
+        hp, hw = continuum.fit_results_to_host(fp), continuum.fit_results_to_host(fw)
+        both = (hp["status"] == 0) & (hw["status"] == 0)
+        sc = np.maximum(1.0, np.maximum(np.abs(hp["zero_point"]), np.abs(hp["slope"])))
+        d = np.maximum(np.abs(hw["zero_point"] - hp["zero_point"]),
+                       np.abs(hw["slope"] - hp["slope"]))[both] / sc[both]
+        dc = ((hw["chi2"] - hp["chi2"]) / np.maximum(np.abs(hp["chi2"]), hp["ndata"]))[both]
+        per_iter.append({"plain_ms": best_p * 1e3, "learned_ms": best_w * 1e3,
+                         "speedup": best_p / best_w,
+                         "fallback_fraction": float(fb.float().mean().item()),
+                         "ab_max_rel": float(d.max()) if d.size else None,
+                         "chi2_excess_max_rel": float(dc.max()) if dc.size else None,
+                         "chi2_abs_max_rel": float(np.abs(dc).max()) if dc.size else None,
+                         "status_agree": float(np.mean((hp["status"] == 0) ==
+                                                       (hw["status"] == 0)))})
+        eng_c.update_model(spectra, fp, iteration == iters - 1)
+        del fp, fw
+    loop_plain = sum(r["plain_ms"] for r in per_iter)
+    loop_learned = sum(r["learned_ms"] for r in per_iter)
+    same_state = {"per_iteration": per_iter,
+                  "plain_fits_per_s": eval_raw.num * iters / (loop_plain / 1e3),
+                  "learned_fits_per_s": eval_raw.num * iters / (loop_learned / 1e3),
+                  "learned_over_plain": loop_plain / loop_learned,
+                  "ab_max_rel": max(r["ab_max_rel"] or 0.0 for r in per_iter),
+                  "chi2_excess_max_rel": max(r["chi2_excess_max_rel"] or 0.0 for r in per_iter),
+                  "certificate": {"chi2_tol": learned.CHI2_TOL, "ab_tol": learned.AB_TOL}}
+    del eng_c
+
     nfits = eval_raw.num * iters
     # bytes per forest-fit: 40 n + 32 (n pixels; four FP64 inputs, continuum out)
     npix = float(eval_raw.pix_offset[-1])
@@ -940,6 +980,7 @@ def continuum_leg(args, cpu_seconds):
         "fit_roofline": {"bound": "hbm", "achieved": achieved, "peak": pk.get("hbm_gbs"),
                          "unit": "GB/s", "frac": achieved / pk.get("hbm_gbs", 6800.0),
                          "bytes_per_launch": fit_bytes, "peak_source": source},
+        "fit_stage_same_model_state": same_state,
         "deltas_to_xi_plain_vs_learned": e2e_corr,
         "training": {"forests": args.continuum_train, "samples": num_samples, "epochs": len(hist),
                      "collect_s": collect_s, "train_s": train_s, "loss_first": hist[0],

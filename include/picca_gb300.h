@@ -338,6 +338,22 @@ int pg_cont_fit_select(pg_plan *plan, const pg_spectra *spectra, const pg_cont_m
                        int32_t max_iter, double tol, int32_t mode, const pg_cont_fit *out,
                        void *stream);
 
+/* The learned warm start's fit (no counterpart in the reference): Newton
+ * iterations with FP32 per-pixel terms from start[2*f..] (required), ended
+ * by a certificate instead of a step size. Once a Newton step d = -H^-1 g of
+ * chi2 is at most sqrt(ab_tol) * max(1, |a|, |b|) (the error after it is of
+ * order |d|^2), the step is taken and the new point is certified with its
+ * gradient g' and the last Hessian: the remaining step H^-1 g' at most
+ * ab_tol * max(1, |a|, |b|) and half the Newton decrement g'.H^-1 g' / 2 (the
+ * excess of chi2 over the minimum of its quadratic model) at most
+ * chi2_tol * max(|chi2|, ndata). Forests not certified within max_iter get
+ * status 1 (the caller re-fits them with the plain fit). No FP64 finish;
+ * forests longer than 224 pixels are fitted to convergence in FP64. */
+int pg_cont_fit_warm(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
+                     const double *start, const int32_t *forest_index, int64_t num_index,
+                     int32_t max_iter, double chi2_tol, double ab_tol, const pg_cont_fit *out,
+                     void *stream);
+
 /* Accumulate the histograms of one Dr16 iteration from fitted continua
  * (forests with status != 0 are skipped, as bad_continuum_reason is). */
 int pg_cont_stacks_accumulate(pg_plan *plan, const pg_spectra *spectra,

@@ -91,8 +91,12 @@ def _bind():
                                               _P(ContFitC), _P(ContStacksC), ctypes.c_void_p]
     lib.pg_cont_deltas.argtypes = [ctypes.c_void_p, _P(SpectraC), _P(ContModelC), _P(ContFitC),
                                    ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
-    for name in ("pg_cont_fit_batch", "pg_cont_fit_select", "pg_cont_stacks_accumulate",
-                 "pg_cont_deltas"):
+    lib.pg_cont_fit_warm.argtypes = [ctypes.c_void_p, _P(SpectraC), _P(ContModelC),
+                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int64,
+                                     ctypes.c_int32, ctypes.c_double, ctypes.c_double,
+                                     _P(ContFitC), ctypes.c_void_p]
+    for name in ("pg_cont_fit_batch", "pg_cont_fit_select", "pg_cont_fit_warm",
+                 "pg_cont_stacks_accumulate", "pg_cont_deltas"):
         getattr(lib, name).restype = ctypes.c_int
     lib._cont_bound = True
     return lib
@@ -242,14 +246,7 @@ class Dr16Gpu:
         dev = self.device
         n = spectra.num
         if out is None:
-            out = {"zero_point": torch.empty(n, dtype=torch.float64, device=dev),
-                   "slope": torch.empty(n, dtype=torch.float64, device=dev),
-                   "chi2": torch.empty(n, dtype=torch.float64, device=dev),
-                   "ndata": torch.empty(n, dtype=torch.int32, device=dev),
-                   "status": torch.empty(n, dtype=torch.int32, device=dev),
-                   "iterations": torch.empty(n, dtype=torch.int32, device=dev),
-                   "continuum": torch.empty(max(spectra.num_pixels, 1), dtype=torch.float64,
-                                            device=dev)}
+            out = self._new_fit(spectra)
         fit_c = ContFitC(*[out[k].data_ptr() for k in ("zero_point", "slope", "chi2", "ndata",
                                                         "status", "iterations", "continuum")])
         model, keep = self._model()
@@ -281,6 +278,39 @@ class Dr16Gpu:
                         ctypes.byref(fit_c), self._stream()), "continuum refinement")
                     keep["refine"] = (warm, refine)
         out["_keep"] = (keep, start, fit_c, index)
+        return out
+
+    def _new_fit(self, spectra):
+        n = spectra.num
+        dev = self.device
+        return {"zero_point": torch.empty(n, dtype=torch.float64, device=dev),
+                "slope": torch.empty(n, dtype=torch.float64, device=dev),
+                "chi2": torch.empty(n, dtype=torch.float64, device=dev),
+                "ndata": torch.empty(n, dtype=torch.int32, device=dev),
+                "status": torch.empty(n, dtype=torch.int32, device=dev),
+                "iterations": torch.empty(n, dtype=torch.int32, device=dev),
+                "continuum": torch.empty(max(spectra.num_pixels, 1), dtype=torch.float64,
+                                         device=dev)}
+
+    def fit_warm(self, spectra, start, max_iter=3, chi2_tol=1e-7, ab_tol=1e-5):
+        """Certified Newton fits from the warm start ``start`` (FP64 [num, 2],
+        device): a forest gets status 0 only when its point is certified
+        against its own chi2 (remaining Newton step at most ab_tol of
+        max(1, |a|, |b|), chi2 excess over the quadratic model's minimum at
+        most chi2_tol of max(|chi2|, ndata)); the others get status 1 and are
+        left for the plain fit."""
+        lib = _bind()
+        out = self._new_fit(spectra)
+        fit_c = ContFitC(*[out[k].data_ptr() for k in ("zero_point", "slope", "chi2", "ndata",
+                                                        "status", "iterations", "continuum")])
+        model, keep = self._model()
+        start = torch.as_tensor(start, dtype=torch.float64, device=self.device).contiguous()
+        with torch.cuda.device(self.device):
+            check(lib.pg_cont_fit_warm(
+                self.plan.handle, ctypes.byref(spectra.c), ctypes.byref(model),
+                start.data_ptr(), None, spectra.num, int(max_iter), float(chi2_tol),
+                float(ab_tol), ctypes.byref(fit_c), self._stream()), "warm continuum fit")
+        out["_keep"] = (keep, start, fit_c, None)
         return out
 
     def _stacks(self, spectra, fit, mean_cont=True, var_stats=True, delta_stack=True):

@@ -422,6 +422,29 @@ int pg_cont_fit_select(pg_plan *plan, const pg_spectra *spectra, const pg_cont_m
                            *out, scratch_of(plan), plan->num_sms, st);
 }
 
+int pg_cont_fit_warm(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
+                     const double *start, const int32_t *forest_index, int64_t num_index,
+                     int32_t max_iter, double chi2_tol, double ab_tol, const pg_cont_fit *out,
+                     void *stream) {
+    if (!plan || !start) return PG_ERR_INVALID_ARGUMENT;
+    int rc;
+    if ((rc = validate_spectra(spectra)) || (rc = validate_model(model)) ||
+        (rc = validate_fit(out, false)))
+        return rc;
+    if (max_iter < 1 || !(chi2_tol > 0) || !(ab_tol > 0) || !(ab_tol < 1))
+        return PG_ERR_INVALID_ARGUMENT;
+    if (num_index < 0 || (forest_index == nullptr && num_index != spectra->num) ||
+        num_index > INT32_MAX)
+        return PG_ERR_INVALID_ARGUMENT;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    if ((rc = reset_scratch(plan, st))) return rc;
+    return launch_cont_fit(*spectra, *model, start, forest_index, num_index, max_iter, 1e-10,
+                           PG_FIT_MIXED, *out, scratch_of(plan), plan->num_sms, st,
+                           (float)chi2_tol, (float)ab_tol);
+}
+
 int pg_cont_stacks_accumulate(pg_plan *plan, const pg_spectra *spectra,
                               const pg_cont_model *model, const pg_cont_fit *fit,
                               const pg_cont_stacks *stacks, void *stream) {

@@ -619,10 +619,22 @@ __device__ __forceinline__ void eval_all_f(const PixelTerms<float> &px, float a,
     for (int k = 0; k < 6; ++k) s[k] = warp_sum_f(s[k]);
 }
 
+// cert_chi2 > 0 selects the certificate stop of the warm-started fit
+// (pg_cont_fit_warm). Once a Newton step d = -H^-1 g is at most
+// sqrt(cert_ab) * max(1, |a|, |b|) (Newton's convergence is quadratic, so the
+// error after it is of order |d|^2), the step is taken and the iteration
+// ends; the final pass, which evaluates chi2 at the new point anyway, also
+// sums the gradient g' there and certifies the point: the remaining step
+// H^-1 g' (with the last Hessian) at most cert_ab * max(1, |a|, |b|) and half
+// the Newton decrement, g'.H^-1 g' / 2 (chi2's excess over the minimum of its
+// quadratic model), at most cert_chi2 * max(|chi2|, ndata). There is no FP64
+// finish; a forest not certified within max_iter iterations gets status 1
+// (the caller re-fits it with the plain fit).
 __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
     const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
     const double *__restrict__ start, const int32_t *__restrict__ index, int64_t count,
-    int max_iter, double tol, const __grid_constant__ pg_cont_fit out, Scratch *scratch) {
+    int max_iter, double tol, const __grid_constant__ pg_cont_fit out, Scratch *scratch,
+    float cert_chi2, float cert_ab) {
     extern __shared__ __align__(16) unsigned char smem[];
     const MixedTables tab = load_tables(m, smem);
     const int lane = threadIdx.x & 31;
@@ -721,6 +733,7 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
         int it = 0;
         // max_iter == 0 with a start: evaluate the model at the given (a, b)
         const bool evaluate_only = max_iter == 0 && start != nullptr;
+        const bool certify = cert_chi2 > 0.f;
         bool converged = evaluate_only;
         for (; it < max_iter; ++it) {
             // Newton step. The 2x2 determinant and numerators are formed in
@@ -729,7 +742,9 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
             // when the data barely separate a from b. The quotient and the
             // rest of the step logic are FP32.
             float da = 0.f, db = 0.f;
+            bool newton = true;  // d = -H^-1 g (not the gradient fallback)
             if (m.order == 0) {
+                newton = s[3] > 0.f;
                 da = s[3] > 0.f ? -s[1] / s[3] : -s[1];
             } else {
                 if (lane == 0) {
@@ -750,11 +765,27 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
                     // singular Hessian or not a descent direction: gradient step
                     da = -s[1] / (scale > 0.f ? scale : 1.f);
                     db = -s[2] / (scale > 0.f ? scale : 1.f);
+                    newton = false;
                 }
             }
             const float ref = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));
             float trial[6];
             float t = 1.f;
+            // a Newton step small enough that the point after it is within
+            // cert_ab: take it; the final pass certifies the new point
+            const float take = sqrtf(cert_ab);
+            if (certify && newton && fabsf(da) <= take * ref && fabsf(db) <= take * ref) {
+                float hi = ah + da, bb = hi - ah;
+                al += (ah - (hi - bb)) + (da - bb);
+                ah = hi;
+                hi = bh + db;
+                bb = hi - bh;
+                bl += (bh - (hi - bb)) + (db - bb);
+                bh = hi;
+                converged = true;
+                ++it;
+                break;
+            }
             if (fabsf(da) < 1e-3f * ref && fabsf(db) < 1e-3f * ref) {
                 eval_all_f(px, ah + da, bh + db, const_w, trial);
             } else {
@@ -784,7 +815,7 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
 #pragma unroll
             for (int k = 0; k < 6; ++k) s[k] = trial[k];
             const float ref2 = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));
-            if (fabsf(t * da) < eff_tol * ref2 && fabsf(t * db) < eff_tol * ref2) {
+            if (!certify && fabsf(t * da) < eff_tol * ref2 && fabsf(t * db) < eff_tol * ref2) {
                 converged = true;
                 ++it;
                 break;
@@ -795,7 +826,7 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
         // the scale of the gradient's FP32 rounding: the per-pixel roundings
         // are independent, so it grows as the root of the sum of squares of
         // the per-pixel gradient terms
-        float cs = 0.f, ce = 0.f, ga_abs = 0.f, gb_abs = 0.f;
+        float cs = 0.f, ce = 0.f, ga_abs = 0.f, gb_abs = 0.f, ga_s = 0.f, gb_s = 0.f;
         const float af = ah, bf = bh;
 #pragma unroll
         for (int k = 0; k < kContK; ++k) {
@@ -810,6 +841,11 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
             const float g = fabsf(2.f * rid) + rid * rid * fabsf(dd) + fabsf(dd * id);
             ga_abs += (g * px.ja[k]) * (g * px.ja[k]);
             gb_abs += (g * px.jb[k]) * (g * px.jb[k]);
+            if (certify) {
+                const float gs = -2.f * rid - rid * rid * dd + dd * id;
+                ga_s += gs * px.ja[k];
+                gb_s += gs * px.jb[k];
+            }
             const float term = r * rid + (const_w ? 0.f : logf(d));
             const float ns = cs + term;
             const float bb = ns - cs;
@@ -828,11 +864,38 @@ __global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
         const double chi2 = (double)cs + (double)ce;
         ga_abs = warp_sum_f(ga_abs);
         gb_abs = warp_sum_f(gb_abs);
+        if (certify) {
+            ga_s = warp_sum_f(ga_s);
+            gb_s = warp_sum_f(gb_s);
+            // certificate at the accepted point, with the last Hessian
+            bool cert = false;
+            if (converged) {
+                const float ref = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));
+                float ra = 0.f, rb = 0.f;
+                bool ok_h = true;
+                if (m.order == 0) {
+                    ok_h = s[3] > 0.f;
+                    ra = ok_h ? -ga_s / s[3] : 0.f;
+                } else {
+                    const double s3 = s[3], s4 = s[4], s5 = s[5];
+                    const double det = fma(s3, s5, -s4 * s4);
+                    ok_h = det > 0. && s[3] > 0.f;
+                    if (ok_h) {
+                        ra = -(float)((s5 * ga_s - s4 * gb_s) / det);
+                        rb = -(float)((s3 * gb_s - s4 * ga_s) / det);
+                    }
+                }
+                const float half_dec = -0.5f * (ra * ga_s + rb * gb_s);
+                cert = ok_h && fabsf(ra) <= cert_ab * ref && fabsf(rb) <= cert_ab * ref &&
+                       half_dec <= cert_chi2 * fmaxf(fabsf(cs + ce), (float)nd);
+            }
+            converged = cert;
+        }
         // estimate of the optimum's shift by that rounding, |H^-1| (8 u
         // rms(g)): large when the data barely separate a from b (a forest
         // covering a short stretch of the rest-frame window)
         bool refine = false;
-        if (lane == 0 && converged && !evaluate_only) {
+        if (lane == 0 && converged && !evaluate_only && !certify) {
             const float ua = 8.f * 5.96e-8f * sqrtf(ga_abs);
             const float ub = 8.f * 5.96e-8f * sqrtf(gb_abs);
             const float ref = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));
@@ -1185,7 +1248,8 @@ unsigned blocks_for(int64_t num, int num_sms) {
 
 int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *start,
                     const int32_t *index, int64_t count, int max_iter, double tol, int mode,
-                    const pg_cont_fit &out, Scratch *scratch, int num_sms, cudaStream_t stream) {
+                    const pg_cont_fit &out, Scratch *scratch, int num_sms, cudaStream_t stream,
+                    float cert_chi2, float cert_ab) {
     if (count <= 0) return PG_OK;
     const unsigned blocks = blocks_for(count, num_sms);
     if (mode == PG_FIT_MIXED) {
@@ -1194,8 +1258,8 @@ int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *
         cudaError_t err = cudaFuncSetAttribute(
             cont_fit_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return check_cuda(err);
-        cont_fit_mixed_kernel<<<blocks, kContBlock, smem, stream>>>(sp, m, start, index, count,
-                                                                    max_iter, tol, out, scratch);
+        cont_fit_mixed_kernel<<<blocks, kContBlock, smem, stream>>>(
+            sp, m, start, index, count, max_iter, tol, out, scratch, cert_chi2, cert_ab);
     } else {
         cont_fit_kernel<double><<<blocks, kContBlock, 0, stream>>>(sp, m, start, index, count,
                                                                     max_iter, tol, out, scratch);
@@ -1207,11 +1271,14 @@ int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *
     err = cudaFuncSetAttribute(cont_fit_long_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                (int)long_smem);
     if (err != cudaSuccess) return check_cuda(err);
+    // the long kernel has no certificate: under it the warm-started fit of a
+    // long forest runs to convergence with the plain fit's iteration limit
+    const int long_iter = cert_chi2 > 0.f && max_iter < 100 ? 100 : max_iter;
     int64_t long_blocks = (count + kLongWarps - 1) / kLongWarps;
     if (long_blocks > (int64_t)num_sms * 8) long_blocks = (int64_t)num_sms * 8;
     cont_fit_long_kernel<<<(unsigned)(long_blocks < 1 ? 1 : long_blocks), 32 * kLongWarps,
-                           long_smem, stream>>>(sp, m, start, index, count, max_iter, tol, out,
-                                                scratch);
+                           long_smem, stream>>>(sp, m, start, index, count, long_iter,
+                                                cert_chi2 > 0.f ? 1e-10 : tol, out, scratch);
     return check_cuda(cudaGetLastError());
 }
 

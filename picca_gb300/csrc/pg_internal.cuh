@@ -296,7 +296,8 @@ int launch_fast_metal(const pg_fast_metal_params &p, const pg_fast_metal_side &a
 
 int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *start,
                     const int32_t *index, int64_t count, int max_iter, double tol, int mode,
-                    const pg_cont_fit &out, Scratch *scratch, int num_sms, cudaStream_t stream);
+                    const pg_cont_fit &out, Scratch *scratch, int num_sms, cudaStream_t stream,
+                    float cert_chi2 = 0.f, float cert_ab = 0.f);
 int launch_cont_stacks(const pg_spectra &sp, const pg_cont_model &m, const pg_cont_fit &fit,
                        const pg_cont_stacks &st, Scratch *scratch, int num_sms,
                        cudaStream_t stream);

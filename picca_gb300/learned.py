@@ -219,17 +219,25 @@ def predict_start(mlp, feat, a0):
     return torch.stack([a0 * (1.0 + y[:, 0]), a0 * y[:, 1]], dim=1).contiguous()
 
 
-def warm_fit(engine, spectra, mlp, warm_max_iter=8, mode=None):
-    """Warm-started fits with plain-fit fallback. Returns (fit dict, start,
-    fallback mask)."""
+CHI2_TOL = 1e-7
+AB_TOL = 1e-5
+
+
+def warm_fit(engine, spectra, mlp, warm_max_iter=3, mode=None, chi2_tol=CHI2_TOL,
+             ab_tol=AB_TOL):
+    """Warm-started fits, each judged on the GPU by its own certificate
+    (Dr16Gpu.fit_warm: the remaining Newton step and the chi2 excess over the
+    local quadratic minimum, both bounded per forest); forests the network
+    placed too far for ``warm_max_iter`` certified Newton steps are re-fitted
+    by the plain fit, in place. Returns (fit dict, start, fallback mask)."""
     model_c, keep = engine._model()
     feat, a0 = features(engine, spectra, model_c)
     start = predict_start(mlp, feat, a0)
-    fit = engine.fit(spectra, start=start, mode=mode, max_iter=warm_max_iter)
+    fit = engine.fit_warm(spectra, start, max_iter=warm_max_iter, chi2_tol=chi2_tol,
+                          ab_tol=ab_tol)
     fallback = fit["status"] != 0
     index = torch.nonzero(fallback).flatten().to(torch.int32)
     if index.numel():
-        # plain fits of the fallback forests only, written in place
         keep_fit = fit["_keep"]
         engine.fit(spectra, mode=mode, index=index, out=fit)
         fit["_keep"] = keep_fit
@@ -254,7 +262,7 @@ def collect_training(engine, spectra):
     return torch.cat(feats), torch.cat(targs), fit
 
 
-def run_warm(engine, spectra, mlp, warm_max_iter=8, mode=None):
+def run_warm(engine, spectra, mlp, warm_max_iter=3, mode=None):
     """The Dr16 loop with learned warm starts (and plain-fit fallback) at
     every iteration. Returns (last fit, per-iteration statistics)."""
     stats = []

@@ -9,6 +9,9 @@
   fit of another set reaches the plain fit's optimum ((a, b) within 1e-4,
   chi2 within 1e-6 relative) with fewer Newton iterations than the plain
   start, and falls back to the plain fit for a small fraction of forests.
+* Certificate: started at the FP64 optimum, the certified fit accepts every
+  forest in one iteration and stays there; started 10% away with a single
+  iteration allowed, it accepts none of the register-kernel forests.
 """
 
 import numpy as np
@@ -81,7 +84,7 @@ def test_warm_start_reaches_plain_optimum_faster(cuda):
     # evaluation: the same model state for both starts
     ev = continuum.DeviceSpectra(eval_raw, eng.device)
     plain = continuum.fit_results_to_host(eng.fit(ev))
-    warm, _, fallback = learned.warm_fit(eng, ev, net, warm_max_iter=8)
+    warm, _, fallback = learned.warm_fit(eng, ev, net)
     warm = continuum.fit_results_to_host(warm)
     ok = (plain["status"] == 0) & (warm["status"] == 0)
     assert ok.mean() > 0.95
@@ -96,3 +99,31 @@ def test_warm_start_reaches_plain_optimum_faster(cuda):
     warm_iters = warm["iterations"][~fallback].mean()
     plain_iters = plain["iterations"][~fallback].mean()
     assert warm_iters < plain_iters, (warm_iters, plain_iters)
+
+
+def test_certificate_accepts_optimum_rejects_far_start(cuda):
+    torch = cuda
+    from picca_gb300 import continuum, synthetic_spectra
+    raw = synthetic_spectra.make_raw_forests(2000, 303)
+    eng = continuum.Dr16Gpu(raw.grid, num_iterations=1)
+    sp = continuum.DeviceSpectra(raw, eng.device)
+    ref = eng.fit(sp)
+    ok = (ref["status"] == 0).cpu().numpy()
+    start = torch.stack([ref["zero_point"], ref["slope"]], 1).contiguous()
+    start = torch.nan_to_num(start)
+    cert = continuum.fit_results_to_host(eng.fit_warm(sp, start, max_iter=3))
+    host = continuum.fit_results_to_host(ref)
+    assert np.all(cert["status"][ok] == 0)
+    assert np.all(cert["iterations"][ok] <= 1)
+    scale = np.maximum(1.0, np.maximum(np.abs(host["zero_point"]), np.abs(host["slope"])))
+    assert np.all(np.abs(cert["zero_point"] - host["zero_point"])[ok] <= 1e-5 * scale[ok])
+    assert np.all(np.abs(cert["slope"] - host["slope"])[ok] <= 1e-5 * scale[ok])
+    chi_scale = np.maximum(np.abs(host["chi2"]), host["ndata"])
+    assert np.all(np.abs(cert["chi2"] - host["chi2"])[ok] <= 1e-6 * chi_scale[ok])
+    # 10% off, one iteration: the Newton step is too long to be taken uncertified
+    far = start.clone()
+    far[:, 0] *= 1.1
+    far[:, 1] += 0.1 * far[:, 0]
+    short = np.diff(raw.pix_offset) <= 224
+    res = continuum.fit_results_to_host(eng.fit_warm(sp, far, max_iter=1))
+    assert np.all(res["status"][ok & short] == 1)
