@@ -50,8 +50,11 @@ def _setup(f):
     wave = str(f["wave_solution"])
     step = 3e-4 if wave == "log" else 0.8
     grid = synthetic_spectra.Grid(step=step, wave_solution=wave)
-    assert np.array_equal(grid.log_lambda_grid, f["log_lambda_grid"])
-    assert np.array_equal(grid.log_lambda_rest_frame_grid, f["log_lambda_rest_frame_grid"])
+    # the linear grid is log10 of the wavelengths, which libm may round one
+    # ulp apart on another machine: the fixture's own grids are used
+    for key in ("log_lambda_grid", "log_lambda_rest_frame_grid"):
+        assert np.allclose(getattr(grid, key), f[key], rtol=0, atol=1e-14)
+        setattr(grid, key, f[key].copy())
     raw = synthetic_spectra.RawForests(
         pix_offset=f["pix_offset"], log_lambda=f["log_lambda"], flux=f["flux"],
         ivar=f["ivar"], transmission_correction=f["transmission_correction"],
