@@ -619,6 +619,253 @@ __device__ __forceinline__ void eval_all_f(const PixelTerms<float> &px, float a,
     for (int k = 0; k < 6; ++k) s[k] = warp_sum_f(s[k]);
 }
 
+// ---- FP64 inputs on the integer pipe -------------------------------------
+// GB300's FP64 pipe is narrow (1/64 of FP32). The mixed fit converts its FP64
+// inputs with integer operations on the bit patterns and forms the one
+// difference that needs more than FP32 (L - Lmin) from two-float parts.
+
+// v rounded to FP32 (round half away from zero on the dropped bits: equal to
+// round-to-nearest-even except on exact ties); FP64 zeros and subnormals give
+// a signed zero; values outside the FP32 range take the conversion path.
+__device__ __forceinline__ float f64_to_f32(double v) {
+    const unsigned hw = (unsigned)__double2hiint(v), lw = (unsigned)__double2loint(v);
+    const unsigned e = (hw >> 20) & 0x7FFu;
+    if (e - 897u <= 253u) {
+        const unsigned mag = ((((hw & 0x7FFFFFFFu) - (896u << 20)) << 3) | (lw >> 29)) +
+                             ((lw >> 28) & 1u);
+        return __uint_as_float((hw & 0x80000000u) | mag);
+    }
+    if (e == 0u) return __uint_as_float(hw & 0x80000000u);
+    return __double2float_rn(v);
+}
+
+// v = hi + lo: hi is v truncated to 24 significant bits, lo the remaining 29
+// bits rounded to FP32 (|v - hi - lo| <= 2^-48 |v|) for 2^-74 <= |v| < 2^127.
+__device__ __forceinline__ float2 split_f64(double v) {
+    const unsigned hw = (unsigned)__double2hiint(v), lw = (unsigned)__double2loint(v);
+    const unsigned e = (hw >> 20) & 0x7FFu;
+    if (e - 949u <= 200u) {
+        const unsigned sign = hw & 0x80000000u;
+        const float hi =
+            __uint_as_float(sign | ((((hw & 0x7FFFFFFFu) - (896u << 20)) << 3) | (lw >> 29)));
+        const unsigned rem = lw & 0x1FFFFFFFu;
+        // the 29-bit remainder as (6 bits) 2^23 + (23 bits), each exact in FP32
+        const float r_lo = __uint_as_float(0x4B000000u | (rem & 0x7FFFFFu)) - 8388608.f;
+        const float r_hi = __uint_as_float(0x4B000000u | (rem >> 23)) - 8388608.f;
+        const float r = fmaf(r_hi, 8388608.f, r_lo) * __uint_as_float((e - 948u) << 23);
+        return make_float2(hi, __uint_as_float(__float_as_uint(r) | sign));
+    }
+    if (e == 0u) return make_float2(__uint_as_float(hw & 0x80000000u), 0.f);
+    const float hi = __double2float_rn(v);
+    return make_float2(hi, __double2float_rn(v - (double)hi));
+}
+
+// x (finite, normal or zero) exactly in FP64
+__device__ __forceinline__ double f32_to_f64(float x) {
+    const unsigned u = __float_as_uint(x);
+    const unsigned ex = (u >> 23) & 0xFFu;
+    if (ex - 1u <= 253u)
+        return __hiloint2double((int)((u & 0x80000000u) | (((u & 0x7FFFFFFFu) >> 3) + (896u << 20))),
+                                (int)(u << 29));
+    if ((u & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
+    return (double)x;
+}
+
+// a b - c d with one rounding's accuracy (Kahan's difference of products)
+__device__ __forceinline__ float diff_prod(float a, float b, float c, float d) {
+    const float w = c * d;
+    const float e = fmaf(-c, d, w);
+    return fmaf(a, b, -w) + e;
+}
+
+// ---- model tables of the mixed fit (shared memory) ----------------------
+// Mean continuum nodes as FP32 offsets from the rest-frame grid start (the
+// pixels' rest-frame coordinate is formed as L - Lmin, exact in FP32 to its
+// last bit); variance functions as FP32 cubics, the three functions of an
+// interval interleaved (eta, var_lss, fudge: c3 c2 c1 c0 each). Uniformly
+// spaced nodes or breaks (the usual case) are found by one multiply and a
+// correction step, others by bisection.
+struct FitTables {
+    const float *mc_off, *mc_y, *mc_slope, *brk;
+    const float4 *coef;
+    int nmc, m;
+    float mc_off0, mc_inv_step, brk0, brk_inv_step;
+    bool mc_uniform, brk_uniform;
+};
+
+__host__ __device__ inline size_t fit_smem_bytes(int nmc, int m) {
+    return (size_t)(3 * nmc + m + 8) * 4 + 16 + (size_t)3 * m * 16 + 16;
+}
+
+__device__ FitTables load_fit_tables(const pg_cont_model &m, unsigned char *smem) {
+    __shared__ int s_uniform[2];
+    FitTables t;
+    const int nmc = m.num_mean_cont, mi = m.use_constant_weight ? 0 : m.num_var_intervals;
+    float4 *coef = reinterpret_cast<float4 *>(smem);
+    float *mc_off = reinterpret_cast<float *>(coef + 3 * mi);
+    float *mc_y = mc_off + nmc;
+    float *mc_slope = mc_y + nmc;
+    float *brk = mc_slope + nmc;
+    if (threadIdx.x == 0) s_uniform[0] = s_uniform[1] = 1;
+    __syncthreads();
+    const double rest_min = m.log_lambda_rest_min;
+    const double mc_step = nmc > 1 ? (m.mean_cont_x[nmc - 1] - m.mean_cont_x[0]) / (nmc - 1) : 1.;
+    for (int i = threadIdx.x; i < nmc; i += blockDim.x) {
+        const double x = m.mean_cont_x[i], y = m.mean_cont_y[i];
+        mc_off[i] = (float)(x - rest_min);
+        mc_y[i] = (float)y;
+        mc_slope[i] = i + 1 < nmc ? (float)((m.mean_cont_y[i + 1] - y) / (m.mean_cont_x[i + 1] - x))
+                                  : 0.f;
+        if (fabs(x - m.mean_cont_x[0] - i * mc_step) > 1e-3 * mc_step) s_uniform[0] = 0;
+    }
+    const double brk_step = mi > 0 ? (m.var_breaks[mi] - m.var_breaks[0]) / mi : 1.;
+    for (int i = threadIdx.x; i <= mi; i += blockDim.x) {
+        brk[i] = (float)m.var_breaks[i];
+        if (fabs(m.var_breaks[i] - m.var_breaks[0] - i * brk_step) > 1e-3 * brk_step)
+            s_uniform[1] = 0;
+    }
+    for (int i = threadIdx.x; i < mi; i += blockDim.x) {
+        coef[3 * i] = make_float4((float)m.eta_coef[i], (float)m.eta_coef[mi + i],
+                                  (float)m.eta_coef[2 * mi + i], (float)m.eta_coef[3 * mi + i]);
+        coef[3 * i + 1] =
+            make_float4((float)m.var_lss_coef[i], (float)m.var_lss_coef[mi + i],
+                        (float)m.var_lss_coef[2 * mi + i], (float)m.var_lss_coef[3 * mi + i]);
+        coef[3 * i + 2] =
+            make_float4((float)m.fudge_coef[i], (float)m.fudge_coef[mi + i],
+                        (float)m.fudge_coef[2 * mi + i], (float)m.fudge_coef[3 * mi + i]);
+    }
+    __syncthreads();
+    t.mc_off = mc_off; t.mc_y = mc_y; t.mc_slope = mc_slope; t.brk = brk; t.coef = coef;
+    t.nmc = nmc; t.m = mi;
+    t.mc_off0 = nmc > 0 ? mc_off[0] : 0.f;
+    t.mc_inv_step = (float)(1.0 / mc_step);
+    t.mc_uniform = s_uniform[0] != 0 && nmc > 2;
+    t.brk0 = mi > 0 ? brk[0] : 0.f;
+    t.brk_inv_step = (float)(1.0 / brk_step);
+    t.brk_uniform = s_uniform[1] != 0 && mi > 1;
+    return t;
+}
+
+// mean continuum at rest-frame offset u = L - Lmin (linear interpolation
+// with extrapolation, interp_linear's intervals)
+__device__ __forceinline__ float fit_mean_cont(const FitTables &t, float u) {
+    int i;
+    const int top = t.nmc - 2;
+    if (t.mc_uniform) {
+        i = __float2int_rd((u - t.mc_off0) * t.mc_inv_step);
+        i = i < 0 ? 0 : (i > top ? top : i);
+        if (i > 0 && u < t.mc_off[i]) --i;
+        else if (i < top && u >= t.mc_off[i + 1]) ++i;
+    } else {
+        int lo = 0, hi = t.nmc;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (t.mc_off[mid] < u) lo = mid + 1;
+            else hi = mid;
+        }
+        i = lo < 1 ? 0 : (lo > t.nmc - 1 ? t.nmc - 2 : lo - 1);
+    }
+    return fmaf(t.mc_slope[i], u - t.mc_off[i], t.mc_y[i]);
+}
+
+// eta, var_lss and fudge at observed log lambda v (eval_ppoly's intervals)
+__device__ __forceinline__ void fit_var_funcs(const FitTables &t, float v, float &eta,
+                                              float &var_lss, float &fudge) {
+    int i;
+    const int top = t.m - 1;
+    if (t.brk_uniform) {
+        i = __float2int_rd((v - t.brk0) * t.brk_inv_step);
+        i = i < 0 ? 0 : (i > top ? top : i);
+        if (i > 0 && v < t.brk[i]) --i;
+        else if (i < top && v >= t.brk[i + 1]) ++i;
+    } else {
+        int lo = 0, hi = t.m + 1;
+        while (lo < hi) {
+            const int mid = (lo + hi) >> 1;
+            if (t.brk[mid] <= v) lo = mid + 1;
+            else hi = mid;
+        }
+        i = lo - 1;
+        i = i < 0 ? 0 : (i > top ? top : i);
+    }
+    const float dx = v - t.brk[i];
+    const float4 ce = t.coef[3 * i], cv = t.coef[3 * i + 1], cf = t.coef[3 * i + 2];
+    eta = fmaf(fmaf(fmaf(ce.x, dx, ce.y), dx, ce.z), dx, ce.w);
+    var_lss = fmaf(fmaf(fmaf(cv.x, dx, cv.y), dx, cv.z), dx, cv.w);
+    fudge = fmaf(fmaf(fmaf(cf.x, dx, cf.y), dx, cf.z), dx, cf.w);
+}
+
+// One lane's pixels of the mixed fit. Unused and masked slots hold
+// mc = 0, f = 0, q = 1, vl = fi = 0 and contribute exactly nothing.
+struct FitPixels {
+    float mc[kContK], x[kContK], f[kContK], q[kContK], vl[kContK], fi[kContK];
+};
+
+// chi2 (with kVal), gradient and Hessian in (a, b) of one lane's pixels,
+// summed over the warp: s = {chi2, ga, gb, haa, hab, hbb}. The per-pixel
+// algebra with h = dD/dC / 2, e = h / D:
+//     dchi2/dC / 2   = e - r/D (1 + r h / D)
+//     d2chi2/dC2 / 2 = 1/D + (h' ) (1/D - (r/D)^2) + e (4 (r/D)(1 + r h/D) - 2 e)
+// where h' = d2D/dC2 / 2 = vl + 6 fi C^2. Newton iterations use the
+// approximate reciprocal (two ulps), the reported values are recomputed
+// with IEEE division.
+template <bool kVal>
+__device__ __forceinline__ void fit_terms(const FitPixels &px, int nk, float a, float b,
+                                          bool const_w, float s[6]) {
+    float val = 0.f, ga = 0.f, gb = 0.f, haa = 0.f, hab = 0.f, hbb = 0.f;
+#pragma unroll
+    for (int k = 0; k < kContK; ++k) {
+        if (k >= nk) break;
+        const float c = px.mc[k] * fmaf(b, px.x[k], a);
+        const float c2 = c * c;
+        const float t1 = fmaf(px.fi[k], c2, px.vl[k]);
+        const float d = fmaf(t1, c2, px.q[k]);
+        const float hd = c * fmaf(px.fi[k], c2, t1);          // (dD/dC) / 2
+        const float h2 = fmaf(4.f * px.fi[k], c2, fmaf(px.fi[k], c2, t1));  // vl + 6 fi C^2
+        const float r = px.f[k] - c;
+        const float id = kVal ? 1.f / d : __fdividef(1.f, d);
+        const float rid = r * id;
+        const float e = hd * id;
+        const float w1 = fmaf(rid, hd, 1.f);
+        const float g = fmaf(-rid, w1, e);
+        const float hh = fmaf(h2, fmaf(-rid, rid, id), id) + e * fmaf(4.f * rid, w1, -2.f * e);
+        const float gj = g * px.mc[k];
+        ga += gj;
+        gb = fmaf(gj, px.x[k], gb);
+        const float hj = hh * px.mc[k] * px.mc[k];
+        haa += hj;
+        const float hjx = hj * px.x[k];
+        hab += hjx;
+        hbb = fmaf(hjx, px.x[k], hbb);
+        if (kVal) val += fmaf(r, rid, const_w ? 0.f : logf(d));
+    }
+    // gradient and Hessian of chi2 (the factors 2 of the half-derivatives)
+    s[0] = val;
+    s[1] = 2.f * ga; s[2] = 2.f * gb;
+    s[3] = 2.f * haa; s[4] = 2.f * hab; s[5] = 2.f * hbb;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+#pragma unroll
+        for (int j = kVal ? 0 : 1; j < 6; ++j) s[j] += __shfl_xor_sync(0xffffffffu, s[j], o);
+    }
+}
+
+constexpr int kFitGroup = 8;  // forests per work item of the mixed fit
+
+struct FitSlot {
+    int64_t f, off;
+    int n, nd, status, it, write;
+    float lm_hi, lm_lo;     // Lmin = rest-frame start + log10(1 + z), two floats
+    float ah, al, bh, bl;   // the start, then the result (two-float sums)
+    float cs, ce;           // chi2 (compensated)
+};
+
+// Mixed-precision fit: FP32 per-pixel terms, (a, b) as two-float sums.
+// Forests are handed out kFitGroup at a time from a work counter; the
+// per-forest FP64 scalars (log10(1 + z), the start, the outputs) are
+// computed by the group's lanes in parallel rather than by one lane per
+// forest.
+//
 // cert_chi2 > 0 selects the certificate stop of the warm-started fit
 // (pg_cont_fit_warm). Once a Newton step d = -H^-1 g is at most
 // sqrt(cert_ab) * max(1, |a|, |b|) (Newton's convergence is quadratic, so the
@@ -630,319 +877,350 @@ __device__ __forceinline__ void eval_all_f(const PixelTerms<float> &px, float a,
 // quadratic model), at most cert_chi2 * max(|chi2|, ndata). There is no FP64
 // finish; a forest not certified within max_iter iterations gets status 1
 // (the caller re-fits it with the plain fit).
-__global__ void __launch_bounds__(kContBlock) cont_fit_mixed_kernel(
+__global__ void __launch_bounds__(kContBlock, 3) cont_fit_mixed_kernel(
     const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
     const double *__restrict__ start, const int32_t *__restrict__ index, int64_t count,
     int max_iter, double tol, const __grid_constant__ pg_cont_fit out, Scratch *scratch,
     float cert_chi2, float cert_ab) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const MixedTables tab = load_tables(m, smem);
+    const FitTables tab = load_fit_tables(m, smem);
     const int lane = threadIdx.x & 31;
-    const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const bool const_w = m.use_constant_weight != 0;
     const float eff_tol = tol > 1e-6 ? (float)tol : 1e-6f;
-    const int mi = tab.m;
-    for (int64_t w = warp_global; w < count; w += nwarps) {
-        const int64_t f = index ? (int64_t)index[w] : w;
-        const int64_t off = sp.pix_offset[f];
-        const int64_t n64 = sp.pix_offset[f + 1] - off;
-        if (n64 > 32 * kContK) continue;  // a long forest: cont_fit_long_kernel
-        if (n64 <= 0) {
-            if (lane == 0) {
-                out.zero_point[f] = NAN;
-                out.slope[f] = NAN;
-                out.chi2[f] = NAN;
-                out.ndata[f] = 0;
-                out.status[f] = 1;
-                out.iterations[f] = 0;
-            }
-            continue;
-        }
-        const int n = (int)n64;
-        // scalar FP64 work runs on lane 0 and is broadcast: GB300's FP64
-        // pipe is narrow, and a warp-wide scalar computation would cost 32
-        // lanes' worth of it
-        double zp1 = 0.;
-        if (lane == 0) zp1 = log10(1 + sp.z_qso[f]);
-        zp1 = __shfl_sync(0xffffffffu, zp1, 0);
-        const double ll_min = m.log_lambda_rest_min + zp1;
-        const float inv_span = (float)(1.0 / (m.log_lambda_rest_max - m.log_lambda_rest_min));
-        PixelTerms<float> px;
-        px.valid = 0;
-        float sfi = 0.f, si = 0.f;
-        float xs[kContK];
-#pragma unroll
-        for (int k = 0; k < kContK; ++k) {
-            const int p = lane + 32 * k;
-            px.ja[k] = px.jb[k] = px.f[k] = px.q[k] = px.vl[k] = px.fi[k] = 0.f;
-            xs[k] = 0.f;
-            if (p < n) {
-                const double ll = sp.log_lambda[off + p];
-                const float fl = (float)sp.flux[off + p];
-                const float iv = (float)sp.ivar[off + p];
-                sfi += fl * iv;
-                si += iv;
-                if (iv > 0.f) {
-                    const float mc = interp_mc(tab, ll - zp1) * (float)sp.transmission_correction[off + p];
-                    const float x = (float)(ll - ll_min) * inv_span;
-                    xs[k] = x;
-                    px.ja[k] = mc;
-                    px.jb[k] = x * mc;
-                    px.f[k] = fl;
-                    if (const_w) {
-                        px.q[k] = 1.f;
-                    } else {
-                        const float llf = (float)ll;
-                        const float eta = ppoly_f(tab.brk_f, tab.coef_f, mi, llf);
-                        px.q[k] = eta / fmaxf(iv, 1.17549435e-38f);
-                        px.vl[k] = ppoly_f(tab.brk_f, tab.coef_f + 4 * mi, mi, llf);
-                        px.fi[k] = ppoly_f(tab.brk_f, tab.coef_f + 8 * mi, mi, llf) * iv;
-                    }
-                    px.valid |= 1u << k;
+    const bool evaluate_only = max_iter == 0 && start != nullptr;
+    const bool certify = cert_chi2 > 0.f;
+    const float inv_span = (float)(1.0 / (m.log_lambda_rest_max - m.log_lambda_rest_min));
+    const int64_t num_groups = (count + kFitGroup - 1) / kFitGroup;
+    // the group's per-forest scalars and results, in shared memory (not
+    // registers) while the warp fits the forests one after the other
+    __shared__ FitSlot s_slots[kContBlock / 32][kFitGroup];
+    FitSlot *slots = s_slots[threadIdx.x >> 5];
+    for (;;) {
+        int64_t group = 0;
+        if (lane == 0) group = atomicAdd(&scratch->work_counter, 1);
+        group = __shfl_sync(0xffffffffu, group, 0);
+        if (group >= num_groups) break;
+        if (lane < kFitGroup) {
+            FitSlot sl;
+            sl.f = -1;
+            sl.off = 0;
+            sl.n = 0;
+            sl.lm_hi = sl.lm_lo = sl.ah = sl.al = sl.bh = sl.bl = 0.f;
+            sl.cs = NAN;
+            sl.ce = 0.f;
+            sl.nd = 0;
+            sl.status = 1;
+            sl.it = 0;
+            sl.write = 0;
+            if (group * kFitGroup + lane < count) {
+                const int64_t w = group * kFitGroup + lane;
+                sl.f = index ? (int64_t)index[w] : w;
+                sl.off = sp.pix_offset[sl.f];
+                sl.n = (int)(sp.pix_offset[sl.f + 1] - sl.off);
+                const float2 lm = split_f64(m.log_lambda_rest_min + log10(1. + sp.z_qso[sl.f]));
+                sl.lm_hi = lm.x;
+                sl.lm_lo = lm.y;
+                if (start) {
+                    const float2 sa = split_f64(start[2 * sl.f]);
+                    const float2 sb =
+                        m.order == 0 ? make_float2(0.f, 0.f) : split_f64(start[2 * sl.f + 1]);
+                    // renormalise (hi + lo) to a two-float sum
+                    sl.ah = sa.x + sa.y;
+                    sl.al = sa.y - (sl.ah - sa.x);
+                    sl.bh = sb.x + sb.y;
+                    sl.bl = sb.y - (sl.bh - sb.x);
                 }
             }
+            slots[lane] = sl;
         }
-        // starting point (utils.py:92): FP32 sums, only a start
-        const float a0f = warp_sum_f(sfi) / warp_sum_f(si);
-        int nd = 0;
+        __syncwarp();
+        for (int j = 0; j < kFitGroup; ++j) {
+            const int64_t f = slots[j].f;
+            if (f < 0) break;
+            const int64_t off = slots[j].off;
+            const int n = slots[j].n;
+            if (n > 32 * kContK) continue;  // a long forest: cont_fit_long_kernel
+            if (lane == j) slots[j].write = 1;
+            if (n <= 0) continue;           // empty: the defaults (status 1, NaN)
+            const float lmh = slots[j].lm_hi;
+            const float lml = slots[j].lm_lo;
+            const int nk = (n + 31) >> 5;
+            FitPixels px;
+            unsigned valid = 0;
+            float sfi = 0.f, si = 0.f;
 #pragma unroll
-        for (int k = 0; k < kContK; ++k) {
-            if ((px.valid >> k) & 1u) {
-                const float c = a0f * px.ja[k];
-                const float c2 = c * c;
-                const float d = px.q[k] + px.vl[k] * c2 + px.fi[k] * c2 * c2;
-                nd += (d > 0.f) ? 1 : 0;
+            for (int k = 0; k < kContK; ++k) {
+                px.mc[k] = px.x[k] = px.f[k] = px.vl[k] = px.fi[k] = 0.f;
+                px.q[k] = 1.f;
+                const int p = lane + 32 * k;
+                if (k < nk && p < n) {
+                    const float iv = f64_to_f32(sp.ivar[off + p]);
+                    const float fl = f64_to_f32(sp.flux[off + p]);
+                    sfi = fmaf(fl, iv, sfi);
+                    si += iv;
+                    if (iv > 0.f) {
+                        const float2 ll = split_f64(sp.log_lambda[off + p]);
+                        const float u = (ll.x - lmh) + (ll.y - lml);  // L - Lmin
+                        px.x[k] = u * inv_span;
+                        px.mc[k] = fit_mean_cont(tab, u) * f64_to_f32(sp.transmission_correction[off + p]);
+                        px.f[k] = fl;
+                        if (!const_w) {
+                            float eta, var_lss, fudge;
+                            fit_var_funcs(tab, ll.x + ll.y, eta, var_lss, fudge);
+                            px.q[k] = eta / fmaxf(iv, 1.17549435e-38f);
+                            px.vl[k] = var_lss;
+                            px.fi[k] = fudge * iv;
+                        }
+                        valid |= 1u << k;
+                    }
+                }
             }
-        }
 #pragma unroll
-        for (int o = 16; o > 0; o >>= 1) nd += __shfl_xor_sync(0xffffffffu, nd, o);
-        // (a, b) as unevaluated sums of two floats (hi + lo): the steps are
-        // accumulated without rounding them away
-        float ah = a0f, al = 0.f, bh = 0.f, bl = 0.f;
-        if (start) {
-            const double a_s = start[2 * f];
-            const double b_s = m.order == 0 ? 0. : start[2 * f + 1];
-            ah = (float)a_s;
-            al = (float)(a_s - (double)ah);
-            bh = (float)b_s;
-            bl = (float)(b_s - (double)bh);
-        }
-        float s[6];
-        eval_all_f(px, ah, bh, const_w, s);
-        int it = 0;
-        // max_iter == 0 with a start: evaluate the model at the given (a, b)
-        const bool evaluate_only = max_iter == 0 && start != nullptr;
-        const bool certify = cert_chi2 > 0.f;
-        bool converged = evaluate_only;
-        for (; it < max_iter; ++it) {
-            // Newton step. The 2x2 determinant and numerators are formed in
-            // FP64 from the FP32 sums (products of two FP32 numbers are exact
-            // in FP64, so only the final subtraction rounds): they cancel
-            // when the data barely separate a from b. The quotient and the
-            // rest of the step logic are FP32.
-            float da = 0.f, db = 0.f;
-            bool newton = true;  // d = -H^-1 g (not the gradient fallback)
-            if (m.order == 0) {
-                newton = s[3] > 0.f;
-                da = s[3] > 0.f ? -s[1] / s[3] : -s[1];
+            for (int o = 16; o > 0; o >>= 1) {
+                sfi += __shfl_xor_sync(0xffffffffu, sfi, o);
+                si += __shfl_xor_sync(0xffffffffu, si, o);
+            }
+            // starting point (utils.py:92): FP32 sums, only a start
+            const float a0f = sfi / si;
+            int nd = 0;
+#pragma unroll
+            for (int k = 0; k < kContK; ++k) {
+                if ((valid >> k) & 1u) {
+                    const float c = a0f * px.mc[k];
+                    const float c2 = c * c;
+                    nd += fmaf(fmaf(px.fi[k], c2, px.vl[k]), c2, px.q[k]) > 0.f ? 1 : 0;
+                }
+            }
+            nd = __reduce_add_sync(0xffffffffu, nd);
+            float ah = a0f, al = 0.f, bh = 0.f, bl = 0.f;
+            if (start) {
+                ah = slots[j].ah;
+                al = slots[j].al;
+                bh = slots[j].bh;
+                bl = slots[j].bl;
+            }
+            float s[6];
+            bool have_val = false;
+            if (evaluate_only) {
+                fit_terms<false>(px, nk, ah, bh, const_w, s);
             } else {
-                if (lane == 0) {
-                    const double s1 = s[1], s2 = s[2], s3 = s[3], s4 = s[4], s5 = s[5];
-                    const double det = fma(s3, s5, -s4 * s4);
-                    if (det > 0. && s[3] > 0.f) {
-                        const float inv = (float)(1.0 / det);
-                        da = -(float)fma(s5, s1, -s4 * s2) * inv;
-                        db = -(float)fma(s3, s2, -s4 * s1) * inv;
-                    } else {
-                        da = db = 0.f;
-                    }
-                }
-                da = __shfl_sync(0xffffffffu, da, 0);
-                db = __shfl_sync(0xffffffffu, db, 0);
-                const float scale = fmaxf(fabsf(s[3]), fabsf(s[5]));
-                if ((da == 0.f && db == 0.f) || da * s[1] + db * s[2] >= 0.f) {
-                    // singular Hessian or not a descent direction: gradient step
-                    da = -s[1] / (scale > 0.f ? scale : 1.f);
-                    db = -s[2] / (scale > 0.f ? scale : 1.f);
-                    newton = false;
-                }
+                fit_terms<true>(px, nk, ah, bh, const_w, s);
+                have_val = true;
             }
-            const float ref = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));
-            float trial[6];
-            float t = 1.f;
-            // a Newton step small enough that the point after it is within
-            // cert_ab: take it; the final pass certifies the new point
-            const float take = sqrtf(cert_ab);
-            if (certify && newton && fabsf(da) <= take * ref && fabsf(db) <= take * ref) {
-                float hi = ah + da, bb = hi - ah;
-                al += (ah - (hi - bb)) + (da - bb);
-                ah = hi;
-                hi = bh + db;
-                bb = hi - bh;
-                bl += (bh - (hi - bb)) + (db - bb);
-                bh = hi;
-                converged = true;
-                ++it;
-                break;
-            }
-            if (fabsf(da) < 1e-3f * ref && fabsf(db) < 1e-3f * ref) {
-                eval_all_f(px, ah + da, bh + db, const_w, trial);
-            } else {
-                const float slope_dir = da * s[1] + db * s[2];
-                bool accepted = false;
-                for (int ls = 0; ls < 40; ++ls) {
-                    eval_all_f(px, ah + t * da, bh + t * db, const_w, trial);
-                    if (isfinite(trial[0]) && trial[0] <= s[0] + 1e-4f * t * slope_dir) {
-                        accepted = true;
-                        break;
-                    }
-                    t *= 0.5f;
-                }
-                if (!accepted) break;
-            }
-            {
-                // (ah, al) += t da exactly to FP32-pair precision (TwoSum)
-                const float sa = t * da, sb = t * db;
-                float hi = ah + sa, bb = hi - ah;
-                al += (ah - (hi - bb)) + (sa - bb);
-                ah = hi;
-                hi = bh + sb;
-                bb = hi - bh;
-                bl += (bh - (hi - bb)) + (sb - bb);
-                bh = hi;
-            }
-#pragma unroll
-            for (int k = 0; k < 6; ++k) s[k] = trial[k];
-            const float ref2 = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));
-            if (!certify && fabsf(t * da) < eff_tol * ref2 && fabsf(t * db) < eff_tol * ref2) {
-                converged = true;
-                ++it;
-                break;
-            }
-        }
-        const double a = (double)ah + (double)al, b = (double)bh + (double)bl;
-        // chi2 at the solution (compensated FP32 sums, lanes and warp) and
-        // the scale of the gradient's FP32 rounding: the per-pixel roundings
-        // are independent, so it grows as the root of the sum of squares of
-        // the per-pixel gradient terms
-        float cs = 0.f, ce = 0.f, ga_abs = 0.f, gb_abs = 0.f, ga_s = 0.f, gb_s = 0.f;
-        const float af = ah, bf = bh;
-#pragma unroll
-        for (int k = 0; k < kContK; ++k) {
-            if (!((px.valid >> k) & 1u)) continue;
-            const float c = af * px.ja[k] + bf * px.jb[k];
-            const float c2 = c * c;
-            const float d = px.q[k] + px.vl[k] * c2 + px.fi[k] * c2 * c2;
-            const float r = px.f[k] - c;
-            const float id = 1.f / d;
-            const float rid = r * id;
-            const float dd = 2.f * px.vl[k] * c + 4.f * px.fi[k] * c2 * c;
-            const float g = fabsf(2.f * rid) + rid * rid * fabsf(dd) + fabsf(dd * id);
-            ga_abs += (g * px.ja[k]) * (g * px.ja[k]);
-            gb_abs += (g * px.jb[k]) * (g * px.jb[k]);
-            if (certify) {
-                const float gs = -2.f * rid - rid * rid * dd + dd * id;
-                ga_s += gs * px.ja[k];
-                gb_s += gs * px.jb[k];
-            }
-            const float term = r * rid + (const_w ? 0.f : logf(d));
-            const float ns = cs + term;
-            const float bb = ns - cs;
-            ce += (cs - (ns - bb)) + (term - bb);
-            cs = ns;
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) {
-            const float os = __shfl_xor_sync(0xffffffffu, cs, o);
-            const float oe = __shfl_xor_sync(0xffffffffu, ce, o);
-            const float ns = cs + os;
-            const float bb = ns - cs;
-            ce += oe + ((cs - (ns - bb)) + (os - bb));
-            cs = ns;
-        }
-        const double chi2 = (double)cs + (double)ce;
-        ga_abs = warp_sum_f(ga_abs);
-        gb_abs = warp_sum_f(gb_abs);
-        if (certify) {
-            ga_s = warp_sum_f(ga_s);
-            gb_s = warp_sum_f(gb_s);
-            // certificate at the accepted point, with the last Hessian
-            bool cert = false;
-            if (converged) {
-                const float ref = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));
-                float ra = 0.f, rb = 0.f;
-                bool ok_h = true;
+            int it = 0;
+            bool converged = evaluate_only;
+            for (; it < max_iter; ++it) {
+                // Newton step from the exact-product 2x2 solve
+                float da, db;
+                bool newton = true;  // d = -H^-1 g (not the gradient fallback)
                 if (m.order == 0) {
-                    ok_h = s[3] > 0.f;
-                    ra = ok_h ? -ga_s / s[3] : 0.f;
+                    newton = s[3] > 0.f;
+                    da = newton ? -s[1] / s[3] : -s[1];
+                    db = 0.f;
                 } else {
-                    const double s3 = s[3], s4 = s[4], s5 = s[5];
-                    const double det = fma(s3, s5, -s4 * s4);
-                    ok_h = det > 0. && s[3] > 0.f;
-                    if (ok_h) {
-                        ra = -(float)((s5 * ga_s - s4 * gb_s) / det);
-                        rb = -(float)((s3 * gb_s - s4 * ga_s) / det);
+                    const float det = diff_prod(s[3], s[5], s[4], s[4]);
+                    da = db = 0.f;
+                    if (det > 0.f && s[3] > 0.f) {
+                        da = -diff_prod(s[5], s[1], s[4], s[2]) / det;
+                        db = -diff_prod(s[3], s[2], s[4], s[1]) / det;
+                    }
+                    if ((da == 0.f && db == 0.f) || da * s[1] + db * s[2] >= 0.f) {
+                        // singular Hessian or not a descent direction: gradient step
+                        const float scale = fmaxf(fabsf(s[3]), fabsf(s[5]));
+                        da = -s[1] / (scale > 0.f ? scale : 1.f);
+                        db = -s[2] / (scale > 0.f ? scale : 1.f);
+                        newton = false;
                     }
                 }
-                const float half_dec = -0.5f * (ra * ga_s + rb * gb_s);
-                cert = ok_h && fabsf(ra) <= cert_ab * ref && fabsf(rb) <= cert_ab * ref &&
-                       half_dec <= cert_chi2 * fmaxf(fabsf(cs + ce), (float)nd);
-            }
-            converged = cert;
-        }
-        // estimate of the optimum's shift by that rounding, |H^-1| (8 u
-        // rms(g)): large when the data barely separate a from b (a forest
-        // covering a short stretch of the rest-frame window)
-        bool refine = false;
-        if (lane == 0 && converged && !evaluate_only && !certify) {
-            const float ua = 8.f * 5.96e-8f * sqrtf(ga_abs);
-            const float ub = 8.f * 5.96e-8f * sqrtf(gb_abs);
-            const float ref = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));
-            float ea, eb;
-            if (m.order == 0) {
-                ea = s[3] > 0.f ? ua / s[3] : INFINITY;
-                eb = 0.f;
-            } else {
-                const double s3 = s[3], s4 = s[4], s5 = s[5];
-                const float det = (float)fma(s3, s5, -s4 * s4);
-                ea = det > 0.f ? (fabsf(s[5]) * ua + fabsf(s[4]) * ub) / det : INFINITY;
-                eb = det > 0.f ? (fabsf(s[4]) * ua + fabsf(s[3]) * ub) / det : INFINITY;
-            }
-            refine = !(ea <= 2e-6f * ref && eb <= 2e-6f * ref);
-        }
-        bool negative = false, all_zero = true;
+                const float ref = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));
+                float t = 1.f;
+                // a Newton step small enough that the point after it is within
+                // cert_ab: take it; the final pass certifies the new point
+                if (certify && newton && fabsf(da) <= sqrtf(cert_ab) * ref &&
+                    fabsf(db) <= sqrtf(cert_ab) * ref) {
+                    float hi = ah + da, bb = hi - ah;
+                    al += (ah - (hi - bb)) + (da - bb);
+                    ah = hi;
+                    hi = bh + db;
+                    bb = hi - bh;
+                    bl += (bh - (hi - bb)) + (db - bb);
+                    bh = hi;
+                    converged = true;
+                    ++it;
+                    break;
+                }
+                float trial[6];
+                if (fabsf(da) < 1e-3f * ref && fabsf(db) < 1e-3f * ref) {
+                    fit_terms<false>(px, nk, ah + da, bh + db, const_w, trial);
+                    have_val = false;
+                } else {
+                    if (!have_val) fit_terms<true>(px, nk, ah, bh, const_w, s);
+                    const float slope_dir = da * s[1] + db * s[2];
+                    bool accepted = false;
+                    for (int ls = 0; ls < 40; ++ls) {
+                        fit_terms<true>(px, nk, ah + t * da, bh + t * db, const_w, trial);
+                        if (isfinite(trial[0]) && trial[0] <= s[0] + 1e-4f * t * slope_dir) {
+                            accepted = true;
+                            break;
+                        }
+                        t *= 0.5f;
+                    }
+                    if (!accepted) break;
+                    have_val = true;
+                }
+                {
+                    // (ah, al) += t da exactly to FP32-pair precision (TwoSum)
+                    const float sa = t * da, sb = t * db;
+                    float hi = ah + sa, bb = hi - ah;
+                    al += (ah - (hi - bb)) + (sa - bb);
+                    ah = hi;
+                    hi = bh + sb;
+                    bb = hi - bh;
+                    bl += (bh - (hi - bb)) + (sb - bb);
+                    bh = hi;
+                }
 #pragma unroll
-        for (int k = 0; k < kContK; ++k) {
-            const int p = lane + 32 * k;
-            if (p >= n) continue;
-            float mc;
-            if ((px.valid >> k) & 1u) {
-                mc = px.ja[k];
-            } else {
-                const double ll = sp.log_lambda[off + p];
-                mc = interp_mc(tab, ll - zp1) * (float)sp.transmission_correction[off + p];
-                xs[k] = (float)(ll - ll_min) * inv_span;
+                for (int k = 0; k < 6; ++k) s[k] = trial[k];
+                const float ref2 = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));
+                if (!certify && fabsf(t * da) < eff_tol * ref2 && fabsf(t * db) < eff_tol * ref2) {
+                    converged = true;
+                    ++it;
+                    break;
+                }
             }
-            const float c = (bf * xs[k] + af) * mc;
-            if (out.continuum) out.continuum[off + p] = (double)c;
-            negative |= c < 0.f;
-            all_zero &= c == 0.f;
+            // chi2 at the solution (compensated FP32 sums, lanes and warp),
+            // the scale of the gradient's FP32 rounding (the per-pixel
+            // roundings are independent, so it grows as the root of the sum
+            // of squares of the per-pixel gradient terms), the gradient for
+            // the certificate, and the continuum
+            float cs = 0.f, ce = 0.f, ga_abs = 0.f, gb_abs = 0.f, ga_s = 0.f, gb_s = 0.f;
+            bool negative = false, all_zero = true;
+            const float af = ah, bf = bh;
+#pragma unroll
+            for (int k = 0; k < kContK; ++k) {
+                const int p = lane + 32 * k;
+                if (k >= nk) break;
+                if (p >= n) continue;
+                float cont;
+                if ((valid >> k) & 1u) {
+                    const float lin = fmaf(bf, px.x[k], af);
+                    const float c = px.mc[k] * lin;
+                    cont = c;
+                    const float c2 = c * c;
+                    const float t1 = fmaf(px.fi[k], c2, px.vl[k]);
+                    const float d = fmaf(t1, c2, px.q[k]);
+                    const float r = px.f[k] - c;
+                    const float id = 1.f / d;
+                    const float rid = r * id;
+                    const float dd = 2.f * c * fmaf(px.fi[k], c2, t1);
+                    const float g = fabsf(2.f * rid) + rid * rid * fabsf(dd) + fabsf(dd * id);
+                    const float jb = px.x[k] * px.mc[k];
+                    ga_abs += (g * px.mc[k]) * (g * px.mc[k]);
+                    gb_abs += (g * jb) * (g * jb);
+                    if (certify) {
+                        const float gs = fmaf(-rid, fmaf(rid, dd, 2.f), dd * id);
+                        ga_s = fmaf(gs, px.mc[k], ga_s);
+                        gb_s = fmaf(gs, jb, gb_s);
+                    }
+                    const float term = fmaf(r, rid, const_w ? 0.f : logf(d));
+                    const float ns = cs + term;
+                    const float bb = ns - cs;
+                    ce += (cs - (ns - bb)) + (term - bb);
+                    cs = ns;
+                } else {
+                    // masked pixel: the continuum only
+                    const float2 ll = split_f64(sp.log_lambda[off + p]);
+                    const float u = (ll.x - lmh) + (ll.y - lml);
+                    const float mc = fit_mean_cont(tab, u) *
+                                     f64_to_f32(sp.transmission_correction[off + p]);
+                    cont = mc * fmaf(bf, u * inv_span, af);
+                }
+                if (out.continuum) out.continuum[off + p] = f32_to_f64(cont);
+                negative |= cont < 0.f;
+                all_zero &= cont == 0.f;
+            }
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                const float os = __shfl_xor_sync(0xffffffffu, cs, o);
+                const float oe = __shfl_xor_sync(0xffffffffu, ce, o);
+                const float ns = cs + os;
+                const float bb = ns - cs;
+                ce += oe + ((cs - (ns - bb)) + (os - bb));
+                cs = ns;
+                ga_abs += __shfl_xor_sync(0xffffffffu, ga_abs, o);
+                gb_abs += __shfl_xor_sync(0xffffffffu, gb_abs, o);
+                if (certify) {
+                    ga_s += __shfl_xor_sync(0xffffffffu, ga_s, o);
+                    gb_s += __shfl_xor_sync(0xffffffffu, gb_s, o);
+                }
+            }
+            negative = __any_sync(0xffffffffu, negative);
+            all_zero = __all_sync(0xffffffffu, all_zero);
+            const float ref = fmaxf(1.f, fmaxf(fabsf(ah), fabsf(bh)));
+            if (certify) {
+                // certificate at the accepted point, with the last Hessian
+                bool cert = false;
+                if (converged) {
+                    float ra = 0.f, rb = 0.f;
+                    bool ok_h;
+                    if (m.order == 0) {
+                        ok_h = s[3] > 0.f;
+                        ra = ok_h ? -ga_s / s[3] : 0.f;
+                    } else {
+                        const float det = diff_prod(s[3], s[5], s[4], s[4]);
+                        ok_h = det > 0.f && s[3] > 0.f;
+                        if (ok_h) {
+                            ra = -diff_prod(s[5], ga_s, s[4], gb_s) / det;
+                            rb = -diff_prod(s[3], gb_s, s[4], ga_s) / det;
+                        }
+                    }
+                    const float half_dec = -0.5f * (ra * ga_s + rb * gb_s);
+                    cert = ok_h && fabsf(ra) <= cert_ab * ref && fabsf(rb) <= cert_ab * ref &&
+                           half_dec <= cert_chi2 * fmaxf(fabsf(cs + ce), (float)nd);
+                }
+                converged = cert;
+            }
+            // estimate of the optimum's shift by that rounding, |H^-1| (8 u
+            // rms(g)): large when the data barely separate a from b (a forest
+            // covering a short stretch of the rest-frame window)
+            bool refine = false;
+            if (converged && !evaluate_only && !certify) {
+                const float ua = 8.f * 5.96e-8f * sqrtf(ga_abs);
+                const float ub = 8.f * 5.96e-8f * sqrtf(gb_abs);
+                float ea, eb;
+                if (m.order == 0) {
+                    ea = s[3] > 0.f ? ua / s[3] : INFINITY;
+                    eb = 0.f;
+                } else {
+                    const float det = diff_prod(s[3], s[5], s[4], s[4]);
+                    ea = det > 0.f ? (fabsf(s[5]) * ua + fabsf(s[4]) * ub) / det : INFINITY;
+                    eb = det > 0.f ? (fabsf(s[4]) * ua + fabsf(s[3]) * ub) / det : INFINITY;
+                }
+                refine = !(ea <= 2e-6f * ref && eb <= 2e-6f * ref);
+            }
+            if (lane == j) {
+                int status = converged ? (refine ? 4 : 0) : 1;
+                if (negative) status = 2;
+                if (all_zero) status = 3;
+                FitSlot &sl = slots[j];
+                sl.status = status;
+                sl.ah = ah; sl.al = al; sl.bh = bh; sl.bl = bl; sl.cs = cs; sl.ce = ce;
+                sl.nd = nd;
+                sl.it = it;
+            }
         }
-        negative = __any_sync(0xffffffffu, negative);
-        all_zero = __all_sync(0xffffffffu, all_zero);
-        if (lane == 0) {
-            int status = converged ? (refine ? 4 : 0) : 1;
-            if (negative) status = 2;
-            if (all_zero) status = 3;
-            const bool keep = status == 0 || status == 4;
-            out.zero_point[f] = keep ? a : NAN;
-            out.slope[f] = keep ? b : NAN;
-            out.chi2[f] = keep ? chi2 : NAN;
-            out.ndata[f] = nd;
-            out.status[f] = status;
-            out.iterations[f] = it;
+        __syncwarp();
+        if (lane < kFitGroup && slots[lane].write) {
+            const FitSlot sl = slots[lane];
+            const bool keep = sl.status == 0 || sl.status == 4;
+            out.zero_point[sl.f] = keep ? f32_to_f64(sl.ah) + f32_to_f64(sl.al) : NAN;
+            out.slope[sl.f] = keep ? f32_to_f64(sl.bh) + f32_to_f64(sl.bl) : NAN;
+            out.chi2[sl.f] = keep ? f32_to_f64(sl.cs) + f32_to_f64(sl.ce) : NAN;
+            out.ndata[sl.f] = sl.nd;
+            out.status[sl.f] = sl.status;
+            out.iterations[sl.f] = sl.it;
         }
+        __syncwarp();
     }
 }
 
@@ -1253,12 +1531,21 @@ int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *
     if (count <= 0) return PG_OK;
     const unsigned blocks = blocks_for(count, num_sms);
     if (mode == PG_FIT_MIXED) {
-        const size_t smem = mixed_smem_bytes(m.num_mean_cont, m.num_var_intervals);
+        const size_t smem = fit_smem_bytes(m.num_mean_cont, m.num_var_intervals);
         if (smem > 200 * 1024) return PG_ERR_UNSUPPORTED;
         cudaError_t err = cudaFuncSetAttribute(
             cont_fit_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
         if (err != cudaSuccess) return check_cuda(err);
-        cont_fit_mixed_kernel<<<blocks, kContBlock, smem, stream>>>(
+        // persistent blocks drawing groups of forests from the work counter
+        int per_sm = 0;
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cont_fit_mixed_kernel,
+                                                            kContBlock, smem);
+        if (err != cudaSuccess) return check_cuda(err);
+        const int64_t groups = (count + kFitGroup - 1) / kFitGroup;
+        int64_t mixed_blocks = (groups + kContBlock / 32 - 1) / (kContBlock / 32);
+        const int64_t resident = (int64_t)num_sms * (per_sm > 0 ? per_sm : 1);
+        if (mixed_blocks > resident) mixed_blocks = resident;
+        cont_fit_mixed_kernel<<<(unsigned)mixed_blocks, kContBlock, smem, stream>>>(
             sp, m, start, index, count, max_iter, tol, out, scratch, cert_chi2, cert_ab);
     } else {
         cont_fit_kernel<double><<<blocks, kContBlock, 0, stream>>>(sp, m, start, index, count,
