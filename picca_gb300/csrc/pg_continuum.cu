@@ -365,153 +365,165 @@ __global__ void __launch_bounds__(32 * kLongWarps) cont_fit_long_kernel(
     const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const bool const_w = m.use_constant_weight != 0;
-    for (int64_t w = warp_global; w < count; w += nwarps) {
-        const int64_t f = index ? (int64_t)index[w] : w;
-        const int64_t off = sp.pix_offset[f];
-        const int64_t n64 = sp.pix_offset[f + 1] - off;
-        if (n64 <= 32 * kContK) continue;  // the register kernels' forests
-        if (n64 > 32 * kLongK) {
-            if (lane == 0) {
-                report_error(scratch, PG_ERR_UNSUPPORTED, (int32_t)f);
-                out.zero_point[f] = NAN;
-                out.slope[f] = NAN;
-                out.chi2[f] = NAN;
-                out.ndata[f] = 0;
-                out.status[f] = 1;
-                out.iterations[f] = 0;
-            }
-            continue;
+    // lanes test 32 forests at a time; the warp fits the long ones among them
+    for (int64_t base = warp_global * 32; base < count; base += nwarps * 32) {
+        int64_t lane_f = -1;
+        bool is_long = false;
+        if (base + lane < count) {
+            lane_f = index ? (int64_t)index[base + lane] : base + lane;
+            is_long = sp.pix_offset[lane_f + 1] - sp.pix_offset[lane_f] > 32 * kContK;
         }
-        const int n = (int)n64;
-        const int nk = (n + 31) / 32;
-        const double zp1 = log10(1 + sp.z_qso[f]);
-        const double ll_min = m.log_lambda_rest_min + zp1;
-        const double ll_max = m.log_lambda_rest_max + zp1;
-        unsigned valid = 0;
-        double sfi = 0., si = 0.;
-        __syncwarp();
-        for (int k = 0; k < nk; ++k) {
-            const int p = lane + 32 * k;
-            const int e = k * 32 + lane;
-            double ja = 0, jb = 0, fl = 0, q = 0, vl = 0, fi = 0;
-            if (p < n) {
-                const double ll = sp.log_lambda[off + p];
-                fl = sp.flux[off + p];
-                const double iv = sp.ivar[off + p];
-                sfi += fl * iv;
-                si += iv;
-                if (iv > 0) {
-                    const ModelEval ev = eval_model(m, ll, zp1, sp.transmission_correction[off + p]);
-                    const double x = (ll - ll_min) / (ll_max - ll_min);
-                    ja = ev.mc;
-                    jb = x * ev.mc;
-                    q = const_w ? 1. : ev.eta / iv;
-                    vl = const_w ? 0. : ev.var_lss;
-                    fi = const_w ? 0. : ev.fudge * iv;
-                    valid |= 1u << k;
+        unsigned todo = __ballot_sync(0xffffffffu, is_long);
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int64_t f = __shfl_sync(0xffffffffu, lane_f, src);
+            const int64_t off = sp.pix_offset[f];
+            const int64_t n64 = sp.pix_offset[f + 1] - off;
+            if (n64 <= 32 * kContK) continue;  // the register kernels' forests
+            if (n64 > 32 * kLongK) {
+                if (lane == 0) {
+                    report_error(scratch, PG_ERR_UNSUPPORTED, (int32_t)f);
+                    out.zero_point[f] = NAN;
+                    out.slope[f] = NAN;
+                    out.chi2[f] = NAN;
+                    out.ndata[f] = 0;
+                    out.status[f] = 1;
+                    out.iterations[f] = 0;
                 }
+                continue;
             }
-            slab[e] = ja; slab[S + e] = jb; slab[2 * S + e] = fl;
-            slab[3 * S + e] = q; slab[4 * S + e] = vl; slab[5 * S + e] = fi;
-        }
-        __syncwarp();
-        sfi = warp_sum(sfi);
-        si = warp_sum(si);
-        const double a0 = sfi / si;  // utils.py:92
-        int nd = 0;
-        for (int k = 0; k < nk; ++k) {
-            if ((valid >> k) & 1u) {
+            const int n = (int)n64;
+            const int nk = (n + 31) / 32;
+            const double zp1 = log10(1 + sp.z_qso[f]);
+            const double ll_min = m.log_lambda_rest_min + zp1;
+            const double ll_max = m.log_lambda_rest_max + zp1;
+            unsigned valid = 0;
+            double sfi = 0., si = 0.;
+            __syncwarp();
+            for (int k = 0; k < nk; ++k) {
+                const int p = lane + 32 * k;
                 const int e = k * 32 + lane;
-                const double c = a0 * slab[e];
-                const double d = slab[3 * S + e] + slab[4 * S + e] * c * c +
-                                 slab[5 * S + e] * c * c * c * c;
-                nd += (d > 0.) ? 1 : 0;
+                double ja = 0, jb = 0, fl = 0, q = 0, vl = 0, fi = 0;
+                if (p < n) {
+                    const double ll = sp.log_lambda[off + p];
+                    fl = sp.flux[off + p];
+                    const double iv = sp.ivar[off + p];
+                    sfi += fl * iv;
+                    si += iv;
+                    if (iv > 0) {
+                        const ModelEval ev = eval_model(m, ll, zp1, sp.transmission_correction[off + p]);
+                        const double x = (ll - ll_min) / (ll_max - ll_min);
+                        ja = ev.mc;
+                        jb = x * ev.mc;
+                        q = const_w ? 1. : ev.eta / iv;
+                        vl = const_w ? 0. : ev.var_lss;
+                        fi = const_w ? 0. : ev.fudge * iv;
+                        valid |= 1u << k;
+                    }
+                }
+                slab[e] = ja; slab[S + e] = jb; slab[2 * S + e] = fl;
+                slab[3 * S + e] = q; slab[4 * S + e] = vl; slab[5 * S + e] = fi;
             }
-        }
-#pragma unroll
-        for (int o = 16; o > 0; o >>= 1) nd += __shfl_xor_sync(0xffffffffu, nd, o);
-        double a = a0, b = 0.;
-        if (start) {
-            a = start[2 * f];
-            b = m.order == 0 ? 0. : start[2 * f + 1];
-        }
-        double s[6];
-        long_terms(slab, valid, nk, a, b, const_w, s);
-        int it = 0;
-        bool converged = max_iter == 0 && start != nullptr;
-        for (; it < max_iter; ++it) {
-            double da, db;
-            if (m.order == 0) {
-                da = s[3] > 0 ? -s[1] / s[3] : -s[1];
-                db = 0.;
-            } else {
-                const double det = s[3] * s[5] - s[4] * s[4];
-                if (det > 0 && s[3] > 0) {
-                    da = -(s[5] * s[1] - s[4] * s[2]) / det;
-                    db = -(s[3] * s[2] - s[4] * s[1]) / det;
+            __syncwarp();
+            sfi = warp_sum(sfi);
+            si = warp_sum(si);
+            const double a0 = sfi / si;  // utils.py:92
+            int nd = 0;
+            for (int k = 0; k < nk; ++k) {
+                if ((valid >> k) & 1u) {
+                    const int e = k * 32 + lane;
+                    const double c = a0 * slab[e];
+                    const double d = slab[3 * S + e] + slab[4 * S + e] * c * c +
+                                     slab[5 * S + e] * c * c * c * c;
+                    nd += (d > 0.) ? 1 : 0;
+                }
+            }
+    #pragma unroll
+            for (int o = 16; o > 0; o >>= 1) nd += __shfl_xor_sync(0xffffffffu, nd, o);
+            double a = a0, b = 0.;
+            if (start) {
+                a = start[2 * f];
+                b = m.order == 0 ? 0. : start[2 * f + 1];
+            }
+            double s[6];
+            long_terms(slab, valid, nk, a, b, const_w, s);
+            int it = 0;
+            bool converged = max_iter == 0 && start != nullptr;
+            for (; it < max_iter; ++it) {
+                double da, db;
+                if (m.order == 0) {
+                    da = s[3] > 0 ? -s[1] / s[3] : -s[1];
+                    db = 0.;
                 } else {
-                    const double scale = fmax(fabs(s[3]), fabs(s[5]));
-                    da = -s[1] / (scale > 0 ? scale : 1.);
-                    db = -s[2] / (scale > 0 ? scale : 1.);
+                    const double det = s[3] * s[5] - s[4] * s[4];
+                    if (det > 0 && s[3] > 0) {
+                        da = -(s[5] * s[1] - s[4] * s[2]) / det;
+                        db = -(s[3] * s[2] - s[4] * s[1]) / det;
+                    } else {
+                        const double scale = fmax(fabs(s[3]), fabs(s[5]));
+                        da = -s[1] / (scale > 0 ? scale : 1.);
+                        db = -s[2] / (scale > 0 ? scale : 1.);
+                    }
+                    if (da * s[1] + db * s[2] >= 0) {  // not a descent direction
+                        const double scale = fmax(fabs(s[3]), fabs(s[5]));
+                        da = -s[1] / (scale > 0 ? scale : 1.);
+                        db = -s[2] / (scale > 0 ? scale : 1.);
+                    }
                 }
-                if (da * s[1] + db * s[2] >= 0) {  // not a descent direction
-                    const double scale = fmax(fabs(s[3]), fabs(s[5]));
-                    da = -s[1] / (scale > 0 ? scale : 1.);
-                    db = -s[2] / (scale > 0 ? scale : 1.);
+                const double slope_dir = da * s[1] + db * s[2];
+                double t = 1.;
+                double trial[6];
+                bool accepted = false;
+                for (int ls = 0; ls < 40; ++ls) {
+                    long_terms(slab, valid, nk, a + t * da, b + t * db, const_w, trial);
+                    if (isfinite(trial[0]) && trial[0] <= s[0] + 1e-4 * t * slope_dir) {
+                        accepted = true;
+                        break;
+                    }
+                    t *= 0.5;
                 }
-            }
-            const double slope_dir = da * s[1] + db * s[2];
-            double t = 1.;
-            double trial[6];
-            bool accepted = false;
-            for (int ls = 0; ls < 40; ++ls) {
-                long_terms(slab, valid, nk, a + t * da, b + t * db, const_w, trial);
-                if (isfinite(trial[0]) && trial[0] <= s[0] + 1e-4 * t * slope_dir) {
-                    accepted = true;
+                if (!accepted) {
+                    converged = fabs(s[1]) + fabs(s[2]) < 1e-6 * fmax(1., fabs(s[0]));
                     break;
                 }
-                t *= 0.5;
+                a += t * da;
+                b += t * db;
+    #pragma unroll
+                for (int k = 0; k < 6; ++k) s[k] = trial[k];
+                if (fabs(t * da) < tol * fmax(1., fmax(fabs(a), fabs(b))) &&
+                    fabs(t * db) < tol * fmax(1., fmax(fabs(a), fabs(b)))) {
+                    converged = true;
+                    ++it;
+                    break;
+                }
             }
-            if (!accepted) {
-                converged = fabs(s[1]) + fabs(s[2]) < 1e-6 * fmax(1., fabs(s[0]));
-                break;
+            double fin[6];
+            long_terms(slab, valid, nk, a, b, const_w, fin);
+            bool negative = false, all_zero = true;
+            for (int p = lane; p < n; p += 32) {
+                const double ll = sp.log_lambda[off + p];
+                const double mc = interp_linear(m.mean_cont_x, m.mean_cont_y, m.num_mean_cont,
+                                                ll - zp1) * sp.transmission_correction[off + p];
+                const double line = b * (ll - ll_min) / (ll_max - ll_min) + a;
+                const double c = line * mc;
+                if (out.continuum) out.continuum[off + p] = c;
+                negative |= c < 0;
+                all_zero &= c == 0;
             }
-            a += t * da;
-            b += t * db;
-#pragma unroll
-            for (int k = 0; k < 6; ++k) s[k] = trial[k];
-            if (fabs(t * da) < tol * fmax(1., fmax(fabs(a), fabs(b))) &&
-                fabs(t * db) < tol * fmax(1., fmax(fabs(a), fabs(b)))) {
-                converged = true;
-                ++it;
-                break;
+            negative = __any_sync(0xffffffffu, negative);
+            all_zero = __all_sync(0xffffffffu, all_zero);
+            if (lane == 0) {
+                int status = converged ? 0 : 1;
+                if (negative) status = 2;
+                if (all_zero) status = 3;
+                out.zero_point[f] = status == 0 ? a : NAN;
+                out.slope[f] = status == 0 ? b : NAN;
+                out.chi2[f] = status == 0 ? fin[0] : NAN;
+                out.ndata[f] = nd;
+                out.status[f] = status;
+                out.iterations[f] = it;
             }
-        }
-        double fin[6];
-        long_terms(slab, valid, nk, a, b, const_w, fin);
-        bool negative = false, all_zero = true;
-        for (int p = lane; p < n; p += 32) {
-            const double ll = sp.log_lambda[off + p];
-            const double mc = interp_linear(m.mean_cont_x, m.mean_cont_y, m.num_mean_cont,
-                                            ll - zp1) * sp.transmission_correction[off + p];
-            const double line = b * (ll - ll_min) / (ll_max - ll_min) + a;
-            const double c = line * mc;
-            if (out.continuum) out.continuum[off + p] = c;
-            negative |= c < 0;
-            all_zero &= c == 0;
-        }
-        negative = __any_sync(0xffffffffu, negative);
-        all_zero = __all_sync(0xffffffffu, all_zero);
-        if (lane == 0) {
-            int status = converged ? 0 : 1;
-            if (negative) status = 2;
-            if (all_zero) status = 3;
-            out.zero_point[f] = status == 0 ? a : NAN;
-            out.slope[f] = status == 0 ? b : NAN;
-            out.chi2[f] = status == 0 ? fin[0] : NAN;
-            out.ndata[f] = nd;
-            out.status[f] = status;
-            out.iterations[f] = it;
         }
     }
 }
@@ -795,49 +807,54 @@ __device__ __forceinline__ void fit_var_funcs(const FitTables &t, float v, float
     fudge = fmaf(fmaf(fmaf(cf.x, dx, cf.y), dx, cf.z), dx, cf.w);
 }
 
-// One lane's pixels of the mixed fit. Unused and masked slots hold
-// mc = 0, f = 0, q = 1, vl = fi = 0 and contribute exactly nothing.
-struct FitPixels {
-    float mc[kContK], x[kContK], f[kContK], q[kContK], vl[kContK], fi[kContK];
+// One lane's pixels of the mixed fit, in the warp's shared-memory slab
+// (slot k of lane l at k * 32 + l: conflict-free, and no lane reads another
+// lane's entries). Unused and masked slots hold mc = 0, f = 0, q = 1,
+// vl = fi = 0 and contribute exactly nothing.
+struct FitSlab {
+    float4 *a;  // mc, x, f, q
+    float2 *b;  // vl, fi
 };
 
-// chi2 (with kVal), gradient and Hessian in (a, b) of one lane's pixels,
+constexpr size_t kFitSlabBytes = (size_t)kContK * 32 * (sizeof(float4) + sizeof(float2));
+
+// chi2 (with want_val), gradient and Hessian in (a, b) of one lane's pixels,
 // summed over the warp: s = {chi2, ga, gb, haa, hab, hbb}. The per-pixel
 // algebra with h = dD/dC / 2, e = h / D:
 //     dchi2/dC / 2   = e - r/D (1 + r h / D)
-//     d2chi2/dC2 / 2 = 1/D + (h' ) (1/D - (r/D)^2) + e (4 (r/D)(1 + r h/D) - 2 e)
-// where h' = d2D/dC2 / 2 = vl + 6 fi C^2. Newton iterations use the
-// approximate reciprocal (two ulps), the reported values are recomputed
-// with IEEE division.
-template <bool kVal>
-__device__ __forceinline__ void fit_terms(const FitPixels &px, int nk, float a, float b,
-                                          bool const_w, float s[6]) {
+//     d2chi2/dC2 / 2 = 1/D + h' (1/D - (r/D)^2) + e (4 (r/D)(1 + r h/D) - 2 e)
+// where h' = d2D/dC2 / 2 = vl + 6 fi C^2. Without want_val (the Newton
+// iterations near the optimum) the reciprocal is the approximate one (two
+// ulps) and chi2 itself is not formed.
+__device__ __forceinline__ void fit_terms(const FitSlab &px, int lane, int nk, float a, float b,
+                                          bool const_w, bool want_val, float s[6]) {
     float val = 0.f, ga = 0.f, gb = 0.f, haa = 0.f, hab = 0.f, hbb = 0.f;
-#pragma unroll
-    for (int k = 0; k < kContK; ++k) {
-        if (k >= nk) break;
-        const float c = px.mc[k] * fmaf(b, px.x[k], a);
+#pragma unroll 1
+    for (int k = 0; k < nk; ++k) {
+        const float4 pa = px.a[k * 32 + lane];
+        const float2 pb = px.b[k * 32 + lane];
+        const float c = pa.x * fmaf(b, pa.y, a);
         const float c2 = c * c;
-        const float t1 = fmaf(px.fi[k], c2, px.vl[k]);
-        const float d = fmaf(t1, c2, px.q[k]);
-        const float hd = c * fmaf(px.fi[k], c2, t1);          // (dD/dC) / 2
-        const float h2 = fmaf(4.f * px.fi[k], c2, fmaf(px.fi[k], c2, t1));  // vl + 6 fi C^2
-        const float r = px.f[k] - c;
-        const float id = kVal ? 1.f / d : __fdividef(1.f, d);
+        const float t1 = fmaf(pb.y, c2, pb.x);
+        const float d = fmaf(t1, c2, pa.w);
+        const float hd = c * fmaf(pb.y, c2, t1);                         // (dD/dC) / 2
+        const float h2 = fmaf(4.f * pb.y, c2, fmaf(pb.y, c2, t1));       // vl + 6 fi C^2
+        const float r = pa.z - c;
+        const float id = want_val ? 1.f / d : __fdividef(1.f, d);
         const float rid = r * id;
         const float e = hd * id;
         const float w1 = fmaf(rid, hd, 1.f);
         const float g = fmaf(-rid, w1, e);
         const float hh = fmaf(h2, fmaf(-rid, rid, id), id) + e * fmaf(4.f * rid, w1, -2.f * e);
-        const float gj = g * px.mc[k];
+        const float gj = g * pa.x;
         ga += gj;
-        gb = fmaf(gj, px.x[k], gb);
-        const float hj = hh * px.mc[k] * px.mc[k];
+        gb = fmaf(gj, pa.y, gb);
+        const float hj = hh * pa.x * pa.x;
         haa += hj;
-        const float hjx = hj * px.x[k];
+        const float hjx = hj * pa.y;
         hab += hjx;
-        hbb = fmaf(hjx, px.x[k], hbb);
-        if (kVal) val += fmaf(r, rid, const_w ? 0.f : logf(d));
+        hbb = fmaf(hjx, pa.y, hbb);
+        if (want_val) val += fmaf(r, rid, const_w ? 0.f : logf(d));
     }
     // gradient and Hessian of chi2 (the factors 2 of the half-derivatives)
     s[0] = val;
@@ -846,7 +863,7 @@ __device__ __forceinline__ void fit_terms(const FitPixels &px, int nk, float a, 
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) {
 #pragma unroll
-        for (int j = kVal ? 0 : 1; j < 6; ++j) s[j] += __shfl_xor_sync(0xffffffffu, s[j], o);
+        for (int q = 0; q < 6; ++q) s[q] += __shfl_xor_sync(0xffffffffu, s[q], o);
     }
 }
 
@@ -877,14 +894,17 @@ struct FitSlot {
 // quadratic model), at most cert_chi2 * max(|chi2|, ndata). There is no FP64
 // finish; a forest not certified within max_iter iterations gets status 1
 // (the caller re-fits it with the plain fit).
-__global__ void __launch_bounds__(kContBlock, 3) cont_fit_mixed_kernel(
+__global__ void __launch_bounds__(kContBlock, 4) cont_fit_mixed_kernel(
     const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
     const double *__restrict__ start, const int32_t *__restrict__ index, int64_t count,
     int max_iter, double tol, const __grid_constant__ pg_cont_fit out, Scratch *scratch,
     float cert_chi2, float cert_ab) {
     extern __shared__ __align__(16) unsigned char smem[];
-    const FitTables tab = load_fit_tables(m, smem);
+    const FitTables tab = load_fit_tables(m, smem + kFitSlabBytes * (kContBlock / 32));
     const int lane = threadIdx.x & 31;
+    FitSlab px;
+    px.a = reinterpret_cast<float4 *>(smem + kFitSlabBytes * (threadIdx.x >> 5));
+    px.b = reinterpret_cast<float2 *>(px.a + kContK * 32);
     const bool const_w = m.use_constant_weight != 0;
     const float eff_tol = tol > 1e-6 ? (float)tol : 1e-6f;
     const bool evaluate_only = max_iter == 0 && start != nullptr;
@@ -945,15 +965,14 @@ __global__ void __launch_bounds__(kContBlock, 3) cont_fit_mixed_kernel(
             const float lmh = slots[j].lm_hi;
             const float lml = slots[j].lm_lo;
             const int nk = (n + 31) >> 5;
-            FitPixels px;
             unsigned valid = 0;
             float sfi = 0.f, si = 0.f;
-#pragma unroll
-            for (int k = 0; k < kContK; ++k) {
-                px.mc[k] = px.x[k] = px.f[k] = px.vl[k] = px.fi[k] = 0.f;
-                px.q[k] = 1.f;
+#pragma unroll 1
+            for (int k = 0; k < nk; ++k) {
+                float4 pa = make_float4(0.f, 0.f, 0.f, 1.f);
+                float2 pb = make_float2(0.f, 0.f);
                 const int p = lane + 32 * k;
-                if (k < nk && p < n) {
+                if (p < n) {
                     const float iv = f64_to_f32(sp.ivar[off + p]);
                     const float fl = f64_to_f32(sp.flux[off + p]);
                     sfi = fmaf(fl, iv, sfi);
@@ -961,19 +980,21 @@ __global__ void __launch_bounds__(kContBlock, 3) cont_fit_mixed_kernel(
                     if (iv > 0.f) {
                         const float2 ll = split_f64(sp.log_lambda[off + p]);
                         const float u = (ll.x - lmh) + (ll.y - lml);  // L - Lmin
-                        px.x[k] = u * inv_span;
-                        px.mc[k] = fit_mean_cont(tab, u) * f64_to_f32(sp.transmission_correction[off + p]);
-                        px.f[k] = fl;
+                        pa.y = u * inv_span;
+                        pa.x = fit_mean_cont(tab, u) * f64_to_f32(sp.transmission_correction[off + p]);
+                        pa.z = fl;
                         if (!const_w) {
                             float eta, var_lss, fudge;
                             fit_var_funcs(tab, ll.x + ll.y, eta, var_lss, fudge);
-                            px.q[k] = eta / fmaxf(iv, 1.17549435e-38f);
-                            px.vl[k] = var_lss;
-                            px.fi[k] = fudge * iv;
+                            pa.w = eta / fmaxf(iv, 1.17549435e-38f);
+                            pb.x = var_lss;
+                            pb.y = fudge * iv;
                         }
                         valid |= 1u << k;
                     }
                 }
+                px.a[k * 32 + lane] = pa;
+                px.b[k * 32 + lane] = pb;
             }
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) {
@@ -983,12 +1004,14 @@ __global__ void __launch_bounds__(kContBlock, 3) cont_fit_mixed_kernel(
             // starting point (utils.py:92): FP32 sums, only a start
             const float a0f = sfi / si;
             int nd = 0;
-#pragma unroll
-            for (int k = 0; k < kContK; ++k) {
+#pragma unroll 1
+            for (int k = 0; k < nk; ++k) {
                 if ((valid >> k) & 1u) {
-                    const float c = a0f * px.mc[k];
+                    const float4 pa = px.a[k * 32 + lane];
+                    const float2 pb = px.b[k * 32 + lane];
+                    const float c = a0f * pa.x;
                     const float c2 = c * c;
-                    nd += fmaf(fmaf(px.fi[k], c2, px.vl[k]), c2, px.q[k]) > 0.f ? 1 : 0;
+                    nd += fmaf(fmaf(pb.y, c2, pb.x), c2, pa.w) > 0.f ? 1 : 0;
                 }
             }
             nd = __reduce_add_sync(0xffffffffu, nd);
@@ -1001,12 +1024,8 @@ __global__ void __launch_bounds__(kContBlock, 3) cont_fit_mixed_kernel(
             }
             float s[6];
             bool have_val = false;
-            if (evaluate_only) {
-                fit_terms<false>(px, nk, ah, bh, const_w, s);
-            } else {
-                fit_terms<true>(px, nk, ah, bh, const_w, s);
-                have_val = true;
-            }
+            fit_terms(px, lane, nk, ah, bh, const_w, !evaluate_only, s);
+            have_val = !evaluate_only;
             int it = 0;
             bool converged = evaluate_only;
             for (; it < max_iter; ++it) {
@@ -1051,14 +1070,14 @@ __global__ void __launch_bounds__(kContBlock, 3) cont_fit_mixed_kernel(
                 }
                 float trial[6];
                 if (fabsf(da) < 1e-3f * ref && fabsf(db) < 1e-3f * ref) {
-                    fit_terms<false>(px, nk, ah + da, bh + db, const_w, trial);
+                    fit_terms(px, lane, nk, ah + da, bh + db, const_w, false, trial);
                     have_val = false;
                 } else {
-                    if (!have_val) fit_terms<true>(px, nk, ah, bh, const_w, s);
+                    if (!have_val) fit_terms(px, lane, nk, ah, bh, const_w, true, s);
                     const float slope_dir = da * s[1] + db * s[2];
                     bool accepted = false;
                     for (int ls = 0; ls < 40; ++ls) {
-                        fit_terms<true>(px, nk, ah + t * da, bh + t * db, const_w, trial);
+                        fit_terms(px, lane, nk, ah + t * da, bh + t * db, const_w, true, trial);
                         if (isfinite(trial[0]) && trial[0] <= s[0] + 1e-4f * t * slope_dir) {
                             accepted = true;
                             break;
@@ -1096,30 +1115,30 @@ __global__ void __launch_bounds__(kContBlock, 3) cont_fit_mixed_kernel(
             float cs = 0.f, ce = 0.f, ga_abs = 0.f, gb_abs = 0.f, ga_s = 0.f, gb_s = 0.f;
             bool negative = false, all_zero = true;
             const float af = ah, bf = bh;
-#pragma unroll
-            for (int k = 0; k < kContK; ++k) {
+#pragma unroll 1
+            for (int k = 0; k < nk; ++k) {
                 const int p = lane + 32 * k;
-                if (k >= nk) break;
                 if (p >= n) continue;
                 float cont;
                 if ((valid >> k) & 1u) {
-                    const float lin = fmaf(bf, px.x[k], af);
-                    const float c = px.mc[k] * lin;
+                    const float4 pa = px.a[k * 32 + lane];
+                    const float2 pb = px.b[k * 32 + lane];
+                    const float c = pa.x * fmaf(bf, pa.y, af);
                     cont = c;
                     const float c2 = c * c;
-                    const float t1 = fmaf(px.fi[k], c2, px.vl[k]);
-                    const float d = fmaf(t1, c2, px.q[k]);
-                    const float r = px.f[k] - c;
+                    const float t1 = fmaf(pb.y, c2, pb.x);
+                    const float d = fmaf(t1, c2, pa.w);
+                    const float r = pa.z - c;
                     const float id = 1.f / d;
                     const float rid = r * id;
-                    const float dd = 2.f * c * fmaf(px.fi[k], c2, t1);
+                    const float dd = 2.f * c * fmaf(pb.y, c2, t1);
                     const float g = fabsf(2.f * rid) + rid * rid * fabsf(dd) + fabsf(dd * id);
-                    const float jb = px.x[k] * px.mc[k];
-                    ga_abs += (g * px.mc[k]) * (g * px.mc[k]);
+                    const float jb = pa.y * pa.x;
+                    ga_abs += (g * pa.x) * (g * pa.x);
                     gb_abs += (g * jb) * (g * jb);
                     if (certify) {
                         const float gs = fmaf(-rid, fmaf(rid, dd, 2.f), dd * id);
-                        ga_s = fmaf(gs, px.mc[k], ga_s);
+                        ga_s = fmaf(gs, pa.x, ga_s);
                         gb_s = fmaf(gs, jb, gb_s);
                     }
                     const float term = fmaf(r, rid, const_w ? 0.f : logf(d));
@@ -1531,7 +1550,8 @@ int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *
     if (count <= 0) return PG_OK;
     const unsigned blocks = blocks_for(count, num_sms);
     if (mode == PG_FIT_MIXED) {
-        const size_t smem = fit_smem_bytes(m.num_mean_cont, m.num_var_intervals);
+        const size_t smem = kFitSlabBytes * (kContBlock / 32) +
+                            fit_smem_bytes(m.num_mean_cont, m.num_var_intervals);
         if (smem > 200 * 1024) return PG_ERR_UNSUPPORTED;
         cudaError_t err = cudaFuncSetAttribute(
             cont_fit_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
@@ -1561,7 +1581,7 @@ int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *
     // the long kernel has no certificate: under it the warm-started fit of a
     // long forest runs to convergence with the plain fit's iteration limit
     const int long_iter = cert_chi2 > 0.f && max_iter < 100 ? 100 : max_iter;
-    int64_t long_blocks = (count + kLongWarps - 1) / kLongWarps;
+    int64_t long_blocks = (count + 32 * kLongWarps - 1) / (32 * kLongWarps);
     if (long_blocks > (int64_t)num_sms * 8) long_blocks = (int64_t)num_sms * 8;
     cont_fit_long_kernel<<<(unsigned)(long_blocks < 1 ? 1 : long_blocks), 32 * kLongWarps,
                            long_smem, stream>>>(sp, m, start, index, count, long_iter,
