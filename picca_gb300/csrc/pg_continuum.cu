@@ -1267,169 +1267,396 @@ __device__ __forceinline__ int64_t find_bin(double x, double grid0, double step,
     return (int64_t)((x - grid0) / step + 0.5);
 }
 
-// Histograms of one Dr16 iteration. A persistent block per SM (one warp per
-// forest, pixels across lanes) accumulates the rest-frame mean continuum, the
-// observed-frame stack and the variance statistics in shared-memory FP64
-// histograms and adds them to the global sums once at the end: 400k forests
-// add to a few thousand bins, and global atomics from every warp would
-// contend on them. The variance functions (three cubic pieces on the same
-// breakpoints, staged in shared memory) are evaluated with one interval
-// search per pixel, and the forest weight once per pixel.
-constexpr int kStackBlock = 512;
-
-__host__ __device__ inline size_t stack_smem_doubles(const pg_cont_stacks &st, int m) {
-    const int nvar = st.var_lambda_bins * kVarBins;
-    return (size_t)2 * st.rest_bins + (size_t)2 * st.obs_bins + (size_t)5 * nvar + (m + 1) +
-           (size_t)12 * m;
-}
-
-// eta, var_lss and fudge at v: one search (searchsorted right, the end
-// pieces extrapolated) and the three cubics as eval_ppoly evaluates them.
-__device__ __forceinline__ void var_funcs(const double *brk, const double *coef, int m, double v,
-                                          double &eta, double &vlss, double &fudge) {
-    int lo = 0, hi = m + 1;
+// eta, var_lss and fudge at v in FP64 from the model's coefficient arrays:
+// one search (searchsorted right, the end pieces extrapolated) and the three
+// cubics as eval_ppoly evaluates them.
+__device__ void var_funcs_f64(const pg_cont_model &m, double v, double &eta, double &vlss,
+                              double &fudge) {
+    const int mi = m.num_var_intervals;
+    int lo = 0, hi = mi + 1;
     while (lo < hi) {
         const int mid = (lo + hi) >> 1;
-        if (brk[mid] <= v) lo = mid + 1;
+        if (m.var_breaks[mid] <= v) lo = mid + 1;
         else hi = mid;
     }
     int i = lo - 1;
-    i = i < 0 ? 0 : (i > m - 1 ? m - 1 : i);
-    const double dx = v - brk[i];
-    const double *c = coef;
-    eta = ((c[i] * dx + c[m + i]) * dx + c[2 * m + i]) * dx + c[3 * m + i];
-    c += 4 * m;
-    vlss = ((c[i] * dx + c[m + i]) * dx + c[2 * m + i]) * dx + c[3 * m + i];
-    c += 4 * m;
-    fudge = ((c[i] * dx + c[m + i]) * dx + c[2 * m + i]) * dx + c[3 * m + i];
+    i = i < 0 ? 0 : (i > mi - 1 ? mi - 1 : i);
+    const double dx = v - m.var_breaks[i];
+    const double *c = m.eta_coef;
+    eta = ((c[i] * dx + c[mi + i]) * dx + c[2 * mi + i]) * dx + c[3 * mi + i];
+    c = m.var_lss_coef;
+    vlss = ((c[i] * dx + c[mi + i]) * dx + c[2 * mi + i]) * dx + c[3 * mi + i];
+    c = m.fudge_coef;
+    fudge = ((c[i] * dx + c[mi + i]) * dx + c[2 * mi + i]) * dx + c[3 * mi + i];
+}
+
+// ---- two-float (double-float) arithmetic -----------------------------------
+// Values as unevaluated sums hi + lo of two floats (about 48 significant
+// bits): the FP32 pipe stands in for the narrow FP64 pipe where FP32 alone
+// would lose the reference's FP64 accuracy.
+struct dfl {
+    float hi, lo;
+};
+
+__device__ __forceinline__ dfl dfl_fast(float a, float b) {  // |a| >= |b|
+    const float s = a + b;
+    return {s, b - (s - a)};
+}
+
+__device__ __forceinline__ dfl dfl_of(double v) {
+    const float2 p = split_f64(v);
+    return dfl_fast(p.x, p.y);
+}
+
+__device__ __forceinline__ dfl dfl_two_sum(float a, float b) {
+    const float s = a + b;
+    const float bb = s - a;
+    return {s, (a - (s - bb)) + (b - bb)};
+}
+
+__device__ __forceinline__ dfl dfl_add(dfl x, dfl y) {
+    dfl s = dfl_two_sum(x.hi, y.hi);
+    const dfl t = dfl_two_sum(x.lo, y.lo);
+    s.lo += t.hi;
+    s = dfl_fast(s.hi, s.lo);
+    s.lo += t.lo;
+    return dfl_fast(s.hi, s.lo);
+}
+
+__device__ __forceinline__ dfl dfl_mul(dfl x, dfl y) {
+    const float p = x.hi * y.hi;
+    float e = fmaf(x.hi, y.hi, -p);
+    e = fmaf(x.hi, y.lo, fmaf(x.lo, y.hi, e));
+    return dfl_fast(p, e);
+}
+
+// x / y: a quotient estimate corrected once with the exact residual
+__device__ __forceinline__ dfl dfl_div(dfl x, dfl y) {
+    const float q1 = __fdividef(x.hi, y.hi);
+    const float p = q1 * y.hi;
+    const float pe = fmaf(q1, y.hi, -p);
+    // r = x - q1 y, from the exact product p + pe (+ q1 y.lo)
+    const dfl r = dfl_add(x, dfl{-p, -fmaf(q1, y.lo, pe)});
+    const float q2 = __fdividef(r.hi, y.hi);
+    return dfl_fast(q1, q2);
+}
+
+__device__ __forceinline__ double dfl_to_f64(dfl x) { return f32_to_f64(x.hi) + f32_to_f64(x.lo); }
+
+// hi/lo histogram bin += x: FP32 atomic adds whose rounding error is
+// recovered exactly from the value each one replaced (TwoSum against the
+// returned old value) and added to the low word with the low part of x
+__device__ __forceinline__ void hist_add(float *hi, float *lo, int bin, dfl x) {
+    const float old = atomicAdd(&hi[bin], x.hi);
+    const float s = old + x.hi;
+    const float bb = s - old;
+    const float err = (old - (s - bb)) + (x.hi - bb);
+    atomicAdd(&lo[bin], err + x.lo);
+}
+
+// trunc(t) of a bin coordinate t evaluated in FP32 with absolute error
+// below guard: certain when t is farther than guard from an integer
+__device__ __forceinline__ bool bin_certain(float t, float guard, int &bin) {
+    const float a = fabsf(t);
+    const float fr = a - truncf(a);
+    bin = __float2int_rz(t);  // toward zero, as astype(int64)
+    return a < 1.0e6f && fr > guard && fr < 1.f - guard;
+}
+
+// Histograms of one Dr16 iteration. Persistent blocks (one warp per forest,
+// pixels across lanes, forests drawn kStackGroup at a time from the work
+// counter) accumulate the rest-frame mean continuum, the observed-frame stack
+// and the variance statistics in shared memory and add them to the global
+// FP64 sums once at the end: 400k forests add to a few thousand bins.
+//
+// GB300's FP64 pipe is 1/64 of its FP32 pipe, so the per-pixel arithmetic is
+// two-float: the FP64 inputs are split on the integer pipe, the weights,
+// flux ratios and delta moments are formed with FP32 error-free
+// transformations (relative error about 1e-13, against the 1e-16 of the
+// reference's FP64), and the histograms are hi/lo pairs of FP32 words. Bin
+// indices are evaluated in FP32 and used where they are certain (farther
+// than a guard from a bin edge); the few pixels within the guard take the
+// reference's FP64 formula. The variance functions are tabulated (FP64,
+// stored as two floats) on the observed-frame grid and read for pixels on a
+// grid node (all of them for forests rebinned to the grid); others evaluate
+// them in FP64.
+constexpr int kStackBlock = 512;
+constexpr int kStackGroup = 8;
+
+struct StackSlot {
+    int64_t off;
+    int n, skip;
+    double zp1;
+    float zr_hi, zr_lo;  // log10(1 + z) + rest grid start (log grid) or log10(1 + z) (linear)
+};
+
+__host__ __device__ inline size_t stack_smem_bytes(const pg_cont_stacks &st, bool table) {
+    const size_t nvar = (size_t)st.var_lambda_bins * kVarBins;
+    return (size_t)8 * (2 * st.rest_bins + 2 * st.obs_bins + 3 * nvar) + (size_t)8 * nvar +
+           (table ? (size_t)32 * st.obs_bins : 0) + 64;
 }
 
 __global__ void __launch_bounds__(kStackBlock) cont_stacks_kernel(
     const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
     const __grid_constant__ pg_cont_fit fit, const __grid_constant__ pg_cont_stacks st,
-    Scratch *scratch) {
+    Scratch *scratch, int use_table) {
     extern __shared__ __align__(16) unsigned char smem_raw[];
     __shared__ uint32_t seen[kStackBlock / 32][64];  // per-warp bitmap of var bins (<= 2048)
+    __shared__ StackSlot s_slots[kStackBlock / 32][kStackGroup];
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
     const int nvar = st.var_lambda_bins * kVarBins;
     const int mi = m.use_constant_weight ? 0 : m.num_var_intervals;
-    double *base = reinterpret_cast<double *>(smem_raw);
-    double *mc_num = base, *mc_w = mc_num + st.rest_bins;
-    double *s_num = mc_w + st.rest_bins, *s_w = s_num + st.obs_bins;
-    double *v_mean = s_w + st.obs_bins, *v_d2 = v_mean + nvar, *v_d4 = v_d2 + nvar;
-    double *v_np = v_d4 + nvar, *v_nq = v_np + nvar;
-    double *brk = v_nq + nvar, *coef = brk + (mi + 1);
-    const int nhist = 2 * st.rest_bins + 2 * st.obs_bins + 5 * nvar;
-    for (int k = threadIdx.x; k < nhist; k += blockDim.x) base[k] = 0.;
-    for (int k = threadIdx.x; k <= mi && mi > 0; k += blockDim.x) brk[k] = m.var_breaks[k];
-    for (int k = threadIdx.x; k < 4 * mi; k += blockDim.x) {
-        coef[k] = m.eta_coef[k];
-        coef[4 * mi + k] = m.var_lss_coef[k];
-        coef[8 * mi + k] = m.fudge_coef[k];
+    const int R = st.rest_bins, O = st.obs_bins;
+    // layout: table (float4 x 2 per obs bin), then hi/lo FP32 histograms, then counts
+    float4 *table = reinterpret_cast<float4 *>(smem_raw);
+    float *hist = reinterpret_cast<float *>(smem_raw + (use_table ? (size_t)32 * O : 0));
+    float *mc_num_h = hist, *mc_num_l = mc_num_h + R, *mc_w_h = mc_num_l + R, *mc_w_l = mc_w_h + R;
+    float *s_num_h = mc_w_l + R, *s_num_l = s_num_h + O, *s_w_h = s_num_l + O, *s_w_l = s_w_h + O;
+    float *v_mean_h = s_w_l + O, *v_mean_l = v_mean_h + nvar;
+    float *v_d2_h = v_mean_l + nvar, *v_d2_l = v_d2_h + nvar;
+    float *v_d4_h = v_d2_l + nvar, *v_d4_l = v_d4_h + nvar;
+    uint32_t *v_np = reinterpret_cast<uint32_t *>(v_d4_l + nvar), *v_nq = v_np + nvar;
+    const int nwords = 4 * R + 4 * O + 8 * nvar;
+    for (int k = threadIdx.x; k < nwords; k += blockDim.x) hist[k] = 0.f;
+    if (use_table) {
+        // variance functions on the observed-frame grid nodes
+        for (int j = threadIdx.x; j < O; j += blockDim.x) {
+            const double g = st.obs_grid0 + j * st.obs_step;
+            const double node = st.wave_lin ? log10(g) : g;
+            double eta, vlss, fudge;
+            var_funcs_f64(m, node, eta, vlss, fudge);
+            const dfl n = dfl_of(node), e = dfl_of(eta), v = dfl_of(vlss), f = dfl_of(fudge);
+            table[2 * j] = make_float4(n.hi, n.lo, e.hi, e.lo);
+            table[2 * j + 1] = make_float4(v.hi, v.lo, f.hi, f.lo);
+        }
     }
     __syncthreads();
-    const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const bool do_mc = st.mean_cont_num != nullptr;
     const bool do_stack = st.stack_num != nullptr;
     const bool do_var = st.var_mean != nullptr && nvar <= 2048;
-    for (int64_t f = warp_global; f < sp.num; f += nwarps) {
-        if (fit.status[f] != 0) continue;
-        const int64_t off = sp.pix_offset[f];
-        const int64_t n = sp.pix_offset[f + 1] - off;
-        const double zp1 = log10(1 + sp.z_qso[f]);
-        if (do_var) {
-            for (int k = lane; k < 64; k += 32) seen[wib][k] = 0u;
-            __syncwarp();
+    const bool lin = st.wave_lin != 0;
+    const double mod64 = m.var_lss_mod;
+    const dfl mod = dfl_of(mod64);
+    const dfl obs0 = dfl_of(lin ? st.obs_grid0 : st.obs_grid0);
+    const dfl var0 = dfl_of(st.var_grid0);
+    const float inv_obs = (float)(1.0 / st.obs_step), inv_rest = (float)(1.0 / st.rest_step);
+    const float inv_var = (float)(1.0 / st.var_step);
+    const float guard = lin ? 5e-3f : 1e-3f;
+    constexpr float kLn10 = 2.302585093f;
+    const int64_t num_groups = (sp.num + kStackGroup - 1) / kStackGroup;
+    StackSlot *slots = s_slots[wib];
+    for (;;) {
+        int64_t group = 0;
+        if (lane == 0) group = atomicAdd(&scratch->work_counter, 1);
+        group = __shfl_sync(0xffffffffu, group, 0);
+        if (group >= num_groups) break;
+        if (lane < kStackGroup) {
+            StackSlot sl;
+            const int64_t f = group * kStackGroup + lane;
+            sl.skip = 1;
+            sl.off = 0;
+            sl.n = 0;
+            sl.zp1 = 0.;
+            sl.zr_hi = sl.zr_lo = 0.f;
+            if (f < sp.num && fit.status[f] == 0) {
+                sl.skip = 0;
+                sl.off = sp.pix_offset[f];
+                sl.n = (int)(sp.pix_offset[f + 1] - sl.off);
+                sl.zp1 = log10(1 + sp.z_qso[f]);
+                const dfl zr = dfl_of(lin ? sl.zp1 : sl.zp1 + st.rest_grid0);
+                sl.zr_hi = zr.hi;
+                sl.zr_lo = zr.lo;
+            }
+            slots[lane] = sl;
         }
-        for (int64_t p = lane; p < n; p += 32) {
-            const double ll = sp.log_lambda[off + p], fl = sp.flux[off + p];
-            const double iv = sp.ivar[off + p];
-            const double cont = fit.continuum[off + p];
-            if (do_mc || do_stack) {
-                // compute_forest_weights (dr16_expected_flux.py:466-488)
-                double w = 0.;
-                if (iv > 0) {
-                    const double var_pipe = 1. / iv / (cont * cont);
-                    double eta = 0., vlss = 1., fudge = 0.;
-                    if (mi > 0) var_funcs(brk, coef, mi, ll, eta, vlss, fudge);
-                    w = 1.0 / (eta * var_pipe + m.var_lss_mod * vlss + fudge / var_pipe);
-                }
-                if (do_mc) {
-                    // _compute_mean_cont: (f / (C + 1e-16)) * w binned in the rest frame
-                    const int64_t bin = find_bin(ll - zp1, st.rest_grid0, st.rest_step, st.wave_lin);
-                    if (bin >= 0 && bin < st.rest_bins) {
-                        atomicAdd(&mc_num[bin], fl / (cont + 1e-16) * w);
-                        atomicAdd(&mc_w[bin], w);
+        __syncwarp();
+        for (int jf = 0; jf < kStackGroup; ++jf) {
+            if (slots[jf].skip) continue;
+            const int64_t off = slots[jf].off;
+            const int n = slots[jf].n;
+            const double zp1 = slots[jf].zp1;
+            const dfl zr = {slots[jf].zr_hi, slots[jf].zr_lo};
+            if (do_var) {
+                for (int k = lane; k < 64; k += 32) seen[wib][k] = 0u;
+                __syncwarp();
+            }
+            for (int p = lane; p < n; p += 32) {
+                const double ll = sp.log_lambda[off + p];
+                const double iv64 = sp.ivar[off + p];
+                const dfl L = dfl_of(ll), F = dfl_of(sp.flux[off + p]);
+                const dfl C = dfl_of(fit.continuum[off + p]);
+                const dfl IV = dfl_of(iv64);
+                const bool has_iv = iv64 > 0;
+                // observed-frame bin (stack, variance-function table)
+                int jobs = -1;
+                if (do_stack || use_table) {
+                    float t;
+                    if (lin) {
+                        const float lam = exp10f(L.hi) * fmaf(L.lo, kLn10, 1.f);
+                        t = fmaf(lam - (float)st.obs_grid0, inv_obs, 0.5f);
                     } else {
-                        report_error(scratch, PG_ERR_BIN_RANGE, (int32_t)bin);
+                        t = fmaf((L.hi - obs0.hi) + (L.lo - obs0.lo), inv_obs, 0.5f);
+                    }
+                    if (!bin_certain(t, guard, jobs))
+                        jobs = (int)find_bin(ll, st.obs_grid0, st.obs_step, st.wave_lin);
+                }
+                // X = ivar C^2 and var_pipe = 1 / X
+                dfl X = {0.f, 0.f}, vp = {0.f, 0.f}, Q = {0.f, 0.f};
+                if (has_iv) {
+                    X = dfl_mul(IV, dfl_mul(C, C));
+                    vp = dfl_div(dfl{1.f, 0.f}, X);
+                    Q = dfl_div(F, C);
+                }
+                if (do_mc || do_stack) {
+                    // compute_forest_weights (dr16_expected_flux.py:466-488)
+                    dfl w = {0.f, 0.f};
+                    if (has_iv) {
+                        dfl eta = {0.f, 0.f}, vlss = {1.f, 0.f}, fudge = {0.f, 0.f};
+                        if (mi > 0) {
+                            bool done = false;
+                            if (use_table && jobs >= 0 && jobs < O) {
+                                const float4 t0 = table[2 * jobs];
+                                if (fabsf((L.hi - t0.x) + (L.lo - t0.y)) <= 1e-12f) {
+                                    const float4 t1 = table[2 * jobs + 1];
+                                    eta = dfl{t0.z, t0.w};
+                                    vlss = dfl{t1.x, t1.y};
+                                    fudge = dfl{t1.z, t1.w};
+                                    done = true;
+                                }
+                            }
+                            if (!done) {
+                                double e, v, f;
+                                var_funcs_f64(m, ll, e, v, f);
+                                eta = dfl_of(e);
+                                vlss = dfl_of(v);
+                                fudge = dfl_of(f);
+                            }
+                        }
+                        const dfl den = dfl_add(dfl_add(dfl_mul(eta, vp), dfl_mul(mod, vlss)),
+                                                dfl_mul(fudge, X));
+                        w = dfl_div(dfl{1.f, 0.f}, den);
+                    }
+                    if (do_mc) {
+                        // _compute_mean_cont: (f / (C + 1e-16)) * w binned in the rest frame
+                        float t;
+                        if (lin) {
+                            const dfl x = dfl_add(L, dfl{-zr.hi, -zr.lo});
+                            const float lam = exp10f(x.hi) * fmaf(x.lo, kLn10, 1.f);
+                            t = fmaf(lam - (float)st.rest_grid0, inv_rest, 0.5f);
+                        } else {
+                            t = fmaf((L.hi - zr.hi) + (L.lo - zr.lo), inv_rest, 0.5f);
+                        }
+                        int bin;
+                        if (!bin_certain(t, guard, bin))
+                            bin = (int)find_bin(ll - zp1, st.rest_grid0, st.rest_step, st.wave_lin);
+                        if (bin >= 0 && bin < R) {
+                            if (has_iv) {
+                                dfl ratio = Q;
+                                if (!(fabsf(C.hi) > 1e-4f)) {
+                                    // the 1e-16 offset matters: the reference's formula
+                                    const double c64 = fit.continuum[off + p];
+                                    ratio = dfl_of(sp.flux[off + p] / (c64 + 1e-16));
+                                }
+                                hist_add(mc_num_h, mc_num_l, bin, dfl_mul(ratio, w));
+                                hist_add(mc_w_h, mc_w_l, bin, w);
+                            }
+                        } else {
+                            report_error(scratch, PG_ERR_BIN_RANGE, bin);
+                        }
+                    }
+                    if (do_stack) {
+                        // compute_delta_stack: delta = f / C where ivar > 0
+                        if (jobs >= 0 && jobs < O) {
+                            if (has_iv) {
+                                hist_add(s_num_h, s_num_l, jobs, dfl_mul(Q, w));
+                                hist_add(s_w_h, s_w_l, jobs, w);
+                            }
+                        } else {
+                            report_error(scratch, PG_ERR_BIN_RANGE, jobs);
+                        }
                     }
                 }
-                if (do_stack) {
-                    // compute_delta_stack: delta = f / C where ivar > 0
-                    const double delta = iv > 0 ? fl / cont : 0.;
-                    const int64_t bin = find_bin(ll, st.obs_grid0, st.obs_step, st.wave_lin);
-                    if (bin >= 0 && bin < st.obs_bins) {
-                        atomicAdd(&s_num[bin], delta * w);
-                        atomicAdd(&s_w[bin], w);
+                if (do_var && has_iv) {
+                    // LeastsSquaresVarStats.initialize_delta_arrays
+                    // (least_squares_var_stats.py:134-184)
+                    constexpr float kMin = (float)kVarPipeMin, kMax = (float)kVarPipeMax;
+                    const float lv = log10f(vp.hi) + vp.lo / (vp.hi * kLn10);
+                    bool in_range;
+                    int vbin = 0;
+                    const float tv = (lv - kMin) * (float)(kVarBins / (kVarPipeMax - kVarPipeMin));
+                    if (fabsf(lv - kMin) > 1e-4f && fabsf(lv - kMax) > 1e-4f &&
+                        bin_certain(tv, 1e-3f, vbin)) {
+                        in_range = lv > kMin && lv < kMax;
                     } else {
-                        report_error(scratch, PG_ERR_BIN_RANGE, (int32_t)bin);
+                        const double c64 = fit.continuum[off + p];
+                        const double lv64 = log10(1 / iv64 / (c64 * c64));
+                        in_range = lv64 > kVarPipeMin && lv64 < kVarPipeMax;
+                        vbin = (int)((lv64 - kVarPipeMin) / (kVarPipeMax - kVarPipeMin) * kVarBins);
+                    }
+                    if (in_range) {
+                        float t;
+                        if (lin) {
+                            const float lam = exp10f(L.hi) * fmaf(L.lo, kLn10, 1.f);
+                            t = fmaf(lam - (float)st.var_grid0, inv_var, 0.5f);
+                        } else {
+                            t = fmaf((L.hi - var0.hi) + (L.lo - var0.lo), inv_var, 0.5f);
+                        }
+                        int lbin;
+                        if (!bin_certain(t, guard, lbin))
+                            lbin = (int)find_bin(ll, st.var_grid0, st.var_step, st.wave_lin);
+                        const int64_t bin = vbin + (int64_t)kVarBins * lbin;
+                        if (lbin >= 0 && bin >= 0 && bin < nvar) {
+                            const dfl delta = dfl_add(Q, dfl{-1.f, 0.f});
+                            const dfl d2 = dfl_mul(delta, delta);
+                            hist_add(v_mean_h, v_mean_l, (int)bin, delta);
+                            hist_add(v_d2_h, v_d2_l, (int)bin, d2);
+                            hist_add(v_d4_h, v_d4_l, (int)bin, dfl_mul(d2, d2));
+                            atomicAdd(&v_np[bin], 1u);
+                            atomicOr(&seen[wib][bin >> 5], 1u << (bin & 31));
+                        } else {
+                            report_error(scratch, PG_ERR_BIN_RANGE, (int32_t)bin);
+                        }
                     }
                 }
             }
-            if (do_var && iv > 0) {
-                // LeastsSquaresVarStats.initialize_delta_arrays
-                const double var_pipe = 1 / iv / (cont * cont);
-                const double lv = log10(var_pipe);
-                if (lv > kVarPipeMin && lv < kVarPipeMax) {
-                    const int vbin = (int)((lv - kVarPipeMin) / (kVarPipeMax - kVarPipeMin) * kVarBins);
-                    const int64_t lbin = find_bin(ll, st.var_grid0, st.var_step, st.wave_lin);
-                    const int64_t bin = vbin + (int64_t)kVarBins * lbin;
-                    if (bin >= 0 && bin < nvar) {
-                        const double delta = fl / cont - 1;
-                        const double d2 = delta * delta;
-                        atomicAdd(&v_mean[bin], delta);
-                        atomicAdd(&v_d2[bin], d2);
-                        atomicAdd(&v_d4[bin], d2 * d2);
-                        atomicAdd(&v_np[bin], 1.0);
-                        atomicOr(&seen[wib][bin >> 5], 1u << (bin & 31));
-                    } else {
-                        report_error(scratch, PG_ERR_BIN_RANGE, (int32_t)bin);
+            if (do_var) {
+                __syncwarp();
+                for (int k = lane; k < 64; k += 32) {
+                    uint32_t bits = seen[wib][k];
+                    while (bits) {
+                        const int bit = __ffs(bits) - 1;
+                        bits &= bits - 1;
+                        atomicAdd(&v_nq[k * 32 + bit], 1u);
                     }
                 }
+                __syncwarp();
             }
         }
-        if (do_var) {
-            __syncwarp();
-            for (int k = lane; k < 64; k += 32) {
-                uint32_t bits = seen[wib][k];
-                while (bits) {
-                    const int bit = __ffs(bits) - 1;
-                    bits &= bits - 1;
-                    atomicAdd(&v_nq[k * 32 + bit], 1.0);
-                }
-            }
-            __syncwarp();
-        }
+        __syncwarp();
     }
     __syncthreads();
-    // one add per nonzero bin and block
-    auto flush = [&](double *dst, const double *src, int count) {
+    // one FP64 add per nonzero bin and block
+    auto flush = [&](double *dst, const float *h, const float *l, int count) {
         if (!dst) return;
         for (int k = threadIdx.x; k < count; k += blockDim.x)
-            if (src[k] != 0.) atomicAdd(&dst[k], src[k]);
+            if (h[k] != 0.f || l[k] != 0.f) atomicAdd(&dst[k], (double)h[k] + (double)l[k]);
     };
-    flush(st.mean_cont_num, mc_num, st.rest_bins);
-    flush(st.mean_cont_weight, mc_w, st.rest_bins);
-    flush(st.stack_num, s_num, st.obs_bins);
-    flush(st.stack_weight, s_w, st.obs_bins);
+    auto flush_count = [&](double *dst, const uint32_t *c, int count) {
+        if (!dst) return;
+        for (int k = threadIdx.x; k < count; k += blockDim.x)
+            if (c[k]) atomicAdd(&dst[k], (double)c[k]);
+    };
+    flush(st.mean_cont_num, mc_num_h, mc_num_l, R);
+    flush(st.mean_cont_weight, mc_w_h, mc_w_l, R);
+    flush(st.stack_num, s_num_h, s_num_l, O);
+    flush(st.stack_weight, s_w_h, s_w_l, O);
     if (do_var) {
-        flush(st.var_mean, v_mean, nvar);
-        flush(st.var_delta2, v_d2, nvar);
-        flush(st.var_delta4, v_d4, nvar);
-        flush(st.var_npix, v_np, nvar);
-        flush(st.var_nqso, v_nq, nvar);
+        flush(st.var_mean, v_mean_h, v_mean_l, nvar);
+        flush(st.var_delta2, v_d2_h, v_d2_l, nvar);
+        flush(st.var_delta4, v_d4_h, v_d4_l, nvar);
+        flush_count(st.var_npix, v_np, nvar);
+        flush_count(st.var_nqso, v_nq, nvar);
     }
 }
 
@@ -1594,16 +1821,24 @@ int launch_cont_stacks(const pg_spectra &sp, const pg_cont_model &m, const pg_co
                        cudaStream_t stream) {
     if (sp.num <= 0) return PG_OK;
     if (st.var_mean && st.var_lambda_bins * kVarBins > 2048) return PG_ERR_UNSUPPORTED;
-    const int mi = m.use_constant_weight ? 0 : m.num_var_intervals;
-    const size_t smem = stack_smem_doubles(st, mi) * sizeof(double);
+    const bool want_table = !m.use_constant_weight && (st.mean_cont_num || st.stack_num);
+    // the variance-function table when it fits beside the histograms
+    int use_table = want_table && stack_smem_bytes(st, true) <= 200 * 1024 ? 1 : 0;
+    const size_t smem = stack_smem_bytes(st, use_table != 0);
     if (smem > 200 * 1024) return PG_ERR_UNSUPPORTED;
     cudaError_t err = cudaFuncSetAttribute(cont_stacks_kernel,
                                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return check_cuda(err);
-    int64_t blocks = (sp.num + kStackBlock / 32 - 1) / (kStackBlock / 32);
-    if (blocks > num_sms) blocks = num_sms;
+    int per_sm = 0;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cont_stacks_kernel, kStackBlock,
+                                                        smem);
+    if (err != cudaSuccess) return check_cuda(err);
+    const int64_t groups = (sp.num + kStackGroup - 1) / kStackGroup;
+    int64_t blocks = (groups + kStackBlock / 32 - 1) / (kStackBlock / 32);
+    const int64_t resident = (int64_t)num_sms * (per_sm > 0 ? per_sm : 1);
+    if (blocks > resident) blocks = resident;
     cont_stacks_kernel<<<(unsigned)(blocks < 1 ? 1 : blocks), kStackBlock, smem, stream>>>(
-        sp, m, fit, st, scratch);
+        sp, m, fit, st, scratch, use_table);
     return check_cuda(cudaGetLastError());
 }
 
