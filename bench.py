@@ -856,6 +856,9 @@ def continuum_leg(args, cpu_seconds):
     plain_fit, plain_s = timed_loop(lambda: eng_p.run(spectra))
     fit_ms = [a.elapsed_time(b) for a, b in fit_events]
     plain = continuum.fit_results_to_host(plain_fit)
+    # forests the mixed fit finishes in two-float, on the last model state
+    eng_p.fit = orig_fit
+    eng_p.fit(spectra, count_refined=True)
 
     # the same first-iteration fit with every per-pixel term in FP64
     eng_64 = continuum.Dr16Gpu(eval_raw.grid, num_iterations=1)
@@ -964,9 +967,10 @@ def continuum_leg(args, cpu_seconds):
     achieved = fit_bytes / (np.mean(fit_ms) / 1e3) / 1e9
     return {
         "forests": eval_raw.num, "iterations": iters,
-        "solver": "damped Newton, warp per forest; FP32 per-pixel terms, FP64 2x2 solve",
+        "solver": ("damped Newton, warp per forest; FP32 per-pixel terms, exact-product FP32 "
+                   "2x2 solve, two-float finish of the forests FP32 rounding could move"),
         "fp64_terms_fit_s": fp64_s, "mixed_vs_fp64_ab_max_rel": float(d_mixed.max()),
-        "fp64_finish_fraction": float(np.mean(eng_p.refined) / eval_raw.num),
+        "two_float_finish_fraction": float(eng_p.refined[-1] / eval_raw.num),
         "mixed_vs_fp64_chi2_max_rel": float(dchi_mixed.max()),
         "plain_fits_per_s": nfits / plain_s, "learned_fits_per_s": nfits / warm_s,
         "learned_over_plain": plain_s / warm_s,

@@ -121,7 +121,8 @@ typedef struct pg_run_stats {
     int32_t error_detail;       /* e.g. offending bin index                   */
     int64_t rechecked_pairs;    /* FP32_GUARD: pairs re-decided in FP64       */
     int64_t recheck_overflows;  /* FP32_GUARD: early recheck-queue drains     */
-    int64_t work_items;         /* work items processed                        */
+    int64_t work_items;         /* work items processed; pg_cont_fit_select in
+                                   PG_FIT_MIXED: forests finished in two-float */
     int64_t gemm_macs;          /* pg_cf_dmat: multiply-adds of the per-pair
                                    products of the eta terms               */
     int64_t visited_pairs;      /* FP32_GUARD cf: lane steps of the diagonal
@@ -278,8 +279,7 @@ typedef struct pg_cont_model {
 /* Per-forest fit results (device pointers, [num]); continuum is per pixel
  * ([num_pixels], may be NULL). status: 0 ok, 1 not converged, 2 negative
  * continuum, 3 zero continuum (the bad_continuum_reason values of
- * compute_continuum), 4 mixed-precision fit to be finished in FP64 (see
- * pg_cont_fit_select). */
+ * compute_continuum). */
 typedef struct pg_cont_fit {
     double *zero_point, *slope, *chi2;
     int32_t *ndata, *status, *iterations;
@@ -309,8 +309,10 @@ typedef struct pg_cont_stacks {
 } pg_cont_stacks;
 
 #define PG_FIT_FP64 0        /* per-pixel chi2 terms in FP64                   */
-#define PG_FIT_MIXED 1       /* per-pixel terms in FP32, sums and the 2x2
-                                Newton solve in FP64                         */
+#define PG_FIT_MIXED 1       /* per-pixel terms in FP32 (FP64 inputs converted
+                                on the integer pipe), exact-product FP32 2x2
+                                Newton solves, a two-float finish where FP32
+                                rounding could move the optimum          */
 
 /* Fit (zero_point, slope) of every forest by damped Newton iterations on the
  * chi2 of the continuum model. start (optional, [2*num], device) gives a
@@ -331,8 +333,10 @@ int pg_cont_fit_batch(pg_plan *plan, const pg_spectra *spectra, const pg_cont_mo
  * max(tol, 1e-6) * max(1, |a|, |b|), and the continuum is formed in FP32.
  * A converged mixed fit whose optimum the FP32 rounding of the gradient is
  * estimated to move by more than 2e-6 * max(1, |a|, |b|) (a forest whose
- * pixels barely separate a from b) gets status 4 with its (a, b): finish it
- * with PG_FIT_FP64 on those forests, starting from that (a, b). */
+ * pixels barely separate a from b) is finished in the same call by Newton
+ * steps with two-float per-pixel terms and gradient (FP64 accuracy without
+ * the FP64 pipe) until the step is below 1e-11 * max(1, |a|, |b|);
+ * pg_plan_stats' work_items counts those forests. */
 int pg_cont_fit_select(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
                        const double *start, const int32_t *forest_index, int64_t num_index,
                        int32_t max_iter, double tol, int32_t mode, const pg_cont_fit *out,

@@ -34,7 +34,6 @@ FIT_FP64 = 0
 FIT_MIXED = 1
 STATUS_REASONS = {0: None, 1: "minuit didn't converge", 2: "negative continuum",
                   3: "zero continuum"}
-STATUS_REFINE = 4  # mixed-precision fit to be finished in FP64 (never left in results)
 
 _P = ctypes.POINTER
 
@@ -195,7 +194,7 @@ class Dr16Gpu:
         self.stack_y = None
         self.stack_weight = None
         self.history = []
-        self.refined = []  # forests finished in FP64 per mixed fit
+        self.refined = []  # forests finished in two-float per counted mixed fit
 
     # -- model -------------------------------------------------------------
     def _model(self, with_stack=False):
@@ -238,7 +237,8 @@ class Dr16Gpu:
         return ctypes.c_void_p(torch.cuda.current_stream(self.device).cuda_stream)
 
     # -- steps -------------------------------------------------------------
-    def fit(self, spectra, start=None, mode=None, max_iter=None, index=None, out=None):
+    def fit(self, spectra, start=None, mode=None, max_iter=None, index=None, out=None,
+            count_refined=False):
         """Continuum fit of every forest (or of the forests listed in the
         int32 device tensor ``index``, written into an existing result dict
         ``out``); returns a dict of device tensors."""
@@ -264,19 +264,9 @@ class Dr16Gpu:
                 n if index is None else int(index.numel()),
                 int(self.max_iter if max_iter is None else max_iter), float(self.tol), mode,
                 ctypes.byref(fit_c), self._stream()), "continuum fit")
-            if mode == FIT_MIXED:
-                # forests whose optimum the FP32 terms cannot place to 1e-7:
-                # FP64 Newton from the mixed solution
-                refine = torch.nonzero(out["status"] == STATUS_REFINE).flatten().to(torch.int32)
-                self.refined.append(int(refine.numel()))
-                if refine.numel():
-                    warm = torch.stack([out["zero_point"], out["slope"]], dim=1).contiguous()
-                    check(lib.pg_cont_fit_select(
-                        self.plan.handle, ctypes.byref(spectra.c), ctypes.byref(model),
-                        warm.data_ptr(), refine.data_ptr(), int(refine.numel()),
-                        int(max_iter or self.max_iter), float(self.tol), FIT_FP64,
-                        ctypes.byref(fit_c), self._stream()), "continuum refinement")
-                    keep["refine"] = (warm, refine)
+            if count_refined and mode == FIT_MIXED:
+                # forests the mixed fit finished in two-float (synchronises)
+                self.refined.append(int(self.plan.stats().work_items))
         out["_keep"] = (keep, start, fit_c, index)
         return out
 

@@ -637,50 +637,48 @@ __device__ __forceinline__ void eval_all_f(const PixelTerms<float> &px, float a,
 // difference that needs more than FP32 (L - Lmin) from two-float parts.
 
 // v rounded to FP32 (round half away from zero on the dropped bits: equal to
-// round-to-nearest-even except on exact ties); FP64 zeros and subnormals give
-// a signed zero; values outside the FP32 range take the conversion path.
+// round-to-nearest-even except on exact ties). Integer operations only:
+// magnitudes below the FP32 normal range give a signed zero (flush to zero),
+// above it a signed infinity; NaN stays NaN.
 __device__ __forceinline__ float f64_to_f32(double v) {
     const unsigned hw = (unsigned)__double2hiint(v), lw = (unsigned)__double2loint(v);
+    const unsigned sign = hw & 0x80000000u;
     const unsigned e = (hw >> 20) & 0x7FFu;
-    if (e - 897u <= 253u) {
-        const unsigned mag = ((((hw & 0x7FFFFFFFu) - (896u << 20)) << 3) | (lw >> 29)) +
-                             ((lw >> 28) & 1u);
-        return __uint_as_float((hw & 0x80000000u) | mag);
-    }
-    if (e == 0u) return __uint_as_float(hw & 0x80000000u);
-    return __double2float_rn(v);
+    const unsigned mag = ((((hw & 0x7FFFFFFFu) - (896u << 20)) << 3) | (lw >> 29)) +
+                         ((lw >> 28) & 1u);
+    const bool nan = e == 0x7FFu && ((hw & 0xFFFFFu) | lw) != 0u;
+    const unsigned bits = e < 897u ? 0u : (e > 1150u ? (nan ? 0x7FC00000u : 0x7F800000u) : mag);
+    return __uint_as_float(sign | bits);
 }
 
 // v = hi + lo: hi is v truncated to 24 significant bits, lo the remaining 29
-// bits rounded to FP32 (|v - hi - lo| <= 2^-48 |v|) for 2^-74 <= |v| < 2^127.
+// bits rounded to FP32 (|v - hi - lo| <= 2^-48 |v|) for 2^-74 <= |v| < 2^127;
+// outside that range hi = f64_to_f32(v) and lo = 0. Integer operations only.
 __device__ __forceinline__ float2 split_f64(double v) {
     const unsigned hw = (unsigned)__double2hiint(v), lw = (unsigned)__double2loint(v);
     const unsigned e = (hw >> 20) & 0x7FFu;
-    if (e - 949u <= 200u) {
-        const unsigned sign = hw & 0x80000000u;
-        const float hi =
-            __uint_as_float(sign | ((((hw & 0x7FFFFFFFu) - (896u << 20)) << 3) | (lw >> 29)));
-        const unsigned rem = lw & 0x1FFFFFFFu;
-        // the 29-bit remainder as (6 bits) 2^23 + (23 bits), each exact in FP32
-        const float r_lo = __uint_as_float(0x4B000000u | (rem & 0x7FFFFFu)) - 8388608.f;
-        const float r_hi = __uint_as_float(0x4B000000u | (rem >> 23)) - 8388608.f;
-        const float r = fmaf(r_hi, 8388608.f, r_lo) * __uint_as_float((e - 948u) << 23);
-        return make_float2(hi, __uint_as_float(__float_as_uint(r) | sign));
-    }
-    if (e == 0u) return make_float2(__uint_as_float(hw & 0x80000000u), 0.f);
-    const float hi = __double2float_rn(v);
-    return make_float2(hi, __double2float_rn(v - (double)hi));
+    const unsigned sign = hw & 0x80000000u;
+    const float hi =
+        __uint_as_float(sign | ((((hw & 0x7FFFFFFFu) - (896u << 20)) << 3) | (lw >> 29)));
+    const unsigned rem = lw & 0x1FFFFFFFu;
+    // the 29-bit remainder as (6 bits) 2^23 + (23 bits), each exact in FP32
+    const float r_lo = __uint_as_float(0x4B000000u | (rem & 0x7FFFFFu)) - 8388608.f;
+    const float r_hi = __uint_as_float(0x4B000000u | (rem >> 23)) - 8388608.f;
+    const float r = fmaf(r_hi, 8388608.f, r_lo) * __uint_as_float(((e - 948u) & 0xFFu) << 23);
+    const bool normal = e - 949u <= 200u;
+    return make_float2(normal ? hi : f64_to_f32(v),
+                       normal ? __uint_as_float(__float_as_uint(r) | sign) : 0.f);
 }
 
-// x (finite, normal or zero) exactly in FP64
+// x exactly in FP64 (integer operations; FP32 subnormals give a signed zero)
 __device__ __forceinline__ double f32_to_f64(float x) {
     const unsigned u = __float_as_uint(x);
+    const unsigned sign = u & 0x80000000u;
     const unsigned ex = (u >> 23) & 0xFFu;
-    if (ex - 1u <= 253u)
-        return __hiloint2double((int)((u & 0x80000000u) | (((u & 0x7FFFFFFFu) >> 3) + (896u << 20))),
-                                (int)(u << 29));
-    if ((u & 0x7FFFFFFFu) == 0u) return __hiloint2double((int)(u & 0x80000000u), 0);
-    return (double)x;
+    const unsigned hw_n = sign | (((u & 0x7FFFFFFFu) >> 3) + (896u << 20));
+    const unsigned hw_s = sign | 0x7FF00000u | ((u & 0x7FFFFFu) >> 3);  // inf, NaN
+    const unsigned hw = ex == 0u ? sign : (ex == 0xFFu ? hw_s : hw_n);
+    return __hiloint2double((int)hw, ex == 0u ? 0 : (int)(u << 29));
 }
 
 // a b - c d with one rounding's accuracy (Kahan's difference of products)
@@ -986,7 +984,7 @@ __global__ void __launch_bounds__(kContBlock, 4) cont_fit_mixed_kernel(
                         if (!const_w) {
                             float eta, var_lss, fudge;
                             fit_var_funcs(tab, ll.x + ll.y, eta, var_lss, fudge);
-                            pa.w = eta / fmaxf(iv, 1.17549435e-38f);
+                            pa.w = __fdividef(eta, fmaxf(iv, 1.17549435e-38f));
                             pb.x = var_lss;
                             pb.y = fudge * iv;
                         }
@@ -1363,6 +1361,264 @@ __device__ __forceinline__ bool bin_certain(float t, float guard, int &bin) {
     return a < 1.0e6f && fr > guard && fr < 1.f - guard;
 }
 
+// ---- two-float finish of the mixed fit ------------------------------------
+// The forests the mixed fit flagged (status 4: FP32 rounding could move their
+// optimum by more than 2e-6 of max(1, |a|, |b|), a short stretch of the
+// rest-frame window barely separating a from b) are finished here, in the
+// same call, to FP64 accuracy without the FP64 pipe: every per-pixel input
+// (x, the mean continuum, the variance functions) is formed in two-float
+// arithmetic from the FP64 model, the gradient of chi2 is summed in
+// two-float, and Newton steps from the mixed solution (the Hessian in FP32
+// is enough for a correction step) run until the step is below 1e-11 of
+// max(1, |a|, |b|). chi2 is re-evaluated with the logarithm in FP32 plus its
+// first-order two-float correction.
+constexpr int kRefineWarps = 4;
+constexpr size_t kRefineSlabBytes = (size_t)kContK * 32 * 3 * sizeof(float4);
+
+__host__ __device__ inline size_t refine_smem_bytes(int nmc, int m) {
+    return (size_t)kRefineWarps * kRefineSlabBytes + (size_t)3 * nmc * 8 + (size_t)(m + 1) * 8 +
+           (size_t)12 * m * 8 + 16;
+}
+
+// sign of x - y (two-float values)
+__device__ __forceinline__ bool dfl_less(dfl x, dfl y) {
+    return (x.hi - y.hi) + (x.lo - y.lo) < 0.f;
+}
+
+__device__ __forceinline__ dfl dfl_neg(dfl x) { return {-x.hi, -x.lo}; }
+
+__device__ __forceinline__ dfl warp_sum_dfl(dfl v) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+        const dfl w = {__shfl_xor_sync(0xffffffffu, v.hi, o), __shfl_xor_sync(0xffffffffu, v.lo, o)};
+        v = dfl_add(v, w);
+    }
+    return v;
+}
+
+__global__ void __launch_bounds__(32 * kRefineWarps) cont_fit_refine_kernel(
+    const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
+    const int32_t *__restrict__ index, int64_t count, const __grid_constant__ pg_cont_fit out,
+    Scratch *scratch) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    const int lane = threadIdx.x & 31;
+    const int nmc = m.num_mean_cont;
+    const int mi = m.use_constant_weight ? 0 : m.num_var_intervals;
+    const bool const_w = mi == 0;
+    float4 *slab = reinterpret_cast<float4 *>(smem + kRefineSlabBytes * (threadIdx.x >> 5));
+    dfl *node = reinterpret_cast<dfl *>(smem + kRefineSlabBytes * kRefineWarps);  // off, y, slope
+    dfl *brk = node + 3 * nmc;
+    dfl *coef = brk + (mi + 1);  // [i][12]: eta, var_lss, fudge (c3 c2 c1 c0)
+    const double rest_min = m.log_lambda_rest_min;
+    for (int i = threadIdx.x; i < nmc; i += blockDim.x) {
+        const double x = m.mean_cont_x[i], y = m.mean_cont_y[i];
+        node[3 * i] = dfl_of(x - rest_min);
+        node[3 * i + 1] = dfl_of(y);
+        node[3 * i + 2] = dfl_of(i + 1 < nmc ? (m.mean_cont_y[i + 1] - y) / (m.mean_cont_x[i + 1] - x)
+                                             : 0.);
+    }
+    for (int i = threadIdx.x; i <= mi; i += blockDim.x) brk[i] = dfl_of(m.var_breaks[i]);
+    for (int i = threadIdx.x; i < mi; i += blockDim.x) {
+        for (int k = 0; k < 4; ++k) {
+            coef[12 * i + k] = dfl_of(m.eta_coef[k * mi + i]);
+            coef[12 * i + 4 + k] = dfl_of(m.var_lss_coef[k * mi + i]);
+            coef[12 * i + 8 + k] = dfl_of(m.fudge_coef[k * mi + i]);
+        }
+    }
+    __syncthreads();
+    const dfl inv_span = dfl_of(1.0 / (m.log_lambda_rest_max - m.log_lambda_rest_min));
+    const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
+    for (int64_t base = warp_global * 32; base < count; base += nwarps * 32) {
+        int64_t lane_f = -1;
+        bool flagged = false;
+        double lane_lmin = 0.;
+        if (base + lane < count) {
+            lane_f = index ? (int64_t)index[base + lane] : base + lane;
+            flagged = out.status[lane_f] == 4;
+            if (flagged) lane_lmin = rest_min + log10(1. + sp.z_qso[lane_f]);
+        }
+        unsigned todo = __ballot_sync(0xffffffffu, flagged);
+        while (todo) {
+            const int src = __ffs(todo) - 1;
+            todo &= todo - 1;
+            const int64_t f = __shfl_sync(0xffffffffu, lane_f, src);
+            const dfl lmin = dfl_of(__shfl_sync(0xffffffffu, lane_lmin, src));
+            const int64_t off = sp.pix_offset[f];
+            const int n = (int)(sp.pix_offset[f + 1] - off);
+            const int nk = (n + 31) >> 5;
+            // two-float pixel terms: slab[3 (k 32 + lane) + {0, 1, 2}] =
+            // (mc, x), (f, q), (vl, fi), each as hi, lo
+            unsigned valid = 0;
+            for (int k = 0; k < nk; ++k) {
+                const int p = lane + 32 * k;
+                dfl mc = {0.f, 0.f}, x = {0.f, 0.f}, fl = {0.f, 0.f}, q = {1.f, 0.f};
+                dfl vl = {0.f, 0.f}, fi = {0.f, 0.f};
+                if (p < n) {
+                    const dfl L = dfl_of(sp.log_lambda[off + p]);
+                    const dfl u = dfl_add(L, dfl_neg(lmin));  // L - Lmin
+                    x = dfl_mul(u, inv_span);
+                    int lo = 0, hi = nmc;
+                    while (lo < hi) {
+                        const int mid = (lo + hi) >> 1;
+                        if (dfl_less(node[3 * mid], u)) lo = mid + 1;
+                        else hi = mid;
+                    }
+                    const int i = lo < 1 ? 0 : (lo > nmc - 1 ? nmc - 2 : lo - 1);
+                    mc = dfl_add(node[3 * i + 1],
+                                 dfl_mul(node[3 * i + 2], dfl_add(u, dfl_neg(node[3 * i]))));
+                    mc = dfl_mul(mc, dfl_of(sp.transmission_correction[off + p]));
+                    const dfl iv = dfl_of(sp.ivar[off + p]);
+                    if (iv.hi > 0.f) {
+                        fl = dfl_of(sp.flux[off + p]);
+                        if (!const_w) {
+                            int a = 0, b = mi + 1;
+                            while (a < b) {
+                                const int mid = (a + b) >> 1;
+                                if (!dfl_less(L, brk[mid])) a = mid + 1;
+                                else b = mid;
+                            }
+                            int j = a - 1;
+                            j = j < 0 ? 0 : (j > mi - 1 ? mi - 1 : j);
+                            const dfl dx = dfl_add(L, dfl_neg(brk[j]));
+                            dfl v3[3];
+#pragma unroll
+                            for (int g = 0; g < 3; ++g) {
+                                const dfl *c = coef + 12 * j + 4 * g;
+                                dfl acc = c[0];
+                                acc = dfl_add(dfl_mul(acc, dx), c[1]);
+                                acc = dfl_add(dfl_mul(acc, dx), c[2]);
+                                v3[g] = dfl_add(dfl_mul(acc, dx), c[3]);
+                            }
+                            q = dfl_div(v3[0], iv);
+                            vl = v3[1];
+                            fi = dfl_mul(v3[2], iv);
+                        }
+                        valid |= 1u << k;
+                    }
+                }
+                float4 *e = slab + 3 * (k * 32 + lane);
+                e[0] = make_float4(mc.hi, mc.lo, x.hi, x.lo);
+                e[1] = make_float4(fl.hi, fl.lo, q.hi, q.lo);
+                e[2] = make_float4(vl.hi, vl.lo, fi.hi, fi.lo);
+            }
+            dfl a = dfl_of(out.zero_point[f]);
+            dfl b = m.order == 0 ? dfl{0.f, 0.f} : dfl_of(out.slope[f]);
+            int it = 0;
+            bool converged = false;
+            float h3 = 0.f, h4 = 0.f, h5 = 0.f;
+            for (; it < 10; ++it) {
+                // gradient (two-float) and Hessian (FP32) at (a, b)
+                dfl ga = {0.f, 0.f}, gb = {0.f, 0.f};
+                float haa = 0.f, hab = 0.f, hbb = 0.f;
+                for (int k = 0; k < nk; ++k) {
+                    if (!((valid >> k) & 1u)) continue;
+                    const float4 *e = slab + 3 * (k * 32 + lane);
+                    const float4 e0 = e[0], e1 = e[1], e2 = e[2];
+                    const dfl mc = {e0.x, e0.y}, x = {e0.z, e0.w}, fl = {e1.x, e1.y};
+                    const dfl q = {e1.z, e1.w}, vl = {e2.x, e2.y}, fi = {e2.z, e2.w};
+                    const dfl c = dfl_mul(mc, dfl_add(a, dfl_mul(b, x)));
+                    const dfl c2 = dfl_mul(c, c);
+                    const dfl fc2 = dfl_mul(fi, c2);
+                    const dfl t1 = dfl_add(vl, fc2);
+                    const dfl d = dfl_add(q, dfl_mul(t1, c2));
+                    const dfl hd = dfl_mul(c, dfl_add(t1, fc2));
+                    const dfl r = dfl_add(fl, dfl_neg(c));
+                    const dfl id = dfl_div(dfl{1.f, 0.f}, d);
+                    const dfl rid = dfl_mul(r, id);
+                    const dfl e_ = dfl_mul(hd, id);
+                    const dfl w1 = dfl_add(dfl{1.f, 0.f}, dfl_mul(rid, hd));
+                    const dfl g = dfl_add(e_, dfl_neg(dfl_mul(rid, w1)));
+                    const dfl gj = dfl_mul(g, mc);
+                    ga = dfl_add(ga, gj);
+                    gb = dfl_add(gb, dfl_mul(gj, x));
+                    // Hessian from the leading parts
+                    const float h2 = fmaf(5.f * fi.hi, c2.hi, t1.hi);
+                    const float hh = fmaf(h2, fmaf(-rid.hi, rid.hi, id.hi), id.hi) +
+                                     e_.hi * fmaf(4.f * rid.hi, w1.hi, -2.f * e_.hi);
+                    const float hj = hh * mc.hi * mc.hi;
+                    haa += hj;
+                    hab = fmaf(hj, x.hi, hab);
+                    hbb = fmaf(hj * x.hi, x.hi, hbb);
+                }
+                ga = warp_sum_dfl(ga);
+                gb = warp_sum_dfl(gb);
+#pragma unroll
+                for (int o = 16; o > 0; o >>= 1) {
+                    haa += __shfl_xor_sync(0xffffffffu, haa, o);
+                    hab += __shfl_xor_sync(0xffffffffu, hab, o);
+                    hbb += __shfl_xor_sync(0xffffffffu, hbb, o);
+                }
+                // half-derivatives: the factors 2 cancel in the Newton step
+                h3 = 2.f * haa;
+                h4 = 2.f * hab;
+                h5 = 2.f * hbb;
+                const float g1 = 2.f * (ga.hi + ga.lo), g2 = 2.f * (gb.hi + gb.lo);
+                float da, db;
+                if (m.order == 0) {
+                    if (!(h3 > 0.f)) break;
+                    da = -g1 / h3;
+                    db = 0.f;
+                } else {
+                    const float det = diff_prod(h3, h5, h4, h4);
+                    if (!(det > 0.f && h3 > 0.f)) break;
+                    da = -diff_prod(h5, g1, h4, g2) / det;
+                    db = -diff_prod(h3, g2, h4, g1) / det;
+                }
+                if (!isfinite(da) || !isfinite(db)) break;
+                a = dfl_add(a, dfl{da, 0.f});
+                b = dfl_add(b, dfl{db, 0.f});
+                const float ref = fmaxf(1.f, fmaxf(fabsf(a.hi), fabsf(b.hi)));
+                if (fabsf(da) <= 1e-11f * ref && fabsf(db) <= 1e-11f * ref) {
+                    converged = true;
+                    ++it;
+                    break;
+                }
+            }
+            // chi2 and the continuum at the solution
+            dfl chi = {0.f, 0.f};
+            bool negative = false, all_zero = true;
+            for (int k = 0; k < nk; ++k) {
+                const int p = lane + 32 * k;
+                if (p >= n) continue;
+                const float4 *e = slab + 3 * (k * 32 + lane);
+                const float4 e0 = e[0];
+                const dfl mc = {e0.x, e0.y}, x = {e0.z, e0.w};
+                const dfl c = dfl_mul(mc, dfl_add(a, dfl_mul(b, x)));
+                if ((valid >> k) & 1u) {
+                    const float4 e1 = e[1], e2 = e[2];
+                    const dfl fl = {e1.x, e1.y}, q = {e1.z, e1.w};
+                    const dfl vl = {e2.x, e2.y}, fi = {e2.z, e2.w};
+                    const dfl c2 = dfl_mul(c, c);
+                    const dfl d = dfl_add(q, dfl_mul(dfl_add(vl, dfl_mul(fi, c2)), c2));
+                    const dfl r = dfl_add(fl, dfl_neg(c));
+                    const dfl term = dfl_div(dfl_mul(r, r), d);
+                    chi = dfl_add(chi, term);
+                    if (!const_w) chi = dfl_add(chi, dfl_fast(logf(d.hi), d.lo / d.hi));
+                }
+                if (out.continuum) out.continuum[off + p] = dfl_to_f64(c);
+                negative |= c.hi < 0.f;
+                all_zero &= c.hi == 0.f;
+            }
+            chi = warp_sum_dfl(chi);
+            negative = __any_sync(0xffffffffu, negative);
+            all_zero = __all_sync(0xffffffffu, all_zero);
+            if (lane == 0) {
+                int status = converged ? 0 : 1;
+                if (negative) status = 2;
+                if (all_zero) status = 3;
+                const bool keep = status == 0;
+                out.zero_point[f] = keep ? dfl_to_f64(a) : NAN;
+                out.slope[f] = keep ? dfl_to_f64(b) : NAN;
+                out.chi2[f] = keep ? dfl_to_f64(chi) : NAN;
+                out.status[f] = status;
+                out.iterations[f] += it;
+                atomicAdd(&scratch->work_items, 1ull);
+            }
+        }
+    }
+}
+
 // Histograms of one Dr16 iteration. Persistent blocks (one warp per forest,
 // pixels across lanes, forests drawn kStackGroup at a time from the work
 // counter) accumulate the rest-frame mean continuum, the observed-frame stack
@@ -1487,7 +1743,7 @@ __global__ void __launch_bounds__(kStackBlock) cont_stacks_kernel(
                 const dfl L = dfl_of(ll), F = dfl_of(sp.flux[off + p]);
                 const dfl C = dfl_of(fit.continuum[off + p]);
                 const dfl IV = dfl_of(iv64);
-                const bool has_iv = iv64 > 0;
+                const bool has_iv = IV.hi > 0.f;
                 // observed-frame bin (stack, variance-function table)
                 int jobs = -1;
                 if (do_stack || use_table) {
@@ -1813,7 +2069,24 @@ int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *
     cont_fit_long_kernel<<<(unsigned)(long_blocks < 1 ? 1 : long_blocks), 32 * kLongWarps,
                            long_smem, stream>>>(sp, m, start, index, count, long_iter,
                                                 cert_chi2 > 0.f ? 1e-10 : tol, out, scratch);
-    return check_cuda(cudaGetLastError());
+    err = cudaGetLastError();
+    if (err != cudaSuccess) return check_cuda(err);
+    if (mode == PG_FIT_MIXED && max_iter > 0 && !(cert_chi2 > 0.f)) {
+        // the two-float finish of the forests flagged status 4, same stream
+        const size_t rsmem = refine_smem_bytes(m.num_mean_cont, m.num_var_intervals);
+        if (rsmem > 200 * 1024) return PG_ERR_UNSUPPORTED;
+        err = cudaFuncSetAttribute(cont_fit_refine_kernel,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
+        if (err != cudaSuccess) return check_cuda(err);
+        int64_t rblocks = (count + 32 * 32 * kRefineWarps - 1) / (32 * 32 * kRefineWarps);
+        if (rblocks > (int64_t)num_sms * 8) rblocks = (int64_t)num_sms * 8;
+        // at least one block per SM: the flagged forests are scattered
+        if (rblocks < num_sms) rblocks = num_sms;
+        cont_fit_refine_kernel<<<(unsigned)rblocks, 32 * kRefineWarps, rsmem, stream>>>(
+            sp, m, index, count, out, scratch);
+        err = cudaGetLastError();
+    }
+    return check_cuda(err);
 }
 
 int launch_cont_stacks(const pg_spectra &sp, const pg_cont_model &m, const pg_cont_fit &fit,
