@@ -381,19 +381,15 @@ class Dr16Gpu:
             self.log_lambda_var_func_grid)
         fudge = interp1d(self.var_x, self.fudge, kind="cubic", fill_value="extrapolate")(
             self.log_lambda_var_func_grid)
-        npix_bin = np.zeros(nvb)
-        valid = np.zeros(nvb, bool)
-        for index in range(nvb):
-            sl = slice(index * NUM_VAR_BINS, (index + 1) * NUM_VAR_BINS)
-            npix_bin[index] = num_pixels[sl].sum()
-            sol = fit_var_bin(var_delta[sl], var2_delta[sl], num_qso[sl], var_pipe_values,
-                              self.min_num_qso_in_fit, self.limit_eta, self.limit_var_lss,
-                              (eta[index], vlss[index], fudge[index] / FUDGE_REF))
-            if sol is None:
-                eta[index], vlss[index], fudge[index] = ETA_DEFAULT, VAR_LSS_DEFAULT, FUDGE_DEFAULT
-            else:
-                eta[index], vlss[index], fudge[index] = sol
-                valid[index] = True
+        shape = (nvb, NUM_VAR_BINS)
+        npix_bin = num_pixels.reshape(shape).sum(axis=1)
+        sols, failed = fit_var_bins(
+            var_delta.reshape(shape), var2_delta.reshape(shape), num_qso.reshape(shape),
+            var_pipe_values, self.min_num_qso_in_fit, self.limit_eta, self.limit_var_lss,
+            np.stack([eta, vlss, fudge / FUDGE_REF], axis=1))
+        eta, vlss, fudge = sols[:, 0].copy(), sols[:, 1].copy(), sols[:, 2].copy()
+        eta[failed], vlss[failed], fudge[failed] = ETA_DEFAULT, VAR_LSS_DEFAULT, FUDGE_DEFAULT
+        valid = ~failed
         w = npix_bin > 0
         self.var_x = self.log_lambda_var_func_grid[w]
         self.eta, self.var_lss, self.fudge = eta[w], vlss[w], fudge[w]
@@ -491,36 +487,85 @@ def _faces(limit_eta, limit_var_lss):
     return out
 
 
-def box_lsq3(mat, rhs, limit_eta, limit_var_lss):
-    """Exact minimiser of ||mat x - rhs||^2 over eta in limit_eta, var_lss in
-    limit_var_lss, fudge' >= 0 (three columns). The objective is convex, so
-    its minimum over the box is the least-squares solution of one face (the
-    free variables solved with the others held at their bounds) that lies in
-    the box; every face is solved and the best feasible one kept. Returns
-    None when a face's system is rank deficient (the caller then uses an
-    iterative bounded solver)."""
-    gram = mat.T @ mat
-    mty = mat.T @ rhs
-    best, best_val = None, np.inf
+def box_lsq3_gram(gram, mty, limit_eta, limit_var_lss):
+    """Exact minimisers of x' G x - 2 x' m (the least squares ||A x - y||^2
+    through its Gram matrix G = A'A and m = A'y) over eta in limit_eta,
+    var_lss in limit_var_lss, fudge' >= 0, for a batch of problems
+    (gram [B, 3, 3], mty [B, 3]). The objective is convex, so its minimum over
+    the box is the solution of one face (the free variables solved with the
+    others held at their bounds) that lies in the box; every face is solved
+    for every problem at once and the best feasible one kept. Returns (x
+    [B, 3], ok [B]); ok is False where a face's system is rank deficient (the
+    caller then uses an iterative bounded solver)."""
+    gram = np.asarray(gram, dtype=np.float64)
+    mty = np.asarray(mty, dtype=np.float64)
+    nb = gram.shape[0]
     lo = np.array([limit_eta[0], limit_var_lss[0], 0.0])
     hi = np.array([limit_eta[1], limit_var_lss[1], np.inf])
+    best = np.zeros((nb, 3))
+    best_val = np.full(nb, np.inf)
+    ok = np.ones(nb, bool)
     for face in _faces(limit_eta, limit_var_lss):
-        x = np.array([0.0 if b is None else b for b in face])
+        x = np.tile(np.array([0.0 if b is None else b for b in face]), (nb, 1))
         free = [k for k in range(3) if face[k] is None]
+        feasible = np.ones(nb, bool)
         if free:
             fixed = [k for k in range(3) if face[k] is not None]
-            sub = gram[np.ix_(free, free)]
-            if np.linalg.matrix_rank(sub) < len(free):
-                return None
-            r = mty[free] - (gram[np.ix_(free, fixed)] @ x[fixed] if fixed else 0.0)
-            x[free] = np.linalg.solve(sub, r)
-            if np.any(x[free] < lo[free] - 1e-15) or np.any(x[free] > hi[free] + 1e-15):
-                continue
-        res = mat @ x - rhs
-        val = float(res @ res)
-        if val < best_val:
-            best, best_val = x, val
-    return best
+            sub = gram[:, free][:, :, free]
+            eig = np.linalg.eigvalsh(sub)
+            # numpy.linalg.matrix_rank's tolerance on the (symmetric) Gram block
+            rank = (eig > eig.max(axis=1, keepdims=True) * len(free) *
+                    np.finfo(np.float64).eps).sum(axis=1)
+            ok &= rank == len(free)
+            r = mty[:, free]
+            if fixed:
+                r = r - np.einsum("bij,j->bi", gram[:, free][:, :, fixed], x[0, fixed])
+            safe = np.where((rank == len(free))[:, None, None], sub, np.eye(len(free)))
+            x[:, free] = np.linalg.solve(safe, r[..., None])[..., 0]
+            feasible = (np.all(x[:, free] >= lo[free] - 1e-15, axis=1) &
+                        np.all(x[:, free] <= hi[free] + 1e-15, axis=1))
+        val = np.einsum("bi,bij,bj->b", x, gram, x) - 2 * np.einsum("bi,bi->b", x, mty)
+        take = feasible & (val < best_val)
+        best[take] = x[take]
+        best_val[take] = val[take]
+    return best, ok
+
+
+def box_lsq3(mat, rhs, limit_eta, limit_var_lss):
+    """box_lsq3_gram for one problem given as (A, y); None when a face's
+    system is rank deficient."""
+    x, ok = box_lsq3_gram((mat.T @ mat)[None], (mat.T @ rhs)[None], limit_eta, limit_var_lss)
+    return x[0] if ok[0] else None
+
+
+def fit_var_bins(var_delta, var2_delta, num_qso, var_pipe_values, min_num_qso, limit_eta,
+                 limit_var_lss, start):
+    """(eta, var_lss, fudge) of every wavelength bin at once (arrays
+    [bins, NUM_VAR_BINS]; start [bins, 3] with fudge / FUDGE_REF): the
+    batched form of fit_var_bin. Returns [bins, 3] (fudge in its own units)
+    and a mask of the bins whose fit failed."""
+    sel = (num_qso > min_num_qso) & (var2_delta > 0)
+    wsq = np.where(sel, 1.0 / np.where(sel, var2_delta, 1.0), 0.0)  # wgt^2
+    cols = np.stack([var_pipe_values, np.ones_like(var_pipe_values),
+                     FUDGE_REF / var_pipe_values], axis=1)
+    gram = np.einsum("bi,ij,ik->bjk", wsq, cols, cols)
+    mty = np.einsum("bi,ij->bj", wsq * np.where(sel, var_delta, 0.0), cols)
+    x, ok = box_lsq3_gram(gram, mty, limit_eta, limit_var_lss)
+    out = np.array(x)
+    failed = np.zeros(len(out), bool)
+    for b in range(len(out)):
+        if not sel[b].any():
+            # flat chi2: the minimiser stays at its starting point
+            out[b] = start[b]
+        elif not ok[b]:
+            sol = fit_var_bin(var_delta[b], var2_delta[b], num_qso[b], var_pipe_values,
+                              min_num_qso, limit_eta, limit_var_lss, start[b])
+            if sol is None:
+                failed[b] = True
+            else:
+                out[b] = (sol[0], sol[1], sol[2] / FUDGE_REF)
+    out[:, 2] *= FUDGE_REF
+    return out, failed
 
 
 def fit_var_bin(var_delta, var2_delta, num_qso, var_pipe_values, min_num_qso, limit_eta,

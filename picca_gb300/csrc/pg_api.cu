@@ -492,7 +492,9 @@ int pg_mlp_features(pg_plan *plan, const pg_spectra *spectra, const pg_cont_mode
     if ((rc = select_device(plan))) return rc;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
     plan->last_stream = st;
-    return launch_mlp_features(*spectra, *model, features, feat_stride, a0, plan->num_sms, st);
+    if ((rc = reset_scratch(plan, st))) return rc;
+    return launch_mlp_features(*spectra, *model, features, feat_stride, a0, scratch_of(plan),
+                               plan->num_sms, st);
 }
 
 int pg_xcf_dmat_work_bytes(pg_plan *plan, const pg_corr_params *params,

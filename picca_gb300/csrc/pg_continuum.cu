@@ -546,90 +546,12 @@ __global__ void __launch_bounds__(32 * kLongWarps) cont_fit_long_kernel(
 // relative). The reported chi2 sums the FP32 terms with compensation; the
 // continuum is (b x + a) mc in FP32, stored as FP64.
 // ---------------------------------------------------------------------------
-struct MixedTables {
-    const double *mcx_d;
-    const float *mcx_f, *mcy_f, *slope_f;
-    const float *brk_f, *coef_f;  // coef_f: eta, var_lss, fudge, each [4][m]
-    int nmc, m;
-};
-
-__host__ __device__ inline size_t mixed_smem_bytes(int nmc, int m) {
-    return (size_t)nmc * 8 + (size_t)nmc * 12 + (size_t)(m + 1) * 4 + (size_t)12 * m * 4 + 16;
-}
-
-__device__ MixedTables load_tables(const pg_cont_model &m, unsigned char *smem) {
-    MixedTables t;
-    const int nmc = m.num_mean_cont, mi = m.num_var_intervals;
-    double *mcx_d = reinterpret_cast<double *>(smem);
-    float *mcx_f = reinterpret_cast<float *>(mcx_d + nmc);
-    float *mcy_f = mcx_f + nmc;
-    float *slope_f = mcy_f + nmc;
-    float *brk_f = slope_f + nmc;
-    float *coef_f = brk_f + mi + 1;
-    for (int i = threadIdx.x; i < nmc; i += blockDim.x) {
-        const double x = m.mean_cont_x[i], y = m.mean_cont_y[i];
-        mcx_d[i] = x;
-        mcx_f[i] = (float)x;
-        mcy_f[i] = (float)y;
-        slope_f[i] = i + 1 < nmc ? (float)((m.mean_cont_y[i + 1] - y) / (m.mean_cont_x[i + 1] - x))
-                                 : 0.f;
-    }
-    if (!m.use_constant_weight) {
-        for (int i = threadIdx.x; i <= mi; i += blockDim.x) brk_f[i] = (float)m.var_breaks[i];
-        for (int i = threadIdx.x; i < 4 * mi; i += blockDim.x) {
-            coef_f[i] = (float)m.eta_coef[i];
-            coef_f[4 * mi + i] = (float)m.var_lss_coef[i];
-            coef_f[8 * mi + i] = (float)m.fudge_coef[i];
-        }
-    }
-    __syncthreads();
-    t.mcx_d = mcx_d; t.mcx_f = mcx_f; t.mcy_f = mcy_f; t.slope_f = slope_f;
-    t.brk_f = brk_f; t.coef_f = coef_f; t.nmc = nmc; t.m = mi;
-    return t;
-}
-
-// Linear interpolation with extrapolation (interp_linear) searched in FP32;
-// v - x_lo is formed in FP64. Next to a node the FP32 search may pick the
-// neighbouring interval, which changes the value by (slope difference) x
-// (FP32 rounding of v), far below the FP32 rounding of the result.
-__device__ __forceinline__ float interp_mc(const MixedTables &t, double v) {
-    const float vf = (float)v;
-    int lo = 0, hi = t.nmc;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (t.mcx_f[mid] < vf) lo = mid + 1;
-        else hi = mid;
-    }
-    const int idx = lo < 1 ? 1 : (lo > t.nmc - 1 ? t.nmc - 1 : lo);
-    const float dv = (float)(v - t.mcx_d[idx - 1]);
-    return t.slope_f[idx - 1] * dv + t.mcy_f[idx - 1];
-}
-
-__device__ __forceinline__ float ppoly_f(const float *brk, const float *coef, int m, float v) {
-    int lo = 0, hi = m + 1;
-    while (lo < hi) {
-        const int mid = (lo + hi) >> 1;
-        if (brk[mid] <= v) lo = mid + 1;
-        else hi = mid;
-    }
-    int i = lo - 1;
-    i = i < 0 ? 0 : (i > m - 1 ? m - 1 : i);
-    const float dx = v - brk[i];
-    return ((coef[i] * dx + coef[m + i]) * dx + coef[2 * m + i]) * dx + coef[3 * m + i];
-}
-
 __device__ __forceinline__ float warp_sum_f(float v) {
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     return v;
 }
 
-__device__ __forceinline__ void eval_all_f(const PixelTerms<float> &px, float a, float b,
-                                           bool const_w, float s[6]) {
-    lane_terms<float, float, float, float>(px, a, b, const_w, s);
-#pragma unroll
-    for (int k = 0; k < 6; ++k) s[k] = warp_sum_f(s[k]);
-}
 
 // ---- FP64 inputs on the integer pipe -------------------------------------
 // GB300's FP64 pipe is narrow (1/64 of FP32). The mixed fit converts its FP64
@@ -679,6 +601,10 @@ __device__ __forceinline__ double f32_to_f64(float x) {
     const unsigned hw_s = sign | 0x7FF00000u | ((u & 0x7FFFFFu) >> 3);  // inf, NaN
     const unsigned hw = ex == 0u ? sign : (ex == 0xFFu ? hw_s : hw_n);
     return __hiloint2double((int)hw, ex == 0u ? 0 : (int)(u << 29));
+}
+
+__device__ __forceinline__ void prefetch_l2(const void *p) {
+    asm volatile("prefetch.global.L2 [%0];" ::"l"(p));
 }
 
 // a b - c d with one rounding's accuracy (Kahan's difference of products)
@@ -963,9 +889,20 @@ __global__ void __launch_bounds__(kContBlock, 4) cont_fit_mixed_kernel(
             const float lmh = slots[j].lm_hi;
             const float lml = slots[j].lm_lo;
             const int nk = (n + 31) >> 5;
+            if (j + 1 < kFitGroup && slots[j + 1].f >= 0) {
+                // the group's next forest into L2 while this one is fitted
+                const int64_t noff = slots[j + 1].off;
+                const int nn = slots[j + 1].n < 32 * kContK ? slots[j + 1].n : 32 * kContK;
+                for (int p = lane; p < nn; p += 32) {
+                    prefetch_l2(sp.log_lambda + noff + p);
+                    prefetch_l2(sp.flux + noff + p);
+                    prefetch_l2(sp.ivar + noff + p);
+                    prefetch_l2(sp.transmission_correction + noff + p);
+                }
+            }
             unsigned valid = 0;
             float sfi = 0.f, si = 0.f;
-#pragma unroll 1
+#pragma unroll 2
             for (int k = 0; k < nk; ++k) {
                 float4 pa = make_float4(0.f, 0.f, 0.f, 1.f);
                 float2 pb = make_float2(0.f, 0.f);
@@ -1945,74 +1882,88 @@ __global__ void __launch_bounds__(kContBlock) cont_deltas_kernel(
 constexpr int kFeatBins = 64;
 
 // Warm-start network inputs (see pg_mlp_features in include/picca_gb300.h).
-// FP32 per pixel (the features are rounded to BF16): the mean continuum is
-// interpolated from the shared-memory tables of the mixed fit, with the
-// rest-frame coordinate's close-operand differences formed in FP64.
+// FP32 per pixel (the features are rounded to BF16) with the mixed fit's
+// integer-pipe conversions and tables: the rest-frame coordinate is formed
+// as L - Lmin from two-float parts, log10(1 + z) by the lanes of a group of
+// forests in parallel.
 __global__ void __launch_bounds__(kContBlock) mlp_features_kernel(
     const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model m,
-    __nv_bfloat16 *__restrict__ feat, int stride, double *__restrict__ a0_out) {
+    __nv_bfloat16 *__restrict__ feat, int stride, double *__restrict__ a0_out, Scratch *scratch) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ float sums[kContBlock / 32][2][kFeatBins];
-    const MixedTables tab = load_tables(m, smem);
+    __shared__ float s_lm[kContBlock / 32][kFitGroup][2];
+    const FitTables tab = load_fit_tables(m, smem);
     const int lane = threadIdx.x & 31;
     const int wib = threadIdx.x >> 5;
-    const int64_t warp_global = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int64_t nwarps = ((int64_t)gridDim.x * blockDim.x) >> 5;
     const float bins_per_span =
         (float)(kFeatBins / (m.log_lambda_rest_max - m.log_lambda_rest_min));
-    for (int64_t f = warp_global; f < sp.num; f += nwarps) {
-        for (int k = lane; k < kFeatBins; k += 32) {
-            sums[wib][0][k] = 0.f;
-            sums[wib][1][k] = 0.f;
+    const int64_t num_groups = (sp.num + kFitGroup - 1) / kFitGroup;
+    for (;;) {
+        int64_t group = 0;
+        if (lane == 0) group = atomicAdd(&scratch->work_counter, 1);
+        group = __shfl_sync(0xffffffffu, group, 0);
+        if (group >= num_groups) break;
+        if (lane < kFitGroup && group * kFitGroup + lane < sp.num) {
+            const int64_t f = group * kFitGroup + lane;
+            const float2 lm = split_f64(m.log_lambda_rest_min + log10(1. + sp.z_qso[f]));
+            s_lm[wib][lane][0] = lm.x;
+            s_lm[wib][lane][1] = lm.y;
         }
         __syncwarp();
-        const int64_t off = sp.pix_offset[f];
-        const int64_t n = sp.pix_offset[f + 1] - off;
-        double zp1 = 0.;
-        if (lane == 0) zp1 = log10(1 + sp.z_qso[f]);
-        zp1 = __shfl_sync(0xffffffffu, zp1, 0);
-        const double rest0 = zp1 + m.log_lambda_rest_min;
-        float sfi = 0.f, si = 0.f, snr = 0.f, cnt = 0.f;
-        for (int64_t p = lane; p < n; p += 32) {
-            const double ll = sp.log_lambda[off + p];
-            const float fl = (float)sp.flux[off + p];
-            const float iv = (float)sp.ivar[off + p];
-            sfi += fl * iv;
-            si += iv;
-            if (iv > 0.f) {
-                snr += fl * sqrtf(iv);
-                cnt += 1.f;
-                const float mc =
-                    interp_mc(tab, ll - zp1) * (float)sp.transmission_correction[off + p];
-                int bin = (int)floorf((float)(ll - rest0) * bins_per_span);
-                bin = bin < 0 ? 0 : (bin >= kFeatBins ? kFeatBins - 1 : bin);
-                if (mc != 0.f) {
-                    atomicAdd(&sums[wib][0][bin], fl / mc * iv);
-                    atomicAdd(&sums[wib][1][bin], iv);
+        for (int j = 0; j < kFitGroup; ++j) {
+            const int64_t f = group * kFitGroup + j;
+            if (f >= sp.num) break;
+            for (int k = lane; k < kFeatBins; k += 32) {
+                sums[wib][0][k] = 0.f;
+                sums[wib][1][k] = 0.f;
+            }
+            __syncwarp();
+            const int64_t off = sp.pix_offset[f];
+            const int64_t n = sp.pix_offset[f + 1] - off;
+            const float lmh = s_lm[wib][j][0], lml = s_lm[wib][j][1];
+            float sfi = 0.f, si = 0.f, snr = 0.f, cnt = 0.f;
+            for (int64_t p = lane; p < n; p += 32) {
+                const float fl = f64_to_f32(sp.flux[off + p]);
+                const float iv = f64_to_f32(sp.ivar[off + p]);
+                sfi = fmaf(fl, iv, sfi);
+                si += iv;
+                if (iv > 0.f) {
+                    snr = fmaf(fl, sqrtf(iv), snr);
+                    cnt += 1.f;
+                    const float2 ll = split_f64(sp.log_lambda[off + p]);
+                    const float u = (ll.x - lmh) + (ll.y - lml);  // L - Lmin
+                    const float mc =
+                        fit_mean_cont(tab, u) * f64_to_f32(sp.transmission_correction[off + p]);
+                    int bin = __float2int_rd(u * bins_per_span);
+                    bin = bin < 0 ? 0 : (bin >= kFeatBins ? kFeatBins - 1 : bin);
+                    if (mc != 0.f) {
+                        atomicAdd(&sums[wib][0][bin], __fdividef(fl, mc) * iv);
+                        atomicAdd(&sums[wib][1][bin], iv);
+                    }
                 }
             }
-        }
-        sfi = warp_sum_f(sfi);
-        si = warp_sum_f(si);
-        snr = warp_sum_f(snr);
-        cnt = warp_sum_f(cnt);
-        __syncwarp();
-        const float a0 = si > 0.f ? sfi / si : 0.f;
-        __nv_bfloat16 *row = feat + f * (int64_t)stride;
-        for (int k = lane; k < stride; k += 32) {
-            float v = 0.f;
-            if (k < kFeatBins) {
-                const float w = sums[wib][1][k];
-                v = (w > 0.f && a0 != 0.f) ? sums[wib][0][k] / w / a0 - 1.f : 0.f;
-            } else if (k == kFeatBins) {
-                v = (float)(sp.z_qso[f] - 3.0);
-            } else if (k == kFeatBins + 1) {
-                v = logf(fmaxf(cnt > 0.f ? snr / cnt : 0.f, 1e-3f));
+            sfi = warp_sum_f(sfi);
+            si = warp_sum_f(si);
+            snr = warp_sum_f(snr);
+            cnt = warp_sum_f(cnt);
+            __syncwarp();
+            const float a0 = si > 0.f ? sfi / si : 0.f;
+            __nv_bfloat16 *row = feat + f * (int64_t)stride;
+            for (int k = lane; k < stride; k += 32) {
+                float v = 0.f;
+                if (k < kFeatBins) {
+                    const float w = sums[wib][1][k];
+                    v = (w > 0.f && a0 != 0.f) ? sums[wib][0][k] / w / a0 - 1.f : 0.f;
+                } else if (k == kFeatBins) {
+                    v = f64_to_f32(sp.z_qso[f]) - 3.f;
+                } else if (k == kFeatBins + 1) {
+                    v = logf(fmaxf(cnt > 0.f ? snr / cnt : 0.f, 1e-3f));
+                }
+                row[k] = __float2bfloat16(v);
             }
-            row[k] = __float2bfloat16(v);
+            if (lane == 0) a0_out[f] = f32_to_f64(a0);
+            __syncwarp();
         }
-        if (lane == 0) a0_out[f] = (double)a0;
-        __syncwarp();
     }
 }
 
@@ -2078,10 +2029,14 @@ int launch_cont_fit(const pg_spectra &sp, const pg_cont_model &m, const double *
         err = cudaFuncSetAttribute(cont_fit_refine_kernel,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)rsmem);
         if (err != cudaSuccess) return check_cuda(err);
-        int64_t rblocks = (count + 32 * 32 * kRefineWarps - 1) / (32 * 32 * kRefineWarps);
-        if (rblocks > (int64_t)num_sms * 8) rblocks = (int64_t)num_sms * 8;
-        // at least one block per SM: the flagged forests are scattered
-        if (rblocks < num_sms) rblocks = num_sms;
+        // every SM filled: the flagged forests are scattered over the list
+        int per_sm = 0;
+        err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cont_fit_refine_kernel,
+                                                            32 * kRefineWarps, rsmem);
+        if (err != cudaSuccess) return check_cuda(err);
+        int64_t rblocks = (int64_t)num_sms * (per_sm > 0 ? per_sm : 1);
+        const int64_t need = (count + 32 * kRefineWarps - 1) / (32 * kRefineWarps);
+        if (rblocks > need) rblocks = need;
         cont_fit_refine_kernel<<<(unsigned)rblocks, 32 * kRefineWarps, rsmem, stream>>>(
             sp, m, index, count, out, scratch);
         err = cudaGetLastError();
@@ -2116,15 +2071,23 @@ int launch_cont_stacks(const pg_spectra &sp, const pg_cont_model &m, const pg_co
 }
 
 int launch_mlp_features(const pg_spectra &sp, const pg_cont_model &m, uint16_t *features,
-                        int stride, double *a0, int num_sms, cudaStream_t stream) {
+                        int stride, double *a0, Scratch *scratch, int num_sms, cudaStream_t stream) {
     if (sp.num <= 0) return PG_OK;
-    const size_t smem = mixed_smem_bytes(m.num_mean_cont, m.num_var_intervals);
+    const size_t smem = fit_smem_bytes(m.num_mean_cont, m.num_var_intervals);
     if (smem > 200 * 1024) return PG_ERR_UNSUPPORTED;
     cudaError_t err = cudaFuncSetAttribute(
         mlp_features_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return check_cuda(err);
-    mlp_features_kernel<<<blocks_for(sp.num, num_sms), kContBlock, smem, stream>>>(
-        sp, m, reinterpret_cast<__nv_bfloat16 *>(features), stride, a0);
+    int per_sm = 0;
+    err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, mlp_features_kernel, kContBlock,
+                                                        smem);
+    if (err != cudaSuccess) return check_cuda(err);
+    const int64_t groups = (sp.num + kFitGroup - 1) / kFitGroup;
+    int64_t blocks = (groups + kContBlock / 32 - 1) / (kContBlock / 32);
+    const int64_t resident = (int64_t)num_sms * (per_sm > 0 ? per_sm : 1);
+    if (blocks > resident) blocks = resident;
+    mlp_features_kernel<<<(unsigned)blocks, kContBlock, smem, stream>>>(
+        sp, m, reinterpret_cast<__nv_bfloat16 *>(features), stride, a0, scratch);
     return check_cuda(cudaGetLastError());
 }
 

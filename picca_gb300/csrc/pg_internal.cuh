@@ -304,6 +304,7 @@ int launch_cont_stacks(const pg_spectra &sp, const pg_cont_model &m, const pg_co
 int launch_cont_deltas(const pg_spectra &sp, const pg_cont_model &m, const pg_cont_fit &fit,
                        double *delta, double *weights, int num_sms, cudaStream_t stream);
 int launch_mlp_features(const pg_spectra &sp, const pg_cont_model &m, uint16_t *features,
-                        int stride, double *a0, int num_sms, cudaStream_t stream);
+                        int stride, double *a0, Scratch *scratch, int num_sms,
+                        cudaStream_t stream);
 
 }  // namespace pg
