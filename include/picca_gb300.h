@@ -406,6 +406,23 @@ int pg_mlp_adam(float *params, const float *grads, float *m1, float *m2, uint16_
 /* bf16 copy of an FP32 array. */
 int pg_mlp_to_bf16(const float *x, uint16_t *y, int64_t n, void *stream);
 
+/* Inference forward pass of the warm-start network (no counterpart in the
+ * reference) as one fused kernel on the 5th-generation tensor cores:
+ * tcgen05.mma BF16 x BF16 -> FP32 with the accumulator in tensor memory,
+ * 128 forests per tile through all four layers on one SM (bias + GELU
+ * epilogues in FP32, hidden activations rounded to BF16 as in
+ * pg_mlp_gemm's forward). pg_mlp_pack writes the BF16 weights of the
+ * 66-256-256-256-2 network (params16: per layer W [fan_in][fan_out] then the
+ * bias, as pg_mlp_to_bf16 makes them) into the operand image the kernel
+ * copies to shared memory (pg_mlp_packed_elems() bf16 elements, 16-byte
+ * aligned); pg_mlp_forward reads x [m, stride] bf16 (stride >= 80, a
+ * multiple of 8, columns 66..79 zero), the FP32 biases from params and
+ * writes y [m, 2] FP32. */
+int64_t pg_mlp_packed_elems(void);
+int pg_mlp_pack(const uint16_t *params16, uint16_t *packed, void *stream);
+int pg_mlp_forward(pg_plan *plan, const uint16_t *packed, const float *params, const uint16_t *x,
+                   int64_t m, int32_t stride, float *y, void *stream);
+
 /* Per-forest input features of the warm-start network: 64 bins of
  * flux / mean continuum over the rest-frame range (ivar-weighted means,
  * divided by the forest's ivar-weighted mean flux a0, minus 1; empty bins

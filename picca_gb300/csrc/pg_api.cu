@@ -484,6 +484,29 @@ int pg_cont_deltas(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model
     return launch_cont_deltas(*spectra, *model, *fit, delta, weights, plan->num_sms, st);
 }
 
+int64_t pg_mlp_packed_elems(void) { return mlp_packed_elems(); }
+
+int pg_mlp_pack(const uint16_t *params16, uint16_t *packed, void *stream) {
+    if (!params16 || !packed) return PG_ERR_INVALID_ARGUMENT;
+    return launch_mlp_pack(params16, packed, static_cast<cudaStream_t>(stream));
+}
+
+int pg_mlp_forward(pg_plan *plan, const uint16_t *packed, const float *params, const uint16_t *x,
+                   int64_t m, int32_t stride, float *y, void *stream) {
+    if (!plan || !packed || !params || !y || m < 0 || (m > 0 && !x)) return PG_ERR_INVALID_ARGUMENT;
+    // rows are read as 16-byte vectors: 80 padded features, 16-byte aligned
+    if (stride < 80 || stride % 8 != 0 || (reinterpret_cast<uintptr_t>(x) & 15u) ||
+        (reinterpret_cast<uintptr_t>(packed) & 15u))
+        return PG_ERR_INVALID_ARGUMENT;
+    int rc;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    if ((rc = reset_scratch(plan, st))) return rc;
+    return launch_mlp_forward_tc(packed, params, x, m, stride, y, scratch_of(plan), plan->num_sms,
+                                 st);
+}
+
 int pg_mlp_features(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
                     uint16_t *features, int32_t feat_stride, double *a0, void *stream) {
     if (!plan || !features || !a0 || feat_stride < 66) return PG_ERR_INVALID_ARGUMENT;

@@ -303,6 +303,11 @@ int launch_cont_stacks(const pg_spectra &sp, const pg_cont_model &m, const pg_co
                        cudaStream_t stream);
 int launch_cont_deltas(const pg_spectra &sp, const pg_cont_model &m, const pg_cont_fit &fit,
                        double *delta, double *weights, int num_sms, cudaStream_t stream);
+int64_t mlp_packed_elems();
+int launch_mlp_pack(const uint16_t *params16, uint16_t *packed, cudaStream_t stream);
+int launch_mlp_forward_tc(const uint16_t *packed, const float *params, const uint16_t *x, int64_t m,
+                          int stride, float *y, Scratch *scratch, int num_sms,
+                          cudaStream_t stream);
 int launch_mlp_features(const pg_spectra &sp, const pg_cont_model &m, uint16_t *features,
                         int stride, double *a0, Scratch *scratch, int num_sms,
                         cudaStream_t stream);

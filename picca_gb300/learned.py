@@ -4,10 +4,11 @@ A 66 -> 256 -> 256 -> 256 -> 2 MLP with GELU activations predicts, from a
 forest's flux divided by the current mean continuum (64 rest-frame bins),
 its redshift and signal-to-noise, the continuum parameters relative to the
 reference starting point a0 (the ivar-weighted mean flux,
-expected_fluxes/utils.py:92): targets (a/a0 - 1, b/a0). Every matrix product
-runs in the library's BF16 tensor-core GEMM with FP32 accumulation (forward
-with fused bias + GELU, backward with fused GELU derivative), and training
-uses the library's Adam kernel on FP32 master weights.
+expected_fluxes/utils.py:92): targets (a/a0 - 1, b/a0). Training runs every
+matrix product in the library's BF16 GEMM with FP32 accumulation (forward
+with fused bias + GELU, backward with fused GELU derivative) and the
+library's Adam kernel on FP32 master weights; inference (the warm start)
+runs the whole network in one fused tcgen05 kernel (pg_mlp_forward).
 
 The plain fit stays the reference: ``warm_fit`` starts the damped Newton
 solver from the prediction with a small iteration budget and re-fits from
@@ -44,8 +45,12 @@ def _bind():
     lib.pg_mlp_to_bf16.argtypes = [vp, vp, i64, vp]
     lib.pg_mlp_features.argtypes = [vp, ctypes.POINTER(continuum.SpectraC),
                                     ctypes.POINTER(continuum.ContModelC), vp, i32, vp, vp]
+    lib.pg_mlp_packed_elems.argtypes = []
+    lib.pg_mlp_packed_elems.restype = ctypes.c_int64
+    lib.pg_mlp_pack.argtypes = [vp, vp, vp]
+    lib.pg_mlp_forward.argtypes = [vp, vp, vp, vp, i64, i32, vp, vp]
     for name in ("pg_mlp_gemm", "pg_mlp_colsum", "pg_mlp_mse_grad", "pg_mlp_adam",
-                 "pg_mlp_to_bf16", "pg_mlp_features"):
+                 "pg_mlp_to_bf16", "pg_mlp_features", "pg_mlp_pack", "pg_mlp_forward"):
         getattr(lib, name).restype = ctypes.c_int
     lib._mlp_bound = True
     return lib
@@ -82,6 +87,11 @@ class WarmStartMLP:
         self.m1 = torch.zeros_like(self.params)
         self.m2 = torch.zeros_like(self.params)
         self.params16 = torch.empty(total, dtype=torch.bfloat16, device=self.device)
+        # the tensor-core operand image of the weights, rebuilt when they change
+        self.packed = torch.empty(int(_bind().pg_mlp_packed_elems()), dtype=torch.bfloat16,
+                                  device=self.device)
+        self._packed_step = -1
+        self._plan = None
         self.step = 0
         self._sync16()
 
@@ -95,6 +105,7 @@ class WarmStartMLP:
         return out
 
     def _sync16(self):
+        self._packed_step = -1
         check(_bind().pg_mlp_to_bf16(self.params.data_ptr(), self.params16.data_ptr(),
                                      self.params.numel(), self._stream()), "to_bf16")
 
@@ -108,6 +119,24 @@ class WarmStartMLP:
                                   _ptr(cf), ldc, beta, self._stream()), "mlp gemm")
 
     # forward ---------------------------------------------------------------
+    def forward_fused(self, x16):
+        """Inference forward pass in one tcgen05 kernel (pg_mlp_forward):
+        x16 bf16 [m, FEATURE_STRIDE] -> FP32 [m, 2]."""
+        lib = _bind()
+        if self._packed_step != self.step:
+            check(lib.pg_mlp_pack(self.params16.data_ptr(), self.packed.data_ptr(),
+                                  self._stream()), "mlp pack")
+            self._packed_step = self.step
+        if self._plan is None:
+            from ._native import Plan
+            self._plan = Plan()
+        m = x16.shape[0]
+        y = torch.empty(m, NUM_OUT, dtype=torch.float32, device=self.device)
+        check(lib.pg_mlp_forward(self._plan.handle, self.packed.data_ptr(), self.params.data_ptr(),
+                                 x16.data_ptr(), m, x16.stride(0), y.data_ptr(), self._stream()),
+              "mlp forward")
+        return y
+
     def forward(self, x16, keep=False):
         """x16: bf16 [m, FEATURE_STRIDE] (first 66 columns used). Returns
         the FP32 output [m, 2] and, with keep=True, the activations."""
@@ -214,8 +243,9 @@ def targets_from_fit(fit, a0):
 
 
 def predict_start(mlp, feat, a0):
-    """Warm start (a, b) per forest, FP64 [num, 2]."""
-    y = mlp.forward(feat).double()
+    """Warm start (a, b) per forest, FP64 [num, 2] (the fused tensor-core
+    forward pass)."""
+    y = mlp.forward_fused(feat).double()
     return torch.stack([a0 * (1.0 + y[:, 0]), a0 * y[:, 1]], dim=1).contiguous()
 
 

@@ -4,7 +4,8 @@
   GELU derivative, column sums, MSE gradient) and Adam against the FP64
   oracle that applies the same BF16 storage rounding; tolerance 1e-2 in
   relative norm (FP32 accumulation and BF16 storage of the outputs), Adam
-  to 1e-5 relative.
+  to 1e-5 relative. The fused tcgen05 inference kernel against the GEMM
+  forward (5e-3) and the oracle (1e-2), tails of 1 and 300 rows included.
 * Method: after training on plain fits of one set of forests, the warm-started
   fit of another set reaches the plain fit's optimum ((a, b) within 1e-4,
   chi2 within 1e-6 relative) with fewer Newton iterations than the plain
@@ -70,6 +71,34 @@ def test_forward_backward_adam_match_oracle(cuda):
     net.adam_step(lr=1e-3)
     p_ref, _, _ = om.adam(p0, g0, np.zeros_like(p0), np.zeros_like(p0), 1, lr=1e-3)
     assert np.allclose(net.params.cpu().double().numpy(), p_ref, rtol=1e-5, atol=1e-7)
+
+
+@pytest.mark.parametrize("m", [1, 300, 4096])
+def test_fused_forward_matches_gemm_forward_and_oracle(cuda, m):
+    """The fused tcgen05 inference kernel against the layer-by-layer GEMM
+    forward (same BF16 roundings, FP32 sums in another order: 5e-3 in
+    relative norm) and the FP64 oracle with BF16 storage rounding (1e-2)."""
+    torch = cuda
+    from oracle import mlp as om
+    from picca_gb300 import learned
+    net = learned.WarmStartMLP(seed=5)
+    rng = np.random.default_rng(m)
+    x = np.zeros((m, learned.FEATURE_STRIDE), dtype=np.float32)
+    x[:, :learned.NUM_FEATURES] = rng.normal(0, 0.5, (m, learned.NUM_FEATURES))
+    x16 = torch.tensor(x, device="cuda").bfloat16()
+    fused = net.forward_fused(x16).cpu().numpy()
+    gemm = net.forward(x16).cpu().numpy()
+    assert _rel(fused, gemm) < 5e-3
+    views = net._views(net.params.cpu().double())
+    weights = [(w.numpy().reshape(a, b), bb.numpy()) for (w, bb), (a, b) in
+               zip(views, learned.WarmStartMLP.SHAPES)]
+    y_ref, _ = om.forward(x[:, :learned.NUM_FEATURES].astype(np.float64), weights,
+                          quantize=True)
+    assert _rel(fused, y_ref) < 1e-2
+    # after an optimiser step the operand image is rebuilt
+    net.grads.normal_(0, 1e-2)
+    net.adam_step(lr=1e-2)
+    assert _rel(net.forward_fused(x16).cpu().numpy(), net.forward(x16).cpu().numpy()) < 5e-3
 
 
 def test_warm_start_reaches_plain_optimum_faster(cuda):
