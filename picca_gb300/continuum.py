@@ -16,6 +16,7 @@ expected_flux.py:328-349).
 """
 
 import ctypes
+import hashlib
 
 import numpy as np
 import torch
@@ -195,9 +196,33 @@ class Dr16Gpu:
         self.stack_weight = None
         self.history = []
         self.refined = []  # forests finished in two-float per counted mixed fit
+        self._model_cache = {}
 
     # -- model -------------------------------------------------------------
+    def _model_key(self, with_stack):
+        parts = [self.mean_cont_x, self.mean_cont_y, self.var_x, self.eta, self.var_lss,
+                 self.fudge]
+        if with_stack:
+            parts += [self.stack_x, self.stack_y]
+        h = hashlib.blake2b(digest_size=16)
+        for a in parts:
+            h.update(b"-" if a is None else np.ascontiguousarray(a, dtype=np.float64).tobytes())
+            h.update(b"|")
+        return (with_stack, self.var_lss_mod, self.order, bool(self.use_constant_weight),
+                h.digest())
+
     def _model(self, with_stack=False):
+        """The device model of the current state, rebuilt only when the state
+        (mean continuum, variance functions, stack) changed."""
+        key = self._model_key(with_stack)
+        cached = self._model_cache.get(with_stack)
+        if cached is not None and cached[0] == key:
+            return cached[1], cached[2]
+        model, keep = self._build_model(with_stack)
+        self._model_cache[with_stack] = (key, model, keep)
+        return model, keep
+
+    def _build_model(self, with_stack=False):
         dev = self.device
         keep = {}
         keep["mcx"] = torch.as_tensor(self.mean_cont_x, dtype=torch.float64).to(dev)
