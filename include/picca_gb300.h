@@ -143,6 +143,21 @@ int pg_plan_destroy(pg_plan *plan);
 /* Synchronise the plan's last stream and read its statistics. */
 int pg_plan_stats(pg_plan *plan, pg_run_stats *stats);
 
+/* Launch shapes of the precision-form pair kernels on this plan (no
+ * counterpart in the reference): warps per CTA and CTAs per SM (each CTA
+ * keeps its own shared-memory histogram, so CTAs per SM is the number of
+ * histogram replicas on an SM). 0 selects the default: the most warps the
+ * shared memory allows (20 for pg_cf_xi, 16 for pg_xcf_xi) and as many CTAs
+ * as fit. The results do not depend on the shape beyond the summation order
+ * of the FP32-compensated sums (the pair counts are identical). The
+ * no-allocation entry pg_cf_xi_static always uses the default. */
+typedef struct pg_tuning {
+    int32_t cf_warps, cf_blocks_per_sm;
+    int32_t xcf_warps, xcf_blocks_per_sm;
+} pg_tuning;
+int pg_plan_set_tuning(pg_plan *plan, const pg_tuning *tuning);
+int pg_plan_get_tuning(pg_plan *plan, pg_tuning *tuning);
+
 /* Neighbour lists of every forest of s1 against s2 (s2 == NULL: auto-
  * correlation of s1 with itself, keeping ra1 > ra2 as cf.py:129-135).
  * Two passes: with offsets == NULL write counts[s1->num]; then, with the

@@ -11,6 +11,7 @@ struct pg_plan {
     int num_sms;
     void *scratch;      // pg::Scratch followed by the precision-form constants
     cudaStream_t last_stream;
+    pg_tuning tuning;   // launch shapes of the precision-form pair kernels (0: default)
 };
 
 namespace pg {
@@ -139,6 +140,21 @@ int pg_plan_destroy(pg_plan *plan) {
     return rc;
 }
 
+int pg_plan_set_tuning(pg_plan *plan, const pg_tuning *tuning) {
+    if (!plan || !tuning) return PG_ERR_INVALID_ARGUMENT;
+    if (tuning->cf_warps < 0 || tuning->cf_warps > 32 || tuning->cf_blocks_per_sm < 0 ||
+        tuning->xcf_warps < 0 || tuning->xcf_warps > 32 || tuning->xcf_blocks_per_sm < 0)
+        return PG_ERR_INVALID_ARGUMENT;
+    plan->tuning = *tuning;
+    return PG_OK;
+}
+
+int pg_plan_get_tuning(pg_plan *plan, pg_tuning *tuning) {
+    if (!plan || !tuning) return PG_ERR_INVALID_ARGUMENT;
+    *tuning = plan->tuning;
+    return PG_OK;
+}
+
 int pg_plan_stats(pg_plan *plan, pg_run_stats *stats) {
     if (!plan || !stats) return PG_ERR_INVALID_ARGUMENT;
     int rc = check_cuda(cudaStreamSynchronize(plan->last_stream));
@@ -263,7 +279,8 @@ int pg_cf_xi(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *s
     if (fast)
         return launch_cf_xi_fast(b, params->ang_max, *s1, other, nbr_offsets, nbr_index,
                                  nbr_angle, work_order, num_work, *out, scratch_of(plan),
-                                 fast_const_of(plan), plan->num_sms, st);
+                                 fast_const_of(plan), plan->num_sms, st,
+                                 LaunchTuning{plan->tuning.cf_warps, plan->tuning.cf_blocks_per_sm});
     return launch_cf_xi_fp64(b, *s1, other, nbr_offsets, nbr_index, nbr_angle, work_order,
                              num_work, *out,
                              scratch_of(plan), plan->num_sms, st);
@@ -291,9 +308,10 @@ int pg_xcf_xi(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *
     const bool fast = mode == PG_MODE_FP32_GUARD && !b.rmu && !b.ang_corr &&
                       forests->max_pixels <= 65535;
     if (fast)
-        return launch_xcf_xi_fast(b, params->ang_max, *forests, *objs, nbr_offsets, nbr_index,
-                                  nbr_angle, work_order, num_work, *out, scratch_of(plan),
-                                  fast_const_of(plan), plan->num_sms, st);
+        return launch_xcf_xi_fast(
+            b, params->ang_max, *forests, *objs, nbr_offsets, nbr_index, nbr_angle, work_order,
+            num_work, *out, scratch_of(plan), fast_const_of(plan), plan->num_sms, st,
+            LaunchTuning{plan->tuning.xcf_warps, plan->tuning.xcf_blocks_per_sm});
     return launch_xcf_xi_fp64(b, *forests, *objs, nbr_offsets, nbr_index, nbr_angle, work_order,
                               num_work,
                               *out, scratch_of(plan), plan->num_sms, st);

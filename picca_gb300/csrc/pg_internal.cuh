@@ -203,18 +203,26 @@ int launch_xcf_xi_fp64(const Binning &b, const pg_forest_set &forests, const pg_
                        Scratch *scratch, int num_sms, cudaStream_t stream);
 // Size of the device buffer holding the precision-form constants.
 size_t fast_const_bytes();
+// Launch shape of the precision-form pair kernels: warps per CTA (the CTA
+// size) and CTAs per SM (each CTA holds one copy of the shared histogram);
+// 0 selects the default (the most warps shared memory allows, as many CTAs
+// as fit).
+struct LaunchTuning {
+    int warps = 0;
+    int blocks_per_sm = 0;
+};
 int launch_cf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &s1,
                       const pg_forest_set &s2, const int64_t *nbr_offsets,
                       const int32_t *nbr_index, const double *nbr_angle,
                       const int32_t *work_order, int64_t num_work,
                       const pg_xi_rows &out, Scratch *scratch, void *fast_const, int num_sms,
-                      cudaStream_t stream);
+                      cudaStream_t stream, LaunchTuning tuning = LaunchTuning());
 int launch_xcf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &forests,
                        const pg_forest_set &objs, const int64_t *nbr_offsets,
                        const int32_t *nbr_index, const double *nbr_angle,
                        const int32_t *work_order, int64_t num_work,
                        const pg_xi_rows &out, Scratch *scratch, void *fast_const, int num_sms,
-                       cudaStream_t stream);
+                       cudaStream_t stream, LaunchTuning tuning = LaunchTuning());
 
 // Distortion matrix (pg_dmat.cu). Default number of U and E rows a CTA keeps
 // before the bins of one forest pair are split into chunks.

@@ -957,7 +957,8 @@ FastConst make_fast_const(const Binning &b) {
 __global__ void store_const_kernel(FastConst value, FastConst *dst) { *dst = value; }
 
 template <typename K>
-int persistent_grid(K kernel, int block, size_t smem, int num_sms, int64_t num_work, int *grid) {
+int persistent_grid(K kernel, int block, size_t smem, int num_sms, int64_t num_work, int *grid,
+                    int blocks_per_sm = 0) {
     cudaError_t err = cudaFuncSetAttribute(kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                            (int)smem);
     if (err != cudaSuccess) return check_cuda(err);
@@ -965,6 +966,7 @@ int persistent_grid(K kernel, int block, size_t smem, int num_sms, int64_t num_w
     err = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, block, smem);
     if (err != cudaSuccess) return check_cuda(err);
     if (per_sm < 1) return PG_ERR_UNSUPPORTED;
+    if (blocks_per_sm > 0 && blocks_per_sm < per_sm) per_sm = blocks_per_sm;
     int64_t g = (int64_t)num_sms * per_sm;
     if (g > num_work) g = num_work;
     *grid = (int)(g < 1 ? 1 : g);
@@ -985,12 +987,14 @@ int launch_cf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &s1,
                       const int32_t *nbr_index, const double *nbr_angle,
                       const int32_t *work_order, int64_t num_work,
                       const pg_xi_rows &out, Scratch *scratch, void *fast_const, int num_sms,
-                      cudaStream_t stream) {
+                      cudaStream_t stream, LaunchTuning tuning) {
     if (num_work <= 0) return PG_OK;
     FastConst *fc = static_cast<FastConst *>(fast_const);
     const int max_pix1 = s1.max_pixels;
-    // as many warps (up to kCfBlock / 32) as shared memory leaves room for
+    // as many warps (up to kCfBlock / 32, or the tuned count) as shared
+    // memory leaves room for
     int nwarps = kCfBlock / 32;
+    if (tuning.warps > 0 && tuning.warps < nwarps) nwarps = tuning.warps;
     while (nwarps > 1 && cf_smem(b.nbins, max_pix1, nwarps).total > 227 * 1024) --nwarps;
     const int block = nwarps * 32;
     const size_t smem = cf_smem(b.nbins, max_pix1, nwarps).total;
@@ -1003,7 +1007,8 @@ int launch_cf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &s1,
     const bool lowx = autoc && b.r_par_min == 0.0;
     int grid = 0;
 #define PG_LAUNCH_CF(A, E, L)                                                                  \
-    rc = persistent_grid(cf_xi_diag_kernel<A, E, L>, block, smem, num_sms, num_work, &grid);   \
+    rc = persistent_grid(cf_xi_diag_kernel<A, E, L>, block, smem, num_sms, num_work, &grid,    \
+                         tuning.blocks_per_sm);                                                \
     if (rc) return rc;                                                                         \
     cf_xi_diag_kernel<A, E, L><<<grid, block, smem, stream>>>(b, fc, s1, s2, nbr_offsets,      \
                                                               nbr_index, nbr_angle,            \
@@ -1024,10 +1029,11 @@ int launch_xcf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &fo
                        const int32_t *nbr_index, const double *nbr_angle,
                        const int32_t *work_order, int64_t num_work,
                        const pg_xi_rows &out, Scratch *scratch, void *fast_const, int num_sms,
-                       cudaStream_t stream) {
+                       cudaStream_t stream, LaunchTuning tuning) {
     if (num_work <= 0) return PG_OK;
     FastConst *fc = static_cast<FastConst *>(fast_const);
-    const int block = kXcfBlock;
+    const int block =
+        tuning.warps > 0 && tuning.warps < kXcfBlock / 32 ? tuning.warps * 32 : kXcfBlock;
     const int max_pix1 = forests.max_pixels;
     const size_t smem = smem_layout(b.nbins, max_pix1, block / 32, false).total;
     if (smem > 227 * 1024) return PG_ERR_UNSUPPORTED;
@@ -1037,13 +1043,15 @@ int launch_xcf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &fo
     const bool extra = b.zmin_on || b.zmax_on;
     int grid = 0;
     if (extra) {
-        rc = persistent_grid(xcf_xi_fast_kernel<true>, block, smem, num_sms, num_work, &grid);
+        rc = persistent_grid(xcf_xi_fast_kernel<true>, block, smem, num_sms, num_work, &grid,
+                             tuning.blocks_per_sm);
         if (rc) return rc;
         xcf_xi_fast_kernel<true><<<grid, block, smem, stream>>>(
             b, fc, forests, objs, nbr_offsets, nbr_index, nbr_angle, work_order, num_work, out,
             scratch, max_pix1);
     } else {
-        rc = persistent_grid(xcf_xi_fast_kernel<false>, block, smem, num_sms, num_work, &grid);
+        rc = persistent_grid(xcf_xi_fast_kernel<false>, block, smem, num_sms, num_work, &grid,
+                             tuning.blocks_per_sm);
         if (rc) return rc;
         xcf_xi_fast_kernel<false><<<grid, block, smem, stream>>>(
             b, fc, forests, objs, nbr_offsets, nbr_index, nbr_angle, work_order, num_work, out,

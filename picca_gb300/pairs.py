@@ -316,6 +316,40 @@ class PairEngine:
         return self.last_stats
 
 
+class GraphStep:
+    """One accumulation step (rows zeroed, then the pair kernel with its
+    scratch reset and constants) captured once in a CUDA graph and replayed
+    with a single graph launch. The neighbour lists, work order and rows are
+    the captured buffers: refill them in place between replays (same sizes)
+    to run another step of the same shape. Replays are asynchronous on the
+    current stream."""
+
+    def __init__(self, engine, params, dev1, dev2, offsets, index, order, num_work, rows, mode,
+                 xcf=False):
+        self.engine = engine
+        self._keep = (params, dev1, dev2, offsets, index, order, rows)
+        dev = engine.device
+
+        def step():
+            for r in rows:
+                r.zero_()
+            engine.accumulate(params, dev1, dev2, offsets, index, order, num_work, rows, mode,
+                              xcf=xcf)
+
+        # one eager step first: kernel modules loaded and attributes set
+        # outside the capture
+        step()
+        torch.cuda.synchronize(dev)
+        engine.stats()
+        self.graph = torch.cuda.CUDAGraph()
+        with torch.cuda.device(dev), torch.cuda.graph(self.graph):
+            step()
+        torch.cuda.synchronize(dev)
+
+    def replay(self):
+        self.graph.replay()
+
+
 def rows_to_numpy(rows, num_rows, nbins):
     """Device rows -> numpy (we, xi, rp, rt, z, nb), each [num_rows, nbins]."""
     return [r.view(num_rows, nbins).cpu().numpy() for r in rows]
