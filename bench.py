@@ -69,6 +69,9 @@ def parse():
     p.add_argument("--profile-items", type=int, default=0,
                    help="profiling aid: run the pair kernel once on this many randomly chosen "
                         "work items of the workload and exit (no timing, no JSON line)")
+    p.add_argument("--tune-items", type=int, default=2000,
+                   help="work items the launch-shape tuner and the graph comparison time "
+                        "(0: default launch shape, no graph comparison)")
     p.add_argument("--legs", default="xcf,continuum",
                    help="comma-separated extra legs: xcf, continuum, dmat, wick, delta_io "
                         "(dmat and wick also run alone with --dmat-only / --wick-only)")
@@ -992,6 +995,46 @@ def continuum_leg(args, cpu_seconds):
     }
 
 
+def graph_saving(engine, cparams, dev, offsets, index, order, num_work, num_rows, nbins, mode,
+                 sample_items, reps=5):
+    """Per-step time of the accumulation on a sample of work items launched
+    eagerly (rows zeroed, scratch reset, constants, the kernel) and replayed
+    from a CUDA graph (pairs.GraphStep), CUDA events on the current stream."""
+    from picca_gb300 import pairs
+    gen = torch.Generator(device=order.device).manual_seed(2)
+    n = min(int(sample_items), int(num_work))
+    sub = order[:num_work][torch.randperm(num_work, device=order.device,
+                                          generator=gen)[:n]].contiguous()
+    rows = engine.alloc_rows(num_rows, nbins)
+
+    def timed(fn):
+        out = []
+        for _ in range(reps):
+            a = torch.cuda.Event(enable_timing=True)
+            b = torch.cuda.Event(enable_timing=True)
+            a.record()
+            fn()
+            b.record()
+            torch.cuda.synchronize()
+            out.append(a.elapsed_time(b))
+        return float(np.median(out))
+
+    def eager():
+        for r in rows:
+            r.zero_()
+        engine.accumulate(cparams, dev, None, offsets, index, sub, n, rows, mode)
+
+    eager()
+    eager_ms = timed(eager)
+    g = pairs.GraphStep(engine, cparams, dev, None, offsets, index, sub, n, rows, mode)
+    graph_ms = timed(g.replay)
+    engine.stats()
+    return {"sample_items": n, "eager_ms": eager_ms, "graph_ms": graph_ms,
+            "saving_ms_per_step": eager_ms - graph_ms,
+            "note": "a full step is one long kernel: the launch overhead a graph removes is "
+                    "this saving per step"}
+
+
 def survey_quasars(cfg, fs):
     """Quasar catalogue of a workload: 600k on the 8,000 deg^2 band (75 per
     deg^2, the forests' z law), 1.5 per forest otherwise, same area."""
@@ -1059,6 +1102,17 @@ def xcf_leg(args, fs, ang_max, steps, warmup):
             kern.append((e0, e1))
         return rows, cand, (offsets, index, order, num_work)
 
+    tuning = None
+    if args.tune_items > 0:
+        from picca_gb300 import autotune
+        offsets_t, index_t, total_t = engine.neighbours(params, d1, d2, xcf=True)
+        order_t, num_work_t, _ = engine.work_order(d1, d2, offsets_t, index_t, total_t,
+                                                   xcf=True)
+        tuning = autotune.tune_pairs(engine, params, d1, d2, offsets_t, index_t, order_t,
+                                     num_work_t, nrows, pairs.MODE_FP32_GUARD, xcf=True,
+                                     grid=CONFIGS[args.config][2],
+                                     sample_items=4 * args.tune_items)
+        del offsets_t, index_t, order_t
     for _ in range(warmup):
         step()
     torch.cuda.synchronize()
@@ -1094,6 +1148,7 @@ def xcf_leg(args, fs, ang_max, steps, warmup):
                      "traffic": None, "kernel_ms": kmean * 1e3,
                      "peak_source": f"SMs x 128 FP32 lanes x 2 x sm_max_mhz ({source} peaks file)"},
         "precision_check_vs_fp64_kernel": check,
+        "tuning": tuning,
         "cpu_baseline": {"value": cpu_val, "unit": "pixel-quasar-pairs/s", "cores": cores,
                          "kind": "port", "sample": cpu_desc},
     }
@@ -1282,6 +1337,21 @@ def run_ours(args):
                           "workload": CONFIGS[args.config][3]}), flush=True)
         return
 
+    # launch shape of the pair kernel, tuned on a sample of the work items
+    # (cached per device, bins, grid and mode), and the CUDA-graph replay of
+    # a step on the same sample against its eager launches
+    tuning, graph_info = None, None
+    if mode != pairs.MODE_FP64 and args.tune_items > 0:
+        from picca_gb300 import autotune
+        offsets_t, index_t, total_t = engine.neighbours(cparams, dev)
+        order_t, num_work_t, _ = engine.work_order(dev, None, offsets_t, index_t, total_t)
+        tuning = autotune.tune_pairs(engine, cparams, dev, None, offsets_t, index_t, order_t,
+                                     num_work_t, num_rows, mode, grid=CONFIGS[args.config][2],
+                                     sample_items=args.tune_items)
+        graph_info = graph_saving(engine, cparams, dev, offsets_t, index_t, order_t, num_work_t,
+                                  num_rows, nbins, mode, args.tune_items)
+        del offsets_t, index_t, order_t
+
     for _ in range(args.warmup):
         step()
     torch.cuda.synchronize()
@@ -1415,6 +1485,8 @@ def run_ours(args):
                      "peak_source": f"SMs x 128 FP32 lanes x 2 x sm_max_mhz ({source} peaks file)",
                      "flops_per_launch": flops},
         "precision_check_vs_fp64_kernel": check,
+        "tuning": tuning,
+        "graph": graph_info,
         "rechecked_pairs_last_step": int(stats.rechecked_pairs),
         "evaluated_pixel_pairs_last_step": int(stats.visited_pairs),
         "clocks": clocks,
