@@ -46,3 +46,45 @@ def test_rejects_unknown_option_and_folder_prefix():
         mod.Dr16ExpectedFlux({"not an option": "1"}, grid=object())
     with pytest.raises(mod.ExpectedFluxError):
         mod.Dr16ExpectedFlux({"iter out prefix": "a/b"}, grid=object())
+
+
+def test_plugin_loads_through_picca_class_from_string():
+    """The plugin loaded the way picca's Config loads an expected-flux class
+    (config.py:367-393): ``class_from_string`` with the configured module
+    name, the ExpectedFlux subclass check, and the options and defaults the
+    module exports, in a separate process with the stand-ins of
+    tests/golden/make_golden.py for picca's third-party imports. Needs a picca
+    checkout: PICCA_REFERENCE_PY names its ``py`` directory (skipped
+    otherwise)."""
+    import os
+    import subprocess
+    import sys
+    ref = os.environ.get("PICCA_REFERENCE_PY")
+    if not ref or not os.path.isdir(os.path.join(ref, "picca")):
+        pytest.skip("PICCA_REFERENCE_PY does not name a picca checkout's py directory")
+    here = os.path.dirname(os.path.abspath(__file__))
+    script = f"""
+import sys
+sys.dont_write_bytecode = True
+sys.path.insert(0, {os.path.dirname(here)!r})
+sys.path.insert(0, {os.path.join(here, 'golden')!r})
+import make_golden
+make_golden._install_stand_ins()
+sys.path.insert(0, {ref!r})
+from picca.delta_extraction.utils import class_from_string
+from picca.delta_extraction.expected_flux import ExpectedFlux, accepted_options as base_opts
+import picca.delta_extraction.expected_fluxes.dr16_expected_flux as ref_mod
+cls, defaults, accepted = class_from_string(
+    "Dr16ExpectedFlux", "picca_gb300.delta_extraction.expected_fluxes.dr16_expected_flux")
+assert issubclass(cls, ExpectedFlux), cls.__mro__
+assert cls.__module__ == "picca_gb300.delta_extraction.expected_fluxes.dr16_expected_flux"
+want = set(ref_mod.accepted_options) | set(base_opts)
+assert set(accepted) | set(base_opts) == want, (sorted(accepted), sorted(want))
+for key, value in ref_mod.defaults.items():
+    assert defaults[key] == value, (key, defaults[key], value)
+print("loaded", cls.__name__, len(accepted))
+"""
+    res = subprocess.run([sys.executable, "-c", script], capture_output=True, text=True,
+                         timeout=300)
+    assert res.returncode == 0, res.stderr[-3000:]
+    assert "loaded Dr16ExpectedFlux" in res.stdout
