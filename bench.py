@@ -44,9 +44,12 @@ METRIC = "cf pixel-pairs/s at stated FP64-oracle error; continuum fits/s plain v
 # DRAM bytes (read + write) of the pair kernel per candidate pixel pair, from
 # an ncu capture of the kernel on a sample of work items (profiles/); the
 # roofline entry scales it to the launch by the candidate pairs processed.
-# None until the diagonal-sweep kernel has been captured.
-PAIR_DRAM_BYTES_PER_CANDIDATE = None
-PAIR_TRAFFIC_SOURCE = "not captured for this kernel yet"
+# Captured on 200 random work items of the 400k-forest survey: 1.251 GB for
+# 5.41e9 candidate pixel pairs.
+PAIR_DRAM_BYTES_PER_CANDIDATE = 0.2314
+PAIR_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of cf_xi_diag_kernel "
+                       "on 200 random work items of this survey, scaled by candidate pairs "
+                       "(profiles/cf_xi_diag_kernel_400k_survey_sample.md)")
 
 
 def parse():
@@ -88,6 +91,8 @@ def parse():
                    help="forest rejection of the Wick covariance legs")
     p.add_argument("--wick-only", action="store_true",
                    help="run only the Wick covariance legs (one JSON line)")
+    p.add_argument("--continuum-only", action="store_true",
+                   help="run only the continuum leg (plain and learned fits; one JSON line)")
     p.add_argument("--continuum-correlation", type=int, default=50_000,
                    help="forests whose plain- and learned-fit deltas are correlated (0 skips)")
     return p.parse_args()
@@ -1289,6 +1294,10 @@ def run_ours(args):
             dist.barrier()
         torch.cuda.synchronize()
 
+    if args.continuum_only:
+        if rank == 0:
+            print(json.dumps(continuum_leg(args, args.cpu_seconds)), flush=True)
+        return
     fs, params, ang_max = make_workload(args.config)
     if args.wick_only:
         if rank == 0:
