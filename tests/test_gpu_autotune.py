@@ -3,8 +3,10 @@ replay of a step.
 
 * Every candidate launch shape (warps per CTA, CTAs per SM) of the auto- and
   cross-correlation precision-form kernels gives pair counts identical to the
-  default shape, and the other sums equal to 1e-12 (relative, or of the
-  column's largest value; only the order of the sums changes with the shape).
+  default shape; the weight and xi sums (error-free in the block
+  histograms) equal to 1e-12 and the r_par, r_trans and z sums (plain FP32
+  block sums) to 2e-6, relative or of the column's largest value: only the
+  order of the sums changes with the shape.
 * ``tune_pairs`` picks one of the candidates, caches it, and a second call
   reads the cache without timing.
 * A step captured in a CUDA graph and replayed gives the same rows as the
@@ -67,8 +69,11 @@ def test_every_launch_shape_gives_identical_pair_counts(cuda, xcf):
         got = _run(*work, xcf)
         np.testing.assert_array_equal(got[5], ref[5], err_msg=str(cand))
         for k in range(5):
-            np.testing.assert_allclose(got[k], ref[k], rtol=1e-12,
-                                       atol=1e-12 * np.abs(ref[k]).max(),
+            # weights and xi are summed error-free in the block histograms;
+            # r_par, r_trans and z sums are plain FP32 sums there
+            rtol = 1e-12 if k < 2 else 2e-6
+            np.testing.assert_allclose(got[k], ref[k], rtol=rtol,
+                                       atol=rtol * np.abs(ref[k]).max(),
                                        err_msg=f"{cand} column {k}")
 
 
@@ -103,5 +108,6 @@ def test_graph_replay_matches_eager(cuda):
         got = [r.cpu().numpy() for r in rows]
         np.testing.assert_array_equal(got[5], eager[5])
         for k in range(5):
-            np.testing.assert_allclose(got[k], eager[k], rtol=1e-12,
-                                       atol=1e-12 * np.abs(eager[k]).max())
+            rtol = 1e-12 if k < 2 else 2e-6
+            np.testing.assert_allclose(got[k], eager[k], rtol=rtol,
+                                       atol=rtol * np.abs(eager[k]).max())
