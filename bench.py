@@ -1005,6 +1005,8 @@ def graph_saving(engine, cparams, dev, offsets, index, order, num_work, num_rows
     """Per-step time of the accumulation on a sample of work items launched
     eagerly (rows zeroed, scratch reset, constants, the kernel) and replayed
     from a CUDA graph (pairs.GraphStep), CUDA events on the current stream."""
+    import torch
+
     from picca_gb300 import pairs
     gen = torch.Generator(device=order.device).manual_seed(2)
     n = min(int(sample_items), int(num_work))

@@ -750,7 +750,7 @@ constexpr size_t kFitSlabBytes = (size_t)kContK * 32 * (sizeof(float4) + sizeof(
 // where h' = d2D/dC2 / 2 = vl + 6 fi C^2. Without want_val (the Newton
 // iterations near the optimum) the reciprocal is the approximate one (two
 // ulps) and chi2 itself is not formed.
-__device__ __forceinline__ void fit_terms(const FitSlab &px, int lane, int nk, float a, float b,
+__device__ __noinline__ void fit_terms(const FitSlab &px, int lane, int nk, float a, float b,
                                           bool const_w, bool want_val, float s[6]) {
     float val = 0.f, ga = 0.f, gb = 0.f, haa = 0.f, hab = 0.f, hbb = 0.f;
 #pragma unroll 1
