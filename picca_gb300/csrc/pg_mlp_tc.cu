@@ -2,14 +2,16 @@
 // network as one fused Blackwell kernel (no counterpart in the reference;
 // see include/picca_gb300.h).
 //
-// A persistent CTA (8 warps) takes 128 forests at a time through all four
+// A persistent CTA (16 warps) takes 128 forests at a time through all four
 // layers without leaving the SM: the feature tile and each hidden activation
 // live in shared memory as the A operand of tcgen05.mma (BF16 x BF16 -> FP32,
 // M = 128, N = 256, K = 16 per instruction, issued by one thread), the
 // accumulator lives in tensor memory (256 columns), and the epilogue (bias,
 // GELU, BF16 rounding) reads it back with tcgen05.ld and writes the next
 // layer's A operand in place. The weights are pre-packed once into the exact
-// shared-memory image of the B operand (pg_mlp_pack) and copied in per layer.
+// shared-memory image of the B operand (pg_mlp_pack) and copied in per layer
+// with asynchronous copies issued as soon as the previous MMAs completed, so
+// that they overlap the epilogue.
 //
 // Operand layout (no swizzle, K-major): 8-row x 16-byte core matrices, row
 // group g and K chunk c at byte (g * KC + c) * 128 with KC = K / 8 chunks, so
@@ -24,7 +26,7 @@
 namespace pg {
 namespace {
 
-constexpr int kTcThreads = 256;  // 8 warps: two per TMEM lane quarter
+constexpr int kTcThreads = 512;  // 16 warps: four per TMEM lane quarter
 constexpr int kTcRows = 128;     // forests per tile (the MMA's M)
 constexpr int kHidden = 256;
 constexpr int kIn = 66, kInPad = 80;  // features, padded to a multiple of 16
@@ -81,6 +83,18 @@ __device__ __forceinline__ void tc_fence_after() {
 
 __device__ __forceinline__ void proxy_fence() {
     asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+}
+
+// 16-byte global -> shared copy through the asynchronous copy path;
+// src_bytes = 0 fills the 16 bytes with zeros (nothing is read)
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gsrc, uint32_t src_bytes) {
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;" ::"r"(smem_u32(smem_dst)),
+                 "l"(gsrc), "r"(src_bytes)
+                 : "memory");
+}
+
+__device__ __forceinline__ void cp_async_wait_all() {
+    asm volatile("cp.async.wait_all;" ::: "memory");
 }
 
 // bounded wait on an mbarrier phase; false when the bound ran out
@@ -198,32 +212,43 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_forward_tc_kernel(
     const uint32_t tmem = s_tmem;
     const uint32_t a_addr = smem_u32(A), w_addr = smem_u32(W);
     const int quarter = warp & 3;  // this warp's TMEM lanes: 32 quarter .. + 31
-    const int half = warp >> 2;    // this warp's half of the 256 columns
+    const int part = warp >> 2;    // this warp's quarter of the 256 columns
     const int row = quarter * 32 + lane;
     const uint32_t t_lane = tmem + ((uint32_t)(quarter * 32) << 16);
     uint32_t parity = 0;
     bool ok = true;
     const int64_t ntiles = (m + kTcRows - 1) / kTcRows;
-    for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
-        const int64_t row0 = tile * kTcRows;
+    // operand copies go through the asynchronous copy path, so that the
+    // copy for the next MMA overlaps the epilogue of the current one
+    auto copy_w = [&](int layer) {
+        const int64_t woff = layer == 0 ? 0 : kPackW1 + (int64_t)(layer - 1) * kPackW2;
+        const int64_t welems = layer == 0 ? kPackW1 : (layer == 3 ? kPackW4 : kPackW2);
+        const uint4 *src = packed + woff / 8;
+        for (int64_t e = tid; e < welems / 8; e += kTcThreads)
+            cp_async16(reinterpret_cast<uint4 *>(W) + e, src + e, 16u);
+    };
+    auto copy_x = [&](int64_t row0) {
         // features -> A (K = 80: 10 chunks per row), rows past m zero
         for (int e = tid; e < kTcRows * (kInPad / 8); e += kTcThreads) {
             const int r = e / (kInPad / 8), c = e % (kInPad / 8);
-            uint4 v = make_uint4(0u, 0u, 0u, 0u);
-            if (row0 + r < m) v = *reinterpret_cast<const uint4 *>(x + (row0 + r) * stride + 8 * c);
-            *reinterpret_cast<uint4 *>(A + img_off(r, c, kInPad / 8)) = v;
+            const bool in = row0 + r < m;
+            cp_async16(A + img_off(r, c, kInPad / 8), in ? x + (row0 + r) * stride + 8 * c : x,
+                       in ? 16u : 0u);
         }
+    };
+    if ((int64_t)blockIdx.x < ntiles) {
+        copy_x((int64_t)blockIdx.x * kTcRows);
+        copy_w(0);
+    }
+    cp_async_wait_all();
+    proxy_fence();
+    tc_fence_before();
+    __syncthreads();
+    for (int64_t tile = blockIdx.x; tile < ntiles && ok; tile += gridDim.x) {
+        const int64_t row0 = tile * kTcRows;
         for (int layer = 0; layer < 4; ++layer) {
             const int kc = layer == 0 ? kInPad / 8 : kHidden / 8;
             const int n = layer == 3 ? kOutPad : kHidden;
-            const int64_t woff = layer == 0 ? 0 : kPackW1 + (int64_t)(layer - 1) * kPackW2;
-            const int64_t welems = layer == 0 ? kPackW1 : (layer == 3 ? kPackW4 : kPackW2);
-            const uint4 *src = packed + woff / 8;
-            for (int64_t e = tid; e < welems / 8; e += kTcThreads)
-                reinterpret_cast<uint4 *>(W)[e] = src[e];
-            proxy_fence();
-            tc_fence_before();
-            __syncthreads();
             if (tid == 0) {
                 tc_fence_after();
                 const uint32_t idesc = tc_idesc(kTcRows, n);
@@ -237,12 +262,21 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_forward_tc_kernel(
             parity ^= 1u;
             tc_fence_after();
             if (!ok) break;
+            // both operands are free once the MMAs completed: start the copies
+            // of the next layer's weights (or of the next tile's features and
+            // first weights) under the epilogue
+            if (layer < 3) {
+                copy_w(layer + 1);
+            } else if (tile + gridDim.x < ntiles) {
+                copy_x((tile + gridDim.x) * kTcRows);
+                copy_w(0);
+            }
             if (layer < 3) {
                 // bias + GELU, rounded to BF16 into A: the next layer's input
                 const float *bias = s_bias + layer * kHidden;
 #pragma unroll 1
-                for (int j = 0; j < 4; ++j) {
-                    const int col0 = half * 128 + 32 * j;
+                for (int j = 0; j < 2; ++j) {
+                    const int col0 = part * 64 + 32 * j;
                     float v[32];
                     tmem_ld32(t_lane + (uint32_t)col0, v);
 #pragma unroll
@@ -261,7 +295,7 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_forward_tc_kernel(
                             make_uint4(w[0], w[1], w[2], w[3]);
                     }
                 }
-            } else if (half == 0) {
+            } else if (part == 0) {
                 float v[32];
                 tmem_ld32(t_lane, v);
                 if (row0 + row < m) {
@@ -269,11 +303,14 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_forward_tc_kernel(
                     y[(row0 + row) * kOut + 1] = v[1] + s_bias[3 * kHidden + 1];
                 }
             }
-            // TMEM reads and the A writes done before the next MMA
+            // copies landed, TMEM reads and A writes done before the next MMA
+            cp_async_wait_all();
+            proxy_fence();
             tc_fence_before();
             __syncthreads();
         }
     }
+    cp_async_wait_all();
     if (!ok && tid == 0) report_error(scratch, PG_ERR_TIMEOUT, 0);
     tc_fence_before();
     __syncthreads();
