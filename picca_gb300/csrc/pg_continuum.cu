@@ -1922,24 +1922,51 @@ __global__ void __launch_bounds__(kContBlock) mlp_features_kernel(
             const int64_t n = sp.pix_offset[f + 1] - off;
             const float lmh = s_lm[wib][j][0], lml = s_lm[wib][j][1];
             float sfi = 0.f, si = 0.f, snr = 0.f, cnt = 0.f;
-            for (int64_t p = lane; p < n; p += 32) {
-                const float fl = f64_to_f32(sp.flux[off + p]);
-                const float iv = f64_to_f32(sp.ivar[off + p]);
-                sfi = fmaf(fl, iv, sfi);
-                si += iv;
-                if (iv > 0.f) {
-                    snr = fmaf(fl, sqrtf(iv), snr);
-                    cnt += 1.f;
-                    const float2 ll = split_f64(sp.log_lambda[off + p]);
-                    const float u = (ll.x - lmh) + (ll.y - lml);  // L - Lmin
-                    const float mc =
-                        fit_mean_cont(tab, u) * f64_to_f32(sp.transmission_correction[off + p]);
-                    int bin = __float2int_rd(u * bins_per_span);
-                    bin = bin < 0 ? 0 : (bin >= kFeatBins ? kFeatBins - 1 : bin);
-                    if (mc != 0.f) {
-                        atomicAdd(&sums[wib][0][bin], __fdividef(fl, mc) * iv);
-                        atomicAdd(&sums[wib][1][bin], iv);
+            for (int64_t base = 0; base < n; base += 32) {
+                const int64_t p = base + lane;
+                int bin = -1;
+                float num = 0.f, den = 0.f;
+                if (p < n) {
+                    const float fl = f64_to_f32(sp.flux[off + p]);
+                    const float iv = f64_to_f32(sp.ivar[off + p]);
+                    sfi = fmaf(fl, iv, sfi);
+                    si += iv;
+                    if (iv > 0.f) {
+                        snr = fmaf(fl, sqrtf(iv), snr);
+                        cnt += 1.f;
+                        const float2 ll = split_f64(sp.log_lambda[off + p]);
+                        const float u = (ll.x - lmh) + (ll.y - lml);  // L - Lmin
+                        const float mc = fit_mean_cont(tab, u) *
+                                         f64_to_f32(sp.transmission_correction[off + p]);
+                        if (mc != 0.f) {
+                            bin = __float2int_rd(u * bins_per_span);
+                            bin = bin < 0 ? 0 : (bin >= kFeatBins ? kFeatBins - 1 : bin);
+                            num = __fdividef(fl, mc) * iv;
+                            den = iv;
+                        }
                     }
+                }
+                // consecutive pixels fall in runs of one bin across the
+                // lanes: a segmented scan over the maximal runs of equal bins
+                // leaves each run's sum at its last lane, which alone adds it
+                // to the bin
+                const int prev = __shfl_up_sync(0xffffffffu, bin, 1);
+                const unsigned heads = __ballot_sync(0xffffffffu, lane == 0 || prev != bin);
+                const unsigned upto = lane == 31 ? 0xffffffffu : ((2u << lane) - 1u);
+                const int start = 31 - __clz(heads & upto);  // first lane of this run
+#pragma unroll
+                for (int o = 1; o < 32; o <<= 1) {
+                    const float tn = __shfl_up_sync(0xffffffffu, num, o);
+                    const float td = __shfl_up_sync(0xffffffffu, den, o);
+                    if (lane - o >= start) {
+                        num += tn;
+                        den += td;
+                    }
+                }
+                const int next = __shfl_down_sync(0xffffffffu, bin, 1);
+                if (bin >= 0 && (lane == 31 || next != bin)) {
+                    atomicAdd(&sums[wib][0][bin], num);
+                    atomicAdd(&sums[wib][1][bin], den);
                 }
             }
             sfi = warp_sum_f(sfi);
