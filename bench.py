@@ -956,6 +956,18 @@ def continuum_leg(args, cpu_seconds):
                                                        (hw["status"] == 0)))})
         eng_c.update_model(spectra, fp, iteration == iters - 1)
         del fp, fw
+    # the learned stage's parts on the final model state: features, and the
+    # network by the fused tcgen05 kernel and by the layer-by-layer GEMMs
+    model_c, keep_c = eng_c._model()
+    (feat, _), feat_s = timed_loop(lambda: learned.features(eng_c, spectra, model_c))
+    net.forward_fused(feat)
+    y_fused, fused_s = timed_loop(lambda: net.forward_fused(feat))
+    y_gemm, gemm_s = timed_loop(lambda: net.forward(feat))
+    parts = {"features_ms": feat_s * 1e3, "network_fused_tcgen05_ms": fused_s * 1e3,
+             "network_layer_gemms_ms": gemm_s * 1e3,
+             "network_fused_vs_gemms_rel_norm": float((y_fused - y_gemm).norm() /
+                                                      y_gemm.norm())}
+    del feat, y_fused, y_gemm, keep_c
     loop_plain = sum(r["plain_ms"] for r in per_iter)
     loop_learned = sum(r["learned_ms"] for r in per_iter)
     same_state = {"per_iteration": per_iter,
@@ -964,7 +976,8 @@ def continuum_leg(args, cpu_seconds):
                   "learned_over_plain": loop_plain / loop_learned,
                   "ab_max_rel": max(r["ab_max_rel"] or 0.0 for r in per_iter),
                   "chi2_excess_max_rel": max(r["chi2_excess_max_rel"] or 0.0 for r in per_iter),
-                  "certificate": {"chi2_tol": learned.CHI2_TOL, "ab_tol": learned.AB_TOL}}
+                  "certificate": {"chi2_tol": learned.CHI2_TOL, "ab_tol": learned.AB_TOL},
+                  "learned_stage_parts": parts}
     del eng_c
 
     nfits = eval_raw.num * iters
