@@ -963,7 +963,9 @@ def continuum_leg(args, cpu_seconds):
     net.forward_fused(feat)
     y_fused, fused_s = timed_loop(lambda: net.forward_fused(feat))
     y_gemm, gemm_s = timed_loop(lambda: net.forward(feat))
-    parts = {"features_ms": feat_s * 1e3, "network_fused_tcgen05_ms": fused_s * 1e3,
+    _, both_s = timed_loop(lambda: net.warm_start(eng_c, spectra, model_c))
+    parts = {"features_and_network_one_kernel_ms": both_s * 1e3,
+             "features_ms": feat_s * 1e3, "network_fused_tcgen05_ms": fused_s * 1e3,
              "network_layer_gemms_ms": gemm_s * 1e3,
              "network_fused_vs_gemms_rel_norm": float((y_fused - y_gemm).norm() /
                                                       y_gemm.norm())}

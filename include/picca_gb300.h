@@ -438,6 +438,15 @@ int pg_mlp_pack(const uint16_t *params16, uint16_t *packed, void *stream);
 int pg_mlp_forward(pg_plan *plan, const uint16_t *packed, const float *params, const uint16_t *x,
                    int64_t m, int32_t stride, float *y, void *stream);
 
+/* pg_mlp_features and pg_mlp_forward in one kernel (no counterpart in the
+ * reference): each tile's features are formed from the spectra and the
+ * current model straight into the tensor-core operand in shared memory
+ * (the same values pg_mlp_features writes), then the network runs on them;
+ * writes y [num, 2] FP32 and a0 [num] FP64. */
+int pg_mlp_warm_start(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
+                      const uint16_t *packed, const float *params, float *y, double *a0,
+                      void *stream);
+
 /* Per-forest input features of the warm-start network: 64 bins of
  * flux / mean continuum over the rest-frame range (ivar-weighted means,
  * divided by the forest's ivar-weighted mean flux a0, minus 1; empty bins

@@ -525,6 +525,21 @@ int pg_mlp_forward(pg_plan *plan, const uint16_t *packed, const float *params, c
                                  st);
 }
 
+int pg_mlp_warm_start(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
+                      const uint16_t *packed, const float *params, float *y, double *a0,
+                      void *stream) {
+    if (!plan || !packed || !params || !y || !a0) return PG_ERR_INVALID_ARGUMENT;
+    if (reinterpret_cast<uintptr_t>(packed) & 15u) return PG_ERR_INVALID_ARGUMENT;
+    int rc;
+    if ((rc = validate_spectra(spectra)) || (rc = validate_model(model))) return rc;
+    if ((rc = select_device(plan))) return rc;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    plan->last_stream = st;
+    if ((rc = reset_scratch(plan, st))) return rc;
+    return launch_mlp_warm_start_tc(*spectra, *model, packed, params, y, a0, scratch_of(plan),
+                                    plan->num_sms, st);
+}
+
 int pg_mlp_features(pg_plan *plan, const pg_spectra *spectra, const pg_cont_model *model,
                     uint16_t *features, int32_t feat_stride, double *a0, void *stream) {
     if (!plan || !features || !a0 || feat_stride < 66) return PG_ERR_INVALID_ARGUMENT;

@@ -316,6 +316,9 @@ int launch_mlp_pack(const uint16_t *params16, uint16_t *packed, cudaStream_t str
 int launch_mlp_forward_tc(const uint16_t *packed, const float *params, const uint16_t *x, int64_t m,
                           int stride, float *y, Scratch *scratch, int num_sms,
                           cudaStream_t stream);
+int launch_mlp_warm_start_tc(const pg_spectra &sp, const pg_cont_model &model,
+                             const uint16_t *packed, const float *params, float *y, double *a0,
+                             Scratch *scratch, int num_sms, cudaStream_t stream);
 int launch_mlp_features(const pg_spectra &sp, const pg_cont_model &m, uint16_t *features,
                         int stride, double *a0, Scratch *scratch, int num_sms,
                         cudaStream_t stream);

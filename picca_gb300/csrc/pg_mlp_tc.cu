@@ -21,6 +21,7 @@
 // bytes in.
 #include <cuda_bf16.h>
 
+#include "pg_cont_common.cuh"
 #include "pg_internal.cuh"
 
 namespace pg {
@@ -173,12 +174,24 @@ __global__ void mlp_pack_kernel(const __nv_bfloat16 *__restrict__ params,
                                        : __float2bfloat16(0.f);
 }
 
+// FEAT = false: the features are read from x [m, stride]. FEAT = true (the
+// warm start in one kernel): each warp forms the features of 8 of the tile's
+// forests from the spectra (forest_feature_sums, the model tables in shared
+// memory after the operand buffers) straight into the A operand, and writes
+// their a0; m = sp.num.
+template <bool FEAT>
 __global__ void __launch_bounds__(kTcThreads, 1) mlp_forward_tc_kernel(
     const __nv_bfloat16 *__restrict__ x, int64_t m, int stride, const uint4 *__restrict__ packed,
-    const float *__restrict__ params, float *__restrict__ y, Scratch *scratch) {
+    const float *__restrict__ params, float *__restrict__ y, Scratch *scratch,
+    const __grid_constant__ pg_spectra sp, const __grid_constant__ pg_cont_model model,
+    double *__restrict__ a0_out) {
     extern __shared__ __align__(1024) unsigned char smem[];
     unsigned char *A = smem;
     unsigned char *W = smem + kTcABytes;
+    __shared__ float s_feat_sums[FEAT ? kTcThreads / 32 : 1][2][kFeatBins];
+    __shared__ float s_lm[FEAT ? kTcThreads / 32 : 1][8][2];
+    FitTables tab{};
+    if (FEAT) tab = load_fit_tables(model, smem + kTcABytes + kTcWBytes);
     __shared__ float s_bias[3 * kHidden + kOutPad];
     __shared__ __align__(8) uint64_t s_mbar;
     __shared__ uint32_t s_tmem;
@@ -228,12 +241,49 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_forward_tc_kernel(
             cp_async16(reinterpret_cast<uint4 *>(W) + e, src + e, 16u);
     };
     auto copy_x = [&](int64_t row0) {
-        // features -> A (K = 80: 10 chunks per row), rows past m zero
-        for (int e = tid; e < kTcRows * (kInPad / 8); e += kTcThreads) {
-            const int r = e / (kInPad / 8), c = e % (kInPad / 8);
-            const bool in = row0 + r < m;
-            cp_async16(A + img_off(r, c, kInPad / 8), in ? x + (row0 + r) * stride + 8 * c : x,
-                       in ? 16u : 0u);
+        if (!FEAT) {
+            // features -> A (K = 80: 10 chunks per row), rows past m zero
+            for (int e = tid; e < kTcRows * (kInPad / 8); e += kTcThreads) {
+                const int r = e / (kInPad / 8), c = e % (kInPad / 8);
+                const bool in = row0 + r < m;
+                cp_async16(A + img_off(r, c, kInPad / 8),
+                           in ? x + (row0 + r) * stride + 8 * c : x, in ? 16u : 0u);
+            }
+            return;
+        }
+        // the warp's 8 forests of the tile, features formed in place
+        const float bins_per_span =
+            (float)(kFeatBins / (model.log_lambda_rest_max - model.log_lambda_rest_min));
+        const int r0 = warp * 8;
+        if (lane < 8 && row0 + r0 + lane < m) {
+            const float2 lm = forest_lmin(sp, model, row0 + r0 + lane);
+            s_lm[warp][lane][0] = lm.x;
+            s_lm[warp][lane][1] = lm.y;
+        }
+        __syncwarp();
+        for (int j = 0; j < 8; ++j) {
+            const int r = r0 + j;
+            const int64_t f = row0 + r;
+            FeatScalars fs{0.f, 0.f, 0.f};
+            if (f < m) {
+                fs = forest_feature_sums(sp, tab, f, s_lm[warp][j][0], s_lm[warp][j][1],
+                                         bins_per_span, s_feat_sums[warp], lane);
+                if (lane == 0) a0_out[f] = f32_to_f64(fs.a0);
+            }
+            if (lane < kInPad / 8) {
+                uint32_t w[4];
+#pragma unroll
+                for (int i = 0; i < 4; ++i) {
+                    const int k = 8 * lane + 2 * i;
+                    const float lo = f < m ? forest_feature(s_feat_sums[warp], fs, k) : 0.f;
+                    const float hi = f < m ? forest_feature(s_feat_sums[warp], fs, k + 1) : 0.f;
+                    w[i] = (uint32_t)__bfloat16_as_ushort(__float2bfloat16(lo)) |
+                           ((uint32_t)__bfloat16_as_ushort(__float2bfloat16(hi)) << 16);
+                }
+                *reinterpret_cast<uint4 *>(A + img_off(r, lane, kInPad / 8)) =
+                    make_uint4(w[0], w[1], w[2], w[3]);
+            }
+            __syncwarp();
         }
     };
     if ((int64_t)blockIdx.x < ntiles) {
@@ -268,8 +318,8 @@ __global__ void __launch_bounds__(kTcThreads, 1) mlp_forward_tc_kernel(
             if (layer < 3) {
                 copy_w(layer + 1);
             } else if (tile + gridDim.x < ntiles) {
-                copy_x((tile + gridDim.x) * kTcRows);
                 copy_w(0);
+                copy_x((tile + gridDim.x) * kTcRows);
             }
             if (layer < 3) {
                 // bias + GELU, rounded to BF16 into A: the next layer's input
@@ -340,13 +390,33 @@ int launch_mlp_forward_tc(const uint16_t *packed, const float *params, const uin
     if (m <= 0) return PG_OK;
     const size_t smem = kTcABytes + kTcWBytes;
     cudaError_t err = cudaFuncSetAttribute(
-        mlp_forward_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+        mlp_forward_tc_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     if (err != cudaSuccess) return check_cuda(err);
     const int64_t ntiles = (m + kTcRows - 1) / kTcRows;
     const unsigned blocks = (unsigned)(ntiles < num_sms ? ntiles : num_sms);
-    mlp_forward_tc_kernel<<<blocks, kTcThreads, smem, stream>>>(
+    pg_spectra no_sp{};
+    pg_cont_model no_model{};
+    mlp_forward_tc_kernel<false><<<blocks, kTcThreads, smem, stream>>>(
         reinterpret_cast<const __nv_bfloat16 *>(x), m, stride,
-        reinterpret_cast<const uint4 *>(packed), params, y, scratch);
+        reinterpret_cast<const uint4 *>(packed), params, y, scratch, no_sp, no_model, nullptr);
+    return check_cuda(cudaGetLastError());
+}
+
+int launch_mlp_warm_start_tc(const pg_spectra &sp, const pg_cont_model &model,
+                             const uint16_t *packed, const float *params, float *y, double *a0,
+                             Scratch *scratch, int num_sms, cudaStream_t stream) {
+    if (sp.num <= 0) return PG_OK;
+    const size_t smem =
+        kTcABytes + kTcWBytes + fit_smem_bytes(model.num_mean_cont, model.num_var_intervals);
+    if (smem > 220 * 1024) return PG_ERR_UNSUPPORTED;
+    cudaError_t err = cudaFuncSetAttribute(
+        mlp_forward_tc_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    if (err != cudaSuccess) return check_cuda(err);
+    const int64_t ntiles = (sp.num + kTcRows - 1) / kTcRows;
+    const unsigned blocks = (unsigned)(ntiles < num_sms ? ntiles : num_sms);
+    mlp_forward_tc_kernel<true><<<blocks, kTcThreads, smem, stream>>>(
+        nullptr, sp.num, 0, reinterpret_cast<const uint4 *>(packed), params, y, scratch, sp, model,
+        a0);
     return check_cuda(cudaGetLastError());
 }
 

@@ -49,8 +49,11 @@ def _bind():
     lib.pg_mlp_packed_elems.restype = ctypes.c_int64
     lib.pg_mlp_pack.argtypes = [vp, vp, vp]
     lib.pg_mlp_forward.argtypes = [vp, vp, vp, vp, i64, i32, vp, vp]
+    lib.pg_mlp_warm_start.argtypes = [vp, ctypes.POINTER(continuum.SpectraC),
+                                      ctypes.POINTER(continuum.ContModelC), vp, vp, vp, vp, vp]
     for name in ("pg_mlp_gemm", "pg_mlp_colsum", "pg_mlp_mse_grad", "pg_mlp_adam",
-                 "pg_mlp_to_bf16", "pg_mlp_features", "pg_mlp_pack", "pg_mlp_forward"):
+                 "pg_mlp_to_bf16", "pg_mlp_features", "pg_mlp_pack", "pg_mlp_forward",
+                 "pg_mlp_warm_start"):
         getattr(lib, name).restype = ctypes.c_int
     lib._mlp_bound = True
     return lib
@@ -123,19 +126,35 @@ class WarmStartMLP:
         """Inference forward pass in one tcgen05 kernel (pg_mlp_forward):
         x16 bf16 [m, FEATURE_STRIDE] -> FP32 [m, 2]."""
         lib = _bind()
-        if self._packed_step != self.step:
-            check(lib.pg_mlp_pack(self.params16.data_ptr(), self.packed.data_ptr(),
-                                  self._stream()), "mlp pack")
-            self._packed_step = self.step
-        if self._plan is None:
-            from ._native import Plan
-            self._plan = Plan()
+        self._ensure_packed()
         m = x16.shape[0]
         y = torch.empty(m, NUM_OUT, dtype=torch.float32, device=self.device)
         check(lib.pg_mlp_forward(self._plan.handle, self.packed.data_ptr(), self.params.data_ptr(),
                                  x16.data_ptr(), m, x16.stride(0), y.data_ptr(), self._stream()),
               "mlp forward")
         return y
+
+    def _ensure_packed(self):
+        if self._packed_step != self.step:
+            check(_bind().pg_mlp_pack(self.params16.data_ptr(), self.packed.data_ptr(),
+                                      self._stream()), "mlp pack")
+            self._packed_step = self.step
+        if self._plan is None:
+            from ._native import Plan
+            self._plan = Plan()
+
+    def warm_start(self, engine, spectra, model_c):
+        """Features and network in one kernel (pg_mlp_warm_start): returns the
+        FP32 output [num, 2] and a0 (FP64 [num])."""
+        self._ensure_packed()
+        n = spectra.num
+        y = torch.empty(max(n, 1), NUM_OUT, dtype=torch.float32, device=self.device)
+        a0 = torch.empty(max(n, 1), dtype=torch.float64, device=self.device)
+        check(_bind().pg_mlp_warm_start(self._plan.handle, ctypes.byref(spectra.c),
+                                        ctypes.byref(model_c), self.packed.data_ptr(),
+                                        self.params.data_ptr(), y.data_ptr(), a0.data_ptr(),
+                                        self._stream()), "mlp warm start")
+        return y[:n], a0[:n]
 
     def forward(self, x16, keep=False):
         """x16: bf16 [m, FEATURE_STRIDE] (first 66 columns used). Returns
@@ -255,14 +274,16 @@ AB_TOL = 1e-5
 
 def warm_fit(engine, spectra, mlp, warm_max_iter=3, mode=None, chi2_tol=CHI2_TOL,
              ab_tol=AB_TOL):
-    """Warm-started fits, each judged on the GPU by its own certificate
+    """Warm-started fits (features and network in one fused kernel,
+    pg_mlp_warm_start), each judged on the GPU by its own certificate
     (Dr16Gpu.fit_warm: the remaining Newton step and the chi2 excess over the
     local quadratic minimum, both bounded per forest); forests the network
     placed too far for ``warm_max_iter`` certified Newton steps are re-fitted
     by the plain fit, in place. Returns (fit dict, start, fallback mask)."""
     model_c, keep = engine._model()
-    feat, a0 = features(engine, spectra, model_c)
-    start = predict_start(mlp, feat, a0)
+    y, a0 = mlp.warm_start(engine, spectra, model_c)
+    y = y.double()
+    start = torch.stack([a0 * (1.0 + y[:, 0]), a0 * y[:, 1]], dim=1).contiguous()
     fit = engine.fit_warm(spectra, start, max_iter=warm_max_iter, chi2_tol=chi2_tol,
                           ab_tol=ab_tol)
     fallback = fit["status"] != 0

@@ -165,3 +165,21 @@ def test_certificate_accepts_optimum_rejects_far_start(cuda):
     short = np.diff(raw.pix_offset) <= 224
     res = continuum.fit_results_to_host(eng.fit_warm(sp, far, max_iter=1))
     assert np.all(res["status"][ok & short] == 1)
+
+
+def test_fused_warm_start_matches_features_then_network(cuda):
+    """pg_mlp_warm_start (features formed inside the tensor-core kernel)
+    gives the a0 of pg_mlp_features and the network output of
+    pg_mlp_forward on its features (700 forests: a partial last tile)."""
+    torch = cuda
+    from picca_gb300 import continuum, learned, synthetic_spectra
+    raw = synthetic_spectra.make_raw_forests(700, 404)
+    eng = continuum.Dr16Gpu(raw.grid, num_iterations=1)
+    sp = continuum.DeviceSpectra(raw, eng.device)
+    net = learned.WarmStartMLP(seed=7)
+    model_c, keep = eng._model()
+    feat, a0 = learned.features(eng, sp, model_c)
+    y_ref = net.forward_fused(feat)
+    y, a0_f = net.warm_start(eng, sp, model_c)
+    assert torch.equal(a0[:700], a0_f)
+    assert float((y - y_ref).norm() / y_ref.norm()) < 1e-6
