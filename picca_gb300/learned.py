@@ -274,16 +274,18 @@ AB_TOL = 1e-5
 
 def warm_fit(engine, spectra, mlp, warm_max_iter=3, mode=None, chi2_tol=CHI2_TOL,
              ab_tol=AB_TOL):
-    """Warm-started fits (features and network in one fused kernel,
-    pg_mlp_warm_start), each judged on the GPU by its own certificate
+    """Warm-started fits (the features kernel, then the fused tcgen05
+    network), each judged on the GPU by its own certificate
     (Dr16Gpu.fit_warm: the remaining Newton step and the chi2 excess over the
     local quadratic minimum, both bounded per forest); forests the network
     placed too far for ``warm_max_iter`` certified Newton steps are re-fitted
     by the plain fit, in place. Returns (fit dict, start, fallback mask)."""
     model_c, keep = engine._model()
-    y, a0 = mlp.warm_start(engine, spectra, model_c)
-    y = y.double()
-    start = torch.stack([a0 * (1.0 + y[:, 0]), a0 * y[:, 1]], dim=1).contiguous()
+    # features and network as two kernels: the one-kernel form
+    # (WarmStartMLP.warm_start) is slower, its feature pass runs on the few
+    # warps the tensor-core kernel leaves room for
+    feat, a0 = features(engine, spectra, model_c)
+    start = predict_start(mlp, feat, a0)
     fit = engine.fit_warm(spectra, start, max_iter=warm_max_iter, chi2_tol=chi2_tol,
                           ab_tol=ab_tol)
     fallback = fit["status"] != 0
