@@ -273,8 +273,10 @@ int pg_cf_xi(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *s
     if ((rc = reset_scratch(plan, st))) return rc;
     const Binning b = make_binning(*params);
     const pg_forest_set &other = s2 ? *s2 : *s1;
-    // the precision form covers the standard (r_par, r_trans) geometry
-    const bool fast = mode == PG_MODE_FP32_GUARD && !b.rmu && !b.ang_corr &&
+    // the precision form covers the (r_par, r_trans) geometry with every cut
+    // and the r-mu binning without the z-pair, zerr and half-plate cuts
+    const bool rmu_cuts = b.rmu && (b.remove_shp || b.zmin_on || b.zmax_on || b.zerr_on);
+    const bool fast = mode == PG_MODE_FP32_GUARD && !rmu_cuts && !b.ang_corr &&
                       s1->max_pixels <= 65535;
     if (fast)
         return launch_cf_xi_fast(b, params->ang_max, *s1, other, nbr_offsets, nbr_index,

@@ -71,7 +71,9 @@ constexpr int kCfBlock = 640;
 constexpr int kXcfBlock = 512;
 
 struct FastConst {
-    double inv_p, inv_t;
+    double inv_p, inv_t;    // histogram scales: r_par (mu with r-mu bins) and r_trans (r)
+    double geom_p;          // scale of the staged r_par geometry (inv_p; the r scale with
+                            // r-mu bins, where both coordinates are in r-bin units)
     float pc;               // r_par_min * inv_p + 1/2
     float g0_par;           // guard band of x' without the |rho1| term
     float g_rho;            // guard band of x' per unit of the work item's max |rho1|
@@ -83,6 +85,9 @@ struct FastConst {
     int hstride;            // histogram array stride (nbins rounded up to 4)
     int lower_exact;        // auto-correlation with r_par_min = 0: x = |p| >= 0, so
                             // the lower edge of bin 0 can never be crossed
+    // r-mu binning: mu = r_par / r in bins of inv_mu = np / (mu_max - mu_min)
+    float inv_mu, mu_off;   // mu_off = mu_min * inv_mu + 1/2
+    float g_mu0;            // guard of x_mu without the r_par error term
 };
 
 // Guard of the r_par coordinate of one work item (see make_fast_const).
@@ -381,7 +386,15 @@ __host__ __device__ inline CfSmem cf_smem(int nbins, int max_pix1, int nwarps) {
 //
 // EXTRA: half-plate veto, z-pair cuts or zerr cut may be active.
 // LOWX: auto-correlation with r_par_min = 0 (lower edge of bin 0 exempt).
-template <bool AUTO, bool EXTRA, bool LOWX>
+// RMU: r-mu bins (--rmu-binning, py/picca/cf.py:354-358; not with EXTRA):
+// both coordinates are staged in r-bin units, so that per pair
+// r = sqrt(p^2 + t^2) (one FMA and a reciprocal square root) and
+// mu = |p| / r (p / r for two fields); the guard of mu grows as the absolute
+// error of p over r, and pairs at r ~ 0 (or whose mu guard exceeds 1/4) are
+// re-decided in FP64. Runs along diagonals work as before: r and mu change
+// slowly along a diagonal. The r_par histogram sums mu w, the r_trans one
+// r w in r-bin units.
+template <bool AUTO, bool EXTRA, bool LOWX, bool RMU>
 __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
     const __grid_constant__ Binning b, const FastConst *__restrict__ fcp,
     const __grid_constant__ pg_forest_set s1, const __grid_constant__ pg_forest_set s2,
@@ -408,8 +421,9 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
     const float t_end = (float)nt + 1.f;  // x_tr' at or above this: rejected, a bin of margin
     // accepted range of p with one bin of margin each side: x = p - pmin in
     // [-1, np + 1]; |p| <= np + 1 for auto-correlations
-    const float p_lo = AUTO ? -(float)(np + 1u) : pmin_f - 1.f;
-    const float p_hi = AUTO ? (float)(np + 1u) : pmin_f + (float)np + 1.f;
+    const float p_lo = RMU ? -(float)(nt + 1u) : (AUTO ? -(float)(np + 1u) : pmin_f - 1.f);
+    const float p_hi = RMU ? (float)(nt + 1u) : (AUTO ? (float)(np + 1u) : pmin_f + (float)np + 1.f);
+    const float inv_mu = fcp->inv_mu, mu_off = fcp->mu_off, g_mu0 = fcp->g_mu0;
     const int hs = fcp->hstride;
     const CfSmem L = cf_smem(nbins, max_pix1, nwarps);
     float *h = reinterpret_cast<float *>(smem + L.cells);
@@ -450,6 +464,9 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                                            const_cast<float4 *>(p1x), &max_rho_bits);
         const ParGuard pg = par_guard(fcp, __uint_as_float(max_rho_bits));
         const float h_par = pg.h_par, low_clamp = pg.low_clamp;
+        // r-mu: r carries the errors of both staged coordinates
+        const float g_pp = pg.guard_v;
+        const float h_r = h_tr - g_pp;
         const int64_t k1 = nbr_offsets[f1 + 1];
         int head = 0, tail = 0;  // run ring of this warp (warp-uniform)
         int qn = 0;              // FP64 re-decision queue of this warp
@@ -507,7 +524,7 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                 }
             }
             __syncwarp();
-            const float cp = (float)(chalf * inv_p);
+            const float cp = (float)(chalf * (RMU ? fcp->geom_p : inv_p));
             const float st = (float)(shalf * inv_t);
             for (int jc = 0; jc < n2; jc += kChunk) {
                 const int jn = min(kChunk, n2 - jc);
@@ -529,7 +546,7 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                     // hi + lo enters the summed r_par
                     const double nb_d = -((double)cp * rho2_d);
                     const float nb_h = -__fmul_rn(cp, rho2);
-                    buf[jl] = make_float4(nb_h, ok ? __fmaf_rn(st, d2, -0.5f) : kFar,
+                    buf[jl] = make_float4(nb_h, ok ? __fmaf_rn(st, d2, RMU ? 0.f : -0.5f) : kFar,
                                           (float)s2.z[jj], ok ? weight32(w2) : 0.f);
                     const float2 dw = split2(s2.delta[jj] * w2);
                     bufx[jl] = make_float4(dw.x, dw.y, (float)(nb_d - (double)nb_h), 0.f);
@@ -613,15 +630,30 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                         const float pp = __fmaf_rn(cp, q1.x, q2.x);
                         const float v = fabsf(pp);
                         const float pv = AUTO ? v : pp;
-                        const float xp = LOWX ? fmaxf(pv - pc, low_clamp) : pv - pc;
                         const float xt = __fmaf_rn(st, q1.y, q2.y);
-                        float fp, ft;
-                        const unsigned ip = round_rem(xp, fp);
-                        const unsigned it = round_rem(xt, ft);
+                        float fp, ft, ru = 0.f, sinv = 0.f;
+                        unsigned ip, it;
+                        bool near;
+                        if (RMU) {
+                            const float r2 = __fmaf_rn(pp, pp, xt * xt);
+                            sinv = rsqrtf(r2);
+                            ru = r2 * sinv;
+                            const float mu = pv * sinv;
+                            float xm = __fmaf_rn(mu, inv_mu, -mu_off);
+                            if (LOWX) xm = fmaxf(xm, low_clamp);
+                            ip = round_rem(xm, fp);
+                            it = round_rem(ru - 0.5f, ft);
+                            const float gm = __fmaf_rn(g_pp * sinv, inv_mu, g_mu0);
+                            near = !(gm < 0.25f) | (fabsf(fp) > 0.5f - gm) | (fabsf(ft) > h_r);
+                        } else {
+                            const float xp = LOWX ? fmaxf(pv - pc, low_clamp) : pv - pc;
+                            ip = round_rem(xp, fp);
+                            it = round_rem(xt, ft);
+                            near = (fabsf(fp) > h_par) | (fabsf(ft) > h_tr);
+                        }
                         // a pixel without weight or vetoed (w staged as 0) pairs with
                         // nothing: neither accepted nor queued for re-decision
                         in &= (q1.w != 0.f) & (q2.w != 0.f);
-                        bool near = (fabsf(fp) > h_par) | (fabsf(ft) > h_tr);
                         bool ok = (ip < np) & (it < nt);
                         const float zs = q1.z + q2.z;
                         if (EXTRA) {
@@ -662,9 +694,17 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                             r_w += w12;
                             // r_par (bin units) from the hi + lo distances:
                             // relative precision for the summed r_par
-                            const float pp_s = pp + __fmaf_rn(cp, x1.z, x2.z);
-                            r_pw = __fmaf_rn(AUTO ? fabsf(pp_s) : pp_s, w12, r_pw);
-                            r_tw = __fmaf_rn(xt + 0.5f, w12, r_tw);
+                            if (RMU) {
+                                // mu from the hi + lo distances: relative
+                                // precision for the summed mu near mu = 0
+                                const float pp_s = pp + __fmaf_rn(cp, x1.z, x2.z);
+                                r_pw = __fmaf_rn((AUTO ? fabsf(pp_s) : pp_s) * sinv, w12, r_pw);
+                                r_tw = __fmaf_rn(ru, w12, r_tw);
+                            } else {
+                                const float pp_s = pp + __fmaf_rn(cp, x1.z, x2.z);
+                                r_pw = __fmaf_rn(AUTO ? fabsf(pp_s) : pp_s, w12, r_pw);
+                                r_tw = __fmaf_rn(xt + 0.5f, w12, r_tw);
+                            }
                             r_zw = __fmaf_rn(zs, w12, r_zw);
                             ++run_n;
                         }
@@ -935,11 +975,28 @@ FastConst make_fast_const(const Binning &b) {
     const double u = 1.0 / 16777216.0;
     fc.inv_p = (double)b.np / b.r_par_range;
     fc.inv_t = (double)b.nt / b.r_trans_max;
+    fc.geom_p = fc.inv_p;
     const double pmin = b.r_par_min * fc.inv_p;
     fc.pc = (float)(pmin + 0.5);
     fc.g0_par = (float)(16 * u * (b.np + fabs(pmin) + 2) + 1e-6);
     fc.g_rho = (float)(8 * u * fc.inv_p);
+    if (b.rmu) {
+        // r-mu bins (py/picca/cf.py:354-358): r_par and r_trans are staged in
+        // r-bin units, r = sqrt(r_par^2 + r_trans^2) and mu = r_par / r per
+        // pair; the r_par histogram holds mu (scale 1). g0_par and g_rho
+        // bound the absolute error of the staged r_par in r-bin units.
+        fc.geom_p = fc.inv_t;
+        fc.inv_p = 1.0;
+        fc.pc = 0.5f;
+        fc.g0_par = (float)(16 * u * (b.nt + 2) + 1e-6);
+        fc.g_rho = (float)(8 * u * fc.inv_t);
+        fc.inv_mu = (float)((double)b.np / b.r_par_range);
+        fc.mu_off = (float)(b.r_par_min * (double)b.np / b.r_par_range + 0.5);
+        fc.g_mu0 = (float)(16 * u * (b.np + fabs(b.r_par_min * b.np / b.r_par_range) + 2) + 1e-6);
+    }
     double g_tr = 16 * u * (b.nt + 2) + 1e-6;
+    // r-mu: r also carries the reciprocal square root and the sum of squares
+    if (b.rmu) g_tr = 32 * u * (b.nt + 2) + 1e-6;
     if (!(g_tr < 0.05)) g_tr = 0.05;
     fc.h_tr = (float)(0.5 - g_tr);
     fc.guard_z = 1e-5f;  // z1 + z2 < 20: FP32 error below 5e-6
@@ -1003,23 +1060,29 @@ int launch_cf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &s1,
     int rc = prepare_fast(b, fc, stream);
     if (rc) return rc;
     const bool extra = b.remove_shp || b.zmin_on || b.zmax_on || b.zerr_on;
+    if (b.rmu && extra) return PG_ERR_UNSUPPORTED;  // callers use the FP64 kernel
     const bool autoc = !b.x_correlation;
     const bool lowx = autoc && b.r_par_min == 0.0;
     int grid = 0;
-#define PG_LAUNCH_CF(A, E, L)                                                                  \
-    rc = persistent_grid(cf_xi_diag_kernel<A, E, L>, block, smem, num_sms, num_work, &grid,    \
+#define PG_LAUNCH_CF(A, E, L, R)                                                               \
+    rc = persistent_grid(cf_xi_diag_kernel<A, E, L, R>, block, smem, num_sms, num_work, &grid, \
                          tuning.blocks_per_sm);                                                \
     if (rc) return rc;                                                                         \
-    cf_xi_diag_kernel<A, E, L><<<grid, block, smem, stream>>>(b, fc, s1, s2, nbr_offsets,      \
-                                                              nbr_index, nbr_angle,            \
-                                                              work_order, num_work, out,       \
-                                                              scratch, max_pix1);
-    if (autoc && lowx && !extra) { PG_LAUNCH_CF(true, false, true) }
-    else if (autoc && lowx && extra) { PG_LAUNCH_CF(true, true, true) }
-    else if (autoc && !extra) { PG_LAUNCH_CF(true, false, false) }
-    else if (autoc && extra) { PG_LAUNCH_CF(true, true, false) }
-    else if (!extra) { PG_LAUNCH_CF(false, false, false) }
-    else { PG_LAUNCH_CF(false, true, false) }
+    cf_xi_diag_kernel<A, E, L, R><<<grid, block, smem, stream>>>(b, fc, s1, s2, nbr_offsets,   \
+                                                                 nbr_index, nbr_angle,         \
+                                                                 work_order, num_work, out,    \
+                                                                 scratch, max_pix1);
+    if (b.rmu) {
+        if (autoc && lowx) { PG_LAUNCH_CF(true, false, true, true) }
+        else if (autoc) { PG_LAUNCH_CF(true, false, false, true) }
+        else { PG_LAUNCH_CF(false, false, false, true) }
+    }
+    else if (autoc && lowx && !extra) { PG_LAUNCH_CF(true, false, true, false) }
+    else if (autoc && lowx && extra) { PG_LAUNCH_CF(true, true, true, false) }
+    else if (autoc && !extra) { PG_LAUNCH_CF(true, false, false, false) }
+    else if (autoc && extra) { PG_LAUNCH_CF(true, true, false, false) }
+    else if (!extra) { PG_LAUNCH_CF(false, false, false, false) }
+    else { PG_LAUNCH_CF(false, true, false, false) }
 #undef PG_LAUNCH_CF
     return check_cuda(cudaGetLastError());
 }

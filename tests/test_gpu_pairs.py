@@ -168,10 +168,14 @@ def _synthetic_sets(seed=7, num=600, xcf=False, grid="log"):
 
 
 @pytest.mark.parametrize("precision", MODES)
-@pytest.mark.parametrize("variant", ["auto", "cross", "auto_cuts", "auto_lin"])
+@pytest.mark.parametrize("variant", ["auto", "cross", "auto_cuts", "auto_lin", "auto_rmu",
+                                     "cross_rmu"])
 def test_cf_gpu_matches_oracle_synthetic(cuda, precision, variant):
     """``auto_lin``: forests on the DESI-like linear grid (0.8 Angstrom,
-    150-600 pixels), which the pair kernel stages in several chunks."""
+    150-600 pixels), which the pair kernel stages in several chunks.
+    ``*_rmu``: r-mu bins (--rmu-binning; mu in [0, 1] for the auto, [-1, 1]
+    for two fields), which the precision form computes per pair from the
+    staged coordinates."""
     from oracle import cpu as oracle
     from picca_gb300 import pairs, synthetic
     fs, _ = _synthetic_sets(grid="lin" if variant == "auto_lin" else "log",
@@ -182,10 +186,14 @@ def test_cf_gpu_matches_oracle_synthetic(cuda, precision, variant):
     fs2 = None
     kwargs = dict(r_par_min=0.0, r_par_max=200.0, r_trans_max=200.0, num_bins_r_par=50,
                   num_bins_r_trans=50)
-    if variant == "cross":
+    if variant in ("cross", "cross_rmu"):
         fs2 = synthetic.make_forests(500, 99, (150.0, 156.0), (0.0, 6.0), 2.1, 3.5, "uniform",
                                      thingid_start=5000)
         kwargs.update(r_par_min=-200.0, num_bins_r_par=100, x_correlation=True)
+    if variant == "auto_rmu":
+        kwargs.update(r_par_min=0.0, r_par_max=1.0, rmu_binning=True)
+    if variant == "cross_rmu":
+        kwargs.update(r_par_min=-1.0, r_par_max=1.0, rmu_binning=True)
     if variant == "auto_cuts":
         fs.plate[:] = np.arange(fs.num) % 3
         fs.fiberid[:] = (np.arange(fs.num) * 37) % 1000
