@@ -631,13 +631,13 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                         const float v = fabsf(pp);
                         const float pv = AUTO ? v : pp;
                         const float xt = __fmaf_rn(st, q1.y, q2.y);
-                        float fp, ft, ru = 0.f, sinv = 0.f;
+                        float fp, ft;
                         unsigned ip, it;
                         bool near;
                         if (RMU) {
                             const float r2 = __fmaf_rn(pp, pp, xt * xt);
-                            sinv = rsqrtf(r2);
-                            ru = r2 * sinv;
+                            const float sinv = rsqrtf(r2);
+                            const float ru = r2 * sinv;
                             const float mu = pv * sinv;
                             float xm = __fmaf_rn(mu, inv_mu, -mu_off);
                             if (LOWX) xm = fmaxf(xm, low_clamp);
@@ -695,11 +695,14 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                             // r_par (bin units) from the hi + lo distances:
                             // relative precision for the summed r_par
                             if (RMU) {
-                                // mu from the hi + lo distances: relative
-                                // precision for the summed mu near mu = 0
+                                // r and mu from the hi + lo distances: the
+                                // staged r_par carries an absolute error that
+                                // is large relative to a small r
                                 const float pp_s = pp + __fmaf_rn(cp, x1.z, x2.z);
-                                r_pw = __fmaf_rn((AUTO ? fabsf(pp_s) : pp_s) * sinv, w12, r_pw);
-                                r_tw = __fmaf_rn(ru, w12, r_tw);
+                                const float r2s = __fmaf_rn(pp_s, pp_s, xt * xt);
+                                const float ss = rsqrtf(r2s);
+                                r_pw = __fmaf_rn((AUTO ? fabsf(pp_s) : pp_s) * ss, w12, r_pw);
+                                r_tw = __fmaf_rn(r2s * ss, w12, r_tw);
                             } else {
                                 const float pp_s = pp + __fmaf_rn(cp, x1.z, x2.z);
                                 r_pw = __fmaf_rn(AUTO ? fabsf(pp_s) : pp_s, w12, r_pw);
