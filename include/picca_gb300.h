@@ -211,7 +211,10 @@ int pg_xcf_neighbours_grouped(pg_plan *plan, const pg_corr_params *params,
  * rows out[s1->row[f]]. nbr_angle (optional, parallel to nbr_index) gives
  * the angular separation of each listed pair; NULL computes it from the unit
  * vectors as QSO.get_angle_between does. mode = PG_MODE_FP64 or
- * PG_MODE_FP32_GUARD. */
+ * PG_MODE_FP32_GUARD; the precision form covers the (r_par, r_trans) bins
+ * with every cut and the r-mu bins without the z-pair, zerr and half-plate
+ * cuts; the angular binning and r-mu with those cuts run in FP64 in either
+ * mode. */
 int pg_cf_xi(pg_plan *plan, const pg_corr_params *params, const pg_forest_set *s1,
              const pg_forest_set *s2, const int64_t *nbr_offsets, const int32_t *nbr_index,
              const double *nbr_angle, const int32_t *work_order, int64_t num_work,
