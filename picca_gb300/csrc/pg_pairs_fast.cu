@@ -3,9 +3,11 @@
 // FP64 rows.
 //
 // Persistent structure: one work item = one forest of set 1 with all its
-// neighbours; the forest-1 pixels are staged in shared memory, warps take
-// neighbour forests dynamically, and each lane holds P consecutive forest-2
-// pixels in registers while it loops over the forest-1 pixels.
+// neighbours; the forest-1 pixels are staged in shared memory and warps take
+// neighbours dynamically. The auto-correlation sweeps each forest pair
+// along diagonals (cf_xi_diag_kernel), the cross-correlation each quasar
+// along the forest (xcf_xi_fast_kernel); both sum runs of consecutive pairs
+// of one bin in registers.
 //
 // Geometry. Comoving distances are taken relative to R, the distance of the
 // middle pixel of forest 1 (one FP64 subtraction per pixel, exact), and
@@ -66,7 +68,6 @@ constexpr int kCfQueue = 128;                 // FP64 recheck entries per warp (
 constexpr int kAccQ = 64;                     // run ring per warp (<= 31 + 32 entries held)
 constexpr int kChunk = 128;                   // forest-2 pixels staged per warp at a time
 constexpr int kRunMax = 64;                   // pairs summed in FP32 registers per run
-constexpr int kXcfP = 2;                      // quasars per lane per pass
 constexpr int kCfBlock = 640;
 constexpr int kXcfBlock = 512;
 
@@ -794,6 +795,20 @@ __device__ __forceinline__ void xcf_drain(const Binning &b, const FastConst *__r
     __syncwarp();
 }
 
+// The cross-correlation as runs along the forest. A lane owns one quasar of
+// a group of 32 neighbours and steps the forest pixels i with the others
+// (pixel i is a broadcast read of shared memory); along the forest r_par and
+// r_trans change slowly, so consecutive accepted pairs of a lane share their
+// bin for several steps and are summed in registers as a run, which goes to
+// the block histogram through the warp's ring when the bin changes (as in
+// cf_xi_diag_kernel). Binary searches on the staged forest give each lane
+// the pixels whose p = cp*rho1 + nB lies within one bin of the accepted
+// r_par range and whose x_tr' is below the end of the r_trans range
+// (requires rho and dist_m non-decreasing along the forest, checked;
+// otherwise every pixel is swept); the skipped pairs are at least one bin
+// outside the accepted ranges, so the reference rejects them too. Pairs
+// within the guard band of an edge or a cut are re-decided in FP64
+// (xcf_drain).
 template <bool EXTRA>
 __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
     const __grid_constant__ Binning b, const FastConst *__restrict__ fcp,
@@ -814,10 +829,15 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
     const float h_tr = fcp->h_tr;
     const unsigned np = fcp->np, nt = fcp->nt;
     const int hs = fcp->hstride;
-    const SmemLayout L = smem_layout(nbins, max_pix1, nwarps, false);
+    // accepted range of p with one bin of margin each side, and of x_tr'
+    const float p_lo = (pc - 0.5f) - 1.f, p_hi = (pc - 0.5f) + (float)np + 1.f;
+    const float t_end = (float)nt + 1.f;
+    const SmemLayout L = smem_layout(nbins, max_pix1, nwarps, true);
     float *h = reinterpret_cast<float *>(smem + L.cells);
     float4 *p1 = reinterpret_cast<float4 *>(smem + L.p1);
     float4 *p2 = reinterpret_cast<float4 *>(smem + L.p2);
+    float4 *acc0 = reinterpret_cast<float4 *>(smem + L.acc0) + (size_t)warp * kAccQ;
+    float4 *acc1 = reinterpret_cast<float4 *>(smem + L.acc1) + (size_t)warp * kAccQ;
     uint32_t *queue = reinterpret_cast<uint32_t *>(smem + L.queue) + warp * kQueue;
     zero_all(h, H_COUNT * hs);
     unsigned long long rechecks = 0, overflows = 0;
@@ -837,111 +857,167 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
         }
         const int n1 = (int)n1_64;
         const double r_ref = fs.r_comov[ctx.a0 + n1 / 2];
-        stage_forest1(fs, ctx.a0, n1, r_ref, p1, p2, &max_rho_bits);
+        const bool sorted1 = stage_forest1(fs, ctx.a0, n1, r_ref, p1, p2, &max_rho_bits);
         const ParGuard pg = par_guard(fcp, __uint_as_float(max_rho_bits));
         const float h_par = pg.h_par;
         ctx.x1 = fs.x_cart[f]; ctx.y1 = fs.y_cart[f]; ctx.zc1 = fs.z_cart[f];
         ctx.ra1 = fs.ra[f]; ctx.dec1 = fs.dec[f]; ctx.cd1 = fs.cos_dec[f];
         ctx.k0 = nbr_offsets[f];
         const int nq = (int)nq_64;
-        for (int kb = warp * 32 * kXcfP; kb < nq; kb += nwarps * 32 * kXcfP) {
-            float cp[kXcfP], st[kXcfP], nb[kXcfP], nbl[kXcfP], t[kXcfP], zv[kXcfP], wvh[kXcfP],
-                wvl[kXcfP];
-            bool any = false;
-#pragma unroll
-            for (int p = 0; p < kXcfP; ++p) {
-                const int kk = kb + lane + 32 * p;
-                cp[p] = 1.f; st[p] = 0.f; nb[p] = kFar; nbl[p] = 0.f; t[p] = kFar; zv[p] = kFar;
-                wvh[p] = 0.f; wvl[p] = 0.f;
-                if (kk < nq) {
-                    const int64_t g = nbr_index[ctx.k0 + kk];
-                    const double wq = objs.obj_weight[g];
-                    if (wq != 0) {
-                        any = true;
-                        const double ang =
-                            nbr_angle ? nbr_angle[ctx.k0 + kk]
-                                      : angle_between(ctx.x1, ctx.y1, ctx.zc1, ctx.ra1, ctx.dec1,
-                                                      ctx.cd1, objs.x_cart[g], objs.y_cart[g],
-                                                      objs.z_cart[g], objs.ra[g], objs.dec[g]);
-                        cp[p] = (float)(cos(ang / 2) * inv_p);
-                        st[p] = (float)(sin(ang / 2) * inv_t);
-                        const double rho_d = objs.obj_r_comov[g] - r_ref;
-                        const float rho_q = (float)rho_d;
-                        nb[p] = -__fmul_rn(cp[p], rho_q);
-                        nbl[p] = (float)(-((double)cp[p] * rho_d) - (double)nb[p]);
-                        t[p] = __fmaf_rn(st[p], (float)objs.obj_dist_m[g], -0.5f);
-                        zv[p] = (float)objs.z_qso[g];
-                        wvh[p] = weight32(wq);
-                        wvl[p] = (float)(wq - (double)wvh[p]);
-                    }
+        int head = 0, tail = 0;  // run ring of this warp (warp-uniform)
+        int qn = 0;              // FP64 re-decision queue of this warp
+        for (int kb = warp * 32; kb < nq; kb += nwarps * 32) {
+            const int kk = kb + lane;
+            float cp = 1.f, st = 0.f, nb = kFar, nbl = 0.f, t = kFar, zv = kFar;
+            float wvh = 0.f, wvl = 0.f;
+            bool valid = false;
+            if (kk < nq) {
+                const int64_t g = nbr_index[ctx.k0 + kk];
+                const double wq = objs.obj_weight[g];
+                if (wq != 0) {
+                    valid = true;
+                    const double ang =
+                        nbr_angle ? nbr_angle[ctx.k0 + kk]
+                                  : angle_between(ctx.x1, ctx.y1, ctx.zc1, ctx.ra1, ctx.dec1,
+                                                  ctx.cd1, objs.x_cart[g], objs.y_cart[g],
+                                                  objs.z_cart[g], objs.ra[g], objs.dec[g]);
+                    cp = (float)(cos(ang / 2) * inv_p);
+                    st = (float)(sin(ang / 2) * inv_t);
+                    const double rho_d = objs.obj_r_comov[g] - r_ref;
+                    const float rho_q = (float)rho_d;
+                    nb = -__fmul_rn(cp, rho_q);
+                    nbl = (float)(-((double)cp * rho_d) - (double)nb);
+                    t = __fmaf_rn(st, (float)objs.obj_dist_m[g], -0.5f);
+                    zv = (float)objs.z_qso[g];
+                    wvh = weight32(wq);
+                    wvl = (float)(wq - (double)wvh);
                 }
             }
-            if (!__any_sync(0xffffffffu, any)) continue;
-            int qn = 0;
-            for (int i = 0; i < n1; ++i) {
+            // this lane's pixels [ia, ib): p and x_tr' are non-decreasing
+            // along a sorted forest
+            int ia = 0, ib = valid ? n1 : 0;
+            if (sorted1 && valid) {
+                int lo = 0, hi = n1;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (__fmaf_rn(cp, p1[mid].x, nb) < p_lo) lo = mid + 1;
+                    else hi = mid;
+                }
+                ia = lo;
+                hi = n1;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (__fmaf_rn(cp, p1[mid].x, nb) <= p_hi) lo = mid + 1;
+                    else hi = mid;
+                }
+                ib = lo;
+                lo = ia;
+                hi = ib;
+                while (lo < hi) {
+                    const int mid = (lo + hi) >> 1;
+                    if (__fmaf_rn(st, p1[mid].y, t) < t_end) lo = mid + 1;
+                    else hi = mid;
+                }
+                ib = lo;
+            }
+            int g_lo = ia < ib ? ia : INT_MAX, g_hi = ia < ib ? ib : INT_MIN;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) {
+                g_lo = min(g_lo, __shfl_xor_sync(0xffffffffu, g_lo, o));
+                g_hi = max(g_hi, __shfl_xor_sync(0xffffffffu, g_hi, o));
+            }
+            if (g_lo >= g_hi) continue;
+            unsigned run_bin = 0xFFFFFFFFu;
+            int run_n = 0;
+            float r_xi = 0.f, r_xil = 0.f, r_w = 0.f, r_pw = 0.f, r_tw = 0.f, r_zw = 0.f;
+            auto store_runs = [&](bool flag) {
+                const unsigned m = __ballot_sync(0xffffffffu, flag);
+                const int pos = (tail + __popc(m & lt_mask)) & (kAccQ - 1);
+                if (flag) {
+                    acc0[pos] = make_float4(r_xi, r_xil, r_w, r_pw);
+                    acc1[pos] = make_float4(r_tw, r_zw, __uint_as_float(run_bin),
+                                            __uint_as_float((unsigned)run_n));
+                }
+                tail += __popc(m);
+            };
+            for (int i = g_lo; i < g_hi; ++i) {
                 const float4 q = p1[i];
-                if (q.w == 0.f) continue;
-                const float4 qd = p2[i];
-                unsigned near_mask = 0;
-#pragma unroll
-                for (int p = 0; p < kXcfP; ++p) {
-                    const float pv = __fmaf_rn(cp[p], q.x, nb[p]);
-                    const float xt = __fmaf_rn(st[p], q.y, t[p]);
-                    float fp, ft;
-                    const unsigned ip = round_rem(pv - pc, fp);
-                    const unsigned it = round_rem(xt, ft);
-                    bool near = (fabsf(fp) > h_par) | (fabsf(ft) > h_tr);
-                    bool ok = (ip < np) & (it < nt);
-                    const float zs = q.z + zv[p];
-                    if (EXTRA) {
-                        if (b.zmin_on) {
-                            near |= fabsf(zs - fcp->zmin2) < fcp->guard_z;
-                            ok &= !(zs < fcp->zmin2);
-                        }
-                        if (b.zmax_on) {
-                            near |= fabsf(zs - fcp->zmax2) < fcp->guard_z;
-                            ok &= !(zs > fcp->zmax2);
-                        }
+                bool in = (i >= ia) & (i < ib) & (q.w != 0.f);
+                const float pv = __fmaf_rn(cp, q.x, nb);
+                const float xt = __fmaf_rn(st, q.y, t);
+                float fp, ft;
+                const unsigned ip = round_rem(pv - pc, fp);
+                const unsigned it = round_rem(xt, ft);
+                bool near = (fabsf(fp) > h_par) | (fabsf(ft) > h_tr);
+                bool ok = (ip < np) & (it < nt);
+                const float zs = q.z + zv;
+                if (EXTRA) {
+                    if (b.zmin_on) {
+                        near |= fabsf(zs - fcp->zmin2) < fcp->guard_z;
+                        ok &= !(zs < fcp->zmin2);
                     }
-                    near_mask |= (unsigned)near << p;
-                    if (ok & !near) {
-                        const float w12 = q.w * wvh[p];
-                        const unsigned bin = ip * nt + it;
-                        float th, tl;
-                        two_prod(qd.x, qd.y, wvh[p], wvl[p], th, tl);
-                        // summed r_par from the hi + lo distances
-                        const float pv_s = pv + __fmaf_rn(cp[p], qd.z, nbl[p]);
-                        hist_add(h, hs, bin, th, tl, w12, pv_s * w12, (xt + 0.5f) * w12,
-                                 zs * w12, 1);
+                    if (b.zmax_on) {
+                        near |= fabsf(zs - fcp->zmax2) < fcp->guard_z;
+                        ok &= !(zs > fcp->zmax2);
                     }
                 }
-                if (__any_sync(0xffffffffu, near_mask != 0)) {
-#pragma unroll
-                    for (int p = 0; p < kXcfP; ++p) {
-                        const bool near = (near_mask >> p) & 1u;
-                        const unsigned nmask = __ballot_sync(0xffffffffu, near);
-                        if (!nmask) continue;
-                        const int cnt = __popc(nmask);
-                        if (qn + cnt > kQueue) {
-                            xcf_drain(b, fcp, fs, objs, nbr_index, nbr_angle, ctx, queue, qn, h,
-                                      scratch);
-                            rechecks += qn;
-                            ++overflows;
-                            qn = 0;
-                        }
-                        if (near) {
-                            const int pos = qn + __popc(nmask & lt_mask);
-                            queue[pos] = ((uint32_t)i << 16) | (uint32_t)(kb + lane + 32 * p);
-                        }
-                        qn += cnt;
+                near &= in;
+                const bool acc = in & ok & !near;
+                const unsigned bin = ip * nt + it;
+                const bool brk = acc & ((bin != run_bin) | (run_n >= kRunMax));
+                const bool flush = brk & (run_n > 0);
+                if (__any_sync(0xffffffffu, flush)) {
+                    store_runs(flush);
+                    if (flush) {
+                        run_n = 0;
+                        r_xi = r_xil = r_w = r_pw = r_tw = r_zw = 0.f;
                     }
+                }
+                if (brk) run_bin = bin;
+                if (acc) {
+                    const float4 qd = p2[i];
+                    const float w12 = q.w * wvh;
+                    float th, tl;
+                    // delta1 w1 * w2 (py/picca/xcf.py:308) as hi + lo
+                    two_prod(qd.x, qd.y, wvh, wvl, th, tl);
+                    two_sum_into(r_xi, r_xil, th);
+                    r_xil += tl;
+                    r_w += w12;
+                    // summed r_par from the hi + lo distances
+                    const float pv_s = pv + __fmaf_rn(cp, qd.z, nbl);
+                    r_pw = __fmaf_rn(pv_s, w12, r_pw);
+                    r_tw = __fmaf_rn(xt + 0.5f, w12, r_tw);
+                    r_zw = __fmaf_rn(zs, w12, r_zw);
+                    ++run_n;
+                }
+                if (__any_sync(0xffffffffu, near)) {
+                    if (qn > kQueue - 32) {
+                        xcf_drain(b, fcp, fs, objs, nbr_index, nbr_angle, ctx, queue, qn, h,
+                                  scratch);
+                        rechecks += qn;
+                        ++overflows;
+                        qn = 0;
+                    }
+                    const unsigned nmask = __ballot_sync(0xffffffffu, near);
+                    if (near) queue[qn + __popc(nmask & lt_mask)] = ((uint32_t)i << 16) | (uint32_t)kk;
+                    qn += __popc(nmask);
+                }
+                if (tail - head >= 32) {
+                    apply_runs<true>(acc0, acc1, head, 32, h, hs);
+                    head += 32;
                 }
             }
-            if (qn) {
-                xcf_drain(b, fcp, fs, objs, nbr_index, nbr_angle, ctx, queue, qn, h, scratch);
-                rechecks += qn;
+            store_runs(run_n > 0);
+            while (tail - head >= 32) {
+                apply_runs<true>(acc0, acc1, head, 32, h, hs);
+                head += 32;
             }
         }
+        if (qn) {
+            xcf_drain(b, fcp, fs, objs, nbr_index, nbr_angle, ctx, queue, qn, h, scratch);
+            rechecks += qn;
+        }
+        if (tail != head) apply_runs<false>(acc0, acc1, head, tail - head, h, hs);
         __syncthreads();
         flush_rows(h, *fcp, out, row);
         if (threadIdx.x == 0) atomicAdd(&scratch->work_items, 1ull);
@@ -1098,10 +1174,14 @@ int launch_xcf_xi_fast(const Binning &b, double ang_max, const pg_forest_set &fo
                        cudaStream_t stream, LaunchTuning tuning) {
     if (num_work <= 0) return PG_OK;
     FastConst *fc = static_cast<FastConst *>(fast_const);
-    const int block =
-        tuning.warps > 0 && tuning.warps < kXcfBlock / 32 ? tuning.warps * 32 : kXcfBlock;
     const int max_pix1 = forests.max_pixels;
-    const size_t smem = smem_layout(b.nbins, max_pix1, block / 32, false).total;
+    // as many warps (up to kXcfBlock / 32, or the tuned count) as shared
+    // memory leaves room for (histograms, forest, per-warp rings and queues)
+    int nwarps = kXcfBlock / 32;
+    if (tuning.warps > 0 && tuning.warps < nwarps) nwarps = tuning.warps;
+    while (nwarps > 1 && smem_layout(b.nbins, max_pix1, nwarps, true).total > 227 * 1024) --nwarps;
+    const int block = nwarps * 32;
+    const size_t smem = smem_layout(b.nbins, max_pix1, nwarps, true).total;
     if (smem > 227 * 1024) return PG_ERR_UNSUPPORTED;
     (void)ang_max;
     int rc = prepare_fast(b, fc, stream);
