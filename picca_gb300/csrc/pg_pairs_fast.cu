@@ -213,8 +213,15 @@ __device__ __forceinline__ unsigned round_rem(float x, float &rem) {
 // the start). p1: float4 (rho, dist_m, z, w) per forest pixel; p2: float4
 // (delta*w hi, lo, rho lo, 0); queue: the FP64 re-decision entries.
 struct SmemLayout {
-    size_t cells, p1, p2, acc0, acc1, queue, total;
+    size_t cells, p1, p2, acc0, acc1, queue, order, buckets, total;
 };
+
+// The cross-correlation kernel visits a forest's quasars in order of
+// distance (kXcfBuckets buckets of kXcfBucketMpc along the line of sight,
+// relative to the forest's middle pixel) when it has at most kXcfOrderMax.
+constexpr int kXcfOrderMax = 4096;
+constexpr int kXcfBuckets = 128;
+constexpr float kXcfBucketMpc = 8.f;
 
 __host__ __device__ inline SmemLayout smem_layout(int nbins, int max_pix1, int nwarps,
                                                   bool acc_queue) {
@@ -226,7 +233,9 @@ __host__ __device__ inline SmemLayout smem_layout(int nbins, int max_pix1, int n
     l.acc0 = l.p2 + mp * 16;
     l.acc1 = l.acc0 + (acc_queue ? (size_t)nwarps * kAccQ * 16 : 0);
     l.queue = l.acc1 + (acc_queue ? (size_t)nwarps * kAccQ * 16 : 0);
-    l.total = l.queue + (size_t)nwarps * kQueue * 4;
+    l.order = l.queue + (size_t)nwarps * kQueue * 4;
+    l.buckets = l.order + (acc_queue ? (size_t)kXcfOrderMax * 2 : 0);
+    l.total = l.buckets + (acc_queue ? (size_t)kXcfBuckets * 4 : 0);
     return l;
 }
 
@@ -839,6 +848,8 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
     float4 *acc0 = reinterpret_cast<float4 *>(smem + L.acc0) + (size_t)warp * kAccQ;
     float4 *acc1 = reinterpret_cast<float4 *>(smem + L.acc1) + (size_t)warp * kAccQ;
     uint32_t *queue = reinterpret_cast<uint32_t *>(smem + L.queue) + warp * kQueue;
+    uint16_t *qorder = reinterpret_cast<uint16_t *>(smem + L.order);
+    int *buckets = reinterpret_cast<int *>(smem + L.buckets);
     zero_all(h, H_COUNT * hs);
     unsigned long long rechecks = 0, overflows = 0;
 
@@ -864,10 +875,44 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
         ctx.ra1 = fs.ra[f]; ctx.dec1 = fs.dec[f]; ctx.cd1 = fs.cos_dec[f];
         ctx.k0 = nbr_offsets[f];
         const int nq = (int)nq_64;
+        // the quasars in order of distance (a counting sort into buckets),
+        // so that the 32 quasars of a pass cover nearby stretches of the
+        // forest and the passes over quasars that pair with nothing end at
+        // their empty ranges
+        const bool by_distance = nq <= kXcfOrderMax;
+        if (by_distance) {
+            for (int e = threadIdx.x; e < kXcfBuckets; e += blockDim.x) buckets[e] = 0;
+            __syncthreads();
+            auto bucket_of = [&](int k) {
+                const double rq = objs.obj_r_comov[nbr_index[ctx.k0 + k]] - r_ref;
+                const int e = __float2int_rd((float)rq * (1.f / kXcfBucketMpc)) + kXcfBuckets / 2;
+                return e < 0 ? 0 : (e >= kXcfBuckets ? kXcfBuckets - 1 : e);
+            };
+            for (int k = threadIdx.x; k < nq; k += blockDim.x) atomicAdd(&buckets[bucket_of(k)], 1);
+            __syncthreads();
+            if (warp == 0) {  // exclusive prefix sum of the bucket counts
+                int carry = 0;
+                for (int e0 = 0; e0 < kXcfBuckets; e0 += 32) {
+                    const int c = buckets[e0 + lane];
+                    int incl = c;
+#pragma unroll
+                    for (int o = 1; o < 32; o <<= 1) {
+                        const int t2 = __shfl_up_sync(0xffffffffu, incl, o);
+                        if (lane >= o) incl += t2;
+                    }
+                    buckets[e0 + lane] = carry + incl - c;
+                    carry += __shfl_sync(0xffffffffu, incl, 31);
+                }
+            }
+            __syncthreads();
+            for (int k = threadIdx.x; k < nq; k += blockDim.x)
+                qorder[atomicAdd(&buckets[bucket_of(k)], 1)] = (uint16_t)k;
+            __syncthreads();
+        }
         int head = 0, tail = 0;  // run ring of this warp (warp-uniform)
         int qn = 0;              // FP64 re-decision queue of this warp
         for (int kb = warp * 32; kb < nq; kb += nwarps * 32) {
-            const int kk = kb + lane;
+            const int kk = kb + lane < nq ? (by_distance ? (int)qorder[kb + lane] : kb + lane) : nq;
             float cp = 1.f, st = 0.f, nb = kFar, nbl = 0.f, t = kFar, zv = kFar;
             float wvh = 0.f, wvl = 0.f;
             bool valid = false;
