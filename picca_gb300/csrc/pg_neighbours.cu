@@ -27,7 +27,8 @@ struct NbrArgs {
     const double *x2, *y2, *z2, *ra2, *dec2, *zq2, *robj2;
     const int64_t *id2;
     double ang_max;
-    float dot_threshold;
+    float dot_threshold;  // below: certainly farther than ang_max
+    float dot_sure;       // above: certainly closer than ang_max
     // xcf filters
     double zerr_deg, zerr_kms, r_par_min_f, r_par_max_f;
     int32_t zerr_on, precut_on;
@@ -41,16 +42,29 @@ struct Query {
     int64_t id;
 };
 
+// The FP64 angle (and, for the xcf pre-cut, cos(ang / 2)) is formed only
+// where a decision needs it: a pair whose FP32 cosine is above dot_sure is
+// within ang_max whatever the rounding, and a pre-cut whose FP32 estimate is
+// farther than its error bound from the limit has the exact outcome. Both
+// shortcuts give the FP64 decision itself, so the lists are unchanged; they
+// remove the FP64 trigonometry that otherwise runs for almost every
+// candidate (a warp executes it when any of its lanes needs it).
 template <int MODE>
-__device__ __forceinline__ bool is_neighbour(const NbrArgs &a, const Query &q, int64_t g) {
+__device__ __forceinline__ bool is_neighbour(const NbrArgs &a, const Query &q, int64_t g,
+                                             float dot) {
     if (a.id2[g] == q.id) return false;
-    const double ang = angle_between(q.x, q.y, q.z, q.ra, q.dec, q.cosdec, a.x2[g], a.y2[g],
-                                     a.z2[g], a.ra2[g], a.dec2[g]);
-    if (!(ang < a.ang_max)) return false;
+    double ang = -1.0;
+    auto exact_angle = [&]() {
+        if (ang < 0.0)
+            ang = angle_between(q.x, q.y, q.z, q.ra, q.dec, q.cosdec, a.x2[g], a.y2[g], a.z2[g],
+                                a.ra2[g], a.dec2[g]);
+        return ang;
+    };
+    if (!(dot > a.dot_sure) && !(exact_angle() < a.ang_max)) return false;
     if (MODE == 1 && !(q.ra > a.ra2[g])) return false;
     if (MODE == 2) {
         if (a.zerr_on) {
-            const double ang_deg = __dmul_rn(180.0 / kPi, ang);
+            const double ang_deg = __dmul_rn(180.0 / kPi, exact_angle());
             const double zq = a.zq2[g];
             const double z_qq = __dmul_rn(0.5, __dadd_rn(q.zq, zq));
             double dv = fabs(__dsub_rn(q.zq, zq)) / __dadd_rn(1.0, z_qq);
@@ -58,10 +72,24 @@ __device__ __forceinline__ bool is_neighbour(const NbrArgs &a, const Query &q, i
             if (ang_deg < a.zerr_deg && dv < a.zerr_kms) return false;
         }
         if (a.precut_on) {
-            const double c = cos(ang / 2.);
             const double robj = a.robj2[g];
-            if (!(__dmul_rn(__dsub_rn(q.rfirst, robj), c) < a.r_par_max_f)) return false;
-            if (!(__dmul_rn(__dsub_rn(q.rlast, robj), c) > a.r_par_min_f)) return false;
+            const double u1 = __dsub_rn(q.rfirst, robj), u2 = __dsub_rn(q.rlast, robj);
+            // cos(ang / 2) = sqrt((1 + cos ang) / 2) from the FP32 cosine:
+            // within 2e-6 (the cosine to 1e-5 at worst near ang_max, the
+            // square root halving it); the limits are decided from it when
+            // farther than that from the product
+            const float ch = sqrtf(fmaxf(0.5f * (1.f + dot), 0.f));
+            const double e1 = fabs(u1) * 4e-6 + 1e-9, e2 = fabs(u2) * 4e-6 + 1e-9;
+            const double p1 = u1 * (double)ch, p2 = u2 * (double)ch;
+            bool lo_ok, hi_ok;
+            if (p1 < a.r_par_max_f - e1) hi_ok = true;
+            else if (p1 > a.r_par_max_f + e1) hi_ok = false;
+            else hi_ok = __dmul_rn(u1, cos(exact_angle() / 2.)) < a.r_par_max_f;
+            if (!hi_ok) return false;
+            if (p2 > a.r_par_min_f + e2) lo_ok = true;
+            else if (p2 < a.r_par_min_f - e2) lo_ok = false;
+            else lo_ok = __dmul_rn(u2, cos(exact_angle() / 2.)) > a.r_par_min_f;
+            if (!lo_ok) return false;
         }
     }
     return true;
@@ -95,7 +123,7 @@ __device__ __forceinline__ void scan_tile(const NbrArgs &a, const Query &q, floa
         const float dot = __fmaf_rn(fz, t.z, __fmaf_rn(fy, t.y, fx * t.x));
         if (dot <= a.dot_threshold) continue;
         const int64_t g = t0 + k;
-        if (!is_neighbour<MODE>(a, q, g)) continue;
+        if (!is_neighbour<MODE>(a, q, g, dot)) continue;
         if (offsets) index[out + n] = (int32_t)g;
         ++n;
     }
@@ -163,6 +191,13 @@ float dot_threshold(double ang_max) {
     return (float)cos(ang_max) - 1e-5f;
 }
 
+// FP32 unit-vector cosines are accurate to ~4e-7: above this value the FP64
+// angle is below ang_max (2 = never: decide every pair in FP64)
+float dot_sure(double ang_max) {
+    if (ang_max < 1e-3 || ang_max >= kPi) return 2.0f;
+    return (float)cos(ang_max) + 1e-5f;
+}
+
 }  // namespace
 
 int launch_cf_neighbours(const pg_corr_params &p, const pg_forest_set &s1, const pg_forest_set &s2,
@@ -177,6 +212,7 @@ int launch_cf_neighbours(const pg_corr_params &p, const pg_forest_set &s1, const
     a.ra2 = s2.ra; a.dec2 = s2.dec; a.id2 = s2.thingid;
     a.ang_max = p.ang_max;
     a.dot_threshold = dot_threshold(p.ang_max);
+    a.dot_sure = dot_sure(p.ang_max);
     if (a.n1 == 0) return PG_OK;
     if (groups) {
         if (groups->num_blocks <= 0) return PG_OK;
@@ -213,6 +249,7 @@ int launch_xcf_neighbours(const pg_corr_params &p, const pg_forest_set &forests,
     a.id2 = objs.thingid;
     a.ang_max = p.ang_max;
     a.dot_threshold = dot_threshold(p.ang_max);
+    a.dot_sure = dot_sure(p.ang_max);
     a.zerr_on = !isnan(p.zerr_cut_deg) && !isnan(p.zerr_cut_kms);
     a.zerr_deg = p.zerr_cut_deg;
     a.zerr_kms = p.zerr_cut_kms;
