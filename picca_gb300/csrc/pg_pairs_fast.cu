@@ -631,11 +631,23 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                         }
                         tail += __popc(m);
                     };
-                    for (int i = g_lo; i < g_hi; ++i) {
+                    // one pair of the lane's diagonal: its bin and whether it
+                    // is accepted or queued (the geometry of two consecutive
+                    // pairs is evaluated before either enters the run, so
+                    // that their dependency chains overlap)
+                    struct PairEval {
+                        unsigned bin;
+                        int jl;
+                        float pp, xt, zs, w12;
+                        bool acc, near;
+                    };
+                    auto eval = [&](int i, PairEval &e) {
                         bool in = (i >= ia) & (i < ib);
-                        if (EXTRA && zerr_pair) in &= ((veto1[i >> 5] >> (i & 31)) & 1u) == 0u;
+                        if (EXTRA && zerr_pair && in) in = ((veto1[i >> 5] >> (i & 31)) & 1u) == 0u;
                         const int jl = in ? i + joff : 0;
-                        const float4 q1 = p1[i];
+                        // i <= g_hi <= n1: the clamp keeps the (unused) read of
+                        // a lane past its range inside forest 1
+                        const float4 q1 = p1[min(i, n1 - 1)];
                         const float4 q2 = buf[jl];
                         const float pp = __fmaf_rn(cp, q1.x, q2.x);
                         const float v = fabsf(pp);
@@ -661,8 +673,8 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                             it = round_rem(xt, ft);
                             near = (fabsf(fp) > h_par) | (fabsf(ft) > h_tr);
                         }
-                        // a pixel without weight or vetoed (w staged as 0) pairs with
-                        // nothing: neither accepted nor queued for re-decision
+                        // a pixel without weight or vetoed (w staged as 0) pairs
+                        // with nothing: neither accepted nor queued
                         in &= (q1.w != 0.f) & (q2.w != 0.f);
                         bool ok = (ip < np) & (it < nt);
                         const float zs = q1.z + q2.z;
@@ -681,9 +693,19 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                             }
                         }
                         near &= in;
-                        const bool acc = in & ok & !near;
-                        const unsigned bin = ip * nt + it;
-                        const bool brk = acc & ((bin != run_bin) | (run_n >= kRunMax));
+                        e.acc = in & ok & !near;
+                        e.near = near;
+                        e.bin = ip * nt + it;
+                        e.jl = jl;
+                        e.pp = pp;
+                        e.xt = xt;
+                        e.zs = zs;
+                        e.w12 = q1.w * q2.w;
+                    };
+                    // the pair enters the lane's run (a new run when its bin
+                    // differs or the run is full)
+                    auto take = [&](const PairEval &e, int i) {
+                        const bool brk = e.acc & ((e.bin != run_bin) | (run_n >= kRunMax));
                         const bool flush = brk & (run_n > 0);
                         if (__any_sync(0xffffffffu, flush)) {
                             store_runs(flush);
@@ -691,12 +713,16 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                                 run_n = 0;
                                 r_xi = r_xil = r_w = r_pw = r_tw = r_zw = 0.f;
                             }
+                            if (tail - head >= 32) {
+                                apply_runs<true>(acc0, acc1, head, 32, h, hs);
+                                head += 32;
+                            }
                         }
-                        if (brk) run_bin = bin;
-                        if (acc) {
+                        if (brk) run_bin = e.bin;
+                        if (e.acc) {
                             const float4 x1 = p1x[i];
-                            const float4 x2 = bufx[jl];
-                            const float w12 = q1.w * q2.w;
+                            const float4 x2 = bufx[e.jl];
+                            const float w12 = e.w12;
                             float th, tl;
                             two_prod(x1.x, x1.y, x2.x, x2.y, th, tl);
                             two_sum_into(r_xi, r_xil, th);
@@ -704,39 +730,46 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                             r_w += w12;
                             // r_par (bin units) from the hi + lo distances:
                             // relative precision for the summed r_par
+                            const float pp_s = e.pp + __fmaf_rn(cp, x1.z, x2.z);
                             if (RMU) {
                                 // r and mu from the hi + lo distances: the
                                 // staged r_par carries an absolute error that
                                 // is large relative to a small r
-                                const float pp_s = pp + __fmaf_rn(cp, x1.z, x2.z);
-                                const float r2s = __fmaf_rn(pp_s, pp_s, xt * xt);
+                                const float r2s = __fmaf_rn(pp_s, pp_s, e.xt * e.xt);
                                 const float ss = rsqrtf(r2s);
                                 r_pw = __fmaf_rn((AUTO ? fabsf(pp_s) : pp_s) * ss, w12, r_pw);
                                 r_tw = __fmaf_rn(r2s * ss, w12, r_tw);
                             } else {
-                                const float pp_s = pp + __fmaf_rn(cp, x1.z, x2.z);
                                 r_pw = __fmaf_rn(AUTO ? fabsf(pp_s) : pp_s, w12, r_pw);
-                                r_tw = __fmaf_rn(xt + 0.5f, w12, r_tw);
+                                r_tw = __fmaf_rn(e.xt + 0.5f, w12, r_tw);
                             }
-                            r_zw = __fmaf_rn(zs, w12, r_zw);
+                            r_zw = __fmaf_rn(e.zs, w12, r_zw);
                             ++run_n;
                         }
-                        if (__any_sync(0xffffffffu, near)) {
+                    };
+                    for (int i = g_lo; i < g_hi; i += 2) {
+                        PairEval ea, eb;
+                        eval(i, ea);
+                        eval(i + 1, eb);  // i + 1 = g_hi: outside every lane's range
+                        take(ea, i);
+                        take(eb, i + 1);
+                        if (__any_sync(0xffffffffu, ea.near | eb.near)) {
                             // rare path: queue the pairs near an edge for FP64 re-decision
-                            if (qn > kCfQueue - 32) {
+                            if (qn > kCfQueue - 64) {
                                 cf_drain(b, fcp, s1, s2, ctx, queue, qn, h, scratch);
                                 if (lane == 0) atomicAdd(&scratch->recheck_overflows, 1ull);
                                 qn = 0;
                             }
-                            const unsigned nmask = __ballot_sync(0xffffffffu, near);
-                            if (near)
+                            unsigned nmask = __ballot_sync(0xffffffffu, ea.near);
+                            if (ea.near)
                                 queue[qn + __popc(nmask & lt_mask)] =
                                     ((uint32_t)i << 16) | (uint32_t)(i + d);
                             qn += __popc(nmask);
-                        }
-                        if (tail - head >= 32) {
-                            apply_runs<true>(acc0, acc1, head, 32, h, hs);
-                            head += 32;
+                            nmask = __ballot_sync(0xffffffffu, eb.near);
+                            if (eb.near)
+                                queue[qn + __popc(nmask & lt_mask)] =
+                                    ((uint32_t)(i + 1) << 16) | (uint32_t)(i + 1 + d);
+                            qn += __popc(nmask);
                         }
                     }
                     store_runs(run_n > 0);
