@@ -608,7 +608,13 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                         }
                         ib = lo;
                     }
-                    int g_lo = ia < ib ? ia : INT_MAX, g_hi = ia < ib ? ib : INT_MIN;
+                    // the lanes step the chunk's pixel together (s = j - jc, a
+                    // broadcast read) and each its own forest-1 pixel
+                    // i = s - joff: their ranges of s share the chunk's ends
+                    // and differ only where forest 1 ends or the sweep is
+                    // trimmed
+                    const int sa = ia + joff, sb = ib + joff;  // empty when ia >= ib
+                    int g_lo = ia < ib ? sa : INT_MAX, g_hi = ia < ib ? sb : INT_MIN;
 #pragma unroll
                     for (int o = 16; o > 0; o >>= 1) {
                         g_lo = min(g_lo, __shfl_xor_sync(0xffffffffu, g_lo, o));
@@ -637,18 +643,18 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                     // that their dependency chains overlap)
                     struct PairEval {
                         unsigned bin;
-                        int jl;
+                        int i;
                         float pp, xt, zs, w12;
                         bool acc, near;
                     };
-                    auto eval = [&](int i, PairEval &e) {
-                        bool in = (i >= ia) & (i < ib);
+                    auto eval = [&](int js, PairEval &e) {
+                        bool in = (js >= sa) & (js < sb);
+                        const int i = in ? js - joff : 0;
                         if (EXTRA && zerr_pair && in) in = ((veto1[i >> 5] >> (i & 31)) & 1u) == 0u;
-                        const int jl = in ? i + joff : 0;
-                        // i <= g_hi <= n1: the clamp keeps the (unused) read of
-                        // a lane past its range inside forest 1
-                        const float4 q1 = p1[min(i, n1 - 1)];
-                        const float4 q2 = buf[jl];
+                        // js <= g_hi <= jn: the clamp keeps the (unused) read
+                        // one past the group's range inside the chunk
+                        const float4 q1 = p1[i];
+                        const float4 q2 = buf[min(js, jn - 1)];
                         const float pp = __fmaf_rn(cp, q1.x, q2.x);
                         const float v = fabsf(pp);
                         const float pv = AUTO ? v : pp;
@@ -696,7 +702,7 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                         e.acc = in & ok & !near;
                         e.near = near;
                         e.bin = ip * nt + it;
-                        e.jl = jl;
+                        e.i = i;
                         e.pp = pp;
                         e.xt = xt;
                         e.zs = zs;
@@ -704,7 +710,7 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                     };
                     // the pair enters the lane's run (a new run when its bin
                     // differs or the run is full)
-                    auto take = [&](const PairEval &e, int i) {
+                    auto take = [&](const PairEval &e, int js) {
                         const bool brk = e.acc & ((e.bin != run_bin) | (run_n >= kRunMax));
                         const bool flush = brk & (run_n > 0);
                         if (__any_sync(0xffffffffu, flush)) {
@@ -720,8 +726,8 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                         }
                         if (brk) run_bin = e.bin;
                         if (e.acc) {
-                            const float4 x1 = p1x[i];
-                            const float4 x2 = bufx[e.jl];
+                            const float4 x1 = p1x[e.i];
+                            const float4 x2 = bufx[js];
                             const float w12 = e.w12;
                             float th, tl;
                             two_prod(x1.x, x1.y, x2.x, x2.y, th, tl);
@@ -747,12 +753,12 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                             ++run_n;
                         }
                     };
-                    for (int i = g_lo; i < g_hi; i += 2) {
+                    for (int js = g_lo; js < g_hi; js += 2) {
                         PairEval ea, eb;
-                        eval(i, ea);
-                        eval(i + 1, eb);  // i + 1 = g_hi: outside every lane's range
-                        take(ea, i);
-                        take(eb, i + 1);
+                        eval(js, ea);
+                        eval(js + 1, eb);  // js + 1 = g_hi: outside every lane's range
+                        take(ea, js);
+                        take(eb, js + 1);
                         if (__any_sync(0xffffffffu, ea.near | eb.near)) {
                             // rare path: queue the pairs near an edge for FP64 re-decision
                             if (qn > kCfQueue - 64) {
@@ -763,12 +769,12 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                             unsigned nmask = __ballot_sync(0xffffffffu, ea.near);
                             if (ea.near)
                                 queue[qn + __popc(nmask & lt_mask)] =
-                                    ((uint32_t)i << 16) | (uint32_t)(i + d);
+                                    ((uint32_t)ea.i << 16) | (uint32_t)(ea.i + d);
                             qn += __popc(nmask);
                             nmask = __ballot_sync(0xffffffffu, eb.near);
                             if (eb.near)
                                 queue[qn + __popc(nmask & lt_mask)] =
-                                    ((uint32_t)(i + 1) << 16) | (uint32_t)(i + 1 + d);
+                                    ((uint32_t)eb.i << 16) | (uint32_t)(eb.i + d);
                             qn += __popc(nmask);
                         }
                     }
