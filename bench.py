@@ -44,9 +44,9 @@ METRIC = "cf pixel-pairs/s at stated FP64-oracle error; continuum fits/s plain v
 # DRAM bytes (read + write) of the pair kernel per candidate pixel pair, from
 # an ncu capture of the kernel on a sample of work items (profiles/); the
 # roofline entry scales it to the launch by the candidate pairs processed.
-# Captured on 200 random work items of the 400k-forest survey: 1.251 GB for
-# 5.41e9 candidate pixel pairs.
-PAIR_DRAM_BYTES_PER_CANDIDATE = 0.2314
+# Captured on 200 random work items of the 400k-forest survey: 1.249 GB for
+# 5.405e9 candidate pixel pairs.
+PAIR_DRAM_BYTES_PER_CANDIDATE = 0.2311
 PAIR_TRAFFIC_SOURCE = ("ncu dram__bytes_read.sum + dram__bytes_write.sum of cf_xi_diag_kernel "
                        "on 200 random work items of this survey, scaled by candidate pairs "
                        "(profiles/cf_xi_diag_kernel_400k_survey_sample.md)")
