@@ -377,11 +377,13 @@ __host__ __device__ inline CfSmem cf_smem(int nbins, int max_pix1, int nwarps) {
 // form diagonal d; along it r1 - r2 and d1 + d2 change slowly (pixels on the
 // same wavelength grid), so consecutive pairs of a diagonal share their bin
 // for tens of steps. A lane owns one diagonal of a group of 32 consecutive
-// ones and steps i with the others (forest-1 pixel i is a broadcast read of
-// shared memory, forest-2 pixel i + d a read of the warp's staged chunk),
-// summing consecutive accepted pairs of one bin in registers (a run); a run
-// goes to the block histogram only when its bin changes, through a ring
-// that applies 32 runs with every lane active.
+// ones and steps along it with the others, two pairs per step: the lanes
+// share the forest-2 pixel j of the warp's staged chunk (a broadcast read of
+// shared memory) and each reads its own forest-1 pixel i = j - d, so that
+// the group's ranges share the chunk's ends. Consecutive accepted pairs of
+// one bin are summed in registers (a run); a run goes to the block
+// histogram only when its bin changes, through a ring that applies 32 runs
+// with every lane active.
 //
 // Work skipped, every skip exact: forest 2 is staged in chunks of kChunk
 // pixels; per chunk, binary searches give for every forest-1 pixel i the
