@@ -74,20 +74,23 @@ __device__ __forceinline__ bool is_neighbour(const NbrArgs &a, const Query &q, i
         if (a.precut_on) {
             const double robj = a.robj2[g];
             const double u1 = __dsub_rn(q.rfirst, robj), u2 = __dsub_rn(q.rlast, robj);
-            // cos(ang / 2) = sqrt((1 + cos ang) / 2) from the FP32 cosine:
-            // within 2e-6 (the cosine to 1e-5 at worst near ang_max, the
-            // square root halving it); the limits are decided from it when
-            // farther than that from the product
-            const float ch = sqrtf(fmaxf(0.5f * (1.f + dot), 0.f));
+            // cos(ang / 2) = sqrt(x), x = (1 + cos ang) / 2, from the FP32
+            // cosine (within 4e-7): for x >= 1/4 (ang <= 120 deg) its
+            // relative error is below 1e-6, and a limit farther than 4e-6
+            // of |u| from the product is decided from it; otherwise (and
+            // for wider angles) the FP64 cos(ang / 2) decides
+            const float xh = 0.5f * (1.f + dot);
+            const bool est = xh >= 0.25f;
+            const float ch = sqrtf(fmaxf(xh, 0.f));
             const double e1 = fabs(u1) * 4e-6 + 1e-9, e2 = fabs(u2) * 4e-6 + 1e-9;
             const double p1 = u1 * (double)ch, p2 = u2 * (double)ch;
             bool lo_ok, hi_ok;
-            if (p1 < a.r_par_max_f - e1) hi_ok = true;
-            else if (p1 > a.r_par_max_f + e1) hi_ok = false;
+            if (est && p1 < a.r_par_max_f - e1) hi_ok = true;
+            else if (est && p1 > a.r_par_max_f + e1) hi_ok = false;
             else hi_ok = __dmul_rn(u1, cos(exact_angle() / 2.)) < a.r_par_max_f;
             if (!hi_ok) return false;
-            if (p2 > a.r_par_min_f + e2) lo_ok = true;
-            else if (p2 < a.r_par_min_f - e2) lo_ok = false;
+            if (est && p2 > a.r_par_min_f + e2) lo_ok = true;
+            else if (est && p2 < a.r_par_min_f - e2) lo_ok = false;
             else lo_ok = __dmul_rn(u2, cos(exact_angle() / 2.)) > a.r_par_min_f;
             if (!lo_ok) return false;
         }
