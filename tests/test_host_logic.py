@@ -116,3 +116,25 @@ def test_neighbour_groups_cover_every_neighbour():
             covered[first:end] += 1
             assert np.all(grp1[first:end] == grp)
         assert np.all(covered == 1)
+
+
+def test_tuning_cache_round_trip(tmp_path, monkeypatch):
+    """The launch-shape cache: JSON round trip, a damaged file reads as
+    empty, and the environment variable moves the cache."""
+    from picca_gb300 import autotune
+    path = str(tmp_path / "sub" / "tuning.json")
+    table = {"GB300|cf|bins=2500|grid=log|mode=1": {
+        "choice": [16, 0], "sample_items": 2000,
+        "alternatives": [{"warps": 0, "ctas_per_sm": 0, "ms": 80.0},
+                         {"warps": 16, "ctas_per_sm": 0, "ms": 79.0}]}}
+    autotune._save(path, table)
+    assert autotune._load(path) == table
+    assert not [f for f in os.listdir(tmp_path / "sub") if ".tmp" in f]
+    with open(path, "w") as fh:
+        fh.write("{not json")
+    assert autotune._load(path) == {}
+    assert autotune._load(str(tmp_path / "missing.json")) == {}
+    monkeypatch.setenv("PICCA_GB300_TUNE_CACHE", path)
+    assert autotune.default_cache_path() == path
+    monkeypatch.delenv("PICCA_GB300_TUNE_CACHE")
+    assert autotune.default_cache_path().endswith(os.path.join("picca_gb300", "pair_tuning.json"))
