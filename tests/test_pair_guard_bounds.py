@@ -1,0 +1,77 @@
+"""The guard bands of the precision-form pair kernel
+(picca_gb300/csrc/pg_pairs_fast.cu: make_fast_const, stage_forest1, the
+chunk staging and the per-pair FMAs), checked on the CPU: the kernel's FP32
+evaluation of the bin coordinates x' (r_par) and x_tr' (r_trans), emulated
+with FP32 roundings and single-rounding FMAs, stays within the guard bands
+of the exact (FP64) values for every pixel pair within one bin of the
+accepted ranges. A pair outside its band is decided from FP32 alone, so this
+is what makes the FP32 bins equal to the reference's FP64 bins."""
+
+import numpy as np
+
+from picca_gb300 import synthetic
+
+f32 = np.float32
+U = 2.0 ** -24
+
+
+def _fma32(a, b, c):
+    # products of FP32 values are exact in FP64; one rounding to FP32
+    return (a.astype(np.float64) * b.astype(np.float64) + np.float64(c)).astype(f32)
+
+
+def _guards(np_, nt, r_par_min, r_par_range, r_trans_max, max_rho):
+    inv_p = np_ / r_par_range
+    pmin = r_par_min * inv_p
+    g_par = 16 * U * (np_ + abs(pmin) + 2) + 1e-6 + 8 * U * inv_p * max_rho
+    g_tr = 16 * U * (nt + 2) + 1e-6
+    return g_par, g_tr
+
+
+def test_fp32_bin_coordinates_within_guards():
+    np_, nt, r_par_max, r_trans_max = 50, 50, 200.0, 200.0
+    fs = synthetic.make_forests(400, 17, (150.0, 156.0), (0.0, 6.0), 2.1, 3.5, "uniform")
+    ang_max = synthetic.correlation_ang_max(r_trans_max, float(fs.z.min()))
+    inv_p, inv_t = np_ / r_par_max, nt / r_trans_max
+    pc = f32(0.5)
+    v = np.stack([fs.x_cart, fs.y_cart, fs.z_cart], axis=1)
+    rng = np.random.default_rng(3)
+    checked = 0
+    worst_par = worst_tr = 0.0
+    for f1 in rng.choice(fs.num, size=60, replace=False):
+        cosang = np.clip(v @ v[f1], -1, 1)
+        nbrs = np.nonzero((np.arccos(cosang) < ang_max) & (np.arange(fs.num) != f1))[0][:20]
+        a0, a1 = fs.pix_offset[f1], fs.pix_offset[f1 + 1]
+        r1, d1 = fs.r_comov[a0:a1], fs.dist_m[a0:a1]
+        r_ref = r1[(a1 - a0) // 2]
+        rho1 = (r1 - r_ref).astype(f32)
+        max_rho = float(np.abs(rho1).max())
+        g_par, g_tr = _guards(np_, nt, 0.0, r_par_max, r_trans_max, max_rho)
+        for g in nbrs:
+            ang = float(np.arccos(cosang[g]))
+            c, s = np.cos(ang / 2), np.sin(ang / 2)
+            cp, st = f32(c * inv_p), f32(s * inv_t)
+            b0, b1 = fs.pix_offset[g], fs.pix_offset[g + 1]
+            r2, d2 = fs.r_comov[b0:b1], fs.dist_m[b0:b1]
+            # chunk staging: nB = -(cp * rho2) rounded once, t = st d2 - 1/2 (FMA)
+            nb = (-(cp.astype(np.float64) * (r2 - r_ref).astype(f32).astype(np.float64))).astype(f32)
+            t = _fma32(np.full(b1 - b0, st), d2.astype(f32), -0.5)
+            # per pair: p = cp rho1 + nB (FMA), x' = |p| - pc; x_tr' = st d1 + t (FMA)
+            p = _fma32(np.full((a1 - a0, b1 - b0), cp), rho1[:, None], nb[None, :])
+            xp = (np.abs(p) - pc).astype(f32)
+            xt = _fma32(np.full((a1 - a0, b1 - b0), st), d1.astype(f32)[:, None], t[None, :])
+            # the reference's FP64 values in the same units
+            x_exact = np.abs((r1[:, None] - r2[None, :]) * c) * inv_p - 0.5
+            xt_exact = (d1[:, None] + d2[None, :]) * s * inv_t - 0.5
+            keep = (x_exact >= -1) & (x_exact <= np_ + 1) & (xt_exact >= -1) & (xt_exact <= nt + 1)
+            err_par = np.abs(xp.astype(np.float64) - x_exact)[keep]
+            err_tr = np.abs(xt.astype(np.float64) - xt_exact)[keep]
+            if err_par.size:
+                assert err_par.max() < g_par, (err_par.max(), g_par)
+                assert err_tr.max() < g_tr, (err_tr.max(), g_tr)
+                worst_par = max(worst_par, err_par.max() / g_par)
+                worst_tr = max(worst_tr, err_tr.max() / g_tr)
+                checked += err_par.size
+    assert checked > 100_000
+    # the bands are not vacuous: the errors use a sizeable part of them
+    assert worst_par > 0.01 and worst_tr > 0.01
