@@ -75,3 +75,54 @@ def test_fp32_bin_coordinates_within_guards():
     assert checked > 100_000
     # the bands are not vacuous: the errors use a sizeable part of them
     assert worst_par > 0.01 and worst_tr > 0.01
+
+
+def test_fp32_cross_bin_coordinates_within_guards():
+    """The delta x quasar form (xcf_xi_fast_kernel): signed r_par from -200
+    to 200 in 100 bins, the quasar staged as nB = -cp rho_q and
+    t = st d_q - 1/2, per pixel p = cp rho1 + nB and x_tr' = st d1 + t."""
+    np_, nt, r_par_min, r_par_max, r_trans_max = 100, 50, -200.0, 200.0, 200.0
+    fs = synthetic.make_forests(300, 21, (150.0, 156.0), (0.0, 6.0), 2.1, 3.5, "uniform")
+    qs = synthetic.make_quasars(600, 22, (150.0, 156.0), (0.0, 6.0))
+    ang_max = synthetic.correlation_ang_max(r_trans_max, float(fs.z.min()))
+    inv_p, inv_t = np_ / (r_par_max - r_par_min), nt / r_trans_max
+    pmin = r_par_min * inv_p
+    pc = f32(pmin + 0.5)
+    vq = np.stack([qs.x_cart, qs.y_cart, qs.z_cart], axis=1)
+    rng = np.random.default_rng(4)
+    checked = 0
+    worst_par = worst_tr = 0.0
+    for f1 in rng.choice(fs.num, size=80, replace=False):
+        v1 = np.array([fs.x_cart[f1], fs.y_cart[f1], fs.z_cart[f1]])
+        cosang = np.clip(vq @ v1, -1, 1)
+        nbrs = np.nonzero(np.arccos(cosang) < ang_max)[0]
+        a0, a1 = fs.pix_offset[f1], fs.pix_offset[f1 + 1]
+        r1, d1 = fs.r_comov[a0:a1], fs.dist_m[a0:a1]
+        r_ref = r1[(a1 - a0) // 2]
+        rho1 = (r1 - r_ref).astype(f32)
+        g_par, g_tr = _guards(np_, nt, r_par_min, r_par_max - r_par_min, r_trans_max,
+                              float(np.abs(rho1).max()))
+        if not nbrs.size:
+            continue
+        ang = np.arccos(cosang[nbrs])
+        c, s = np.cos(ang / 2), np.sin(ang / 2)
+        cp, st = (c * inv_p).astype(f32), (s * inv_t).astype(f32)
+        rq, dq = qs.obj_r_comov[nbrs], qs.obj_dist_m[nbrs]
+        nb = (-(cp.astype(np.float64) * (rq - r_ref).astype(f32).astype(np.float64))).astype(f32)
+        t = _fma32(st, dq.astype(f32), -0.5)
+        p = _fma32(cp[None, :], rho1[:, None], nb[None, :])
+        xp = (p - pc).astype(f32)
+        xt = _fma32(st[None, :], d1.astype(f32)[:, None], t[None, :])
+        x_exact = (r1[:, None] - rq[None, :]) * c[None, :] * inv_p - pmin - 0.5
+        xt_exact = (d1[:, None] + dq[None, :]) * s[None, :] * inv_t - 0.5
+        keep = (x_exact >= -1) & (x_exact <= np_ + 1) & (xt_exact >= -1) & (xt_exact <= nt + 1)
+        err_par = np.abs(xp.astype(np.float64) - x_exact)[keep]
+        err_tr = np.abs(xt.astype(np.float64) - xt_exact)[keep]
+        if err_par.size:
+            assert err_par.max() < g_par, (err_par.max(), g_par)
+            assert err_tr.max() < g_tr, (err_tr.max(), g_tr)
+            worst_par = max(worst_par, err_par.max() / g_par)
+            worst_tr = max(worst_tr, err_tr.max() / g_tr)
+            checked += err_par.size
+    assert checked > 20_000
+    assert worst_par > 0.01 and worst_tr > 0.01
