@@ -1026,9 +1026,19 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
                 }
                 tail += __popc(m);
             };
-            for (int i = g_lo; i < g_hi; ++i) {
-                const float4 q = p1[i];
-                bool in = (i >= ia) & (i < ib) & (q.w != 0.f);
+            // one forest pixel against this lane's quasar; two consecutive
+            // pixels are evaluated before either enters the run, so that
+            // their dependency chains overlap
+            struct PairEval {
+                unsigned bin;
+                float pv, xt, zs, w;
+                bool acc, near;
+            };
+            auto eval = [&](int i, PairEval &e) {
+                // i <= g_hi <= n1: the clamp keeps the (unused) read one
+                // past the group's range inside the forest
+                const float4 q = p1[min(i, n1 - 1)];
+                const bool in = (i >= ia) & (i < ib) & (q.w != 0.f);
                 const float pv = __fmaf_rn(cp, q.x, nb);
                 const float xt = __fmaf_rn(st, q.y, t);
                 float fp, ft;
@@ -1048,9 +1058,16 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
                     }
                 }
                 near &= in;
-                const bool acc = in & ok & !near;
-                const unsigned bin = ip * nt + it;
-                const bool brk = acc & ((bin != run_bin) | (run_n >= kRunMax));
+                e.acc = in & ok & !near;
+                e.near = near;
+                e.bin = ip * nt + it;
+                e.pv = pv;
+                e.xt = xt;
+                e.zs = zs;
+                e.w = q.w;
+            };
+            auto take = [&](const PairEval &e, int i) {
+                const bool brk = e.acc & ((e.bin != run_bin) | (run_n >= kRunMax));
                 const bool flush = brk & (run_n > 0);
                 if (__any_sync(0xffffffffu, flush)) {
                     store_runs(flush);
@@ -1058,11 +1075,15 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
                         run_n = 0;
                         r_xi = r_xil = r_w = r_pw = r_tw = r_zw = 0.f;
                     }
+                    if (tail - head >= 32) {
+                        apply_runs<true>(acc0, acc1, head, 32, h, hs);
+                        head += 32;
+                    }
                 }
-                if (brk) run_bin = bin;
-                if (acc) {
+                if (brk) run_bin = e.bin;
+                if (e.acc) {
                     const float4 qd = p2[i];
-                    const float w12 = q.w * wvh;
+                    const float w12 = e.w * wvh;
                     float th, tl;
                     // delta1 w1 * w2 (py/picca/xcf.py:308) as hi + lo
                     two_prod(qd.x, qd.y, wvh, wvl, th, tl);
@@ -1070,27 +1091,36 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
                     r_xil += tl;
                     r_w += w12;
                     // summed r_par from the hi + lo distances
-                    const float pv_s = pv + __fmaf_rn(cp, qd.z, nbl);
+                    const float pv_s = e.pv + __fmaf_rn(cp, qd.z, nbl);
                     r_pw = __fmaf_rn(pv_s, w12, r_pw);
-                    r_tw = __fmaf_rn(xt + 0.5f, w12, r_tw);
-                    r_zw = __fmaf_rn(zs, w12, r_zw);
+                    r_tw = __fmaf_rn(e.xt + 0.5f, w12, r_tw);
+                    r_zw = __fmaf_rn(e.zs, w12, r_zw);
                     ++run_n;
                 }
-                if (__any_sync(0xffffffffu, near)) {
-                    if (qn > kQueue - 32) {
+            };
+            for (int i = g_lo; i < g_hi; i += 2) {
+                PairEval ea, eb;
+                eval(i, ea);
+                eval(i + 1, eb);  // i + 1 = g_hi: outside every lane's range
+                take(ea, i);
+                take(eb, i + 1);
+                if (__any_sync(0xffffffffu, ea.near | eb.near)) {
+                    if (qn > kQueue - 64) {
                         xcf_drain(b, fcp, fs, objs, nbr_index, nbr_angle, ctx, queue, qn, h,
                                   scratch);
                         rechecks += qn;
                         ++overflows;
                         qn = 0;
                     }
-                    const unsigned nmask = __ballot_sync(0xffffffffu, near);
-                    if (near) queue[qn + __popc(nmask & lt_mask)] = ((uint32_t)i << 16) | (uint32_t)kk;
+                    unsigned nmask = __ballot_sync(0xffffffffu, ea.near);
+                    if (ea.near)
+                        queue[qn + __popc(nmask & lt_mask)] = ((uint32_t)i << 16) | (uint32_t)kk;
                     qn += __popc(nmask);
-                }
-                if (tail - head >= 32) {
-                    apply_runs<true>(acc0, acc1, head, 32, h, hs);
-                    head += 32;
+                    nmask = __ballot_sync(0xffffffffu, eb.near);
+                    if (eb.near)
+                        queue[qn + __popc(nmask & lt_mask)] =
+                            ((uint32_t)(i + 1) << 16) | (uint32_t)kk;
+                    qn += __popc(nmask);
                 }
             }
             store_runs(run_n > 0);
