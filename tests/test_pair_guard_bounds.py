@@ -126,3 +126,80 @@ def test_fp32_cross_bin_coordinates_within_guards():
             checked += err_par.size
     assert checked > 20_000
     assert worst_par > 0.01 and worst_tr > 0.01
+
+
+def _move_ulps(x, k):
+    bits = x.view(np.int32).astype(np.int64) + k
+    return bits.astype(np.int32).view(f32)
+
+
+def _round_rem(x):
+    # round to nearest even (the kernel's magic-number add) and the remainder
+    r = np.rint(x.astype(np.float64))
+    return r.astype(np.int64), (x.astype(np.float64) - r)
+
+
+def test_fp32_rmu_bins_outside_guards_equal_fp64():
+    """r-mu binning (auto, mu in [0, 1] in 50 bins, r in [0, 200] in 50): the
+    kernel's FP32 r = r2 rsqrt(r2) and mu = |p| rsqrt(r2), with rsqrtf taken
+    up to 2 units in the last place off (its documented error); every pair
+    that the kernel does not queue for the FP64 re-decision gets the FP64
+    bins and acceptance."""
+    np_, nt, r_trans_max = 50, 50, 200.0
+    fs = synthetic.make_forests(300, 23, (150.0, 156.0), (0.0, 6.0), 2.1, 3.5, "uniform")
+    ang_max = synthetic.correlation_ang_max(r_trans_max, float(fs.z.min()))
+    inv_t = nt / r_trans_max
+    inv_mu, mu_off = f32(np_ / 1.0), f32(0.5)
+    g_mu0 = 16 * U * (np_ + 2) + 1e-6
+    g_tr = 32 * U * (nt + 2) + 1e-6
+    v = np.stack([fs.x_cart, fs.y_cart, fs.z_cart], axis=1)
+    rng = np.random.default_rng(5)
+    checked = queued = 0
+    for f1 in rng.choice(fs.num, size=40, replace=False):
+        cosang = np.clip(v @ v[f1], -1, 1)
+        nbrs = np.nonzero((np.arccos(cosang) < ang_max) & (np.arange(fs.num) != f1))[0][:12]
+        a0, a1 = fs.pix_offset[f1], fs.pix_offset[f1 + 1]
+        r1, d1 = fs.r_comov[a0:a1], fs.dist_m[a0:a1]
+        r_ref = r1[(a1 - a0) // 2]
+        rho1 = (r1 - r_ref).astype(f32)
+        g = min(16 * U * (nt + 2) + 1e-6 + 8 * U * inv_t * float(np.abs(rho1).max()), 0.05)
+        low_clamp = f32(-0.5 + 2 * g)
+        h_r = f32(0.5 - g_tr - g)
+        for k in nbrs:
+            ang = float(np.arccos(cosang[k]))
+            c, s = np.cos(ang / 2), np.sin(ang / 2)
+            cp, st = f32(c * inv_t), f32(s * inv_t)
+            b0, b1 = fs.pix_offset[k], fs.pix_offset[k + 1]
+            r2, d2 = fs.r_comov[b0:b1], fs.dist_m[b0:b1]
+            nb = (-(np.float64(cp) * (r2 - r_ref).astype(f32).astype(np.float64))).astype(f32)
+            t2 = (np.float64(st) * d2.astype(f32).astype(np.float64)).astype(f32)
+            shape = (a1 - a0, b1 - b0)
+            pp = _fma32(np.full(shape, cp), rho1[:, None], nb[None, :])
+            xt = _fma32(np.full(shape, st), d1.astype(f32)[:, None], t2[None, :])
+            rr = _fma32(pp, pp, (xt.astype(np.float64) ** 2).astype(f32))
+            sinv = _move_ulps((1.0 / np.sqrt(rr.astype(np.float64))).astype(f32),
+                              rng.integers(-2, 3, shape))
+            ru = (rr.astype(np.float64) * sinv).astype(f32)
+            mu = (np.abs(pp).astype(np.float64) * sinv).astype(f32)
+            xm = np.maximum(_fma32(mu, inv_mu, -mu_off), low_clamp)
+            ip, fp = _round_rem(xm)
+            it, ft = _round_rem((ru - f32(0.5)).astype(f32))
+            gm = _fma32((f32(g) * sinv).astype(f32), inv_mu, g_mu0)
+            near = ~(gm < 0.25) | (np.abs(fp) > 0.5 - gm) | (np.abs(ft) > h_r)
+            acc32 = (ip >= 0) & (ip < np_) & (it >= 0) & (it < nt)
+            # the reference: r and mu from the FP64 r_par, r_trans
+            rp = (r1[:, None] - r2[None, :]) * c
+            rt = (d1[:, None] + d2[None, :]) * s
+            r = np.sqrt(rp ** 2 + rt ** 2)
+            with np.errstate(invalid="ignore", divide="ignore"):
+                mu64 = np.abs(rp) / r
+            bmu, br = np.floor(mu64 * np_).astype(np.int64), np.floor(r * inv_t).astype(np.int64)
+            acc64 = (r > 0) & (bmu < np_) & (br < nt)
+            sure = ~near & (r > 0)
+            assert np.array_equal(acc32[sure], acc64[sure])
+            both = sure & acc64
+            assert np.array_equal(ip[both], bmu[both]) and np.array_equal(it[both], br[both])
+            checked += int(sure.sum())
+            queued += int(near.sum())
+    assert checked > 100_000
+    assert queued < 0.01 * checked
