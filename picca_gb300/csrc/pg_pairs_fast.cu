@@ -63,6 +63,10 @@ namespace {
 constexpr float kMagic = 12582912.0f;        // 1.5 * 2^23
 constexpr unsigned kMagicBits = 0x4B400000u;  // bits of 1.5 * 2^23
 constexpr float kFar = 1e30f;                 // nB, t and z of an empty slot
+// cos(1e-3): above it (angles below 1e-3 rad, and the reference's flat-sky
+// branch below 2 arcsec) the cross-correlation kernel takes cos and sin of
+// half the angle from the angle itself, not from the half-angle identities
+constexpr double kCosHalfAngleForm = 0.9999995;
 constexpr int kQueue = 256;                   // FP64 recheck entries per warp (cross)
 constexpr int kCfQueue = 128;                 // FP64 recheck entries per warp (auto)
 constexpr int kAccQ = 64;                     // run ring per warp (<= 31 + 32 entries held)
@@ -962,13 +966,32 @@ __global__ void __launch_bounds__(kXcfBlock, 1) xcf_xi_fast_kernel(
                 const double wq = objs.obj_weight[g];
                 if (wq != 0) {
                     valid = true;
-                    const double ang =
-                        nbr_angle ? nbr_angle[ctx.k0 + kk]
-                                  : angle_between(ctx.x1, ctx.y1, ctx.zc1, ctx.ra1, ctx.dec1,
-                                                  ctx.cd1, objs.x_cart[g], objs.y_cart[g],
-                                                  objs.z_cart[g], objs.ra[g], objs.dec[g]);
-                    cp = (float)(cos(ang / 2) * inv_p);
-                    st = (float)(sin(ang / 2) * inv_t);
+                    // cos and sin of half the angle, needed here to FP32
+                    // accuracy only (the FP64 re-decision forms its own)
+                    double chalf, shalf;
+                    const double x2 = objs.x_cart[g], y2 = objs.y_cart[g], z2 = objs.z_cart[g];
+                    const double cosang = __dadd_rn(
+                        __dadd_rn(__dmul_rn(x2, ctx.x1), __dmul_rn(y2, ctx.y1)),
+                        __dmul_rn(z2, ctx.zc1));
+                    if (!nbr_angle && cosang < kCosHalfAngleForm) {
+                        // half-angle identities on the clipped dot product: its
+                        // FP64 rounding moves 1 - cos by a few 1e-16, below
+                        // 1e-9 of it above 1e-3 rad; one square root each
+                        // instead of arccos, cos and sin
+                        const double cc = fmax(cosang, -1.0);
+                        chalf = __dsqrt_rn(__dmul_rn(0.5, __dadd_rn(1.0, cc)));
+                        shalf = __dsqrt_rn(__dmul_rn(0.5, __dsub_rn(1.0, cc)));
+                    } else {
+                        const double ang =
+                            nbr_angle ? nbr_angle[ctx.k0 + kk]
+                                      : angle_between(ctx.x1, ctx.y1, ctx.zc1, ctx.ra1,
+                                                      ctx.dec1, ctx.cd1, x2, y2, z2, objs.ra[g],
+                                                      objs.dec[g]);
+                        chalf = cos(ang / 2);
+                        shalf = sin(ang / 2);
+                    }
+                    cp = (float)(chalf * inv_p);
+                    st = (float)(shalf * inv_t);
                     const double rho_d = objs.obj_r_comov[g] - r_ref;
                     const float rho_q = (float)rho_d;
                     nb = -__fmul_rn(cp, rho_q);
