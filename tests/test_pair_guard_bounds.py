@@ -203,3 +203,23 @@ def test_fp32_rmu_bins_outside_guards_equal_fp64():
             queued += int(near.sum())
     assert checked > 100_000
     assert queued < 0.01 * checked
+
+
+def test_half_angle_identities_give_the_fp32_constants():
+    """The cross-correlation kernel forms cos and sin of half the angle from
+    the half-angle identities on the FP64 dot product above 1e-3 rad; the FP32
+    constants cp and st it derives are those of the trigonometric form."""
+    rng = np.random.default_rng(9)
+    ang = np.concatenate([rng.uniform(1e-3, 0.3, 1_000_000), np.geomspace(1e-3, 3.0, 10_000)])
+    cosang = np.cos(ang)
+    trig = np.arccos(cosang) / 2
+    for inv in (0.25, 0.5, 100.0 / 400.0):
+        cp_trig = (np.cos(trig) * inv).astype(f32)
+        st_trig = (np.sin(trig) * inv).astype(f32)
+        cp_half = (np.sqrt(0.5 * (1.0 + cosang)) * inv).astype(f32)
+        st_half = (np.sqrt(0.5 * (1.0 - cosang)) * inv).astype(f32)
+        assert np.array_equal(cp_half, cp_trig)
+        # sin: at most one unit in the last place apart, where the two FP64
+        # values straddle an FP32 rounding boundary
+        ulps = np.abs(st_half.view(np.int32).astype(np.int64) - st_trig.view(np.int32))
+        assert ulps.max() <= 1 and (ulps > 0).mean() < 1e-4
