@@ -64,8 +64,8 @@ constexpr float kMagic = 12582912.0f;        // 1.5 * 2^23
 constexpr unsigned kMagicBits = 0x4B400000u;  // bits of 1.5 * 2^23
 constexpr float kFar = 1e30f;                 // nB, t and z of an empty slot
 // cos(1e-3): above it (angles below 1e-3 rad, and the reference's flat-sky
-// branch below 2 arcsec) the cross-correlation kernel takes cos and sin of
-// half the angle from the angle itself, not from the half-angle identities
+// branch below 2 arcsec) the pair kernels take cos and sin of half the angle
+// from the angle itself, not from the half-angle identities
 constexpr double kCosHalfAngleForm = 0.9999995;
 constexpr int kQueue = 256;                   // FP64 recheck entries per warp (cross)
 constexpr int kCfQueue = 128;                 // FP64 recheck entries per warp (auto)
@@ -500,12 +500,29 @@ __global__ void __launch_bounds__(kCfBlock, 1) cf_xi_diag_kernel(
                 continue;
             }
             const int n2 = (int)n2_64;
-            const double ang = nbr_angle ? nbr_angle[k]
-                                         : angle_between(f1_geom[0], f1_geom[1], f1_geom[2],
-                                                         f1_geom[3], f1_geom[4], f1_geom[5],
-                                                         s2.x_cart[g], s2.y_cart[g],
-                                                         s2.z_cart[g], s2.ra[g], s2.dec[g]);
-            const double chalf = cos(ang / 2), shalf = sin(ang / 2);
+            // cos and sin of half the angle: from the half-angle identities
+            // on the FP64 dot product (one square root each; the FP64
+            // rounding of the dot moves 1 - cos by a few 1e-16, below 1e-9
+            // of it above 1e-3 rad), else from the angle itself. The angle
+            // is needed only by the zerr cut (the angular binning never
+            // runs here)
+            double ang = 0.0, chalf, shalf;
+            const double x2 = s2.x_cart[g], y2 = s2.y_cart[g], z2 = s2.z_cart[g];
+            const double cosang =
+                __dadd_rn(__dadd_rn(__dmul_rn(x2, f1_geom[0]), __dmul_rn(y2, f1_geom[1])),
+                          __dmul_rn(z2, f1_geom[2]));
+            if (!nbr_angle && !(EXTRA && b.zerr_on) && cosang < kCosHalfAngleForm) {
+                const double cc = fmax(cosang, -1.0);
+                chalf = __dsqrt_rn(__dmul_rn(0.5, __dadd_rn(1.0, cc)));
+                shalf = __dsqrt_rn(__dmul_rn(0.5, __dsub_rn(1.0, cc)));
+            } else {
+                ang = nbr_angle ? nbr_angle[k]
+                                : angle_between(f1_geom[0], f1_geom[1], f1_geom[2], f1_geom[3],
+                                                f1_geom[4], f1_geom[5], x2, y2, z2, s2.ra[g],
+                                                s2.dec[g]);
+                chalf = cos(ang / 2);
+                shalf = sin(ang / 2);
+            }
             bool shp = false, zerr_pair = false;
             if (EXTRA) {
                 if (b.remove_shp) {
