@@ -1269,14 +1269,18 @@ def run_reference(args):
     for _ in range(args.warmup):
         cpu_sample(fs, params, ang_max, min(2.0, seconds), args.config)
     desc, cores = "", 1
+    step_ms = []
     for _ in range(args.steps):
+        t0 = time.perf_counter()
         v, desc, cores = cpu_sample(fs, params, ang_max, seconds, args.config)
+        step_ms.append((time.perf_counter() - t0) * 1e3)
         vals.append(v)
     value = float(np.median(vals))
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "pixel-pairs/s",
         "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
-        "ms_per_step": None, "higher_is_better": True, "scaling": "weak",
+        # a step is one bounded sample of the workload (``sample`` below)
+        "ms_per_step": float(np.median(step_ms)), "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": workload_name(args.config), "bins": "50x50",
                    "r_par": "0-200", "r_trans": "0-200"},

@@ -28,6 +28,7 @@ def test_reference_arm_prints_one_contract_line():
                 "cpu_baseline", "e2e"):
         assert key in line, key
     assert line["impl"] == "reference"
+    assert line["ms_per_step"] > 0
     assert line["value"] > 0 and line["cpu_baseline"]["value"] == line["value"]
     assert line["cpu_baseline"]["kind"] in ("port", "reference")
     assert line["cpu_baseline"]["cores"] >= 1
